@@ -1,0 +1,232 @@
+/*
+ * planetsim_gb300.h - C ABI of the GB300 (sm_103a) implicit heat-transport path of
+ * PlanetSim (fgianni/planet_game).
+ *
+ * Every entry point is plain C: opaque handles, plain pointers and sizes, an int
+ * status (PSGB_OK = 0) and a thread-local message from psgb_last_error(). Array
+ * arguments are HOST pointers when `memory` is PSGB_MEMORY_HOST (the call copies,
+ * runs and synchronises) or DEVICE pointers when it is PSGB_MEMORY_DEVICE (the call
+ * is ordered on `stream`, a cudaStream_t or NULL for the legacy default stream).
+ * Cell arrays are in the reference's cell order (the order make_icosphere
+ * produces); edge arrays in its edge-id order; CSR arrays in its
+ * TransportGraph order.
+ *
+ * Each entry point names the reference interface it replaces; the C++ shim that
+ * re-exports those interfaces with their original signatures is described with the
+ * library's integration notes.
+ */
+#ifndef PLANETSIM_GB300_H
+#define PLANETSIM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PSGB_ABI_VERSION 1
+
+/* status codes */
+#define PSGB_OK 0
+#define PSGB_ERR_INVALID_ARGUMENT 1 /* std::invalid_argument in the reference */
+#define PSGB_ERR_OUT_OF_MEMORY 2
+#define PSGB_ERR_NOT_CONVERGED 3    /* iteration or refinement cap reached */
+#define PSGB_ERR_BREAKDOWN 4        /* Krylov breakdown (rho, omega or shadow.v = 0) */
+#define PSGB_ERR_NON_FINITE 5
+#define PSGB_ERR_CUDA 6
+#define PSGB_ERR_LOGIC 7            /* std::logic_error in the reference */
+#define PSGB_ERR_BUDGET 8           /* admission refused by the HBM budget */
+
+#define PSGB_MEMORY_HOST 0
+#define PSGB_MEMORY_DEVICE 1
+
+#define PSGB_DTYPE_F64 0
+#define PSGB_DTYPE_F32 1
+
+#define PSGB_PRECISION_FP64 0       /* plain FP64 Krylov + multigrid */
+#define PSGB_PRECISION_MIXED 1      /* FP32 inner Krylov + multigrid, FP64 refinement */
+
+#define PSGB_METHOD_PCG 0
+#define PSGB_METHOD_BICGSTAB 1
+
+typedef struct psgb_planet psgb_planet;
+typedef struct psgb_batch psgb_batch;
+
+/* Last error message of the calling thread ("" if none). */
+const char* psgb_last_error(void);
+int psgb_abi_version(void);
+
+/* ---- mesh, transport graph and multigrid hierarchy ------------------------------
+ * Replaces make_icosphere (sim/planet/mesh/icosphere.cpp:200) +
+ * mesh_transport_graph (sim/planet/surface/heat_transport.cpp:433) + the
+ * GraphMultigrid constructor (heat_transport.hpp:62, heat_transport.cpp:549-552).
+ * The mesh is bit-identical to the reference's; the hierarchy's aggregates, coarse
+ * patterns and Galerkin targets equal the reference's build_hierarchy. */
+int psgb_planet_create(uint32_t level, double radius_m, psgb_planet** out);
+void psgb_planet_destroy(psgb_planet* planet);
+
+typedef struct psgb_planet_info {
+    uint64_t cells, edges, directed_edges, corners;
+    uint32_t levels;             /* multigrid levels (the last one is solved densely) */
+    uint32_t level_rows[8];      /* rows per multigrid level */
+    uint64_t device_bytes;       /* HBM held by the planet (mesh + its solo batch) */
+} psgb_planet_info;
+int psgb_planet_info_get(const psgb_planet* planet, psgb_planet_info* out);
+
+/* Host views of the mesh arrays (valid while the planet lives); layout as the
+ * reference PlanetMesh (sim/planet/mesh/planet_mesh.hpp:44-125). */
+typedef struct psgb_mesh_view {
+    const double* center;        /* [cells][3] */
+    const double* east;          /* [cells][3] */
+    const double* north;         /* [cells][3] */
+    const double* area_m2;       /* [cells] */
+    const uint32_t* source_vertex;
+    const uint32_t* edge_offset; /* [cells] first directed edge */
+    const uint8_t* edge_count;   /* [cells] 5 or 6 */
+    const uint32_t* neighbor;    /* [directed] */
+    const uint32_t* edge;        /* [directed] */
+    const uint32_t* corner;      /* [directed] first corner of each directed edge */
+    const float* normal_east;    /* [directed] */
+    const float* normal_north;   /* [directed] */
+    const uint32_t* edge_first;  /* [edges] */
+    const uint32_t* edge_second; /* [edges] */
+    const double* edge_length_m; /* [edges] */
+    const double* edge_distance_m;
+    const double* corner_unit;   /* [corners][3] */
+    const double* graph_weight;  /* [directed] l/d, the TransportGraph weight */
+    const double* graph_weight_sum; /* [cells] */
+} psgb_mesh_view;
+int psgb_planet_mesh_view(const psgb_planet* planet, psgb_mesh_view* out);
+
+/* Integer structure of one multigrid level (heat_transport.cpp:54-66): CSR
+ * offsets [rows + 1] and columns, aggregate of each row ([rows], none on the
+ * coarsest level) and the Galerkin target of each off-diagonal (-1: the aggregate's
+ * diagonal). Host pointers, valid while the planet lives; sizes in `sizes`:
+ * {rows, off-diagonals, aggregate length, target length}. */
+int psgb_planet_hierarchy_level(const psgb_planet* planet, uint32_t level, uint64_t sizes[4],
+                                const uint32_t** offset, const uint32_t** column,
+                                const uint32_t** aggregate, const int64_t** target);
+
+/* ---- finite-volume operators: sim/planet/operators/finite_volume.hpp:21-44 ----- */
+/* laplacian<T>(mesh, scalar, result): cells -> cells */
+int psgb_laplacian(psgb_planet* planet, int dtype, const void* scalar, void* result, int memory,
+                   void* stream);
+/* gradient<T>(mesh, scalar, east, north): cells -> 2 x cells */
+int psgb_gradient(psgb_planet* planet, int dtype, const void* scalar, void* east, void* north,
+                  int memory, void* stream);
+/* divergence<T>(mesh, edge_normal_flux, result): edges -> cells */
+int psgb_divergence(psgb_planet* planet, int dtype, const void* edge_flux, void* result, int memory,
+                    void* stream);
+
+/* ---- heat transport: sim/planet/surface/heat_transport.hpp -------------------- */
+/* diffusion_source (heat_transport.hpp:122): K * laplacian, W/m^2 */
+int psgb_diffusion_source(psgb_planet* planet, double conductance_W_K, const double* temperature_K,
+                          double* source_W_m2, int memory, void* stream);
+
+/* GraphMultigrid::set_matrix (heat_transport.hpp:69): diagonal [cells], off-diagonals
+ * in the graph's CSR order [directed]. */
+int psgb_multigrid_set_matrix(psgb_planet* planet, const double* diagonal, const double* off_diagonal,
+                              int memory, void* stream);
+/* GraphMultigrid::precondition (heat_transport.hpp:70): one V-cycle, x = M^-1 rhs.
+ * The GB300 V-cycle smooths with damped Jacobi (the reference: block-hybrid
+ * symmetric Gauss-Seidel), so x approximates the same inverse differently. */
+int psgb_multigrid_precondition(psgb_planet* planet, int dtype, const void* rhs, void* solution,
+                                int memory, void* stream);
+
+typedef struct psgb_solve_options {
+    int precision;               /* PSGB_PRECISION_* */
+    int method;                  /* PSGB_METHOD_* */
+    double tolerance;            /* ||b - A x||_2 <= tolerance ||b||_2, FP64 residual */
+    double inner_tolerance;      /* mixed precision: residual reduction per refinement */
+    int max_iterations;          /* Krylov iterations per (inner) solve */
+    int max_refinements;         /* FP64 refinement steps */
+    int poll;                    /* Krylov iterations between host status reads */
+    int pre_sweeps, post_sweeps; /* Jacobi sweeps per level */
+    double jacobi_omega;         /* Jacobi damping */
+} psgb_solve_options;
+void psgb_solve_options_default(psgb_solve_options* out);
+
+typedef struct psgb_solve_report {
+    int status;                  /* PSGB_OK or PSGB_ERR_* */
+    int refinements;             /* FP64 refinement steps taken */
+    int iterations;              /* Krylov iterations, summed over refinements */
+    double relative_residual;    /* ||b - A x|| / ||b|| in FP64 */
+} psgb_solve_report;
+
+/* The linear solve of the implicit step on the planet's graph:
+ *   (A_c / s_c) x_c + K sum_e w_e (x_c - x_n) = rhs_c      (s_c > 0; else x_c = 0 rows)
+ * Replaces solve_newton_system (heat_transport.cpp:337-429). x holds the initial
+ * guess on entry (zeros reproduce the reference's start). */
+int psgb_solve_newton_system(psgb_planet* planet, const psgb_solve_options* options,
+                             double conductance_W_K, const double* slope, const double* rhs,
+                             double* x, psgb_solve_report* report, int memory, void* stream);
+
+/* One implicit diffusive heat-transport sub-step with the linear column response
+ * T = T0 + (dt/C)(S + H): the response solve_implicit_transport
+ * (heat_transport.cpp:595-772) receives from a linear tile, solved directly:
+ *   (C/dt M + K L) T = C/dt M T0 + M S,
+ * then the conservative flux form H = K lap(T) and T_new = T0 + (dt/C)(S + H). */
+typedef struct psgb_step_params {
+    double heat_capacity_J_m2_K; /* C */
+    double dt_s;                 /* dt */
+    double conductance_W_K;      /* K (used when edge_conductance is NULL) */
+    const double* edge_conductance; /* optional, per undirected edge [edges], W/K; HOST */
+} psgb_step_params;
+
+typedef struct psgb_step_report {
+    psgb_solve_report solve;
+    double sum_W;                /* sum A H (zero to rounding) */
+    double absolute_sum_W;       /* sum A |H| */
+    double dissipation_W_K;      /* sum A H T (<= 0) */
+    double closure;              /* |sum A C dT/dt - sum A S| / sum A |S| */
+} psgb_step_report;
+
+int psgb_transport_step(psgb_planet* planet, const psgb_step_params* params,
+                        const psgb_solve_options* options, const double* t0_K, const double* source_W_m2,
+                        double* t_new_K, double* transport_W_m2, psgb_step_report* report, int memory,
+                        void* stream);
+
+/* ---- batches: many planets of uneven levels solved together -------------------
+ * Concatenated block layout (each planet padded to 256-row tiles), per-planet
+ * convergence masks, one stream of launches for all planets. */
+int psgb_batch_create(psgb_planet* const* planets, uint32_t count, psgb_batch** out);
+void psgb_batch_destroy(psgb_batch* batch);
+uint64_t psgb_batch_device_bytes(const psgb_batch* batch);
+/* Per planet i: params[i], t0[i], source[i] in, t_new[i] (and optionally
+ * transport[i]) out, reports[i]. */
+int psgb_batch_transport_step(psgb_batch* batch, const psgb_step_params* params,
+                              const psgb_solve_options* options, const double* const* t0_K,
+                              const double* const* source_W_m2, double* const* t_new_K,
+                              double* const* transport_W_m2, psgb_step_report* reports, int memory,
+                              void* stream);
+
+/* ---- column radiation: sim/planet/atmosphere/atmosphere_column.hpp ----------------
+ * column_radiation (humidity variant, :85-104) + cloud_optics (:599-623) +
+ * add_cloud_longwave (:627-634) + longwave_fluxes (:125-143) for `cells` columns of
+ * `layers` (1..16) equal-mass layers; layer-major arrays [layers][cells]. */
+typedef struct psgb_column_constants {
+    double dry_optical_depth, vapour_absorption_m2_kg, in_cloud_water_path_kg_m2,
+        effective_radius_m, cloud_asymmetry, cloud_longwave_absorption_m2_kg,
+        reference_pressure_Pa, gravity_m_s2, stefan_boltzmann;
+} psgb_column_constants;
+/* outputs: emissivity, absorbed [layers][cells]; fraction, reflectance [layers][cells];
+ * scalars [5][cells] = downward surface LW, OLR, SW transmission, column cloud
+ * fraction, column cloud optical depth. */
+int psgb_column_radiation(uint32_t cells, uint32_t layers, const psgb_column_constants* constants,
+                          const double* temperature_K, const double* humidity, const double* cloud_water,
+                          const double* surface_temperature_K, const double* surface_pressure_Pa,
+                          double* emissivity, double* absorbed, double* fraction, double* reflectance,
+                          double* scalars, int memory, void* stream);
+
+/* ---- inputs ---------------------------------------------------------------------
+ * Sub-step-mean insolation of sub-step `substep` for the Earth-development planet
+ * (compute_substep_mean_insolation, sim/planet/orbit/substep_forcing.cpp:102-127),
+ * computed on the host; cells floats. */
+int psgb_substep_mean_insolation(const psgb_planet* planet, int64_t substep, float* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PLANETSIM_GB300_H */

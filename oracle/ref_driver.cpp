@@ -1,0 +1,440 @@
+// Test-only C-ABI driver over the reference PlanetSim library, compiled from the
+// reference sources by oracle/Makefile.ref into oracle/_ref/libref_driver.so.
+//
+// This is oracle infrastructure: it is loaded only by tests/golden/make_golden.py
+// (to write the golden fixtures) and by the pinning tests that compare the
+// restated oracle (oracle/planetsim_oracle.cpp) with the reference itself. No
+// product code loads it. It adds no arithmetic of its own: every number it returns
+// is computed by the reference's functions named beside each entry point.
+//
+// heat_transport.cpp is included textually so that the anonymous-namespace
+// multigrid pieces (Level, build_hierarchy, coarsen_values, v_cycle,
+// solve_newton_system) can be driven directly, which is how the aggregates,
+// coarse patterns and Galerkin scatter targets are checked bit for bit.
+
+#include "sim/planet/surface/heat_transport.cpp"
+
+#include "sim/planet/atmosphere/atmosphere.hpp"
+#include "sim/planet/atmosphere/atmosphere_column.hpp"
+#include "sim/planet/atmosphere/saturation.hpp"
+#include "sim/planet/mesh/icosphere.hpp"
+#include "sim/planet/operators/finite_volume.hpp"
+#include "sim/planet/orbit/climate_calendar.hpp"
+#include "sim/planet/orbit/substep_forcing.hpp"
+#include "sim/planet/planet_parameters.hpp"
+
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <vector>
+
+using namespace planetsim;
+
+namespace {
+
+struct RefHierarchy {
+    std::vector<Level> levels;
+};
+
+std::vector<double> copy_in(const double* values, std::size_t n) {
+    return std::vector<double>(values, values + n);
+}
+
+}  // namespace
+
+extern "C" {
+
+// ---- mesh: make_icosphere (sim/planet/mesh/icosphere.cpp:200-419) ----------
+void* refd_mesh_new(std::uint32_t level, double radius_m) {
+    return new PlanetMesh(make_icosphere(level, radius_m));
+}
+
+void refd_mesh_free(void* mesh) { delete static_cast<PlanetMesh*>(mesh); }
+
+void refd_mesh_counts(void* handle, std::uint64_t* counts) {
+    const auto& mesh = *static_cast<PlanetMesh*>(handle);
+    counts[0] = mesh.cell_count();
+    counts[1] = mesh.edge_count();
+    counts[2] = mesh.directed_edge_count();
+    counts[3] = mesh.corner_count();
+}
+
+// Per cell: centre/east/north (xyz each), area, source vertex, edge offset, edge count.
+void refd_mesh_cells(void* handle, double* center, double* east, double* north, double* area,
+                     std::uint32_t* source, std::uint32_t* edge_offset, std::uint8_t* edge_count) {
+    const auto& mesh = *static_cast<PlanetMesh*>(handle);
+    std::size_t i = 0;
+    for (const auto& cell : mesh.cells()) {
+        center[3 * i] = cell.center_unit.x;
+        center[3 * i + 1] = cell.center_unit.y;
+        center[3 * i + 2] = cell.center_unit.z;
+        east[3 * i] = cell.east_unit.x;
+        east[3 * i + 1] = cell.east_unit.y;
+        east[3 * i + 2] = cell.east_unit.z;
+        north[3 * i] = cell.north_unit.x;
+        north[3 * i + 1] = cell.north_unit.y;
+        north[3 * i + 2] = cell.north_unit.z;
+        area[i] = cell.area_m2;
+        source[i] = cell.source_vertex_index;
+        edge_offset[i] = cell.edge_offset;
+        edge_count[i] = cell.edge_count;
+        ++i;
+    }
+}
+
+void refd_mesh_cell_edges(void* handle, std::uint32_t* neighbor, std::uint32_t* edge,
+                          float* normal_east, float* normal_north) {
+    const auto& mesh = *static_cast<PlanetMesh*>(handle);
+    std::size_t k = 0;
+    for (const auto& cell : mesh.cells()) {
+        for (const auto& ce : mesh.cell_edges(cell.id)) {
+            neighbor[k] = ce.neighbor.value();
+            edge[k] = ce.edge.value();
+            normal_east[k] = ce.outward_normal_east;
+            normal_north[k] = ce.outward_normal_north;
+            ++k;
+        }
+    }
+}
+
+void refd_mesh_edges(void* handle, std::uint32_t* first, std::uint32_t* second, double* length,
+                     double* distance) {
+    const auto& mesh = *static_cast<PlanetMesh*>(handle);
+    std::size_t e = 0;
+    for (const auto& edge : mesh.edges()) {
+        first[e] = edge.first_cell.value();
+        second[e] = edge.second_cell.value();
+        length[e] = edge.length_m;
+        distance[e] = edge.centroid_distance_m;
+        ++e;
+    }
+}
+
+void refd_mesh_corners(void* handle, double* corners, std::uint32_t* cell_corner) {
+    const auto& mesh = *static_cast<PlanetMesh*>(handle);
+    std::size_t c = 0;
+    for (const auto& corner : mesh.corners_unit()) {
+        corners[3 * c] = corner.x;
+        corners[3 * c + 1] = corner.y;
+        corners[3 * c + 2] = corner.z;
+        ++c;
+    }
+    std::size_t k = 0;
+    for (const auto& cell : mesh.cells()) {
+        for (const auto index : mesh.cell_corners(cell.id)) {
+            cell_corner[k++] = index;
+        }
+    }
+}
+
+// ---- transport graph: mesh_transport_graph (heat_transport.cpp:433-452) ----
+void refd_graph(void* handle, double* area, std::uint64_t* offset, std::uint64_t* neighbour,
+                double* weight, double* weight_sum) {
+    const auto graph = mesh_transport_graph(*static_cast<PlanetMesh*>(handle));
+    for (std::size_t i = 0; i < graph.size(); ++i) {
+        area[i] = graph.area_m2[i];
+        weight_sum[i] = graph.weight_sum[i];
+    }
+    for (std::size_t i = 0; i < graph.offset.size(); ++i) {
+        offset[i] = graph.offset[i];
+    }
+    for (std::size_t k = 0; k < graph.neighbour.size(); ++k) {
+        neighbour[k] = graph.neighbour[k];
+        weight[k] = graph.weight[k];
+    }
+}
+
+// ---- hierarchy: build_hierarchy (heat_transport.cpp:175-200) --------------
+void* refd_hierarchy_new(void* handle) {
+    const auto graph = mesh_transport_graph(*static_cast<PlanetMesh*>(handle));
+    auto* h = new RefHierarchy;
+    h->levels = build_hierarchy(graph, graph.size());
+    return h;
+}
+
+void refd_hierarchy_free(void* h) { delete static_cast<RefHierarchy*>(h); }
+
+std::uint64_t refd_hierarchy_level_count(void* h) {
+    return static_cast<RefHierarchy*>(h)->levels.size();
+}
+
+// sizes[0] = rows, sizes[1] = off-diagonal entries, sizes[2] = aggregate length,
+// sizes[3] = target length.
+void refd_hierarchy_level_sizes(void* h, std::uint64_t index, std::uint64_t* sizes) {
+    const Level& level = static_cast<RefHierarchy*>(h)->levels[index];
+    sizes[0] = level.size;
+    sizes[1] = level.column.size();
+    sizes[2] = level.aggregate.size();
+    sizes[3] = level.target.size();
+}
+
+// Integer structure of one level; `target` uses -1 for the aggregate's diagonal.
+void refd_hierarchy_level(void* h, std::uint64_t index, std::int64_t* offset,
+                          std::int64_t* column, std::int64_t* aggregate, std::int64_t* target,
+                          double* diagonal, double* value) {
+    const Level& level = static_cast<RefHierarchy*>(h)->levels[index];
+    for (std::size_t i = 0; i < level.offset.size(); ++i) offset[i] = static_cast<std::int64_t>(level.offset[i]);
+    for (std::size_t i = 0; i < level.column.size(); ++i) column[i] = static_cast<std::int64_t>(level.column[i]);
+    for (std::size_t i = 0; i < level.aggregate.size(); ++i) aggregate[i] = static_cast<std::int64_t>(level.aggregate[i]);
+    for (std::size_t i = 0; i < level.target.size(); ++i) {
+        target[i] = level.target[i] == diagonal_target ? -1 : static_cast<std::int64_t>(level.target[i]);
+    }
+    for (std::size_t i = 0; i < level.diagonal.size(); ++i) diagonal[i] = level.diagonal[i];
+    for (std::size_t i = 0; i < level.value.size(); ++i) value[i] = level.value[i];
+}
+
+// set_matrix on the hierarchy: fine values in, Galerkin values on every level
+// (coarsen_values, heat_transport.cpp:157-171) and the coarsest Cholesky
+// factor (factor_dense, :202-226).
+void refd_hierarchy_set_matrix(void* h, const double* diagonal, const double* off) {
+    auto& levels = static_cast<RefHierarchy*>(h)->levels;
+    Level& fine = levels.front();
+    std::copy(diagonal, diagonal + fine.size, fine.diagonal.begin());
+    std::copy(off, off + fine.value.size(), fine.value.begin());
+    for (std::size_t index = 0; index + 1U < levels.size(); ++index) {
+        coarsen_values(levels[index], levels[index + 1U]);
+    }
+    factor_dense(levels.back());
+}
+
+void refd_hierarchy_factor(void* h, double* factor) {
+    const auto& level = static_cast<RefHierarchy*>(h)->levels.back();
+    std::copy(level.factor.begin(), level.factor.end(), factor);
+}
+
+// One V-cycle (v_cycle, heat_transport.cpp:288-326) with the mesh's 256-cell blocks.
+void refd_hierarchy_vcycle(void* h, void* mesh_handle, const double* rhs, double* out) {
+    const auto& levels = static_cast<RefHierarchy*>(h)->levels;
+    const auto& mesh = *static_cast<PlanetMesh*>(mesh_handle);
+    const Parallel parallel{mesh.blocks(), 1U};
+    std::vector<double> b = copy_in(rhs, levels.front().size);
+    std::vector<double> x;
+    v_cycle(levels, 0U, b, x, parallel);
+    std::copy(x.begin(), x.end(), out);
+}
+
+// ---- FV operators (finite_volume.cpp:34-111) --------------------------------
+void refd_laplacian_f64(void* handle, const double* in, double* out) {
+    const auto& mesh = *static_cast<PlanetMesh*>(handle);
+    Field2D<double> scalar(copy_in(in, mesh.cell_count()));
+    Field2D<double> result(mesh.cell_count(), 0.0);
+    laplacian(mesh, scalar, result, 1U);
+    std::copy(result.values().begin(), result.values().end(), out);
+}
+
+void refd_laplacian_f32(void* handle, const float* in, float* out) {
+    const auto& mesh = *static_cast<PlanetMesh*>(handle);
+    Field2D<float> scalar(std::vector<float>(in, in + mesh.cell_count()));
+    Field2D<float> result(mesh.cell_count(), 0.0F);
+    laplacian(mesh, scalar, result, 1U);
+    std::copy(result.values().begin(), result.values().end(), out);
+}
+
+void refd_gradient_f64(void* handle, const double* in, double* east, double* north) {
+    const auto& mesh = *static_cast<PlanetMesh*>(handle);
+    Field2D<double> scalar(copy_in(in, mesh.cell_count()));
+    Field2D<double> e(mesh.cell_count(), 0.0);
+    Field2D<double> n(mesh.cell_count(), 0.0);
+    gradient(mesh, scalar, e, n, 1U);
+    std::copy(e.values().begin(), e.values().end(), east);
+    std::copy(n.values().begin(), n.values().end(), north);
+}
+
+void refd_gradient_f32(void* handle, const float* in, float* east, float* north) {
+    const auto& mesh = *static_cast<PlanetMesh*>(handle);
+    Field2D<float> scalar(std::vector<float>(in, in + mesh.cell_count()));
+    Field2D<float> e(mesh.cell_count(), 0.0F);
+    Field2D<float> n(mesh.cell_count(), 0.0F);
+    gradient(mesh, scalar, e, n, 1U);
+    std::copy(e.values().begin(), e.values().end(), east);
+    std::copy(n.values().begin(), n.values().end(), north);
+}
+
+void refd_divergence_f64(void* handle, const double* flux, double* out) {
+    const auto& mesh = *static_cast<PlanetMesh*>(handle);
+    EdgeField<double> edge_flux(mesh.edge_count(), 0.0);
+    for (std::size_t e = 0; e < mesh.edge_count(); ++e) {
+        edge_flux[EdgeId{static_cast<std::uint32_t>(e)}] = flux[e];
+    }
+    Field2D<double> result(mesh.cell_count(), 0.0);
+    divergence(mesh, edge_flux, result, 1U);
+    std::copy(result.values().begin(), result.values().end(), out);
+}
+
+void refd_divergence_f32(void* handle, const float* flux, float* out) {
+    const auto& mesh = *static_cast<PlanetMesh*>(handle);
+    EdgeField<float> edge_flux(mesh.edge_count(), 0.0F);
+    for (std::size_t e = 0; e < mesh.edge_count(); ++e) {
+        edge_flux[EdgeId{static_cast<std::uint32_t>(e)}] = flux[e];
+    }
+    Field2D<float> result(mesh.cell_count(), 0.0F);
+    divergence(mesh, edge_flux, result, 1U);
+    std::copy(result.values().begin(), result.values().end(), out);
+}
+
+// ---- diffusion_source (heat_transport.cpp:579-593) --------------------------
+void refd_diffusion_source(void* handle, double conductance, const double* temperature,
+                           double* source) {
+    const auto& mesh = *static_cast<PlanetMesh*>(handle);
+    const auto graph = mesh_transport_graph(mesh);
+    Field2D<double> t(copy_in(temperature, mesh.cell_count()));
+    Field2D<double> s;
+    diffusion_source(graph, conductance, t, s, 1U);
+    std::copy(s.values().begin(), s.values().end(), source);
+}
+
+// ---- solve_implicit_transport with a linear response (heat_transport.cpp:595-772)
+// mean = base + slope * h. stats: [newton, cg, consistency, sum, abs_sum, dissipation].
+void refd_solve_linear(void* handle, double conductance, const double* base, const double* slope,
+                       double cg_tolerance, double newton_tolerance, std::uint64_t workers,
+                       double* mean_out, double* source_out, double* stats) {
+    const auto& mesh = *static_cast<PlanetMesh*>(handle);
+    const auto graph = mesh_transport_graph(mesh);
+    const std::size_t n = mesh.cell_count();
+    const TransportResponse response = [&](const Field2D<double>& source, Field2D<double>& mean,
+                                           Field2D<double>& slope_out) {
+        for (std::size_t cell = 0; cell < n; ++cell) {
+            mean[cell] = base[cell] + slope[cell] * source[cell];
+            slope_out[cell] = slope[cell];
+        }
+    };
+    const Field2D<double> floor(n, -std::numeric_limits<double>::infinity());
+    ImplicitTransportSettings settings;
+    settings.cg_relative_tolerance = cg_tolerance;
+    settings.newton_tolerance_W_m2 = newton_tolerance;
+    const auto result = solve_implicit_transport(graph, conductance, floor, response, settings,
+                                                 static_cast<std::size_t>(workers));
+    std::copy(result.mean_K.values().begin(), result.mean_K.values().end(), mean_out);
+    std::copy(result.source_W_m2.values().begin(), result.source_W_m2.values().end(), source_out);
+    stats[0] = result.newton_iterations;
+    stats[1] = result.cg_iterations;
+    stats[2] = result.consistency_residual_W_m2;
+    stats[3] = result.sum_W;
+    stats[4] = result.absolute_sum_W;
+    stats[5] = result.dissipation_W_K;
+}
+
+// ---- the assembled SPD system by the reference's own PCG + SGS V-cycle ------
+// solve_newton_system (heat_transport.cpp:337-429): (A/s) x + K L x = rhs.
+int refd_pcg(void* handle, double conductance, const double* slope, const double* rhs,
+             double relative_tolerance, int max_iterations, std::uint64_t workers, double* x_out) {
+    const auto& mesh = *static_cast<PlanetMesh*>(handle);
+    const auto graph = mesh_transport_graph(mesh);
+    const std::size_t n = mesh.cell_count();
+    std::vector<Level> levels = build_hierarchy(graph, n);
+    Field2D<double> s(copy_in(slope, n));
+    Field2D<double> b(copy_in(rhs, n));
+    Field2D<double> x;
+    ImplicitTransportSettings settings;
+    settings.cg_relative_tolerance = relative_tolerance;
+    settings.max_cg_iterations = max_iterations;
+    const int iterations = solve_newton_system(graph, conductance, s, b, levels, x, settings,
+                                               static_cast<std::size_t>(workers));
+    std::copy(x.values().begin(), x.values().end(), x_out);
+    return iterations;
+}
+
+// ---- column radiation (atmosphere_column.hpp:85-143, 599-634) ---------------
+// One column of `layers` <= 8 equal-mass layers. Inputs: layer temperature,
+// humidity, cloud water (kg/kg); surface T and pressure; gravity; optical
+// constants [tau_d, kappa_v, W_c, r_e, g, kappa_l]. Outputs per layer:
+// emissivity (with clouds), absorbed longwave, cloud fraction, reflectance;
+// scalars: [downward surface LW, OLR, SW transmission, column fraction,
+// column optical depth].
+int refd_column_radiation(std::uint32_t layers, const double* temperature, const double* humidity,
+                          const double* cloud_water, double surface_temperature,
+                          double surface_pressure, double gravity, const double* constants,
+                          double* emissivity, double* absorbed, double* fraction,
+                          double* reflectance, double* scalars) {
+    if (layers == 0U || layers > max_column_layers) {
+        return -1;
+    }
+    AtmosphereParameters parameters;
+    parameters.layer_count = layers;
+    parameters.dry_optical_depth = constants[0];
+    parameters.vapour_absorption_m2_kg = constants[1];
+    parameters.cloud_in_cloud_water_path_kg_m2 = constants[2];
+    parameters.cloud_effective_radius_m = constants[3];
+    parameters.cloud_asymmetry = constants[4];
+    parameters.cloud_longwave_absorption_m2_kg = constants[5];
+    ColumnRadiation column = column_radiation(parameters, surface_pressure, gravity,
+                                              std::span<const double>(humidity, layers));
+    ColumnMoisture moisture;
+    moisture.layer_mass_kg_m2 = surface_pressure / (gravity * static_cast<double>(layers));
+    for (std::size_t k = 0; k < layers; ++k) {
+        moisture.humidity_kg_kg[k] = humidity[k];
+        moisture.cloud_water_kg_kg[k] = cloud_water[k];
+        moisture.pressure_Pa[k] = layer_sigma(k, layers) * surface_pressure;
+    }
+    const CloudOptics optics = cloud_optics(parameters, column, moisture);
+    add_cloud_longwave(column, optics);
+    LayerArray emission{};
+    for (std::size_t k = 0; k < layers; ++k) {
+        const double t2 = temperature[k] * temperature[k];
+        emission[k] = column.emissivity[k] * column_stefan_boltzmann_W_m2_K4 * t2 * t2;
+    }
+    const double ts2 = surface_temperature * surface_temperature;
+    const LongwaveFluxes fluxes =
+        longwave_fluxes(column, emission, column_stefan_boltzmann_W_m2_K4 * ts2 * ts2);
+    for (std::size_t k = 0; k < layers; ++k) {
+        emissivity[k] = column.emissivity[k];
+        absorbed[k] = fluxes.absorbed_in[k];
+        fraction[k] = optics.fraction[k];
+        reflectance[k] = optics.reflectance[k];
+    }
+    scalars[0] = fluxes.downward_surface_W_m2;
+    scalars[1] = fluxes.outgoing_W_m2;
+    scalars[2] = optics.transmission;
+    scalars[3] = optics.column_fraction;
+    scalars[4] = optics.column_optical_depth;
+    return 0;
+}
+
+double refd_layer_sigma(std::uint64_t layer, std::uint64_t layers) {
+    return layer_sigma(layer, layers);
+}
+
+double refd_saturation_specific_humidity(double temperature, double pressure) {
+    return saturation_specific_humidity(temperature, pressure);
+}
+
+double refd_surface_gravity_earth() {
+    return surface_gravity_m_s2(PlanetParameters::earth_development());
+}
+
+// Earth-like optical constants (atmosphere.hpp:79-82,120-121).
+void refd_earth_like_constants(double* constants) {
+    AtmosphereParameters p;
+    constants[0] = earth_like_dry_optical_depth;
+    constants[1] = earth_like_vapour_absorption_m2_kg;
+    constants[2] = p.cloud_in_cloud_water_path_kg_m2;
+    constants[3] = p.cloud_effective_radius_m;
+    constants[4] = p.cloud_asymmetry;
+    constants[5] = p.cloud_longwave_absorption_m2_kg;
+}
+
+// ---- sub-step-mean insolation (substep_forcing.cpp:75-127) ------------------
+void refd_insolation(void* handle, std::int64_t substep, float* out) {
+    const auto& mesh = *static_cast<PlanetMesh*>(handle);
+    const auto parameters = PlanetParameters::earth_development();
+    Field2D<float> field(mesh.cell_count(), 0.0F);
+    compute_substep_mean_insolation(mesh, parameters, climate_substep(substep, parameters), field,
+                                    1U);
+    std::copy(field.values().begin(), field.values().end(), out);
+}
+
+// The 16 quadrature nodes: [time, weight, sin decl, cos decl, flux] each.
+void refd_insolation_nodes(std::int64_t substep, double* nodes) {
+    const auto parameters = PlanetParameters::earth_development();
+    const auto table = substep_forcing_nodes(parameters, climate_substep(substep, parameters));
+    for (std::size_t i = 0; i < table.size(); ++i) {
+        nodes[5 * i] = table[i].time_s;
+        nodes[5 * i + 1] = table[i].weight;
+        nodes[5 * i + 2] = table[i].sin_declination;
+        nodes[5 * i + 3] = table[i].cos_declination;
+        nodes[5 * i + 4] = table[i].incident_flux_W_m2;
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,24 @@
+"""GB300-native (sm_103a) implicit heat-transport sub-step of PlanetSim.
+
+The product is the C-ABI library ``lib/libplanetsim_gb300.so`` (declared in
+``include/planetsim_gb300.h``); this package builds it in-tree and mirrors the
+reference's C++ operator and solver API over it.
+"""
+from .api import (  # noqa: F401
+    Batch,
+    GraphMultigrid,
+    PlanetMesh,
+    TransportGraph,
+    column_constants,
+    column_radiation,
+    diffusion_source,
+    divergence,
+    gradient,
+    laplacian,
+    make_icosphere,
+    mesh_transport_graph,
+    solve_newton_system,
+    solve_options,
+    transport_step,
+)
+from .capi import GB300Error  # noqa: F401

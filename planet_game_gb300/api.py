@@ -1,0 +1,389 @@
+"""Python mirror of the reference's operator and solver API over the GB300 C-ABI.
+
+Names follow the reference headers: ``make_icosphere`` / ``PlanetMesh``
+(sim/planet/mesh/icosphere.hpp, planet_mesh.hpp), ``mesh_transport_graph`` /
+``TransportGraph``, ``GraphMultigrid`` and ``diffusion_source``
+(sim/planet/surface/heat_transport.hpp), ``laplacian`` / ``gradient`` /
+``divergence`` (sim/planet/operators/finite_volume.hpp). Errors raise the same
+Python exception families the reference raises in C++ (ValueError for
+std::invalid_argument, RuntimeError otherwise).
+
+Arrays are numpy (host memory; each call copies in and out) or CUDA torch tensors
+(device memory; the call is ordered on torch's current stream). Everything computes on
+the GPU through the C-ABI; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import capi
+
+_DT = {np.dtype(np.float64): capi.DTYPE_F64, np.dtype(np.float32): capi.DTYPE_F32}
+
+
+def _raise(code: int) -> None:
+    if code == capi.OK:
+        return
+    msg = capi.load().psgb_last_error().decode()
+    if code == capi.ERR_INVALID_ARGUMENT:
+        raise ValueError(msg)
+    raise capi.GB300Error(code, msg)
+
+
+def _is_torch(a) -> bool:
+    return type(a).__module__.startswith("torch")
+
+
+def _ptr(a):
+    if _is_torch(a):
+        if not a.is_cuda or not a.is_contiguous():
+            raise ValueError("torch tensors must be contiguous CUDA tensors")
+        return C.c_void_p(a.data_ptr())
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("numpy arrays must be C-contiguous")
+    return C.c_void_p(a.ctypes.data)
+
+
+def _memory_of(*arrays) -> tuple[int, C.c_void_p]:
+    kinds = {_is_torch(a) for a in arrays if a is not None}
+    if len(kinds) != 1:
+        raise ValueError("pass either all numpy arrays or all CUDA tensors")
+    if kinds.pop():
+        import torch
+
+        return capi.MEMORY_DEVICE, C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    return capi.MEMORY_HOST, C.c_void_p(None)
+
+
+def _dtype_code(a) -> int:
+    if _is_torch(a):
+        import torch
+
+        return {torch.float64: capi.DTYPE_F64, torch.float32: capi.DTYPE_F32}[a.dtype]
+    return _DT[a.dtype]
+
+
+def _empty_like(a, shape, dtype=None):
+    if _is_torch(a):
+        import torch
+
+        return torch.empty(shape, dtype=dtype or a.dtype, device=a.device)
+    return np.empty(shape, dtype=dtype or a.dtype)
+
+
+def _view(ptr: int, dtype, count: int) -> np.ndarray:
+    if count == 0:
+        return np.empty(0, dtype=dtype)
+    buf = (C.c_char * (count * np.dtype(dtype).itemsize)).from_address(ptr)
+    return np.frombuffer(buf, dtype=dtype, count=count).copy()
+
+
+class PlanetMesh:
+    """A planet's SCVT mesh, its transport graph and multigrid hierarchy (one handle).
+
+    Built by the host builder that reproduces the reference's make_icosphere bit for bit;
+    the device copy is uploaded on first GPU use.
+    """
+
+    def __init__(self, level: int, radius_m: float):
+        lib = capi.load()
+        h = C.c_void_p()
+        _raise(lib.psgb_planet_create(C.c_uint32(level), C.c_double(radius_m), C.byref(h)))
+        self._h = h
+        self.subdivision = int(level)
+        self.radius_m = float(radius_m)
+        info = capi.PlanetInfo()
+        _raise(lib.psgb_planet_info_get(h, C.byref(info)))
+        self.cell_count = int(info.cells)
+        self.edge_count = int(info.edges)
+        self.directed_edge_count = int(info.directed_edges)
+        self.corner_count = int(info.corners)
+        self.level_rows = [int(info.level_rows[i]) for i in range(info.levels)]
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            capi.load().psgb_planet_destroy(h)
+            self._h = None
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def device_bytes(self) -> int:
+        info = capi.PlanetInfo()
+        _raise(capi.load().psgb_planet_info_get(self._h, C.byref(info)))
+        return int(info.device_bytes)
+
+    def arrays(self) -> dict[str, np.ndarray]:
+        """Copies of the mesh arrays (the reference PlanetMesh's fields, flattened)."""
+        v = capi.MeshView()
+        _raise(capi.load().psgb_planet_mesh_view(self._h, C.byref(v)))
+        n, e, d, k = self.cell_count, self.edge_count, self.directed_edge_count, self.corner_count
+        return {
+            "center": _view(v.center, np.float64, 3 * n).reshape(n, 3),
+            "east": _view(v.east, np.float64, 3 * n).reshape(n, 3),
+            "north": _view(v.north, np.float64, 3 * n).reshape(n, 3),
+            "area_m2": _view(v.area_m2, np.float64, n),
+            "source_vertex": _view(v.source_vertex, np.uint32, n),
+            "edge_offset": _view(v.edge_offset, np.uint32, n),
+            "edge_count": _view(v.edge_count, np.uint8, n),
+            "neighbor": _view(v.neighbor, np.uint32, d),
+            "edge": _view(v.edge, np.uint32, d),
+            "corner": _view(v.corner, np.uint32, d),
+            "normal_east": _view(v.normal_east, np.float32, d),
+            "normal_north": _view(v.normal_north, np.float32, d),
+            "edge_first": _view(v.edge_first, np.uint32, e),
+            "edge_second": _view(v.edge_second, np.uint32, e),
+            "edge_length_m": _view(v.edge_length_m, np.float64, e),
+            "edge_distance_m": _view(v.edge_distance_m, np.float64, e),
+            "corner_unit": _view(v.corner_unit, np.float64, 3 * k).reshape(k, 3),
+            "graph_weight": _view(v.graph_weight, np.float64, d),
+            "graph_weight_sum": _view(v.graph_weight_sum, np.float64, n),
+        }
+
+    def hierarchy_level(self, level: int) -> dict[str, np.ndarray]:
+        sizes = (C.c_uint64 * 4)()
+        ptrs = [C.c_void_p() for _ in range(4)]
+        _raise(capi.load().psgb_planet_hierarchy_level(self._h, level, sizes, *[C.byref(p) for p in ptrs]))
+        rows, nnz, na, nt = (int(s) for s in sizes)
+        return {
+            "offset": _view(ptrs[0].value or 0, np.uint32, rows + 1),
+            "column": _view(ptrs[1].value or 0, np.uint32, nnz),
+            "aggregate": _view(ptrs[2].value or 0, np.uint32, na) if na else np.empty(0, np.uint32),
+            "target": _view(ptrs[3].value or 0, np.int64, nt) if nt else np.empty(0, np.int64),
+        }
+
+    def substep_mean_insolation(self, substep: int = 0) -> np.ndarray:
+        out = np.empty(self.cell_count, dtype=np.float32)
+        _raise(capi.load().psgb_substep_mean_insolation(self._h, C.c_int64(substep), _ptr(out)))
+        return out
+
+
+def make_icosphere(subdivision: int, radius_m: float) -> PlanetMesh:
+    return PlanetMesh(subdivision, radius_m)
+
+
+@dataclass
+class TransportGraph:
+    """CSR transport graph of a mesh (heat_transport.hpp:27-36)."""
+
+    mesh: PlanetMesh
+    area_m2: np.ndarray
+    offset: np.ndarray
+    neighbour: np.ndarray
+    weight: np.ndarray
+    weight_sum: np.ndarray
+
+    def size(self) -> int:
+        return len(self.area_m2)
+
+
+def mesh_transport_graph(mesh: PlanetMesh) -> TransportGraph:
+    a = mesh.arrays()
+    offset = np.append(a["edge_offset"].astype(np.uint64), np.uint64(mesh.directed_edge_count))
+    return TransportGraph(mesh, a["area_m2"], offset, a["neighbor"].astype(np.uint64), a["graph_weight"],
+                          a["graph_weight_sum"])
+
+
+# ---- finite-volume operators --------------------------------------------------------
+
+def laplacian(mesh: PlanetMesh, scalar):
+    out = _empty_like(scalar, (mesh.cell_count,))
+    mem, st = _memory_of(scalar, out)
+    _raise(capi.load().psgb_laplacian(mesh.handle, _dtype_code(scalar), _ptr(scalar), _ptr(out), mem, st))
+    return out
+
+
+def gradient(mesh: PlanetMesh, scalar):
+    east = _empty_like(scalar, (mesh.cell_count,))
+    north = _empty_like(scalar, (mesh.cell_count,))
+    mem, st = _memory_of(scalar, east)
+    _raise(capi.load().psgb_gradient(mesh.handle, _dtype_code(scalar), _ptr(scalar), _ptr(east), _ptr(north),
+                                     mem, st))
+    return east, north
+
+
+def divergence(mesh: PlanetMesh, edge_flux):
+    out = _empty_like(edge_flux, (mesh.cell_count,))
+    mem, st = _memory_of(edge_flux, out)
+    _raise(capi.load().psgb_divergence(mesh.handle, _dtype_code(edge_flux), _ptr(edge_flux), _ptr(out), mem, st))
+    return out
+
+
+def diffusion_source(mesh: PlanetMesh, conductance_W_K: float, temperature_K):
+    out = _empty_like(temperature_K, (mesh.cell_count,))
+    mem, st = _memory_of(temperature_K, out)
+    _raise(capi.load().psgb_diffusion_source(mesh.handle, C.c_double(conductance_W_K), _ptr(temperature_K),
+                                             _ptr(out), mem, st))
+    return out
+
+
+# ---- multigrid and solves -------------------------------------------------------------
+
+class GraphMultigrid:
+    """The transport's aggregation-multigrid V-cycle (heat_transport.hpp:60-76) on the GPU."""
+
+    def __init__(self, mesh: PlanetMesh):
+        self.mesh = mesh
+
+    def set_matrix(self, diagonal, off_diagonal) -> None:
+        if len(diagonal) != self.mesh.cell_count or len(off_diagonal) != self.mesh.directed_edge_count:
+            raise ValueError("multigrid matrix does not match the graph")
+        mem, st = _memory_of(diagonal, off_diagonal)
+        _raise(capi.load().psgb_multigrid_set_matrix(self.mesh.handle, _ptr(diagonal), _ptr(off_diagonal), mem, st))
+
+    def precondition(self, rhs):
+        out = _empty_like(rhs, (self.mesh.cell_count,))
+        mem, st = _memory_of(rhs, out)
+        _raise(capi.load().psgb_multigrid_precondition(self.mesh.handle, _dtype_code(rhs), _ptr(rhs), _ptr(out),
+                                                       mem, st))
+        return out
+
+
+def solve_options(**kw) -> capi.SolveOptions:
+    o = capi.default_options()
+    names = {
+        "precision": {"fp64": capi.PRECISION_FP64, "mixed": capi.PRECISION_MIXED},
+        "method": {"pcg": capi.METHOD_PCG, "bicgstab": capi.METHOD_BICGSTAB},
+    }
+    for k, v in kw.items():
+        if k in names and isinstance(v, str):
+            v = names[k][v]
+        setattr(o, k, v)
+    return o
+
+
+@dataclass
+class SolveResult:
+    status: int
+    refinements: int
+    iterations: int
+    relative_residual: float
+
+
+def solve_newton_system(mesh: PlanetMesh, conductance_W_K: float, slope, rhs, x0=None, **options):
+    """(A/s) x + K L x = rhs on the mesh graph (the reference's solve_newton_system)."""
+    x = np.zeros(mesh.cell_count) if x0 is None else (x0.clone() if _is_torch(x0) else np.array(x0, dtype=np.float64))
+    rep = capi.SolveReport()
+    o = solve_options(**options)
+    mem, st = _memory_of(slope, rhs, x)
+    code = capi.load().psgb_solve_newton_system(mesh.handle, C.byref(o), C.c_double(conductance_W_K), _ptr(slope),
+                                                _ptr(rhs), _ptr(x), C.byref(rep), mem, st)
+    if code not in (capi.OK, capi.ERR_NOT_CONVERGED, capi.ERR_BREAKDOWN):
+        _raise(code)
+    return x, SolveResult(rep.status, rep.refinements, rep.iterations, rep.relative_residual)
+
+
+@dataclass
+class StepResult:
+    status: int
+    refinements: int
+    iterations: int
+    relative_residual: float
+    sum_W: float
+    absolute_sum_W: float
+    dissipation_W_K: float
+    closure: float
+
+
+def _step_result(r: capi.StepReport) -> StepResult:
+    return StepResult(r.solve.status, r.solve.refinements, r.solve.iterations, r.solve.relative_residual, r.sum_W,
+                      r.absolute_sum_W, r.dissipation_W_K, r.closure)
+
+
+def step_params(heat_capacity_J_m2_K: float, dt_s: float, conductance_W_K: float = 0.0,
+                edge_conductance: np.ndarray | None = None) -> capi.StepParams:
+    p = capi.StepParams(heat_capacity_J_m2_K, dt_s, conductance_W_K, None)
+    if edge_conductance is not None:
+        arr = np.ascontiguousarray(edge_conductance, dtype=np.float64)
+        p.edge_conductance = arr.ctypes.data
+        p._keep = arr  # keep the host array alive with the struct
+    return p
+
+
+def transport_step(mesh: PlanetMesh, t0_K, source_W_m2, heat_capacity_J_m2_K: float, dt_s: float,
+                   conductance_W_K: float = 0.0, edge_conductance=None, **options):
+    """One implicit heat-transport sub-step with the linear column response."""
+    t_new = _empty_like(t0_K, (mesh.cell_count,))
+    h = _empty_like(t0_K, (mesh.cell_count,))
+    params = step_params(heat_capacity_J_m2_K, dt_s, conductance_W_K, edge_conductance)
+    o = solve_options(**options)
+    rep = capi.StepReport()
+    mem, st = _memory_of(t0_K, source_W_m2, t_new, h)
+    code = capi.load().psgb_transport_step(mesh.handle, C.byref(params), C.byref(o), _ptr(t0_K), _ptr(source_W_m2),
+                                           _ptr(t_new), _ptr(h), C.byref(rep), mem, st)
+    if code not in (capi.OK, capi.ERR_NOT_CONVERGED, capi.ERR_BREAKDOWN):
+        _raise(code)
+    return t_new, h, _step_result(rep)
+
+
+class Batch:
+    """Many planets of uneven levels in one concatenated layout, solved together."""
+
+    def __init__(self, meshes: list[PlanetMesh]):
+        self.meshes = list(meshes)
+        arr = (C.c_void_p * len(meshes))(*[m.handle.value for m in meshes])
+        h = C.c_void_p()
+        _raise(capi.load().psgb_batch_create(arr, len(meshes), C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            capi.load().psgb_batch_destroy(h)
+            self._h = None
+
+    def device_bytes(self) -> int:
+        return int(capi.load().psgb_batch_device_bytes(self._h))
+
+    def transport_step(self, t0, sources, heat_capacity, dt, conductance=None, edge_conductance=None,
+                       out=None, transport_out=None, **options):
+        n = len(self.meshes)
+        params = (capi.StepParams * n)()
+        keep = []
+        for i in range(n):
+            p = step_params(heat_capacity[i] if np.ndim(heat_capacity) else heat_capacity,
+                            dt[i] if np.ndim(dt) else dt,
+                            (conductance[i] if np.ndim(conductance) else conductance) if conductance is not None else 0.0,
+                            edge_conductance[i] if edge_conductance is not None else None)
+            keep.append(p)
+            params[i] = p
+        if out is None:
+            out = [_empty_like(t0[i], (m.cell_count,)) for i, m in enumerate(self.meshes)]
+        mem, st = _memory_of(*t0, *sources, *out)
+        arrs = lambda xs: (C.c_void_p * n)(*[_ptr(x).value for x in xs])
+        h_arr = arrs(transport_out) if transport_out is not None else None
+        o = solve_options(**options)
+        reps = (capi.StepReport * n)()
+        code = capi.load().psgb_batch_transport_step(self._h, params, C.byref(o), arrs(t0), arrs(sources), arrs(out),
+                                                     h_arr, reps, mem, st)
+        if code not in (capi.OK, capi.ERR_NOT_CONVERGED, capi.ERR_BREAKDOWN):
+            _raise(code)
+        return out, [_step_result(r) for r in reps]
+
+
+# ---- column radiation ----------------------------------------------------------------
+
+def column_constants(**kw) -> capi.ColumnConstants:
+    k = capi.ColumnConstants()
+    for name, value in kw.items():
+        setattr(k, name, value)
+    return k
+
+
+def column_radiation(constants: capi.ColumnConstants, temperature_K, humidity, cloud_water, surface_temperature_K,
+                     surface_pressure_Pa):
+    """Layer-major [layers, cells] inputs; returns emissivity, absorbed, fraction,
+    reflectance ([layers, cells]) and scalars [5, cells]."""
+    layers, cells = temperature_K.shape
+    outs = [_empty_like(temperature_K, (layers, cells)) for _ in range(4)]
+    scal = _empty_like(temperature_K, (5, cells))
+    mem, st = _memory_of(temperature_K, humidity, cloud_water, surface_temperature_K, surface_pressure_Pa, scal)
+    _raise(capi.load().psgb_column_radiation(cells, layers, C.byref(constants), _ptr(temperature_K), _ptr(humidity),
+                                             _ptr(cloud_water), _ptr(surface_temperature_K),
+                                             _ptr(surface_pressure_Pa), *[_ptr(o) for o in outs], _ptr(scal), mem, st))
+    return (*outs, scal)

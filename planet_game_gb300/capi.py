@@ -1,0 +1,143 @@
+"""ctypes declarations of the C-ABI in include/planetsim_gb300.h.
+
+The library is the in-tree ``planet_game_gb300/lib/libplanetsim_gb300.so``. Loading
+it never falls back to anything else: if the file is missing, ``load()`` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIBRARY = Path(__file__).resolve().parent / "lib" / "libplanetsim_gb300.so"
+
+OK = 0
+ERR_INVALID_ARGUMENT = 1
+ERR_OUT_OF_MEMORY = 2
+ERR_NOT_CONVERGED = 3
+ERR_BREAKDOWN = 4
+ERR_NON_FINITE = 5
+ERR_CUDA = 6
+ERR_LOGIC = 7
+ERR_BUDGET = 8
+
+MEMORY_HOST = 0
+MEMORY_DEVICE = 1
+DTYPE_F64 = 0
+DTYPE_F32 = 1
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
+METHOD_PCG = 0
+METHOD_BICGSTAB = 1
+
+
+class PlanetInfo(C.Structure):
+    _fields_ = [("cells", C.c_uint64), ("edges", C.c_uint64), ("directed_edges", C.c_uint64),
+                ("corners", C.c_uint64), ("levels", C.c_uint32), ("level_rows", C.c_uint32 * 8),
+                ("device_bytes", C.c_uint64)]
+
+
+class MeshView(C.Structure):
+    _fields_ = [(name, C.c_void_p) for name in (
+        "center", "east", "north", "area_m2", "source_vertex", "edge_offset", "edge_count", "neighbor",
+        "edge", "corner", "normal_east", "normal_north", "edge_first", "edge_second", "edge_length_m",
+        "edge_distance_m", "corner_unit", "graph_weight", "graph_weight_sum")]
+
+
+class SolveOptions(C.Structure):
+    _fields_ = [("precision", C.c_int), ("method", C.c_int), ("tolerance", C.c_double),
+                ("inner_tolerance", C.c_double), ("max_iterations", C.c_int), ("max_refinements", C.c_int),
+                ("poll", C.c_int), ("pre_sweeps", C.c_int), ("post_sweeps", C.c_int),
+                ("jacobi_omega", C.c_double)]
+
+
+class SolveReport(C.Structure):
+    _fields_ = [("status", C.c_int), ("refinements", C.c_int), ("iterations", C.c_int),
+                ("relative_residual", C.c_double)]
+
+
+class StepParams(C.Structure):
+    _fields_ = [("heat_capacity_J_m2_K", C.c_double), ("dt_s", C.c_double), ("conductance_W_K", C.c_double),
+                ("edge_conductance", C.c_void_p)]
+
+
+class StepReport(C.Structure):
+    _fields_ = [("solve", SolveReport), ("sum_W", C.c_double), ("absolute_sum_W", C.c_double),
+                ("dissipation_W_K", C.c_double), ("closure", C.c_double)]
+
+
+class ColumnConstants(C.Structure):
+    _fields_ = [(name, C.c_double) for name in (
+        "dry_optical_depth", "vapour_absorption_m2_kg", "in_cloud_water_path_kg_m2", "effective_radius_m",
+        "cloud_asymmetry", "cloud_longwave_absorption_m2_kg", "reference_pressure_Pa", "gravity_m_s2",
+        "stefan_boltzmann")]
+
+
+P = C.c_void_p
+_SIGNATURES = {
+    "psgb_last_error": (C.c_char_p, []),
+    "psgb_abi_version": (C.c_int, []),
+    "psgb_planet_create": (C.c_int, [C.c_uint32, C.c_double, C.POINTER(P)]),
+    "psgb_planet_destroy": (None, [P]),
+    "psgb_planet_info_get": (C.c_int, [P, C.POINTER(PlanetInfo)]),
+    "psgb_planet_mesh_view": (C.c_int, [P, C.POINTER(MeshView)]),
+    "psgb_planet_hierarchy_level": (C.c_int, [P, C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(P), C.POINTER(P),
+                                              C.POINTER(P), C.POINTER(P)]),
+    "psgb_laplacian": (C.c_int, [P, C.c_int, P, P, C.c_int, P]),
+    "psgb_gradient": (C.c_int, [P, C.c_int, P, P, P, C.c_int, P]),
+    "psgb_divergence": (C.c_int, [P, C.c_int, P, P, C.c_int, P]),
+    "psgb_diffusion_source": (C.c_int, [P, C.c_double, P, P, C.c_int, P]),
+    "psgb_multigrid_set_matrix": (C.c_int, [P, P, P, C.c_int, P]),
+    "psgb_multigrid_precondition": (C.c_int, [P, C.c_int, P, P, C.c_int, P]),
+    "psgb_solve_options_default": (None, [C.POINTER(SolveOptions)]),
+    "psgb_solve_newton_system": (C.c_int, [P, C.POINTER(SolveOptions), C.c_double, P, P, P,
+                                           C.POINTER(SolveReport), C.c_int, P]),
+    "psgb_transport_step": (C.c_int, [P, C.POINTER(StepParams), C.POINTER(SolveOptions), P, P, P, P,
+                                      C.POINTER(StepReport), C.c_int, P]),
+    "psgb_batch_create": (C.c_int, [C.POINTER(P), C.c_uint32, C.POINTER(P)]),
+    "psgb_batch_destroy": (None, [P]),
+    "psgb_batch_device_bytes": (C.c_uint64, [P]),
+    "psgb_batch_transport_step": (C.c_int, [P, C.POINTER(StepParams), C.POINTER(SolveOptions), C.POINTER(P),
+                                            C.POINTER(P), C.POINTER(P), C.POINTER(P), C.POINTER(StepReport),
+                                            C.c_int, P]),
+    "psgb_column_radiation": (C.c_int, [C.c_uint32, C.c_uint32, C.POINTER(ColumnConstants), P, P, P, P, P, P, P,
+                                        P, P, P, C.c_int, P]),
+    "psgb_substep_mean_insolation": (C.c_int, [P, C.c_int64, P]),
+}
+
+# Every symbol the header declares (checked by the CPU test suite).
+EXPORTED = tuple(_SIGNATURES)
+
+_lib: C.CDLL | None = None
+
+
+class GB300Error(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"planetsim_gb300 error {code}: {message}")
+        self.code = code
+
+
+def load() -> C.CDLL:
+    """Load the in-tree library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIBRARY.exists():
+            raise FileNotFoundError(f"{LIBRARY} is missing: run planet_game_gb300.build.build_library()")
+        lib = C.CDLL(str(LIBRARY))
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def check(code: int) -> int:
+    if code != OK:
+        raise GB300Error(code, load().psgb_last_error().decode())
+    return code
+
+
+def default_options() -> SolveOptions:
+    o = SolveOptions()
+    load().psgb_solve_options_default(C.byref(o))
+    return o

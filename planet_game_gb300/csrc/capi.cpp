@@ -1,0 +1,682 @@
+// C-ABI of the GB300 heat-transport path (include/planetsim_gb300.h).
+//
+// Maps the reference's exception conventions onto status codes:
+// std::invalid_argument -> PSGB_ERR_INVALID_ARGUMENT, std::logic_error ->
+// PSGB_ERR_LOGIC, allocation failures -> PSGB_ERR_OUT_OF_MEMORY, CUDA errors ->
+// PSGB_ERR_CUDA; the message is kept per thread for psgb_last_error().
+#include "../../include/planetsim_gb300.h"
+
+#include "column.hpp"
+#include "host/insolation.hpp"
+#include "operators.hpp"
+#include "solver.hpp"
+
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+struct psgb_planet {
+    std::unique_ptr<psgb::Planet> planet;
+    // lazily created device staging for host-memory calls
+    psgb::DeviceStore stage_store;
+    std::vector<double*> stage;
+    std::size_t stage_len = 0;
+};
+
+struct psgb_batch {
+    std::unique_ptr<psgb::Batch> batch;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& message) {
+    g_last_error = message;
+    return code;
+}
+
+template <typename F>
+int guarded(F&& body) {
+    try {
+        g_last_error.clear();
+        return body();
+    } catch (const std::invalid_argument& e) {
+        return fail(PSGB_ERR_INVALID_ARGUMENT, e.what());
+    } catch (const std::bad_alloc& e) {
+        return fail(PSGB_ERR_OUT_OF_MEMORY, e.what());
+    } catch (const psgb::CudaError& e) {
+        const std::string m = e.what();
+        return fail(m.find("out of memory") != std::string::npos ? PSGB_ERR_OUT_OF_MEMORY : PSGB_ERR_CUDA, m);
+    } catch (const std::logic_error& e) {
+        return fail(PSGB_ERR_LOGIC, e.what());
+    } catch (const std::exception& e) {
+        return fail(PSGB_ERR_CUDA, e.what());
+    }
+}
+
+cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
+
+void require(bool ok, const char* message) {
+    if (!ok) throw std::invalid_argument(message);
+}
+
+void require_memory(int memory) {
+    require(memory == PSGB_MEMORY_HOST || memory == PSGB_MEMORY_DEVICE, "memory must be PSGB_MEMORY_HOST or PSGB_MEMORY_DEVICE");
+}
+
+std::size_t dtype_size(int dtype) {
+    if (dtype == PSGB_DTYPE_F64) return 8;
+    if (dtype == PSGB_DTYPE_F32) return 4;
+    throw std::invalid_argument("dtype must be PSGB_DTYPE_F64 or PSGB_DTYPE_F32");
+}
+
+// The planet's device state, uploaded on first use.
+const psgb::DevMesh& device_mesh(psgb_planet* h) {
+    psgb::upload_planet(*h->planet);
+    return h->planet->dev;
+}
+
+// Device staging buffers of max(P, edges) doubles each.
+double* stage(psgb_planet* h, int index) {
+    const psgb::DevMesh& d = device_mesh(h);
+    const std::size_t len = std::max<std::size_t>(d.p, d.edges);
+    while (static_cast<int>(h->stage.size()) <= index) h->stage.push_back(h->stage_store.alloc<double>(len));
+    h->stage_len = len;
+    return h->stage[index];
+}
+
+psgb::Batch& solo(psgb_planet* h) {
+    if (!h->planet->solo) h->planet->solo = psgb::make_batch({h->planet.get()});
+    return *h->planet->solo;
+}
+
+// Copy `count` elements in (host or device source) to a device destination.
+void copy_in(void* dst, const void* src, std::size_t bytes, int memory, cudaStream_t st) {
+    PSGB_CUDA(cudaMemcpyAsync(dst, src, bytes, memory == PSGB_MEMORY_HOST ? cudaMemcpyHostToDevice
+                                                                        : cudaMemcpyDeviceToDevice, st));
+}
+void copy_out(void* dst, const void* src, std::size_t bytes, int memory, cudaStream_t st) {
+    PSGB_CUDA(cudaMemcpyAsync(dst, src, bytes, memory == PSGB_MEMORY_HOST ? cudaMemcpyDeviceToHost
+                                                                        : cudaMemcpyDeviceToDevice, st));
+}
+
+psgb::SolveOptions to_options(const psgb_solve_options* o) {
+    psgb_solve_options d;
+    psgb_solve_options_default(&d);
+    if (o == nullptr) o = &d;
+    psgb::SolveOptions s;
+    require(o->precision == PSGB_PRECISION_FP64 || o->precision == PSGB_PRECISION_MIXED, "unknown precision");
+    require(o->method == PSGB_METHOD_PCG || o->method == PSGB_METHOD_BICGSTAB, "unknown Krylov method");
+    require(o->tolerance > 0.0 && std::isfinite(o->tolerance), "tolerance must be positive");
+    require(o->inner_tolerance > 0.0 && o->inner_tolerance < 1.0, "inner tolerance must be in (0, 1)");
+    require(o->max_iterations > 0 && o->max_refinements > 0 && o->poll > 0, "iteration limits must be positive");
+    require(o->pre_sweeps >= 1 && o->post_sweeps >= 0 && o->pre_sweeps <= 8 && o->post_sweeps <= 8,
+            "Jacobi sweeps must be 1..8 (pre) and 0..8 (post)");
+    require(o->jacobi_omega > 0.0 && o->jacobi_omega < 2.0, "Jacobi damping must be in (0, 2)");
+    s.precision = o->precision;
+    s.method = o->method;
+    s.tolerance = o->tolerance;
+    s.inner_tolerance = o->inner_tolerance;
+    s.max_iterations = o->max_iterations;
+    s.max_refinements = o->max_refinements;
+    s.poll = o->poll;
+    return s;
+}
+
+void apply_smoother(psgb::Batch& b, const psgb_solve_options* o) {
+    psgb_solve_options d;
+    psgb_solve_options_default(&d);
+    if (o == nullptr) o = &d;
+    b.smoother.pre = o->pre_sweeps;
+    b.smoother.post = o->post_sweeps;
+    b.smoother.omega = o->jacobi_omega;
+}
+
+int status_of(const psgb::InstanceScalars& s) {
+    switch (s.outer_status) {
+        case psgb::kConverged: return PSGB_OK;
+        case psgb::kNonFinite: return PSGB_ERR_NON_FINITE;
+        case psgb::kCap: return s.status == psgb::kBreakdown ? PSGB_ERR_BREAKDOWN : PSGB_ERR_NOT_CONVERGED;
+        default: return PSGB_ERR_NOT_CONVERGED;
+    }
+}
+
+void fill_report(const psgb::InstanceScalars& s, psgb_solve_report* r) {
+    if (r == nullptr) return;
+    r->status = status_of(s);
+    r->refinements = s.refinements;
+    r->iterations = s.inner_total;
+    r->relative_residual = s.outer_b_norm > 0.0 ? s.outer_r_norm / s.outer_b_norm : 0.0;
+}
+
+// Per-entry conductance in the batch's fine ELL layout from per-undirected-edge values.
+void scatter_edge_conductance(const psgb::Planet& p, const double* per_edge, std::int64_t base,
+                              std::size_t P0, std::vector<double>& out) {
+    const psgb::HostMesh& m = p.mesh;
+    for (std::size_t c = 0; c < m.cells; ++c) {
+        for (std::uint32_t k = 0; k < m.edge_count[c]; ++k) {
+            const double g = per_edge[m.nb_edge[m.edge_offset[c] + k]];
+            if (!(g >= 0.0) || !std::isfinite(g)) throw std::invalid_argument("edge conductance must be finite and non-negative");
+            out[k * P0 + base + c] = g;
+        }
+    }
+}
+
+// Assemble (A/s + K L) on every planet of the batch unless the parameters equal the
+// ones the current matrix was built from.
+void assemble_step_matrix(psgb::Batch& b, const psgb_step_params* params, cudaStream_t st) {
+    const std::uint32_t I = b.instances;
+    std::vector<double> key;
+    bool per_edge = false;
+    for (std::uint32_t i = 0; i < I; ++i) {
+        const psgb_step_params& p = params[i];
+        require(p.heat_capacity_J_m2_K > 0.0 && std::isfinite(p.heat_capacity_J_m2_K), "heat capacity must be finite and positive");
+        require(p.dt_s > 0.0 && std::isfinite(p.dt_s), "time step must be finite and positive");
+        if (p.edge_conductance == nullptr) {
+            require(p.conductance_W_K > 0.0 && std::isfinite(p.conductance_W_K), "transport conductance must be finite and positive");
+        }
+        key.push_back(p.heat_capacity_J_m2_K);
+        key.push_back(p.dt_s);
+        key.push_back(p.edge_conductance == nullptr ? p.conductance_W_K : -1.0);
+        if (p.edge_conductance != nullptr) {
+            per_edge = true;
+            const std::size_t e = b.planets[i]->mesh.edges;
+            key.insert(key.end(), p.edge_conductance, p.edge_conductance + e);
+        }
+    }
+    if (b.matrix_ready && key == b.assembled_key) return;
+    const std::size_t P0 = b.levels[0].rows;
+    std::vector<double> slope_of(I), conductance(I);
+    for (std::uint32_t i = 0; i < I; ++i) {
+        slope_of[i] = params[i].dt_s / params[i].heat_capacity_J_m2_K;
+        conductance[i] = params[i].edge_conductance == nullptr ? params[i].conductance_W_K : 0.0;
+    }
+    PSGB_CUDA(cudaMemcpyAsync(b.slope_of, slope_of.data(), I * sizeof(double), cudaMemcpyHostToDevice, st));
+    PSGB_CUDA(cudaMemcpyAsync(b.conductance, conductance.data(), I * sizeof(double), cudaMemcpyHostToDevice, st));
+    const double* edge_g = nullptr;
+    if (per_edge) {
+        if (b.edge_g == nullptr) b.edge_g = b.store.alloc<double>(6 * P0);
+        std::vector<double> g(6 * P0, 0.0);
+        for (std::uint32_t i = 0; i < I; ++i) {
+            if (params[i].edge_conductance != nullptr) {
+                scatter_edge_conductance(*b.planets[i], params[i].edge_conductance, b.fine_base[i], P0, g);
+            } else {
+                const psgb::HostMesh& m = b.planets[i]->mesh;
+                for (std::size_t c = 0; c < m.cells; ++c)
+                    for (std::uint32_t k = 0; k < m.edge_count[c]; ++k) g[k * P0 + b.fine_base[i] + c] = params[i].conductance_W_K;
+            }
+        }
+        PSGB_CUDA(cudaMemcpyAsync(b.edge_g, g.data(), g.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+        PSGB_CUDA(cudaStreamSynchronize(st));
+        edge_g = b.edge_g;
+    }
+    // slope field (dt/C per cell of every planet) in b.tmp2
+    std::vector<double> slope(P0, 1.0);
+    for (std::uint32_t i = 0; i < I; ++i) {
+        const std::size_t n = b.planets[i]->mesh.cells;
+        for (std::size_t c = 0; c < n; ++c) slope[b.fine_base[i] + c] = slope_of[i];
+    }
+    PSGB_CUDA(cudaMemcpyAsync(b.tmp2, slope.data(), P0 * sizeof(double), cudaMemcpyHostToDevice, st));
+    psgb::assemble_transport(b, b.tmp2, b.conductance, edge_g, st);
+    psgb::prepare_levels(b, st);
+    PSGB_CUDA(cudaStreamSynchronize(st));
+    b.assembled_key = key;
+    b.step_edge_conductance = edge_g;
+}
+
+// One transport step on every planet of a batch; inputs already in b.t0 / b.src.
+void run_step(psgb::Batch& b, const psgb::SolveOptions& opt, cudaStream_t st) {
+    psgb::StepView v = step_view(b);
+    psgb::launch_step_rhs(v, b.t0, b.src, b.bb, b.tmp, b.xr, st);
+    psgb::solve(b, opt, b.bb, b.xr, st);
+    psgb::launch_step_finish(v, b.xr, b.t0, b.src, b.hout, b.tnew, b.partial, b.sums, st);
+    PSGB_CUDA(cudaGetLastError());
+}
+
+void step_reports(psgb::Batch& b, psgb_step_report* reports, cudaStream_t st) {
+    std::vector<double> sums(std::size_t(b.instances) * 8);
+    PSGB_CUDA(cudaMemcpyAsync(sums.data(), b.sums, sums.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    PSGB_CUDA(cudaStreamSynchronize(st));
+    if (reports == nullptr) return;
+    for (std::uint32_t i = 0; i < b.instances; ++i) {
+        psgb_step_report& r = reports[i];
+        fill_report(b.host_scalars[i], &r.solve);
+        const double* s = &sums[std::size_t(i) * 8];
+        r.sum_W = s[0];
+        r.absolute_sum_W = s[1];
+        r.dissipation_W_K = s[2];
+        r.closure = s[4] > 0.0 ? std::fabs(s[5] - s[3]) / s[4] : std::fabs(s[5] - s[3]);
+    }
+}
+
+}  // namespace
+
+
+extern "C" {
+
+const char* psgb_last_error(void) { return g_last_error.c_str(); }
+int psgb_abi_version(void) { return PSGB_ABI_VERSION; }
+
+void psgb_solve_options_default(psgb_solve_options* out) {
+    if (out == nullptr) return;
+    out->precision = PSGB_PRECISION_FP64;
+    out->method = PSGB_METHOD_BICGSTAB;
+    out->tolerance = 1e-10;
+    out->inner_tolerance = 1e-4;
+    out->max_iterations = 1000;
+    out->max_refinements = 20;
+    out->poll = 4;
+    out->pre_sweeps = 2;
+    out->post_sweeps = 2;
+    out->jacobi_omega = 0.8;
+}
+
+int psgb_planet_create(uint32_t level, double radius_m, psgb_planet** out) {
+    return guarded([&] {
+        require(out != nullptr, "output handle pointer is null");
+        *out = nullptr;
+        auto h = std::make_unique<psgb_planet>();
+        h->planet = psgb::make_planet(level, radius_m);
+        *out = h.release();
+        return PSGB_OK;
+    });
+}
+
+void psgb_planet_destroy(psgb_planet* planet) { delete planet; }
+
+int psgb_planet_info_get(const psgb_planet* h, psgb_planet_info* out) {
+    return guarded([&] {
+        require(h != nullptr && out != nullptr, "null argument");
+        const psgb::Planet& p = *h->planet;
+        std::memset(out, 0, sizeof(*out));
+        out->cells = p.mesh.cells;
+        out->edges = p.mesh.edges;
+        out->directed_edges = p.mesh.directed;
+        out->corners = p.mesh.corners;
+        out->levels = static_cast<uint32_t>(p.hierarchy.levels.size());
+        for (std::size_t l = 0; l < p.hierarchy.levels.size() && l < 8; ++l) out->level_rows[l] = p.hierarchy.levels[l].size;
+        out->device_bytes = p.store.bytes() + (p.solo ? p.solo->store.bytes() : 0) + h->stage_store.bytes();
+        return PSGB_OK;
+    });
+}
+
+int psgb_planet_mesh_view(const psgb_planet* h, psgb_mesh_view* out) {
+    return guarded([&] {
+        require(h != nullptr && out != nullptr, "null argument");
+        const psgb::HostMesh& m = h->planet->mesh;
+        out->center = m.center.data();
+        out->east = m.east.data();
+        out->north = m.north.data();
+        out->area_m2 = m.area_m2.data();
+        out->source_vertex = m.source_vertex.data();
+        out->edge_offset = m.edge_offset.data();
+        out->edge_count = m.edge_count.data();
+        out->neighbor = m.nb_cell.data();
+        out->edge = m.nb_edge.data();
+        out->corner = m.nb_corner.data();
+        out->normal_east = m.normal_east.data();
+        out->normal_north = m.normal_north.data();
+        out->edge_first = m.edge_first.data();
+        out->edge_second = m.edge_second.data();
+        out->edge_length_m = m.edge_length_m.data();
+        out->edge_distance_m = m.edge_distance_m.data();
+        out->corner_unit = m.corner_unit.data();
+        out->graph_weight = h->planet->graph.weight.data();
+        out->graph_weight_sum = h->planet->graph.weight_sum.data();
+        return PSGB_OK;
+    });
+}
+
+int psgb_planet_hierarchy_level(const psgb_planet* h, uint32_t level, uint64_t sizes[4],
+                                const uint32_t** offset, const uint32_t** column,
+                                const uint32_t** aggregate, const int64_t** target) {
+    return guarded([&] {
+        require(h != nullptr && sizes != nullptr, "null argument");
+        const auto& levels = h->planet->hierarchy.levels;
+        require(level < levels.size(), "multigrid level out of range");
+        const psgb::HostLevel& l = levels[level];
+        sizes[0] = l.size;
+        sizes[1] = l.column.size();
+        sizes[2] = l.aggregate.size();
+        sizes[3] = l.target.size();
+        if (offset) *offset = l.offset.data();
+        if (column) *column = l.column.data();
+        if (aggregate) *aggregate = l.aggregate.data();
+        if (target) *target = l.target.data();
+        return PSGB_OK;
+    });
+}
+
+int psgb_laplacian(psgb_planet* h, int dtype, const void* scalar, void* result, int memory, void* stream) {
+    return guarded([&] {
+        require(h != nullptr && scalar != nullptr && result != nullptr, "null argument");
+        require_memory(memory);
+        const std::size_t es = dtype_size(dtype);
+        const psgb::DevMesh& d = device_mesh(h);
+        cudaStream_t st = as_stream(stream);
+        const void* in = scalar;
+        void* out = result;
+        if (memory == PSGB_MEMORY_HOST) {
+            double* a = stage(h, 0);
+            double* b = stage(h, 1);
+            copy_in(a, scalar, d.n * es, memory, st);
+            in = a;
+            out = b;
+        }
+        if (dtype == PSGB_DTYPE_F64) psgb::launch_laplacian<double>(d, static_cast<const double*>(in), static_cast<double*>(out), st);
+        else psgb::launch_laplacian<float>(d, static_cast<const float*>(in), static_cast<float*>(out), st);
+        PSGB_CUDA(cudaGetLastError());
+        if (memory == PSGB_MEMORY_HOST) {
+            copy_out(result, out, d.n * es, memory, st);
+            PSGB_CUDA(cudaStreamSynchronize(st));
+        }
+        return PSGB_OK;
+    });
+}
+
+int psgb_gradient(psgb_planet* h, int dtype, const void* scalar, void* east, void* north, int memory, void* stream) {
+    return guarded([&] {
+        require(h != nullptr && scalar != nullptr && east != nullptr && north != nullptr, "null argument");
+        require_memory(memory);
+        const std::size_t es = dtype_size(dtype);
+        const psgb::DevMesh& d = device_mesh(h);
+        cudaStream_t st = as_stream(stream);
+        const void* in = scalar;
+        void *e = east, *n = north;
+        if (memory == PSGB_MEMORY_HOST) {
+            double* a = stage(h, 0);
+            copy_in(a, scalar, d.n * es, memory, st);
+            in = a;
+            e = stage(h, 1);
+            n = stage(h, 2);
+        }
+        if (dtype == PSGB_DTYPE_F64) psgb::launch_gradient<double>(d, static_cast<const double*>(in), static_cast<double*>(e), static_cast<double*>(n), st);
+        else psgb::launch_gradient<float>(d, static_cast<const float*>(in), static_cast<float*>(e), static_cast<float*>(n), st);
+        PSGB_CUDA(cudaGetLastError());
+        if (memory == PSGB_MEMORY_HOST) {
+            copy_out(east, e, d.n * es, memory, st);
+            copy_out(north, n, d.n * es, memory, st);
+            PSGB_CUDA(cudaStreamSynchronize(st));
+        }
+        return PSGB_OK;
+    });
+}
+
+int psgb_divergence(psgb_planet* h, int dtype, const void* edge_flux, void* result, int memory, void* stream) {
+    return guarded([&] {
+        require(h != nullptr && edge_flux != nullptr && result != nullptr, "null argument");
+        require_memory(memory);
+        const std::size_t es = dtype_size(dtype);
+        const psgb::DevMesh& d = device_mesh(h);
+        cudaStream_t st = as_stream(stream);
+        const void* in = edge_flux;
+        void* out = result;
+        if (memory == PSGB_MEMORY_HOST) {
+            double* a = stage(h, 0);
+            copy_in(a, edge_flux, d.edges * es, memory, st);
+            in = a;
+            out = stage(h, 1);
+        }
+        if (dtype == PSGB_DTYPE_F64) psgb::launch_divergence<double>(d, static_cast<const double*>(in), static_cast<double*>(out), st);
+        else psgb::launch_divergence<float>(d, static_cast<const float*>(in), static_cast<float*>(out), st);
+        PSGB_CUDA(cudaGetLastError());
+        if (memory == PSGB_MEMORY_HOST) {
+            copy_out(result, out, d.n * es, memory, st);
+            PSGB_CUDA(cudaStreamSynchronize(st));
+        }
+        return PSGB_OK;
+    });
+}
+
+int psgb_diffusion_source(psgb_planet* h, double conductance_W_K, const double* temperature_K,
+                          double* source_W_m2, int memory, void* stream) {
+    return guarded([&] {
+        require(h != nullptr && temperature_K != nullptr && source_W_m2 != nullptr, "null argument");
+        require_memory(memory);
+        const psgb::DevMesh& d = device_mesh(h);
+        cudaStream_t st = as_stream(stream);
+        const double* in = temperature_K;
+        double* out = source_W_m2;
+        if (memory == PSGB_MEMORY_HOST) {
+            double* a = stage(h, 0);
+            copy_in(a, temperature_K, d.n * 8, memory, st);
+            in = a;
+            out = stage(h, 1);
+        }
+        psgb::launch_diffusion_source(d, conductance_W_K, in, out, st);
+        PSGB_CUDA(cudaGetLastError());
+        if (memory == PSGB_MEMORY_HOST) {
+            copy_out(source_W_m2, out, d.n * 8, memory, st);
+            PSGB_CUDA(cudaStreamSynchronize(st));
+        }
+        return PSGB_OK;
+    });
+}
+
+int psgb_multigrid_set_matrix(psgb_planet* h, const double* diagonal, const double* off_diagonal, int memory,
+                              void* stream) {
+    return guarded([&] {
+        require(h != nullptr && diagonal != nullptr && off_diagonal != nullptr, "null argument");
+        require_memory(memory);
+        psgb::Batch& b = solo(h);
+        const psgb::Planet& p = *h->planet;
+        cudaStream_t st = as_stream(stream);
+        if (b.csr_values == nullptr) b.csr_values = b.store.alloc<double>(p.mesh.directed);
+        copy_in(b.tmp2, diagonal, p.mesh.cells * 8, memory, st);
+        copy_in(b.csr_values, off_diagonal, p.mesh.directed * 8, memory, st);
+        psgb::set_matrix_csr(b, b.tmp2, b.csr_values, st);
+        psgb::prepare_levels(b, st);
+        PSGB_CUDA(cudaStreamSynchronize(st));
+        b.assembled_key.clear();
+        return PSGB_OK;
+    });
+}
+
+int psgb_multigrid_precondition(psgb_planet* h, int dtype, const void* rhs, void* solution, int memory,
+                                void* stream) {
+    return guarded([&] {
+        require(h != nullptr && rhs != nullptr && solution != nullptr, "null argument");
+        require_memory(memory);
+        const std::size_t es = dtype_size(dtype);
+        psgb::Batch& b = solo(h);
+        require(b.matrix_ready, "precondition before set_matrix");
+        const std::size_t n = h->planet->mesh.cells;
+        cudaStream_t st = as_stream(stream);
+        if (dtype == PSGB_DTYPE_F64) {
+            copy_in(b.bb, rhs, n * es, memory, st);
+            psgb::vcycle<double>(b, b.bb, b.k64[9], psgb::kGateAlways, false, st);
+            PSGB_CUDA(cudaGetLastError());
+            copy_out(solution, b.k64[9], n * es, memory, st);
+        } else {
+            copy_in(b.k32[8], rhs, n * es, memory, st);
+            psgb::vcycle<float>(b, b.k32[8], b.k32[9], psgb::kGateAlways, false, st);
+            PSGB_CUDA(cudaGetLastError());
+            copy_out(solution, b.k32[9], n * es, memory, st);
+        }
+        if (memory == PSGB_MEMORY_HOST) PSGB_CUDA(cudaStreamSynchronize(st));
+        return PSGB_OK;
+    });
+}
+
+int psgb_solve_newton_system(psgb_planet* h, const psgb_solve_options* options, double conductance_W_K,
+                             const double* slope, const double* rhs, double* x, psgb_solve_report* report,
+                             int memory, void* stream) {
+    return guarded([&] {
+        require(h != nullptr && slope != nullptr && rhs != nullptr && x != nullptr, "null argument");
+        require_memory(memory);
+        require(std::isfinite(conductance_W_K) && conductance_W_K > 0.0, "transport conductance must be finite and positive");
+        const psgb::SolveOptions opt = to_options(options);
+        psgb::Batch& b = solo(h);
+        apply_smoother(b, options);
+        const std::size_t n = h->planet->mesh.cells;
+        cudaStream_t st = as_stream(stream);
+        copy_in(b.tmp2, slope, n * 8, memory, st);
+        PSGB_CUDA(cudaMemcpyAsync(b.conductance, &conductance_W_K, sizeof(double), cudaMemcpyHostToDevice, st));
+        psgb::assemble_transport(b, b.tmp2, b.conductance, nullptr, st);
+        psgb::prepare_levels(b, st);
+        b.assembled_key.clear();
+        copy_in(b.bb, rhs, n * 8, memory, st);
+        psgb::launch_mask_rhs(n, b.tmp2, b.bb, st);
+        copy_in(b.xr, x, n * 8, memory, st);
+        psgb::solve(b, opt, b.bb, b.xr, st);
+        copy_out(x, b.xr, n * 8, memory, st);
+        PSGB_CUDA(cudaStreamSynchronize(st));
+        fill_report(b.host_scalars[0], report);
+        return status_of(b.host_scalars[0]);
+    });
+}
+
+int psgb_transport_step(psgb_planet* h, const psgb_step_params* params, const psgb_solve_options* options,
+                        const double* t0_K, const double* source_W_m2, double* t_new_K, double* transport_W_m2,
+                        psgb_step_report* report, int memory, void* stream) {
+    return guarded([&] {
+        require(h != nullptr && params != nullptr && t0_K != nullptr && source_W_m2 != nullptr && t_new_K != nullptr,
+                "null argument");
+        require_memory(memory);
+        const psgb::SolveOptions opt = to_options(options);
+        psgb::Batch& b = solo(h);
+        apply_smoother(b, options);
+        cudaStream_t st = as_stream(stream);
+        assemble_step_matrix(b, params, st);
+        const std::size_t n = h->planet->mesh.cells;
+        copy_in(b.t0, t0_K, n * 8, memory, st);
+        copy_in(b.src, source_W_m2, n * 8, memory, st);
+        run_step(b, opt, st);
+        copy_out(t_new_K, b.tnew, n * 8, memory, st);
+        if (transport_W_m2 != nullptr) copy_out(transport_W_m2, b.hout, n * 8, memory, st);
+        psgb_step_report local;
+        step_reports(b, &local, st);
+        if (report != nullptr) *report = local;
+        return local.solve.status;
+    });
+}
+
+int psgb_batch_create(psgb_planet* const* planets, uint32_t count, psgb_batch** out) {
+    return guarded([&] {
+        require(planets != nullptr && out != nullptr && count > 0, "a batch needs planets");
+        *out = nullptr;
+        std::vector<psgb::Planet*> list;
+        for (uint32_t i = 0; i < count; ++i) {
+            require(planets[i] != nullptr, "null planet in batch");
+            list.push_back(planets[i]->planet.get());
+        }
+        auto h = std::make_unique<psgb_batch>();
+        h->batch = psgb::make_batch(list);
+        *out = h.release();
+        return PSGB_OK;
+    });
+}
+
+void psgb_batch_destroy(psgb_batch* batch) { delete batch; }
+
+uint64_t psgb_batch_device_bytes(const psgb_batch* batch) {
+    return batch == nullptr ? 0 : batch->batch->store.bytes();
+}
+
+int psgb_batch_transport_step(psgb_batch* h, const psgb_step_params* params, const psgb_solve_options* options,
+                              const double* const* t0_K, const double* const* source_W_m2,
+                              double* const* t_new_K, double* const* transport_W_m2, psgb_step_report* reports,
+                              int memory, void* stream) {
+    return guarded([&] {
+        require(h != nullptr && params != nullptr && t0_K != nullptr && source_W_m2 != nullptr && t_new_K != nullptr,
+                "null argument");
+        require_memory(memory);
+        const psgb::SolveOptions opt = to_options(options);
+        psgb::Batch& b = *h->batch;
+        apply_smoother(b, options);
+        cudaStream_t st = as_stream(stream);
+        assemble_step_matrix(b, params, st);
+        for (std::uint32_t i = 0; i < b.instances; ++i) {
+            const std::size_t n = b.planets[i]->mesh.cells;
+            require(t0_K[i] != nullptr && source_W_m2[i] != nullptr && t_new_K[i] != nullptr, "null planet array");
+            copy_in(b.t0 + b.fine_base[i], t0_K[i], n * 8, memory, st);
+            copy_in(b.src + b.fine_base[i], source_W_m2[i], n * 8, memory, st);
+        }
+        run_step(b, opt, st);
+        for (std::uint32_t i = 0; i < b.instances; ++i) {
+            const std::size_t n = b.planets[i]->mesh.cells;
+            copy_out(t_new_K[i], b.tnew + b.fine_base[i], n * 8, memory, st);
+            if (transport_W_m2 != nullptr && transport_W_m2[i] != nullptr) {
+                copy_out(transport_W_m2[i], b.hout + b.fine_base[i], n * 8, memory, st);
+            }
+        }
+        std::vector<psgb_step_report> local(b.instances);
+        step_reports(b, local.data(), st);
+        int worst = PSGB_OK;
+        for (std::uint32_t i = 0; i < b.instances; ++i) {
+            if (reports != nullptr) reports[i] = local[i];
+            if (local[i].solve.status != PSGB_OK && worst == PSGB_OK) worst = local[i].solve.status;
+        }
+        return worst;
+    });
+}
+
+int psgb_column_radiation(uint32_t cells, uint32_t layers, const psgb_column_constants* constants,
+                          const double* temperature_K, const double* humidity, const double* cloud_water,
+                          const double* surface_temperature_K, const double* surface_pressure_Pa,
+                          double* emissivity, double* absorbed, double* fraction, double* reflectance,
+                          double* scalars, int memory, void* stream) {
+    return guarded([&] {
+        require(constants != nullptr && temperature_K != nullptr && humidity != nullptr && cloud_water != nullptr &&
+                    surface_temperature_K != nullptr && surface_pressure_Pa != nullptr && emissivity != nullptr &&
+                    absorbed != nullptr && fraction != nullptr && reflectance != nullptr && scalars != nullptr,
+                "null argument");
+        require(layers >= 1 && layers <= 16, "column radiation supports 1 to 16 layers");
+        require_memory(memory);
+        const psgb::ColumnConstants k{constants->dry_optical_depth, constants->vapour_absorption_m2_kg,
+                                      constants->in_cloud_water_path_kg_m2, constants->effective_radius_m,
+                                      constants->cloud_asymmetry, constants->cloud_longwave_absorption_m2_kg,
+                                      constants->reference_pressure_Pa, constants->gravity_m_s2,
+                                      constants->stefan_boltzmann};
+        require(k.gravity > 0.0 && k.reference_pressure > 0.0 && k.in_cloud_water_path > 0.0 && k.effective_radius > 0.0,
+                "column constants must be positive");
+        if (cells == 0) return PSGB_OK;
+        cudaStream_t st = as_stream(stream);
+        if (memory == PSGB_MEMORY_DEVICE) {
+            psgb::launch_column_radiation(cells, layers, k, temperature_K, humidity, cloud_water, surface_temperature_K,
+                                          surface_pressure_Pa, emissivity, absorbed, fraction, reflectance, scalars, st);
+            PSGB_CUDA(cudaGetLastError());
+            return PSGB_OK;
+        }
+        const std::size_t lc = std::size_t(layers) * cells;
+        psgb::DeviceStore tmp;
+        double* d_t = tmp.alloc<double>(lc);
+        double* d_q = tmp.alloc<double>(lc);
+        double* d_l = tmp.alloc<double>(lc);
+        double* d_ts = tmp.alloc<double>(cells);
+        double* d_ps = tmp.alloc<double>(cells);
+        double* d_e = tmp.alloc<double>(lc);
+        double* d_a = tmp.alloc<double>(lc);
+        double* d_f = tmp.alloc<double>(lc);
+        double* d_r = tmp.alloc<double>(lc);
+        double* d_s = tmp.alloc<double>(std::size_t(5) * cells);
+        copy_in(d_t, temperature_K, lc * 8, memory, st);
+        copy_in(d_q, humidity, lc * 8, memory, st);
+        copy_in(d_l, cloud_water, lc * 8, memory, st);
+        copy_in(d_ts, surface_temperature_K, cells * 8, memory, st);
+        copy_in(d_ps, surface_pressure_Pa, cells * 8, memory, st);
+        psgb::launch_column_radiation(cells, layers, k, d_t, d_q, d_l, d_ts, d_ps, d_e, d_a, d_f, d_r, d_s, st);
+        PSGB_CUDA(cudaGetLastError());
+        copy_out(emissivity, d_e, lc * 8, memory, st);
+        copy_out(absorbed, d_a, lc * 8, memory, st);
+        copy_out(fraction, d_f, lc * 8, memory, st);
+        copy_out(reflectance, d_r, lc * 8, memory, st);
+        copy_out(scalars, d_s, std::size_t(5) * cells * 8, memory, st);
+        PSGB_CUDA(cudaStreamSynchronize(st));
+        return PSGB_OK;
+    });
+}
+
+int psgb_substep_mean_insolation(const psgb_planet* h, int64_t substep, float* out) {
+    return guarded([&] {
+        require(h != nullptr && out != nullptr, "null argument");
+        psgb::substep_mean_insolation(h->planet->mesh, substep, out);
+        return PSGB_OK;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,370 @@
+// Aggregation-multigrid kernels for sm_103a (GB300).
+//
+// Replaces the CPU V-cycle of the reference (sim/planet/surface/heat_transport.cpp:
+// coarsen_values :157-171, factor_dense/solve_dense :202-243, gauss_seidel :258-286,
+// v_cycle :288-326). The hierarchy's structure is the reference's; the smoother is
+// damped Jacobi (both sweeps of a level read only the previous iterate, so every row
+// is independent), the coarsest level is solved with an explicit dense inverse.
+//
+// All kernels are HBM/L2 streaming kernels over ELL slot-major rows: one thread per
+// row, 256-row tiles, neighbour gathers served mostly from L2 thanks to the
+// reference's space-filling cell order. No tensor cores (sparse stencils).
+#include "common.cuh"
+#include "kernels.hpp"
+
+#include <stdexcept>
+
+namespace psgb {
+namespace {
+
+__device__ __forceinline__ bool gate_open(const InstanceScalars* sc, int inst, int gate) {
+    if (gate == kGateAlways) return true;
+    const InstanceScalars& s = sc[inst];
+    if (gate == kGateOuter) return s.outer_status == kRunning;
+    if (s.status != kRunning) return false;
+    if (gate == kGateSecondHalf && s.half_done) return false;
+    return true;
+}
+
+// Returns the row this thread owns, or -1 (padding row, gated tile, non-sweep tile).
+template <typename T>
+__device__ __forceinline__ int owned_row(const LevelView<T>& lv, const InstanceScalars* sc, int gate,
+                                         bool need_sweep) {
+    const int tile = blockIdx.x;
+    if (threadIdx.x >= lv.tile_rows[tile]) return -1;
+    if (need_sweep && !lv.tile_sweep[tile]) return -1;
+    if (!gate_open(sc, lv.tile_inst[tile], gate)) return -1;
+    return tile * kTile + threadIdx.x;
+}
+
+// ---- assembly -------------------------------------------------------------
+
+__global__ void k_assemble_transport(LevelView<double> lv, const double* __restrict__ w,
+                                     const double* __restrict__ wsum, const double* __restrict__ area,
+                                     const double* __restrict__ slope,
+                                     const double* __restrict__ conductance,
+                                     const double* __restrict__ edge_conductance,
+                                     double* __restrict__ vd) {
+    const int tile = blockIdx.x;
+    const int row = tile * kTile + threadIdx.x;
+    const std::uint32_t P = lv.rows, W = lv.width;
+    if (threadIdx.x >= lv.tile_rows[tile]) {
+        // padding rows: identity, no couplings
+        for (std::uint32_t j = 0; j < W; ++j) vd[j * P + row] = 0.0;
+        vd[W * P + row] = 1.0;
+        return;
+    }
+    const double K = conductance[lv.tile_inst[tile]];
+    const double s = slope[row];
+    const bool free_row = s > 0.0;
+    double diag;
+    if (edge_conductance == nullptr) {
+        diag = free_row ? dadd(__ddiv_rn(area[row], s), dmul(K, wsum[row])) : 1.0;
+    } else {
+        double sum = 0.0;
+        for (std::uint32_t j = 0; j < 6; ++j) sum = dadd(sum, dmul(edge_conductance[j * P + row], w[j * P + row]));
+        diag = free_row ? dadd(__ddiv_rn(area[row], s), sum) : 1.0;
+    }
+    vd[W * P + row] = diag;
+    for (std::uint32_t j = 0; j < W; ++j) {
+        double v = 0.0;
+        if (j < 6) {
+            const int nb = lv.col[j * P + row];
+            const double g = edge_conductance == nullptr ? K : edge_conductance[j * P + row];
+            const double wj = w[j * P + row];
+            if (free_row && nb != row && slope[nb] > 0.0) v = dmul(-g, wj);
+        }
+        vd[j * P + row] = v;
+    }
+}
+
+__global__ void k_set_matrix_csr(std::uint32_t n, std::uint32_t P, std::uint32_t W,
+                                 const std::uint32_t* __restrict__ off_begin,
+                                 const double* __restrict__ diag, const double* __restrict__ off,
+                                 double* __restrict__ vd) {
+    const std::uint32_t row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= P) return;
+    if (row >= n) {
+        for (std::uint32_t j = 0; j < W; ++j) vd[j * P + row] = 0.0;
+        vd[W * P + row] = 1.0;
+        return;
+    }
+    const std::uint32_t b = off_begin[row], e = off_begin[row + 1];
+    for (std::uint32_t j = 0; j < W; ++j) vd[j * P + row] = (b + j < e) ? off[b + j] : 0.0;
+    vd[W * P + row] = diag[row];
+}
+
+// Galerkin values: each coarse entry sums its fine sources in the reference's
+// order (rows ascending, then the row's entries), from 0.0 - bit-identical to
+// coarsen_values.
+__global__ void k_galerkin(std::uint32_t lists, const std::uint32_t* __restrict__ offset,
+                           const std::uint32_t* __restrict__ source, const double* __restrict__ fine,
+                           double* __restrict__ coarse) {
+    const std::uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= lists) return;
+    double sum = 0.0;
+    for (std::uint32_t k = offset[id]; k < offset[id + 1]; ++k) sum = dadd(sum, fine[source[k]]);
+    coarse[id] = sum;
+}
+
+__global__ void k_finalize_level(std::uint32_t P, std::uint32_t W, double* __restrict__ vd64,
+                                 float* __restrict__ vd32, double* __restrict__ inv64,
+                                 float* __restrict__ inv32) {
+    const std::uint32_t row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= P) return;
+    double d = vd64[W * P + row];
+    if (d == 0.0) {   // absent rows of a shorter planet: keep them an identity
+        d = 1.0;
+        vd64[W * P + row] = 1.0;
+    }
+    for (std::uint32_t j = 0; j < W; ++j) vd32[j * P + row] = static_cast<float>(vd64[j * P + row]);
+    vd32[W * P + row] = static_cast<float>(d);
+    const double inv = 1.0 / d;
+    inv64[row] = inv;
+    inv32[row] = static_cast<float>(inv);
+}
+
+// Dense inverse of every planet's coarsest level (symmetric positive definite):
+// assemble from the ELL values, then in-place Gauss-Jordan without pivoting. One CTA
+// per planet; the matrix lives in global memory (<= 400 x 400 doubles).
+__global__ void __launch_bounds__(1024) k_dense_invert(DenseView dense, int level, LevelView<double> lv,
+                                                       double* __restrict__ work,
+                                                       double* __restrict__ inv64,
+                                                       float* __restrict__ inv32) {
+    const int inst = blockIdx.x;
+    if (dense.level[inst] != level) return;
+    const int n = static_cast<int>(dense.size[inst]);
+    const std::int64_t base = dense.row_base[inst];
+    double* a = work + dense.offset[inst];
+    const std::uint32_t P = lv.rows, W = lv.width;
+    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) a[idx] = 0.0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const std::int64_t row = base + i;
+        a[i * n + i] = lv.vd[W * P + row];
+        for (std::uint32_t j = 0; j < W; ++j) {
+            const std::int64_t c = lv.col[j * P + row];
+            if (c == row) continue;
+            a[i * n + (c - base)] += lv.vd[j * P + row];
+        }
+    }
+    __syncthreads();
+    __shared__ double f[400];
+    __shared__ double pivot_inv;
+    for (int k = 0; k < n; ++k) {
+        if (threadIdx.x == 0) pivot_inv = 1.0 / a[k * n + k];
+        __syncthreads();
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+            a[k * n + j] = (j == k ? 1.0 : a[k * n + j]) * pivot_inv;
+        }
+        for (int i = threadIdx.x; i < n; i += blockDim.x) f[i] = a[i * n + k];
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+            const int i = idx / n, j = idx - i * n;
+            if (i == k) continue;
+            const double aij = (j == k) ? 0.0 : a[idx];
+            a[idx] = aij - f[i] * a[k * n + j];
+        }
+        __syncthreads();
+    }
+    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+        inv64[dense.offset[inst] + idx] = a[idx];
+        inv32[dense.offset[inst] + idx] = static_cast<float>(a[idx]);
+    }
+}
+
+// ---- V-cycle pieces ----------------------------------------------------------
+
+template <typename T>
+__global__ void k_smooth_zero(LevelView<T> lv, const T* __restrict__ b, T* __restrict__ x, T omega,
+                              const InstanceScalars* sc, int gate) {
+    const int row = owned_row(lv, sc, gate, true);
+    if (row < 0) return;
+    x[row] = omega * lv.inv[row] * b[row];
+}
+
+template <typename T, int W>
+__global__ void k_smooth(LevelView<T> lv, const T* __restrict__ b, const T* __restrict__ x,
+                         T* __restrict__ y, T omega, const InstanceScalars* sc, int gate) {
+    const int row = owned_row(lv, sc, gate, true);
+    if (row < 0) return;
+    const std::uint32_t P = lv.rows;
+    T s = b[row];
+#pragma unroll
+    for (int j = 0; j < W; ++j) s -= lv.vd[j * P + row] * x[lv.col[j * P + row]];
+    const T xo = x[row];
+    y[row] = xo + omega * (lv.inv[row] * s - xo);
+}
+
+template <typename T, int W>
+__global__ void k_residual(LevelView<T> lv, const T* __restrict__ b, const T* __restrict__ x,
+                           T* __restrict__ r, const InstanceScalars* sc, int gate) {
+    const int row = owned_row(lv, sc, gate, true);
+    if (row < 0) return;
+    const std::uint32_t P = lv.rows;
+    T s = b[row] - lv.vd[W * P + row] * x[row];
+#pragma unroll
+    for (int j = 0; j < W; ++j) s -= lv.vd[j * P + row] * x[lv.col[j * P + row]];
+    r[row] = s;
+}
+
+template <typename T, int W>
+__global__ void k_spmv(LevelView<T> lv, const T* __restrict__ x, T* __restrict__ y) {
+    const int tile = blockIdx.x;
+    if (threadIdx.x >= lv.tile_rows[tile]) return;
+    const int row = tile * kTile + threadIdx.x;
+    const std::uint32_t P = lv.rows;
+    T s = lv.vd[W * P + row] * x[row];
+#pragma unroll
+    for (int j = 0; j < W; ++j) s += lv.vd[j * P + row] * x[lv.col[j * P + row]];
+    y[row] = s;
+}
+
+// Coarse right-hand side: each coarse row sums its members' residuals in
+// ascending fine-row order (the reference's order, heat_transport.cpp:316-319).
+template <typename T>
+__global__ void k_restrict(LevelView<T> coarse, const std::uint32_t* __restrict__ moff,
+                           const std::uint32_t* __restrict__ member, const T* __restrict__ r,
+                           T* __restrict__ bc, const InstanceScalars* sc, int gate) {
+    const int tile = blockIdx.x;
+    if (threadIdx.x >= coarse.tile_rows[tile]) return;
+    if (!gate_open(sc, coarse.tile_inst[tile], gate)) return;
+    const int row = tile * kTile + threadIdx.x;
+    T s = T(0);
+    for (std::uint32_t k = moff[row]; k < moff[row + 1]; ++k) s += r[member[k]];
+    bc[row] = s;
+}
+
+template <typename T>
+__global__ void k_prolong(LevelView<T> lv, const std::int32_t* __restrict__ agg, const T* __restrict__ xc,
+                          T* __restrict__ x, const InstanceScalars* sc, int gate) {
+    const int row = owned_row(lv, sc, gate, true);
+    if (row < 0) return;
+    x[row] += xc[agg[row]];
+}
+
+// Coarsest level: x = A^-1 b, one warp per row, lanes over columns.
+template <typename T>
+__global__ void k_dense_solve(DenseView dense, int level, const T* __restrict__ inv,
+                              const T* __restrict__ b, T* __restrict__ x, const InstanceScalars* sc,
+                              int gate) {
+    const int inst = blockIdx.y;
+    if (dense.level[inst] != level) return;
+    if (!gate_open(sc, inst, gate)) return;
+    const int n = static_cast<int>(dense.size[inst]);
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= n) return;
+    const std::int64_t base = dense.row_base[inst];
+    const T* a = inv + dense.offset[inst] + static_cast<std::int64_t>(warp) * n;
+    T s = T(0);
+    for (int j = lane; j < n; j += 32) s += a[j] * b[base + j];
+    s = warp_sum(s);
+    if (lane == 0) x[base + warp] = s;
+}
+
+inline dim3 tiles_grid(std::uint32_t tiles) { return dim3(tiles); }
+
+}  // namespace
+
+// ---- launchers -----------------------------------------------------------------
+
+void launch_assemble_transport(const LevelView<double>& fine, const double* w, const double* wsum,
+                               const double* area, const double* slope, const double* conductance,
+                               const double* edge_conductance, double* vd, cudaStream_t stream) {
+    k_assemble_transport<<<fine.tiles, kTile, 0, stream>>>(fine, w, wsum, area, slope, conductance,
+                                                          edge_conductance, vd);
+}
+
+void launch_set_matrix_csr(std::uint32_t n, std::uint32_t rows, std::uint32_t width,
+                           const std::uint32_t* csr_offset, const double* diag, const double* off,
+                           double* vd, cudaStream_t stream) {
+    k_set_matrix_csr<<<(rows + 255) / 256, 256, 0, stream>>>(n, rows, width, csr_offset, diag, off, vd);
+}
+
+void launch_galerkin(std::uint32_t lists, const std::uint32_t* offset, const std::uint32_t* source,
+                     const double* fine_vd, double* coarse_vd, cudaStream_t stream) {
+    k_galerkin<<<(lists + 255) / 256, 256, 0, stream>>>(lists, offset, source, fine_vd, coarse_vd);
+}
+
+void launch_finalize_level(std::uint32_t rows, std::uint32_t width, double* vd64, float* vd32,
+                           double* inv64, float* inv32, cudaStream_t stream) {
+    k_finalize_level<<<(rows + 255) / 256, 256, 0, stream>>>(rows, width, vd64, vd32, inv64, inv32);
+}
+
+void launch_dense_invert(const DenseView& dense, int level, const LevelView<double>& lv,
+                         double* work, double* inv64, float* inv32, cudaStream_t stream) {
+    k_dense_invert<<<dense.instances, 1024, 0, stream>>>(dense, level, lv, work, inv64, inv32);
+}
+
+#define PSGB_WIDTH_DISPATCH(width, KERNEL, ...)                                 \
+    switch (width) {                                                            \
+        case 6: KERNEL<T, 6><<<lv.tiles, kTile, 0, stream>>>(__VA_ARGS__); break; \
+        case 8: KERNEL<T, 8><<<lv.tiles, kTile, 0, stream>>>(__VA_ARGS__); break; \
+        case 12: KERNEL<T, 12><<<lv.tiles, kTile, 0, stream>>>(__VA_ARGS__); break; \
+        case 16: KERNEL<T, 16><<<lv.tiles, kTile, 0, stream>>>(__VA_ARGS__); break; \
+        default: throw std::logic_error("unsupported ELL width");               \
+    }
+
+template <typename T>
+void launch_smooth_zero(const LevelView<T>& lv, const T* b, T* x, T omega, const InstanceScalars* sc,
+                        int gate, cudaStream_t stream) {
+    k_smooth_zero<T><<<lv.tiles, kTile, 0, stream>>>(lv, b, x, omega, sc, gate);
+}
+
+template <typename T>
+void launch_smooth(const LevelView<T>& lv, const T* b, const T* x, T* y, T omega,
+                   const InstanceScalars* sc, int gate, cudaStream_t stream) {
+    PSGB_WIDTH_DISPATCH(lv.width, k_smooth, lv, b, x, y, omega, sc, gate);
+}
+
+template <typename T>
+void launch_residual(const LevelView<T>& lv, const T* b, const T* x, T* r, const InstanceScalars* sc,
+                     int gate, cudaStream_t stream) {
+    PSGB_WIDTH_DISPATCH(lv.width, k_residual, lv, b, x, r, sc, gate);
+}
+
+template <typename T>
+void launch_spmv(const LevelView<T>& lv, const T* x, T* y, cudaStream_t stream) {
+    PSGB_WIDTH_DISPATCH(lv.width, k_spmv, lv, x, y);
+}
+
+template <typename T>
+void launch_restrict(const LevelView<T>& coarse, const std::uint32_t* member_offset,
+                     const std::uint32_t* member, const T* r, T* bc, const InstanceScalars* sc,
+                     int gate, cudaStream_t stream) {
+    k_restrict<T><<<coarse.tiles, kTile, 0, stream>>>(coarse, member_offset, member, r, bc, sc, gate);
+}
+
+template <typename T>
+void launch_prolong(const LevelView<T>& fine, const std::int32_t* agg, const T* xc, T* x,
+                    const InstanceScalars* sc, int gate, cudaStream_t stream) {
+    k_prolong<T><<<fine.tiles, kTile, 0, stream>>>(fine, agg, xc, x, sc, gate);
+}
+
+template <typename T>
+void launch_dense_solve(const DenseView& dense, int level, std::uint32_t max_rows, const T* inv,
+                        const T* b, T* x, const InstanceScalars* sc, int gate, cudaStream_t stream) {
+    const dim3 grid((max_rows * 32 + 255) / 256, dense.instances);
+    k_dense_solve<T><<<grid, 256, 0, stream>>>(dense, level, inv, b, x, sc, gate);
+}
+
+#define PSGB_INSTANTIATE(T)                                                                           \
+    template void launch_smooth_zero<T>(const LevelView<T>&, const T*, T*, T, const InstanceScalars*, \
+                                        int, cudaStream_t);                                           \
+    template void launch_smooth<T>(const LevelView<T>&, const T*, const T*, T*, T,                     \
+                                   const InstanceScalars*, int, cudaStream_t);                        \
+    template void launch_residual<T>(const LevelView<T>&, const T*, const T*, T*,                      \
+                                     const InstanceScalars*, int, cudaStream_t);                      \
+    template void launch_spmv<T>(const LevelView<T>&, const T*, T*, cudaStream_t);                     \
+    template void launch_restrict<T>(const LevelView<T>&, const std::uint32_t*, const std::uint32_t*,  \
+                                     const T*, T*, const InstanceScalars*, int, cudaStream_t);        \
+    template void launch_prolong<T>(const LevelView<T>&, const std::int32_t*, const T*, T*,            \
+                                    const InstanceScalars*, int, cudaStream_t);                       \
+    template void launch_dense_solve<T>(const DenseView&, int, std::uint32_t, const T*, const T*, T*,  \
+                                        const InstanceScalars*, int, cudaStream_t);
+
+PSGB_INSTANTIATE(float)
+PSGB_INSTANTIATE(double)
+
+}  // namespace psgb

@@ -1,0 +1,197 @@
+// Internal (non-ABI) structures of the GB300 heat-transport library.
+//
+// Planet  : one mesh (level, radius) with its transport graph and multigrid
+//           hierarchy structure, the operator geometry resident in HBM.
+// Batch   : any number of planets concatenated level by level, each planet's rows
+//           padded to whole 256-row tiles, with the Krylov/V-cycle workspace. A
+//           one-planet batch is the plain drop-in solve; a many-planet batch is
+//           the concatenated block layout solved by one stream of launches.
+#pragma once
+
+#include "host/hierarchy.hpp"
+#include "host/mesh.hpp"
+#include "kernels.hpp"
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace psgb {
+
+constexpr std::uint32_t kTileRows = 256;
+
+struct CudaError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+#define PSGB_CUDA(call)                                                                    \
+    do {                                                                                   \
+        cudaError_t psgb_err_ = (call);                                                    \
+        if (psgb_err_ != cudaSuccess) {                                                    \
+            throw ::psgb::CudaError(std::string(#call) + ": " + cudaGetErrorString(psgb_err_)); \
+        }                                                                                  \
+    } while (0)
+
+// Device allocations owned by one object; counts bytes for the HBM budget.
+class DeviceStore {
+  public:
+    DeviceStore() = default;
+    DeviceStore(const DeviceStore&) = delete;
+    DeviceStore& operator=(const DeviceStore&) = delete;
+    ~DeviceStore() { release(); }
+    template <typename T>
+    T* alloc(std::size_t count) {
+        if (count == 0) count = 1;
+        void* p = nullptr;
+        const std::size_t bytes = (count * sizeof(T) + 255) / 256 * 256;
+        PSGB_CUDA(cudaMalloc(&p, bytes));
+        ptrs_.push_back(p);
+        bytes_ += bytes;
+        return static_cast<T*>(p);
+    }
+    template <typename T>
+    T* upload(const std::vector<T>& host) {
+        T* d = alloc<T>(host.size());
+        if (!host.empty()) PSGB_CUDA(cudaMemcpy(d, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice));
+        return d;
+    }
+    void release() {
+        for (void* p : ptrs_) cudaFree(p);
+        ptrs_.clear();
+        bytes_ = 0;
+    }
+    std::size_t bytes() const { return bytes_; }
+
+  private:
+    std::vector<void*> ptrs_;
+    std::size_t bytes_ = 0;
+};
+
+// Fine-level operator geometry, ELL slot-major over P = pad_rows(N) rows.
+struct DevMesh {
+    std::uint32_t n = 0, p = 0, edges = 0;
+    std::int32_t* nbr = nullptr;       // [6][P]; padding slot -> own row
+    std::int32_t* edge = nullptr;      // [6][P]; padding slot -> 0 (masked)
+    std::uint8_t* first = nullptr;     // [P] bit j: this cell is edge slot j's first cell
+    std::uint8_t* degree = nullptr;    // [P]
+    double* w = nullptr;               // [6][P] l/d; 0 in padding slots
+    double* dist = nullptr;            // [6][P] centroid distance; 1 in padding slots
+    float* ne = nullptr;               // [6][P] FP32 outward normal (east)
+    float* nn = nullptr;               // [6][P] FP32 outward normal (north)
+    double* area = nullptr;            // [P]; 1 in padding rows
+    double* gm = nullptr;              // [4][P] m_ee, m_en, m_nn, det of the LSQ gradient
+    double* edge_length = nullptr;     // [E]
+};
+
+struct Planet {
+    HostMesh mesh;
+    TransportGraph graph;
+    HostHierarchy hierarchy;
+    DevMesh dev;
+    DeviceStore store;
+    bool uploaded = false;
+    std::unique_ptr<struct Batch> solo;   // the one-planet batch (drop-in calls)
+};
+
+// One level of the concatenated hierarchy.
+struct BatchLevel {
+    std::uint32_t rows = 0;            // padded total P
+    std::uint32_t tiles = 0;
+    std::uint32_t width = 0;           // device ELL width (6, 8, 12, 16)
+    std::int32_t* col = nullptr;       // [width][P]
+    double* vd64 = nullptr;            // [width][P] off-diagonals, then [P] diagonal
+    double* inv64 = nullptr;           // [P] 1 / diagonal
+    float* vd32 = nullptr;
+    float* inv32 = nullptr;
+    std::int32_t* tile_inst = nullptr;    // [tiles]
+    std::int32_t* tile_rows = nullptr;    // [tiles] valid rows (0..256)
+    std::uint8_t* tile_sweep = nullptr;   // [tiles] 1: the planet smooths on this level
+    // transition to the next level (absent on the deepest level)
+    std::int32_t* agg = nullptr;              // [P] global row on the next level
+    std::uint32_t* member_offset = nullptr;   // next level: [P_next + 1]
+    std::uint32_t* member = nullptr;
+    std::uint32_t* gal_offset = nullptr;      // next level: [(width_next + 1) * P_next + 1]
+    std::uint32_t* gal_source = nullptr;
+    std::uint32_t gal_lists = 0;
+    // vectors (x: iterate, y: Jacobi ping-pong, b: right-hand side, r: residual)
+    double* x64 = nullptr; double* y64 = nullptr; double* b64 = nullptr; double* r64 = nullptr;
+    float* x32 = nullptr; float* y32 = nullptr; float* b32 = nullptr; float* r32 = nullptr;
+    std::vector<std::int64_t> base;    // [instances] row base, -1 if the planet has no such level
+    std::vector<std::uint32_t> count;  // [instances] rows
+};
+
+struct DenseCoarse {
+    std::vector<std::int32_t> level;   // coarsest level per planet
+    std::vector<std::uint64_t> offset; // inverse offset per planet
+    std::vector<std::uint32_t> size;
+    std::vector<std::int64_t> row_base;
+    std::uint32_t max_rows = 0;
+    double* inv64 = nullptr;           // concatenated row-major inverses
+    float* inv32 = nullptr;
+    double* work = nullptr;
+    std::int32_t* d_level = nullptr;
+    std::uint64_t* d_offset = nullptr;
+    std::uint32_t* d_size = nullptr;
+    std::int64_t* d_row_base = nullptr;
+};
+
+struct SmootherConfig {
+    int pre = 2, post = 2;             // damped Jacobi sweeps per level
+    double omega = 0.8;                // damping factor
+};
+
+struct Batch {
+    std::vector<Planet*> planets;
+    std::uint32_t instances = 0;
+    std::vector<BatchLevel> levels;
+    DenseCoarse dense;
+    DeviceStore store;
+    SmootherConfig smoother;
+    std::vector<std::int64_t> fine_base;      // fine-level row base per planet
+    // fine-level graph data for assembly and the transport operator
+    double* area = nullptr;            // [P0]; 1 in padding rows
+    double* w = nullptr;               // [6][P0] graph weight l/d (0 in padding slots)
+    double* wsum = nullptr;            // [P0] the graph's weight_sum
+    double* conductance = nullptr;     // [instances] scratch for assembly
+    // Krylov vectors on the fine level
+    static constexpr int kVectors = 10;
+    double* k64[kVectors] = {};
+    float* k32[kVectors] = {};
+    // FP64 refinement
+    double* xr = nullptr;              // solution
+    double* rr = nullptr;              // residual
+    double* bb = nullptr;              // right-hand side
+    double* tmp = nullptr;             // [P0] general scratch
+    double* tmp2 = nullptr;            // [P0] general scratch
+    // reductions
+    double* partial = nullptr;         // [tiles0][8]
+    unsigned* ticket = nullptr;        // [instances]
+    std::uint32_t* tile_begin = nullptr;  // [instances + 1] fine-level tile ranges
+    InstanceScalars* scalars = nullptr;   // [instances]
+    std::vector<InstanceScalars> host_scalars;
+    InstanceScalars* pinned_scalars = nullptr;   // pinned host mirror
+    bool matrix_ready = false;
+    // transport-step buffers (fine layout)
+    double* slope_of = nullptr;        // [instances] dt / C
+    double* t0 = nullptr;              // [P0]
+    double* src = nullptr;             // [P0]
+    double* hout = nullptr;            // [P0]
+    double* tnew = nullptr;            // [P0]
+    double* sums = nullptr;            // [instances][8]
+    double* edge_g = nullptr;          // [6][P0] per-entry conductance (lazily)
+    const double* step_edge_conductance = nullptr;   // edge_g when the matrix uses it
+    double* csr_values = nullptr;      // one-planet batches: set_matrix staging
+    std::uint32_t* csr_offset = nullptr;   // one-planet batches: the graph's CSR offsets
+    // the parameters the current matrix was assembled with
+    std::vector<double> assembled_key;
+    std::uint64_t assembled_bytes_hint = 0;
+    ~Batch() {
+        if (pinned_scalars != nullptr) cudaFreeHost(pinned_scalars);
+    }
+};
+
+}  // namespace psgb

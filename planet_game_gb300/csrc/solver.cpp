@@ -1,0 +1,538 @@
+// Host driver: planet upload, batch layout, V-cycle and Krylov orchestration.
+//
+// A batch concatenates planets level by level. Planet i's rows on level l occupy
+// [base_l[i], base_l[i] + n_il), padded to whole 256-row tiles, so that every tile
+// belongs to one planet: per-planet dot products, convergence and gating are then
+// decided per tile. A one-planet batch is the drop-in solve of the reference's
+// solve_newton_system/GraphMultigrid (sim/planet/surface/heat_transport.cpp:337-429,
+// 545-577); a many-planet batch solves uneven planets with the same launches.
+#include "solver.hpp"
+
+#include "kernels.hpp"
+#include "krylov.hpp"
+
+#include <algorithm>
+#include <cstring>
+#include <stdexcept>
+
+namespace psgb {
+
+namespace {
+
+template <typename T>
+void upload_to(T* dst, const std::vector<T>& host) {
+    if (!host.empty()) PSGB_CUDA(cudaMemcpy(dst, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice));
+}
+
+}  // namespace
+
+std::unique_ptr<Planet> make_planet(std::uint32_t level, double radius_m) {
+    auto planet = std::make_unique<Planet>();
+    planet->mesh = build_icosphere(level, radius_m);
+    planet->graph = transport_graph(planet->mesh);
+    planet->hierarchy = build_hierarchy(planet->graph);
+    for (const auto& lv : planet->hierarchy.levels) {
+        if (lv.width > 16) throw std::logic_error("hierarchy level wider than 16");
+    }
+    if (planet->hierarchy.levels.back().size > coarsest_rows) {
+        throw std::logic_error("coarsest multigrid level exceeds 400 rows");
+    }
+    return planet;
+}
+
+void upload_planet(Planet& planet_ref) {
+    if (planet_ref.uploaded) return;
+    Planet* planet = &planet_ref;
+    // Operator geometry (finite_volume.cpp:34-111), ELL slot-major over P rows.
+    const HostMesh& m = planet->mesh;
+    DevMesh& d = planet->dev;
+    d.n = static_cast<std::uint32_t>(m.cells);
+    d.p = pad_rows(d.n);
+    d.edges = static_cast<std::uint32_t>(m.edges);
+    const std::size_t P = d.p;
+    std::vector<std::int32_t> nbr(6 * P), edge(6 * P, 0);
+    std::vector<std::uint8_t> first(P, 0), degree(P, 0);
+    std::vector<double> w(6 * P, 0.0), dist(6 * P, 1.0), area(P, 1.0), gm(4 * P, 0.0);
+    std::vector<float> ne(6 * P, 0.0F), nn(6 * P, 0.0F);
+    for (std::size_t r = 0; r < P; ++r)
+        for (int j = 0; j < 6; ++j) nbr[j * P + r] = static_cast<std::int32_t>(r);
+    for (std::size_t c = 0; c < m.cells; ++c) {
+        const std::uint32_t base = m.edge_offset[c];
+        degree[c] = m.edge_count[c];
+        area[c] = m.area_m2[c];
+        double mee = 0.0, men = 0.0, mnn = 0.0;
+        for (std::uint32_t k = 0; k < m.edge_count[c]; ++k) {
+            const std::uint32_t e = m.nb_edge[base + k];
+            nbr[k * P + c] = static_cast<std::int32_t>(m.nb_cell[base + k]);
+            edge[k * P + c] = static_cast<std::int32_t>(e);
+            if (m.edge_first[e] == c) first[c] |= static_cast<std::uint8_t>(1u << k);
+            w[k * P + c] = planet->graph.weight[base + k];
+            dist[k * P + c] = m.edge_distance_m[e];
+            ne[k * P + c] = m.normal_east[base + k];
+            nn[k * P + c] = m.normal_north[base + k];
+            const double a = static_cast<double>(m.normal_east[base + k]);
+            const double b = static_cast<double>(m.normal_north[base + k]);
+            mee += a * a;
+            men += a * b;
+            mnn += b * b;
+        }
+        gm[0 * P + c] = mee;
+        gm[1 * P + c] = men;
+        gm[2 * P + c] = mnn;
+        gm[3 * P + c] = mee * mnn - men * men;
+    }
+    d.nbr = planet->store.upload(nbr);
+    d.edge = planet->store.upload(edge);
+    d.first = planet->store.upload(first);
+    d.degree = planet->store.upload(degree);
+    d.w = planet->store.upload(w);
+    d.dist = planet->store.upload(dist);
+    d.ne = planet->store.upload(ne);
+    d.nn = planet->store.upload(nn);
+    d.area = planet->store.upload(area);
+    d.gm = planet->store.upload(gm);
+    d.edge_length = planet->store.upload(m.edge_length_m);
+    planet->uploaded = true;
+}
+
+std::unique_ptr<Batch> make_batch(const std::vector<Planet*>& planets) {
+    if (planets.empty()) throw std::invalid_argument("a batch needs at least one planet");
+    for (Planet* p : planets) upload_planet(*p);
+    auto bp = std::make_unique<Batch>();
+    Batch& b = *bp;
+    b.planets = planets;
+    b.instances = static_cast<std::uint32_t>(planets.size());
+    const std::uint32_t I = b.instances;
+    std::size_t depth = 0;
+    for (auto* p : planets) depth = std::max(depth, p->hierarchy.levels.size());
+    b.levels.resize(depth);
+
+    // Row bases, tiles and widths per level.
+    for (std::size_t l = 0; l < depth; ++l) {
+        BatchLevel& L = b.levels[l];
+        L.base.assign(I, -1);
+        L.count.assign(I, 0);
+        std::uint32_t rows = 0, width = 0;
+        for (std::uint32_t i = 0; i < I; ++i) {
+            const auto& H = planets[i]->hierarchy.levels;
+            if (l >= H.size()) continue;
+            L.base[i] = rows;
+            L.count[i] = H[l].size;
+            rows += pad_rows(H[l].size);
+            width = std::max(width, H[l].width);
+        }
+        L.rows = rows;
+        L.tiles = rows / kTileRows;
+        L.width = device_width(std::max<std::uint32_t>(width, 1));
+        if (l == 0) L.width = 6;
+    }
+    b.fine_base = b.levels[0].base;
+
+    // Tile metadata and ELL columns.
+    for (std::size_t l = 0; l < depth; ++l) {
+        BatchLevel& L = b.levels[l];
+        const std::size_t P = L.rows, W = L.width;
+        std::vector<std::int32_t> tile_inst(L.tiles), tile_rows(L.tiles);
+        std::vector<std::uint8_t> tile_sweep(L.tiles);
+        std::vector<std::int32_t> col(W * P);
+        for (std::size_t r = 0; r < P; ++r)
+            for (std::size_t j = 0; j < W; ++j) col[j * P + r] = static_cast<std::int32_t>(r);
+        for (std::uint32_t i = 0; i < I; ++i) {
+            if (L.base[i] < 0) continue;
+            const auto& H = planets[i]->hierarchy.levels;
+            const HostLevel& hl = H[l];
+            const std::uint32_t t0 = static_cast<std::uint32_t>(L.base[i] / kTileRows);
+            const std::uint32_t nt = pad_rows(hl.size) / kTileRows;
+            for (std::uint32_t t = 0; t < nt; ++t) {
+                tile_inst[t0 + t] = static_cast<std::int32_t>(i);
+                tile_rows[t0 + t] = static_cast<std::int32_t>(std::min<std::uint32_t>(kTileRows, hl.size - t * kTileRows));
+                tile_sweep[t0 + t] = (l + 1 < H.size()) ? 1 : 0;
+            }
+            for (std::uint32_t r = 0; r < hl.size; ++r) {
+                for (std::uint32_t k = hl.offset[r]; k < hl.offset[r + 1]; ++k) {
+                    col[(k - hl.offset[r]) * P + L.base[i] + r] = static_cast<std::int32_t>(L.base[i] + hl.column[k]);
+                }
+            }
+        }
+        L.tile_inst = b.store.upload(tile_inst);
+        L.tile_rows = b.store.upload(tile_rows);
+        L.tile_sweep = b.store.upload(tile_sweep);
+        L.col = b.store.upload(col);
+        L.vd64 = b.store.alloc<double>((W + 1) * P);
+        L.vd32 = b.store.alloc<float>((W + 1) * P);
+        L.inv64 = b.store.alloc<double>(P);
+        L.inv32 = b.store.alloc<float>(P);
+        PSGB_CUDA(cudaMemset(L.vd64, 0, (W + 1) * P * sizeof(double)));
+        L.x64 = b.store.alloc<double>(P); L.y64 = b.store.alloc<double>(P);
+        L.b64 = b.store.alloc<double>(P); L.r64 = b.store.alloc<double>(P);
+        L.x32 = b.store.alloc<float>(P); L.y32 = b.store.alloc<float>(P);
+        L.b32 = b.store.alloc<float>(P); L.r32 = b.store.alloc<float>(P);
+        for (double* v : {L.x64, L.y64, L.b64, L.r64}) PSGB_CUDA(cudaMemset(v, 0, P * sizeof(double)));
+        for (float* v : {L.x32, L.y32, L.b32, L.r32}) PSGB_CUDA(cudaMemset(v, 0, P * sizeof(float)));
+    }
+
+    // Level transitions: aggregates, restriction members, Galerkin gather lists.
+    for (std::size_t l = 0; l + 1 < depth; ++l) {
+        BatchLevel& F = b.levels[l];
+        BatchLevel& C = b.levels[l + 1];
+        const std::size_t Pf = F.rows, Wf = F.width, Pc = C.rows, Wc = C.width;
+        std::vector<std::int32_t> agg(Pf, -1);
+        std::vector<std::vector<std::uint32_t>> members(Pc);
+        std::vector<std::vector<std::uint32_t>> lists((Wc + 1) * Pc);
+        for (std::uint32_t i = 0; i < I; ++i) {
+            if (C.base[i] < 0) continue;
+            const HostLevel& hf = planets[i]->hierarchy.levels[l];
+            const HostLevel& hc = planets[i]->hierarchy.levels[l + 1];
+            const std::int64_t bf = F.base[i], bc = C.base[i];
+            for (std::uint32_t r = 0; r < hf.size; ++r) {
+                const std::uint32_t a = hf.aggregate[r];
+                const std::size_t gr = bf + r, ga = bc + a;
+                agg[gr] = static_cast<std::int32_t>(ga);
+                members[ga].push_back(static_cast<std::uint32_t>(gr));
+                lists[Wc * Pc + ga].push_back(static_cast<std::uint32_t>(Wf * Pf + gr));
+                for (std::uint32_t k = hf.offset[r]; k < hf.offset[r + 1]; ++k) {
+                    const std::uint32_t src = static_cast<std::uint32_t>((k - hf.offset[r]) * Pf + gr);
+                    if (hf.target[k] < 0) {
+                        lists[Wc * Pc + ga].push_back(src);
+                    } else {
+                        const std::uint32_t j = static_cast<std::uint32_t>(hf.target[k]) - hc.offset[a];
+                        lists[j * Pc + ga].push_back(src);
+                    }
+                }
+            }
+        }
+        std::vector<std::uint32_t> moff(Pc + 1, 0), mem;
+        for (std::size_t a = 0; a < Pc; ++a) {
+            mem.insert(mem.end(), members[a].begin(), members[a].end());
+            moff[a + 1] = static_cast<std::uint32_t>(mem.size());
+        }
+        std::vector<std::uint32_t> goff(lists.size() + 1, 0), gsrc;
+        for (std::size_t id = 0; id < lists.size(); ++id) {
+            gsrc.insert(gsrc.end(), lists[id].begin(), lists[id].end());
+            goff[id + 1] = static_cast<std::uint32_t>(gsrc.size());
+        }
+        F.agg = b.store.upload(agg);
+        F.member_offset = b.store.upload(moff);
+        F.member = b.store.upload(mem);
+        F.gal_offset = b.store.upload(goff);
+        F.gal_source = b.store.upload(gsrc);
+        F.gal_lists = static_cast<std::uint32_t>(lists.size());
+    }
+
+    // Coarsest levels: dense inverses.
+    DenseCoarse& D = b.dense;
+    D.level.resize(I); D.offset.resize(I); D.size.resize(I); D.row_base.resize(I);
+    std::uint64_t total = 0;
+    for (std::uint32_t i = 0; i < I; ++i) {
+        const auto& H = planets[i]->hierarchy.levels;
+        const int c = static_cast<int>(H.size()) - 1;
+        D.level[i] = c;
+        D.size[i] = H[c].size;
+        D.offset[i] = total;
+        D.row_base[i] = b.levels[c].base[i];
+        D.max_rows = std::max(D.max_rows, H[c].size);
+        total += std::uint64_t(H[c].size) * H[c].size;
+    }
+    D.inv64 = b.store.alloc<double>(total);
+    D.inv32 = b.store.alloc<float>(total);
+    D.work = b.store.alloc<double>(total);
+    D.d_level = b.store.upload(D.level);
+    D.d_offset = b.store.upload(D.offset);
+    D.d_size = b.store.upload(D.size);
+    D.d_row_base = b.store.upload(D.row_base);
+
+    // Fine-level graph data and Krylov workspace.
+    const BatchLevel& F = b.levels[0];
+    const std::size_t P0 = F.rows;
+    std::vector<double> area(P0, 1.0), w(6 * P0, 0.0), wsum(P0, 0.0);
+    std::vector<std::uint32_t> tile_begin(I + 1, 0);
+    for (std::uint32_t i = 0; i < I; ++i) {
+        const TransportGraph& g = planets[i]->graph;
+        const std::int64_t base = F.base[i];
+        for (std::size_t c = 0; c < g.size(); ++c) {
+            area[base + c] = g.area_m2[c];
+            wsum[base + c] = g.weight_sum[c];
+            for (std::uint32_t k = g.offset[c]; k < g.offset[c + 1]; ++k) {
+                w[(k - g.offset[c]) * P0 + base + c] = g.weight[k];
+            }
+        }
+        tile_begin[i] = static_cast<std::uint32_t>(base / kTileRows);
+    }
+    tile_begin[I] = F.tiles;
+    b.area = b.store.upload(area);
+    b.w = b.store.upload(w);
+    b.wsum = b.store.upload(wsum);
+    b.conductance = b.store.alloc<double>(I);
+    for (int v = 0; v < Batch::kVectors; ++v) {
+        b.k64[v] = b.store.alloc<double>(P0);
+        b.k32[v] = b.store.alloc<float>(P0);
+        PSGB_CUDA(cudaMemset(b.k64[v], 0, P0 * sizeof(double)));
+        PSGB_CUDA(cudaMemset(b.k32[v], 0, P0 * sizeof(float)));
+    }
+    b.xr = b.store.alloc<double>(P0);
+    b.rr = b.store.alloc<double>(P0);
+    b.bb = b.store.alloc<double>(P0);
+    b.tmp = b.store.alloc<double>(P0);
+    b.tmp2 = b.store.alloc<double>(P0);
+    for (double* v : {b.xr, b.rr, b.bb, b.tmp, b.tmp2}) PSGB_CUDA(cudaMemset(v, 0, P0 * sizeof(double)));
+    b.partial = b.store.alloc<double>(std::size_t(F.tiles) * 8);
+    b.ticket = b.store.alloc<unsigned>(I);
+    PSGB_CUDA(cudaMemset(b.ticket, 0, I * sizeof(unsigned)));
+    b.tile_begin = b.store.upload(tile_begin);
+    b.scalars = b.store.alloc<InstanceScalars>(I);
+    PSGB_CUDA(cudaMemset(b.scalars, 0, I * sizeof(InstanceScalars)));
+    b.host_scalars.assign(I, InstanceScalars{});
+    PSGB_CUDA(cudaMallocHost(&b.pinned_scalars, I * sizeof(InstanceScalars)));
+    b.slope_of = b.store.alloc<double>(I);
+    b.t0 = b.store.alloc<double>(P0);
+    b.src = b.store.alloc<double>(P0);
+    b.hout = b.store.alloc<double>(P0);
+    b.tnew = b.store.alloc<double>(P0);
+    for (double* v : {b.t0, b.src, b.hout, b.tnew}) PSGB_CUDA(cudaMemset(v, 0, P0 * sizeof(double)));
+    b.sums = b.store.alloc<double>(std::size_t(I) * 8);
+    if (I == 1) b.csr_offset = b.store.upload(planets[0]->graph.offset);
+    return bp;
+}
+
+template <typename T>
+static LevelView<T> make_view(const BatchLevel& L, const T* vd, const T* inv) {
+    return LevelView<T>{L.rows, L.width, L.tiles, L.col, vd, inv, L.tile_inst, L.tile_rows, L.tile_sweep};
+}
+
+StepView step_view(const Batch& b) {
+    const BatchLevel& F = b.levels[0];
+    return StepView{F.rows, F.tiles, b.instances, F.tile_inst, F.tile_rows, b.tile_begin, F.col, b.w, b.area,
+                    b.conductance, b.step_edge_conductance, b.slope_of};
+}
+
+LevelView<double> view64(const Batch& b, std::size_t level) {
+    const BatchLevel& L = b.levels[level];
+    return make_view<double>(L, L.vd64, L.inv64);
+}
+
+LevelView<float> view32(const Batch& b, std::size_t level) {
+    const BatchLevel& L = b.levels[level];
+    return make_view<float>(L, L.vd32, L.inv32);
+}
+
+namespace {
+
+template <typename T>
+struct Pick;
+template <>
+struct Pick<double> {
+    static LevelView<double> view(const Batch& b, std::size_t l) { return view64(b, l); }
+    static double* x(BatchLevel& L) { return L.x64; }
+    static double* y(BatchLevel& L) { return L.y64; }
+    static double* bvec(BatchLevel& L) { return L.b64; }
+    static double* r(BatchLevel& L) { return L.r64; }
+    static const double* inv(const DenseCoarse& D) { return D.inv64; }
+    static double** k(Batch& b) { return b.k64; }
+};
+template <>
+struct Pick<float> {
+    static LevelView<float> view(const Batch& b, std::size_t l) { return view32(b, l); }
+    static float* x(BatchLevel& L) { return L.x32; }
+    static float* y(BatchLevel& L) { return L.y32; }
+    static float* bvec(BatchLevel& L) { return L.b32; }
+    static float* r(BatchLevel& L) { return L.r32; }
+    static const float* inv(const DenseCoarse& D) { return D.inv32; }
+    static float** k(Batch& b) { return b.k32; }
+};
+
+DenseView dense_view(const Batch& b) {
+    const DenseCoarse& D = b.dense;
+    return DenseView{b.instances, D.d_level, D.d_offset, D.d_size, D.d_row_base};
+}
+
+}  // namespace
+
+void assemble_transport(Batch& b, const double* slope, const double* conductance,
+                        const double* edge_conductance, cudaStream_t st) {
+    const LevelView<double> fine = view64(b, 0);
+    launch_assemble_transport(fine, b.w, b.wsum, b.area, slope, conductance, edge_conductance,
+                              b.levels[0].vd64, st);
+}
+
+void set_matrix_csr(Batch& b, const double* diag, const double* off, cudaStream_t st) {
+    if (b.instances != 1) throw std::invalid_argument("set_matrix applies to a one-planet batch");
+    Planet& p = *b.planets[0];
+    launch_set_matrix_csr(static_cast<std::uint32_t>(p.graph.size()), b.levels[0].rows, b.levels[0].width,
+                          b.csr_offset, diag, off, b.levels[0].vd64, st);
+}
+
+void prepare_levels(Batch& b, cudaStream_t st) {
+    for (std::size_t l = 0; l + 1 < b.levels.size(); ++l) {
+        BatchLevel& F = b.levels[l];
+        BatchLevel& C = b.levels[l + 1];
+        launch_galerkin(F.gal_lists, F.gal_offset, F.gal_source, F.vd64, C.vd64, st);
+    }
+    for (std::size_t l = 0; l < b.levels.size(); ++l) {
+        BatchLevel& L = b.levels[l];
+        launch_finalize_level(L.rows, L.width, L.vd64, L.vd32, L.inv64, L.inv32, st);
+    }
+    const DenseView dv = dense_view(b);
+    for (std::size_t l = 0; l < b.levels.size(); ++l) {
+        bool any = false;
+        for (auto c : b.dense.level) any = any || (c == static_cast<int>(l));
+        if (!any) continue;
+        launch_dense_invert(dv, static_cast<int>(l), view64(b, l), b.dense.work, b.dense.inv64,
+                            b.dense.inv32, st);
+    }
+    PSGB_CUDA(cudaGetLastError());
+    b.matrix_ready = true;
+}
+
+// The buffer the first (zero-start) sweep of a level must write so that, after all
+// of the level's sweeps, the iterate ends in `x`.
+static bool starts_in_x(const SmootherConfig& s) { return ((s.pre - 1 + s.post) % 2) == 0; }
+
+template <typename T>
+T* vcycle_first_target(Batch& b, T* x) {
+    return starts_in_x(b.smoother) ? x : Pick<T>::y(b.levels[0]);
+}
+
+template <typename T>
+void vcycle(Batch& b, const T* rhs, T* x, int gate, bool first_sweep_done, cudaStream_t st) {
+    const std::size_t depth = b.levels.size();
+    const SmootherConfig& sm = b.smoother;
+    const T omega = static_cast<T>(sm.omega);
+    const DenseView dv = dense_view(b);
+    std::vector<T*> cur(depth), other(depth);
+    std::vector<const T*> rhs_of(depth);
+    for (std::size_t l = 0; l < depth; ++l) {
+        BatchLevel& L = b.levels[l];
+        T* X = (l == 0) ? x : Pick<T>::x(L);
+        T* Y = Pick<T>::y(L);
+        cur[l] = starts_in_x(sm) ? X : Y;
+        other[l] = starts_in_x(sm) ? Y : X;
+        rhs_of[l] = (l == 0) ? rhs : Pick<T>::bvec(L);
+    }
+    // Planets whose only level is the fine one: dense solve there.
+    launch_dense_solve<T>(dv, 0, b.dense.max_rows, Pick<T>::inv(b.dense), rhs, x, b.scalars, gate, st);
+    for (std::size_t l = 0; l + 1 < depth; ++l) {
+        const LevelView<T> lv = Pick<T>::view(b, l);
+        BatchLevel& L = b.levels[l];
+        if (!(l == 0 && first_sweep_done)) launch_smooth_zero<T>(lv, rhs_of[l], cur[l], omega, b.scalars, gate, st);
+        for (int k = 1; k < sm.pre; ++k) {
+            launch_smooth<T>(lv, rhs_of[l], cur[l], other[l], omega, b.scalars, gate, st);
+            std::swap(cur[l], other[l]);
+        }
+        launch_residual<T>(lv, rhs_of[l], cur[l], Pick<T>::r(L), b.scalars, gate, st);
+        BatchLevel& C = b.levels[l + 1];
+        const LevelView<T> cv = Pick<T>::view(b, l + 1);
+        launch_restrict<T>(cv, L.member_offset, L.member, Pick<T>::r(L), Pick<T>::bvec(C), b.scalars, gate, st);
+        launch_dense_solve<T>(dv, static_cast<int>(l + 1), b.dense.max_rows, Pick<T>::inv(b.dense),
+                              Pick<T>::bvec(C), Pick<T>::x(C), b.scalars, gate, st);
+    }
+    for (std::size_t l = depth - 1; l-- > 0;) {
+        const LevelView<T> lv = Pick<T>::view(b, l);
+        BatchLevel& L = b.levels[l];
+        launch_prolong<T>(lv, L.agg, Pick<T>::x(b.levels[l + 1]), cur[l], b.scalars, gate, st);
+        for (int k = 0; k < sm.post; ++k) {
+            launch_smooth<T>(lv, rhs_of[l], cur[l], other[l], omega, b.scalars, gate, st);
+            std::swap(cur[l], other[l]);
+        }
+    }
+}
+
+template void vcycle<double>(Batch&, const double*, double*, int, bool, cudaStream_t);
+template void vcycle<float>(Batch&, const float*, float*, int, bool, cudaStream_t);
+template double* vcycle_first_target<double>(Batch&, double*);
+template float* vcycle_first_target<float>(Batch&, float*);
+
+namespace {
+
+ReduceCtx reduce_ctx(Batch& b) { return ReduceCtx{b.partial, b.ticket, b.tile_begin, b.scalars}; }
+
+bool all_done(Batch& b, cudaStream_t st, bool outer) {
+    PSGB_CUDA(cudaMemcpyAsync(b.pinned_scalars, b.scalars, b.instances * sizeof(InstanceScalars),
+                              cudaMemcpyDeviceToHost, st));
+    PSGB_CUDA(cudaStreamSynchronize(st));
+    for (std::uint32_t i = 0; i < b.instances; ++i) {
+        const InstanceScalars& s = b.pinned_scalars[i];
+        if (outer ? s.outer_status == kRunning : (s.outer_status == kRunning && s.status == kRunning)) return false;
+    }
+    return true;
+}
+
+// Inner Krylov solve A x = rhs (level-0 vectors in T), x0 = 0.
+template <typename T>
+void krylov(Batch& b, const SolveOptions& opt, const T* rhs, T* x, double tol, cudaStream_t st) {
+    using K = KrylovLaunch<T>;
+    const LevelView<T> lv = Pick<T>::view(b, 0);
+    const ReduceCtx ctx = reduce_ctx(b);
+    T** v = Pick<T>::k(b);
+    const T omega_j = static_cast<T>(b.smoother.omega);
+    const int max_it = opt.max_iterations;
+    if (opt.method == kBiCGSTAB) {
+        T *r = v[0], *shadow = v[1], *p = v[2], *vv = v[3], *phat = v[4], *s = v[5], *shat = v[6], *t = v[7];
+        K::bicg_init(lv, rhs, x, r, shadow, p, vv, ctx, tol, max_it, st);
+        int it = 0;
+        while (it < max_it) {
+            for (int k = 0; k < opt.poll; ++k, ++it) {
+                T* first = vcycle_first_target<T>(b, phat);
+                K::bicg_p(lv, r, vv, p, first, omega_j, b.scalars, st);
+                vcycle<T>(b, p, phat, kGateRunning, true, st);
+                K::bicg_v(lv, phat, vv, shadow, ctx, st);
+                T* first_s = vcycle_first_target<T>(b, shat);
+                K::bicg_s(lv, r, vv, s, first_s, omega_j, ctx, st);
+                vcycle<T>(b, s, shat, kGateSecondHalf, true, st);
+                K::bicg_t(lv, shat, t, s, ctx, st);
+                K::bicg_x(lv, phat, shat, s, t, x, r, shadow, ctx, st);
+            }
+            PSGB_CUDA(cudaGetLastError());
+            if (all_done(b, st, false)) break;
+        }
+    } else {
+        T *r = v[0], *p = v[2], *q = v[3], *z = v[4];
+        T* first = vcycle_first_target<T>(b, z);
+        K::pcg_init(lv, rhs, x, r, p, first, omega_j, ctx, tol, max_it, st);
+        vcycle<T>(b, r, z, kGateRunning, true, st);
+        int it = 0;
+        while (it < max_it) {
+            for (int k = 0; k < opt.poll; ++k, ++it) {
+                K::pcg_rz(lv, r, z, ctx, st);
+                K::pcg_p(lv, z, p, b.scalars, st);
+                K::pcg_q(lv, p, q, ctx, st);
+                K::pcg_xr(lv, p, q, x, r, first, omega_j, ctx, st);
+                vcycle<T>(b, r, z, kGateRunning, true, st);
+            }
+            PSGB_CUDA(cudaGetLastError());
+            if (all_done(b, st, false)) break;
+        }
+    }
+}
+
+}  // namespace
+
+void solve(Batch& b, const SolveOptions& opt, const double* rhs, double* x, cudaStream_t st) {
+    if (!b.matrix_ready) throw std::logic_error("solve before the matrix was set");
+    const LevelView<double> lv64 = view64(b, 0);
+    const ReduceCtx ctx = reduce_ctx(b);
+    launch_outer_init(lv64, rhs, ctx, opt.tolerance, opt.max_refinements, st);
+    // Inner target: max(inner_tol * ||r||, tolerance * ||b|| / 2); the plain FP64 solve
+    // reaches the outer target in one refinement, the mixed one in a few.
+    const double inner_tol = opt.precision == kMixed ? opt.inner_tolerance : 1e-3 * opt.tolerance;
+    for (int refine = 0; refine <= opt.max_refinements; ++refine) {
+        if (opt.precision == kMixed) {
+            launch_outer_residual<float>(lv64, rhs, x, b.rr, b.k32[8], ctx, opt.max_refinements, st);
+        } else {
+            launch_outer_residual<double>(lv64, rhs, x, b.rr, b.k64[8], ctx, opt.max_refinements, st);
+        }
+        if (all_done(b, st, true)) break;
+        if (opt.precision == kMixed) {
+            krylov<float>(b, opt, b.k32[8], b.k32[9], inner_tol, st);
+            launch_outer_update<float>(lv64, b.k32[9], x, b.scalars, b.instances, st);
+        } else {
+            krylov<double>(b, opt, b.k64[8], b.k64[9], inner_tol, st);
+            launch_outer_update<double>(lv64, b.k64[9], x, b.scalars, b.instances, st);
+        }
+    }
+    PSGB_CUDA(cudaMemcpyAsync(b.pinned_scalars, b.scalars, b.instances * sizeof(InstanceScalars),
+                              cudaMemcpyDeviceToHost, st));
+    PSGB_CUDA(cudaStreamSynchronize(st));
+    std::memcpy(b.host_scalars.data(), b.pinned_scalars, b.instances * sizeof(InstanceScalars));
+}
+
+}  // namespace psgb
