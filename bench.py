@@ -1,0 +1,417 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 implicit heat-transport sub-step (PlanetSim).
+
+Workload (default, `--workload batch`): the batched uneven-planet sub-step - 64 planets
+(16 x L4, 24 x L5, 16 x L6, 8 x L7; 2,252,928 cells), radius U(3e6, 9e6) m, per-edge
+diffusivity lognormal (median 1e6 m^2/s, sigma 0.5), the config-0 state and sources;
+FP32 multigrid-preconditioned BiCGSTAB inside FP64 iterative refinement to a 1e-10
+relative residual, all 64 planets solved together in the concatenated block layout. A
+step is one sub-step of every planet; the metric is sub-steps/s (planets x steps / s).
+
+`--workload l8` times the L8 plain-FP64 drop-in solve (one planet) instead.
+
+Reported beside it, in the same JSON line: the plain one-planet-at-a-time FP64 GPU
+solve of the same planets (the drop-in comparator), the end-to-end rate through the
+C-ABI with host buffers, the dominant kernel's roofline (CUDA events on its launching
+stream during a profiled pass over the same steps, algorithmic bytes counted on the
+device), a CPU baseline (the oracle's port of the reference's FP64 PCG solve, one
+host core, a bounded sample) and the SM clocks sampled during the timed region.
+
+`--impl reference` times the reference algorithm on the host cores instead (the oracle
+port, all cores, one process per core), on the same workload, metric and unit.
+
+Multi-GPU (`torchrun ... --gpus N`): planets are independent, so every rank solves its
+own replica of the workload with no data-path collective ("replicas only"); the value
+is the units of all ranks over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_HBM_GBS = 6800.0
+TRAFFIC_FILE = ROOT / "profiles" / "traffic.json"
+
+
+# ---- distributed helpers -----------------------------------------------------------------
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def init_dist(world: int, backend: str):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def max_over_ranks(value: float, dist, device=None) -> float:
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ---- clocks ---------------------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if self.proc is None or self.file is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        rows = [line.split(",") for line in Path(self.file.name).read_text().splitlines() if line.strip()]
+        os.unlink(self.file.name)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for name, flag in zip(names, r[5:9]):
+                if flag.strip().lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks() -> tuple[float, str]:
+    if MEASURED_PEAKS.exists():
+        return float(json.loads(MEASURED_PEAKS.read_text())["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+# ---- workloads ---------------------------------------------------------------------------------
+
+def make_workload(kind: str, seed: int):
+    """Planets and their inputs (host numpy)."""
+    import planet_game_gb300 as pg
+    from planet_game_gb300 import workloads as W
+
+    planets = []
+    if kind == "batch":
+        for i, spec in enumerate(W.planet_mix(seed)):
+            m = pg.make_icosphere(spec.level, spec.radius)
+            kappa = W.lognormal_edge_diffusivity(m.edge_count, spec.seed)
+            inp = W.step_inputs(m, spec.seed, edge_diffusivity=kappa)
+            planets.append((m, inp))
+    elif kind == "l8":
+        m = pg.make_icosphere(8, W.EARTH_RADIUS)
+        planets.append((m, W.step_inputs(m, seed)))
+    else:
+        raise SystemExit(f"unknown workload {kind}")
+    return planets
+
+
+def precision_for(kind: str) -> str:
+    return "mixed" if kind == "batch" else "fp64"
+
+
+SOLVER = dict(method="bicgstab", tolerance=1e-10, inner_tolerance=1e-4, poll=4)
+
+
+# ---- the GB300 arm ---------------------------------------------------------------------------------
+
+def run_gb300(args, rank, world, local_rank):
+    import torch
+
+    import planet_game_gb300 as pg
+    from planet_game_gb300 import capi
+
+    torch.cuda.set_device(local_rank)
+    dist = init_dist(world, "nccl")
+    dev = torch.device("cuda", local_rank)
+    planets = make_workload(args.workload, args.seed)
+    meshes = [m for m, _ in planets]
+    cells = sum(m.cell_count for m in meshes)
+    prec = precision_for(args.workload)
+    batch = pg.Batch(meshes)
+    t0_d = [torch.from_numpy(inp.t0).to(dev) for _, inp in planets]
+    s_d = [torch.from_numpy(inp.source).to(dev) for _, inp in planets]
+    out_d = [torch.empty_like(t) for t in t0_d]
+    heat = [inp.heat_capacity for _, inp in planets]
+    dt = [inp.dt for _, inp in planets]
+    cond = [inp.conductance for _, inp in planets]
+    edge_g = [inp.edge_conductance for _, inp in planets] if planets[0][1].edge_conductance is not None else None
+    lib = capi.load()
+
+    def step(t0, src, out):
+        _, reps = batch.transport_step(t0, src, heat, dt, conductance=cond, edge_conductance=edge_g, out=out,
+                                       precision=prec, **SOLVER)
+        return reps
+
+    for _ in range(args.warmup):
+        reps = step(t0_d, s_d, out_d)
+    torch.cuda.synchronize()
+    bad = [r for r in reps if r.status != 0 or r.relative_residual > 1e-10 or r.closure > 1e-12]
+    if bad:
+        raise SystemExit(f"solve failed its gates: {bad[0]}")
+
+    # timed region: inputs resident in HBM
+    stream = torch.cuda.current_stream()
+    launches0 = lib.psgb_launch_count()
+    with ClockSampler(local_rank) as clocks:
+        barrier(dist)
+        torch.cuda.synchronize()
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        iters = []
+        for _ in range(args.steps):
+            reps = step(t0_d, s_d, out_d)
+            iters.append(sum(r.iterations * m.cell_count for r, m in zip(reps, meshes)))
+        end.record(stream)
+        torch.cuda.synchronize()
+        barrier(dist)
+    launches = lib.psgb_launch_count() - launches0
+    elapsed = max_over_ranks(start.elapsed_time(end) / 1e3, dist, dev)
+    units = len(meshes) * args.steps * world
+    value = units / elapsed
+    clock = clocks.summary()
+    refinements = [r.refinements for r in reps]
+
+    # end to end: host buffers, copies inside the timed region
+    t0_h = [inp.t0 for _, inp in planets]
+    s_h = [inp.source for _, inp in planets]
+    out_h = [np.empty_like(x) for x in t0_h]
+    barrier(dist)
+    torch.cuda.synchronize()
+    t_e2e = time.perf_counter()
+    for _ in range(args.steps):
+        step(t0_h, s_h, out_h)
+    torch.cuda.synchronize()
+    e2e_elapsed = max_over_ranks(time.perf_counter() - t_e2e, dist, dev)
+    e2e = {"value": units / e2e_elapsed, "unit": "sub-steps/s", "h2d_bytes_per_step": cells * 16,
+           "d2h_bytes_per_step": cells * 8}
+
+    # profiled pass: the dominant kernel family timed with events on its stream
+    prof_family = b"smooth"
+    capi.check(lib.psgb_profile_begin(prof_family))
+    for _ in range(args.steps):
+        step(t0_d, s_d, out_d)
+    import ctypes as C
+
+    ms, nl, nbytes = C.c_double(), C.c_uint64(), C.c_uint64()
+    capi.check(lib.psgb_profile_end(C.byref(ms), C.byref(nl), C.byref(nbytes)))
+    peak, peak_kind = peaks()
+    achieved = nbytes.value / (ms.value / 1e3) / 1e9 if ms.value > 0 else None
+    traffic = None
+    if TRAFFIC_FILE.exists():
+        t = json.loads(TRAFFIC_FILE.read_text()).get(args.workload)
+        if t:
+            traffic = t.get("dram_bytes_per_launch")
+    roofline = {"bound": "hbm", "kernel": "k_smooth (Jacobi sweep, all levels)", "achieved": achieved,
+                "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                "launches": int(nl.value), "avg_launch_us": ms.value * 1e3 / max(1, nl.value),
+                "bytes_per_launch": nbytes.value / max(1, nl.value)}
+
+    # the plain one-planet-at-a-time FP64 GPU drop-in on the same planets
+    plain = None
+    if rank == 0 and not args.skip_plain:
+        for i, (m, inp) in enumerate(planets):   # warm the solo batches
+            pg.transport_step(m, t0_d[i], s_d[i], inp.heat_capacity, inp.dt, inp.conductance,
+                              edge_conductance=inp.edge_conductance, precision="fp64", **SOLVER)
+        torch.cuda.synchronize()
+        tp = time.perf_counter()
+        plain_iters = 0
+        for i, (m, inp) in enumerate(planets):
+            _, _, r = pg.transport_step(m, t0_d[i], s_d[i], inp.heat_capacity, inp.dt, inp.conductance,
+                                        edge_conductance=inp.edge_conductance, precision="fp64", **SOLVER)
+            plain_iters += r.iterations
+            if r.status != 0:
+                raise SystemExit(f"plain FP64 solve failed: {r}")
+        torch.cuda.synchronize()
+        plain = {"value": len(planets) / (time.perf_counter() - tp), "unit": "sub-steps/s",
+                 "krylov_iterations": plain_iters, "solver": "FP64 AMG-BiCGSTAB, one planet per call"}
+
+    cpu = cpu_baseline(planets, args) if (rank == 0 and not args.skip_cpu) else None
+    if rank == 0:
+        line = {
+            "metric": "sub-steps/s at 1e-10 relative residual",
+            "value": value,
+            "unit": "sub-steps/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": elapsed * 1e3 / args.steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32 inner, f64 refinement" if prec == "mixed" else "f64",
+            "data": "synthetic",
+            "config": {
+                "workload": ("64 uneven planets (16xL4, 24xL5, 16xL6, 8xL7; 2,252,928 cells), per-edge lognormal "
+                             "diffusivity, one batched sub-step per step" if args.workload == "batch"
+                             else "one L8 planet (655,362 cells), plain FP64 drop-in solve"),
+                "planets": len(meshes), "cells": cells, "precision": prec, "krylov": "BiCGSTAB",
+                "smoother": "damped Jacobi 2+2, omega 0.8", "tolerance": 1e-10,
+                "krylov_iterations_per_step": sum(r.iterations for r in reps), "refinements_last_step": max(refinements),
+                "cell_iterations_per_s": statistics.mean(iters) * world / (elapsed / args.steps),
+                "l2": "working set larger than the 129 MB L2 (no flush needed)" if cells > 1_000_000 else
+                      "working set may be L2 resident",
+                "plain_fp64_one_at_a_time": plain,
+                "parallelism": f"replicas x{world}",
+            },
+            "e2e": e2e,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clock,
+            "gpu_launches": int(launches),
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+# ---- CPU baseline and the reference arm ------------------------------------------------------
+
+def _oracle_solve(payload):
+    """One planet's sub-step by the oracle's port of the reference (FP64 PCG + SGS V-cycle)."""
+    arrays, inp, edge_g, tol = payload
+    from oracle import oracle as O
+
+    om = O.OracleMesh(arrays)
+    h = O.OracleHierarchy(om)
+    t = time.perf_counter()
+    out = h.transport_step(inp["conductance"], inp["heat_capacity"], inp["dt"], inp["t0"], inp["source"], tol=tol,
+                           edge_g=None if edge_g is None else om.directed_conductance(edge_g))
+    return time.perf_counter() - t, out["iterations"]
+
+
+def _payload(m, inp):
+    return (m.arrays(), {"conductance": inp.conductance, "heat_capacity": inp.heat_capacity, "dt": inp.dt,
+                         "t0": inp.t0, "source": inp.source}, inp.edge_conductance, 1e-10)
+
+
+def cpu_baseline(planets, args):
+    """A bounded sample on one host core: every planet of the mix once (about 10-30 s)."""
+    from oracle import oracle as O  # noqa: F401  (the checker; timed here as the CPU baseline)
+
+    total, iters = 0.0, 0
+    for m, inp in planets:
+        dt, it = _oracle_solve(_payload(m, inp))
+        total += dt
+        iters += it
+    return {"value": len(planets) / total, "unit": "sub-steps/s", "cores": 1, "kind": "port",
+            "sample": f"all {len(planets)} planets of the workload once, one core, FP64 PCG + SGS V-cycle to 1e-10",
+            "pcg_iterations": iters}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    import multiprocessing as mp
+
+    planets = make_workload(args.workload, args.seed)
+    payloads = [_payload(m, inp) for m, inp in planets]
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(processes=cores) as pool:
+        for _ in range(args.warmup):
+            pool.map(_oracle_solve, payloads, chunksize=1)
+        t = time.perf_counter()
+        for _ in range(args.steps):
+            results = pool.map(_oracle_solve, payloads, chunksize=1)
+        elapsed = time.perf_counter() - t
+    value = len(planets) * args.steps / elapsed
+    line = {
+        "impl": "reference",
+        "metric": "sub-steps/s at 1e-10 relative residual",
+        "value": value,
+        "unit": "sub-steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": elapsed * 1e3 / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "same planets and inputs as the GB300 arm", "planets": len(planets),
+                   "cells": sum(m.cell_count for m, _ in planets), "pcg_iterations": sum(r[1] for r in results)},
+        "cpu_baseline": {"value": value, "unit": "sub-steps/s", "cores": cores, "kind": "port",
+                         "sample": "every planet of the workload per step, one process per core"},
+        "e2e": {"value": value, "unit": "sub-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=["batch", "l8"], default="batch")
+    ap.add_argument("--seed", type=int, default=2026)
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-plain", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local_rank = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    run_gb300(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -134,6 +134,11 @@ int psgb_multigrid_set_matrix(psgb_planet* planet, const double* diagonal, const
 int psgb_multigrid_precondition(psgb_planet* planet, int dtype, const void* rhs, void* solution,
                                 int memory, void* stream);
 
+/* The values the GPU holds on multigrid level `level` after set_matrix / a step's
+ * assembly: diagonal [rows] and off-diagonals in the level's CSR order (FP64; the
+ * Galerkin sums of heat_transport.cpp:157-171, in the reference's summation order). */
+int psgb_multigrid_level_values(psgb_planet* planet, uint32_t level, double* diagonal, double* off_diagonal);
+
 typedef struct psgb_solve_options {
     int precision;               /* PSGB_PRECISION_* */
     int method;                  /* PSGB_METHOD_* */
@@ -218,6 +223,17 @@ int psgb_column_radiation(uint32_t cells, uint32_t layers, const psgb_column_con
                           const double* surface_temperature_K, const double* surface_pressure_Pa,
                           double* emissivity, double* absorbed, double* fraction, double* reflectance,
                           double* scalars, int memory, void* stream);
+
+/* ---- launch accounting and kernel timing (no counterpart in the reference) -------
+ * psgb_launch_count: kernels this library has launched since it was loaded.
+ * psgb_profile_begin: from now on, time every launch of one kernel family ("smooth",
+ * "residual", "restrict", "prolong", "dense", "krylov_spmv", "krylov_vector", "refine",
+ * "setup", "step", "operator", "column") with CUDA events on its launching stream.
+ * psgb_profile_end: synchronises, returns the summed device time (ms) and launch count of
+ * that family, and the algorithmic bytes the Jacobi sweeps moved since the profile began. */
+uint64_t psgb_launch_count(void);
+int psgb_profile_begin(const char* family);
+int psgb_profile_end(double* total_ms, uint64_t* launches, uint64_t* swept_bytes);
 
 /* ---- inputs ---------------------------------------------------------------------
  * Sub-step-mean insolation of sub-step `substep` for the Earth-development planet

@@ -1,0 +1,198 @@
+"""ctypes bindings of the CPU oracle (oracle/planetsim_oracle.cpp) - TEST INFRASTRUCTURE.
+
+Imported only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg, as the
+checker and the timed CPU baseline. The product never imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB = Path(__file__).resolve().parent / "lib" / "libplanetsim_oracle.so"
+
+
+class Graph(C.Structure):
+    _fields_ = [("n", C.c_uint64), ("offset", C.c_void_p), ("neighbour", C.c_void_p), ("weight", C.c_void_p),
+                ("weight_sum", C.c_void_p), ("area", C.c_void_p)]
+
+
+class Mesh(C.Structure):
+    _fields_ = [("cells", C.c_uint64), ("edges", C.c_uint64), ("edge_offset", C.c_void_p),
+                ("edge_count", C.c_void_p), ("neighbor", C.c_void_p), ("edge", C.c_void_p),
+                ("normal_east", C.c_void_p), ("normal_north", C.c_void_p), ("edge_first", C.c_void_p),
+                ("edge_length", C.c_void_p), ("edge_distance", C.c_void_p), ("area", C.c_void_p)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            raise FileNotFoundError(f"{LIB} is missing: __graft_entry__.build() compiles the oracle")
+        L = C.CDLL(str(LIB))
+        P = C.c_void_p
+        L.orc_hierarchy_new.restype = P
+        L.orc_hierarchy_new.argtypes = [P]
+        L.orc_hierarchy_free.argtypes = [P]
+        L.orc_hierarchy_levels.restype = C.c_uint64
+        L.orc_hierarchy_levels.argtypes = [P]
+        L.orc_hierarchy_level.argtypes = [P, C.c_uint64, P, P, P, P, P]
+        L.orc_hierarchy_set_matrix.argtypes = [P, P, P]
+        L.orc_hierarchy_values.argtypes = [P, C.c_uint64, P, P]
+        L.orc_vcycle_sgs.argtypes = [P, P, P]
+        L.orc_vcycle_jacobi.argtypes = [P, C.c_int, C.c_int, C.c_double, P, P]
+        L.orc_pcg.restype = C.c_int
+        L.orc_pcg.argtypes = [P, P, C.c_double, P, P, P, C.c_double, C.c_int, P]
+        L.orc_bicgstab.restype = C.c_int
+        L.orc_bicgstab.argtypes = [P, P, C.c_double, P, P, C.c_double, C.c_int, P]
+        L.orc_solve_implicit_transport_linear.argtypes = [P, C.c_double, P, P, C.c_double, C.c_double, P, P, P]
+        L.orc_transport_step.restype = C.c_int
+        L.orc_transport_step.argtypes = [P, P, C.c_double, P, C.c_double, C.c_double, P, P, C.c_double, C.c_int,
+                                         P, P, P, P]
+        L.orc_column_radiation.argtypes = [C.c_uint64, C.c_uint32, P, P, P, P, P, P, P, P, P, P, P]
+        L.orc_saturation_specific_humidity.restype = C.c_double
+        L.orc_saturation_specific_humidity.argtypes = [C.c_double, C.c_double]
+        for name in ("orc_laplacian_f64", "orc_laplacian_f32", "orc_divergence_f64", "orc_divergence_f32"):
+            getattr(L, name).argtypes = [P, P, P]
+        for name in ("orc_gradient_f64", "orc_gradient_f32"):
+            getattr(L, name).argtypes = [P, P, P, P]
+        L.orc_diffusion_source.argtypes = [P, C.c_double, P, P]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return C.c_void_p(a.ctypes.data) if a is not None else C.c_void_p(None)
+
+
+class OracleMesh:
+    """The flat mesh/graph arrays as the oracle's C structs (kept alive here)."""
+
+    def __init__(self, arrays: dict):
+        a = {k: np.ascontiguousarray(v) for k, v in arrays.items()}
+        self.a = a
+        n = len(a["area_m2"])
+        self.n = n
+        self.offset = np.append(a["edge_offset"], np.uint32(len(a["neighbor"]))).astype(np.uint32)
+        self.neighbour = a["neighbor"].astype(np.uint32)
+        self.graph = Graph(n, _p(self.offset), _p(self.neighbour), _p(a["graph_weight"]), _p(a["graph_weight_sum"]),
+                           _p(a["area_m2"]))
+        self.mesh = Mesh(n, len(a["edge_length_m"]), _p(a["edge_offset"]), _p(a["edge_count"]), _p(a["neighbor"]),
+                         _p(a["edge"]), _p(a["normal_east"]), _p(a["normal_north"]), _p(a["edge_first"]),
+                         _p(a["edge_length_m"]), _p(a["edge_distance_m"]), _p(a["area_m2"]))
+
+    def laplacian(self, x):
+        out = np.empty_like(x)
+        getattr(lib(), "orc_laplacian_f64" if x.dtype == np.float64 else "orc_laplacian_f32")(
+            C.byref(self.mesh), _p(x), _p(out))
+        return out
+
+    def gradient(self, x):
+        e, n = np.empty_like(x), np.empty_like(x)
+        getattr(lib(), "orc_gradient_f64" if x.dtype == np.float64 else "orc_gradient_f32")(
+            C.byref(self.mesh), _p(x), _p(e), _p(n))
+        return e, n
+
+    def divergence(self, f):
+        out = np.empty(self.n, dtype=f.dtype)
+        getattr(lib(), "orc_divergence_f64" if f.dtype == np.float64 else "orc_divergence_f32")(
+            C.byref(self.mesh), _p(f), _p(out))
+        return out
+
+    def diffusion_source(self, K, t):
+        out = np.empty(self.n)
+        lib().orc_diffusion_source(C.byref(self.graph), K, _p(t), _p(out))
+        return out
+
+    def directed_conductance(self, per_edge):
+        """Per-CSR-entry values from per-undirected-edge values."""
+        return np.ascontiguousarray(np.asarray(per_edge)[self.a["edge"]], dtype=np.float64)
+
+    def solve_implicit_transport_linear(self, K, base, slope, cg_tol=1e-12, newton_tol=1e-9):
+        mean, src, stats = np.empty(self.n), np.empty(self.n), np.empty(6)
+        lib().orc_solve_implicit_transport_linear(C.byref(self.graph), K, _p(base), _p(slope), cg_tol, newton_tol,
+                                                  _p(mean), _p(src), _p(stats))
+        return mean, src, stats
+
+
+class OracleHierarchy:
+    def __init__(self, om: OracleMesh):
+        self.om = om
+        self.h = C.c_void_p(lib().orc_hierarchy_new(C.byref(om.graph)))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_hierarchy_free(self.h)
+
+    def levels(self) -> int:
+        return int(lib().orc_hierarchy_levels(self.h))
+
+    def level(self, l: int) -> dict:
+        sizes = np.zeros(4, np.uint64)
+        ptrs = [C.c_void_p() for _ in range(4)]
+        lib().orc_hierarchy_level(self.h, l, _p(sizes), *[C.byref(p) for p in ptrs])
+        rows, nnz, na, nt = (int(s) for s in sizes)
+
+        def view(ptr, dtype, count):
+            if count == 0:
+                return np.empty(0, dtype)
+            raw = (C.c_char * (count * np.dtype(dtype).itemsize)).from_address(ptr.value)
+            return np.frombuffer(raw, dtype=dtype, count=count).copy()
+
+        return {"rows": rows, "offset": view(ptrs[0], np.uint32, rows + 1), "column": view(ptrs[1], np.uint32, nnz),
+                "aggregate": view(ptrs[2], np.uint32, na), "target": view(ptrs[3], np.int64, nt)}
+
+    def set_matrix(self, diag, off):
+        diag, off = np.ascontiguousarray(diag, np.float64), np.ascontiguousarray(off, np.float64)
+        lib().orc_hierarchy_set_matrix(self.h, _p(diag), _p(off))
+
+    def values(self, l: int):
+        lv = self.level(l)
+        d, o = np.empty(lv["rows"]), np.empty(len(lv["column"]))
+        lib().orc_hierarchy_values(self.h, l, _p(d), _p(o))
+        return d, o
+
+    def vcycle_sgs(self, rhs):
+        out = np.empty(self.om.n)
+        lib().orc_vcycle_sgs(self.h, _p(np.ascontiguousarray(rhs, np.float64)), _p(out))
+        return out
+
+    def vcycle_jacobi(self, rhs, pre=2, post=2, omega=0.8):
+        out = np.empty(self.om.n)
+        lib().orc_vcycle_jacobi(self.h, pre, post, omega, _p(np.ascontiguousarray(rhs, np.float64)), _p(out))
+        return out
+
+    def pcg(self, K, slope, rhs, tol=1e-12, max_it=2000, edge_g=None):
+        x = np.empty(self.om.n)
+        it = lib().orc_pcg(self.h, C.byref(self.om.graph), K, _p(edge_g), _p(slope), _p(rhs), tol, max_it, _p(x))
+        return x, it
+
+    def bicgstab(self, K, slope, rhs, tol=1e-12, max_it=2000):
+        x = np.empty(self.om.n)
+        it = lib().orc_bicgstab(self.h, C.byref(self.om.graph), K, _p(slope), _p(rhs), tol, max_it, _p(x))
+        return x, it
+
+    def transport_step(self, K, C_heat, dt, t0, src, tol=1e-12, max_it=2000, edge_g=None):
+        n = self.om.n
+        ts, h, tn, sums = np.empty(n), np.empty(n), np.empty(n), np.empty(6)
+        it = lib().orc_transport_step(self.h, C.byref(self.om.graph), K, _p(edge_g), C_heat, dt, _p(t0), _p(src), tol,
+                                      max_it, _p(ts), _p(h), _p(tn), _p(sums))
+        return {"t_solved": ts, "transport": h, "t_new": tn, "sums": sums, "iterations": it}
+
+
+def column_radiation(constants, temperature, humidity, cloud, ts, ps):
+    layers, cells = temperature.shape
+    k = np.ascontiguousarray(constants, dtype=np.float64)
+    ins = [np.ascontiguousarray(a, dtype=np.float64) for a in (temperature, humidity, cloud, ts, ps)]
+    outs = [np.empty((layers, cells)) for _ in range(4)]
+    scal = np.empty((5, cells))
+    lib().orc_column_radiation(cells, layers, _p(k), *[_p(a) for a in ins], *[_p(o) for o in outs], _p(scal))
+    return (*outs, scal)
+
+
+def saturation_specific_humidity(t, p):
+    return lib().orc_saturation_specific_humidity(float(t), float(p))

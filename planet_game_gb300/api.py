@@ -236,6 +236,14 @@ class GraphMultigrid:
         mem, st = _memory_of(diagonal, off_diagonal)
         _raise(capi.load().psgb_multigrid_set_matrix(self.mesh.handle, _ptr(diagonal), _ptr(off_diagonal), mem, st))
 
+    def level_values(self, level: int):
+        """(diagonal, off-diagonals in CSR order) of a level as held on the GPU."""
+        lv = self.mesh.hierarchy_level(level)
+        rows = len(lv["offset"]) - 1
+        d, o = np.empty(rows), np.empty(len(lv["column"]))
+        _raise(capi.load().psgb_multigrid_level_values(self.mesh.handle, level, _ptr(d), _ptr(o)))
+        return d, o
+
     def precondition(self, rhs):
         out = _empty_like(rhs, (self.mesh.cell_count,))
         mem, st = _memory_of(rhs, out)

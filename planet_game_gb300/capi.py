@@ -88,6 +88,7 @@ _SIGNATURES = {
     "psgb_diffusion_source": (C.c_int, [P, C.c_double, P, P, C.c_int, P]),
     "psgb_multigrid_set_matrix": (C.c_int, [P, P, P, C.c_int, P]),
     "psgb_multigrid_precondition": (C.c_int, [P, C.c_int, P, P, C.c_int, P]),
+    "psgb_multigrid_level_values": (C.c_int, [P, C.c_uint32, P, P]),
     "psgb_solve_options_default": (None, [C.POINTER(SolveOptions)]),
     "psgb_solve_newton_system": (C.c_int, [P, C.POINTER(SolveOptions), C.c_double, P, P, P,
                                            C.POINTER(SolveReport), C.c_int, P]),
@@ -102,6 +103,9 @@ _SIGNATURES = {
     "psgb_column_radiation": (C.c_int, [C.c_uint32, C.c_uint32, C.POINTER(ColumnConstants), P, P, P, P, P, P, P,
                                         P, P, P, C.c_int, P]),
     "psgb_substep_mean_insolation": (C.c_int, [P, C.c_int64, P]),
+    "psgb_launch_count": (C.c_uint64, []),
+    "psgb_profile_begin": (C.c_int, [C.c_char_p]),
+    "psgb_profile_end": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
 }
 
 # Every symbol the header declares (checked by the CPU test suite).

@@ -9,6 +9,7 @@
 #include "column.hpp"
 #include "host/insolation.hpp"
 #include "operators.hpp"
+#include "profile.hpp"
 #include "solver.hpp"
 
 #include <cmath>
@@ -51,6 +52,8 @@ int guarded(F&& body) {
     } catch (const psgb::CudaError& e) {
         const std::string m = e.what();
         return fail(m.find("out of memory") != std::string::npos ? PSGB_ERR_OUT_OF_MEMORY : PSGB_ERR_CUDA, m);
+    } catch (const std::overflow_error& e) {
+        return fail(PSGB_ERR_INVALID_ARGUMENT, e.what());
     } catch (const std::logic_error& e) {
         return fail(PSGB_ERR_LOGIC, e.what());
     } catch (const std::exception& e) {
@@ -476,6 +479,26 @@ int psgb_multigrid_set_matrix(psgb_planet* h, const double* diagonal, const doub
     });
 }
 
+int psgb_multigrid_level_values(psgb_planet* h, uint32_t level, double* diagonal, double* off_diagonal) {
+    return guarded([&] {
+        require(h != nullptr && diagonal != nullptr && off_diagonal != nullptr, "null argument");
+        psgb::Batch& b = solo(h);
+        require(b.matrix_ready, "no matrix has been set");
+        const auto& levels = h->planet->hierarchy.levels;
+        require(level < levels.size(), "multigrid level out of range");
+        const psgb::HostLevel& hl = levels[level];
+        const psgb::BatchLevel& L = b.levels[level];
+        const std::size_t P = L.rows, W = L.width;
+        std::vector<double> vd((W + 1) * P);
+        PSGB_CUDA(cudaMemcpy(vd.data(), L.vd64, vd.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        for (std::uint32_t r = 0; r < hl.size; ++r) {
+            diagonal[r] = vd[W * P + r];
+            for (std::uint32_t k = hl.offset[r]; k < hl.offset[r + 1]; ++k) off_diagonal[k] = vd[(k - hl.offset[r]) * P + r];
+        }
+        return PSGB_OK;
+    });
+}
+
 int psgb_multigrid_precondition(psgb_planet* h, int dtype, const void* rhs, void* solution, int memory,
                                 void* stream) {
     return guarded([&] {
@@ -667,6 +690,31 @@ int psgb_column_radiation(uint32_t cells, uint32_t layers, const psgb_column_con
         copy_out(reflectance, d_r, lc * 8, memory, st);
         copy_out(scalars, d_s, std::size_t(5) * cells * 8, memory, st);
         PSGB_CUDA(cudaStreamSynchronize(st));
+        return PSGB_OK;
+    });
+}
+
+uint64_t psgb_launch_count(void) { return psgb::launches_total(); }
+
+int psgb_profile_begin(const char* family) {
+    return guarded([&] {
+        const int f = psgb::family_of(family);
+        require(f >= 0, "unknown kernel family");
+        PSGB_CUDA(cudaDeviceSynchronize());
+        psgb::swept_bytes_exchange();
+        psgb::profile_begin(f);
+        return PSGB_OK;
+    });
+}
+
+int psgb_profile_end(double* total_ms, uint64_t* launches, uint64_t* swept_bytes) {
+    return guarded([&] {
+        require(total_ms != nullptr && launches != nullptr && swept_bytes != nullptr, "null argument");
+        PSGB_CUDA(cudaDeviceSynchronize());
+        std::uint64_t n = 0;
+        if (!psgb::profile_end(total_ms, &n)) throw std::logic_error("no profile is active");
+        *launches = n;
+        *swept_bytes = psgb::swept_bytes_exchange();
         return PSGB_OK;
     });
 }

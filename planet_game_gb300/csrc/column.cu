@@ -15,6 +15,7 @@
 // Layout: layer-major [N][cells] arrays, one thread per cell, the column in registers.
 #include "column.hpp"
 #include "common.cuh"
+#include "profile.hpp"
 
 #include <stdexcept>
 
@@ -95,7 +96,7 @@ void launch_column_radiation(std::uint32_t cells, std::uint32_t layers, const Co
                              double* reflectance, double* scalars, cudaStream_t st) {
     const dim3 grid((cells + 127) / 128), block(128);
 #define PSGB_COLUMN_CASE(N) \
-    case N: k_column<N><<<grid, block, 0, st>>>(cells, k, temp, hum, cloud, ts, ps, emissivity, absorbed, fraction, reflectance, scalars); break;
+    case N: PSGB_LAUNCH(kFamColumn, st, (k_column<N><<<grid, block, 0, st>>>(cells, k, temp, hum, cloud, ts, ps, emissivity, absorbed, fraction, reflectance, scalars))); break;
     switch (layers) {
         PSGB_COLUMN_CASE(1) PSGB_COLUMN_CASE(2) PSGB_COLUMN_CASE(3) PSGB_COLUMN_CASE(4)
         PSGB_COLUMN_CASE(5) PSGB_COLUMN_CASE(6) PSGB_COLUMN_CASE(7) PSGB_COLUMN_CASE(8)

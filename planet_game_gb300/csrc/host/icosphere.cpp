@@ -23,6 +23,9 @@
 #include <cmath>
 #include <limits>
 #include <stdexcept>
+#include <map>
+#include <memory>
+#include <mutex>
 #include <unordered_map>
 
 namespace psgb {
@@ -130,23 +133,17 @@ void lloyd(std::vector<V3>& v, const std::vector<Face>& faces, std::uint32_t ite
     }
 }
 
-}  // namespace
+struct UnitMesh {
+    std::vector<V3> vertices;
+    std::vector<Face> faces;
+};
 
-std::size_t icosphere_cell_count(std::uint32_t level) {
-    if (level > 13) throw std::overflow_error("icosphere level too large for 32-bit ids");
-    return 10u * (std::size_t(1) << (2 * level)) + 2u;
-}
-
-HostMesh build_icosphere(std::uint32_t level, double radius_m) {
-    if (!(radius_m > 0.0) || !std::isfinite(radius_m)) {
-        throw std::invalid_argument("icosphere radius must be finite and positive");
-    }
-    const std::size_t n_cells = icosphere_cell_count(level);
-    const std::size_t n_faces = 20u * (std::size_t(1) << (2 * level));
-
-    std::vector<V3> vert = icosahedron_vertices();
-    std::vector<Face> faces = icosahedron_faces();
-    vert.reserve(n_cells);
+UnitMesh subdivide_and_relax(std::uint32_t level) {
+    UnitMesh u;
+    u.vertices = icosahedron_vertices();
+    u.faces = icosahedron_faces();
+    std::vector<V3>& vert = u.vertices;
+    std::vector<Face>& faces = u.faces;
     for (std::uint32_t l = 0; l < level; ++l) {
         std::unordered_map<std::uint64_t, std::uint32_t> midpoints;
         midpoints.reserve(faces.size() * 2);
@@ -173,6 +170,42 @@ HostMesh build_icosphere(std::uint32_t level, double radius_m) {
         faces.swap(next);
         lloyd(vert, faces, lloyd_iterations);
     }
+    return u;
+}
+
+const UnitMesh& relaxed_unit_mesh(std::uint32_t level) {
+    static std::mutex mutex;
+    static std::map<std::uint32_t, std::unique_ptr<UnitMesh>> cache;
+    std::unique_lock<std::mutex> lock(mutex);
+    auto& entry = cache[level];
+    if (!entry) {
+        lock.unlock();
+        auto built = std::make_unique<UnitMesh>(subdivide_and_relax(level));
+        lock.lock();
+        if (!entry) entry = std::move(built);
+    }
+    return *entry;
+}
+
+}  // namespace
+
+std::size_t icosphere_cell_count(std::uint32_t level) {
+    if (level > 13) throw std::overflow_error("icosphere level too large for 32-bit ids");
+    return 10u * (std::size_t(1) << (2 * level)) + 2u;
+}
+
+HostMesh build_icosphere(std::uint32_t level, double radius_m) {
+    if (!(radius_m > 0.0) || !std::isfinite(radius_m)) {
+        throw std::invalid_argument("icosphere radius must be finite and positive");
+    }
+    const std::size_t n_cells = icosphere_cell_count(level);
+    const std::size_t n_faces = 20u * (std::size_t(1) << (2 * level));
+
+    // The relaxed unit-sphere mesh depends on the level only; the radius enters the
+    // final geometry. It is built once per level and cached for the process.
+    const UnitMesh& unit_mesh = relaxed_unit_mesh(level);
+    const std::vector<V3>& vert = unit_mesh.vertices;
+    const std::vector<Face>& faces = unit_mesh.faces;
     if (faces.size() != n_faces || vert.size() != n_cells) {
         throw std::logic_error("icosphere subdivision produced unexpected counts");
     }

@@ -104,4 +104,7 @@ void launch_dense_solve(const DenseView& dense, int level, std::uint32_t max_row
 template <typename T>
 void launch_spmv(const LevelView<T>& lv, const T* x, T* y, cudaStream_t stream);
 
+// Algorithmic bytes of the Jacobi sweeps since the last call (device counter), and reset.
+std::uint64_t swept_bytes_exchange();
+
 }  // namespace psgb

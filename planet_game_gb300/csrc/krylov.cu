@@ -10,6 +10,7 @@
 // partials in tile order and performs the scalar step. Results are therefore
 // bit-identical run to run and the same for a planet alone or inside a batch.
 #include "common.cuh"
+#include "profile.hpp"
 #include "kernels.hpp"
 #include "krylov.hpp"
 
@@ -436,58 +437,58 @@ __global__ void k_outer_account(InstanceScalars* sc, std::uint32_t instances) {
 template <typename T>
 void KrylovLaunch<T>::bicg_init(const LevelView<T>& lv, const T* b, T* x, T* r, T* shadow, T* p, T* v,
                                 const ReduceCtx& ctx, double tol, int max_it, cudaStream_t st) {
-    k_bicg_init<T><<<lv.tiles, kTile, 0, st>>>(lv, b, x, r, shadow, p, v, ctx, tol, max_it);
+    PSGB_LAUNCH(kFamKrylovVector, st, k_bicg_init<T><<<lv.tiles, kTile, 0, st>>>(lv, b, x, r, shadow, p, v, ctx, tol, max_it));
 }
 template <typename T>
 void KrylovLaunch<T>::bicg_p(const LevelView<T>& lv, const T* r, const T* v, T* p, T* xv, T omega_j,
                              const InstanceScalars* sc, cudaStream_t st) {
-    k_bicg_p<T><<<lv.tiles, kTile, 0, st>>>(lv, r, v, p, xv, omega_j, sc);
+    PSGB_LAUNCH(kFamKrylovVector, st, k_bicg_p<T><<<lv.tiles, kTile, 0, st>>>(lv, r, v, p, xv, omega_j, sc));
 }
 template <typename T>
 void KrylovLaunch<T>::bicg_v(const LevelView<T>& lv, const T* in, T* out, const T* shadow,
                              const ReduceCtx& ctx, cudaStream_t st) {
-    PSGB_W(lv.width, (k_bicg_v<T, W><<<lv.tiles, kTile, 0, st>>>(lv, in, out, shadow, ctx)));
+    PSGB_LAUNCH(kFamKrylovSpmv, st, PSGB_W(lv.width, (k_bicg_v<T, W><<<lv.tiles, kTile, 0, st>>>(lv, in, out, shadow, ctx))));
 }
 template <typename T>
 void KrylovLaunch<T>::bicg_s(const LevelView<T>& lv, const T* r, const T* v, T* s, T* xv, T omega_j,
                              const ReduceCtx& ctx, cudaStream_t st) {
-    k_bicg_s<T><<<lv.tiles, kTile, 0, st>>>(lv, r, v, s, xv, omega_j, ctx);
+    PSGB_LAUNCH(kFamKrylovVector, st, k_bicg_s<T><<<lv.tiles, kTile, 0, st>>>(lv, r, v, s, xv, omega_j, ctx));
 }
 template <typename T>
 void KrylovLaunch<T>::bicg_t(const LevelView<T>& lv, const T* shat, T* t, const T* s,
                              const ReduceCtx& ctx, cudaStream_t st) {
-    PSGB_W(lv.width, (k_bicg_t<T, W><<<lv.tiles, kTile, 0, st>>>(lv, shat, t, s, ctx)));
+    PSGB_LAUNCH(kFamKrylovSpmv, st, PSGB_W(lv.width, (k_bicg_t<T, W><<<lv.tiles, kTile, 0, st>>>(lv, shat, t, s, ctx))));
 }
 template <typename T>
 void KrylovLaunch<T>::bicg_x(const LevelView<T>& lv, const T* phat, const T* shat, const T* s,
                              const T* t, T* x, T* r, const T* shadow, const ReduceCtx& ctx,
                              cudaStream_t st) {
-    k_bicg_x<T><<<lv.tiles, kTile, 0, st>>>(lv, phat, shat, s, t, x, r, shadow, ctx);
+    PSGB_LAUNCH(kFamKrylovVector, st, k_bicg_x<T><<<lv.tiles, kTile, 0, st>>>(lv, phat, shat, s, t, x, r, shadow, ctx));
 }
 template <typename T>
 void KrylovLaunch<T>::pcg_init(const LevelView<T>& lv, const T* b, T* x, T* r, T* p, T* xv, T omega_j,
                                const ReduceCtx& ctx, double tol, int max_it, cudaStream_t st) {
-    k_pcg_init<T><<<lv.tiles, kTile, 0, st>>>(lv, b, x, r, p, xv, omega_j, ctx, tol, max_it);
+    PSGB_LAUNCH(kFamKrylovVector, st, k_pcg_init<T><<<lv.tiles, kTile, 0, st>>>(lv, b, x, r, p, xv, omega_j, ctx, tol, max_it));
 }
 template <typename T>
 void KrylovLaunch<T>::pcg_rz(const LevelView<T>& lv, const T* r, const T* z, const ReduceCtx& ctx,
                              cudaStream_t st) {
-    k_pcg_rz<T><<<lv.tiles, kTile, 0, st>>>(lv, r, z, ctx);
+    PSGB_LAUNCH(kFamKrylovVector, st, k_pcg_rz<T><<<lv.tiles, kTile, 0, st>>>(lv, r, z, ctx));
 }
 template <typename T>
 void KrylovLaunch<T>::pcg_p(const LevelView<T>& lv, const T* z, T* p, const InstanceScalars* sc,
                             cudaStream_t st) {
-    k_pcg_p<T><<<lv.tiles, kTile, 0, st>>>(lv, z, p, sc);
+    PSGB_LAUNCH(kFamKrylovVector, st, k_pcg_p<T><<<lv.tiles, kTile, 0, st>>>(lv, z, p, sc));
 }
 template <typename T>
 void KrylovLaunch<T>::pcg_q(const LevelView<T>& lv, const T* p, T* q, const ReduceCtx& ctx,
                             cudaStream_t st) {
-    PSGB_W(lv.width, (k_pcg_q<T, W><<<lv.tiles, kTile, 0, st>>>(lv, p, q, ctx)));
+    PSGB_LAUNCH(kFamKrylovSpmv, st, PSGB_W(lv.width, (k_pcg_q<T, W><<<lv.tiles, kTile, 0, st>>>(lv, p, q, ctx))));
 }
 template <typename T>
 void KrylovLaunch<T>::pcg_xr(const LevelView<T>& lv, const T* p, const T* q, T* x, T* r, T* xv,
                              T omega_j, const ReduceCtx& ctx, cudaStream_t st) {
-    k_pcg_xr<T><<<lv.tiles, kTile, 0, st>>>(lv, p, q, x, r, xv, omega_j, ctx);
+    PSGB_LAUNCH(kFamKrylovVector, st, k_pcg_xr<T><<<lv.tiles, kTile, 0, st>>>(lv, p, q, x, r, xv, omega_j, ctx));
 }
 
 template struct KrylovLaunch<float>;
@@ -495,20 +496,20 @@ template struct KrylovLaunch<double>;
 
 void launch_outer_init(const LevelView<double>& lv, const double* b, const ReduceCtx& ctx, double tol,
                        int max_refine, cudaStream_t st) {
-    k_outer_init<<<lv.tiles, kTile, 0, st>>>(lv, b, ctx, tol, max_refine);
+    PSGB_LAUNCH(kFamRefine, st, k_outer_init<<<lv.tiles, kTile, 0, st>>>(lv, b, ctx, tol, max_refine));
 }
 
 template <typename TI>
 void launch_outer_residual(const LevelView<double>& lv, const double* b, const double* x, double* r64,
                            TI* rin, const ReduceCtx& ctx, int max_refine, cudaStream_t st) {
-    PSGB_W(lv.width, (k_outer_residual<TI, W><<<lv.tiles, kTile, 0, st>>>(lv, b, x, r64, rin, ctx, max_refine)));
+    PSGB_LAUNCH(kFamRefine, st, PSGB_W(lv.width, (k_outer_residual<TI, W><<<lv.tiles, kTile, 0, st>>>(lv, b, x, r64, rin, ctx, max_refine))));
 }
 
 template <typename TI>
 void launch_outer_update(const LevelView<double>& lv, const TI* delta, double* x, InstanceScalars* sc,
                          std::uint32_t instances, cudaStream_t st) {
-    k_outer_account<<<(instances + 127) / 128, 128, 0, st>>>(sc, instances);
-    k_outer_update<TI><<<lv.tiles, kTile, 0, st>>>(lv, delta, x, sc);
+    PSGB_LAUNCH(kFamRefine, st, k_outer_account<<<(instances + 127) / 128, 128, 0, st>>>(sc, instances));
+    PSGB_LAUNCH(kFamRefine, st, k_outer_update<TI><<<lv.tiles, kTile, 0, st>>>(lv, delta, x, sc));
 }
 
 template void launch_outer_residual<float>(const LevelView<double>&, const double*, const double*, double*,

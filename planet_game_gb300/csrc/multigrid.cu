@@ -10,6 +10,7 @@
 // row, 256-row tiles, neighbour gathers served mostly from L2 thanks to the
 // reference's space-filling cell order. No tensor cores (sparse stencils).
 #include "common.cuh"
+#include "profile.hpp"
 #include "kernels.hpp"
 
 #include <stdexcept>
@@ -175,11 +176,20 @@ __global__ void __launch_bounds__(1024) k_dense_invert(DenseView dense, int leve
 
 // ---- V-cycle pieces ----------------------------------------------------------
 
+// Algorithmic bytes moved by the Jacobi sweeps (one atomic per active tile), read by the
+// profiler: a sweep row reads its W columns and values, 1/diag, b and x and writes y;
+// the zero-start sweep reads 1/diag and b and writes x. Neighbour gathers of x are
+// not counted again.
+__device__ unsigned long long g_swept_bytes;
+
 template <typename T>
 __global__ void k_smooth_zero(LevelView<T> lv, const T* __restrict__ b, T* __restrict__ x, T omega,
                               const InstanceScalars* sc, int gate) {
     const int row = owned_row(lv, sc, gate, true);
     if (row < 0) return;
+    if (threadIdx.x == 0) {
+        atomicAdd(&g_swept_bytes, static_cast<unsigned long long>(lv.tile_rows[blockIdx.x]) * 3ull * sizeof(T));
+    }
     x[row] = omega * lv.inv[row] * b[row];
 }
 
@@ -188,6 +198,10 @@ __global__ void k_smooth(LevelView<T> lv, const T* __restrict__ b, const T* __re
                          T* __restrict__ y, T omega, const InstanceScalars* sc, int gate) {
     const int row = owned_row(lv, sc, gate, true);
     if (row < 0) return;
+    if (threadIdx.x == 0) {
+        atomicAdd(&g_swept_bytes, static_cast<unsigned long long>(lv.tile_rows[blockIdx.x]) *
+                                      (4ull * W + sizeof(T) * (W + 4ull)));
+    }
     const std::uint32_t P = lv.rows;
     T s = b[row];
 #pragma unroll
@@ -267,34 +281,41 @@ inline dim3 tiles_grid(std::uint32_t tiles) { return dim3(tiles); }
 
 }  // namespace
 
+std::uint64_t swept_bytes_exchange() {
+    unsigned long long v = 0, zero = 0;
+    cudaMemcpyFromSymbol(&v, g_swept_bytes, sizeof(v));
+    cudaMemcpyToSymbol(g_swept_bytes, &zero, sizeof(zero));
+    return v;
+}
+
 // ---- launchers -----------------------------------------------------------------
 
 void launch_assemble_transport(const LevelView<double>& fine, const double* w, const double* wsum,
                                const double* area, const double* slope, const double* conductance,
                                const double* edge_conductance, double* vd, cudaStream_t stream) {
-    k_assemble_transport<<<fine.tiles, kTile, 0, stream>>>(fine, w, wsum, area, slope, conductance,
-                                                          edge_conductance, vd);
+    PSGB_LAUNCH(kFamSetup, stream, k_assemble_transport<<<fine.tiles, kTile, 0, stream>>>(fine, w, wsum, area, slope, conductance,
+                                                          edge_conductance, vd));
 }
 
 void launch_set_matrix_csr(std::uint32_t n, std::uint32_t rows, std::uint32_t width,
                            const std::uint32_t* csr_offset, const double* diag, const double* off,
                            double* vd, cudaStream_t stream) {
-    k_set_matrix_csr<<<(rows + 255) / 256, 256, 0, stream>>>(n, rows, width, csr_offset, diag, off, vd);
+    PSGB_LAUNCH(kFamSetup, stream, k_set_matrix_csr<<<(rows + 255) / 256, 256, 0, stream>>>(n, rows, width, csr_offset, diag, off, vd));
 }
 
 void launch_galerkin(std::uint32_t lists, const std::uint32_t* offset, const std::uint32_t* source,
                      const double* fine_vd, double* coarse_vd, cudaStream_t stream) {
-    k_galerkin<<<(lists + 255) / 256, 256, 0, stream>>>(lists, offset, source, fine_vd, coarse_vd);
+    PSGB_LAUNCH(kFamSetup, stream, k_galerkin<<<(lists + 255) / 256, 256, 0, stream>>>(lists, offset, source, fine_vd, coarse_vd));
 }
 
 void launch_finalize_level(std::uint32_t rows, std::uint32_t width, double* vd64, float* vd32,
                            double* inv64, float* inv32, cudaStream_t stream) {
-    k_finalize_level<<<(rows + 255) / 256, 256, 0, stream>>>(rows, width, vd64, vd32, inv64, inv32);
+    PSGB_LAUNCH(kFamSetup, stream, k_finalize_level<<<(rows + 255) / 256, 256, 0, stream>>>(rows, width, vd64, vd32, inv64, inv32));
 }
 
 void launch_dense_invert(const DenseView& dense, int level, const LevelView<double>& lv,
                          double* work, double* inv64, float* inv32, cudaStream_t stream) {
-    k_dense_invert<<<dense.instances, 1024, 0, stream>>>(dense, level, lv, work, inv64, inv32);
+    PSGB_LAUNCH(kFamSetup, stream, k_dense_invert<<<dense.instances, 1024, 0, stream>>>(dense, level, lv, work, inv64, inv32));
 }
 
 #define PSGB_WIDTH_DISPATCH(width, KERNEL, ...)                                 \
@@ -309,44 +330,44 @@ void launch_dense_invert(const DenseView& dense, int level, const LevelView<doub
 template <typename T>
 void launch_smooth_zero(const LevelView<T>& lv, const T* b, T* x, T omega, const InstanceScalars* sc,
                         int gate, cudaStream_t stream) {
-    k_smooth_zero<T><<<lv.tiles, kTile, 0, stream>>>(lv, b, x, omega, sc, gate);
+    PSGB_LAUNCH(kFamSmooth, stream, k_smooth_zero<T><<<lv.tiles, kTile, 0, stream>>>(lv, b, x, omega, sc, gate));
 }
 
 template <typename T>
 void launch_smooth(const LevelView<T>& lv, const T* b, const T* x, T* y, T omega,
                    const InstanceScalars* sc, int gate, cudaStream_t stream) {
-    PSGB_WIDTH_DISPATCH(lv.width, k_smooth, lv, b, x, y, omega, sc, gate);
+    PSGB_LAUNCH(kFamSmooth, stream, PSGB_WIDTH_DISPATCH(lv.width, k_smooth, lv, b, x, y, omega, sc, gate));
 }
 
 template <typename T>
 void launch_residual(const LevelView<T>& lv, const T* b, const T* x, T* r, const InstanceScalars* sc,
                      int gate, cudaStream_t stream) {
-    PSGB_WIDTH_DISPATCH(lv.width, k_residual, lv, b, x, r, sc, gate);
+    PSGB_LAUNCH(kFamResidual, stream, PSGB_WIDTH_DISPATCH(lv.width, k_residual, lv, b, x, r, sc, gate));
 }
 
 template <typename T>
 void launch_spmv(const LevelView<T>& lv, const T* x, T* y, cudaStream_t stream) {
-    PSGB_WIDTH_DISPATCH(lv.width, k_spmv, lv, x, y);
+    PSGB_LAUNCH(kFamKrylovSpmv, stream, PSGB_WIDTH_DISPATCH(lv.width, k_spmv, lv, x, y));
 }
 
 template <typename T>
 void launch_restrict(const LevelView<T>& coarse, const std::uint32_t* member_offset,
                      const std::uint32_t* member, const T* r, T* bc, const InstanceScalars* sc,
                      int gate, cudaStream_t stream) {
-    k_restrict<T><<<coarse.tiles, kTile, 0, stream>>>(coarse, member_offset, member, r, bc, sc, gate);
+    PSGB_LAUNCH(kFamRestrict, stream, k_restrict<T><<<coarse.tiles, kTile, 0, stream>>>(coarse, member_offset, member, r, bc, sc, gate));
 }
 
 template <typename T>
 void launch_prolong(const LevelView<T>& fine, const std::int32_t* agg, const T* xc, T* x,
                     const InstanceScalars* sc, int gate, cudaStream_t stream) {
-    k_prolong<T><<<fine.tiles, kTile, 0, stream>>>(fine, agg, xc, x, sc, gate);
+    PSGB_LAUNCH(kFamProlong, stream, k_prolong<T><<<fine.tiles, kTile, 0, stream>>>(fine, agg, xc, x, sc, gate));
 }
 
 template <typename T>
 void launch_dense_solve(const DenseView& dense, int level, std::uint32_t max_rows, const T* inv,
                         const T* b, T* x, const InstanceScalars* sc, int gate, cudaStream_t stream) {
     const dim3 grid((max_rows * 32 + 255) / 256, dense.instances);
-    k_dense_solve<T><<<grid, 256, 0, stream>>>(dense, level, inv, b, x, sc, gate);
+    PSGB_LAUNCH(kFamDense, stream, k_dense_solve<T><<<grid, 256, 0, stream>>>(dense, level, inv, b, x, sc, gate));
 }
 
 #define PSGB_INSTANTIATE(T)                                                                           \

@@ -12,6 +12,7 @@
 // fused multiply-adds, so diffusion_source and gradient are bit-identical to the
 // reference and the Laplacian differs only by using the precomputed l/d weight.
 #include "common.cuh"
+#include "profile.hpp"
 #include "operators.hpp"
 
 namespace psgb {
@@ -193,26 +194,26 @@ __global__ void k_mask_rhs(std::size_t n, const double* __restrict__ slope, doub
 }  // namespace
 
 void launch_mask_rhs(std::size_t n, const double* slope, double* rhs, cudaStream_t st) {
-    k_mask_rhs<<<static_cast<unsigned>((n + 255) / 256), 256, 0, st>>>(n, slope, rhs);
+    PSGB_LAUNCH(kFamStep, st, k_mask_rhs<<<static_cast<unsigned>((n + 255) / 256), 256, 0, st>>>(n, slope, rhs));
 }
 
 template <typename T>
 void launch_laplacian(const DevMesh& m, const T* in, T* out, cudaStream_t st) {
-    k_laplacian<T><<<(m.n + 255) / 256, 256, 0, st>>>(m.n, m.p, m.nbr, m.w, m.area, in, out);
+    PSGB_LAUNCH(kFamOperator, st, k_laplacian<T><<<(m.n + 255) / 256, 256, 0, st>>>(m.n, m.p, m.nbr, m.w, m.area, in, out));
 }
 template <typename T>
 void launch_gradient(const DevMesh& m, const T* in, T* east, T* north, cudaStream_t st) {
-    k_gradient<T><<<(m.n + 255) / 256, 256, 0, st>>>(m.n, m.p, m.nbr, m.degree, m.dist, m.ne, m.nn, m.gm,
-                                                     in, east, north);
+    PSGB_LAUNCH(kFamOperator, st, k_gradient<T><<<(m.n + 255) / 256, 256, 0, st>>>(m.n, m.p, m.nbr, m.degree, m.dist, m.ne, m.nn, m.gm,
+                                                     in, east, north));
 }
 template <typename T>
 void launch_divergence(const DevMesh& m, const T* flux, T* out, cudaStream_t st) {
-    k_divergence<T><<<(m.n + 255) / 256, 256, 0, st>>>(m.n, m.p, m.edge, m.first, m.degree, m.edge_length,
-                                                       m.area, flux, out);
+    PSGB_LAUNCH(kFamOperator, st, k_divergence<T><<<(m.n + 255) / 256, 256, 0, st>>>(m.n, m.p, m.edge, m.first, m.degree, m.edge_length,
+                                                       m.area, flux, out));
 }
 void launch_diffusion_source(const DevMesh& m, double conductance, const double* t, double* out,
                              cudaStream_t st) {
-    k_diffusion_source<<<(m.n + 255) / 256, 256, 0, st>>>(m.n, m.p, m.nbr, m.w, m.area, conductance, t, out);
+    PSGB_LAUNCH(kFamOperator, st, k_diffusion_source<<<(m.n + 255) / 256, 256, 0, st>>>(m.n, m.p, m.nbr, m.w, m.area, conductance, t, out));
 }
 
 template void launch_laplacian<float>(const DevMesh&, const float*, float*, cudaStream_t);
@@ -224,16 +225,16 @@ template void launch_divergence<double>(const DevMesh&, const double*, double*, 
 
 void launch_step_rhs(const StepView& v, const double* t0, const double* src, double* rhs, double* slope,
                      double* x0, cudaStream_t st) {
-    k_step_rhs<<<v.tiles, kTile, 0, st>>>(v.rows, v.tile_inst, v.tile_rows, v.area, v.slope_of, t0, src,
-                                          rhs, slope, x0);
+    PSGB_LAUNCH(kFamStep, st, k_step_rhs<<<v.tiles, kTile, 0, st>>>(v.rows, v.tile_inst, v.tile_rows, v.area, v.slope_of, t0, src,
+                                          rhs, slope, x0));
 }
 
 void launch_step_finish(const StepView& v, const double* t, const double* t0, const double* src,
                         double* h, double* t_new, double* partial, double* sums, cudaStream_t st) {
-    k_step_finish<<<v.tiles, kTile, 0, st>>>(v.rows, v.tile_inst, v.tile_rows, v.nbr, v.w, v.area,
+    PSGB_LAUNCH(kFamStep, st, k_step_finish<<<v.tiles, kTile, 0, st>>>(v.rows, v.tile_inst, v.tile_rows, v.nbr, v.w, v.area,
                                              v.conductance, v.edge_conductance, v.slope_of, t, t0, src, h,
-                                             t_new, partial);
-    k_sum_tiles<<<v.instances, 32, 0, st>>>(v.instances, v.tile_begin, partial, 6, sums);
+                                             t_new, partial));
+    PSGB_LAUNCH(kFamStep, st, k_sum_tiles<<<v.instances, 32, 0, st>>>(v.instances, v.tile_begin, partial, 6, sums));
 }
 
 }  // namespace psgb

@@ -1,0 +1,96 @@
+// Launch accounting and opt-in per-kernel timing (see profile.hpp).
+#include "profile.hpp"
+
+#include <atomic>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+namespace psgb {
+namespace {
+
+std::atomic<std::uint64_t> g_launches[kFamCount];
+
+struct Profile {
+    std::mutex mu;
+    int family = -1;
+    std::vector<cudaEvent_t> start, stop;
+    std::size_t used = 0;
+    std::uint64_t launches = 0;
+    bool pending = false;
+} g_profile;
+
+constexpr std::size_t kMaxEvents = 1 << 16;
+
+const char* const kNames[kFamCount] = {"smooth", "residual", "restrict", "prolong", "dense", "krylov_spmv",
+                                       "krylov_vector", "refine", "setup", "step", "operator", "column"};
+
+}  // namespace
+
+const char* family_name(int family) { return family >= 0 && family < kFamCount ? kNames[family] : "?"; }
+
+int family_of(const char* name) {
+    for (int f = 0; f < kFamCount; ++f)
+        if (name != nullptr && std::strcmp(name, kNames[f]) == 0) return f;
+    return -1;
+}
+
+void launch_begin(int family, cudaStream_t st) {
+    g_launches[family].fetch_add(1, std::memory_order_relaxed);
+    if (g_profile.family != family) return;
+    std::lock_guard<std::mutex> lock(g_profile.mu);
+    if (g_profile.family != family || g_profile.used >= kMaxEvents) return;
+    if (g_profile.used == g_profile.start.size()) {
+        cudaEvent_t a, b;
+        if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) return;
+        g_profile.start.push_back(a);
+        g_profile.stop.push_back(b);
+    }
+    cudaEventRecord(g_profile.start[g_profile.used], st);
+    g_profile.pending = true;
+}
+
+void launch_end(int family, cudaStream_t st) {
+    if (g_profile.family != family) return;
+    std::lock_guard<std::mutex> lock(g_profile.mu);
+    if (!g_profile.pending) return;
+    cudaEventRecord(g_profile.stop[g_profile.used], st);
+    ++g_profile.used;
+    ++g_profile.launches;
+    g_profile.pending = false;
+}
+
+std::uint64_t launches_total() {
+    std::uint64_t s = 0;
+    for (auto& c : g_launches) s += c.load(std::memory_order_relaxed);
+    return s;
+}
+
+std::uint64_t launches_of(int family) { return g_launches[family].load(std::memory_order_relaxed); }
+
+bool profile_begin(int family) {
+    if (family < 0 || family >= kFamCount) return false;
+    std::lock_guard<std::mutex> lock(g_profile.mu);
+    g_profile.family = family;
+    g_profile.used = 0;
+    g_profile.launches = 0;
+    g_profile.pending = false;
+    return true;
+}
+
+bool profile_end(double* total_ms, std::uint64_t* launches) {
+    std::lock_guard<std::mutex> lock(g_profile.mu);
+    if (g_profile.family < 0) return false;
+    double sum = 0.0;
+    for (std::size_t i = 0; i < g_profile.used; ++i) {
+        cudaEventSynchronize(g_profile.stop[i]);
+        float ms = 0.0F;
+        if (cudaEventElapsedTime(&ms, g_profile.start[i], g_profile.stop[i]) == cudaSuccess) sum += ms;
+    }
+    *total_ms = sum;
+    *launches = g_profile.launches;
+    g_profile.family = -1;
+    return true;
+}
+
+}  // namespace psgb

@@ -1,0 +1,51 @@
+// Launch accounting and opt-in per-kernel timing.
+//
+// Every launcher calls launch_begin/launch_end around its kernel: launches are counted
+// per kernel family, and while a profile is active for one family, a CUDA event pair is
+// recorded on the launching stream around each of its launches. The host reads the
+// summed device time after synchronising (psgb_profile_end in the C-ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace psgb {
+
+enum KernelFamily : int {
+    kFamSmooth = 0,      // Jacobi sweeps (k_smooth, k_smooth_zero)
+    kFamResidual,        // V-cycle residual
+    kFamRestrict,        // restriction
+    kFamProlong,         // prolongation
+    kFamDense,           // coarsest dense solve
+    kFamKrylovSpmv,      // Krylov products with fused dots (bicg_v, bicg_t, pcg_q)
+    kFamKrylovVector,    // Krylov vector updates with fused dots
+    kFamRefine,          // FP64 refinement residual / update
+    kFamSetup,           // assembly, Galerkin, dense inverse, level finalisation
+    kFamStep,            // transport-step right-hand side and flux form
+    kFamOperator,        // finite-volume operators
+    kFamColumn,          // column radiation
+    kFamCount
+};
+
+const char* family_name(int family);
+int family_of(const char* name);
+
+void launch_begin(int family, cudaStream_t st);
+void launch_end(int family, cudaStream_t st);
+
+std::uint64_t launches_total();
+std::uint64_t launches_of(int family);
+
+bool profile_begin(int family);
+// Synchronises the recorded events; returns false if no profile was active.
+bool profile_end(double* total_ms, std::uint64_t* launches);
+
+}  // namespace psgb
+
+#define PSGB_LAUNCH(family, stream, ...)           \
+    do {                                           \
+        ::psgb::launch_begin((family), (stream));  \
+        __VA_ARGS__;                               \
+        ::psgb::launch_end((family), (stream));    \
+    } while (0)

@@ -1,0 +1,250 @@
+"""Writes the golden fixtures of tests/golden/ from the REFERENCE's own code.
+
+The reference PlanetSim sources are compiled where they lie (oracle/Makefile.ref, into
+oracle/_ref/) and driven through oracle/ref_driver.cpp. Every number saved here is
+computed by the reference's functions; the inputs are seeded numpy draws saved with
+them. Run in a container that has the reference checkout:
+
+    python tests/golden/make_golden.py /path/to/planet_game
+
+The fixtures are small (.npz / .json); the GPU machine never needs the reference.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import hashlib
+import json
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+DRIVER = ROOT / "oracle" / "_ref" / "libref_driver.so"
+RADIUS = 6.371e6
+P = C.c_void_p
+
+
+def p(a):
+    return a.ctypes.data_as(P)
+
+
+def P_(handle):
+    return handle if isinstance(handle, P) else P(handle)
+
+
+def load(reference: Path) -> C.CDLL:
+    subprocess.run(["make", "-s", "-f", str(ROOT / "oracle" / "Makefile.ref"), f"REF={reference}",
+                    f"OUT={ROOT / 'oracle' / '_ref'}", "-j8", "-C", str(ROOT)], check=True)
+    R = C.CDLL(str(DRIVER))
+    R.refd_mesh_new.restype = P
+    R.refd_mesh_new.argtypes = [C.c_uint32, C.c_double]
+    R.refd_mesh_free.argtypes = [P]
+    R.refd_hierarchy_new.restype = P
+    R.refd_hierarchy_new.argtypes = [P]
+    R.refd_hierarchy_free.argtypes = [P]
+    R.refd_hierarchy_level_count.restype = C.c_uint64
+    R.refd_hierarchy_level_count.argtypes = [P]
+    R.refd_pcg.restype = C.c_int
+    R.refd_pcg.argtypes = [P, C.c_double, P, P, C.c_double, C.c_int, C.c_uint64, P]
+    R.refd_solve_linear.argtypes = [P, C.c_double, P, P, C.c_double, C.c_double, C.c_uint64, P, P, P]
+    R.refd_diffusion_source.argtypes = [P, C.c_double, P, P]
+    R.refd_saturation_specific_humidity.restype = C.c_double
+    R.refd_saturation_specific_humidity.argtypes = [C.c_double, C.c_double]
+    R.refd_surface_gravity_earth.restype = C.c_double
+    R.refd_column_radiation.restype = C.c_int
+    R.refd_column_radiation.argtypes = [C.c_uint32, P, P, P, C.c_double, C.c_double, C.c_double, P, P, P, P, P, P]
+    R.refd_insolation.argtypes = [P, C.c_int64, P]
+    R.refd_insolation_nodes.argtypes = [C.c_int64, P]
+    return R
+
+
+def mesh_arrays(R, m) -> dict:
+    cnt = np.zeros(4, np.uint64)
+    R.refd_mesh_counts(P_(m), p(cnt))
+    n, e, d, k = (int(x) for x in cnt)
+    a = dict(center=np.zeros((n, 3)), east=np.zeros((n, 3)), north=np.zeros((n, 3)), area_m2=np.zeros(n),
+             source_vertex=np.zeros(n, np.uint32), edge_offset=np.zeros(n, np.uint32), edge_count=np.zeros(n, np.uint8),
+             neighbor=np.zeros(d, np.uint32), edge=np.zeros(d, np.uint32), normal_east=np.zeros(d, np.float32),
+             normal_north=np.zeros(d, np.float32), edge_first=np.zeros(e, np.uint32), edge_second=np.zeros(e, np.uint32),
+             edge_length_m=np.zeros(e), edge_distance_m=np.zeros(e), corner_unit=np.zeros((k, 3)),
+             corner=np.zeros(d, np.uint32))
+    R.refd_mesh_cells(P_(m), *[p(a[x]) for x in ("center", "east", "north", "area_m2", "source_vertex", "edge_offset",
+                                                 "edge_count")])
+    R.refd_mesh_cell_edges(P_(m), *[p(a[x]) for x in ("neighbor", "edge", "normal_east", "normal_north")])
+    R.refd_mesh_edges(P_(m), *[p(a[x]) for x in ("edge_first", "edge_second", "edge_length_m", "edge_distance_m")])
+    R.refd_mesh_corners(P_(m), p(a["corner_unit"]), p(a["corner"]))
+    off = np.zeros(n + 1, np.uint64)
+    nb = np.zeros(d, np.uint64)
+    a["graph_weight"] = np.zeros(d)
+    a["graph_weight_sum"] = np.zeros(n)
+    area = np.zeros(n)
+    R.refd_graph(P_(m), p(area), p(off), p(nb), p(a["graph_weight"]), p(a["graph_weight_sum"]))
+    return a
+
+
+def sha(arr: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(arr).tobytes()).hexdigest()
+
+
+def hierarchy(R, m) -> list[dict]:
+    h = P(R.refd_hierarchy_new(P_(m)))
+    out = []
+    for i in range(int(R.refd_hierarchy_level_count(h))):
+        s = np.zeros(4, np.uint64)
+        R.refd_hierarchy_level_sizes(h, C.c_uint64(i), p(s))
+        rows, nnz, na, nt = (int(x) for x in s)
+        off, col = np.zeros(rows + 1, np.int64), np.zeros(nnz, np.int64)
+        agg, tgt = np.zeros(max(na, 1), np.int64), np.zeros(max(nt, 1), np.int64)
+        dg, val = np.zeros(rows), np.zeros(nnz)
+        R.refd_hierarchy_level(h, C.c_uint64(i), p(off), p(col), p(agg), p(tgt), p(dg), p(val))
+        out.append(dict(offset=off.astype(np.uint32), column=col.astype(np.uint32), aggregate=agg[:na].astype(np.uint32),
+                        target=tgt[:nt]))
+    R.refd_hierarchy_free(h)
+    return out
+
+
+def main(reference: Path) -> None:
+    R = load(reference)
+    rng = np.random.default_rng(20261203)
+    meta = {"radius_m": RADIUS, "mesh_sha256": {}, "hierarchy_sha256": {}}
+
+    # ---- meshes: full arrays at L0-L2, hashes up to L8 --------------------------------
+    for level in range(0, 9):
+        m = R.refd_mesh_new(level, RADIUS)
+        a = mesh_arrays(R, m)
+        meta["mesh_sha256"][str(level)] = {k: sha(v) for k, v in a.items()}
+        if level <= 2:
+            np.savez_compressed(HERE / f"mesh_L{level}.npz", **a)
+        if level >= 3:
+            hl = hierarchy(R, m)
+            meta["hierarchy_sha256"][str(level)] = [{k: sha(v) for k, v in lv.items()} | {"rows": int(len(lv["offset"]) - 1)}
+                                                    for lv in hl]
+        R.refd_mesh_free(P_(m))
+        print("mesh", level, flush=True)
+
+    # ---- operators at L4 (finite_volume.cpp) ------------------------------------------
+    m = P(R.refd_mesh_new(4, RADIUS))
+    a = mesh_arrays(R, m)
+    n, e = len(a["area_m2"]), len(a["edge_length_m"])
+    x64 = rng.standard_normal(n)
+    f64 = rng.standard_normal(e)
+    x32 = rng.standard_normal(n).astype(np.float32)
+    f32 = rng.standard_normal(e).astype(np.float32)
+    out = {"x64": x64, "flux64": f64, "x32": x32, "flux32": f32}
+    for name, xin, dt in (("64", x64, np.float64), ("32", x32, np.float32)):
+        lap, ge, gn = np.empty(n, dt), np.empty(n, dt), np.empty(n, dt)
+        getattr(R, f"refd_laplacian_f{name}")(m, p(xin), p(lap))
+        getattr(R, f"refd_gradient_f{name}")(m, p(xin), p(ge), p(gn))
+        div = np.empty(n, dt)
+        getattr(R, f"refd_divergence_f{name}")(m, p(f64 if name == "64" else f32), p(div))
+        out.update({f"laplacian{name}": lap, f"east{name}": ge, f"north{name}": gn, f"divergence{name}": div})
+    t = 288.0 + rng.normal(0, 10, n)
+    ds = np.empty(n)
+    R.refd_diffusion_source(m, 4e13, p(t), p(ds))
+    out.update({"temperature": t, "diffusion_source": ds, "conductance": 4e13})
+    np.savez_compressed(HERE / "operators_L4.npz", **out)
+
+    # ---- Newton driver with a linear response at L4 (test_heat_transport.cpp:80-107 style)
+    base = 250.0 + 50.0 * rng.random(n)
+    slope = np.where(np.arange(n) % 5 == 0, 0.0, 0.01 + 0.2 * rng.random(n))
+    K = 0.5 * RADIUS * RADIUS
+    mean, src, stats = np.empty(n), np.empty(n), np.empty(6)
+    R.refd_solve_linear(m, K, p(base), p(slope), 1e-6, 1e-6, 4, p(mean), p(src), p(stats))
+    np.savez_compressed(HERE / "newton_L4.npz", base=base, slope=slope, conductance=K, cg_tolerance=1e-6,
+                        newton_tolerance=1e-6, mean=mean, source=src, stats=stats)
+
+    # insolation at L4 (substep_forcing.cpp) and its nodes
+    ins = np.empty(n, np.float32)
+    R.refd_insolation(m, 0, p(ins))
+    nodes = np.empty(80)
+    R.refd_insolation_nodes(0, p(nodes))
+    np.savez_compressed(HERE / "insolation_L4.npz", insolation=ins, nodes=nodes.reshape(16, 5))
+    R.refd_mesh_free(m)
+
+    # ---- multigrid + PCG at L5 with the heat-step matrix ---------------------------------
+    m = P(R.refd_mesh_new(5, RADIUS))
+    a = mesh_arrays(R, m)
+    n = len(a["area_m2"])
+    C_heat, kappa, dt = 4e7, 1e6, 31_556_925.216 / 12.0
+    K = C_heat * kappa
+    s = np.full(n, dt / C_heat)
+    lat = np.arcsin(a["center"][:, 2])
+    t0 = 288.0 - 40.0 * np.sin(lat) ** 2 + rng.normal(0, 0.5, n)
+    ins = np.empty(n, np.float32)
+    R.refd_insolation(m, 0, p(ins))
+    S = 0.7 * ins.astype(np.float64) - (203.3 + 2.09 * (t0 - 273.15))
+    rhs = a["area_m2"] / s * t0 + a["area_m2"] * S
+    diag = a["area_m2"] / s + K * a["graph_weight_sum"]
+    off = -K * a["graph_weight"]
+    h = P(R.refd_hierarchy_new(m))
+    R.refd_hierarchy_set_matrix(h, p(diag), p(off))
+    galerkin = {}
+    for i in range(int(R.refd_hierarchy_level_count(h))):
+        sz = np.zeros(4, np.uint64)
+        R.refd_hierarchy_level_sizes(h, C.c_uint64(i), p(sz))
+        rows, nnz, na, nt = (int(x) for x in sz)
+        o, c = np.zeros(rows + 1, np.int64), np.zeros(nnz, np.int64)
+        ag, tg = np.zeros(max(na, 1), np.int64), np.zeros(max(nt, 1), np.int64)
+        dg, vl = np.zeros(rows), np.zeros(nnz)
+        R.refd_hierarchy_level(h, C.c_uint64(i), p(o), p(c), p(ag), p(tg), p(dg), p(vl))
+        galerkin[f"diag{i}"] = dg
+        galerkin[f"off{i}"] = vl
+    vrhs = rng.standard_normal(n) * 1e12
+    vout = np.empty(n)
+    R.refd_hierarchy_vcycle(h, m, p(vrhs), p(vout))
+    R.refd_hierarchy_free(h)
+    x = np.empty(n)
+    it = R.refd_pcg(m, K, p(s), p(rhs), 1e-12, 2000, 1, p(x))
+    np.savez_compressed(HERE / "heatstep_L5.npz", t0=t0, source=S, insolation=ins, heat_capacity=C_heat,
+                        diffusivity=kappa, dt=dt, rhs=rhs, vcycle_rhs=vrhs, vcycle_out=vout, pcg_x=x,
+                        pcg_iterations=it, pcg_tolerance=1e-12, **galerkin)
+    R.refd_mesh_free(m)
+
+    # ---- column radiation at N = 4 and N = 8 (the reference's maximum) -------------------
+    g = R.refd_surface_gravity_earth()
+    consts = np.zeros(6)
+    R.refd_earth_like_constants(p(consts))
+    cols = 256
+    col_out = {"gravity": g, "constants": consts}
+    for N in (4, 8):
+        ps = 1e5 + rng.normal(0, 1500, cols)
+        ts = 250.0 + 60.0 * rng.random(cols)
+        sigma = 1.0 - (np.arange(N) + 0.5) / N
+        temp = ts[None, :] * sigma[:, None] ** (287.04 * 6.5e-3 / g)
+        q = np.empty((N, cols))
+        for k in range(N):
+            for c in range(cols):
+                q[k, c] = 0.8 * R.refd_saturation_specific_humidity(temp[k, c], sigma[k] * ps[c])
+        frac = rng.random((N, cols))
+        frac[:, ::7] = 0.0                   # clear layers
+        frac[0, 3::11] = 1.5                 # overcast (f capped at 1)
+        ql = frac * consts[2] / (ps[None, :] / (g * N))
+        eps, absb, fr, refl = (np.empty((N, cols)) for _ in range(4))
+        sc = np.empty((5, cols))
+        for c in range(cols):
+            e1, a1, f1, r1, s1 = np.empty(N), np.empty(N), np.empty(N), np.empty(N), np.empty(5)
+            rc = R.refd_column_radiation(N, p(np.ascontiguousarray(temp[:, c])), p(np.ascontiguousarray(q[:, c])),
+                                         p(np.ascontiguousarray(ql[:, c])), float(ts[c]), float(ps[c]), g, p(consts),
+                                         p(e1), p(a1), p(f1), p(r1), p(s1))
+            assert rc == 0
+            eps[:, c], absb[:, c], fr[:, c], refl[:, c], sc[:, c] = e1, a1, f1, r1, s1
+        col_out.update({f"temperature{N}": temp, f"humidity{N}": q, f"cloud_water{N}": ql, f"surface_temperature{N}": ts,
+                        f"surface_pressure{N}": ps, f"emissivity{N}": eps, f"absorbed{N}": absb, f"fraction{N}": fr,
+                        f"reflectance{N}": refl, f"scalars{N}": sc})
+    np.savez_compressed(HERE / "column.npz", **col_out)
+
+    # ---- saturation (saturation.cpp) ------------------------------------------------------
+    T = np.linspace(180.0, 320.0, 57)
+    Pp = np.array([5e3, 2e4, 5e4, 8e4, 1e5])
+    qs = np.array([[R.refd_saturation_specific_humidity(tt, pp) for pp in Pp] for tt in T])
+    np.savez_compressed(HERE / "saturation.npz", temperature=T, pressure=Pp, qsat=qs)
+
+    (HERE / "golden.json").write_text(json.dumps(meta, indent=1, sort_keys=True))
+    print("golden fixtures written")
+
+
+if __name__ == "__main__":
+    main(Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))

@@ -1,0 +1,113 @@
+"""The CPU oracle (oracle/planetsim_oracle.cpp) pinned against the reference's own
+outputs (golden vectors written by tests/golden/make_golden.py from the reference
+sources). Operators, diffusion source, Galerkin values, the SGS V-cycle, PCG and the
+Newton driver are bit-identical; column radiation agrees to the last ulps of libm."""
+import numpy as np
+import pytest
+
+from conftest import golden
+from oracle import oracle as O
+
+
+@pytest.fixture(scope="module")
+def L4(meshes):
+    return O.OracleMesh(meshes(4).arrays())
+
+
+@pytest.fixture(scope="module")
+def L5(meshes):
+    return O.OracleMesh(meshes(5).arrays())
+
+
+def test_operators_f64_bit_identical(L4):
+    g = golden("operators_L4.npz")
+    assert np.array_equal(L4.laplacian(g["x64"]), g["laplacian64"])
+    e, n = L4.gradient(g["x64"])
+    assert np.array_equal(e, g["east64"]) and np.array_equal(n, g["north64"])
+    assert np.array_equal(L4.divergence(g["flux64"]), g["divergence64"])
+    assert np.array_equal(L4.diffusion_source(float(g["conductance"]), g["temperature"]), g["diffusion_source"])
+
+
+def test_operators_f32_bit_identical(L4):
+    g = golden("operators_L4.npz")
+    assert np.array_equal(L4.laplacian(g["x32"]), g["laplacian32"])
+    e, n = L4.gradient(g["x32"])
+    assert np.array_equal(e, g["east32"]) and np.array_equal(n, g["north32"])
+    assert np.array_equal(L4.divergence(g["flux32"]), g["divergence32"])
+
+
+def test_galerkin_values_and_vcycle_bit_identical(L5):
+    g = golden("heatstep_L5.npz")
+    a = L5.a
+    s = float(g["dt"]) / float(g["heat_capacity"])
+    K = float(g["heat_capacity"]) * float(g["diffusivity"])
+    h = O.OracleHierarchy(L5)
+    h.set_matrix(a["area_m2"] / s + K * a["graph_weight_sum"], -K * a["graph_weight"])
+    for lvl in range(h.levels()):
+        d, o = h.values(lvl)
+        assert np.array_equal(d, g[f"diag{lvl}"]), lvl
+        assert np.array_equal(o, g[f"off{lvl}"]), lvl
+    assert np.array_equal(h.vcycle_sgs(g["vcycle_rhs"]), g["vcycle_out"])
+
+
+def test_pcg_bit_identical(L5):
+    g = golden("heatstep_L5.npz")
+    s = float(g["dt"]) / float(g["heat_capacity"])
+    K = float(g["heat_capacity"]) * float(g["diffusivity"])
+    h = O.OracleHierarchy(L5)
+    x, it = h.pcg(K, np.full(L5.n, s), g["rhs"], float(g["pcg_tolerance"]), 2000)
+    assert it == int(g["pcg_iterations"])
+    assert np.array_equal(x, g["pcg_x"])
+
+
+def test_newton_driver_bit_identical(L4):
+    g = golden("newton_L4.npz")
+    mean, src, stats = L4.solve_implicit_transport_linear(float(g["conductance"]), g["base"], g["slope"],
+                                                          float(g["cg_tolerance"]), float(g["newton_tolerance"]))
+    assert np.array_equal(mean, g["mean"])
+    assert np.array_equal(src, g["source"])
+    assert np.array_equal(stats, g["stats"])
+    # the reference test's gates (test_heat_transport.cpp:103-106)
+    assert stats[0] <= 3 and stats[2] <= 1e-6 and abs(stats[3]) <= 1e-13 * stats[4] and stats[5] <= 0.0
+
+
+@pytest.mark.parametrize("layers", [4, 8])
+def test_column_radiation_matches_reference(layers):
+    g = golden("column.npz")
+    k = np.concatenate([g["constants"], [101_325.0, float(g["gravity"]), 5.670374419e-8]])
+    outs = O.column_radiation(k, g[f"temperature{layers}"], g[f"humidity{layers}"], g[f"cloud_water{layers}"],
+                              g[f"surface_temperature{layers}"], g[f"surface_pressure{layers}"])
+    for got, name in zip(outs, ("emissivity", "absorbed", "fraction", "reflectance", "scalars")):
+        np.testing.assert_allclose(got, g[f"{name}{layers}"], rtol=1e-14, atol=1e-300, err_msg=name)
+
+
+def test_saturation_matches_reference():
+    from planet_game_gb300 import workloads as W
+
+    g = golden("saturation.npz")
+    T, P = np.meshgrid(g["temperature"], g["pressure"], indexing="ij")
+    q_oracle = np.vectorize(O.saturation_specific_humidity)(T, P)
+    assert np.array_equal(q_oracle, g["qsat"])
+    np.testing.assert_allclose(W.saturation_specific_humidity(T, P), g["qsat"], rtol=1e-14)
+
+
+def test_bicgstab_and_pcg_agree(L5):
+    """The D1 bridge of the reference (test_advection_diffusion.cpp:166-191): the
+    BiCGSTAB and PCG paths solve the same SPD system."""
+    g = golden("heatstep_L5.npz")
+    s = float(g["dt"]) / float(g["heat_capacity"])
+    K = float(g["heat_capacity"]) * float(g["diffusivity"])
+    h = O.OracleHierarchy(L5)
+    xb, _ = h.bicgstab(K, np.full(L5.n, s), g["rhs"], 1e-12)
+    np.testing.assert_allclose(xb, g["pcg_x"], rtol=1e-9)
+
+
+def test_planted_oracle_mistake_is_caught(L4):
+    """A mistake planted in the oracle's inputs (a flipped weight) must break parity."""
+    g = golden("operators_L4.npz")
+    a = dict(L4.a)
+    w = a["edge_length_m"].copy()
+    w[7] *= 1.0 + 1e-12
+    a["edge_length_m"] = w
+    bad = O.OracleMesh(a)
+    assert not np.array_equal(bad.laplacian(g["x64"]), g["laplacian64"])

@@ -1,0 +1,193 @@
+"""GPU multigrid and implicit heat-transport solves through the C-ABI, against the
+reference's golden vectors (Galerkin values, PCG solution) and the CPU oracle.
+
+Tolerances: the Galerkin values are bit-identical (same summation order); the GPU
+V-cycle (damped Jacobi + explicit coarse inverse) matches the oracle's restatement of
+the same algorithm to 1e-12 relative in FP64 and 1e-5 in FP32; every solve meets
+||b - A x|| <= 1e-10 ||b|| (recomputed here in FP64) and the energy closure <= 1e-12."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from conftest import golden
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+VARIANTS = [("fp64", "bicgstab"), ("fp64", "pcg"), ("mixed", "bicgstab"), ("mixed", "pcg")]
+
+
+def system(a, K, s, edge_g=None):
+    n = len(a["area_m2"])
+    rows = np.repeat(np.arange(n), a["edge_count"].astype(int))
+    g = K if edge_g is None else edge_g
+    off = -g * a["graph_weight"]
+    diag = a["area_m2"] / s - np.bincount(rows, off, minlength=n)
+    return sp.csr_matrix((off, (rows, a["neighbor"].astype(np.int64))), shape=(n, n)) + sp.diags(diag)
+
+
+def test_galerkin_values_bit_identical(meshes):
+    """The GPU Galerkin scatter (K9) sums in the reference's order: bit-identical to the
+    oracle on this host's mesh, and to the reference's golden values within mesh ulps."""
+    import planet_game_gb300 as pg
+
+    g = golden("heatstep_L5.npz")
+    m = meshes(5)
+    a = m.arrays()
+    s = float(g["dt"]) / float(g["heat_capacity"])
+    K = float(g["heat_capacity"]) * float(g["diffusivity"])
+    diag, off = a["area_m2"] / s + K * a["graph_weight_sum"], -K * a["graph_weight"]
+    mg = pg.GraphMultigrid(m)
+    mg.set_matrix(diag, off)
+    h = O.OracleHierarchy(O.OracleMesh(a))
+    h.set_matrix(diag, off)
+    for lvl in range(len(m.level_rows)):
+        d, o = mg.level_values(lvl)
+        do, oo = h.values(lvl)
+        assert np.array_equal(d, do) and np.array_equal(o, oo), lvl
+        assert np.max(np.abs(d - g[f"diag{lvl}"])) <= 1e-12 * np.max(np.abs(g[f"diag{lvl}"]))
+        assert np.max(np.abs(o - g[f"off{lvl}"])) <= 1e-12 * np.max(np.abs(g[f"off{lvl}"]))
+
+
+@pytest.mark.parametrize("level", [4, 5, 6])
+def test_vcycle_matches_oracle_restatement(meshes, level):
+    import planet_game_gb300 as pg
+
+    m = meshes(level)
+    a = m.arrays()
+    s, K = 2.6e6 / 4e7, 4e13
+    diag, off = a["area_m2"] / s + K * a["graph_weight_sum"], -K * a["graph_weight"]
+    mg = pg.GraphMultigrid(m)
+    mg.set_matrix(diag, off)
+    h = O.OracleHierarchy(O.OracleMesh(a))
+    h.set_matrix(diag, off)
+    rhs = np.random.default_rng(level).standard_normal(m.cell_count) * 1e12
+    ref = h.vcycle_jacobi(rhs, 2, 2, 0.8)
+    got = mg.precondition(rhs)
+    assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref))
+    got32 = mg.precondition(rhs.astype(np.float32))
+    assert np.max(np.abs(got32 - ref)) <= 2e-5 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("precision,method", VARIANTS)
+def test_pcg_solution_matches_reference_golden(meshes, precision, method):
+    """The reference's own PCG solution of the L5 heat step, tol 1e-12 (golden)."""
+    import planet_game_gb300 as pg
+
+    g = golden("heatstep_L5.npz")
+    m = meshes(5)
+    n = m.cell_count
+    s = float(g["dt"]) / float(g["heat_capacity"])
+    K = float(g["heat_capacity"]) * float(g["diffusivity"])
+    x, rep = pg.solve_newton_system(m, K, np.full(n, s), g["rhs"], precision=precision, method=method)
+    assert rep.status == 0 and rep.relative_residual <= 1e-10
+    A = system(m.arrays(), K, s)
+    assert np.linalg.norm(g["rhs"] - A @ x) <= 1e-10 * np.linalg.norm(g["rhs"])
+    assert np.max(np.abs(x - g["pcg_x"])) <= 1e-7 * np.max(np.abs(g["pcg_x"]))
+
+
+@pytest.mark.parametrize("level", [4, 5, 6])
+@pytest.mark.parametrize("precision,method", VARIANTS)
+def test_transport_step_against_oracle(meshes, level, precision, method):
+    import planet_game_gb300 as pg
+    from planet_game_gb300 import workloads as W
+
+    m = meshes(level)
+    inp = W.step_inputs(m, seed=level)
+    t_new, H, rep = pg.transport_step(m, inp.t0, inp.source, inp.heat_capacity, inp.dt, inp.conductance,
+                                      precision=precision, method=method)
+    assert rep.status == 0
+    assert rep.relative_residual <= 1e-10
+    assert rep.closure <= 1e-12
+    assert abs(rep.sum_W) <= 1e-13 * rep.absolute_sum_W
+    assert rep.dissipation_W_K <= 0.0
+    a = m.arrays()
+    h = O.OracleHierarchy(O.OracleMesh(a))
+    ref = h.transport_step(inp.conductance, inp.heat_capacity, inp.dt, inp.t0, inp.source, tol=1e-13)
+    # T_new = T0 + s (S + H): compare the applied transport and the new state
+    assert np.max(np.abs(t_new - ref["t_new"])) <= 2e-6
+    assert np.max(np.abs(H - ref["transport"])) <= 2e-6 * inp.heat_capacity / inp.dt
+    # energy closure of the new state in FP64, computed here
+    s = inp.dt / inp.heat_capacity
+    gain = np.sum(a["area_m2"] * (t_new - inp.t0) / s)
+    assert abs(gain - np.sum(a["area_m2"] * inp.source)) <= 1e-12 * np.sum(np.abs(a["area_m2"] * inp.source))
+
+
+def test_newton_system_with_held_cells(meshes):
+    """Held cells (slope 0) are decoupled identity rows with x = 0 (heat_transport.cpp:349-363)."""
+    import planet_game_gb300 as pg
+
+    m = meshes(5)
+    a = m.arrays()
+    n = m.cell_count
+    rng = np.random.default_rng(3)
+    slope = np.where(np.arange(n) % 5 == 0, 0.0, 0.01 + 0.2 * rng.random(n))
+    rhs = rng.normal(0, 1e9, n)
+    K = 0.5 * 6.371e6**2
+    h = O.OracleHierarchy(O.OracleMesh(a))
+    ref, _ = h.pcg(K, slope, rhs, 1e-13)
+    for precision in ("fp64", "mixed"):
+        x, rep = pg.solve_newton_system(m, K, slope, rhs, precision=precision)
+        assert rep.status == 0
+        assert np.all(x[slope == 0.0] == 0.0)
+        np.testing.assert_allclose(x, ref, rtol=0, atol=1e-8 * np.abs(ref).max())
+
+
+def test_per_edge_conductance_matches_oracle(meshes):
+    import planet_game_gb300 as pg
+    from planet_game_gb300 import workloads as W
+
+    m = meshes(5, 4.2e6)
+    kappa = W.lognormal_edge_diffusivity(m.edge_count, seed=11)
+    inp = W.step_inputs(m, seed=2, edge_diffusivity=kappa)
+    t_new, H, rep = pg.transport_step(m, inp.t0, inp.source, inp.heat_capacity, inp.dt,
+                                      edge_conductance=inp.edge_conductance, precision="mixed")
+    assert rep.status == 0 and rep.relative_residual <= 1e-10 and rep.closure <= 1e-12
+    om = O.OracleMesh(m.arrays())
+    h = O.OracleHierarchy(om)
+    ref = h.transport_step(0.0, inp.heat_capacity, inp.dt, inp.t0, inp.source, tol=1e-13,
+                           edge_g=om.directed_conductance(inp.edge_conductance))
+    assert np.max(np.abs(t_new - ref["t_new"])) <= 2e-6
+
+
+def test_batch_equals_solo_bit_for_bit(meshes):
+    """Each result is the same alone and in the mix (uneven levels, radii, conductances)."""
+    import planet_game_gb300 as pg
+    from planet_game_gb300 import workloads as W
+
+    specs = [(4, 3.3e6), (6, 8.1e6), (5, 6.0e6), (4, 5.5e6), (3, 7.0e6), (2, 4.0e6)]
+    ms = [meshes(l, r) for l, r in specs]
+    inputs = [W.step_inputs(m, seed=i, edge_diffusivity=W.lognormal_edge_diffusivity(m.edge_count, 100 + i))
+              for i, m in enumerate(ms)]
+    batch = pg.Batch(ms)
+    for precision in ("fp64", "mixed"):
+        for method in ("bicgstab", "pcg"):
+            outs, reps = batch.transport_step([i.t0 for i in inputs], [i.source for i in inputs], 4e7, inputs[0].dt,
+                                              edge_conductance=[i.edge_conductance for i in inputs],
+                                              precision=precision, method=method)
+            for m, inp, out, rep in zip(ms, inputs, outs, reps):
+                solo, _, srep = pg.transport_step(m, inp.t0, inp.source, inp.heat_capacity, inp.dt,
+                                                  edge_conductance=inp.edge_conductance, precision=precision,
+                                                  method=method)
+                assert rep.status == 0 and rep.relative_residual <= 1e-10 and rep.closure <= 1e-12
+                assert rep.iterations == srep.iterations
+                assert np.array_equal(out, solo)
+
+
+def test_cap_and_non_finite_are_reported(meshes):
+    import planet_game_gb300 as pg
+    from planet_game_gb300 import capi
+    from planet_game_gb300 import workloads as W
+
+    m = meshes(5)
+    inp = W.step_inputs(m, seed=0)
+    _, _, rep = pg.transport_step(m, inp.t0, inp.source, inp.heat_capacity, inp.dt, inp.conductance,
+                                  max_iterations=1, max_refinements=1)
+    assert rep.status == capi.ERR_NOT_CONVERGED
+    bad = inp.t0.copy()
+    bad[17] = np.nan
+    _, _, rep = pg.transport_step(m, bad, inp.source, inp.heat_capacity, inp.dt, inp.conductance)
+    assert rep.status == capi.ERR_NON_FINITE
+    # the planet stays usable after a failed step
+    _, _, rep = pg.transport_step(m, inp.t0, inp.source, inp.heat_capacity, inp.dt, inp.conductance)
+    assert rep.status == 0
