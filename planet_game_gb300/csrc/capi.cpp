@@ -148,6 +148,15 @@ int status_of(const psgb::InstanceScalars& s) {
     }
 }
 
+const char* status_message(int code) {
+    switch (code) {
+        case PSGB_ERR_NON_FINITE: return "solve produced a non-finite residual (non-finite input?)";
+        case PSGB_ERR_BREAKDOWN: return "Krylov breakdown before the tolerance was reached";
+        case PSGB_ERR_NOT_CONVERGED: return "iteration or refinement cap reached before the tolerance";
+        default: return "";
+    }
+}
+
 void fill_report(const psgb::InstanceScalars& s, psgb_solve_report* r) {
     if (r == nullptr) return;
     r->status = status_of(s);
@@ -546,10 +555,14 @@ int psgb_solve_newton_system(psgb_planet* h, const psgb_solve_options* options, 
         psgb::launch_mask_rhs(n, b.tmp2, b.bb, st);
         copy_in(b.xr, x, n * 8, memory, st);
         psgb::solve(b, opt, b.bb, b.xr, st);
+        // held rows are decoupled identity rows with a zero right-hand side: x = 0 exactly
+        psgb::launch_mask_rhs(n, b.tmp2, b.xr, st);
         copy_out(x, b.xr, n * 8, memory, st);
         PSGB_CUDA(cudaStreamSynchronize(st));
         fill_report(b.host_scalars[0], report);
-        return status_of(b.host_scalars[0]);
+        const int code = status_of(b.host_scalars[0]);
+        if (code != PSGB_OK) g_last_error = status_message(code);
+        return code;
     });
 }
 
@@ -574,6 +587,7 @@ int psgb_transport_step(psgb_planet* h, const psgb_step_params* params, const ps
         psgb_step_report local;
         step_reports(b, &local, st);
         if (report != nullptr) *report = local;
+        if (local.solve.status != PSGB_OK) g_last_error = status_message(local.solve.status);
         return local.solve.status;
     });
 }
@@ -634,6 +648,7 @@ int psgb_batch_transport_step(psgb_batch* h, const psgb_step_params* params, con
             if (reports != nullptr) reports[i] = local[i];
             if (local[i].solve.status != PSGB_OK && worst == PSGB_OK) worst = local[i].solve.status;
         }
+        if (worst != PSGB_OK) g_last_error = status_message(worst);
         return worst;
     });
 }

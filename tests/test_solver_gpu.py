@@ -186,8 +186,9 @@ def test_cap_and_non_finite_are_reported(meshes):
     assert rep.status == capi.ERR_NOT_CONVERGED
     bad = inp.t0.copy()
     bad[17] = np.nan
-    _, _, rep = pg.transport_step(m, bad, inp.source, inp.heat_capacity, inp.dt, inp.conductance)
-    assert rep.status == capi.ERR_NON_FINITE
+    with pytest.raises(capi.GB300Error) as err:
+        pg.transport_step(m, bad, inp.source, inp.heat_capacity, inp.dt, inp.conductance)
+    assert err.value.code == capi.ERR_NON_FINITE and "non-finite" in str(err.value)
     # the planet stays usable after a failed step
     _, _, rep = pg.transport_step(m, inp.t0, inp.source, inp.heat_capacity, inp.dt, inp.conductance)
     assert rep.status == 0
