@@ -192,6 +192,20 @@ int psgb_transport_step(psgb_planet* planet, const psgb_step_params* params,
                         double* t_new_K, double* transport_W_m2, psgb_step_report* report, int memory,
                         void* stream);
 
+/* The same step, allocating nothing (no counterpart in the reference). For callers that
+ * may not call cudaMalloc or any other allocating CUDA routine while they run (a fixed
+ * memory budget, code around stream capture or in a latency-critical loop where an
+ * allocation could synchronise the device): all solver workspace lives in one static
+ * 8 MiB device array of this library, which every GPU that loads the library holds until
+ * the process exits. DEVICE pointers only, ordered on `stream`. Planets of at most 10,242
+ * cells (a level-5 mesh); larger ones fail with PSGB_ERR_INVALID_ARGUMENT. The first call
+ * on a device looks up that array's device address; make it before any stream capture.
+ * Calls share the array: calls that overlap on the GPU race, serialise them. */
+int psgb_transport_step_noalloc(psgb_planet* planet, const psgb_step_params* params,
+                                const psgb_solve_options* options, const double* t0_K,
+                                const double* source_W_m2, double* t_new_K, double* transport_W_m2,
+                                psgb_step_report* report, void* stream);
+
 /* ---- batches: many planets of uneven levels solved together -------------------
  * Concatenated block layout (each planet padded to 256-row tiles), per-planet
  * convergence masks, one stream of launches for all planets. */

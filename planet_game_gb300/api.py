@@ -329,6 +329,27 @@ def transport_step(mesh: PlanetMesh, t0_K, source_W_m2, heat_capacity_J_m2_K: fl
     return t_new, h, _step_result(rep)
 
 
+def transport_step_noalloc(mesh: PlanetMesh, t0_K, source_W_m2, heat_capacity_J_m2_K: float, dt_s: float,
+                           conductance_W_K: float = 0.0, edge_conductance=None, **options):
+    """The transport step through the entry point that allocates nothing (CUDA tensors
+    only; the solver workspace is the library's static device scratch)."""
+    if not (_is_torch(t0_K) and _is_torch(source_W_m2)):
+        raise ValueError("the no-allocation step takes CUDA tensors")
+    import torch
+
+    t_new = torch.empty_like(t0_K)
+    h = torch.empty_like(t0_K)
+    params = step_params(heat_capacity_J_m2_K, dt_s, conductance_W_K, edge_conductance)
+    o = solve_options(**options)
+    rep = capi.StepReport()
+    code = capi.load().psgb_transport_step_noalloc(mesh.handle, C.byref(params), C.byref(o), _ptr(t0_K),
+                                                   _ptr(source_W_m2), _ptr(t_new), _ptr(h), C.byref(rep),
+                                                   C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    if code not in (capi.OK, capi.ERR_NOT_CONVERGED, capi.ERR_BREAKDOWN):
+        _raise(code)
+    return t_new, h, _step_result(rep)
+
+
 class Batch:
     """Many planets of uneven levels in one concatenated layout, solved together."""
 

@@ -94,6 +94,8 @@ _SIGNATURES = {
                                            C.POINTER(SolveReport), C.c_int, P]),
     "psgb_transport_step": (C.c_int, [P, C.POINTER(StepParams), C.POINTER(SolveOptions), P, P, P, P,
                                       C.POINTER(StepReport), C.c_int, P]),
+    "psgb_transport_step_noalloc": (C.c_int, [P, C.POINTER(StepParams), C.POINTER(SolveOptions), P, P, P, P,
+                                              C.POINTER(StepReport), P]),
     "psgb_batch_create": (C.c_int, [C.POINTER(P), C.c_uint32, C.POINTER(P)]),
     "psgb_batch_destroy": (None, [P]),
     "psgb_batch_device_bytes": (C.c_uint64, [P]),

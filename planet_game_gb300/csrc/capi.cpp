@@ -5,6 +5,7 @@
 // PSGB_ERR_LOGIC, allocation failures -> PSGB_ERR_OUT_OF_MEMORY, CUDA errors ->
 // PSGB_ERR_CUDA; the message is kept per thread for psgb_last_error().
 #include "../../include/planetsim_gb300.h"
+#include "capi_internal.hpp"
 
 #include "column.hpp"
 #include "host/insolation.hpp"
@@ -12,6 +13,7 @@
 #include "profile.hpp"
 #include "solver.hpp"
 
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -19,19 +21,7 @@
 #include <string>
 #include <vector>
 
-struct psgb_planet {
-    std::unique_ptr<psgb::Planet> planet;
-    // lazily created device staging for host-memory calls
-    psgb::DeviceStore stage_store;
-    std::vector<double*> stage;
-    std::size_t stage_len = 0;
-};
-
-struct psgb_batch {
-    std::unique_ptr<psgb::Batch> batch;
-};
-
-namespace {
+namespace psgb::capi {
 
 thread_local std::string g_last_error;
 
@@ -40,26 +30,12 @@ int fail(int code, const std::string& message) {
     return code;
 }
 
-template <typename F>
-int guarded(F&& body) {
-    try {
-        g_last_error.clear();
-        return body();
-    } catch (const std::invalid_argument& e) {
-        return fail(PSGB_ERR_INVALID_ARGUMENT, e.what());
-    } catch (const std::bad_alloc& e) {
-        return fail(PSGB_ERR_OUT_OF_MEMORY, e.what());
-    } catch (const psgb::CudaError& e) {
-        const std::string m = e.what();
-        return fail(m.find("out of memory") != std::string::npos ? PSGB_ERR_OUT_OF_MEMORY : PSGB_ERR_CUDA, m);
-    } catch (const std::overflow_error& e) {
-        return fail(PSGB_ERR_INVALID_ARGUMENT, e.what());
-    } catch (const std::logic_error& e) {
-        return fail(PSGB_ERR_LOGIC, e.what());
-    } catch (const std::exception& e) {
-        return fail(PSGB_ERR_CUDA, e.what());
-    }
-}
+}  // namespace psgb::capi
+
+namespace {
+
+using psgb::capi::fail;
+using psgb::capi::g_last_error;
 
 cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
 
@@ -106,6 +82,10 @@ void copy_out(void* dst, const void* src, std::size_t bytes, int memory, cudaStr
     PSGB_CUDA(cudaMemcpyAsync(dst, src, bytes, memory == PSGB_MEMORY_HOST ? cudaMemcpyDeviceToHost
                                                                         : cudaMemcpyDeviceToDevice, st));
 }
+
+}  // namespace
+
+namespace psgb::capi {
 
 psgb::SolveOptions to_options(const psgb_solve_options* o) {
     psgb_solve_options d;
@@ -265,6 +245,12 @@ void step_reports(psgb::Batch& b, psgb_step_report* reports, cudaStream_t st) {
     }
 }
 
+}  // namespace psgb::capi
+
+using namespace psgb::capi;
+
+namespace {
+
 }  // namespace
 
 
@@ -291,8 +277,10 @@ int psgb_planet_create(uint32_t level, double radius_m, psgb_planet** out) {
     return guarded([&] {
         require(out != nullptr, "output handle pointer is null");
         *out = nullptr;
+        static std::atomic<std::uint64_t> serials{0};
         auto h = std::make_unique<psgb_planet>();
         h->planet = psgb::make_planet(level, radius_m);
+        h->serial = ++serials;
         *out = h.release();
         return PSGB_OK;
     });

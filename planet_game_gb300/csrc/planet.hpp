@@ -50,11 +50,29 @@ class DeviceStore {
         if (count == 0) count = 1;
         void* p = nullptr;
         const std::size_t bytes = (count * sizeof(T) + 255) / 256 * 256;
+        if (arena_ != nullptr) {
+            // Sub-allocation from caller-provided device memory: no allocation call.
+            if (bytes > arena_capacity_ - bytes_) {
+                throw std::invalid_argument("the no-allocation scratch (" + std::to_string(arena_capacity_) +
+                                            " bytes) is too small for this planet");
+            }
+            p = arena_ + bytes_;
+            bytes_ += bytes;
+            return static_cast<T*>(p);
+        }
         PSGB_CUDA(cudaMalloc(&p, bytes));
         ptrs_.push_back(p);
         bytes_ += bytes;
         return static_cast<T*>(p);
     }
+    // Serve every later alloc() from [base, base + capacity) (256-byte aligned) instead
+    // of cudaMalloc; release() then frees nothing.
+    void use_arena(void* base, std::size_t capacity) {
+        arena_ = static_cast<char*>(base);
+        arena_capacity_ = capacity;
+        bytes_ = 0;
+    }
+    bool arena() const { return arena_ != nullptr; }
     template <typename T>
     T* upload(const std::vector<T>& host) {
         T* d = alloc<T>(host.size());
@@ -71,6 +89,8 @@ class DeviceStore {
   private:
     std::vector<void*> ptrs_;
     std::size_t bytes_ = 0;
+    char* arena_ = nullptr;
+    std::size_t arena_capacity_ = 0;
 };
 
 // Fine-level operator geometry, ELL slot-major over P = pad_rows(N) rows.

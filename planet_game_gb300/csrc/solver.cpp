@@ -96,11 +96,32 @@ void upload_planet(Planet& planet_ref) {
     planet->uploaded = true;
 }
 
+namespace {
+std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* arena, std::size_t arena_bytes);
+}  // namespace
+
 std::unique_ptr<Batch> make_batch(const std::vector<Planet*>& planets) {
+    return build_batch(planets, nullptr, 0);
+}
+
+std::unique_ptr<Batch> make_batch_in(const std::vector<Planet*>& planets, void* arena, std::size_t arena_bytes) {
+    if (arena == nullptr) throw std::invalid_argument("no scratch memory given");
+    return build_batch(planets, arena, arena_bytes);
+}
+
+namespace {
+
+std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* arena, std::size_t arena_bytes) {
     if (planets.empty()) throw std::invalid_argument("a batch needs at least one planet");
-    for (Planet* p : planets) upload_planet(*p);
+    if (arena == nullptr) {
+        for (Planet* p : planets) upload_planet(*p);
+    }
     auto bp = std::make_unique<Batch>();
     Batch& b = *bp;
+    if (arena != nullptr) {
+        b.store.use_arena(arena, arena_bytes);
+        b.use_graphs = false;
+    }
     b.planets = planets;
     b.instances = static_cast<std::uint32_t>(planets.size());
     const std::uint32_t I = b.instances;
@@ -285,7 +306,7 @@ std::unique_ptr<Batch> make_batch(const std::vector<Planet*>& planets) {
     b.scalars = b.store.alloc<InstanceScalars>(I);
     PSGB_CUDA(cudaMemset(b.scalars, 0, I * sizeof(InstanceScalars)));
     b.host_scalars.assign(I, InstanceScalars{});
-    PSGB_CUDA(cudaMallocHost(&b.pinned_scalars, I * sizeof(InstanceScalars)));
+    if (arena == nullptr) PSGB_CUDA(cudaMallocHost(&b.pinned_scalars, I * sizeof(InstanceScalars)));
     b.slope_of = b.store.alloc<double>(I);
     b.t0 = b.store.alloc<double>(P0);
     b.src = b.store.alloc<double>(P0);
@@ -293,12 +314,16 @@ std::unique_ptr<Batch> make_batch(const std::vector<Planet*>& planets) {
     b.tnew = b.store.alloc<double>(P0);
     for (double* v : {b.t0, b.src, b.hout, b.tnew}) PSGB_CUDA(cudaMemset(v, 0, P0 * sizeof(double)));
     b.sums = b.store.alloc<double>(std::size_t(I) * 8);
-    PSGB_CUDA(cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking));
-    PSGB_CUDA(cudaEventCreateWithFlags(&b.fence_in, cudaEventDisableTiming));
-    PSGB_CUDA(cudaEventCreateWithFlags(&b.fence_out, cudaEventDisableTiming));
+    if (arena == nullptr) {
+        PSGB_CUDA(cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking));
+        PSGB_CUDA(cudaEventCreateWithFlags(&b.fence_in, cudaEventDisableTiming));
+        PSGB_CUDA(cudaEventCreateWithFlags(&b.fence_out, cudaEventDisableTiming));
+    }
     if (I == 1) b.csr_offset = b.store.upload(planets[0]->graph.offset);
     return bp;
 }
+
+}  // namespace
 
 template <typename T>
 static LevelView<T> make_view(const BatchLevel& L, const T* vd, const T* inv) {
@@ -465,11 +490,11 @@ namespace {
 ReduceCtx reduce_ctx(Batch& b) { return ReduceCtx{b.partial, b.ticket, b.tile_begin, b.scalars}; }
 
 bool all_done(Batch& b, cudaStream_t st, bool outer) {
-    PSGB_CUDA(cudaMemcpyAsync(b.pinned_scalars, b.scalars, b.instances * sizeof(InstanceScalars),
-                              cudaMemcpyDeviceToHost, st));
+    InstanceScalars* host = b.pinned_scalars != nullptr ? b.pinned_scalars : b.host_scalars.data();
+    PSGB_CUDA(cudaMemcpyAsync(host, b.scalars, b.instances * sizeof(InstanceScalars), cudaMemcpyDeviceToHost, st));
     PSGB_CUDA(cudaStreamSynchronize(st));
     for (std::uint32_t i = 0; i < b.instances; ++i) {
-        const InstanceScalars& s = b.pinned_scalars[i];
+        const InstanceScalars& s = host[i];
         if (outer ? s.outer_status == kRunning : (s.outer_status == kRunning && s.status == kRunning)) return false;
     }
     return true;
@@ -572,9 +597,11 @@ void solve(Batch& b, const SolveOptions& opt, const double* rhs, double* x, cuda
     if (!b.matrix_ready) throw std::logic_error("solve before the matrix was set");
     // The solve runs on the batch's own stream (capturable), ordered after the caller's
     // work and before anything the caller enqueues next.
-    cudaStream_t st = b.stream;
-    PSGB_CUDA(cudaEventRecord(b.fence_in, caller));
-    PSGB_CUDA(cudaStreamWaitEvent(st, b.fence_in, 0));
+    cudaStream_t st = b.stream != nullptr ? b.stream : caller;
+    if (b.stream != nullptr) {
+        PSGB_CUDA(cudaEventRecord(b.fence_in, caller));
+        PSGB_CUDA(cudaStreamWaitEvent(st, b.fence_in, 0));
+    }
     const LevelView<double> lv64 = view64(b, 0);
     const ReduceCtx ctx = reduce_ctx(b);
     launch_outer_init(lv64, rhs, ctx, opt.tolerance, opt.max_refinements, st);
@@ -596,12 +623,16 @@ void solve(Batch& b, const SolveOptions& opt, const double* rhs, double* x, cuda
             launch_outer_update<double>(lv64, b.k64[9], x, b.scalars, b.instances, st);
         }
     }
-    PSGB_CUDA(cudaMemcpyAsync(b.pinned_scalars, b.scalars, b.instances * sizeof(InstanceScalars),
-                              cudaMemcpyDeviceToHost, st));
+    InstanceScalars* host = b.pinned_scalars != nullptr ? b.pinned_scalars : b.host_scalars.data();
+    PSGB_CUDA(cudaMemcpyAsync(host, b.scalars, b.instances * sizeof(InstanceScalars), cudaMemcpyDeviceToHost, st));
     PSGB_CUDA(cudaStreamSynchronize(st));
-    std::memcpy(b.host_scalars.data(), b.pinned_scalars, b.instances * sizeof(InstanceScalars));
-    PSGB_CUDA(cudaEventRecord(b.fence_out, st));
-    PSGB_CUDA(cudaStreamWaitEvent(caller, b.fence_out, 0));
+    if (host != b.host_scalars.data()) {
+        std::memcpy(b.host_scalars.data(), host, b.instances * sizeof(InstanceScalars));
+    }
+    if (b.stream != nullptr) {
+        PSGB_CUDA(cudaEventRecord(b.fence_out, st));
+        PSGB_CUDA(cudaStreamWaitEvent(caller, b.fence_out, 0));
+    }
 }
 
 }  // namespace psgb

@@ -28,6 +28,10 @@ std::unique_ptr<Planet> make_planet(std::uint32_t level, double radius_m);
 void upload_planet(Planet& planet);
 
 std::unique_ptr<Batch> make_batch(const std::vector<Planet*>& planets);
+// The same batch with every device array placed in caller-provided device memory
+// [arena, arena + arena_bytes): no device or pinned allocation, no stream, event or graph
+// creation; the solver then runs directly on the caller's stream.
+std::unique_ptr<Batch> make_batch_in(const std::vector<Planet*>& planets, void* arena, std::size_t arena_bytes);
 
 // The fine-level (padded) row base of planet i inside the batch.
 inline std::int64_t fine_base(const Batch& b, std::size_t i) { return b.fine_base[i]; }
