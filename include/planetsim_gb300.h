@@ -220,6 +220,15 @@ int psgb_batch_transport_step(psgb_batch* batch, const psgb_step_params* params,
                               double* const* transport_W_m2, psgb_step_report* reports, int memory,
                               void* stream);
 
+/* The same with only the planets whose `active[i]` (host, one byte per planet) is
+ * non-zero taking part; the others' arrays may be NULL and their state is untouched
+ * (continuous batching: a request loop steps whichever planets have requests). */
+int psgb_batch_transport_step_masked(psgb_batch* batch, const uint8_t* active, const psgb_step_params* params,
+                                     const psgb_solve_options* options, const double* const* t0_K,
+                                     const double* const* source_W_m2, double* const* t_new_K,
+                                     double* const* transport_W_m2, psgb_step_report* reports, int memory,
+                                     void* stream);
+
 /* ---- column radiation: sim/planet/atmosphere/atmosphere_column.hpp ----------------
  * column_radiation (humidity variant, :85-104) + cloud_optics (:599-623) +
  * add_cloud_longwave (:627-634) + longwave_fluxes (:125-143) for `cells` columns of

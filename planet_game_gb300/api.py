@@ -370,7 +370,8 @@ class Batch:
         return int(capi.load().psgb_batch_device_bytes(self._h))
 
     def transport_step(self, t0, sources, heat_capacity, dt, conductance=None, edge_conductance=None,
-                       out=None, transport_out=None, **options):
+                       out=None, transport_out=None, active=None, **options):
+        """One sub-step of every planet (or of the planets with active[i] true)."""
         n = len(self.meshes)
         params = (capi.StepParams * n)()
         keep = []
@@ -381,15 +382,21 @@ class Batch:
                             edge_conductance[i] if edge_conductance is not None else None)
             keep.append(p)
             params[i] = p
+        on = [True] * n if active is None else [bool(a) for a in active]
         if out is None:
-            out = [_empty_like(t0[i], (m.cell_count,)) for i, m in enumerate(self.meshes)]
-        mem, st = _memory_of(*t0, *sources, *out)
-        arrs = lambda xs: (C.c_void_p * n)(*[_ptr(x).value for x in xs])
+            out = [_empty_like(t0[i], (m.cell_count,)) if on[i] else None for i, m in enumerate(self.meshes)]
+        mem, st = _memory_of(*[x for x in (*t0, *sources, *out) if x is not None])
+        arrs = lambda xs: (C.c_void_p * n)(*[_ptr(x).value if x is not None else None for x in xs])
         h_arr = arrs(transport_out) if transport_out is not None else None
         o = solve_options(**options)
         reps = (capi.StepReport * n)()
-        code = capi.load().psgb_batch_transport_step(self._h, params, C.byref(o), arrs(t0), arrs(sources), arrs(out),
-                                                     h_arr, reps, mem, st)
+        if active is None:
+            code = capi.load().psgb_batch_transport_step(self._h, params, C.byref(o), arrs(t0), arrs(sources),
+                                                         arrs(out), h_arr, reps, mem, st)
+        else:
+            mask = (C.c_uint8 * n)(*[1 if a else 0 for a in on])
+            code = capi.load().psgb_batch_transport_step_masked(self._h, mask, params, C.byref(o), arrs(t0),
+                                                                arrs(sources), arrs(out), h_arr, reps, mem, st)
         if code not in (capi.OK, capi.ERR_NOT_CONVERGED, capi.ERR_BREAKDOWN):
             _raise(code)
         return out, [_step_result(r) for r in reps]

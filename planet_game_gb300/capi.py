@@ -102,6 +102,9 @@ _SIGNATURES = {
     "psgb_batch_transport_step": (C.c_int, [P, C.POINTER(StepParams), C.POINTER(SolveOptions), C.POINTER(P),
                                             C.POINTER(P), C.POINTER(P), C.POINTER(P), C.POINTER(StepReport),
                                             C.c_int, P]),
+    "psgb_batch_transport_step_masked": (C.c_int, [P, P, C.POINTER(StepParams), C.POINTER(SolveOptions),
+                                                   C.POINTER(P), C.POINTER(P), C.POINTER(P), C.POINTER(P),
+                                                   C.POINTER(StepReport), C.c_int, P]),
     "psgb_column_radiation": (C.c_int, [C.c_uint32, C.c_uint32, C.POINTER(ColumnConstants), P, P, P, P, P, P, P,
                                         P, P, P, C.c_int, P]),
     "psgb_substep_mean_insolation": (C.c_int, [P, C.c_int64, P]),

@@ -602,42 +602,83 @@ uint64_t psgb_batch_device_bytes(const psgb_batch* batch) {
     return batch == nullptr ? 0 : batch->batch->store.bytes();
 }
 
+}  // extern "C"
+
+namespace {
+
+int batch_step(psgb_batch* h, const std::uint8_t* active, const psgb_step_params* params,
+               const psgb_solve_options* options, const double* const* t0_K, const double* const* source_W_m2,
+               double* const* t_new_K, double* const* transport_W_m2, psgb_step_report* reports, int memory,
+               void* stream) {
+    require(h != nullptr && params != nullptr && t0_K != nullptr && source_W_m2 != nullptr && t_new_K != nullptr,
+            "null argument");
+    require_memory(memory);
+    const psgb::SolveOptions opt = to_options(options);
+    psgb::Batch& b = *h->batch;
+    apply_smoother(b, options);
+    cudaStream_t st = as_stream(stream);
+    // planets taking part: all, or the caller's mask
+    std::vector<std::uint8_t> mask(b.instances, 1);
+    if (active != nullptr) {
+        for (std::uint32_t i = 0; i < b.instances; ++i) mask[i] = active[i] ? 1 : 0;
+    }
+    if (mask != b.host_active) {
+        PSGB_CUDA(cudaMemcpyAsync(b.active, mask.data(), b.instances, cudaMemcpyHostToDevice, st));
+        b.host_active = mask;
+    }
+    b.active_mask = false;
+    for (auto m : mask) b.active_mask = b.active_mask || m == 0;
+    assemble_step_matrix(b, params, st);
+    for (std::uint32_t i = 0; i < b.instances; ++i) {
+        if (!mask[i]) continue;
+        const std::size_t n = b.planets[i]->mesh.cells;
+        require(t0_K[i] != nullptr && source_W_m2[i] != nullptr && t_new_K[i] != nullptr, "null planet array");
+        copy_in(b.t0 + b.fine_base[i], t0_K[i], n * 8, memory, st);
+        copy_in(b.src + b.fine_base[i], source_W_m2[i], n * 8, memory, st);
+    }
+    run_step(b, opt, st);
+    for (std::uint32_t i = 0; i < b.instances; ++i) {
+        if (!mask[i]) continue;
+        const std::size_t n = b.planets[i]->mesh.cells;
+        copy_out(t_new_K[i], b.tnew + b.fine_base[i], n * 8, memory, st);
+        if (transport_W_m2 != nullptr && transport_W_m2[i] != nullptr) {
+            copy_out(transport_W_m2[i], b.hout + b.fine_base[i], n * 8, memory, st);
+        }
+    }
+    std::vector<psgb_step_report> local(b.instances);
+    step_reports(b, local.data(), st);
+    int worst = PSGB_OK;
+    for (std::uint32_t i = 0; i < b.instances; ++i) {
+        if (reports != nullptr) reports[i] = local[i];
+        if (mask[i] && local[i].solve.status != PSGB_OK && worst == PSGB_OK) worst = local[i].solve.status;
+    }
+    if (worst != PSGB_OK) g_last_error = status_message(worst);
+    return worst;
+}
+
+}  // namespace
+
+extern "C" {
+
 int psgb_batch_transport_step(psgb_batch* h, const psgb_step_params* params, const psgb_solve_options* options,
                               const double* const* t0_K, const double* const* source_W_m2,
                               double* const* t_new_K, double* const* transport_W_m2, psgb_step_report* reports,
                               int memory, void* stream) {
     return guarded([&] {
-        require(h != nullptr && params != nullptr && t0_K != nullptr && source_W_m2 != nullptr && t_new_K != nullptr,
-                "null argument");
-        require_memory(memory);
-        const psgb::SolveOptions opt = to_options(options);
-        psgb::Batch& b = *h->batch;
-        apply_smoother(b, options);
-        cudaStream_t st = as_stream(stream);
-        assemble_step_matrix(b, params, st);
-        for (std::uint32_t i = 0; i < b.instances; ++i) {
-            const std::size_t n = b.planets[i]->mesh.cells;
-            require(t0_K[i] != nullptr && source_W_m2[i] != nullptr && t_new_K[i] != nullptr, "null planet array");
-            copy_in(b.t0 + b.fine_base[i], t0_K[i], n * 8, memory, st);
-            copy_in(b.src + b.fine_base[i], source_W_m2[i], n * 8, memory, st);
-        }
-        run_step(b, opt, st);
-        for (std::uint32_t i = 0; i < b.instances; ++i) {
-            const std::size_t n = b.planets[i]->mesh.cells;
-            copy_out(t_new_K[i], b.tnew + b.fine_base[i], n * 8, memory, st);
-            if (transport_W_m2 != nullptr && transport_W_m2[i] != nullptr) {
-                copy_out(transport_W_m2[i], b.hout + b.fine_base[i], n * 8, memory, st);
-            }
-        }
-        std::vector<psgb_step_report> local(b.instances);
-        step_reports(b, local.data(), st);
-        int worst = PSGB_OK;
-        for (std::uint32_t i = 0; i < b.instances; ++i) {
-            if (reports != nullptr) reports[i] = local[i];
-            if (local[i].solve.status != PSGB_OK && worst == PSGB_OK) worst = local[i].solve.status;
-        }
-        if (worst != PSGB_OK) g_last_error = status_message(worst);
-        return worst;
+        return batch_step(h, nullptr, params, options, t0_K, source_W_m2, t_new_K, transport_W_m2, reports, memory,
+                          stream);
+    });
+}
+
+int psgb_batch_transport_step_masked(psgb_batch* h, const uint8_t* active, const psgb_step_params* params,
+                                     const psgb_solve_options* options, const double* const* t0_K,
+                                     const double* const* source_W_m2, double* const* t_new_K,
+                                     double* const* transport_W_m2, psgb_step_report* reports, int memory,
+                                     void* stream) {
+    return guarded([&] {
+        require(active != nullptr, "null mask");
+        return batch_step(h, active, params, options, t0_K, source_W_m2, t_new_K, transport_W_m2, reports, memory,
+                          stream);
     });
 }
 

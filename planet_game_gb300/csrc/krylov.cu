@@ -354,9 +354,22 @@ __global__ void k_pcg_xr(LevelView<T> lv, const T* __restrict__ p, const T* __re
 
 // ||b|| of the outer problem, and the outer state reset.
 __global__ void k_outer_init(LevelView<double> lv, const double* __restrict__ b, ReduceCtx ctx,
-                             double tol, int max_refine) {
+                             double tol, int max_refine, const std::uint8_t* __restrict__ active) {
     int inst;
     const int row = tile_row(lv, inst);
+    if (active != nullptr && !active[inst]) {
+        // a planet left out of this step: nothing runs for it
+        if (threadIdx.x == 0 && blockIdx.x == ctx.tile_begin[inst]) {
+            InstanceScalars& s = ctx.sc[inst];
+            s.outer_status = kConverged;
+            s.status = kConverged;
+            s.refinements = 0;
+            s.inner_total = 0;
+            s.outer_r_norm = 0.0;
+            s.outer_b_norm = 0.0;
+        }
+        return;
+    }
     double q[1] = {0.0};
     if (row >= 0) q[0] = dmul(b[row], b[row]);
     double sum[1];
@@ -498,8 +511,8 @@ template struct KrylovLaunch<float>;
 template struct KrylovLaunch<double>;
 
 void launch_outer_init(const LevelView<double>& lv, const double* b, const ReduceCtx& ctx, double tol,
-                       int max_refine, cudaStream_t st) {
-    PSGB_LAUNCH(kFamRefine, st, k_outer_init<<<lv.tiles, kTile, 0, st>>>(lv, b, ctx, tol, max_refine));
+                       int max_refine, const std::uint8_t* active, cudaStream_t st) {
+    PSGB_LAUNCH(kFamRefine, st, k_outer_init<<<lv.tiles, kTile, 0, st>>>(lv, b, ctx, tol, max_refine, active));
 }
 
 template <typename TI>

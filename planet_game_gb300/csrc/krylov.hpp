@@ -30,8 +30,9 @@ struct KrylovLaunch {
                        const ReduceCtx& ctx, cudaStream_t st);
 };
 
+// `active` (device, per planet, may be null): planets with 0 are skipped by the solve.
 void launch_outer_init(const LevelView<double>& lv, const double* b, const ReduceCtx& ctx, double tol,
-                       int max_refine, cudaStream_t st);
+                       int max_refine, const std::uint8_t* active, cudaStream_t st);
 template <typename TI>
 void launch_outer_residual(const LevelView<double>& lv, const double* b, const double* x, double* r64,
                            TI* rin, const ReduceCtx& ctx, int max_refine, cudaStream_t st);

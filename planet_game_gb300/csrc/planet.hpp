@@ -224,6 +224,9 @@ struct Batch {
     double* hout = nullptr;            // [P0]
     double* tnew = nullptr;            // [P0]
     double* sums = nullptr;            // [instances][8]
+    std::uint8_t* active = nullptr;    // [instances] planets taking part in the current step
+    std::vector<std::uint8_t> host_active;
+    bool active_mask = false;          // some planet is left out of the current step
     double* edge_g = nullptr;          // [6][P0] per-entry conductance (lazily)
     const double* step_edge_conductance = nullptr;   // edge_g when the matrix uses it
     double* csr_values = nullptr;      // one-planet batches: set_matrix staging

@@ -314,6 +314,9 @@ std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* ar
     b.tnew = b.store.alloc<double>(P0);
     for (double* v : {b.t0, b.src, b.hout, b.tnew}) PSGB_CUDA(cudaMemset(v, 0, P0 * sizeof(double)));
     b.sums = b.store.alloc<double>(std::size_t(I) * 8);
+    b.active = b.store.alloc<std::uint8_t>(I);
+    PSGB_CUDA(cudaMemset(b.active, 1, I));
+    b.host_active.assign(I, 1);
     if (arena == nullptr) {
         PSGB_CUDA(cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking));
         PSGB_CUDA(cudaEventCreateWithFlags(&b.fence_in, cudaEventDisableTiming));
@@ -604,7 +607,7 @@ void solve(Batch& b, const SolveOptions& opt, const double* rhs, double* x, cuda
     }
     const LevelView<double> lv64 = view64(b, 0);
     const ReduceCtx ctx = reduce_ctx(b);
-    launch_outer_init(lv64, rhs, ctx, opt.tolerance, opt.max_refinements, st);
+    launch_outer_init(lv64, rhs, ctx, opt.tolerance, opt.max_refinements, b.active_mask ? b.active : nullptr, st);
     // Inner target: max(inner_tol * ||r||, tolerance * ||b|| / 2); the plain FP64 solve
     // reaches the outer target in one refinement, the mixed one in a few.
     const double inner_tol = opt.precision == kMixed ? opt.inner_tolerance : 1e-3 * opt.tolerance;

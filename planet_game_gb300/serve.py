@@ -1,0 +1,289 @@
+"""Continuous-batching request loop for implicit heat-transport sub-steps.
+
+Requests ask for one sub-step of one planet: the planet's temperature advances from its
+resident state by the implicit step with the request's source term. The server keeps a
+population of planets of mesh levels L4-L8; every planet's mesh, multigrid hierarchy,
+matrix values and state stay resident in HBM.
+
+Lanes: one per mesh level, each a resident batch of that level's planets with its own
+CUDA stream and host thread. A lane works in rounds: it takes, for every planet with
+pending requests, the oldest one, and solves them together (the other planets of the
+batch are masked out); requests that arrive while a round runs are admitted at the next
+round of their lane, while the other lanes keep the device busy - their work overlaps on
+the GPU. Lanes are admitted by an HBM budget: a lane is built when its first request
+arrives if its bytes fit; otherwise the least recently used idle lane is evicted first,
+or the request waits until memory frees up.
+
+The comparator (`OneAtATime`) serves the same trace with the plain drop-in: one request
+at a time, each planet solved alone in plain FP64.
+"""
+from __future__ import annotations
+
+import collections
+import threading
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import api
+from . import workloads as W
+
+
+@dataclass
+class PlanetState:
+    level: int
+    radius: float
+    mesh: api.PlanetMesh
+    state: object                       # device tensor: the resident temperature (K)
+    edge_conductance: np.ndarray | None
+    heat_capacity: float
+    dt: float
+    conductance: float
+
+
+@dataclass
+class ServedRequest:
+    arrival_s: float                    # offered arrival time (relative to the trace start)
+    level: int
+    planet: int                         # index within its level's population
+    source: np.ndarray                  # W/m^2, host
+    done_s: float = -1.0
+    result: np.ndarray | None = None    # the new temperature (host)
+    status: int = -1
+    iterations: int = 0
+    t_in: np.ndarray | None = None      # the state the step started from (for checks)
+
+
+def build_population(per_level: int, levels=(4, 5, 6, 7, 8), seed: int = 7, device=None):
+    """Planets of each level with seeded radii, per-edge diffusivities and initial states."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    population: dict[int, list[PlanetState]] = {}
+    for level in levels:
+        planets = []
+        for k in range(per_level):
+            radius = float(rng.uniform(3e6, 9e6))
+            pseed = int(rng.integers(0, 2**31))
+            m = api.make_icosphere(level, radius)
+            kappa = W.lognormal_edge_diffusivity(m.edge_count, pseed)
+            inp = W.step_inputs(m, pseed, edge_diffusivity=kappa)
+            planets.append(PlanetState(level, radius, m, torch.from_numpy(inp.t0).to(device), inp.edge_conductance,
+                                       inp.heat_capacity, inp.dt, inp.conductance))
+        population[level] = planets
+    return population
+
+
+def make_requests(trace, population, seed: int = 11):
+    """Requests of a trace: each carries a source term for its planet (seeded)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for r in trace:
+        p = population[r.level][r.planet % len(population[r.level])]
+        if not hasattr(p, "_q"):
+            p._lat = W.latitude(p.mesh.arrays()["center"])
+            p._q = p.mesh.substep_mean_insolation(0).astype(np.float64)
+        lat = p._lat
+        base_t = 288.0 - 40.0 * np.sin(lat) ** 2
+        src = 0.7 * p._q - (203.3 + 2.09 * (base_t - 273.15)) + rng.normal(0.0, 5.0, len(lat))
+        out.append(ServedRequest(r.arrival_s, r.level, r.planet % len(population[r.level]), src))
+    return out
+
+
+class _Lane:
+    def __init__(self, server, level):
+        import torch
+
+        self.server = server
+        self.level = level
+        self.planets = server.population[level]
+        self.batch = None
+        self.bytes = 0
+        self.pending: dict[int, collections.deque] = collections.defaultdict(collections.deque)
+        self.cv = threading.Condition(server.lock)
+        self.stream = torch.cuda.Stream()
+        self.last_used = 0.0
+        self.busy = False
+        self.thread = threading.Thread(target=self._run, daemon=True)
+        self.rounds = 0
+
+    def _round(self, reqs: dict[int, ServedRequest]):
+        import torch
+
+        n = len(self.planets)
+        active = [i in reqs for i in range(n)]
+        with torch.cuda.stream(self.stream):
+            t0 = [p.state if active[i] else None for i, p in enumerate(self.planets)]
+            src = [torch.from_numpy(reqs[i].source).to(self.server.device, non_blocking=False) if active[i] else None
+                   for i in range(n)]
+            outs, reps = self.batch.transport_step(
+                t0, src, [p.heat_capacity for p in self.planets], [p.dt for p in self.planets],
+                conductance=[p.conductance for p in self.planets],
+                edge_conductance=[p.edge_conductance for p in self.planets], active=active, **self.server.options)
+            for i, r in reqs.items():
+                if self.server.keep_inputs:
+                    r.t_in = self.planets[i].state.cpu().numpy()
+                self.planets[i].state = outs[i]
+                r.result = outs[i].cpu().numpy()
+                r.status = reps[i].status
+                r.iterations = reps[i].iterations
+        done = time.perf_counter() - self.server.t_start
+        for r in reqs.values():
+            r.done_s = done
+
+    def _run(self):
+        srv = self.server
+        while True:
+            with self.cv:
+                while not srv.stopping and not any(self.pending.values()):
+                    self.cv.wait()
+                if srv.stopping and not any(self.pending.values()):
+                    return
+                reqs = {i: q.popleft() for i, q in self.pending.items() if q}
+                self.busy = True
+            try:
+                self._round(reqs)
+                self.rounds += 1
+            except Exception as exc:  # report, then let the server surface it
+                srv.errors.append(exc)
+                for r in reqs.values():
+                    r.done_s = time.perf_counter() - srv.t_start
+                    r.status = -2
+            with self.cv:
+                self.busy = False
+                self.last_used = time.perf_counter()
+                srv.completed += len(reqs)
+                srv.done_cv.notify_all()
+
+
+class Server:
+    """The continuous-batching request loop (see the module docstring)."""
+
+    def __init__(self, population, budget_bytes: float = 150e9, precision: str = "mixed", method: str = "bicgstab",
+                 device=None, keep_inputs: bool = False, **solver):
+        import torch
+
+        self.population = population
+        self.device = device or torch.device("cuda", 0)
+        self.budget = float(budget_bytes)
+        self.options = dict(precision=precision, method=method, **solver)
+        self.lock = threading.Lock()
+        self.done_cv = threading.Condition(self.lock)
+        self.lanes: dict[int, _Lane] = {}
+        self.resident_bytes = 0
+        self.stopping = False
+        self.completed = 0
+        self.errors: list[Exception] = []
+        self.keep_inputs = keep_inputs
+        self.evictions = 0
+        self.t_start = time.perf_counter()
+
+    # -- admission ------------------------------------------------------------------------
+    def _lane_bytes(self, level) -> int:
+        # resident: the batch's workspace plus every planet's state
+        cells = sum(p.mesh.cell_count for p in self.population[level])
+        return int(cells * 700)   # measured layout cost per cell of a mixed-precision batch, with margin
+
+    def _admit(self, level) -> _Lane | None:
+        """Lane of `level`, built if the budget allows (evicting idle lanes); None: wait."""
+        lane = self.lanes.get(level)
+        if lane is not None and lane.batch is not None:
+            return lane
+        need = self._lane_bytes(level)
+        while self.resident_bytes + need > self.budget:
+            idle = [l for l in self.lanes.values() if l.batch is not None and not l.busy and not any(l.pending.values())]
+            if not idle:
+                return None
+            victim = min(idle, key=lambda l: l.last_used)
+            victim.batch = None
+            self.resident_bytes -= victim.bytes
+            victim.bytes = 0
+            self.evictions += 1
+        if lane is None:
+            lane = _Lane(self, level)
+            self.lanes[level] = lane
+            lane.thread.start()
+        lane.batch = api.Batch([p.mesh for p in self.population[level]])
+        lane.bytes = need
+        self.resident_bytes += need
+        return lane
+
+    def submit(self, req: ServedRequest) -> bool:
+        """Queue a request; False if its lane cannot be admitted yet (memory)."""
+        with self.lock:
+            lane = self._admit(req.level)
+            if lane is None:
+                return False
+            lane.pending[req.planet].append(req)
+            lane.cv.notify()
+            return True
+
+    def run_trace(self, requests: list[ServedRequest], realtime: bool = True):
+        """Replay arrivals (at their offered times when `realtime`), wait for completion."""
+        self.t_start = time.perf_counter()
+        waiting = collections.deque()
+        for r in requests:
+            if realtime:
+                delay = r.arrival_s - (time.perf_counter() - self.t_start)
+                if delay > 0:
+                    time.sleep(delay)
+            waiting.append(r)
+            while waiting and self.submit(waiting[0]):
+                waiting.popleft()
+        while waiting:
+            time.sleep(0.001)
+            while waiting and self.submit(waiting[0]):
+                waiting.popleft()
+        with self.done_cv:
+            while self.completed < len(requests) and not self.errors:
+                self.done_cv.wait(timeout=1.0)
+        if self.errors:
+            raise self.errors[0]
+
+    def close(self):
+        with self.lock:
+            self.stopping = True
+            for lane in self.lanes.values():
+                lane.cv.notify_all()
+        for lane in self.lanes.values():
+            lane.thread.join(timeout=30)
+
+
+class OneAtATime:
+    """The comparator: requests in arrival order, one at a time, plain FP64, each planet
+    solved alone through the single-planet entry point."""
+
+    def __init__(self, population, device=None, **solver):
+        import torch
+
+        self.population = population
+        self.device = device or torch.device("cuda", 0)
+        self.options = {"method": "bicgstab", **solver, "precision": "fp64"}
+
+    def run_trace(self, requests: list[ServedRequest], realtime: bool = True):
+        import torch
+
+        t_start = time.perf_counter()
+        for r in requests:
+            if realtime:
+                delay = r.arrival_s - (time.perf_counter() - t_start)
+                if delay > 0:
+                    time.sleep(delay)
+            p = self.population[r.level][r.planet]
+            src = torch.from_numpy(r.source).to(self.device)
+            out, _, rep = api.transport_step(p.mesh, p.state, src, p.heat_capacity, p.dt, p.conductance,
+                                             edge_conductance=p.edge_conductance, **self.options)
+            p.state = out
+            r.result = out.cpu().numpy()
+            r.status = rep.status
+            r.iterations = rep.iterations
+            r.done_s = time.perf_counter() - t_start
+
+
+def summarize(requests: list[ServedRequest]) -> dict:
+    lat = np.array([r.done_s - r.arrival_s for r in requests])
+    span = max(r.done_s for r in requests) - min(r.arrival_s for r in requests)
+    return {"requests": len(requests), "sub_steps_per_s": len(requests) / span if span > 0 else None,
+            "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "ok": int(sum(r.status == 0 for r in requests))}
