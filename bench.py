@@ -240,13 +240,13 @@ def run_gb300(args, rank, world, local_rank):
            "d2h_bytes_per_step": cells * 8}
 
     # profiled pass: the dominant kernel family timed with events on its stream
-    prof_family = b"smooth"
-    capi.check(lib.psgb_profile_begin(prof_family))
-    for _ in range(args.steps):
-        step(t0_d, s_d, out_d)
     import ctypes as C
 
     ms, nl, nbytes = C.c_double(), C.c_uint64(), C.c_uint64()
+    prof_family = b"persistent" if args.schedule == "persistent" else b"smooth"
+    capi.check(lib.psgb_profile_begin(prof_family))
+    for _ in range(args.steps):
+        step(t0_d, s_d, out_d)
     capi.check(lib.psgb_profile_end(C.byref(ms), C.byref(nl), C.byref(nbytes)))
     peak, peak_kind = peaks()
     achieved = nbytes.value / (ms.value / 1e3) / 1e9 if ms.value > 0 else None
@@ -255,7 +255,9 @@ def run_gb300(args, rank, world, local_rank):
         t = json.loads(TRAFFIC_FILE.read_text()).get(args.workload)
         if t:
             traffic = t.get("dram_bytes_per_launch")
-    roofline = {"bound": "hbm", "kernel": "k_smooth (Jacobi sweep, all levels)", "achieved": achieved,
+    kernel = {b"smooth": "k_smooth (Jacobi sweep, all levels)",
+              b"persistent": "k_persistent_solve (whole refined solve, all levels)"}[prof_family]
+    roofline = {"bound": "hbm", "kernel": kernel, "achieved": achieved,
                 "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                 "launches": int(nl.value), "avg_launch_us": ms.value * 1e3 / max(1, nl.value),
@@ -481,9 +483,12 @@ def main():
     ap.add_argument("--seed", type=int, default=2026)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-plain", action="store_true")
+    ap.add_argument("--schedule", choices=["auto", "kernels", "persistent"], default="auto",
+                    help="persistent: one cooperative kernel per solve; kernels: one kernel per phase")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    SOLVER["schedule"] = SOLVER_SERVE["schedule"] = args.schedule
     rank, world, local_rank = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)

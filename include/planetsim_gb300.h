@@ -50,6 +50,11 @@ extern "C" {
 #define PSGB_METHOD_PCG 0
 #define PSGB_METHOD_BICGSTAB 1
 
+/* How a solve is scheduled on the GPU. */
+#define PSGB_SCHEDULE_AUTO 0        /* the library's choice: currently the kernel schedule (faster on GB300) */
+#define PSGB_SCHEDULE_KERNELS 1     /* one kernel per phase; Krylov chunks replayed as CUDA graphs */
+#define PSGB_SCHEDULE_PERSISTENT 2  /* one cooperative kernel per solve (grid barriers between phases) */
+
 typedef struct psgb_planet psgb_planet;
 typedef struct psgb_batch psgb_batch;
 
@@ -149,6 +154,7 @@ typedef struct psgb_solve_options {
     int poll;                    /* Krylov iterations between host status reads */
     int pre_sweeps, post_sweeps; /* Jacobi sweeps per level */
     double jacobi_omega;         /* Jacobi damping */
+    int schedule;                /* PSGB_SCHEDULE_*; results are identical for every schedule */
 } psgb_solve_options;
 void psgb_solve_options_default(psgb_solve_options* out);
 

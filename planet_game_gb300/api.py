@@ -257,6 +257,8 @@ def solve_options(**kw) -> capi.SolveOptions:
     names = {
         "precision": {"fp64": capi.PRECISION_FP64, "mixed": capi.PRECISION_MIXED},
         "method": {"pcg": capi.METHOD_PCG, "bicgstab": capi.METHOD_BICGSTAB},
+        "schedule": {"auto": capi.SCHEDULE_AUTO, "kernels": capi.SCHEDULE_KERNELS,
+                     "persistent": capi.SCHEDULE_PERSISTENT},
     }
     for k, v in kw.items():
         if k in names and isinstance(v, str):

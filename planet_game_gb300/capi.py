@@ -28,6 +28,9 @@ PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 METHOD_PCG = 0
 METHOD_BICGSTAB = 1
+SCHEDULE_AUTO = 0
+SCHEDULE_KERNELS = 1
+SCHEDULE_PERSISTENT = 2
 
 
 class PlanetInfo(C.Structure):
@@ -47,7 +50,7 @@ class SolveOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("method", C.c_int), ("tolerance", C.c_double),
                 ("inner_tolerance", C.c_double), ("max_iterations", C.c_int), ("max_refinements", C.c_int),
                 ("poll", C.c_int), ("pre_sweeps", C.c_int), ("post_sweeps", C.c_int),
-                ("jacobi_omega", C.c_double)]
+                ("jacobi_omega", C.c_double), ("schedule", C.c_int)]
 
 
 class SolveReport(C.Structure):

@@ -100,6 +100,8 @@ psgb::SolveOptions to_options(const psgb_solve_options* o) {
     require(o->pre_sweeps >= 1 && o->post_sweeps >= 0 && o->pre_sweeps <= 8 && o->post_sweeps <= 8,
             "Jacobi sweeps must be 1..8 (pre) and 0..8 (post)");
     require(o->jacobi_omega > 0.0 && o->jacobi_omega < 2.0, "Jacobi damping must be in (0, 2)");
+    require(o->schedule == PSGB_SCHEDULE_AUTO || o->schedule == PSGB_SCHEDULE_KERNELS ||
+                o->schedule == PSGB_SCHEDULE_PERSISTENT, "unknown schedule");
     s.precision = o->precision;
     s.method = o->method;
     s.tolerance = o->tolerance;
@@ -107,6 +109,7 @@ psgb::SolveOptions to_options(const psgb_solve_options* o) {
     s.max_iterations = o->max_iterations;
     s.max_refinements = o->max_refinements;
     s.poll = o->poll;
+    s.schedule = o->schedule;
     return s;
 }
 
@@ -271,6 +274,7 @@ void psgb_solve_options_default(psgb_solve_options* out) {
     out->pre_sweeps = 2;
     out->post_sweeps = 2;
     out->jacobi_omega = 0.8;
+    out->schedule = PSGB_SCHEDULE_AUTO;
 }
 
 int psgb_planet_create(uint32_t level, double radius_m, psgb_planet** out) {
@@ -745,8 +749,7 @@ int psgb_profile_begin(const char* family) {
         const int f = psgb::family_of(family);
         require(f >= 0, "unknown kernel family");
         PSGB_CUDA(cudaDeviceSynchronize());
-        psgb::swept_bytes_exchange();
-        psgb::profile_begin(f);
+        if (!psgb::profile_begin(f)) throw std::runtime_error("could not start the profile");
         return PSGB_OK;
     });
 }
@@ -758,7 +761,7 @@ int psgb_profile_end(double* total_ms, uint64_t* launches, uint64_t* swept_bytes
         std::uint64_t n = 0;
         if (!psgb::profile_end(total_ms, &n)) throw std::logic_error("no profile is active");
         *launches = n;
-        *swept_bytes = psgb::swept_bytes_exchange();
+        *swept_bytes = psgb::profile_bytes_exchange();
         return PSGB_OK;
     });
 }

@@ -46,6 +46,7 @@ struct LevelView {
     const std::int32_t* tile_inst;
     const std::int32_t* tile_rows;    // valid rows per tile
     const std::uint8_t* tile_sweep;   // 1: the tile's planet smooths on this level
+    unsigned long long* bytes;        // algorithmic-byte counter while profiling, else null
 };
 
 struct ReduceCtx {
@@ -111,7 +112,6 @@ void launch_dense_solve(const DenseView& dense, int level, std::uint32_t max_row
 template <typename T>
 void launch_spmv(const LevelView<T>& lv, const T* x, T* y, cudaStream_t stream);
 
-// Algorithmic bytes of the Jacobi sweeps since the last call (device counter), and reset.
-std::uint64_t swept_bytes_exchange();
+
 
 }  // namespace psgb

@@ -10,33 +10,14 @@
 // row, 256-row tiles, neighbour gathers served mostly from L2 thanks to the
 // reference's space-filling cell order. No tensor cores (sparse stencils).
 #include "common.cuh"
-#include "profile.hpp"
 #include "kernels.hpp"
+#include "phases.cuh"
+#include "profile.hpp"
 
 #include <stdexcept>
 
 namespace psgb {
 namespace {
-
-__device__ __forceinline__ bool gate_open(const InstanceScalars* sc, int inst, int gate) {
-    if (gate == kGateAlways) return true;
-    const InstanceScalars& s = sc[inst];
-    if (gate == kGateOuter) return s.outer_status == kRunning;
-    if (s.status != kRunning) return false;
-    if (gate == kGateSecondHalf && s.half_done) return false;
-    return true;
-}
-
-// Returns the row this thread owns, or -1 (padding row, gated tile, non-sweep tile).
-template <typename T>
-__device__ __forceinline__ int owned_row(const LevelView<T>& lv, const InstanceScalars* sc, int gate,
-                                         bool need_sweep) {
-    const int tile = blockIdx.x;
-    if (threadIdx.x >= lv.tile_rows[tile]) return -1;
-    if (need_sweep && !lv.tile_sweep[tile]) return -1;
-    if (!gate_open(sc, lv.tile_inst[tile], gate)) return -1;
-    return tile * kTile + threadIdx.x;
-}
 
 // ---- assembly -------------------------------------------------------------
 
@@ -174,160 +155,76 @@ __global__ void __launch_bounds__(1024) k_dense_invert(DenseView dense, int leve
     }
 }
 
-// ---- V-cycle pieces ----------------------------------------------------------
-
-// Algorithmic bytes moved by the Jacobi sweeps (one atomic per active tile), read by the
-// profiler: a sweep row reads its W columns and values, 1/diag, b and x and writes y;
-// the zero-start sweep reads 1/diag and b and writes x. Neighbour gathers of x are
-// not counted again.
-__device__ unsigned long long g_swept_bytes;
+// ---- V-cycle pieces: one 256-thread block per tile (the shared phases of phases.cuh) ----
 
 template <typename T>
 __global__ void k_smooth_zero(LevelView<T> lv, const T* __restrict__ b, T* __restrict__ x, T omega,
                               const InstanceScalars* sc, int gate) {
-    const int row = owned_row(lv, sc, gate, true);
-    if (row < 0) return;
-    if (threadIdx.x == 0) {
-        atomicAdd(&g_swept_bytes, static_cast<unsigned long long>(lv.tile_rows[blockIdx.x]) * 3ull * sizeof(T));
-    }
-    x[row] = omega * lv.inv[row] * b[row];
+    ph::smooth_zero<T>(lv, blockIdx.x, threadIdx.x, b, x, omega, sc, gate);
 }
 
 template <typename T, int W>
-__global__ void k_smooth(LevelView<T> lv, const T* __restrict__ b, const T* __restrict__ x,
-                         T* __restrict__ y, T omega, const InstanceScalars* sc, int gate) {
-    const int row = owned_row(lv, sc, gate, true);
-    if (row < 0) return;
-    if (threadIdx.x == 0) {
-        atomicAdd(&g_swept_bytes, static_cast<unsigned long long>(lv.tile_rows[blockIdx.x]) *
-                                      (4ull * W + sizeof(T) * (W + 4ull)));
-    }
-    const std::uint32_t P = lv.rows;
-    T s = b[row];
-#pragma unroll
-    for (int j = 0; j < W; ++j) s -= lv.vd[j * P + row] * x[lv.col[j * P + row]];
-    const T xo = x[row];
-    y[row] = xo + omega * (lv.inv[row] * s - xo);
+__global__ void k_smooth(LevelView<T> lv, const T* __restrict__ b, const T* __restrict__ x, T* __restrict__ y,
+                         T omega, const InstanceScalars* sc, int gate) {
+    ph::smooth<T, W>(lv, blockIdx.x, threadIdx.x, b, x, y, omega, sc, gate);
 }
 
 template <typename T, int W>
-__global__ void k_residual(LevelView<T> lv, const T* __restrict__ b, const T* __restrict__ x,
-                           T* __restrict__ r, const InstanceScalars* sc, int gate) {
-    const int row = owned_row(lv, sc, gate, true);
-    if (row < 0) return;
-    const std::uint32_t P = lv.rows;
-    T s = b[row] - lv.vd[W * P + row] * x[row];
-#pragma unroll
-    for (int j = 0; j < W; ++j) s -= lv.vd[j * P + row] * x[lv.col[j * P + row]];
-    r[row] = s;
+__global__ void k_residual(LevelView<T> lv, const T* __restrict__ b, const T* __restrict__ x, T* __restrict__ r,
+                           const InstanceScalars* sc, int gate) {
+    ph::residual<T, W>(lv, blockIdx.x, threadIdx.x, b, x, r, sc, gate);
 }
 
 template <typename T, int W>
 __global__ void k_spmv(LevelView<T> lv, const T* __restrict__ x, T* __restrict__ y) {
-    const int tile = blockIdx.x;
-    if (threadIdx.x >= lv.tile_rows[tile]) return;
-    const int row = tile * kTile + threadIdx.x;
-    const std::uint32_t P = lv.rows;
-    T s = lv.vd[W * P + row] * x[row];
-#pragma unroll
-    for (int j = 0; j < W; ++j) s += lv.vd[j * P + row] * x[lv.col[j * P + row]];
-    y[row] = s;
+    ph::spmv<T, W>(lv, blockIdx.x, threadIdx.x, x, y);
 }
 
-// Coarse right-hand side: each coarse row sums its members' residuals in
-// ascending fine-row order (the reference's order, heat_transport.cpp:316-319).
 template <typename T>
 __global__ void k_restrict(LevelView<T> coarse, const std::uint32_t* __restrict__ moff,
-                           const std::uint32_t* __restrict__ member, const T* __restrict__ r,
-                           T* __restrict__ bc, const InstanceScalars* sc, int gate) {
-    const int tile = blockIdx.x;
-    if (threadIdx.x >= coarse.tile_rows[tile]) return;
-    if (!gate_open(sc, coarse.tile_inst[tile], gate)) return;
-    const int row = tile * kTile + threadIdx.x;
-    T s = T(0);
-    for (std::uint32_t k = moff[row]; k < moff[row + 1]; ++k) s += r[member[k]];
-    bc[row] = s;
+                           const std::uint32_t* __restrict__ member, const T* __restrict__ r, T* __restrict__ bc,
+                           const InstanceScalars* sc, int gate) {
+    ph::restrict_only<T>(coarse, blockIdx.x, threadIdx.x, moff, member, r, bc, sc, gate);
 }
 
-// Restriction fused with the coarse level's zero-start sweep: b_c = sum of the members'
-// residuals (ascending fine rows), and x_c = omega b_c / diag where the planet smooths
-// on the coarse level (planets whose coarsest level this is only need b_c).
 template <typename T>
 __global__ void k_restrict_zero(LevelView<T> coarse, const std::uint32_t* __restrict__ moff,
                                 const std::uint32_t* __restrict__ member, const T* __restrict__ r,
                                 T* __restrict__ bc, T* __restrict__ xc, T omega, const InstanceScalars* sc,
                                 int gate) {
-    const int tile = blockIdx.x;
-    if (threadIdx.x >= coarse.tile_rows[tile]) return;
-    if (!gate_open(sc, coarse.tile_inst[tile], gate)) return;
-    const int row = tile * kTile + threadIdx.x;
-    T s = T(0);
-    for (std::uint32_t k = moff[row]; k < moff[row + 1]; ++k) s += r[member[k]];
-    bc[row] = s;
-    if (coarse.tile_sweep[tile]) xc[row] = omega * coarse.inv[row] * s;
+    ph::restrict_zero<T>(coarse, blockIdx.x, threadIdx.x, moff, member, r, bc, xc, omega, sc, gate);
 }
 
-// Prolongation fused with the first post-smoothing sweep: with x' = x + e[agg] (formed
-// on the fly for the row and its neighbours), y = x' + omega (D^-1 (b - O x') - x').
 template <typename T, int W>
 __global__ void k_prolong_smooth(LevelView<T> lv, const std::int32_t* __restrict__ agg,
                                  const T* __restrict__ e, const T* __restrict__ b, const T* __restrict__ x,
                                  T* __restrict__ y, T omega, const InstanceScalars* sc, int gate) {
-    const int row = owned_row(lv, sc, gate, true);
-    if (row < 0) return;
-    if (threadIdx.x == 0) {
-        atomicAdd(&g_swept_bytes, static_cast<unsigned long long>(lv.tile_rows[blockIdx.x]) *
-                                      (8ull * W + sizeof(T) * (W + 4ull) + 4ull));
-    }
-    const std::uint32_t P = lv.rows;
-    T s = b[row];
-#pragma unroll
-    for (int j = 0; j < W; ++j) {
-        const int c = lv.col[j * P + row];
-        s -= lv.vd[j * P + row] * (x[c] + e[agg[c]]);
-    }
-    const T xo = x[row] + e[agg[row]];
-    y[row] = xo + omega * (lv.inv[row] * s - xo);
+    ph::prolong_smooth<T, W>(lv, blockIdx.x, threadIdx.x, agg, e, b, x, y, omega, sc, gate);
 }
 
 template <typename T>
 __global__ void k_prolong(LevelView<T> lv, const std::int32_t* __restrict__ agg, const T* __restrict__ xc,
                           T* __restrict__ x, const InstanceScalars* sc, int gate) {
-    const int row = owned_row(lv, sc, gate, true);
-    if (row < 0) return;
-    x[row] += xc[agg[row]];
+    ph::prolong<T>(lv, blockIdx.x, threadIdx.x, agg, xc, x, sc, gate);
 }
 
-// Coarsest level: x = A^-1 b, one warp per row, lanes over columns.
+// Coarsest level: x = A^-1 b, one warp per row.
 template <typename T>
 __global__ void k_dense_solve(DenseView dense, int level, const T* __restrict__ inv,
                               const T* __restrict__ b, T* __restrict__ x, const InstanceScalars* sc,
                               int gate) {
     const int inst = blockIdx.y;
     if (dense.level[inst] != level) return;
-    if (!gate_open(sc, inst, gate)) return;
-    const int n = static_cast<int>(dense.size[inst]);
+    if (!ph::gate_open(sc, inst, gate)) return;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (warp >= n) return;
-    const std::int64_t base = dense.row_base[inst];
-    const T* a = inv + dense.offset[inst] + static_cast<std::int64_t>(warp) * n;
-    T s = T(0);
-    for (int j = lane; j < n; j += 32) s += a[j] * b[base + j];
-    s = warp_sum(s);
-    if (lane == 0) x[base + warp] = s;
+    if (warp >= static_cast<int>(dense.size[inst])) return;
+    ph::dense_row<T>(dense, inst, warp, threadIdx.x & 31, inv, b, x);
 }
 
 inline dim3 tiles_grid(std::uint32_t tiles) { return dim3(tiles); }
 
 }  // namespace
 
-std::uint64_t swept_bytes_exchange() {
-    unsigned long long v = 0, zero = 0;
-    cudaMemcpyFromSymbol(&v, g_swept_bytes, sizeof(v));
-    cudaMemcpyToSymbol(g_swept_bytes, &zero, sizeof(zero));
-    return v;
-}
 
 // ---- launchers -----------------------------------------------------------------
 

@@ -208,6 +208,7 @@ struct Batch {
     unsigned* ticket = nullptr;        // [instances]
     std::uint32_t* tile_begin = nullptr;  // [instances + 1] fine-level tile ranges
     InstanceScalars* scalars = nullptr;   // [instances]
+    unsigned* sync = nullptr;          // [3] grid-barrier state of the persistent solve
     std::vector<InstanceScalars> host_scalars;
     InstanceScalars* pinned_scalars = nullptr;   // pinned host mirror
     bool matrix_ready = false;

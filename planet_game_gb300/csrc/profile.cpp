@@ -25,7 +25,8 @@ struct Profile {
 constexpr std::size_t kMaxEvents = 1 << 16;
 
 const char* const kNames[kFamCount] = {"smooth", "residual", "restrict", "prolong", "dense", "krylov_spmv",
-                                       "krylov_vector", "refine", "setup", "step", "operator", "column"};
+                                       "krylov_vector", "refine", "setup", "step", "operator", "column",
+                                       "persistent"};
 
 }  // namespace
 
@@ -38,6 +39,20 @@ int family_of(const char* name) {
 }
 
 bool profile_active() { return g_profile.family >= 0; }
+
+namespace {
+unsigned long long* g_bytes_counter = nullptr;   // device, allocated by the first profile_begin
+}
+
+unsigned long long* profile_bytes_counter() { return profile_active() ? g_bytes_counter : nullptr; }
+
+std::uint64_t profile_bytes_exchange() {
+    if (g_bytes_counter == nullptr) return 0;
+    unsigned long long v = 0;
+    cudaMemcpy(&v, g_bytes_counter, sizeof(v), cudaMemcpyDeviceToHost);
+    cudaMemset(g_bytes_counter, 0, sizeof(v));
+    return v;
+}
 void set_capturing(bool on) { g_capturing = on; }
 void count_graph_kernels(std::uint64_t kernels) { g_graph_kernels.fetch_add(kernels, std::memory_order_relaxed); }
 
@@ -77,6 +92,10 @@ std::uint64_t launches_of(int family) { return g_launches[family].load(std::memo
 
 bool profile_begin(int family) {
     if (family < 0 || family >= kFamCount) return false;
+    if (g_bytes_counter == nullptr) {
+        if (cudaMalloc(&g_bytes_counter, sizeof(unsigned long long)) != cudaSuccess) return false;
+    }
+    cudaMemset(g_bytes_counter, 0, sizeof(unsigned long long));
     std::lock_guard<std::mutex> lock(g_profile.mu);
     g_profile.family = family;
     g_profile.used = 0;

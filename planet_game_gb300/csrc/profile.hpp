@@ -25,6 +25,7 @@ enum KernelFamily : int {
     kFamStep,            // transport-step right-hand side and flux form
     kFamOperator,        // finite-volume operators
     kFamColumn,          // column radiation
+    kFamPersistent,      // the persistent cooperative solve (one launch per solve)
     kFamCount
 };
 
@@ -44,6 +45,11 @@ bool profile_active();
 // of a graph adds its kernel nodes instead.
 void set_capturing(bool on);
 void count_graph_kernels(std::uint64_t kernels);
+
+// Device counter of algorithmic bytes the solve phases move while a profile records
+// (null otherwise); allocated on the first profile_begin.
+unsigned long long* profile_bytes_counter();
+std::uint64_t profile_bytes_exchange();
 
 bool profile_begin(int family);
 // Synchronises the recorded events; returns false if no profile was active.

@@ -10,6 +10,7 @@
 
 #include "kernels.hpp"
 #include "krylov.hpp"
+#include "persistent.hpp"
 #include "profile.hpp"
 
 #include <algorithm>
@@ -302,6 +303,8 @@ std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* ar
     b.partial = b.store.alloc<double>(std::size_t(F.tiles) * 8);
     b.ticket = b.store.alloc<unsigned>(I);
     PSGB_CUDA(cudaMemset(b.ticket, 0, I * sizeof(unsigned)));
+    b.sync = b.store.alloc<unsigned>(4);
+    PSGB_CUDA(cudaMemset(b.sync, 0, 4 * sizeof(unsigned)));
     b.tile_begin = b.store.upload(tile_begin);
     b.scalars = b.store.alloc<InstanceScalars>(I);
     PSGB_CUDA(cudaMemset(b.scalars, 0, I * sizeof(InstanceScalars)));
@@ -330,7 +333,8 @@ std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* ar
 
 template <typename T>
 static LevelView<T> make_view(const BatchLevel& L, const T* vd, const T* inv) {
-    return LevelView<T>{L.rows, L.width, L.tiles, L.col, vd, inv, L.tile_inst, L.tile_rows, L.tile_sweep};
+    return LevelView<T>{L.rows, L.width, L.tiles, L.col, vd, inv, L.tile_inst, L.tile_rows, L.tile_sweep,
+                        profile_bytes_counter()};
 }
 
 StepView step_view(const Batch& b) {
@@ -594,6 +598,52 @@ void krylov(Batch& b, const SolveOptions& opt, const T* rhs, T* x, double tol, c
     }
 }
 
+// Arguments of the persistent solve: the same vectors, views and scalars the kernel path
+// passes launch by launch.
+template <typename T>
+PersistentArgs<T> persistent_args(Batch& b, const SolveOptions& opt, const double* rhs, double* x, double inner_tol) {
+    PersistentArgs<T> a{};
+    a.depth = static_cast<int>(b.levels.size());
+    for (std::size_t l = 0; l < b.levels.size(); ++l) {
+        BatchLevel& L = b.levels[l];
+        a.level[l] = PersistentLevel<T>{Pick<T>::view(b, l), Pick<T>::x(L), Pick<T>::y(L), Pick<T>::bvec(L),
+                                        Pick<T>::r(L), L.member_offset, L.member, L.agg};
+        a.dense_at[l] = b.dense_at[l] ? 1 : 0;
+    }
+    a.dense = dense_view(b);
+    a.dense_inv = Pick<T>::inv(b.dense);
+    a.fine64 = view64(b, 0);
+    a.rhs64 = rhs;
+    a.x64 = x;
+    a.r64 = b.rr;
+    for (int k = 0; k < Batch::kVectors; ++k) a.k[k] = Pick<T>::k(b)[k];
+    a.ctx = reduce_ctx(b);
+    a.sc = b.scalars;
+    a.instances = b.instances;
+    a.active = b.active_mask ? b.active : nullptr;
+    a.tolerance = opt.tolerance;
+    a.inner_tolerance = inner_tol;
+    a.max_iterations = opt.max_iterations;
+    a.max_refinements = opt.max_refinements;
+    a.method = opt.method;
+    a.pre = b.smoother.pre;
+    a.post = b.smoother.post;
+    a.omega = static_cast<T>(b.smoother.omega);
+    a.starts_in_x = starts_in_x(b.smoother) ? 1 : 0;
+    a.sync = PersistentSync{b.sync, b.sync + 1, b.sync + 2};
+    return a;
+}
+
+// The automatic schedule is the kernel schedule: on GB300 its many resident blocks hide
+// the latency of the small per-tile phases better than one 1024-thread block per SM.
+bool use_persistent(const Batch& b, const SolveOptions& opt) {
+    if (opt.schedule != kSchedulePersistent) return false;
+    if (b.levels.size() > static_cast<std::size_t>(kMaxLevels))
+        throw std::invalid_argument("persistent schedule: hierarchy deeper than 12 levels");
+    if (!persistent_supported()) throw std::runtime_error("persistent schedule: the device cannot run it");
+    return true;
+}
+
 }  // namespace
 
 void solve(Batch& b, const SolveOptions& opt, const double* rhs, double* x, cudaStream_t caller) {
@@ -607,11 +657,22 @@ void solve(Batch& b, const SolveOptions& opt, const double* rhs, double* x, cuda
     }
     const LevelView<double> lv64 = view64(b, 0);
     const ReduceCtx ctx = reduce_ctx(b);
-    launch_outer_init(lv64, rhs, ctx, opt.tolerance, opt.max_refinements, b.active_mask ? b.active : nullptr, st);
+    const bool persistent = use_persistent(b, opt);
     // Inner target: max(inner_tol * ||r||, tolerance * ||b|| / 2); the plain FP64 solve
     // reaches the outer target in one refinement, the mixed one in a few.
     const double inner_tol = opt.precision == kMixed ? opt.inner_tolerance : 1e-3 * opt.tolerance;
-    for (int refine = 0; refine <= opt.max_refinements; ++refine) {
+    if (!persistent) {
+        launch_outer_init(lv64, rhs, ctx, opt.tolerance, opt.max_refinements, b.active_mask ? b.active : nullptr, st);
+    } else {
+        // The whole refinement loop in one cooperative launch (outer_init included).
+        PSGB_CUDA(cudaMemsetAsync(b.sync, 0, 4 * sizeof(unsigned), st));
+        if (opt.precision == kMixed) {
+            launch_persistent<float>(persistent_args<float>(b, opt, rhs, x, inner_tol), st, b.stream != nullptr);
+        } else {
+            launch_persistent<double>(persistent_args<double>(b, opt, rhs, x, inner_tol), st, b.stream != nullptr);
+        }
+    }
+    for (int refine = 0; !persistent && refine <= opt.max_refinements; ++refine) {
         if (opt.precision == kMixed) {
             launch_outer_residual<float>(lv64, rhs, x, b.rr, b.k32[8], ctx, opt.max_refinements, st);
         } else {
@@ -628,7 +689,14 @@ void solve(Batch& b, const SolveOptions& opt, const double* rhs, double* x, cuda
     }
     InstanceScalars* host = b.pinned_scalars != nullptr ? b.pinned_scalars : b.host_scalars.data();
     PSGB_CUDA(cudaMemcpyAsync(host, b.scalars, b.instances * sizeof(InstanceScalars), cudaMemcpyDeviceToHost, st));
+    unsigned barrier_error = 0;
+    if (persistent) {
+        PSGB_CUDA(cudaMemcpyAsync(&barrier_error, b.sync + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    }
     PSGB_CUDA(cudaStreamSynchronize(st));
+    if (barrier_error != 0) {
+        throw std::runtime_error("persistent solve: a grid-barrier wait ran past its iteration limit");
+    }
     if (host != b.host_scalars.data()) {
         std::memcpy(b.host_scalars.data(), host, b.instances * sizeof(InstanceScalars));
     }

@@ -11,6 +11,7 @@ namespace psgb {
 
 enum Precision : int { kFP64 = 0, kMixed = 1 };
 enum Method : int { kPCG = 0, kBiCGSTAB = 1 };
+enum Schedule : int { kScheduleAuto = 0, kScheduleKernels = 1, kSchedulePersistent = 2 };
 
 struct SolveOptions {
     int precision = kFP64;
@@ -20,6 +21,7 @@ struct SolveOptions {
     int max_iterations = 1000;         // Krylov iterations per inner solve
     int max_refinements = 20;
     int poll = 4;                      // Krylov iterations between status reads
+    int schedule = kScheduleAuto;      // persistent kernel or one kernel per phase
 };
 
 // Host-side mesh, graph and hierarchy; no device memory is touched.

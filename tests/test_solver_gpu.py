@@ -192,3 +192,52 @@ def test_cap_and_non_finite_are_reported(meshes):
     # the planet stays usable after a failed step
     _, _, rep = pg.transport_step(m, inp.t0, inp.source, inp.heat_capacity, inp.dt, inp.conductance)
     assert rep.status == 0
+
+
+@pytest.mark.parametrize("precision,method", VARIANTS)
+def test_persistent_schedule_equals_kernel_schedule(meshes, precision, method):
+    """The one-launch persistent solve runs the same per-tile phases as the kernel-per-phase
+    schedule: every planet's result, iteration count and refinement count are identical,
+    for all planets and for a masked subset (continuous batching)."""
+    import planet_game_gb300 as pg
+    from planet_game_gb300 import workloads as W
+
+    specs = [(6, 8.1e6), (4, 3.3e6), (5, 6.0e6), (3, 7.0e6), (7, 5.0e6)]
+    ms = [meshes(l, r) for l, r in specs]
+    inputs = [W.step_inputs(m, seed=20 + i, edge_diffusivity=W.lognormal_edge_diffusivity(m.edge_count, 200 + i))
+              for i, m in enumerate(ms)]
+    batch = pg.Batch(ms)
+    for active in (None, [True, False, True, False, True]):
+        got = {}
+        for schedule in ("kernels", "persistent"):
+            got[schedule] = batch.transport_step(
+                [i.t0 for i in inputs], [i.source for i in inputs], 4e7, inputs[0].dt,
+                edge_conductance=[i.edge_conductance for i in inputs], precision=precision, method=method,
+                schedule=schedule, active=active)
+        (ko, kr), (po, pr) = got["kernels"], got["persistent"]
+        for i in range(len(ms)):
+            if active is not None and not active[i]:
+                continue
+            assert pr[i].status == 0 and pr[i].relative_residual <= 1e-10 and pr[i].closure <= 1e-12
+            assert (pr[i].iterations, pr[i].refinements) == (kr[i].iterations, kr[i].refinements)
+            assert np.array_equal(po[i], ko[i])
+
+
+def test_persistent_schedule_reports_cap_and_non_finite(meshes):
+    import planet_game_gb300 as pg
+    from planet_game_gb300 import capi
+    from planet_game_gb300 import workloads as W
+
+    m = meshes(5)
+    inp = W.step_inputs(m, seed=0)
+    _, _, rep = pg.transport_step(m, inp.t0, inp.source, inp.heat_capacity, inp.dt, inp.conductance,
+                                  max_iterations=1, max_refinements=1, schedule="persistent")
+    assert rep.status == capi.ERR_NOT_CONVERGED
+    bad = inp.t0.copy()
+    bad[17] = np.nan
+    with pytest.raises(capi.GB300Error) as err:
+        pg.transport_step(m, bad, inp.source, inp.heat_capacity, inp.dt, inp.conductance, schedule="persistent")
+    assert err.value.code == capi.ERR_NON_FINITE
+    _, _, rep = pg.transport_step(m, inp.t0, inp.source, inp.heat_capacity, inp.dt, inp.conductance,
+                                  schedule="persistent")
+    assert rep.status == 0
