@@ -14,10 +14,39 @@
 
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <stdexcept>
+#include <string>
+#include <utility>
 
 namespace psgb {
 
 constexpr int kTile = 256;
+
+// Programmatic dependent launch. Solve kernels run back to back on one stream, each
+// short; launched with launch_pdl, a kernel's blocks may be scheduled while its
+// predecessor drains. Every such kernel starts with pdl_begin(): it waits until the
+// predecessor grid has completed and its writes are visible (so nothing is read early),
+// then allows the successor to be scheduled.
+__device__ __forceinline__ void pdl_begin() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... P, typename... A>
+inline void launch_pdl(void (*kernel)(P...), dim3 grid, dim3 block, cudaStream_t st, A&&... args) {
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
+    if (e != cudaSuccess) throw std::runtime_error(std::string("kernel launch: ") + cudaGetErrorString(e));
+}
 
 // Warp-level sum in a fixed butterfly order (result valid in every lane).
 template <typename T>

@@ -64,6 +64,19 @@ struct DenseView {
     const std::int64_t* row_base;     // row base per planet at its coarsest level
 };
 
+// Coarsest-level solves x = A^-1 b of the planets whose coarsest level is one level:
+// `count` blocks of eight rows, (planet, first row) each; one warp per row. A launch on
+// that level (smoothing of the other planets) may carry them in extra blocks.
+template <typename T>
+struct DenseTask {
+    DenseView dense;
+    const int2* blocks;
+    std::uint32_t count;              // 0: no dense work
+    const T* inv;
+    const T* b;
+    T* x;
+};
+
 // ---- multigrid.cu ---------------------------------------------------------
 // Fine-level matrix of the implicit heat step (heat_transport.cpp:351-363):
 // diag = A/s + K Σw (s > 0) else 1; off = -K w where both ends are free.
@@ -88,10 +101,10 @@ void launch_smooth_zero(const LevelView<T>& lv, const T* b, T* x, T omega, const
                         int gate, cudaStream_t stream);
 template <typename T>
 void launch_smooth(const LevelView<T>& lv, const T* b, const T* x, T* y, T omega,
-                   const InstanceScalars* sc, int gate, cudaStream_t stream);
+                   const InstanceScalars* sc, int gate, cudaStream_t stream, const DenseTask<T>& dense = {});
 template <typename T>
 void launch_residual(const LevelView<T>& lv, const T* b, const T* x, T* r, const InstanceScalars* sc,
-                     int gate, cudaStream_t stream);
+                     int gate, cudaStream_t stream, const DenseTask<T>& dense = {});
 template <typename T>
 void launch_restrict(const LevelView<T>& coarse, const std::uint32_t* member_offset,
                      const std::uint32_t* member, const T* r, T* bc, const InstanceScalars* sc,
@@ -107,8 +120,7 @@ template <typename T>
 void launch_prolong(const LevelView<T>& fine, const std::int32_t* agg, const T* xc, T* x,
                     const InstanceScalars* sc, int gate, cudaStream_t stream);
 template <typename T>
-void launch_dense_solve(const DenseView& dense, int level, std::uint32_t max_rows, const T* inv,
-                        const T* b, T* x, const InstanceScalars* sc, int gate, cudaStream_t stream);
+void launch_dense_solve(const DenseTask<T>& dense, const InstanceScalars* sc, int gate, cudaStream_t stream);
 template <typename T>
 void launch_spmv(const LevelView<T>& lv, const T* x, T* y, cudaStream_t stream);
 

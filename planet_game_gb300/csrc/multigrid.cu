@@ -27,6 +27,7 @@ __global__ void k_assemble_transport(LevelView<double> lv, const double* __restr
                                      const double* __restrict__ conductance,
                                      const double* __restrict__ edge_conductance,
                                      double* __restrict__ vd) {
+    pdl_begin();
     const int tile = blockIdx.x;
     const int row = tile * kTile + threadIdx.x;
     const std::uint32_t P = lv.rows, W = lv.width;
@@ -64,6 +65,7 @@ __global__ void k_set_matrix_csr(std::uint32_t n, std::uint32_t P, std::uint32_t
                                  const std::uint32_t* __restrict__ off_begin,
                                  const double* __restrict__ diag, const double* __restrict__ off,
                                  double* __restrict__ vd) {
+    pdl_begin();
     const std::uint32_t row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= P) return;
     if (row >= n) {
@@ -82,6 +84,7 @@ __global__ void k_set_matrix_csr(std::uint32_t n, std::uint32_t P, std::uint32_t
 __global__ void k_galerkin(std::uint32_t lists, const std::uint32_t* __restrict__ offset,
                            const std::uint32_t* __restrict__ source, const double* __restrict__ fine,
                            double* __restrict__ coarse) {
+    pdl_begin();
     const std::uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= lists) return;
     double sum = 0.0;
@@ -92,6 +95,7 @@ __global__ void k_galerkin(std::uint32_t lists, const std::uint32_t* __restrict_
 __global__ void k_finalize_level(std::uint32_t P, std::uint32_t W, double* __restrict__ vd64,
                                  float* __restrict__ vd32, double* __restrict__ inv64,
                                  float* __restrict__ inv32) {
+    pdl_begin();
     const std::uint32_t row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= P) return;
     double d = vd64[W * P + row];
@@ -113,6 +117,7 @@ __global__ void __launch_bounds__(1024) k_dense_invert(DenseView dense, int leve
                                                        double* __restrict__ work,
                                                        double* __restrict__ inv64,
                                                        float* __restrict__ inv32) {
+    pdl_begin();
     const int inst = blockIdx.x;
     if (dense.level[inst] != level) return;
     const int n = static_cast<int>(dense.size[inst]);
@@ -160,23 +165,35 @@ __global__ void __launch_bounds__(1024) k_dense_invert(DenseView dense, int leve
 template <typename T>
 __global__ void k_smooth_zero(LevelView<T> lv, const T* __restrict__ b, T* __restrict__ x, T omega,
                               const InstanceScalars* sc, int gate) {
+    pdl_begin();
     ph::smooth_zero<T>(lv, blockIdx.x, threadIdx.x, b, x, omega, sc, gate);
 }
 
 template <typename T, int W>
 __global__ void k_smooth(LevelView<T> lv, const T* __restrict__ b, const T* __restrict__ x, T* __restrict__ y,
-                         T omega, const InstanceScalars* sc, int gate) {
+                         T omega, const InstanceScalars* sc, int gate, DenseTask<T> dense) {
+    pdl_begin();
+    if (blockIdx.x >= lv.tiles) {
+        ph::dense_block<T>(dense, blockIdx.x - lv.tiles, threadIdx.x, sc, gate);
+        return;
+    }
     ph::smooth<T, W>(lv, blockIdx.x, threadIdx.x, b, x, y, omega, sc, gate);
 }
 
 template <typename T, int W>
 __global__ void k_residual(LevelView<T> lv, const T* __restrict__ b, const T* __restrict__ x, T* __restrict__ r,
-                           const InstanceScalars* sc, int gate) {
+                           const InstanceScalars* sc, int gate, DenseTask<T> dense) {
+    pdl_begin();
+    if (blockIdx.x >= lv.tiles) {
+        ph::dense_block<T>(dense, blockIdx.x - lv.tiles, threadIdx.x, sc, gate);
+        return;
+    }
     ph::residual<T, W>(lv, blockIdx.x, threadIdx.x, b, x, r, sc, gate);
 }
 
 template <typename T, int W>
 __global__ void k_spmv(LevelView<T> lv, const T* __restrict__ x, T* __restrict__ y) {
+    pdl_begin();
     ph::spmv<T, W>(lv, blockIdx.x, threadIdx.x, x, y);
 }
 
@@ -184,6 +201,7 @@ template <typename T>
 __global__ void k_restrict(LevelView<T> coarse, const std::uint32_t* __restrict__ moff,
                            const std::uint32_t* __restrict__ member, const T* __restrict__ r, T* __restrict__ bc,
                            const InstanceScalars* sc, int gate) {
+    pdl_begin();
     ph::restrict_only<T>(coarse, blockIdx.x, threadIdx.x, moff, member, r, bc, sc, gate);
 }
 
@@ -192,6 +210,7 @@ __global__ void k_restrict_zero(LevelView<T> coarse, const std::uint32_t* __rest
                                 const std::uint32_t* __restrict__ member, const T* __restrict__ r,
                                 T* __restrict__ bc, T* __restrict__ xc, T omega, const InstanceScalars* sc,
                                 int gate) {
+    pdl_begin();
     ph::restrict_zero<T>(coarse, blockIdx.x, threadIdx.x, moff, member, r, bc, xc, omega, sc, gate);
 }
 
@@ -199,26 +218,22 @@ template <typename T, int W>
 __global__ void k_prolong_smooth(LevelView<T> lv, const std::int32_t* __restrict__ agg,
                                  const T* __restrict__ e, const T* __restrict__ b, const T* __restrict__ x,
                                  T* __restrict__ y, T omega, const InstanceScalars* sc, int gate) {
+    pdl_begin();
     ph::prolong_smooth<T, W>(lv, blockIdx.x, threadIdx.x, agg, e, b, x, y, omega, sc, gate);
 }
 
 template <typename T>
 __global__ void k_prolong(LevelView<T> lv, const std::int32_t* __restrict__ agg, const T* __restrict__ xc,
                           T* __restrict__ x, const InstanceScalars* sc, int gate) {
+    pdl_begin();
     ph::prolong<T>(lv, blockIdx.x, threadIdx.x, agg, xc, x, sc, gate);
 }
 
-// Coarsest level: x = A^-1 b, one warp per row.
+// Coarsest level: x = A^-1 b, one warp per row, eight rows per block.
 template <typename T>
-__global__ void k_dense_solve(DenseView dense, int level, const T* __restrict__ inv,
-                              const T* __restrict__ b, T* __restrict__ x, const InstanceScalars* sc,
-                              int gate) {
-    const int inst = blockIdx.y;
-    if (dense.level[inst] != level) return;
-    if (!ph::gate_open(sc, inst, gate)) return;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (warp >= static_cast<int>(dense.size[inst])) return;
-    ph::dense_row<T>(dense, inst, warp, threadIdx.x & 31, inv, b, x);
+__global__ void k_dense_solve(DenseTask<T> dense, const InstanceScalars* sc, int gate) {
+    pdl_begin();
+    ph::dense_block<T>(dense, blockIdx.x, threadIdx.x, sc, gate);
 }
 
 inline dim3 tiles_grid(std::uint32_t tiles) { return dim3(tiles); }
@@ -231,56 +246,59 @@ inline dim3 tiles_grid(std::uint32_t tiles) { return dim3(tiles); }
 void launch_assemble_transport(const LevelView<double>& fine, const double* w, const double* wsum,
                                const double* area, const double* slope, const double* conductance,
                                const double* edge_conductance, double* vd, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamSetup, stream, k_assemble_transport<<<fine.tiles, kTile, 0, stream>>>(fine, w, wsum, area, slope, conductance,
+    PSGB_LAUNCH(kFamSetup, stream, launch_pdl(k_assemble_transport, fine.tiles, kTile, stream, fine, w, wsum, area, slope, conductance,
                                                           edge_conductance, vd));
 }
 
 void launch_set_matrix_csr(std::uint32_t n, std::uint32_t rows, std::uint32_t width,
                            const std::uint32_t* csr_offset, const double* diag, const double* off,
                            double* vd, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamSetup, stream, k_set_matrix_csr<<<(rows + 255) / 256, 256, 0, stream>>>(n, rows, width, csr_offset, diag, off, vd));
+    PSGB_LAUNCH(kFamSetup, stream, launch_pdl(k_set_matrix_csr, (rows + 255) / 256, 256, stream, n, rows, width, csr_offset, diag, off, vd));
 }
 
 void launch_galerkin(std::uint32_t lists, const std::uint32_t* offset, const std::uint32_t* source,
                      const double* fine_vd, double* coarse_vd, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamSetup, stream, k_galerkin<<<(lists + 255) / 256, 256, 0, stream>>>(lists, offset, source, fine_vd, coarse_vd));
+    PSGB_LAUNCH(kFamSetup, stream, launch_pdl(k_galerkin, (lists + 255) / 256, 256, stream, lists, offset, source, fine_vd, coarse_vd));
 }
 
 void launch_finalize_level(std::uint32_t rows, std::uint32_t width, double* vd64, float* vd32,
                            double* inv64, float* inv32, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamSetup, stream, k_finalize_level<<<(rows + 255) / 256, 256, 0, stream>>>(rows, width, vd64, vd32, inv64, inv32));
+    PSGB_LAUNCH(kFamSetup, stream, launch_pdl(k_finalize_level, (rows + 255) / 256, 256, stream, rows, width, vd64, vd32, inv64, inv32));
 }
 
 void launch_dense_invert(const DenseView& dense, int level, const LevelView<double>& lv,
                          double* work, double* inv64, float* inv32, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamSetup, stream, k_dense_invert<<<dense.instances, 1024, 0, stream>>>(dense, level, lv, work, inv64, inv32));
+    PSGB_LAUNCH(kFamSetup, stream, launch_pdl(k_dense_invert, dense.instances, 1024, stream, dense, level, lv, work, inv64, inv32));
 }
 
-#define PSGB_WIDTH_DISPATCH(width, KERNEL, ...)                                 \
-    switch (width) {                                                            \
-        case 6: KERNEL<T, 6><<<lv.tiles, kTile, 0, stream>>>(__VA_ARGS__); break; \
-        case 8: KERNEL<T, 8><<<lv.tiles, kTile, 0, stream>>>(__VA_ARGS__); break; \
-        case 12: KERNEL<T, 12><<<lv.tiles, kTile, 0, stream>>>(__VA_ARGS__); break; \
-        case 16: KERNEL<T, 16><<<lv.tiles, kTile, 0, stream>>>(__VA_ARGS__); break; \
-        default: throw std::logic_error("unsupported ELL width");               \
+#define PSGB_WIDTH_DISPATCH_GRID(width, grid, KERNEL, ...)                          \
+    switch (width) {                                                                \
+        case 6: launch_pdl(KERNEL<T, 6>, grid, kTile, stream, __VA_ARGS__); break;    \
+        case 8: launch_pdl(KERNEL<T, 8>, grid, kTile, stream, __VA_ARGS__); break;    \
+        case 12: launch_pdl(KERNEL<T, 12>, grid, kTile, stream, __VA_ARGS__); break;  \
+        case 16: launch_pdl(KERNEL<T, 16>, grid, kTile, stream, __VA_ARGS__); break;  \
+        default: throw std::logic_error("unsupported ELL width");                   \
     }
+#define PSGB_WIDTH_DISPATCH(width, KERNEL, ...) PSGB_WIDTH_DISPATCH_GRID(width, lv.tiles, KERNEL, __VA_ARGS__)
 
 template <typename T>
 void launch_smooth_zero(const LevelView<T>& lv, const T* b, T* x, T omega, const InstanceScalars* sc,
                         int gate, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamSmooth, stream, k_smooth_zero<T><<<lv.tiles, kTile, 0, stream>>>(lv, b, x, omega, sc, gate));
+    PSGB_LAUNCH(kFamSmooth, stream, launch_pdl(k_smooth_zero<T>, lv.tiles, kTile, stream, lv, b, x, omega, sc, gate));
 }
 
 template <typename T>
 void launch_smooth(const LevelView<T>& lv, const T* b, const T* x, T* y, T omega,
-                   const InstanceScalars* sc, int gate, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamSmooth, stream, PSGB_WIDTH_DISPATCH(lv.width, k_smooth, lv, b, x, y, omega, sc, gate));
+                   const InstanceScalars* sc, int gate, cudaStream_t stream, const DenseTask<T>& dense) {
+    PSGB_LAUNCH(kFamSmooth, stream,
+                PSGB_WIDTH_DISPATCH_GRID(lv.width, lv.tiles + dense.count, k_smooth, lv, b, x, y, omega, sc, gate, dense));
 }
 
 template <typename T>
 void launch_residual(const LevelView<T>& lv, const T* b, const T* x, T* r, const InstanceScalars* sc,
-                     int gate, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamResidual, stream, PSGB_WIDTH_DISPATCH(lv.width, k_residual, lv, b, x, r, sc, gate));
+                     int gate, cudaStream_t stream, const DenseTask<T>& dense) {
+    PSGB_LAUNCH(kFamResidual, stream,
+                PSGB_WIDTH_DISPATCH_GRID(lv.width, lv.tiles + dense.count, k_residual, lv, b, x, r, sc, gate, dense));
 }
 
 template <typename T>
@@ -292,14 +310,14 @@ template <typename T>
 void launch_restrict(const LevelView<T>& coarse, const std::uint32_t* member_offset,
                      const std::uint32_t* member, const T* r, T* bc, const InstanceScalars* sc,
                      int gate, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamRestrict, stream, k_restrict<T><<<coarse.tiles, kTile, 0, stream>>>(coarse, member_offset, member, r, bc, sc, gate));
+    PSGB_LAUNCH(kFamRestrict, stream, launch_pdl(k_restrict<T>, coarse.tiles, kTile, stream, coarse, member_offset, member, r, bc, sc, gate));
 }
 
 template <typename T>
 void launch_restrict_zero(const LevelView<T>& coarse, const std::uint32_t* member_offset,
                           const std::uint32_t* member, const T* r, T* bc, T* xc, T omega,
                           const InstanceScalars* sc, int gate, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamRestrict, stream, k_restrict_zero<T><<<coarse.tiles, kTile, 0, stream>>>(coarse, member_offset, member, r, bc, xc, omega, sc, gate));
+    PSGB_LAUNCH(kFamRestrict, stream, launch_pdl(k_restrict_zero<T>, coarse.tiles, kTile, stream, coarse, member_offset, member, r, bc, xc, omega, sc, gate));
 }
 
 template <typename T>
@@ -311,23 +329,22 @@ void launch_prolong_smooth(const LevelView<T>& lv, const std::int32_t* agg, cons
 template <typename T>
 void launch_prolong(const LevelView<T>& fine, const std::int32_t* agg, const T* xc, T* x,
                     const InstanceScalars* sc, int gate, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamProlong, stream, k_prolong<T><<<fine.tiles, kTile, 0, stream>>>(fine, agg, xc, x, sc, gate));
+    PSGB_LAUNCH(kFamProlong, stream, launch_pdl(k_prolong<T>, fine.tiles, kTile, stream, fine, agg, xc, x, sc, gate));
 }
 
 template <typename T>
-void launch_dense_solve(const DenseView& dense, int level, std::uint32_t max_rows, const T* inv,
-                        const T* b, T* x, const InstanceScalars* sc, int gate, cudaStream_t stream) {
-    const dim3 grid((max_rows * 32 + 255) / 256, dense.instances);
-    PSGB_LAUNCH(kFamDense, stream, k_dense_solve<T><<<grid, 256, 0, stream>>>(dense, level, inv, b, x, sc, gate));
+void launch_dense_solve(const DenseTask<T>& dense, const InstanceScalars* sc, int gate, cudaStream_t stream) {
+    if (dense.count == 0) return;
+    PSGB_LAUNCH(kFamDense, stream, launch_pdl(k_dense_solve<T>, dense.count, 256, stream, dense, sc, gate));
 }
 
 #define PSGB_INSTANTIATE(T)                                                                           \
     template void launch_smooth_zero<T>(const LevelView<T>&, const T*, T*, T, const InstanceScalars*, \
                                         int, cudaStream_t);                                           \
     template void launch_smooth<T>(const LevelView<T>&, const T*, const T*, T*, T,                     \
-                                   const InstanceScalars*, int, cudaStream_t);                        \
+                                   const InstanceScalars*, int, cudaStream_t, const DenseTask<T>&);   \
     template void launch_residual<T>(const LevelView<T>&, const T*, const T*, T*,                      \
-                                     const InstanceScalars*, int, cudaStream_t);                      \
+                                     const InstanceScalars*, int, cudaStream_t, const DenseTask<T>&); \
     template void launch_spmv<T>(const LevelView<T>&, const T*, T*, cudaStream_t);                     \
     template void launch_restrict<T>(const LevelView<T>&, const std::uint32_t*, const std::uint32_t*,  \
                                      const T*, T*, const InstanceScalars*, int, cudaStream_t);        \
@@ -337,8 +354,7 @@ void launch_dense_solve(const DenseView& dense, int level, std::uint32_t max_row
                                            const T*, T*, T, const InstanceScalars*, int, cudaStream_t);    \
     template void launch_prolong<T>(const LevelView<T>&, const std::int32_t*, const T*, T*,            \
                                     const InstanceScalars*, int, cudaStream_t);                       \
-    template void launch_dense_solve<T>(const DenseView&, int, std::uint32_t, const T*, const T*, T*,  \
-                                        const InstanceScalars*, int, cudaStream_t);
+    template void launch_dense_solve<T>(const DenseTask<T>&, const InstanceScalars*, int, cudaStream_t);
 
 PSGB_INSTANTIATE(float)
 PSGB_INSTANTIATE(double)

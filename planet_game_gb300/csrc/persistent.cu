@@ -124,16 +124,17 @@ template <typename T>
 using Args = PersistentArgs<T>;
 
 // Coarsest-level solves of the planets whose coarsest level is `level`: one warp per row,
-// warps spread over the whole grid.
+// the rows of the level's dense blocks spread over all warps of the grid.
 template <typename T>
 __device__ void dense_phase(const Args<T>& a, int level, const T* b, T* x, int gate) {
-    const int warp = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    const int warps = static_cast<int>((gridDim.x * blockDim.x) >> 5);
-    for (unsigned inst = 0; inst < a.instances; ++inst) {
-        if (a.dense.level[inst] != level || !ph::gate_open(a.sc, static_cast<int>(inst), gate)) continue;
-        const int n = static_cast<int>(a.dense.size[inst]);
-        for (int row = warp; row < n; row += warps)
-            ph::dense_row<T>(a.dense, static_cast<int>(inst), row, static_cast<int>(threadIdx.x & 31), a.dense_inv, b, x);
+    const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned warps = (gridDim.x * blockDim.x) >> 5;
+    const unsigned begin = a.dense_block_offset[level], rows = (a.dense_block_offset[level + 1] - begin) * 8u;
+    for (unsigned k = warp; k < rows; k += warps) {
+        const int2 blk = a.dense_blocks[begin + k / 8u];
+        const int row = blk.y + static_cast<int>(k % 8u);
+        if (row >= static_cast<int>(a.dense.size[blk.x]) || !ph::gate_open(a.sc, blk.x, gate)) continue;
+        ph::dense_row<T>(a.dense, blk.x, row, static_cast<int>(threadIdx.x & 31), a.dense_inv, b, x);
     }
 }
 
@@ -167,13 +168,19 @@ __device__ bool vcycle(const Args<T>& a, const T* rhs, T* x, int gate) {
         const LevelView<T>& lv = L.view;
         const T* b = l == 0 ? rhs : L.b;
         Pair<T> p = pair_of(a, l, x);
+        // Planets whose coarsest level is this one (l >= 1) solve it in the level's first
+        // phase: they do not smooth here, the others do not need them yet.
+        bool dense = l > 0 && a.dense_at[l];
         for (int k = 1; k < a.pre; ++k) {
+            if (dense) dense_phase<T>(a, l, L.b, L.x, gate);
+            dense = false;
             with_width(lv.width, [&](auto W) {
                 PSGB_TILES(lv, G) ph::smooth<T, decltype(W)::value>(lv, tile, G.lane, b, p.first, p.second, omega, a.sc, gate);
             });
             PSGB_BARRIER(a);
             T* t = p.first; p.first = p.second; p.second = t;
         }
+        if (dense) dense_phase<T>(a, l, L.b, L.x, gate);
         with_width(lv.width, [&](auto W) {
             PSGB_TILES(lv, G) ph::residual<T, decltype(W)::value>(lv, tile, G.lane, b, p.first, L.r, a.sc, gate);
         });
@@ -182,7 +189,7 @@ __device__ bool vcycle(const Args<T>& a, const T* rhs, T* x, int gate) {
         const Pair<T> pc = pair_of(a, l + 1, x);
         PSGB_TILES(C.view, G) ph::restrict_zero<T>(C.view, tile, G.lane, L.member_offset, L.member, L.r, C.b, pc.first, omega, a.sc, gate);
         PSGB_BARRIER(a);
-        if (a.dense_at[l + 1]) {
+        if (l + 2 == a.depth && a.dense_at[l + 1]) {
             dense_phase<T>(a, l + 1, C.b, C.x, gate);
             PSGB_BARRIER(a);
         }

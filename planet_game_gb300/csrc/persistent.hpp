@@ -39,6 +39,8 @@ struct PersistentArgs {
     int depth;
     DenseView dense;
     const T* dense_inv;
+    const int2* dense_blocks;           // blocks of eight coarsest rows, (planet, first row)
+    unsigned dense_block_offset[kMaxLevels + 1];   // per level, into dense_blocks
     LevelView<double> fine64;           // FP64 fine matrix (refinement residual)
     const double* rhs64;
     double* x64;

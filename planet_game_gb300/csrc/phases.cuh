@@ -104,6 +104,25 @@ __device__ __forceinline__ bool finite(double v) { return isfinite(v); }
 
 // ---- V-cycle phases ---------------------------------------------------------------------
 
+// Sum of r over an aggregate's members, in ascending member order (the reference's
+// order). The gathers are issued eight at a time so that they are in flight together;
+// the additions stay sequential, so the sum is the same as the plain loop's.
+template <typename T>
+__device__ __forceinline__ T member_sum(const std::uint32_t* PSGB_PHASE_RESTRICT member, std::uint32_t k0,
+                                        std::uint32_t k1, const T* PSGB_PHASE_RESTRICT r) {
+    T s = T(0);
+    for (std::uint32_t k = k0; k < k1; k += 8) {
+        T v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = (k + j < k1) ? r[member[k + j]] : T(0);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            if (k + j < k1) s += v[j];
+        }
+    }
+    return s;
+}
+
 template <typename T>
 __device__ void smooth_zero(const LevelView<T>& lv, int tile, int lane, const T* PSGB_PHASE_RESTRICT b, T* PSGB_PHASE_RESTRICT x,
                             T omega, const InstanceScalars* sc, int gate) {
@@ -167,8 +186,7 @@ __device__ void restrict_zero(const LevelView<T>& coarse, int tile, int lane, co
     if (!gate_open(sc, coarse.tile_inst[tile], gate)) return;
     if (lane >= rows) return;
     const int row = tile * kTile + lane;
-    T s = T(0);
-    for (std::uint32_t k = moff[row]; k < moff[row + 1]; ++k) s += r[member[k]];
+    const T s = member_sum(member, moff[row], moff[row + 1], r);
     bc[row] = s;
     if (coarse.tile_sweep[tile]) xc[row] = omega * coarse.inv[row] * s;
 }
@@ -180,9 +198,7 @@ __device__ void restrict_only(const LevelView<T>& coarse, int tile, int lane, co
     if (lane >= coarse.tile_rows[tile]) return;
     if (!gate_open(sc, coarse.tile_inst[tile], gate)) return;
     const int row = tile * kTile + lane;
-    T s = T(0);
-    for (std::uint32_t k = moff[row]; k < moff[row + 1]; ++k) s += r[member[k]];
-    bc[row] = s;
+    bc[row] = member_sum(member, moff[row], moff[row + 1], r);
 }
 
 // Prolongation fused with the first post-smoothing sweep: with x' = x + e[agg] (formed on
@@ -227,6 +243,16 @@ __device__ void dense_row(const DenseView& dense, int inst, int rowi, int lane32
     for (int j = lane32; j < n; j += 32) s += a[j] * b[base + j];
     s = warp_sum(s);
     if (lane32 == 0) x[base + rowi] = s;
+}
+
+// Block k of a dense task: eight rows of one planet, one warp per row (256 threads).
+template <typename T>
+__device__ void dense_block(const DenseTask<T>& task, unsigned k, int lane, const InstanceScalars* sc, int gate) {
+    const int2 blk = task.blocks[k];
+    if (!gate_open(sc, blk.x, gate)) return;
+    const int row = blk.y + (lane >> 5);
+    if (row >= static_cast<int>(task.dense.size[blk.x])) return;
+    dense_row<T>(task.dense, blk.x, row, lane & 31, task.inv, task.b, task.x);
 }
 
 // ---- Krylov phases (fine level) ----------------------------------------------------------

@@ -152,6 +152,9 @@ struct DenseCoarse {
     std::vector<std::uint32_t> size;
     std::vector<std::int64_t> row_base;
     std::uint32_t max_rows = 0;
+    // per level: blocks of eight coarsest rows, (planet, first row), for the dense solves
+    std::vector<std::uint32_t> block_offset;   // [levels + 1] into d_blocks
+    int2* d_blocks = nullptr;
     double* inv64 = nullptr;           // concatenated row-major inverses
     float* inv32 = nullptr;
     double* work = nullptr;

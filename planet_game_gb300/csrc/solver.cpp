@@ -258,6 +258,17 @@ std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* ar
     }
     b.dense_at.assign(depth, 0);
     for (std::uint32_t i = 0; i < I; ++i) b.dense_at[static_cast<std::size_t>(D.level[i])] = 1;
+    std::vector<int2> blocks;
+    D.block_offset.assign(depth + 1, 0);
+    for (std::size_t l = 0; l < depth; ++l) {
+        D.block_offset[l] = static_cast<std::uint32_t>(blocks.size());
+        for (std::uint32_t i = 0; i < I; ++i) {
+            if (D.level[i] != static_cast<int>(l)) continue;
+            for (std::uint32_t r = 0; r < D.size[i]; r += 8) blocks.push_back(int2{static_cast<int>(i), static_cast<int>(r)});
+        }
+    }
+    D.block_offset[depth] = static_cast<std::uint32_t>(blocks.size());
+    D.d_blocks = b.store.upload(blocks);
     D.inv64 = b.store.alloc<double>(total);
     D.inv32 = b.store.alloc<float>(total);
     D.work = b.store.alloc<double>(total);
@@ -383,6 +394,14 @@ DenseView dense_view(const Batch& b) {
     return DenseView{b.instances, D.d_level, D.d_offset, D.d_size, D.d_row_base};
 }
 
+// The dense solves of the planets whose coarsest level is `level`.
+template <typename T>
+DenseTask<T> dense_task(Batch& b, std::size_t level, const T* rhs, T* x) {
+    const DenseCoarse& D = b.dense;
+    const std::uint32_t begin = D.block_offset[level], end = D.block_offset[level + 1];
+    return DenseTask<T>{dense_view(b), D.d_blocks + begin, end - begin, Pick<T>::inv(D), rhs, x};
+}
+
 }  // namespace
 
 void assemble_transport(Batch& b, const double* slope, const double* conductance,
@@ -435,7 +454,6 @@ void vcycle(Batch& b, const T* rhs, T* x, int gate, bool first_sweep_done, cudaS
     const std::size_t depth = b.levels.size();
     const SmootherConfig& sm = b.smoother;
     const T omega = static_cast<T>(sm.omega);
-    const DenseView dv = dense_view(b);
     std::vector<T*> cur(depth), other(depth);
     std::vector<const T*> rhs_of(depth);
     for (std::size_t l = 0; l < depth; ++l) {
@@ -447,26 +465,29 @@ void vcycle(Batch& b, const T* rhs, T* x, int gate, bool first_sweep_done, cudaS
         rhs_of[l] = (l == 0) ? rhs : Pick<T>::bvec(L);
     }
     // Planets whose only level is the fine one: dense solve there.
-    if (b.dense_at[0]) {
-        launch_dense_solve<T>(dv, 0, b.dense.max_rows, Pick<T>::inv(b.dense), rhs, x, b.scalars, gate, st);
-    }
+    if (b.dense_at[0]) launch_dense_solve<T>(dense_task<T>(b, 0, rhs, x), b.scalars, gate, st);
     // Down: pre-smoothing, residual, restriction fused with the next level's first sweep.
     for (std::size_t l = 0; l + 1 < depth; ++l) {
         const LevelView<T> lv = Pick<T>::view(b, l);
         BatchLevel& L = b.levels[l];
+        // Planets whose coarsest level is this one (l >= 1) solve it in extra blocks of the
+        // level's first launch: they do not smooth here, the others do not need them yet.
+        DenseTask<T> dense{};
+        if (l > 0 && b.dense_at[l]) dense = dense_task<T>(b, l, Pick<T>::bvec(L), Pick<T>::x(L));
         if (l == 0 && !first_sweep_done) launch_smooth_zero<T>(lv, rhs_of[l], cur[l], omega, b.scalars, gate, st);
         for (int k = 1; k < sm.pre; ++k) {
-            launch_smooth<T>(lv, rhs_of[l], cur[l], other[l], omega, b.scalars, gate, st);
+            launch_smooth<T>(lv, rhs_of[l], cur[l], other[l], omega, b.scalars, gate, st, dense);
+            dense = DenseTask<T>{};
             std::swap(cur[l], other[l]);
         }
-        launch_residual<T>(lv, rhs_of[l], cur[l], Pick<T>::r(L), b.scalars, gate, st);
+        launch_residual<T>(lv, rhs_of[l], cur[l], Pick<T>::r(L), b.scalars, gate, st, dense);
         BatchLevel& C = b.levels[l + 1];
         const LevelView<T> cv = Pick<T>::view(b, l + 1);
         launch_restrict_zero<T>(cv, L.member_offset, L.member, Pick<T>::r(L), Pick<T>::bvec(C), cur[l + 1], omega,
                                 b.scalars, gate, st);
-        if (b.dense_at[l + 1]) {
-            launch_dense_solve<T>(dv, static_cast<int>(l + 1), b.dense.max_rows, Pick<T>::inv(b.dense),
-                                  Pick<T>::bvec(C), Pick<T>::x(C), b.scalars, gate, st);
+        // The deepest level has no smoothing launch: its dense solves run on their own.
+        if (l + 2 == depth && b.dense_at[l + 1]) {
+            launch_dense_solve<T>(dense_task<T>(b, l + 1, Pick<T>::bvec(C), Pick<T>::x(C)), b.scalars, gate, st);
         }
     }
     // Up: prolongation fused with the first post-smoothing sweep.
@@ -612,6 +633,8 @@ PersistentArgs<T> persistent_args(Batch& b, const SolveOptions& opt, const doubl
     }
     a.dense = dense_view(b);
     a.dense_inv = Pick<T>::inv(b.dense);
+    a.dense_blocks = b.dense.d_blocks;
+    for (std::size_t l = 0; l <= b.levels.size(); ++l) a.dense_block_offset[l] = b.dense.block_offset[l];
     a.fine64 = view64(b, 0);
     a.rhs64 = rhs;
     a.x64 = x;
