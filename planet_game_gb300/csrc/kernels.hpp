@@ -23,6 +23,12 @@ struct InstanceScalars {
     int first;           // PCG: first iteration
 };
 
+// Tile word: planet (bits 0-21), valid rows 0..256 (bits 22-30), smooths here (bit 31).
+constexpr std::uint32_t kMaxInstances = 1u << 22;
+inline constexpr std::uint32_t pack_tile(std::int32_t inst, std::int32_t rows, bool sweep) {
+    return static_cast<std::uint32_t>(inst) | (static_cast<std::uint32_t>(rows) << 22) | (sweep ? 0x80000000u : 0u);
+}
+
 enum Status : int { kRunning = 0, kConverged = 1, kBreakdown = 2, kNonFinite = 3, kCap = 4 };
 
 // Gates: which planets a launch works for.
@@ -46,7 +52,10 @@ struct LevelView {
     const std::int32_t* tile_inst;
     const std::int32_t* tile_rows;    // valid rows per tile
     const std::uint8_t* tile_sweep;   // 1: the tile's planet smooths on this level
+    const std::uint32_t* tile_meta;   // the three above in one word (pack_tile), padded to 4 tiles
     unsigned long long* bytes;        // algorithmic-byte counter while profiling, else null
+    std::uint8_t sets_stencil;        // tiles per tile set of the stencil launches (1 or 2)
+    std::uint8_t sets_vector;         // tiles per tile set of the vector launches (1 or 4)
 };
 
 struct ReduceCtx {

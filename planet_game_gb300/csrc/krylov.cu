@@ -23,99 +23,100 @@ namespace {
 
 // One 256-thread block per tile: the shared phases of phases.cuh.
 
-template <typename T>
+template <typename T, int R>
 __global__ void k_bicg_init(LevelView<T> lv, const T* __restrict__ b, T* x, T* r, T* shadow, T* p, T* v,
                             ReduceCtx ctx, double tol, int max_it) {
     pdl_begin();
-    ph::bicg_init<T>(lv, blockIdx.x, 0, threadIdx.x, b, x, r, shadow, p, v, ctx, tol, max_it);
+    ph::bicg_init<T, R>(lv, blockIdx.x * R, 0, threadIdx.x, b, x, r, shadow, p, v, ctx, tol, max_it);
 }
 
-template <typename T>
+template <typename T, int R>
 __global__ void k_bicg_p(LevelView<T> lv, const T* __restrict__ r, const T* __restrict__ v, T* p, T* xv, T omega_j,
                          const InstanceScalars* sc) {
     pdl_begin();
-    ph::bicg_p<T>(lv, blockIdx.x, threadIdx.x, r, v, p, xv, omega_j, sc);
+    ph::bicg_p<T, R>(lv, blockIdx.x * R, threadIdx.x, r, v, p, xv, omega_j, sc);
 }
 
-template <typename T, int W>
+template <typename T, int W, int R>
 __global__ void k_bicg_v(LevelView<T> lv, const T* __restrict__ in, T* __restrict__ out, const T* __restrict__ shadow,
                          ReduceCtx ctx) {
     pdl_begin();
-    ph::bicg_v<T, W>(lv, blockIdx.x, 0, threadIdx.x, in, out, shadow, ctx);
+    ph::bicg_v<T, W, R>(lv, blockIdx.x * R, 0, threadIdx.x, in, out, shadow, ctx);
 }
 
-template <typename T>
+template <typename T, int R>
 __global__ void k_bicg_s(LevelView<T> lv, const T* __restrict__ r, const T* __restrict__ v, T* __restrict__ s_out,
                          T* xv, T omega_j, ReduceCtx ctx) {
     pdl_begin();
-    ph::bicg_s<T>(lv, blockIdx.x, 0, threadIdx.x, r, v, s_out, xv, omega_j, ctx);
+    ph::bicg_s<T, R>(lv, blockIdx.x * R, 0, threadIdx.x, r, v, s_out, xv, omega_j, ctx);
 }
 
-template <typename T, int W>
+template <typename T, int W, int R>
 __global__ void k_bicg_t(LevelView<T> lv, const T* __restrict__ shat, T* __restrict__ t, const T* __restrict__ s_vec,
                          ReduceCtx ctx) {
     pdl_begin();
-    ph::bicg_t<T, W>(lv, blockIdx.x, 0, threadIdx.x, shat, t, s_vec, ctx);
+    ph::bicg_t<T, W, R>(lv, blockIdx.x * R, 0, threadIdx.x, shat, t, s_vec, ctx);
 }
 
-template <typename T>
+template <typename T, int R>
 __global__ void k_bicg_x(LevelView<T> lv, const T* __restrict__ phat, const T* __restrict__ shat,
                          const T* __restrict__ s_vec, const T* __restrict__ t, T* x, T* r,
                          const T* __restrict__ shadow, ReduceCtx ctx) {
     pdl_begin();
-    ph::bicg_x<T>(lv, blockIdx.x, 0, threadIdx.x, phat, shat, s_vec, t, x, r, shadow, ctx);
+    ph::bicg_x<T, R>(lv, blockIdx.x * R, 0, threadIdx.x, phat, shat, s_vec, t, x, r, shadow, ctx);
 }
 
-template <typename T>
+template <typename T, int R>
 __global__ void k_pcg_init(LevelView<T> lv, const T* __restrict__ b, T* x, T* r, T* p, T* xv, T omega_j,
                            ReduceCtx ctx, double tol, int max_it) {
     pdl_begin();
-    ph::pcg_init<T>(lv, blockIdx.x, 0, threadIdx.x, b, x, r, p, xv, omega_j, ctx, tol, max_it);
+    ph::pcg_init<T, R>(lv, blockIdx.x * R, 0, threadIdx.x, b, x, r, p, xv, omega_j, ctx, tol, max_it);
 }
 
-template <typename T>
+template <typename T, int R>
 __global__ void k_pcg_rz(LevelView<T> lv, const T* __restrict__ r, const T* __restrict__ z, ReduceCtx ctx) {
     pdl_begin();
-    ph::pcg_rz<T>(lv, blockIdx.x, 0, threadIdx.x, r, z, ctx);
+    ph::pcg_rz<T, R>(lv, blockIdx.x * R, 0, threadIdx.x, r, z, ctx);
 }
 
-template <typename T>
+template <typename T, int R>
 __global__ void k_pcg_p(LevelView<T> lv, const T* __restrict__ z, T* p, const InstanceScalars* sc) {
     pdl_begin();
-    ph::pcg_p<T>(lv, blockIdx.x, threadIdx.x, z, p, sc);
+    ph::pcg_p<T, R>(lv, blockIdx.x * R, threadIdx.x, z, p, sc);
 }
 
-template <typename T, int W>
+template <typename T, int W, int R>
 __global__ void k_pcg_q(LevelView<T> lv, const T* __restrict__ p, T* __restrict__ q_out, ReduceCtx ctx) {
     pdl_begin();
-    ph::pcg_q<T, W>(lv, blockIdx.x, 0, threadIdx.x, p, q_out, ctx);
+    ph::pcg_q<T, W, R>(lv, blockIdx.x * R, 0, threadIdx.x, p, q_out, ctx);
 }
 
-template <typename T>
+template <typename T, int R>
 __global__ void k_pcg_xr(LevelView<T> lv, const T* __restrict__ p, const T* __restrict__ q_in, T* x, T* r, T* xv,
                          T omega_j, ReduceCtx ctx) {
     pdl_begin();
-    ph::pcg_xr<T>(lv, blockIdx.x, 0, threadIdx.x, p, q_in, x, r, xv, omega_j, ctx);
+    ph::pcg_xr<T, R>(lv, blockIdx.x * R, 0, threadIdx.x, p, q_in, x, r, xv, omega_j, ctx);
 }
 
+template <int R>
 __global__ void k_outer_init(LevelView<double> lv, const double* __restrict__ b, ReduceCtx ctx, double tol,
                              int max_refine, const std::uint8_t* __restrict__ active) {
     pdl_begin();
     static_cast<void>(max_refine);
-    ph::outer_init(lv, blockIdx.x, 0, threadIdx.x, b, ctx, tol, active);
+    ph::outer_init<R>(lv, blockIdx.x * R, 0, threadIdx.x, b, ctx, tol, active);
 }
 
-template <typename TI, int W>
+template <typename TI, int W, int R>
 __global__ void k_outer_residual(LevelView<double> lv, const double* __restrict__ b, const double* __restrict__ x,
                                  double* __restrict__ r64, TI* __restrict__ rin, ReduceCtx ctx, int max_refine) {
     pdl_begin();
-    ph::outer_residual<TI, W>(lv, blockIdx.x, 0, threadIdx.x, b, x, r64, rin, ctx, max_refine);
+    ph::outer_residual<TI, W, R>(lv, blockIdx.x * R, 0, threadIdx.x, b, x, r64, rin, ctx, max_refine);
 }
 
-template <typename TI>
+template <typename TI, int R>
 __global__ void k_outer_update(LevelView<double> lv, const TI* __restrict__ delta, double* x, InstanceScalars* sc) {
     pdl_begin();
-    ph::outer_update<TI>(lv, blockIdx.x, threadIdx.x, delta, x, sc);
+    ph::outer_update<TI, R>(lv, blockIdx.x * R, threadIdx.x, delta, x, sc);
 }
 
 __global__ void k_outer_account(InstanceScalars* sc, std::uint32_t instances) {
@@ -128,70 +129,62 @@ __global__ void k_outer_account(InstanceScalars* sc, std::uint32_t instances) {
 
 // ---- launchers -----------------------------------------------------------------------
 
-#define PSGB_W(width, ...)                                            \
-    switch (width) {                                                  \
-        case 6: { constexpr int W = 6; __VA_ARGS__; } break;           \
-        case 8: { constexpr int W = 8; __VA_ARGS__; } break;           \
-        case 12: { constexpr int W = 12; __VA_ARGS__; } break;         \
-        case 16: { constexpr int W = 16; __VA_ARGS__; } break;         \
-        default: throw std::logic_error("unsupported ELL width");     \
-    }
 
 template <typename T>
 void KrylovLaunch<T>::bicg_init(const LevelView<T>& lv, const T* b, T* x, T* r, T* shadow, T* p, T* v,
                                 const ReduceCtx& ctx, double tol, int max_it, cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovVector, st, launch_pdl(k_bicg_init<T>, lv.tiles, kTile, st, lv, b, x, r, shadow, p, v, ctx, tol, max_it));
+    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_bicg_init<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, b, x, r, shadow, p, v, ctx, tol, max_it)));
 }
 template <typename T>
 void KrylovLaunch<T>::bicg_p(const LevelView<T>& lv, const T* r, const T* v, T* p, T* xv, T omega_j,
                              const InstanceScalars* sc, cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovVector, st, launch_pdl(k_bicg_p<T>, lv.tiles, kTile, st, lv, r, v, p, xv, omega_j, sc));
+    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_bicg_p<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, r, v, p, xv, omega_j, sc)));
 }
 template <typename T>
 void KrylovLaunch<T>::bicg_v(const LevelView<T>& lv, const T* in, T* out, const T* shadow,
                              const ReduceCtx& ctx, cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovSpmv, st, PSGB_W(lv.width, (launch_pdl(k_bicg_v<T, W>, lv.tiles, kTile, st, lv, in, out, shadow, ctx))));
+    PSGB_LAUNCH(kFamKrylovSpmv, st, PSGB_WIDTHS(lv.width, PSGB_STENCIL_SETS(lv.sets_stencil, launch_pdl(k_bicg_v<T, W, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, in, out, shadow, ctx))));
 }
 template <typename T>
 void KrylovLaunch<T>::bicg_s(const LevelView<T>& lv, const T* r, const T* v, T* s, T* xv, T omega_j,
                              const ReduceCtx& ctx, cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovVector, st, launch_pdl(k_bicg_s<T>, lv.tiles, kTile, st, lv, r, v, s, xv, omega_j, ctx));
+    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_bicg_s<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, r, v, s, xv, omega_j, ctx)));
 }
 template <typename T>
 void KrylovLaunch<T>::bicg_t(const LevelView<T>& lv, const T* shat, T* t, const T* s,
                              const ReduceCtx& ctx, cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovSpmv, st, PSGB_W(lv.width, (launch_pdl(k_bicg_t<T, W>, lv.tiles, kTile, st, lv, shat, t, s, ctx))));
+    PSGB_LAUNCH(kFamKrylovSpmv, st, PSGB_WIDTHS(lv.width, PSGB_STENCIL_SETS(lv.sets_stencil, launch_pdl(k_bicg_t<T, W, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, shat, t, s, ctx))));
 }
 template <typename T>
 void KrylovLaunch<T>::bicg_x(const LevelView<T>& lv, const T* phat, const T* shat, const T* s,
                              const T* t, T* x, T* r, const T* shadow, const ReduceCtx& ctx,
                              cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovVector, st, launch_pdl(k_bicg_x<T>, lv.tiles, kTile, st, lv, phat, shat, s, t, x, r, shadow, ctx));
+    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_bicg_x<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, phat, shat, s, t, x, r, shadow, ctx)));
 }
 template <typename T>
 void KrylovLaunch<T>::pcg_init(const LevelView<T>& lv, const T* b, T* x, T* r, T* p, T* xv, T omega_j,
                                const ReduceCtx& ctx, double tol, int max_it, cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovVector, st, launch_pdl(k_pcg_init<T>, lv.tiles, kTile, st, lv, b, x, r, p, xv, omega_j, ctx, tol, max_it));
+    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_pcg_init<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, b, x, r, p, xv, omega_j, ctx, tol, max_it)));
 }
 template <typename T>
 void KrylovLaunch<T>::pcg_rz(const LevelView<T>& lv, const T* r, const T* z, const ReduceCtx& ctx,
                              cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovVector, st, launch_pdl(k_pcg_rz<T>, lv.tiles, kTile, st, lv, r, z, ctx));
+    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_pcg_rz<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, r, z, ctx)));
 }
 template <typename T>
 void KrylovLaunch<T>::pcg_p(const LevelView<T>& lv, const T* z, T* p, const InstanceScalars* sc,
                             cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovVector, st, launch_pdl(k_pcg_p<T>, lv.tiles, kTile, st, lv, z, p, sc));
+    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_pcg_p<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, z, p, sc)));
 }
 template <typename T>
 void KrylovLaunch<T>::pcg_q(const LevelView<T>& lv, const T* p, T* q, const ReduceCtx& ctx,
                             cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovSpmv, st, PSGB_W(lv.width, (launch_pdl(k_pcg_q<T, W>, lv.tiles, kTile, st, lv, p, q, ctx))));
+    PSGB_LAUNCH(kFamKrylovSpmv, st, PSGB_WIDTHS(lv.width, PSGB_STENCIL_SETS(lv.sets_stencil, launch_pdl(k_pcg_q<T, W, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, p, q, ctx))));
 }
 template <typename T>
 void KrylovLaunch<T>::pcg_xr(const LevelView<T>& lv, const T* p, const T* q, T* x, T* r, T* xv,
                              T omega_j, const ReduceCtx& ctx, cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovVector, st, launch_pdl(k_pcg_xr<T>, lv.tiles, kTile, st, lv, p, q, x, r, xv, omega_j, ctx));
+    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_pcg_xr<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, p, q, x, r, xv, omega_j, ctx)));
 }
 
 template struct KrylovLaunch<float>;
@@ -199,20 +192,20 @@ template struct KrylovLaunch<double>;
 
 void launch_outer_init(const LevelView<double>& lv, const double* b, const ReduceCtx& ctx, double tol,
                        int max_refine, const std::uint8_t* active, cudaStream_t st) {
-    PSGB_LAUNCH(kFamRefine, st, launch_pdl(k_outer_init, lv.tiles, kTile, st, lv, b, ctx, tol, max_refine, active));
+    PSGB_LAUNCH(kFamRefine, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_outer_init<R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, b, ctx, tol, max_refine, active)));
 }
 
 template <typename TI>
 void launch_outer_residual(const LevelView<double>& lv, const double* b, const double* x, double* r64,
                            TI* rin, const ReduceCtx& ctx, int max_refine, cudaStream_t st) {
-    PSGB_LAUNCH(kFamRefine, st, PSGB_W(lv.width, (launch_pdl(k_outer_residual<TI, W>, lv.tiles, kTile, st, lv, b, x, r64, rin, ctx, max_refine))));
+    PSGB_LAUNCH(kFamRefine, st, PSGB_WIDTHS(lv.width, PSGB_STENCIL_SETS(lv.sets_stencil, launch_pdl(k_outer_residual<TI, W, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, b, x, r64, rin, ctx, max_refine))));
 }
 
 template <typename TI>
 void launch_outer_update(const LevelView<double>& lv, const TI* delta, double* x, InstanceScalars* sc,
                          std::uint32_t instances, cudaStream_t st) {
     PSGB_LAUNCH(kFamRefine, st, launch_pdl(k_outer_account, (instances + 127) / 128, 128, st, sc, instances));
-    PSGB_LAUNCH(kFamRefine, st, launch_pdl(k_outer_update<TI>, lv.tiles, kTile, st, lv, delta, x, sc));
+    PSGB_LAUNCH(kFamRefine, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_outer_update<TI, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, delta, x, sc)));
 }
 
 template void launch_outer_residual<float>(const LevelView<double>&, const double*, const double*, double*,

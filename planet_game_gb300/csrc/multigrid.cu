@@ -162,39 +162,43 @@ __global__ void __launch_bounds__(1024) k_dense_invert(DenseView dense, int leve
 
 // ---- V-cycle pieces: one 256-thread block per tile (the shared phases of phases.cuh) ----
 
-template <typename T>
+template <typename T, int R>
 __global__ void k_smooth_zero(LevelView<T> lv, const T* __restrict__ b, T* __restrict__ x, T omega,
                               const InstanceScalars* sc, int gate) {
     pdl_begin();
-    ph::smooth_zero<T>(lv, blockIdx.x, threadIdx.x, b, x, omega, sc, gate);
+    ph::smooth_zero<T, R>(lv, blockIdx.x * R, threadIdx.x, b, x, omega, sc, gate);
 }
 
-template <typename T, int W>
+// Blocks past the level's tile sets carry the dense solves of the planets whose coarsest
+// level this is (they do not smooth here).
+template <typename T, int W, int R>
 __global__ void k_smooth(LevelView<T> lv, const T* __restrict__ b, const T* __restrict__ x, T* __restrict__ y,
                          T omega, const InstanceScalars* sc, int gate, DenseTask<T> dense) {
     pdl_begin();
-    if (blockIdx.x >= lv.tiles) {
-        ph::dense_block<T>(dense, blockIdx.x - lv.tiles, threadIdx.x, sc, gate);
+    const unsigned sets = ph::tile_sets(lv.tiles, R);
+    if (blockIdx.x >= sets) {
+        ph::dense_block<T>(dense, blockIdx.x - sets, threadIdx.x, sc, gate);
         return;
     }
-    ph::smooth<T, W>(lv, blockIdx.x, threadIdx.x, b, x, y, omega, sc, gate);
+    ph::smooth<T, W, R>(lv, blockIdx.x * R, threadIdx.x, b, x, y, omega, sc, gate);
 }
 
-template <typename T, int W>
+template <typename T, int W, int R>
 __global__ void k_residual(LevelView<T> lv, const T* __restrict__ b, const T* __restrict__ x, T* __restrict__ r,
                            const InstanceScalars* sc, int gate, DenseTask<T> dense) {
     pdl_begin();
-    if (blockIdx.x >= lv.tiles) {
-        ph::dense_block<T>(dense, blockIdx.x - lv.tiles, threadIdx.x, sc, gate);
+    const unsigned sets = ph::tile_sets(lv.tiles, R);
+    if (blockIdx.x >= sets) {
+        ph::dense_block<T>(dense, blockIdx.x - sets, threadIdx.x, sc, gate);
         return;
     }
-    ph::residual<T, W>(lv, blockIdx.x, threadIdx.x, b, x, r, sc, gate);
+    ph::residual<T, W, R>(lv, blockIdx.x * R, threadIdx.x, b, x, r, sc, gate);
 }
 
-template <typename T, int W>
+template <typename T, int W, int R>
 __global__ void k_spmv(LevelView<T> lv, const T* __restrict__ x, T* __restrict__ y) {
     pdl_begin();
-    ph::spmv<T, W>(lv, blockIdx.x, threadIdx.x, x, y);
+    ph::spmv<T, W, R>(lv, blockIdx.x * R, threadIdx.x, x, y);
 }
 
 template <typename T>
@@ -202,7 +206,7 @@ __global__ void k_restrict(LevelView<T> coarse, const std::uint32_t* __restrict_
                            const std::uint32_t* __restrict__ member, const T* __restrict__ r, T* __restrict__ bc,
                            const InstanceScalars* sc, int gate) {
     pdl_begin();
-    ph::restrict_only<T>(coarse, blockIdx.x, threadIdx.x, moff, member, r, bc, sc, gate);
+    ph::restrict_only<T, ph::kRowsCoarse>(coarse, blockIdx.x * ph::kRowsCoarse, threadIdx.x, moff, member, r, bc, sc, gate);
 }
 
 template <typename T>
@@ -211,22 +215,23 @@ __global__ void k_restrict_zero(LevelView<T> coarse, const std::uint32_t* __rest
                                 T* __restrict__ bc, T* __restrict__ xc, T omega, const InstanceScalars* sc,
                                 int gate) {
     pdl_begin();
-    ph::restrict_zero<T>(coarse, blockIdx.x, threadIdx.x, moff, member, r, bc, xc, omega, sc, gate);
+    ph::restrict_zero<T, ph::kRowsCoarse>(coarse, blockIdx.x * ph::kRowsCoarse, threadIdx.x, moff, member, r, bc, xc, omega,
+                                          sc, gate);
 }
 
-template <typename T, int W>
+template <typename T, int W, int R>
 __global__ void k_prolong_smooth(LevelView<T> lv, const std::int32_t* __restrict__ agg,
                                  const T* __restrict__ e, const T* __restrict__ b, const T* __restrict__ x,
                                  T* __restrict__ y, T omega, const InstanceScalars* sc, int gate) {
     pdl_begin();
-    ph::prolong_smooth<T, W>(lv, blockIdx.x, threadIdx.x, agg, e, b, x, y, omega, sc, gate);
+    ph::prolong_smooth<T, W, R>(lv, blockIdx.x * R, threadIdx.x, agg, e, b, x, y, omega, sc, gate);
 }
 
-template <typename T>
+template <typename T, int R>
 __global__ void k_prolong(LevelView<T> lv, const std::int32_t* __restrict__ agg, const T* __restrict__ xc,
                           T* __restrict__ x, const InstanceScalars* sc, int gate) {
     pdl_begin();
-    ph::prolong<T>(lv, blockIdx.x, threadIdx.x, agg, xc, x, sc, gate);
+    ph::prolong<T, R>(lv, blockIdx.x * R, threadIdx.x, agg, xc, x, sc, gate);
 }
 
 // Coarsest level: x = A^-1 b, one warp per row, eight rows per block.
@@ -236,7 +241,7 @@ __global__ void k_dense_solve(DenseTask<T> dense, const InstanceScalars* sc, int
     ph::dense_block<T>(dense, blockIdx.x, threadIdx.x, sc, gate);
 }
 
-inline dim3 tiles_grid(std::uint32_t tiles) { return dim3(tiles); }
+
 
 }  // namespace
 
@@ -271,65 +276,72 @@ void launch_dense_invert(const DenseView& dense, int level, const LevelView<doub
     PSGB_LAUNCH(kFamSetup, stream, launch_pdl(k_dense_invert, dense.instances, 1024, stream, dense, level, lv, work, inv64, inv32));
 }
 
-#define PSGB_WIDTH_DISPATCH_GRID(width, grid, KERNEL, ...)                          \
-    switch (width) {                                                                \
-        case 6: launch_pdl(KERNEL<T, 6>, grid, kTile, stream, __VA_ARGS__); break;    \
-        case 8: launch_pdl(KERNEL<T, 8>, grid, kTile, stream, __VA_ARGS__); break;    \
-        case 12: launch_pdl(KERNEL<T, 12>, grid, kTile, stream, __VA_ARGS__); break;  \
-        case 16: launch_pdl(KERNEL<T, 16>, grid, kTile, stream, __VA_ARGS__); break;  \
-        default: throw std::logic_error("unsupported ELL width");                   \
-    }
-#define PSGB_WIDTH_DISPATCH(width, KERNEL, ...) PSGB_WIDTH_DISPATCH_GRID(width, lv.tiles, KERNEL, __VA_ARGS__)
-
 template <typename T>
 void launch_smooth_zero(const LevelView<T>& lv, const T* b, T* x, T omega, const InstanceScalars* sc,
                         int gate, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamSmooth, stream, launch_pdl(k_smooth_zero<T>, lv.tiles, kTile, stream, lv, b, x, omega, sc, gate));
+    PSGB_LAUNCH(kFamSmooth, stream,
+                PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_smooth_zero<T, R>, ph::tile_sets(lv.tiles, R), kTile, stream,
+                                                            lv, b, x, omega, sc, gate)));
 }
 
 template <typename T>
 void launch_smooth(const LevelView<T>& lv, const T* b, const T* x, T* y, T omega,
                    const InstanceScalars* sc, int gate, cudaStream_t stream, const DenseTask<T>& dense) {
     PSGB_LAUNCH(kFamSmooth, stream,
-                PSGB_WIDTH_DISPATCH_GRID(lv.width, lv.tiles + dense.count, k_smooth, lv, b, x, y, omega, sc, gate, dense));
+                PSGB_STENCIL_SETS(lv.sets_stencil, PSGB_WIDTHS(lv.width,
+                    launch_pdl(k_smooth<T, W, R>, ph::tile_sets(lv.tiles, R) + dense.count, kTile, stream, lv, b, x, y, omega,
+                               sc, gate, dense))));
 }
 
 template <typename T>
 void launch_residual(const LevelView<T>& lv, const T* b, const T* x, T* r, const InstanceScalars* sc,
                      int gate, cudaStream_t stream, const DenseTask<T>& dense) {
     PSGB_LAUNCH(kFamResidual, stream,
-                PSGB_WIDTH_DISPATCH_GRID(lv.width, lv.tiles + dense.count, k_residual, lv, b, x, r, sc, gate, dense));
+                PSGB_STENCIL_SETS(lv.sets_stencil, PSGB_WIDTHS(lv.width,
+                    launch_pdl(k_residual<T, W, R>, ph::tile_sets(lv.tiles, R) + dense.count, kTile, stream, lv, b, x, r, sc,
+                               gate, dense))));
 }
 
 template <typename T>
 void launch_spmv(const LevelView<T>& lv, const T* x, T* y, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamKrylovSpmv, stream, PSGB_WIDTH_DISPATCH(lv.width, k_spmv, lv, x, y));
+    PSGB_LAUNCH(kFamKrylovSpmv, stream,
+                PSGB_STENCIL_SETS(lv.sets_stencil, PSGB_WIDTHS(lv.width,
+                    launch_pdl(k_spmv<T, W, R>, ph::tile_sets(lv.tiles, R), kTile, stream, lv, x, y))));
 }
 
 template <typename T>
 void launch_restrict(const LevelView<T>& coarse, const std::uint32_t* member_offset,
                      const std::uint32_t* member, const T* r, T* bc, const InstanceScalars* sc,
                      int gate, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamRestrict, stream, launch_pdl(k_restrict<T>, coarse.tiles, kTile, stream, coarse, member_offset, member, r, bc, sc, gate));
+    PSGB_LAUNCH(kFamRestrict, stream,
+                launch_pdl(k_restrict<T>, ph::tile_sets(coarse.tiles, ph::kRowsCoarse), kTile, stream, coarse, member_offset,
+                           member, r, bc, sc, gate));
 }
 
 template <typename T>
 void launch_restrict_zero(const LevelView<T>& coarse, const std::uint32_t* member_offset,
                           const std::uint32_t* member, const T* r, T* bc, T* xc, T omega,
                           const InstanceScalars* sc, int gate, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamRestrict, stream, launch_pdl(k_restrict_zero<T>, coarse.tiles, kTile, stream, coarse, member_offset, member, r, bc, xc, omega, sc, gate));
+    PSGB_LAUNCH(kFamRestrict, stream,
+                launch_pdl(k_restrict_zero<T>, ph::tile_sets(coarse.tiles, ph::kRowsCoarse), kTile, stream, coarse,
+                           member_offset, member, r, bc, xc, omega, sc, gate));
 }
 
 template <typename T>
 void launch_prolong_smooth(const LevelView<T>& lv, const std::int32_t* agg, const T* e, const T* b, const T* x,
                            T* y, T omega, const InstanceScalars* sc, int gate, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamSmooth, stream, PSGB_WIDTH_DISPATCH(lv.width, k_prolong_smooth, lv, agg, e, b, x, y, omega, sc, gate));
+    PSGB_LAUNCH(kFamSmooth, stream,
+                PSGB_STENCIL_SETS(lv.sets_stencil, PSGB_WIDTHS(lv.width,
+                    launch_pdl(k_prolong_smooth<T, W, R>, ph::tile_sets(lv.tiles, R), kTile, stream, lv, agg, e, b, x, y, omega,
+                               sc, gate))));
 }
 
 template <typename T>
 void launch_prolong(const LevelView<T>& fine, const std::int32_t* agg, const T* xc, T* x,
                     const InstanceScalars* sc, int gate, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamProlong, stream, launch_pdl(k_prolong<T>, fine.tiles, kTile, stream, fine, agg, xc, x, sc, gate));
+    PSGB_LAUNCH(kFamProlong, stream,
+                PSGB_VECTOR_SETS(fine.sets_vector, launch_pdl(k_prolong<T, R>, ph::tile_sets(fine.tiles, R), kTile, stream,
+                                                              fine, agg, xc, x, sc, gate)));
 }
 
 template <typename T>

@@ -105,7 +105,11 @@ __device__ __forceinline__ Group group_of() {
                  static_cast<int>(gridDim.x) * ph::kGroups};
 }
 
-#define PSGB_TILES(lv, G) for (int tile = (G).first; tile < static_cast<int>((lv).tiles); tile += (G).stride)
+// Tiles per tile set of every phase here (rows per thread).
+constexpr int kPR = 2;
+
+#define PSGB_SETS(lv, G) \
+    for (int t0 = (G).first * kPR; t0 < static_cast<int>((lv).tiles); t0 += (G).stride * kPR)
 #define PSGB_BARRIER(a) \
     if (!grid_barrier((a).sync)) return false
 
@@ -175,19 +179,19 @@ __device__ bool vcycle(const Args<T>& a, const T* rhs, T* x, int gate) {
             if (dense) dense_phase<T>(a, l, L.b, L.x, gate);
             dense = false;
             with_width(lv.width, [&](auto W) {
-                PSGB_TILES(lv, G) ph::smooth<T, decltype(W)::value>(lv, tile, G.lane, b, p.first, p.second, omega, a.sc, gate);
+                PSGB_SETS(lv, G) ph::smooth<T, decltype(W)::value, kPR>(lv, t0, G.lane, b, p.first, p.second, omega, a.sc, gate);
             });
             PSGB_BARRIER(a);
             T* t = p.first; p.first = p.second; p.second = t;
         }
         if (dense) dense_phase<T>(a, l, L.b, L.x, gate);
         with_width(lv.width, [&](auto W) {
-            PSGB_TILES(lv, G) ph::residual<T, decltype(W)::value>(lv, tile, G.lane, b, p.first, L.r, a.sc, gate);
+            PSGB_SETS(lv, G) ph::residual<T, decltype(W)::value, kPR>(lv, t0, G.lane, b, p.first, L.r, a.sc, gate);
         });
         PSGB_BARRIER(a);
         const PersistentLevel<T>& C = a.level[l + 1];
         const Pair<T> pc = pair_of(a, l + 1, x);
-        PSGB_TILES(C.view, G) ph::restrict_zero<T>(C.view, tile, G.lane, L.member_offset, L.member, L.r, C.b, pc.first, omega, a.sc, gate);
+        PSGB_SETS(C.view, G) ph::restrict_zero<T, kPR>(C.view, t0, G.lane, L.member_offset, L.member, L.r, C.b, pc.first, omega, a.sc, gate);
         PSGB_BARRIER(a);
         if (l + 2 == a.depth && a.dense_at[l + 1]) {
             dense_phase<T>(a, l + 1, C.b, C.x, gate);
@@ -203,18 +207,18 @@ __device__ bool vcycle(const Args<T>& a, const T* rhs, T* x, int gate) {
         Pair<T> p = pair_of(a, l, x);
         if ((a.pre - 1) & 1) { T* t = p.first; p.first = p.second; p.second = t; }   // where the down sweeps ended
         if (a.post == 0) {
-            PSGB_TILES(lv, G) ph::prolong<T>(lv, tile, G.lane, L.agg, e, p.first, a.sc, gate);
+            PSGB_SETS(lv, G) ph::prolong<T, kPR>(lv, t0, G.lane, L.agg, e, p.first, a.sc, gate);
             PSGB_BARRIER(a);
             continue;
         }
         with_width(lv.width, [&](auto W) {
-            PSGB_TILES(lv, G) ph::prolong_smooth<T, decltype(W)::value>(lv, tile, G.lane, L.agg, e, b, p.first, p.second, omega, a.sc, gate);
+            PSGB_SETS(lv, G) ph::prolong_smooth<T, decltype(W)::value, kPR>(lv, t0, G.lane, L.agg, e, b, p.first, p.second, omega, a.sc, gate);
         });
         PSGB_BARRIER(a);
         { T* t = p.first; p.first = p.second; p.second = t; }
         for (int k = 1; k < a.post; ++k) {
             with_width(lv.width, [&](auto W) {
-                PSGB_TILES(lv, G) ph::smooth<T, decltype(W)::value>(lv, tile, G.lane, b, p.first, p.second, omega, a.sc, gate);
+                PSGB_SETS(lv, G) ph::smooth<T, decltype(W)::value, kPR>(lv, t0, G.lane, b, p.first, p.second, omega, a.sc, gate);
             });
             PSGB_BARRIER(a);
             T* t = p.first; p.first = p.second; p.second = t;
@@ -233,27 +237,27 @@ __device__ bool bicgstab(const Args<T>& a) {
     const T* rhs = a.k[8];
     T* x = a.k[9];
     const T omega_j = a.omega;
-    PSGB_TILES(lv, G) ph::bicg_init<T>(lv, tile, G.gid, G.lane, rhs, x, r, shadow, p, v, ctx, a.inner_tolerance, a.max_iterations);
+    PSGB_SETS(lv, G) ph::bicg_init<T, kPR>(lv, t0, G.gid, G.lane, rhs, x, r, shadow, p, v, ctx, a.inner_tolerance, a.max_iterations);
     PSGB_BARRIER(a);
     T* phat_first = pair_of(a, 0, phat).first;
     T* shat_first = pair_of(a, 0, shat).first;
     for (int it = 0; it < a.max_iterations; ++it) {
         if (!any_inner_running(a.sc, a.instances)) break;
-        PSGB_TILES(lv, G) ph::bicg_p<T>(lv, tile, G.lane, r, v, p, phat_first, omega_j, a.sc);
+        PSGB_SETS(lv, G) ph::bicg_p<T, kPR>(lv, t0, G.lane, r, v, p, phat_first, omega_j, a.sc);
         PSGB_BARRIER(a);
         if (!vcycle<T>(a, p, phat, kGateRunning)) return false;
         with_width(lv.width, [&](auto W) {
-            PSGB_TILES(lv, G) ph::bicg_v<T, decltype(W)::value>(lv, tile, G.gid, G.lane, phat, v, shadow, ctx);
+            PSGB_SETS(lv, G) ph::bicg_v<T, decltype(W)::value, kPR>(lv, t0, G.gid, G.lane, phat, v, shadow, ctx);
         });
         PSGB_BARRIER(a);
-        PSGB_TILES(lv, G) ph::bicg_s<T>(lv, tile, G.gid, G.lane, r, v, s, shat_first, omega_j, ctx);
+        PSGB_SETS(lv, G) ph::bicg_s<T, kPR>(lv, t0, G.gid, G.lane, r, v, s, shat_first, omega_j, ctx);
         PSGB_BARRIER(a);
         if (!vcycle<T>(a, s, shat, kGateSecondHalf)) return false;
         with_width(lv.width, [&](auto W) {
-            PSGB_TILES(lv, G) ph::bicg_t<T, decltype(W)::value>(lv, tile, G.gid, G.lane, shat, t, s, ctx);
+            PSGB_SETS(lv, G) ph::bicg_t<T, decltype(W)::value, kPR>(lv, t0, G.gid, G.lane, shat, t, s, ctx);
         });
         PSGB_BARRIER(a);
-        PSGB_TILES(lv, G) ph::bicg_x<T>(lv, tile, G.gid, G.lane, phat, shat, s, t, x, r, shadow, ctx);
+        PSGB_SETS(lv, G) ph::bicg_x<T, kPR>(lv, t0, G.gid, G.lane, phat, shat, s, t, x, r, shadow, ctx);
         PSGB_BARRIER(a);
     }
     return true;
@@ -269,20 +273,20 @@ __device__ bool pcg(const Args<T>& a) {
     T* x = a.k[9];
     const T omega_j = a.omega;
     T* z_first = pair_of(a, 0, z).first;
-    PSGB_TILES(lv, G) ph::pcg_init<T>(lv, tile, G.gid, G.lane, rhs, x, r, p, z_first, omega_j, ctx, a.inner_tolerance, a.max_iterations);
+    PSGB_SETS(lv, G) ph::pcg_init<T, kPR>(lv, t0, G.gid, G.lane, rhs, x, r, p, z_first, omega_j, ctx, a.inner_tolerance, a.max_iterations);
     PSGB_BARRIER(a);
     if (!vcycle<T>(a, r, z, kGateRunning)) return false;
     for (int it = 0; it < a.max_iterations; ++it) {
         if (!any_inner_running(a.sc, a.instances)) break;
-        PSGB_TILES(lv, G) ph::pcg_rz<T>(lv, tile, G.gid, G.lane, r, z, ctx);
+        PSGB_SETS(lv, G) ph::pcg_rz<T, kPR>(lv, t0, G.gid, G.lane, r, z, ctx);
         PSGB_BARRIER(a);
-        PSGB_TILES(lv, G) ph::pcg_p<T>(lv, tile, G.lane, z, p, a.sc);
+        PSGB_SETS(lv, G) ph::pcg_p<T, kPR>(lv, t0, G.lane, z, p, a.sc);
         PSGB_BARRIER(a);
         with_width(lv.width, [&](auto W) {
-            PSGB_TILES(lv, G) ph::pcg_q<T, decltype(W)::value>(lv, tile, G.gid, G.lane, p, q, ctx);
+            PSGB_SETS(lv, G) ph::pcg_q<T, decltype(W)::value, kPR>(lv, t0, G.gid, G.lane, p, q, ctx);
         });
         PSGB_BARRIER(a);
-        PSGB_TILES(lv, G) ph::pcg_xr<T>(lv, tile, G.gid, G.lane, p, q, x, r, z_first, omega_j, ctx);
+        PSGB_SETS(lv, G) ph::pcg_xr<T, kPR>(lv, t0, G.gid, G.lane, p, q, x, r, z_first, omega_j, ctx);
         PSGB_BARRIER(a);
         if (!vcycle<T>(a, r, z, kGateRunning)) return false;
     }
@@ -293,11 +297,11 @@ template <typename T>
 __device__ bool refine(const Args<T>& a) {
     const Group G = group_of();
     const LevelView<double>& f = a.fine64;
-    PSGB_TILES(f, G) ph::outer_init(f, tile, G.gid, G.lane, a.rhs64, a.ctx, a.tolerance, a.active);
+    PSGB_SETS(f, G) ph::outer_init<kPR>(f, t0, G.gid, G.lane, a.rhs64, a.ctx, a.tolerance, a.active);
     PSGB_BARRIER(a);
     for (int round = 0; round <= a.max_refinements; ++round) {
         with_width(f.width, [&](auto W) {
-            PSGB_TILES(f, G) ph::outer_residual<T, decltype(W)::value>(f, tile, G.gid, G.lane, a.rhs64, a.x64, a.r64, a.k[8], a.ctx, a.max_refinements);
+            PSGB_SETS(f, G) ph::outer_residual<T, decltype(W)::value, kPR>(f, t0, G.gid, G.lane, a.rhs64, a.x64, a.r64, a.k[8], a.ctx, a.max_refinements);
         });
         PSGB_BARRIER(a);
         if (!any_outer_running(a.sc, a.instances)) break;
@@ -306,7 +310,7 @@ __device__ bool refine(const Args<T>& a) {
             for (unsigned i = threadIdx.x; i < a.instances; i += blockDim.x) ph::outer_account(a.sc[i]);
         }
         PSGB_BARRIER(a);
-        PSGB_TILES(f, G) ph::outer_update<T>(f, tile, G.lane, a.k[9], a.x64, a.sc);
+        PSGB_SETS(f, G) ph::outer_update<T, kPR>(f, t0, G.lane, a.k[9], a.x64, a.sc);
         PSGB_BARRIER(a);
     }
     return true;

@@ -2,14 +2,26 @@
 // krylov.cu) and the persistent solver (persistent.cu), so both compute every row and
 // every reduction with the same arithmetic in the same order.
 //
-// A "group" is 256 consecutive threads of a block working on one 256-row tile (a block
-// of 256 threads is one group; the persistent kernel runs 1024-thread blocks = 4 groups).
+// A "group" is 256 consecutive threads of a block. A phase call works on a tile set: R
+// consecutive 256-row tiles starting at t0 (a multiple of R), lane l of the group owning
+// row l of each of them. The R rows of a thread are independent, so their loads are in
+// flight together; tiles past the end of the level take part in no store. Per tile, the
+// arithmetic and every reduction tree are those of one tile alone: a dot product's tile
+// partial is the same 256-row tree whatever R is, so results do not depend on R.
+//
+// Loads may run through rows that store nothing (padding rows, tiles of a planet that is
+// masked out, a tile set's tail past the level): every such row indexes valid memory
+// (padded rows point at themselves in `col`, at coarse row 0 in `agg`, and own an empty
+// member range), and only rows of open tiles are stored.
+//
 // Groups synchronise with named barriers (id 1 + group), never with __syncthreads, so the
-// groups of a block can work on different tiles independently.
+// groups of a block can work on different tile sets independently.
 #pragma once
 
 #include "common.cuh"
 #include "kernels.hpp"
+
+#include <stdexcept>
 
 // Vectors a phase reads were written by an earlier phase. A kernel per phase may read
 // them through the read-only (non-coherent) path; the persistent solver, where earlier
@@ -23,6 +35,35 @@ namespace ph {
 
 constexpr int kGroups = 4;   // groups per block at most (1024 threads)
 
+// Tiles per tile set (rows per thread) of the kernel path's launches.
+constexpr int kRowsStencil = 2;   // smoothing, residual, prolongation, Krylov products
+constexpr int kRowsVector = 4;    // vector updates and their dot products
+constexpr int kRowsCoarse = 1;    // restriction (a member loop per row)
+
+__host__ __device__ constexpr unsigned tile_sets(unsigned tiles, int rows) { return (tiles + rows - 1) / rows; }
+
+// Host dispatch on a level's tile-set sizes and ELL width (R and W constexpr in the body).
+#define PSGB_STENCIL_SETS(sets, ...)                                           \
+    switch (sets) {                                                            \
+        case 1: { constexpr int R = 1; __VA_ARGS__; } break;                   \
+        case 2: { constexpr int R = 2; __VA_ARGS__; } break;                   \
+        default: throw std::logic_error("unsupported stencil tile-set size");  \
+    }
+#define PSGB_VECTOR_SETS(sets, ...)                                            \
+    switch (sets) {                                                            \
+        case 1: { constexpr int R = 1; __VA_ARGS__; } break;                   \
+        case 4: { constexpr int R = 4; __VA_ARGS__; } break;                   \
+        default: throw std::logic_error("unsupported vector tile-set size");   \
+    }
+#define PSGB_WIDTHS(width, ...)                                                \
+    switch (width) {                                                           \
+        case 6: { constexpr int W = 6; __VA_ARGS__; } break;                   \
+        case 8: { constexpr int W = 8; __VA_ARGS__; } break;                   \
+        case 12: { constexpr int W = 12; __VA_ARGS__; } break;                 \
+        case 16: { constexpr int W = 16; __VA_ARGS__; } break;                 \
+        default: throw std::logic_error("unsupported ELL width");              \
+    }
+
 __device__ __forceinline__ void group_sync(int gid) {
     asm volatile("bar.sync %0, 256;" ::"r"(gid + 1) : "memory");
 }
@@ -31,20 +72,21 @@ __device__ __forceinline__ void count_bytes(unsigned long long* counter, int lan
     if (counter != nullptr && lane == 0 && bytes != 0) atomicAdd(counter, bytes);
 }
 
-// Sum of NQ values over the 256 threads of a group, in a fixed tree; result in lane 0.
-template <typename A, int NQ>
-__device__ __forceinline__ void group_sum(A (&v)[NQ], int gid, int lane) {
-    __shared__ A scratch[kGroups][NQ][8];
+// Sum of N values over the 256 threads of a group, each value in its own fixed tree
+// (warp butterflies, then the eight warp sums in order); results in lane 0.
+template <typename A, int N>
+__device__ __forceinline__ void group_sum(A (&v)[N], int gid, int lane) {
+    __shared__ A scratch[kGroups][N][8];
     const int w = lane >> 5;
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) {
+    for (int q = 0; q < N; ++q) {
         const A s = warp_sum(v[q]);
         if ((lane & 31) == 0) scratch[gid][q][w] = s;
     }
     group_sync(gid);
     if (lane == 0) {
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) {
+        for (int q = 0; q < N; ++q) {
             A s = scratch[gid][q][0];
 #pragma unroll
             for (int k = 1; k < 8; ++k) s += scratch[gid][q][k];
@@ -54,41 +96,47 @@ __device__ __forceinline__ void group_sum(A (&v)[NQ], int gid, int lane) {
     group_sync(gid);
 }
 
-// Tile partial sums (in the tile's precision A) to FP64 partials; the last tile of a
-// planet to arrive (integer ticket) sums that planet's partials in tile order. Returns
-// true in lane 0 of the group that finalises, with the planet's sums in `out`.
-template <typename A, int NQ>
-__device__ bool tile_reduce(A (&v)[NQ], const ReduceCtx& ctx, int inst, int tile, double (&out)[NQ], int gid,
-                            int lane) {
-    __shared__ int last[kGroups];
-    group_sum<A, NQ>(v, gid, lane);
-    if (lane == 0) {
+// ---- tile sets ----------------------------------------------------------------------------
+
+template <int R>
+struct TileSet {
+    int tile[R];     // tile index (t0 for a tile past the level: loads stay in bounds)
+    int inst[R];     // planet
+    int rows[R];     // valid rows (0 past the level)
+    bool sweep[R];   // the planet smooths on this level
+};
+
+template <int R>
+__device__ __forceinline__ TileSet<R> tile_set(const std::uint32_t* meta, unsigned tiles, int t0) {
+    std::uint32_t w[R];
+    if constexpr (R == 4) {
+        const uint4 v = *reinterpret_cast<const uint4*>(meta + t0);
+        w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
+    } else if constexpr (R == 2) {
+        const uint2 v = *reinterpret_cast<const uint2*>(meta + t0);
+        w[0] = v.x; w[1] = v.y;
+    } else {
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) ctx.partial[tile * 8 + q] = static_cast<double>(v[q]);
-        __threadfence();
-        const unsigned begin = ctx.tile_begin[inst], end = ctx.tile_begin[inst + 1];
-        const unsigned ticket = atomicAdd(&ctx.ticket[inst], 1u);
-        last[gid] = (ticket == end - begin - 1) ? 1 : 0;
+        for (int k = 0; k < R; ++k) w[k] = meta[t0 + k];
     }
-    group_sync(gid);
-    if (!last[gid]) return false;
-    __threadfence();
-    const unsigned begin = ctx.tile_begin[inst], end = ctx.tile_begin[inst + 1];
-    double acc[NQ];
+    TileSet<R> s;
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) acc[q] = 0.0;
-    for (unsigned t = begin + lane; t < end; t += kTile) {
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) acc[q] += __ldcg(&ctx.partial[t * 8 + q]);
+    for (int k = 0; k < R; ++k) {
+        const bool valid = static_cast<unsigned>(t0 + k) < tiles;
+        s.tile[k] = valid ? t0 + k : t0;
+        s.inst[k] = static_cast<int>(w[k] & 0x3FFFFFu);
+        s.rows[k] = valid ? static_cast<int>((w[k] >> 22) & 0x1FFu) : 0;
+        s.sweep[k] = valid && (w[k] >> 31) != 0u;
     }
-    group_sum<double, NQ>(acc, gid, lane);
-    if (lane == 0) {
-        ctx.ticket[inst] = 0;
+    return s;
+}
+
+template <int R>
+__device__ __forceinline__ bool any_of(const bool (&on)[R]) {
+    bool a = false;
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) out[q] = acc[q];
-        return true;
-    }
-    return false;
+    for (int k = 0; k < R; ++k) a = a || on[k];
+    return a;
 }
 
 __device__ __forceinline__ bool gate_open(const InstanceScalars* sc, int inst, int gate) {
@@ -100,7 +148,84 @@ __device__ __forceinline__ bool gate_open(const InstanceScalars* sc, int inst, i
     return true;
 }
 
+__device__ __forceinline__ bool running(const InstanceScalars& s) { return s.status == kRunning; }
+
 __device__ __forceinline__ bool finite(double v) { return isfinite(v); }
+
+// Release/acquire fence at GPU scope: orders this thread's partial stores before its
+// ticket, and the finaliser's ticket observation before its partial loads. Lighter than
+// the sequentially consistent __threadfence(), which the reduction does not need.
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
+// Tile partial sums (in the tiles' precision A) to FP64 partials, one fence and one ticket
+// per run of the set's tiles that belong to one planet; the last tile set of a planet to
+// arrive (integer ticket, so arrival order never matters) sums that planet's partials in
+// tile order. fin[k]: lane 0 holds planet inst[k]'s sums in out[k * NQ + q].
+template <typename A, int NQ, int R>
+__device__ void tiles_reduce(A (&v)[R * NQ], const ReduceCtx& ctx, const TileSet<R>& ts, const bool (&on)[R],
+                             double (&out)[R * NQ], bool (&fin)[R], int gid, int lane) {
+    __shared__ int last[kGroups][R];
+    group_sum<A, R * NQ>(v, gid, lane);
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            if (!on[k]) continue;
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) ctx.partial[ts.tile[k] * 8 + q] = static_cast<double>(v[k * NQ + q]);
+        }
+        fence_acq_rel_gpu();
+#pragma unroll
+        for (int k = 0; k < R; ++k) last[gid][k] = 0;
+        for (int k = 0; k < R;) {
+            if (!on[k]) { ++k; continue; }
+            int e = k + 1;
+            while (e < R && on[e] && ts.inst[e] == ts.inst[k]) ++e;
+            const int inst = ts.inst[k];
+            const unsigned n = ctx.tile_begin[inst + 1] - ctx.tile_begin[inst];
+            const unsigned add = static_cast<unsigned>(e - k);
+            const unsigned old = atomicAdd(&ctx.ticket[inst], add);
+            last[gid][k] = (old + add == n) ? 1 : 0;
+            k = e;
+        }
+        fence_acq_rel_gpu();
+    }
+    group_sync(gid);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        fin[k] = false;
+        if (!last[gid][k]) continue;
+        fence_acq_rel_gpu();
+        const int inst = ts.inst[k];
+        const unsigned begin = ctx.tile_begin[inst], end = ctx.tile_begin[inst + 1];
+        double acc[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) acc[q] = 0.0;
+        // partials of this lane's tiles, in tile order; four loads in flight at a time
+        for (unsigned t0 = begin + lane; t0 < end; t0 += 4 * kTile) {
+            double p[4][NQ];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const unsigned t = t0 + u * kTile;
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) p[u][q] = t < end ? __ldcg(&ctx.partial[t * 8 + q]) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (t0 + u * kTile < end) {
+#pragma unroll
+                    for (int q = 0; q < NQ; ++q) acc[q] += p[u][q];
+                }
+            }
+        }
+        group_sum<double, NQ>(acc, gid, lane);
+        if (lane == 0) {
+            ctx.ticket[inst] = 0;
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) out[k * NQ + q] = acc[q];
+            fin[k] = true;
+        }
+    }
+}
 
 // ---- V-cycle phases ---------------------------------------------------------------------
 
@@ -123,113 +248,182 @@ __device__ __forceinline__ T member_sum(const std::uint32_t* PSGB_PHASE_RESTRICT
     return s;
 }
 
-template <typename T>
-__device__ void smooth_zero(const LevelView<T>& lv, int tile, int lane, const T* PSGB_PHASE_RESTRICT b, T* PSGB_PHASE_RESTRICT x,
-                            T omega, const InstanceScalars* sc, int gate) {
-    const int rows = lv.tile_rows[tile];
-    if (!lv.tile_sweep[tile] || !gate_open(sc, lv.tile_inst[tile], gate)) return;
-    count_bytes(lv.bytes, lane, static_cast<unsigned long long>(rows) * 3ull * sizeof(T));
-    if (lane >= rows) return;
-    const int row = tile * kTile + lane;
-    x[row] = omega * lv.inv[row] * b[row];
+// Zero-start sweep: x = omega D^-1 b.
+template <typename T, int R>
+__device__ void smooth_zero(const LevelView<T>& lv, int t0, int lane, const T* PSGB_PHASE_RESTRICT b,
+                            T* PSGB_PHASE_RESTRICT x, T omega, const InstanceScalars* sc, int gate) {
+    const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
+    bool on[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) on[k] = ts.sweep[k] && gate_open(sc, ts.inst[k], gate);
+    if (!any_of(on)) return;
+    T y[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int row = ts.tile[k] * kTile + lane;
+        y[k] = omega * lv.inv[row] * b[row];
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (!on[k]) continue;
+        count_bytes(lv.bytes, lane, static_cast<unsigned long long>(ts.rows[k]) * 3ull * sizeof(T));
+        if (lane < ts.rows[k]) x[ts.tile[k] * kTile + lane] = y[k];
+    }
 }
 
-template <typename T, int W>
-__device__ void smooth(const LevelView<T>& lv, int tile, int lane, const T* PSGB_PHASE_RESTRICT b, const T* PSGB_PHASE_RESTRICT x,
-                       T* PSGB_PHASE_RESTRICT y, T omega, const InstanceScalars* sc, int gate) {
-    const int rows = lv.tile_rows[tile];
-    if (!lv.tile_sweep[tile] || !gate_open(sc, lv.tile_inst[tile], gate)) return;
-    count_bytes(lv.bytes, lane, static_cast<unsigned long long>(rows) * (4ull * W + sizeof(T) * (W + 4ull)));
-    if (lane >= rows) return;
-    const int row = tile * kTile + lane;
-    const std::uint32_t P = lv.rows;
-    T s = b[row];
+// Damped Jacobi sweep: y = x + omega (D^-1 (b - O x) - x).
+template <typename T, int W, int R>
+__device__ void smooth(const LevelView<T>& lv, int t0, int lane, const T* PSGB_PHASE_RESTRICT b,
+                       const T* PSGB_PHASE_RESTRICT x, T* PSGB_PHASE_RESTRICT y, T omega, const InstanceScalars* sc,
+                       int gate) {
+    const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
+    bool on[R];
 #pragma unroll
-    for (int j = 0; j < W; ++j) s -= lv.vd[j * P + row] * x[lv.col[j * P + row]];
-    const T xo = x[row];
-    y[row] = xo + omega * (lv.inv[row] * s - xo);
+    for (int k = 0; k < R; ++k) on[k] = ts.sweep[k] && gate_open(sc, ts.inst[k], gate);
+    if (!any_of(on)) return;
+    const std::uint32_t P = lv.rows;
+    T out[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int row = ts.tile[k] * kTile + lane;
+        T s = b[row];
+#pragma unroll
+        for (int j = 0; j < W; ++j) s -= lv.vd[j * P + row] * x[lv.col[j * P + row]];
+        const T xo = x[row];
+        out[k] = xo + omega * (lv.inv[row] * s - xo);
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (!on[k]) continue;
+        count_bytes(lv.bytes, lane, static_cast<unsigned long long>(ts.rows[k]) * (4ull * W + sizeof(T) * (W + 4ull)));
+        if (lane < ts.rows[k]) y[ts.tile[k] * kTile + lane] = out[k];
+    }
 }
 
-template <typename T, int W>
-__device__ void residual(const LevelView<T>& lv, int tile, int lane, const T* PSGB_PHASE_RESTRICT b, const T* PSGB_PHASE_RESTRICT x,
-                         T* PSGB_PHASE_RESTRICT r, const InstanceScalars* sc, int gate) {
-    const int rows = lv.tile_rows[tile];
-    if (!lv.tile_sweep[tile] || !gate_open(sc, lv.tile_inst[tile], gate)) return;
-    if (lane >= rows) return;
-    const int row = tile * kTile + lane;
-    const std::uint32_t P = lv.rows;
-    T s = b[row] - lv.vd[W * P + row] * x[row];
+// r = b - A x
+template <typename T, int W, int R>
+__device__ void residual(const LevelView<T>& lv, int t0, int lane, const T* PSGB_PHASE_RESTRICT b,
+                         const T* PSGB_PHASE_RESTRICT x, T* PSGB_PHASE_RESTRICT r, const InstanceScalars* sc, int gate) {
+    const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
+    bool on[R];
 #pragma unroll
-    for (int j = 0; j < W; ++j) s -= lv.vd[j * P + row] * x[lv.col[j * P + row]];
-    r[row] = s;
+    for (int k = 0; k < R; ++k) on[k] = ts.sweep[k] && gate_open(sc, ts.inst[k], gate);
+    if (!any_of(on)) return;
+    const std::uint32_t P = lv.rows;
+    T out[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int row = ts.tile[k] * kTile + lane;
+        T s = b[row] - lv.vd[W * P + row] * x[row];
+#pragma unroll
+        for (int j = 0; j < W; ++j) s -= lv.vd[j * P + row] * x[lv.col[j * P + row]];
+        out[k] = s;
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (on[k] && lane < ts.rows[k]) r[ts.tile[k] * kTile + lane] = out[k];
+    }
 }
 
-template <typename T, int W>
-__device__ void spmv(const LevelView<T>& lv, int tile, int lane, const T* PSGB_PHASE_RESTRICT x, T* PSGB_PHASE_RESTRICT y) {
-    if (lane >= lv.tile_rows[tile]) return;
-    const int row = tile * kTile + lane;
+// y = A x for every planet
+template <typename T, int W, int R>
+__device__ void spmv(const LevelView<T>& lv, int t0, int lane, const T* PSGB_PHASE_RESTRICT x, T* PSGB_PHASE_RESTRICT y) {
+    const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
     const std::uint32_t P = lv.rows;
-    T s = lv.vd[W * P + row] * x[row];
+    T out[R];
 #pragma unroll
-    for (int j = 0; j < W; ++j) s += lv.vd[j * P + row] * x[lv.col[j * P + row]];
-    y[row] = s;
+    for (int k = 0; k < R; ++k) {
+        const int row = ts.tile[k] * kTile + lane;
+        T s = lv.vd[W * P + row] * x[row];
+#pragma unroll
+        for (int j = 0; j < W; ++j) s += lv.vd[j * P + row] * x[lv.col[j * P + row]];
+        out[k] = s;
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (lane < ts.rows[k]) y[ts.tile[k] * kTile + lane] = out[k];
+    }
 }
 
 // Restriction fused with the coarse level's zero-start sweep: b_c = sum of the members'
 // residuals in ascending fine-row order (the reference's order, heat_transport.cpp:316-319);
 // x_c = omega b_c / diag where the planet smooths on the coarse level.
-template <typename T>
-__device__ void restrict_zero(const LevelView<T>& coarse, int tile, int lane, const std::uint32_t* PSGB_PHASE_RESTRICT moff,
-                              const std::uint32_t* PSGB_PHASE_RESTRICT member, const T* PSGB_PHASE_RESTRICT r, T* PSGB_PHASE_RESTRICT bc,
-                              T* PSGB_PHASE_RESTRICT xc, T omega, const InstanceScalars* sc, int gate) {
-    const int rows = coarse.tile_rows[tile];
-    if (!gate_open(sc, coarse.tile_inst[tile], gate)) return;
-    if (lane >= rows) return;
-    const int row = tile * kTile + lane;
-    const T s = member_sum(member, moff[row], moff[row + 1], r);
-    bc[row] = s;
-    if (coarse.tile_sweep[tile]) xc[row] = omega * coarse.inv[row] * s;
+template <typename T, int R>
+__device__ void restrict_zero(const LevelView<T>& coarse, int t0, int lane, const std::uint32_t* PSGB_PHASE_RESTRICT moff,
+                              const std::uint32_t* PSGB_PHASE_RESTRICT member, const T* PSGB_PHASE_RESTRICT r,
+                              T* PSGB_PHASE_RESTRICT bc, T* PSGB_PHASE_RESTRICT xc, T omega, const InstanceScalars* sc,
+                              int gate) {
+    const TileSet<R> ts = tile_set<R>(coarse.tile_meta, coarse.tiles, t0);
+    bool on[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && gate_open(sc, ts.inst[k], gate);
+    if (!any_of(on)) return;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (!on[k] || lane >= ts.rows[k]) continue;
+        const int row = ts.tile[k] * kTile + lane;
+        const T s = member_sum(member, moff[row], moff[row + 1], r);
+        bc[row] = s;
+        if (ts.sweep[k]) xc[row] = omega * coarse.inv[row] * s;
+    }
 }
 
-template <typename T>
-__device__ void restrict_only(const LevelView<T>& coarse, int tile, int lane, const std::uint32_t* PSGB_PHASE_RESTRICT moff,
-                              const std::uint32_t* PSGB_PHASE_RESTRICT member, const T* PSGB_PHASE_RESTRICT r, T* PSGB_PHASE_RESTRICT bc,
-                              const InstanceScalars* sc, int gate) {
-    if (lane >= coarse.tile_rows[tile]) return;
-    if (!gate_open(sc, coarse.tile_inst[tile], gate)) return;
-    const int row = tile * kTile + lane;
-    bc[row] = member_sum(member, moff[row], moff[row + 1], r);
+template <typename T, int R>
+__device__ void restrict_only(const LevelView<T>& coarse, int t0, int lane, const std::uint32_t* PSGB_PHASE_RESTRICT moff,
+                              const std::uint32_t* PSGB_PHASE_RESTRICT member, const T* PSGB_PHASE_RESTRICT r,
+                              T* PSGB_PHASE_RESTRICT bc, const InstanceScalars* sc, int gate) {
+    const TileSet<R> ts = tile_set<R>(coarse.tile_meta, coarse.tiles, t0);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (lane >= ts.rows[k] || !gate_open(sc, ts.inst[k], gate)) continue;
+        const int row = ts.tile[k] * kTile + lane;
+        bc[row] = member_sum(member, moff[row], moff[row + 1], r);
+    }
 }
 
 // Prolongation fused with the first post-smoothing sweep: with x' = x + e[agg] (formed on
 // the fly for the row and its neighbours), y = x' + omega (D^-1 (b - O x') - x').
-template <typename T, int W>
-__device__ void prolong_smooth(const LevelView<T>& lv, int tile, int lane, const std::int32_t* PSGB_PHASE_RESTRICT agg,
+template <typename T, int W, int R>
+__device__ void prolong_smooth(const LevelView<T>& lv, int t0, int lane, const std::int32_t* PSGB_PHASE_RESTRICT agg,
                                const T* PSGB_PHASE_RESTRICT e, const T* PSGB_PHASE_RESTRICT b, const T* PSGB_PHASE_RESTRICT x,
                                T* PSGB_PHASE_RESTRICT y, T omega, const InstanceScalars* sc, int gate) {
-    const int rows = lv.tile_rows[tile];
-    if (!lv.tile_sweep[tile] || !gate_open(sc, lv.tile_inst[tile], gate)) return;
-    count_bytes(lv.bytes, lane, static_cast<unsigned long long>(rows) * (8ull * W + sizeof(T) * (W + 4ull) + 4ull));
-    if (lane >= rows) return;
-    const int row = tile * kTile + lane;
-    const std::uint32_t P = lv.rows;
-    T s = b[row];
+    const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
+    bool on[R];
 #pragma unroll
-    for (int j = 0; j < W; ++j) {
-        const int c = lv.col[j * P + row];
-        s -= lv.vd[j * P + row] * (x[c] + e[agg[c]]);
+    for (int k = 0; k < R; ++k) on[k] = ts.sweep[k] && gate_open(sc, ts.inst[k], gate);
+    if (!any_of(on)) return;
+    const std::uint32_t P = lv.rows;
+    T out[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int row = ts.tile[k] * kTile + lane;
+        T s = b[row];
+#pragma unroll
+        for (int j = 0; j < W; ++j) {
+            const int c = lv.col[j * P + row];
+            s -= lv.vd[j * P + row] * (x[c] + e[agg[c]]);
+        }
+        const T xo = x[row] + e[agg[row]];
+        out[k] = xo + omega * (lv.inv[row] * s - xo);
     }
-    const T xo = x[row] + e[agg[row]];
-    y[row] = xo + omega * (lv.inv[row] * s - xo);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (!on[k]) continue;
+        count_bytes(lv.bytes, lane, static_cast<unsigned long long>(ts.rows[k]) * (8ull * W + sizeof(T) * (W + 4ull) + 4ull));
+        if (lane < ts.rows[k]) y[ts.tile[k] * kTile + lane] = out[k];
+    }
 }
 
-template <typename T>
-__device__ void prolong(const LevelView<T>& lv, int tile, int lane, const std::int32_t* PSGB_PHASE_RESTRICT agg,
+template <typename T, int R>
+__device__ void prolong(const LevelView<T>& lv, int t0, int lane, const std::int32_t* PSGB_PHASE_RESTRICT agg,
                         const T* PSGB_PHASE_RESTRICT xc, T* PSGB_PHASE_RESTRICT x, const InstanceScalars* sc, int gate) {
-    if (lane >= lv.tile_rows[tile]) return;
-    if (!lv.tile_sweep[tile] || !gate_open(sc, lv.tile_inst[tile], gate)) return;
-    const int row = tile * kTile + lane;
-    x[row] += xc[agg[row]];
+    const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (lane >= ts.rows[k] || !ts.sweep[k] || !gate_open(sc, ts.inst[k], gate)) continue;
+        const int row = ts.tile[k] * kTile + lane;
+        x[row] += xc[agg[row]];
+    }
 }
 
 // Coarsest level: x = A^-1 b for one row of one planet, one warp per row.
@@ -257,26 +451,34 @@ __device__ void dense_block(const DenseTask<T>& task, unsigned k, int lane, cons
 
 // ---- Krylov phases (fine level) ----------------------------------------------------------
 
-__device__ __forceinline__ bool running(const InstanceScalars& s) { return s.status == kRunning; }
-
-template <typename T>
-__device__ void bicg_init(const LevelView<T>& lv, int tile, int gid, int lane, const T* PSGB_PHASE_RESTRICT b, T* x, T* r,
+template <typename T, int R>
+__device__ void bicg_init(const LevelView<T>& lv, int t0, int gid, int lane, const T* PSGB_PHASE_RESTRICT b, T* x, T* r,
                           T* shadow, T* p, T* v, const ReduceCtx& ctx, double tol, int max_it) {
-    const int inst = lv.tile_inst[tile];
-    if (ctx.sc[inst].outer_status != kRunning) return;
-    const int row = lane < lv.tile_rows[tile] ? tile * kTile + lane : -1;
-    T q[1] = {T(0)};
-    if (row >= 0) {
+    const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
+    bool on[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && ctx.sc[ts.inst[k]].outer_status == kRunning;
+    if (!any_of(on)) return;
+    T q[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        q[k] = T(0);
+        if (!on[k] || lane >= ts.rows[k]) continue;
+        const int row = ts.tile[k] * kTile + lane;
         const T bv = b[row];
         x[row] = T(0); r[row] = bv; shadow[row] = bv; p[row] = T(0); v[row] = T(0);
-        q[0] = bv * bv;
+        q[k] = bv * bv;
     }
-    double out[1];
-    if (tile_reduce(q, ctx, inst, tile, out, gid, lane)) {
-        InstanceScalars& s = ctx.sc[inst];
-        s.b_norm = sqrt(out[0]);
+    double out[R];
+    bool fin[R];
+    tiles_reduce<T, 1, R>(q, ctx, ts, on, out, fin, gid, lane);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (!fin[k]) continue;
+        InstanceScalars& s = ctx.sc[ts.inst[k]];
+        s.b_norm = sqrt(out[k]);
         s.target = fmax(tol * s.b_norm, 0.5 * s.outer_target);
-        s.rho = out[0]; s.alpha = 1.0; s.omega = 1.0; s.beta = 0.0;
+        s.rho = out[k]; s.alpha = 1.0; s.omega = 1.0; s.beta = 0.0;
         s.iterations = 0; s.half_done = 0; s.max_iterations = max_it; s.first = 1;
         s.r_norm = s.b_norm;
         s.status = !finite(s.b_norm) ? kNonFinite : (s.b_norm > 0.0 ? kRunning : kConverged);
@@ -284,164 +486,245 @@ __device__ void bicg_init(const LevelView<T>& lv, int tile, int gid, int lane, c
 }
 
 // p = r + beta (p - omega v); first smoothing sweep of M p from zero.
-template <typename T>
-__device__ void bicg_p(const LevelView<T>& lv, int tile, int lane, const T* PSGB_PHASE_RESTRICT r, const T* PSGB_PHASE_RESTRICT v,
+template <typename T, int R>
+__device__ void bicg_p(const LevelView<T>& lv, int t0, int lane, const T* PSGB_PHASE_RESTRICT r, const T* PSGB_PHASE_RESTRICT v,
                        T* p, T* xv, T omega_j, const InstanceScalars* sc) {
-    const int inst = lv.tile_inst[tile];
-    if (lane >= lv.tile_rows[tile] || !running(sc[inst])) return;
-    const int row = tile * kTile + lane;
-    const T beta = T(sc[inst].beta), omega = T(sc[inst].omega);
-    const T pv = r[row] + beta * (p[row] - omega * v[row]);
-    p[row] = pv;
-    if (lv.tile_sweep[tile]) xv[row] = omega_j * lv.inv[row] * pv;
+    const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
+    bool on[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && running(sc[ts.inst[k]]);
+    if (!any_of(on)) return;
+    T pv[R], zv[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int row = ts.tile[k] * kTile + lane;
+        const T beta = T(sc[ts.inst[k]].beta), omega = T(sc[ts.inst[k]].omega);
+        pv[k] = r[row] + beta * (p[row] - omega * v[row]);
+        zv[k] = omega_j * lv.inv[row] * pv[k];
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (!on[k] || lane >= ts.rows[k]) continue;
+        const int row = ts.tile[k] * kTile + lane;
+        p[row] = pv[k];
+        if (ts.sweep[k]) xv[row] = zv[k];
+    }
 }
 
 // out = A in; dot(shadow, out) -> alpha = rho / (shadow . v)
-template <typename T, int W>
-__device__ void bicg_v(const LevelView<T>& lv, int tile, int gid, int lane, const T* PSGB_PHASE_RESTRICT in,
+template <typename T, int W, int R>
+__device__ void bicg_v(const LevelView<T>& lv, int t0, int gid, int lane, const T* PSGB_PHASE_RESTRICT in,
                        T* PSGB_PHASE_RESTRICT out, const T* PSGB_PHASE_RESTRICT shadow, const ReduceCtx& ctx) {
-    const int inst = lv.tile_inst[tile];
-    if (!running(ctx.sc[inst])) return;
-    const int row = lane < lv.tile_rows[tile] ? tile * kTile + lane : -1;
-    T q[1] = {T(0)};
-    if (row >= 0) {
-        const std::uint32_t P = lv.rows;
+    const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
+    bool on[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && running(ctx.sc[ts.inst[k]]);
+    if (!any_of(on)) return;
+    const std::uint32_t P = lv.rows;
+    T q[R], y[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int row = ts.tile[k] * kTile + lane;
         T s = lv.vd[W * P + row] * in[row];
 #pragma unroll
         for (int j = 0; j < W; ++j) s += lv.vd[j * P + row] * in[lv.col[j * P + row]];
-        out[row] = s;
-        q[0] = shadow[row] * s;
+        y[k] = s;
+        q[k] = shadow[row] * s;
     }
-    double sum[1];
-    if (tile_reduce(q, ctx, inst, tile, sum, gid, lane)) {
-        InstanceScalars& s = ctx.sc[inst];
-        if (!finite(sum[0])) { s.status = kNonFinite; return; }
-        if (sum[0] == 0.0) { s.status = kBreakdown; return; }
-        s.alpha = s.rho / sum[0];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const bool store = on[k] && lane < ts.rows[k];
+        if (store) out[ts.tile[k] * kTile + lane] = y[k];
+        if (!store) q[k] = T(0);
+    }
+    double sum[R];
+    bool fin[R];
+    tiles_reduce<T, 1, R>(q, ctx, ts, on, sum, fin, gid, lane);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (!fin[k]) continue;
+        InstanceScalars& s = ctx.sc[ts.inst[k]];
+        if (!finite(sum[k])) { s.status = kNonFinite; continue; }
+        if (sum[k] == 0.0) { s.status = kBreakdown; continue; }
+        s.alpha = s.rho / sum[k];
     }
 }
 
 // s = r - alpha v; ||s||: converged at s -> finish with x += alpha p_hat.
-template <typename T>
-__device__ void bicg_s(const LevelView<T>& lv, int tile, int gid, int lane, const T* PSGB_PHASE_RESTRICT r,
+template <typename T, int R>
+__device__ void bicg_s(const LevelView<T>& lv, int t0, int gid, int lane, const T* PSGB_PHASE_RESTRICT r,
                        const T* PSGB_PHASE_RESTRICT v, T* PSGB_PHASE_RESTRICT s_out, T* xv, T omega_j, const ReduceCtx& ctx) {
-    const int inst = lv.tile_inst[tile];
-    if (!running(ctx.sc[inst])) return;
-    const int row = lane < lv.tile_rows[tile] ? tile * kTile + lane : -1;
-    T q[1] = {T(0)};
-    const T alpha = T(ctx.sc[inst].alpha);
-    if (row >= 0) {
-        const T sv = r[row] - alpha * v[row];
-        s_out[row] = sv;
-        q[0] = sv * sv;
-        if (lv.tile_sweep[tile]) xv[row] = omega_j * lv.inv[row] * sv;
+    const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
+    bool on[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && running(ctx.sc[ts.inst[k]]);
+    if (!any_of(on)) return;
+    T q[R], sv[R], zv[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int row = ts.tile[k] * kTile + lane;
+        const T alpha = T(ctx.sc[ts.inst[k]].alpha);
+        sv[k] = r[row] - alpha * v[row];
+        zv[k] = omega_j * lv.inv[row] * sv[k];
     }
-    double sum[1];
-    if (tile_reduce(q, ctx, inst, tile, sum, gid, lane)) {
-        InstanceScalars& s = ctx.sc[inst];
-        s.s_norm = sqrt(sum[0]);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        q[k] = T(0);
+        if (!on[k] || lane >= ts.rows[k]) continue;
+        const int row = ts.tile[k] * kTile + lane;
+        s_out[row] = sv[k];
+        q[k] = sv[k] * sv[k];
+        if (ts.sweep[k]) xv[row] = zv[k];
+    }
+    double sum[R];
+    bool fin[R];
+    tiles_reduce<T, 1, R>(q, ctx, ts, on, sum, fin, gid, lane);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (!fin[k]) continue;
+        InstanceScalars& s = ctx.sc[ts.inst[k]];
+        s.s_norm = sqrt(sum[k]);
         s.iterations += 1;
-        if (!finite(s.s_norm)) { s.status = kNonFinite; return; }
+        if (!finite(s.s_norm)) { s.status = kNonFinite; continue; }
         if (s.s_norm <= s.target) s.half_done = 1;
     }
 }
 
 // t = A s_hat; (t.t, t.s) -> omega
-template <typename T, int W>
-__device__ void bicg_t(const LevelView<T>& lv, int tile, int gid, int lane, const T* PSGB_PHASE_RESTRICT shat,
+template <typename T, int W, int R>
+__device__ void bicg_t(const LevelView<T>& lv, int t0, int gid, int lane, const T* PSGB_PHASE_RESTRICT shat,
                        T* PSGB_PHASE_RESTRICT t, const T* PSGB_PHASE_RESTRICT s_vec, const ReduceCtx& ctx) {
-    const int inst = lv.tile_inst[tile];
-    const InstanceScalars& sc = ctx.sc[inst];
-    if (!running(sc) || sc.half_done) return;
-    const int row = lane < lv.tile_rows[tile] ? tile * kTile + lane : -1;
-    T q[2] = {T(0), T(0)};
-    if (row >= 0) {
-        const std::uint32_t P = lv.rows;
+    const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
+    bool on[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const InstanceScalars& sc = ctx.sc[ts.inst[k]];
+        on[k] = ts.rows[k] > 0 && running(sc) && !sc.half_done;
+    }
+    if (!any_of(on)) return;
+    const std::uint32_t P = lv.rows;
+    T q[2 * R], y[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int row = ts.tile[k] * kTile + lane;
         T s = lv.vd[W * P + row] * shat[row];
 #pragma unroll
         for (int j = 0; j < W; ++j) s += lv.vd[j * P + row] * shat[lv.col[j * P + row]];
-        t[row] = s;
-        q[0] = s * s;
-        q[1] = s * s_vec[row];
+        y[k] = s;
+        q[2 * k] = s * s;
+        q[2 * k + 1] = s * s_vec[row];
     }
-    double sum[2];
-    if (tile_reduce(q, ctx, inst, tile, sum, gid, lane)) {
-        InstanceScalars& s = ctx.sc[inst];
-        s.omega = sum[0] > 0.0 ? sum[1] / sum[0] : 0.0;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const bool store = on[k] && lane < ts.rows[k];
+        if (store) t[ts.tile[k] * kTile + lane] = y[k];
+        if (!store) { q[2 * k] = T(0); q[2 * k + 1] = T(0); }
+    }
+    double sum[2 * R];
+    bool fin[R];
+    tiles_reduce<T, 2, R>(q, ctx, ts, on, sum, fin, gid, lane);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (!fin[k]) continue;
+        InstanceScalars& s = ctx.sc[ts.inst[k]];
+        s.omega = sum[2 * k] > 0.0 ? sum[2 * k + 1] / sum[2 * k] : 0.0;
         if (!finite(s.omega)) s.status = kNonFinite;
     }
 }
 
 // x += alpha p_hat + omega s_hat; r = s - omega t; (r.r, shadow.r) -> next rho/beta.
-template <typename T>
-__device__ void bicg_x(const LevelView<T>& lv, int tile, int gid, int lane, const T* PSGB_PHASE_RESTRICT phat,
-                       const T* PSGB_PHASE_RESTRICT shat, const T* PSGB_PHASE_RESTRICT s_vec, const T* PSGB_PHASE_RESTRICT t, T* x, T* r,
-                       const T* PSGB_PHASE_RESTRICT shadow, const ReduceCtx& ctx) {
-    __shared__ int last[kGroups];
-    const int inst = lv.tile_inst[tile];
-    const InstanceScalars& sc = ctx.sc[inst];
-    if (!running(sc)) return;
-    const T alpha = T(sc.alpha), omega = T(sc.omega);
-    const int row = lane < lv.tile_rows[tile] ? tile * kTile + lane : -1;
-    if (sc.half_done) {
-        // uniform over the planet: finish at s without a reduction
-        if (row >= 0) x[row] += alpha * phat[row];
-        group_sync(gid);
-        if (lane == 0) {
-            __threadfence();
-            const unsigned begin = ctx.tile_begin[inst], end = ctx.tile_begin[inst + 1];
-            const unsigned ticket = atomicAdd(&ctx.ticket[inst], 1u);
-            last[gid] = ticket == end - begin - 1;
-            if (last[gid]) {
-                ctx.ticket[inst] = 0;
-                InstanceScalars& s = ctx.sc[inst];
-                s.r_norm = s.s_norm;
-                s.half_done = 0;
-                s.status = kConverged;
-            }
+// A planet that converged at s (half_done) finishes with x += alpha p_hat instead; its
+// tiles still count through the reduction so that its last tile closes the iteration.
+template <typename T, int R>
+__device__ void bicg_x(const LevelView<T>& lv, int t0, int gid, int lane, const T* PSGB_PHASE_RESTRICT phat,
+                       const T* PSGB_PHASE_RESTRICT shat, const T* PSGB_PHASE_RESTRICT s_vec, const T* PSGB_PHASE_RESTRICT t,
+                       T* x, T* r, const T* PSGB_PHASE_RESTRICT shadow, const ReduceCtx& ctx) {
+    const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
+    bool on[R], half[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const InstanceScalars& sc = ctx.sc[ts.inst[k]];
+        on[k] = ts.rows[k] > 0 && running(sc);
+        half[k] = sc.half_done != 0;
+    }
+    if (!any_of(on)) return;
+    T q[2 * R], xv[R], rv[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int row = ts.tile[k] * kTile + lane;
+        const InstanceScalars& sc = ctx.sc[ts.inst[k]];
+        const T alpha = T(sc.alpha), omega = T(sc.omega);
+        if (half[k]) {
+            xv[k] = x[row] + alpha * phat[row];
+            rv[k] = T(0);
+        } else {
+            xv[k] = x[row] + (alpha * phat[row] + omega * shat[row]);
+            rv[k] = s_vec[row] - omega * t[row];
         }
-        group_sync(gid);
-        return;
+        q[2 * k] = rv[k] * rv[k];
+        q[2 * k + 1] = shadow[row] * rv[k];
     }
-    T q[2] = {T(0), T(0)};
-    if (row >= 0) {
-        x[row] += alpha * phat[row] + omega * shat[row];
-        const T rv = s_vec[row] - omega * t[row];
-        r[row] = rv;
-        q[0] = rv * rv;
-        q[1] = shadow[row] * rv;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const bool store = on[k] && lane < ts.rows[k];
+        if (store) {
+            const int row = ts.tile[k] * kTile + lane;
+            x[row] = xv[k];
+            if (!half[k]) r[row] = rv[k];
+        }
+        if (!store || half[k]) { q[2 * k] = T(0); q[2 * k + 1] = T(0); }
     }
-    double sum[2];
-    if (tile_reduce(q, ctx, inst, tile, sum, gid, lane)) {
-        InstanceScalars& s = ctx.sc[inst];
-        s.r_norm = sqrt(sum[0]);
-        if (!finite(s.r_norm)) { s.status = kNonFinite; return; }
-        if (s.r_norm <= s.target) { s.status = kConverged; return; }
-        const double rho_next = sum[1];
-        if (rho_next == 0.0 || s.omega == 0.0) { s.status = kBreakdown; return; }
+    double sum[2 * R];
+    bool fin[R];
+    tiles_reduce<T, 2, R>(q, ctx, ts, on, sum, fin, gid, lane);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (!fin[k]) continue;
+        InstanceScalars& s = ctx.sc[ts.inst[k]];
+        if (s.half_done) {
+            s.r_norm = s.s_norm;
+            s.half_done = 0;
+            s.status = kConverged;
+            continue;
+        }
+        s.r_norm = sqrt(sum[2 * k]);
+        if (!finite(s.r_norm)) { s.status = kNonFinite; continue; }
+        if (s.r_norm <= s.target) { s.status = kConverged; continue; }
+        const double rho_next = sum[2 * k + 1];
+        if (rho_next == 0.0 || s.omega == 0.0) { s.status = kBreakdown; continue; }
         s.beta = rho_next / s.rho * (s.alpha / s.omega);
         s.rho = rho_next;
         if (s.iterations >= s.max_iterations) s.status = kCap;
     }
 }
 
-template <typename T>
-__device__ void pcg_init(const LevelView<T>& lv, int tile, int gid, int lane, const T* PSGB_PHASE_RESTRICT b, T* x, T* r,
+template <typename T, int R>
+__device__ void pcg_init(const LevelView<T>& lv, int t0, int gid, int lane, const T* PSGB_PHASE_RESTRICT b, T* x, T* r,
                          T* p, T* xv, T omega_j, const ReduceCtx& ctx, double tol, int max_it) {
-    const int inst = lv.tile_inst[tile];
-    if (ctx.sc[inst].outer_status != kRunning) return;
-    const int row = lane < lv.tile_rows[tile] ? tile * kTile + lane : -1;
-    T q[1] = {T(0)};
-    if (row >= 0) {
+    const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
+    bool on[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && ctx.sc[ts.inst[k]].outer_status == kRunning;
+    if (!any_of(on)) return;
+    T q[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        q[k] = T(0);
+        if (!on[k] || lane >= ts.rows[k]) continue;
+        const int row = ts.tile[k] * kTile + lane;
         const T bv = b[row];
         x[row] = T(0); r[row] = bv; p[row] = T(0);
-        if (lv.tile_sweep[tile]) xv[row] = omega_j * lv.inv[row] * bv;
-        q[0] = bv * bv;
+        if (ts.sweep[k]) xv[row] = omega_j * lv.inv[row] * bv;
+        q[k] = bv * bv;
     }
-    double out[1];
-    if (tile_reduce(q, ctx, inst, tile, out, gid, lane)) {
-        InstanceScalars& s = ctx.sc[inst];
-        s.b_norm = sqrt(out[0]);
+    double out[R];
+    bool fin[R];
+    tiles_reduce<T, 1, R>(q, ctx, ts, on, out, fin, gid, lane);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (!fin[k]) continue;
+        InstanceScalars& s = ctx.sc[ts.inst[k]];
+        s.b_norm = sqrt(out[k]);
         s.target = fmax(tol * s.b_norm, 0.5 * s.outer_target);
         s.r_norm = s.b_norm;
         s.iterations = 0; s.half_done = 0; s.max_iterations = max_it; s.first = 1;
@@ -451,96 +734,144 @@ __device__ void pcg_init(const LevelView<T>& lv, int tile, int gid, int lane, co
 }
 
 // rho = r.z, beta = rho / rho_old
-template <typename T>
-__device__ void pcg_rz(const LevelView<T>& lv, int tile, int gid, int lane, const T* PSGB_PHASE_RESTRICT r,
+template <typename T, int R>
+__device__ void pcg_rz(const LevelView<T>& lv, int t0, int gid, int lane, const T* PSGB_PHASE_RESTRICT r,
                        const T* PSGB_PHASE_RESTRICT z, const ReduceCtx& ctx) {
-    const int inst = lv.tile_inst[tile];
-    if (!running(ctx.sc[inst])) return;
-    const int row = lane < lv.tile_rows[tile] ? tile * kTile + lane : -1;
-    T q[1] = {T(0)};
-    if (row >= 0) q[0] = r[row] * z[row];
-    double sum[1];
-    if (tile_reduce(q, ctx, inst, tile, sum, gid, lane)) {
-        InstanceScalars& s = ctx.sc[inst];
-        if (!finite(sum[0])) { s.status = kNonFinite; return; }
-        if (!(sum[0] > 0.0)) { s.status = s.first ? kConverged : kBreakdown; return; }
-        s.beta = s.first ? 0.0 : sum[0] / s.rho;
-        s.rho = sum[0];
+    const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
+    bool on[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && running(ctx.sc[ts.inst[k]]);
+    if (!any_of(on)) return;
+    T q[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int row = ts.tile[k] * kTile + lane;
+        q[k] = (on[k] && lane < ts.rows[k]) ? r[row] * z[row] : T(0);
+    }
+    double sum[R];
+    bool fin[R];
+    tiles_reduce<T, 1, R>(q, ctx, ts, on, sum, fin, gid, lane);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (!fin[k]) continue;
+        InstanceScalars& s = ctx.sc[ts.inst[k]];
+        if (!finite(sum[k])) { s.status = kNonFinite; continue; }
+        if (!(sum[k] > 0.0)) { s.status = s.first ? kConverged : kBreakdown; continue; }
+        s.beta = s.first ? 0.0 : sum[k] / s.rho;
+        s.rho = sum[k];
         s.first = 0;
     }
 }
 
-template <typename T>
-__device__ void pcg_p(const LevelView<T>& lv, int tile, int lane, const T* PSGB_PHASE_RESTRICT z, T* p,
+template <typename T, int R>
+__device__ void pcg_p(const LevelView<T>& lv, int t0, int lane, const T* PSGB_PHASE_RESTRICT z, T* p,
                       const InstanceScalars* sc) {
-    const int inst = lv.tile_inst[tile];
-    if (lane >= lv.tile_rows[tile] || !running(sc[inst])) return;
-    const int row = tile * kTile + lane;
-    p[row] = z[row] + T(sc[inst].beta) * p[row];
+    const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (lane >= ts.rows[k] || !running(sc[ts.inst[k]])) continue;
+        const int row = ts.tile[k] * kTile + lane;
+        p[row] = z[row] + T(sc[ts.inst[k]].beta) * p[row];
+    }
 }
 
 // q = A p; alpha = rho / p.q
-template <typename T, int W>
-__device__ void pcg_q(const LevelView<T>& lv, int tile, int gid, int lane, const T* PSGB_PHASE_RESTRICT p,
+template <typename T, int W, int R>
+__device__ void pcg_q(const LevelView<T>& lv, int t0, int gid, int lane, const T* PSGB_PHASE_RESTRICT p,
                       T* PSGB_PHASE_RESTRICT q_out, const ReduceCtx& ctx) {
-    const int inst = lv.tile_inst[tile];
-    if (!running(ctx.sc[inst])) return;
-    const int row = lane < lv.tile_rows[tile] ? tile * kTile + lane : -1;
-    T q[1] = {T(0)};
-    if (row >= 0) {
-        const std::uint32_t P = lv.rows;
+    const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
+    bool on[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && running(ctx.sc[ts.inst[k]]);
+    if (!any_of(on)) return;
+    const std::uint32_t P = lv.rows;
+    T q[R], y[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int row = ts.tile[k] * kTile + lane;
         T s = lv.vd[W * P + row] * p[row];
 #pragma unroll
         for (int j = 0; j < W; ++j) s += lv.vd[j * P + row] * p[lv.col[j * P + row]];
-        q_out[row] = s;
-        q[0] = p[row] * s;
+        y[k] = s;
+        q[k] = p[row] * s;
     }
-    double sum[1];
-    if (tile_reduce(q, ctx, inst, tile, sum, gid, lane)) {
-        InstanceScalars& s = ctx.sc[inst];
-        if (!finite(sum[0])) { s.status = kNonFinite; return; }
-        if (!(sum[0] > 0.0)) { s.status = kBreakdown; return; }
-        s.alpha = s.rho / sum[0];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const bool store = on[k] && lane < ts.rows[k];
+        if (store) q_out[ts.tile[k] * kTile + lane] = y[k];
+        if (!store) q[k] = T(0);
+    }
+    double sum[R];
+    bool fin[R];
+    tiles_reduce<T, 1, R>(q, ctx, ts, on, sum, fin, gid, lane);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (!fin[k]) continue;
+        InstanceScalars& s = ctx.sc[ts.inst[k]];
+        if (!finite(sum[k])) { s.status = kNonFinite; continue; }
+        if (!(sum[k] > 0.0)) { s.status = kBreakdown; continue; }
+        s.alpha = s.rho / sum[k];
     }
 }
 
 // x += alpha p; r -= alpha q; ||r|| -> converged?; first sweep of M r.
-template <typename T>
-__device__ void pcg_xr(const LevelView<T>& lv, int tile, int gid, int lane, const T* PSGB_PHASE_RESTRICT p,
+template <typename T, int R>
+__device__ void pcg_xr(const LevelView<T>& lv, int t0, int gid, int lane, const T* PSGB_PHASE_RESTRICT p,
                        const T* PSGB_PHASE_RESTRICT q_in, T* x, T* r, T* xv, T omega_j, const ReduceCtx& ctx) {
-    const int inst = lv.tile_inst[tile];
-    if (!running(ctx.sc[inst])) return;
-    const T alpha = T(ctx.sc[inst].alpha);
-    const int row = lane < lv.tile_rows[tile] ? tile * kTile + lane : -1;
-    T q[1] = {T(0)};
-    if (row >= 0) {
-        x[row] += alpha * p[row];
-        const T rv = r[row] - alpha * q_in[row];
-        r[row] = rv;
-        q[0] = rv * rv;
-        if (lv.tile_sweep[tile]) xv[row] = omega_j * lv.inv[row] * rv;
+    const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
+    bool on[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && running(ctx.sc[ts.inst[k]]);
+    if (!any_of(on)) return;
+    T q[R], xn[R], rn[R], zn[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int row = ts.tile[k] * kTile + lane;
+        const T alpha = T(ctx.sc[ts.inst[k]].alpha);
+        xn[k] = x[row] + alpha * p[row];
+        rn[k] = r[row] - alpha * q_in[row];
+        zn[k] = omega_j * lv.inv[row] * rn[k];
     }
-    double sum[1];
-    if (tile_reduce(q, ctx, inst, tile, sum, gid, lane)) {
-        InstanceScalars& s = ctx.sc[inst];
-        s.r_norm = sqrt(sum[0]);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        q[k] = T(0);
+        if (!on[k] || lane >= ts.rows[k]) continue;
+        const int row = ts.tile[k] * kTile + lane;
+        x[row] = xn[k];
+        r[row] = rn[k];
+        q[k] = rn[k] * rn[k];
+        if (ts.sweep[k]) xv[row] = zn[k];
+    }
+    double sum[R];
+    bool fin[R];
+    tiles_reduce<T, 1, R>(q, ctx, ts, on, sum, fin, gid, lane);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (!fin[k]) continue;
+        InstanceScalars& s = ctx.sc[ts.inst[k]];
+        s.r_norm = sqrt(sum[k]);
         s.iterations += 1;
-        if (!finite(s.r_norm)) { s.status = kNonFinite; return; }
-        if (s.r_norm <= s.target) { s.status = kConverged; return; }
+        if (!finite(s.r_norm)) { s.status = kNonFinite; continue; }
+        if (s.r_norm <= s.target) { s.status = kConverged; continue; }
         if (s.iterations >= s.max_iterations) s.status = kCap;
     }
 }
 
 // ---- FP64 refinement ----------------------------------------------------------------------
 
-__device__ inline void outer_init(const LevelView<double>& lv, int tile, int gid, int lane,
-                                  const double* PSGB_PHASE_RESTRICT b, const ReduceCtx& ctx, double tol,
-                                  const std::uint8_t* PSGB_PHASE_RESTRICT active) {
-    const int inst = lv.tile_inst[tile];
-    if (active != nullptr && !active[inst]) {
+template <int R>
+__device__ void outer_init(const LevelView<double>& lv, int t0, int gid, int lane, const double* PSGB_PHASE_RESTRICT b,
+                           const ReduceCtx& ctx, double tol, const std::uint8_t* PSGB_PHASE_RESTRICT active) {
+    const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
+    bool on[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        on[k] = ts.rows[k] > 0;
+        if (!on[k] || active == nullptr || active[ts.inst[k]]) continue;
         // a planet left out of this step: nothing runs for it
-        if (lane == 0 && static_cast<unsigned>(tile) == ctx.tile_begin[inst]) {
-            InstanceScalars& s = ctx.sc[inst];
+        on[k] = false;
+        if (lane == 0 && static_cast<unsigned>(ts.tile[k]) == ctx.tile_begin[ts.inst[k]]) {
+            InstanceScalars& s = ctx.sc[ts.inst[k]];
             s.outer_status = kConverged;
             s.status = kConverged;
             s.refinements = 0;
@@ -548,15 +879,22 @@ __device__ inline void outer_init(const LevelView<double>& lv, int tile, int gid
             s.outer_r_norm = 0.0;
             s.outer_b_norm = 0.0;
         }
-        return;
     }
-    const int row = lane < lv.tile_rows[tile] ? tile * kTile + lane : -1;
-    double q[1] = {0.0};
-    if (row >= 0) q[0] = dmul(b[row], b[row]);
-    double sum[1];
-    if (tile_reduce(q, ctx, inst, tile, sum, gid, lane)) {
-        InstanceScalars& s = ctx.sc[inst];
-        s.outer_b_norm = sqrt(sum[0]);
+    if (!any_of(on)) return;
+    double q[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int row = ts.tile[k] * kTile + lane;
+        q[k] = (on[k] && lane < ts.rows[k]) ? dmul(b[row], b[row]) : 0.0;
+    }
+    double sum[R];
+    bool fin[R];
+    tiles_reduce<double, 1, R>(q, ctx, ts, on, sum, fin, gid, lane);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (!fin[k]) continue;
+        InstanceScalars& s = ctx.sc[ts.inst[k]];
+        s.outer_b_norm = sqrt(sum[k]);
         s.outer_target = tol * s.outer_b_norm;
         s.tolerance = tol;
         s.refinements = 0;
@@ -567,46 +905,62 @@ __device__ inline void outer_init(const LevelView<double>& lv, int tile, int gid
 }
 
 // r = b - A x in FP64 (FP64 matrix), cast to the inner precision; ||r|| decides.
-template <typename TI, int W>
-__device__ void outer_residual(const LevelView<double>& lv, int tile, int gid, int lane, const double* PSGB_PHASE_RESTRICT b,
+template <typename TI, int W, int R>
+__device__ void outer_residual(const LevelView<double>& lv, int t0, int gid, int lane, const double* PSGB_PHASE_RESTRICT b,
                                const double* PSGB_PHASE_RESTRICT x, double* PSGB_PHASE_RESTRICT r64, TI* PSGB_PHASE_RESTRICT rin,
                                const ReduceCtx& ctx, int max_refine) {
-    const int inst = lv.tile_inst[tile];
-    if (ctx.sc[inst].outer_status != kRunning) return;
-    const int row = lane < lv.tile_rows[tile] ? tile * kTile + lane : -1;
-    double q[1] = {0.0};
-    if (row >= 0) {
-        const std::uint32_t P = lv.rows;
+    const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
+    bool on[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && ctx.sc[ts.inst[k]].outer_status == kRunning;
+    if (!any_of(on)) return;
+    const std::uint32_t P = lv.rows;
+    double q[R], rv[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int row = ts.tile[k] * kTile + lane;
         double s = b[row] - lv.vd[W * P + row] * x[row];
 #pragma unroll
         for (int j = 0; j < W; ++j) s -= lv.vd[j * P + row] * x[lv.col[j * P + row]];
-        r64[row] = s;
-        rin[row] = static_cast<TI>(s);
-        q[0] = s * s;
+        rv[k] = s;
     }
-    double sum[1];
-    if (tile_reduce(q, ctx, inst, tile, sum, gid, lane)) {
-        InstanceScalars& s = ctx.sc[inst];
-        s.outer_r_norm = sqrt(sum[0]);
-        if (!finite(s.outer_r_norm)) { s.outer_status = kNonFinite; return; }
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        q[k] = 0.0;
+        if (!on[k] || lane >= ts.rows[k]) continue;
+        const int row = ts.tile[k] * kTile + lane;
+        r64[row] = rv[k];
+        rin[row] = static_cast<TI>(rv[k]);
+        q[k] = rv[k] * rv[k];
+    }
+    double sum[R];
+    bool fin[R];
+    tiles_reduce<double, 1, R>(q, ctx, ts, on, sum, fin, gid, lane);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (!fin[k]) continue;
+        InstanceScalars& s = ctx.sc[ts.inst[k]];
+        s.outer_r_norm = sqrt(sum[k]);
+        if (!finite(s.outer_r_norm)) { s.outer_status = kNonFinite; continue; }
         if (s.outer_r_norm <= s.outer_target || s.outer_b_norm == 0.0) {
             s.outer_status = kConverged;
             s.status = kConverged;
-            return;
+            continue;
         }
-        if (s.refinements >= max_refine) { s.outer_status = kCap; s.status = kConverged; return; }
+        if (s.refinements >= max_refine) { s.outer_status = kCap; s.status = kConverged; continue; }
         s.refinements += 1;
     }
 }
 
 // x += delta (inner solution), for planets still refining.
-template <typename TI>
-__device__ void outer_update(const LevelView<double>& lv, int tile, int lane, const TI* PSGB_PHASE_RESTRICT delta, double* x,
+template <typename TI, int R>
+__device__ void outer_update(const LevelView<double>& lv, int t0, int lane, const TI* PSGB_PHASE_RESTRICT delta, double* x,
                              const InstanceScalars* sc) {
-    const int inst = lv.tile_inst[tile];
-    if (sc[inst].outer_status != kRunning) return;
-    if (lane < lv.tile_rows[tile]) {
-        const int row = tile * kTile + lane;
+    const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        if (lane >= ts.rows[k] || sc[ts.inst[k]].outer_status != kRunning) continue;
+        const int row = ts.tile[k] * kTile + lane;
         x[row] += static_cast<double>(delta[row]);
     }
 }

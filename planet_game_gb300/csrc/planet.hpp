@@ -132,6 +132,9 @@ struct BatchLevel {
     std::int32_t* tile_inst = nullptr;    // [tiles]
     std::int32_t* tile_rows = nullptr;    // [tiles] valid rows (0..256)
     std::uint8_t* tile_sweep = nullptr;   // [tiles] 1: the planet smooths on this level
+    std::uint32_t* tile_meta = nullptr;   // [tiles rounded up to 4] pack_tile(inst, rows, sweep)
+    std::uint8_t sets_stencil = 1;        // tiles per tile set of the level's launches (tuned)
+    std::uint8_t sets_vector = 1;
     // transition to the next level (absent on the deepest level)
     std::int32_t* agg = nullptr;              // [P] global row on the next level
     std::uint32_t* member_offset = nullptr;   // next level: [P_next + 1]

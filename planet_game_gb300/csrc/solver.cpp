@@ -21,6 +21,10 @@ namespace psgb {
 
 namespace {
 
+// Levels with at least this many tiles (two waves of eight 256-thread blocks on 152 SMs)
+// use multi-tile sets by default.
+constexpr std::uint32_t kSetsMinTiles = 2 * 8 * 152;
+
 template <typename T>
 void upload_to(T* dst, const std::vector<T>& host) {
     if (!host.empty()) PSGB_CUDA(cudaMemcpy(dst, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice));
@@ -114,6 +118,7 @@ namespace {
 
 std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* arena, std::size_t arena_bytes) {
     if (planets.empty()) throw std::invalid_argument("a batch needs at least one planet");
+    if (planets.size() >= kMaxInstances) throw std::invalid_argument("a batch holds fewer than 4,194,304 planets");
     if (arena == nullptr) {
         for (Planet* p : planets) upload_planet(*p);
     }
@@ -180,6 +185,14 @@ std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* ar
         L.tile_inst = b.store.upload(tile_inst);
         L.tile_rows = b.store.upload(tile_rows);
         L.tile_sweep = b.store.upload(tile_sweep);
+        // packed per-tile word for the solve phases, padded to whole groups of four tiles
+        std::vector<std::uint32_t> meta((L.tiles + 3) / 4 * 4, 0u);
+        for (std::uint32_t t = 0; t < L.tiles; ++t) meta[t] = pack_tile(tile_inst[t], tile_rows[t], tile_sweep[t] != 0);
+        L.tile_meta = b.store.upload(meta);
+        // Tile sets pay where a level has several waves of 256-row blocks; small levels
+        // need every block they can get.
+        L.sets_stencil = L.tiles >= kSetsMinTiles ? 2 : 1;
+        L.sets_vector = L.tiles >= kSetsMinTiles ? 4 : 1;
         L.col = b.store.upload(col);
         L.vd64 = b.store.alloc<double>((W + 1) * P);
         L.vd32 = b.store.alloc<float>((W + 1) * P);
@@ -199,7 +212,9 @@ std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* ar
         BatchLevel& F = b.levels[l];
         BatchLevel& C = b.levels[l + 1];
         const std::size_t Pf = F.rows, Wf = F.width, Pc = C.rows, Wc = C.width;
-        std::vector<std::int32_t> agg(Pf, -1);
+        // Rows without an aggregate (padding; planets whose coarsest level this is) point at
+        // coarse row 0 so that the phases may load through them; they never store.
+        std::vector<std::int32_t> agg(Pf, 0);
         std::vector<std::vector<std::uint32_t>> members(Pc);
         std::vector<std::vector<std::uint32_t>> lists((Wc + 1) * Pc);
         for (std::uint32_t i = 0; i < I; ++i) {
@@ -344,8 +359,10 @@ std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* ar
 
 template <typename T>
 static LevelView<T> make_view(const BatchLevel& L, const T* vd, const T* inv) {
-    return LevelView<T>{L.rows, L.width, L.tiles, L.col, vd, inv, L.tile_inst, L.tile_rows, L.tile_sweep,
-                        profile_bytes_counter()};
+    return LevelView<T>{L.rows,       L.width,      L.tiles,      L.col,
+                        vd,           inv,          L.tile_inst,  L.tile_rows,
+                        L.tile_sweep, L.tile_meta,  profile_bytes_counter(),
+                        L.sets_stencil, L.sets_vector};
 }
 
 StepView step_view(const Batch& b) {
