@@ -235,6 +235,36 @@ int psgb_batch_transport_step_masked(psgb_batch* batch, const uint8_t* active, c
                                      double* const* transport_W_m2, psgb_step_report* reports, int memory,
                                      void* stream);
 
+/* Per-level settings of a batch's solve. The reference has no counterpart (its smoother
+ * is fixed, heat_transport.cpp:258-286); the autotuner picks them for the batch's GPU:
+ * launch shapes (tiles per thread; never change a result) and damped-Jacobi sweeps per
+ * level (change the preconditioner; every tuned solve still meets the tolerance). */
+#define PSGB_MAX_LEVELS 12
+typedef struct psgb_tuning {
+    uint32_t levels;                      /* multigrid levels of the batch */
+    int pre_sweeps[PSGB_MAX_LEVELS];      /* per level, 1..8 */
+    int post_sweeps[PSGB_MAX_LEVELS];     /* per level, 0..8 */
+    int stencil_tiles[PSGB_MAX_LEVELS];   /* tiles per thread of the stencil launches: 1 or 2 */
+    int vector_tiles[PSGB_MAX_LEVELS];    /* tiles per thread of the vector launches: 1 or 4 */
+    double jacobi_omega;
+    double tuned_solve_ms;                /* autotune: trial solve with the chosen settings */
+    double default_solve_ms;              /* autotune: trial solve with the settings before */
+    int trial_solves;                     /* autotune: solves timed */
+} psgb_tuning;
+
+/* Times trial solves of one sub-step (the inputs as for psgb_batch_transport_step, every
+ * planet taking part; nothing is written back) and keeps the fastest settings that meet
+ * the options' tolerance on every planet. While a batch holds a tuning, its solves use
+ * it instead of the options' uniform sweeps and damping. */
+int psgb_batch_autotune(psgb_batch* batch, const psgb_step_params* params, const psgb_solve_options* options,
+                        const double* const* t0_K, const double* const* source_W_m2, int memory, void* stream,
+                        psgb_tuning* out);
+/* The settings the batch's solves use now. */
+int psgb_batch_get_tuning(const psgb_batch* batch, psgb_tuning* out);
+/* Applies settings (e.g. a tuning kept from an earlier run); NULL returns to the options'
+ * uniform sweeps and the default launch shapes. */
+int psgb_batch_set_tuning(psgb_batch* batch, const psgb_tuning* tuning);
+
 /* ---- column radiation: sim/planet/atmosphere/atmosphere_column.hpp ----------------
  * column_radiation (humidity variant, :85-104) + cloud_optics (:599-623) +
  * add_cloud_longwave (:627-634) + longwave_fluxes (:125-143) for `cells` columns of

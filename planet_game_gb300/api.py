@@ -352,6 +352,14 @@ def transport_step_noalloc(mesh: PlanetMesh, t0_K, source_W_m2, heat_capacity_J_
     return t_new, h, _step_result(rep)
 
 
+def _tuning_dict(t) -> dict:
+    n = int(t.levels)
+    return {"levels": n, "pre_sweeps": list(t.pre_sweeps[:n]), "post_sweeps": list(t.post_sweeps[:n]),
+            "stencil_tiles": list(t.stencil_tiles[:n]), "vector_tiles": list(t.vector_tiles[:n]),
+            "jacobi_omega": float(t.jacobi_omega), "tuned_solve_ms": float(t.tuned_solve_ms),
+            "default_solve_ms": float(t.default_solve_ms), "trial_solves": int(t.trial_solves)}
+
+
 class Batch:
     """Many planets of uneven levels in one concatenated layout, solved together."""
 
@@ -371,19 +379,57 @@ class Batch:
     def device_bytes(self) -> int:
         return int(capi.load().psgb_batch_device_bytes(self._h))
 
-    def transport_step(self, t0, sources, heat_capacity, dt, conductance=None, edge_conductance=None,
-                       out=None, transport_out=None, active=None, **options):
-        """One sub-step of every planet (or of the planets with active[i] true)."""
+    def _params(self, heat_capacity, dt, conductance, edge_conductance):
         n = len(self.meshes)
         params = (capi.StepParams * n)()
-        keep = []
+        params._keep = []   # the structs own the host arrays they point at
         for i in range(n):
             p = step_params(heat_capacity[i] if np.ndim(heat_capacity) else heat_capacity,
                             dt[i] if np.ndim(dt) else dt,
                             (conductance[i] if np.ndim(conductance) else conductance) if conductance is not None else 0.0,
                             edge_conductance[i] if edge_conductance is not None else None)
-            keep.append(p)
+            params._keep.append(p)
             params[i] = p
+        return params
+
+    def autotune(self, t0, sources, heat_capacity, dt, conductance=None, edge_conductance=None, **options) -> dict:
+        """Pick per-level launch shapes and sweeps by timing trial solves of this sub-step;
+        the batch keeps them (see `tuning`). Nothing is written back."""
+        n = len(self.meshes)
+        params = self._params(heat_capacity, dt, conductance, edge_conductance)
+        mem, st = _memory_of(*t0, *sources)
+        arrs = lambda xs: (C.c_void_p * n)(*[_ptr(x).value for x in xs])
+        o = solve_options(**options)
+        t = capi.Tuning()
+        _raise(capi.load().psgb_batch_autotune(self._h, params, C.byref(o), arrs(t0), arrs(sources), mem, st,
+                                               C.byref(t)))
+        return _tuning_dict(t)
+
+    @property
+    def tuning(self) -> dict:
+        t = capi.Tuning()
+        _raise(capi.load().psgb_batch_get_tuning(self._h, C.byref(t)))
+        return _tuning_dict(t)
+
+    def set_tuning(self, tuning: dict | None) -> None:
+        """Apply per-level settings (a dict from `autotune`/`tuning`); None clears them."""
+        if tuning is None:
+            _raise(capi.load().psgb_batch_set_tuning(self._h, None))
+            return
+        t = capi.Tuning()
+        t.levels = len(tuning["pre_sweeps"])
+        for k in ("pre_sweeps", "post_sweeps", "stencil_tiles", "vector_tiles"):
+            arr = getattr(t, k)
+            for l, v in enumerate(tuning[k]):
+                arr[l] = int(v)
+        t.jacobi_omega = float(tuning["jacobi_omega"])
+        _raise(capi.load().psgb_batch_set_tuning(self._h, C.byref(t)))
+
+    def transport_step(self, t0, sources, heat_capacity, dt, conductance=None, edge_conductance=None,
+                       out=None, transport_out=None, active=None, **options):
+        """One sub-step of every planet (or of the planets with active[i] true)."""
+        n = len(self.meshes)
+        params = self._params(heat_capacity, dt, conductance, edge_conductance)
         on = [True] * n if active is None else [bool(a) for a in active]
         if out is None:
             out = [_empty_like(t0[i], (m.cell_count,)) if on[i] else None for i, m in enumerate(self.meshes)]

@@ -53,6 +53,16 @@ class SolveOptions(C.Structure):
                 ("jacobi_omega", C.c_double), ("schedule", C.c_int)]
 
 
+MAX_LEVELS = 12
+
+
+class Tuning(C.Structure):
+    _fields_ = [("levels", C.c_uint32), ("pre_sweeps", C.c_int * MAX_LEVELS), ("post_sweeps", C.c_int * MAX_LEVELS),
+                ("stencil_tiles", C.c_int * MAX_LEVELS), ("vector_tiles", C.c_int * MAX_LEVELS),
+                ("jacobi_omega", C.c_double), ("tuned_solve_ms", C.c_double), ("default_solve_ms", C.c_double),
+                ("trial_solves", C.c_int)]
+
+
 class SolveReport(C.Structure):
     _fields_ = [("status", C.c_int), ("refinements", C.c_int), ("iterations", C.c_int),
                 ("relative_residual", C.c_double)]
@@ -108,6 +118,10 @@ _SIGNATURES = {
     "psgb_batch_transport_step_masked": (C.c_int, [P, P, C.POINTER(StepParams), C.POINTER(SolveOptions),
                                                    C.POINTER(P), C.POINTER(P), C.POINTER(P), C.POINTER(P),
                                                    C.POINTER(StepReport), C.c_int, P]),
+    "psgb_batch_autotune": (C.c_int, [P, C.POINTER(StepParams), C.POINTER(SolveOptions), C.POINTER(P), C.POINTER(P),
+                                      C.c_int, P, C.POINTER(Tuning)]),
+    "psgb_batch_get_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
+    "psgb_batch_set_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
     "psgb_column_radiation": (C.c_int, [C.c_uint32, C.c_uint32, C.POINTER(ColumnConstants), P, P, P, P, P, P, P,
                                         P, P, P, C.c_int, P]),
     "psgb_substep_mean_insolation": (C.c_int, [P, C.c_int64, P]),

@@ -1,0 +1,237 @@
+// Per-level autotuner (see autotune.hpp).
+//
+// 1. Launch shapes, level by level: the level's Jacobi sweep is timed with one and with two
+//    tiles per thread (and, on the fine level, the vector update with one and four), with
+//    CUDA events on the solve's stream; the faster shape is kept. Levels with fewer than
+//    two waves of tiles keep one tile per thread: there every block counts.
+// 2. Sweeps: whole solves of the batch's system are timed for a list of candidates
+//    (uniform pre/post sweeps and damping, then per-level variants of the coarse levels
+//    around the best); a candidate counts only if every planet meets its tolerance. Each
+//    candidate runs once untimed first (CUDA graph recording), then once timed.
+#include "autotune.hpp"
+
+#include "kernels.hpp"
+#include "profile.hpp"
+
+#include <algorithm>
+#include <chrono>
+#include <stdexcept>
+
+namespace psgb {
+
+namespace {
+
+constexpr std::uint32_t kMinTunedTiles = 2 * 152;   // below: one tile per thread
+constexpr int kTimedLaunches = 10;
+
+struct EventPair {
+    cudaEvent_t a = nullptr, b = nullptr;
+    EventPair() {
+        PSGB_CUDA(cudaEventCreate(&a));
+        PSGB_CUDA(cudaEventCreate(&b));
+    }
+    ~EventPair() {
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+    }
+};
+
+template <typename T>
+LevelView<T> view_of(const Batch& b, std::size_t l);
+template <>
+LevelView<float> view_of<float>(const Batch& b, std::size_t l) { return view32(b, l); }
+template <>
+LevelView<double> view_of<double>(const Batch& b, std::size_t l) { return view64(b, l); }
+
+template <typename T>
+struct Vecs {
+    T *x, *y, *rhs;
+};
+template <typename T>
+Vecs<T> vecs_of(BatchLevel& L);
+template <>
+Vecs<float> vecs_of<float>(BatchLevel& L) { return {L.x32, L.y32, L.b32}; }
+template <>
+Vecs<double> vecs_of<double>(BatchLevel& L) { return {L.x64, L.y64, L.b64}; }
+
+// Mean device time of `launch` over kTimedLaunches launches (after warm-up).
+template <typename F>
+double time_launches(cudaStream_t st, F&& launch) {
+    EventPair ev;
+    for (int k = 0; k < 3; ++k) launch();
+    PSGB_CUDA(cudaEventRecord(ev.a, st));
+    for (int k = 0; k < kTimedLaunches; ++k) launch();
+    PSGB_CUDA(cudaEventRecord(ev.b, st));
+    PSGB_CUDA(cudaEventSynchronize(ev.b));
+    float ms = 0.0F;
+    PSGB_CUDA(cudaEventElapsedTime(&ms, ev.a, ev.b));
+    return static_cast<double>(ms) / kTimedLaunches;
+}
+
+template <typename T>
+void tune_shapes(Batch& b, cudaStream_t st) {
+    const T omega = static_cast<T>(b.smoother.omega);
+    for (std::size_t l = 0; l < b.levels.size(); ++l) {
+        BatchLevel& L = b.levels[l];
+        if (L.tiles < kMinTunedTiles) {
+            L.sets_stencil = 1;
+            L.sets_vector = 1;
+            continue;
+        }
+        const Vecs<T> v = vecs_of<T>(L);
+        double best = 0.0;
+        std::uint8_t pick = 1;
+        for (std::uint8_t sets : {std::uint8_t(1), std::uint8_t(2)}) {
+            L.sets_stencil = sets;
+            const LevelView<T> lv = view_of<T>(b, l);
+            const double ms = time_launches(st, [&] { launch_smooth<T>(lv, v.rhs, v.x, v.y, omega, b.scalars, kGateAlways, st); });
+            if (sets == 1 || ms < best) { best = ms; pick = sets; }
+        }
+        L.sets_stencil = pick;
+        if (l != 0) continue;
+        pick = 1;
+        for (std::uint8_t sets : {std::uint8_t(1), std::uint8_t(4)}) {
+            L.sets_vector = sets;
+            const LevelView<T> lv = view_of<T>(b, l);
+            const double ms = time_launches(st, [&] { launch_smooth_zero<T>(lv, v.rhs, v.x, omega, b.scalars, kGateAlways, st); });
+            if (sets == 1 || ms < best) { best = ms; pick = sets; }
+        }
+        L.sets_vector = pick;
+    }
+    PSGB_CUDA(cudaGetLastError());
+}
+
+struct Sweeps {
+    std::vector<int> pre, post;
+    double omega;
+};
+
+void set_sweeps(Batch& b, const Sweeps& s) {
+    b.smoother.level_pre = s.pre;
+    b.smoother.level_post = s.post;
+    b.smoother.omega = s.omega;
+}
+
+bool all_ok(const Batch& b) {
+    for (const InstanceScalars& s : b.host_scalars)
+        if (s.outer_status != kConverged) return false;
+    return true;
+}
+
+// Wall time of one solve from x = 0 (ms); negative if some planet missed its tolerance.
+double trial(Batch& b, const SolveOptions& opt, const double* rhs, double* x, std::size_t rows, cudaStream_t st,
+             int& count) {
+    ++count;
+    PSGB_CUDA(cudaMemsetAsync(x, 0, rows * sizeof(double), st));
+    PSGB_CUDA(cudaStreamSynchronize(st));
+    const auto t0 = std::chrono::steady_clock::now();
+    solve(b, opt, rhs, x, st);
+    PSGB_CUDA(cudaStreamSynchronize(st));
+    const auto t1 = std::chrono::steady_clock::now();
+    if (!all_ok(b)) return -1.0;
+    return std::chrono::duration<double, std::milli>(t1 - t0).count();
+}
+
+}  // namespace
+
+Tuning current_tuning(const Batch& b) {
+    Tuning t;
+    for (std::size_t l = 0; l < b.levels.size(); ++l) {
+        t.pre.push_back(b.smoother.pre_at(l));
+        t.post.push_back(b.smoother.post_at(l));
+        t.sets_stencil.push_back(b.levels[l].sets_stencil);
+        t.sets_vector.push_back(b.levels[l].sets_vector);
+    }
+    t.omega = b.smoother.omega;
+    return t;
+}
+
+void apply_tuning(Batch& b, const Tuning& t) {
+    const std::size_t depth = b.levels.size();
+    if (t.pre.size() != depth || t.post.size() != depth || t.sets_stencil.size() != depth || t.sets_vector.size() != depth)
+        throw std::invalid_argument("tuning levels do not match the batch");
+    for (std::size_t l = 0; l < depth; ++l) {
+        if (t.pre[l] < 1 || t.pre[l] > 8 || t.post[l] < 0 || t.post[l] > 8)
+            throw std::invalid_argument("tuned sweeps must be 1..8 (pre) and 0..8 (post)");
+        if ((t.sets_stencil[l] != 1 && t.sets_stencil[l] != 2) || (t.sets_vector[l] != 1 && t.sets_vector[l] != 4))
+            throw std::invalid_argument("tuned tile sets must be 1 or 2 (stencil) and 1 or 4 (vector)");
+    }
+    if (!(t.omega > 0.0 && t.omega < 2.0)) throw std::invalid_argument("tuned damping must be in (0, 2)");
+    for (std::size_t l = 0; l < depth; ++l) {
+        b.levels[l].sets_stencil = t.sets_stencil[l];
+        b.levels[l].sets_vector = t.sets_vector[l];
+    }
+    b.smoother.level_pre = t.pre;
+    b.smoother.level_post = t.post;
+    b.smoother.omega = t.omega;
+    b.tuned = true;
+}
+
+void clear_tuning(Batch& b) {
+    b.smoother.level_pre.clear();
+    b.smoother.level_post.clear();
+    default_launch_shapes(b);
+    b.tuned = false;
+}
+
+Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x, cudaStream_t st) {
+    if (!b.matrix_ready) throw std::logic_error("autotune before the matrix was set");
+    if (profile_active()) throw std::logic_error("autotune while a profile records");
+    const std::size_t depth = b.levels.size(), rows = b.levels[0].rows;
+    Tuning result;
+    // Settings before tuning: the reference point.
+    const Sweeps before{std::vector<int>(depth, b.smoother.pre_at(0)), std::vector<int>(depth, b.smoother.post_at(0)),
+                        b.smoother.omega};
+    set_sweeps(b, before);
+    default_launch_shapes(b);
+    trial(b, opt, rhs, x, rows, st, result.trials);
+    result.default_ms = trial(b, opt, rhs, x, rows, st, result.trials);
+
+    // 1. launch shapes (result-neutral)
+    if (opt.precision == kMixed) tune_shapes<float>(b, st);
+    else tune_shapes<double>(b, st);
+
+    // 2. sweeps: uniform candidates, then coarse-level variants of the best
+    auto run = [&](const Sweeps& s) {
+        set_sweeps(b, s);
+        if (trial(b, opt, rhs, x, rows, st, result.trials) < 0.0) return -1.0;
+        return trial(b, opt, rhs, x, rows, st, result.trials);
+    };
+    Sweeps best = before;
+    double best_ms = run(before);
+    const struct { int pre, post; double omega; } uniform[] = {
+        {1, 1, 1.0}, {1, 1, 0.8}, {2, 2, 1.0}, {2, 1, 0.9}, {1, 2, 0.9}, {3, 3, 0.8}};
+    for (const auto& u : uniform) {
+        const Sweeps s{std::vector<int>(depth, u.pre), std::vector<int>(depth, u.post), u.omega};
+        const double ms = run(s);
+        if (ms > 0.0 && (best_ms < 0.0 || ms < best_ms)) { best = s; best_ms = ms; }
+    }
+    if (depth > 1) {
+        const int coarse[][2] = {{1, 1}, {2, 2}, {3, 3}, {4, 4}};
+        const Sweeps base = best;
+        for (const auto& c : coarse) {
+            Sweeps s = base;
+            for (std::size_t l = 1; l < depth; ++l) { s.pre[l] = c[0]; s.post[l] = c[1]; }
+            if (s.pre == base.pre && s.post == base.post) continue;
+            const double ms = run(s);
+            if (ms > 0.0 && (best_ms < 0.0 || ms < best_ms)) { best = s; best_ms = ms; }
+        }
+    }
+    if (best_ms < 0.0) {
+        set_sweeps(b, before);
+        throw std::runtime_error("autotune: no candidate met the tolerance on every planet");
+    }
+    set_sweeps(b, best);
+    b.tuned = true;
+    result.pre = best.pre;
+    result.post = best.post;
+    result.omega = best.omega;
+    for (std::size_t l = 0; l < depth; ++l) {
+        result.sets_stencil.push_back(b.levels[l].sets_stencil);
+        result.sets_vector.push_back(b.levels[l].sets_vector);
+    }
+    result.tuned_ms = best_ms;
+    return result;
+}
+
+}  // namespace psgb

@@ -1,0 +1,38 @@
+// Per-level autotuner of a batch: launch shapes (tiles per thread of the stencil and
+// vector launches, which never change a result) and damped-Jacobi sweeps per level
+// (which change the preconditioner, so they are chosen by timing whole solves that must
+// still meet their tolerance).
+#pragma once
+
+#include "solver.hpp"
+
+#include <vector>
+
+namespace psgb {
+
+struct Tuning {
+    std::vector<int> pre, post;                    // sweeps per level
+    std::vector<std::uint8_t> sets_stencil;        // per level: 1 or 2
+    std::vector<std::uint8_t> sets_vector;         // per level: 1 or 4
+    double omega = 0.8;
+    double tuned_ms = 0.0;                         // trial solve with the chosen settings
+    double default_ms = 0.0;                       // trial solve with the settings before tuning
+    int trials = 0;                                // trial solves timed
+};
+
+// Tunes `b` on the system its matrix holds with right-hand side `rhs` (device, fine
+// layout); `x` is device scratch of the fine layout. Leaves the chosen settings applied
+// (b.tuned) and returns them.
+Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x, cudaStream_t st);
+
+// The batch's current settings.
+Tuning current_tuning(const Batch& b);
+
+// Applies settings (from autotune, possibly cached from an earlier run); the sizes must
+// match the batch's depth.
+void apply_tuning(Batch& b, const Tuning& t);
+
+// Back to uniform sweeps from the solve options and default launch shapes.
+void clear_tuning(Batch& b);
+
+}  // namespace psgb

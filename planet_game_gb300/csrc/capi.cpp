@@ -5,6 +5,7 @@
 // PSGB_ERR_LOGIC, allocation failures -> PSGB_ERR_OUT_OF_MEMORY, CUDA errors ->
 // PSGB_ERR_CUDA; the message is kept per thread for psgb_last_error().
 #include "../../include/planetsim_gb300.h"
+#include "autotune.hpp"
 #include "capi_internal.hpp"
 
 #include "column.hpp"
@@ -117,6 +118,7 @@ void apply_smoother(psgb::Batch& b, const psgb_solve_options* o) {
     psgb_solve_options d;
     psgb_solve_options_default(&d);
     if (o == nullptr) o = &d;
+    if (b.tuned) return;   // per-level settings from an autotune take precedence
     b.smoother.pre = o->pre_sweeps;
     b.smoother.post = o->post_sweeps;
     b.smoother.omega = o->jacobi_omega;
@@ -683,6 +685,87 @@ int psgb_batch_transport_step_masked(psgb_batch* h, const uint8_t* active, const
         require(active != nullptr, "null mask");
         return batch_step(h, active, params, options, t0_K, source_W_m2, t_new_K, transport_W_m2, reports, memory,
                           stream);
+    });
+}
+
+namespace {
+
+void fill_tuning(const psgb::Tuning& t, psgb_tuning* out) {
+    std::memset(out, 0, sizeof(*out));
+    out->levels = static_cast<std::uint32_t>(t.pre.size());
+    for (std::size_t l = 0; l < t.pre.size() && l < PSGB_MAX_LEVELS; ++l) {
+        out->pre_sweeps[l] = t.pre[l];
+        out->post_sweeps[l] = t.post[l];
+        out->stencil_tiles[l] = t.sets_stencil[l];
+        out->vector_tiles[l] = t.sets_vector[l];
+    }
+    out->jacobi_omega = t.omega;
+    out->tuned_solve_ms = t.tuned_ms;
+    out->default_solve_ms = t.default_ms;
+    out->trial_solves = t.trials;
+}
+
+}  // namespace
+
+int psgb_batch_autotune(psgb_batch* h, const psgb_step_params* params, const psgb_solve_options* options,
+                        const double* const* t0_K, const double* const* source_W_m2, int memory, void* stream,
+                        psgb_tuning* out) {
+    return guarded([&] {
+        require(h != nullptr && params != nullptr && t0_K != nullptr && source_W_m2 != nullptr, "null argument");
+        require_memory(memory);
+        const psgb::SolveOptions opt = to_options(options);
+        psgb::Batch& b = *h->batch;
+        require(b.levels.size() <= PSGB_MAX_LEVELS, "batch deeper than PSGB_MAX_LEVELS levels");
+        if (!b.tuned) apply_smoother(b, options);
+        cudaStream_t st = as_stream(stream);
+        std::vector<std::uint8_t> all(b.instances, 1);
+        if (all != b.host_active) {
+            PSGB_CUDA(cudaMemcpyAsync(b.active, all.data(), b.instances, cudaMemcpyHostToDevice, st));
+            b.host_active = all;
+        }
+        b.active_mask = false;
+        assemble_step_matrix(b, params, st);
+        for (std::uint32_t i = 0; i < b.instances; ++i) {
+            const std::size_t n = b.planets[i]->mesh.cells;
+            require(t0_K[i] != nullptr && source_W_m2[i] != nullptr, "null planet array");
+            copy_in(b.t0 + b.fine_base[i], t0_K[i], n * 8, memory, st);
+            copy_in(b.src + b.fine_base[i], source_W_m2[i], n * 8, memory, st);
+        }
+        psgb::launch_step_rhs(step_view(b), b.t0, b.src, b.bb, b.tmp, b.xr, st);
+        const psgb::Tuning t = psgb::autotune(b, opt, b.bb, b.tmp2, st);
+        if (out != nullptr) fill_tuning(t, out);
+        return PSGB_OK;
+    });
+}
+
+int psgb_batch_get_tuning(const psgb_batch* h, psgb_tuning* out) {
+    return guarded([&] {
+        require(h != nullptr && out != nullptr, "null argument");
+        require(h->batch->levels.size() <= PSGB_MAX_LEVELS, "batch deeper than PSGB_MAX_LEVELS levels");
+        fill_tuning(psgb::current_tuning(*h->batch), out);
+        return PSGB_OK;
+    });
+}
+
+int psgb_batch_set_tuning(psgb_batch* h, const psgb_tuning* tuning) {
+    return guarded([&] {
+        require(h != nullptr, "null argument");
+        psgb::Batch& b = *h->batch;
+        if (tuning == nullptr) {
+            psgb::clear_tuning(b);
+            return PSGB_OK;
+        }
+        require(tuning->levels == b.levels.size(), "tuning levels do not match the batch");
+        psgb::Tuning t;
+        for (std::uint32_t l = 0; l < tuning->levels; ++l) {
+            t.pre.push_back(tuning->pre_sweeps[l]);
+            t.post.push_back(tuning->post_sweeps[l]);
+            t.sets_stencil.push_back(static_cast<std::uint8_t>(tuning->stencil_tiles[l]));
+            t.sets_vector.push_back(static_cast<std::uint8_t>(tuning->vector_tiles[l]));
+        }
+        t.omega = tuning->jacobi_omega;
+        psgb::apply_tuning(b, t);
+        return PSGB_OK;
     });
 }
 

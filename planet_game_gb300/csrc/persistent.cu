@@ -153,7 +153,7 @@ template <typename T>
 __device__ __forceinline__ Pair<T> pair_of(const Args<T>& a, int l, T* x) {
     T* X = l == 0 ? x : a.level[l].x;
     T* Y = a.level[l].y;
-    return a.starts_in_x ? Pair<T>{X, Y} : Pair<T>{Y, X};
+    return a.starts_in_x[l] ? Pair<T>{X, Y} : Pair<T>{Y, X};
 }
 
 // x = M^-1 rhs for every planet the gate admits. The fine level's zero-start sweep has
@@ -175,7 +175,7 @@ __device__ bool vcycle(const Args<T>& a, const T* rhs, T* x, int gate) {
         // Planets whose coarsest level is this one (l >= 1) solve it in the level's first
         // phase: they do not smooth here, the others do not need them yet.
         bool dense = l > 0 && a.dense_at[l];
-        for (int k = 1; k < a.pre; ++k) {
+        for (int k = 1; k < a.pre[l]; ++k) {
             if (dense) dense_phase<T>(a, l, L.b, L.x, gate);
             dense = false;
             with_width(lv.width, [&](auto W) {
@@ -205,8 +205,8 @@ __device__ bool vcycle(const Args<T>& a, const T* rhs, T* x, int gate) {
         const T* b = l == 0 ? rhs : L.b;
         const T* e = a.level[l + 1].x;
         Pair<T> p = pair_of(a, l, x);
-        if ((a.pre - 1) & 1) { T* t = p.first; p.first = p.second; p.second = t; }   // where the down sweeps ended
-        if (a.post == 0) {
+        if ((a.pre[l] - 1) & 1) { T* t = p.first; p.first = p.second; p.second = t; }   // where the down sweeps ended
+        if (a.post[l] == 0) {
             PSGB_SETS(lv, G) ph::prolong<T, kPR>(lv, t0, G.lane, L.agg, e, p.first, a.sc, gate);
             PSGB_BARRIER(a);
             continue;
@@ -216,7 +216,7 @@ __device__ bool vcycle(const Args<T>& a, const T* rhs, T* x, int gate) {
         });
         PSGB_BARRIER(a);
         { T* t = p.first; p.first = p.second; p.second = t; }
-        for (int k = 1; k < a.post; ++k) {
+        for (int k = 1; k < a.post[l]; ++k) {
             with_width(lv.width, [&](auto W) {
                 PSGB_SETS(lv, G) ph::smooth<T, decltype(W)::value, kPR>(lv, t0, G.lane, b, p.first, p.second, omega, a.sc, gate);
             });

@@ -55,9 +55,9 @@ struct PersistentArgs {
     int max_iterations;
     int max_refinements;
     int method;                         // psgb::Method
-    int pre, post;
+    int pre[kMaxLevels], post[kMaxLevels];   // sweeps per level
+    unsigned char starts_in_x[kMaxLevels];   // the level's first sweep writes x (sweep parity)
     T omega;
-    int starts_in_x;                    // first sweep of a level writes x (sweep parity)
     PersistentSync sync;
 };
 

@@ -168,11 +168,12 @@ struct DenseCoarse {
 };
 
 struct GraphKey {
-    int precision_bytes, method, iterations, pre, post;
+    int precision_bytes, method, iterations;
+    std::vector<int> shape;            // per level: pre, post sweeps and tile-set sizes
     double omega;
     bool operator<(const GraphKey& o) const {
-        return std::tie(precision_bytes, method, iterations, pre, post, omega) <
-               std::tie(o.precision_bytes, o.method, o.iterations, o.pre, o.post, o.omega);
+        return std::tie(precision_bytes, method, iterations, shape, omega) <
+               std::tie(o.precision_bytes, o.method, o.iterations, o.shape, o.omega);
     }
 };
 
@@ -182,8 +183,14 @@ struct GraphEntry {
 };
 
 struct SmootherConfig {
-    int pre = 2, post = 2;             // damped Jacobi sweeps per level
+    int pre = 2, post = 2;             // damped Jacobi sweeps on every level ...
     double omega = 0.8;                // damping factor
+    std::vector<int> level_pre, level_post;   // ... unless set per level (a tuning)
+    int pre_at(std::size_t l) const { return l < level_pre.size() ? level_pre[l] : pre; }
+    int post_at(std::size_t l) const { return l < level_post.size() ? level_post[l] : post; }
+    // The first (zero-start) sweep of level l writes x when the level's sweep count after
+    // it is even, so that its last sweep ends in x.
+    bool starts_in_x(std::size_t l) const { return ((pre_at(l) - 1 + post_at(l)) % 2) == 0; }
 };
 
 struct Batch {
@@ -193,6 +200,7 @@ struct Batch {
     DenseCoarse dense;
     DeviceStore store;
     SmootherConfig smoother;
+    bool tuned = false;                // per-level settings from an autotune: the options' sweeps do not apply
     std::vector<std::int64_t> fine_base;      // fine-level row base per planet
     // fine-level graph data for assembly and the transport operator
     double* area = nullptr;            // [P0]; 1 in padding rows

@@ -32,6 +32,15 @@ void upload_to(T* dst, const std::vector<T>& host) {
 
 }  // namespace
 
+// Tile sets pay where a level has several waves of 256-row blocks; small levels need
+// every block they can get.
+void default_launch_shapes(Batch& b) {
+    for (BatchLevel& L : b.levels) {
+        L.sets_stencil = L.tiles >= kSetsMinTiles ? 2 : 1;
+        L.sets_vector = L.tiles >= kSetsMinTiles ? 4 : 1;
+    }
+}
+
 std::unique_ptr<Planet> make_planet(std::uint32_t level, double radius_m) {
     auto planet = std::make_unique<Planet>();
     planet->mesh = build_icosphere(level, radius_m);
@@ -155,6 +164,7 @@ std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* ar
         if (l == 0) L.width = 6;
     }
     b.fine_base = b.levels[0].base;
+    default_launch_shapes(b);
 
     // Tile metadata and ELL columns.
     for (std::size_t l = 0; l < depth; ++l) {
@@ -189,10 +199,7 @@ std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* ar
         std::vector<std::uint32_t> meta((L.tiles + 3) / 4 * 4, 0u);
         for (std::uint32_t t = 0; t < L.tiles; ++t) meta[t] = pack_tile(tile_inst[t], tile_rows[t], tile_sweep[t] != 0);
         L.tile_meta = b.store.upload(meta);
-        // Tile sets pay where a level has several waves of 256-row blocks; small levels
-        // need every block they can get.
-        L.sets_stencil = L.tiles >= kSetsMinTiles ? 2 : 1;
-        L.sets_vector = L.tiles >= kSetsMinTiles ? 4 : 1;
+
         L.col = b.store.upload(col);
         L.vd64 = b.store.alloc<double>((W + 1) * P);
         L.vd32 = b.store.alloc<float>((W + 1) * P);
@@ -457,13 +464,9 @@ void prepare_levels(Batch& b, cudaStream_t st) {
     b.matrix_ready = true;
 }
 
-// The buffer the first (zero-start) sweep of a level must write so that, after all
-// of the level's sweeps, the iterate ends in `x`.
-static bool starts_in_x(const SmootherConfig& s) { return ((s.pre - 1 + s.post) % 2) == 0; }
-
 template <typename T>
 T* vcycle_first_target(Batch& b, T* x) {
-    return starts_in_x(b.smoother) ? x : Pick<T>::y(b.levels[0]);
+    return b.smoother.starts_in_x(0) ? x : Pick<T>::y(b.levels[0]);
 }
 
 template <typename T>
@@ -477,8 +480,8 @@ void vcycle(Batch& b, const T* rhs, T* x, int gate, bool first_sweep_done, cudaS
         BatchLevel& L = b.levels[l];
         T* X = (l == 0) ? x : Pick<T>::x(L);
         T* Y = Pick<T>::y(L);
-        cur[l] = starts_in_x(sm) ? X : Y;
-        other[l] = starts_in_x(sm) ? Y : X;
+        cur[l] = sm.starts_in_x(l) ? X : Y;
+        other[l] = sm.starts_in_x(l) ? Y : X;
         rhs_of[l] = (l == 0) ? rhs : Pick<T>::bvec(L);
     }
     // Planets whose only level is the fine one: dense solve there.
@@ -492,7 +495,7 @@ void vcycle(Batch& b, const T* rhs, T* x, int gate, bool first_sweep_done, cudaS
         DenseTask<T> dense{};
         if (l > 0 && b.dense_at[l]) dense = dense_task<T>(b, l, Pick<T>::bvec(L), Pick<T>::x(L));
         if (l == 0 && !first_sweep_done) launch_smooth_zero<T>(lv, rhs_of[l], cur[l], omega, b.scalars, gate, st);
-        for (int k = 1; k < sm.pre; ++k) {
+        for (int k = 1; k < sm.pre_at(l); ++k) {
             launch_smooth<T>(lv, rhs_of[l], cur[l], other[l], omega, b.scalars, gate, st, dense);
             dense = DenseTask<T>{};
             std::swap(cur[l], other[l]);
@@ -512,13 +515,13 @@ void vcycle(Batch& b, const T* rhs, T* x, int gate, bool first_sweep_done, cudaS
         const LevelView<T> lv = Pick<T>::view(b, l);
         BatchLevel& L = b.levels[l];
         const T* e = Pick<T>::x(b.levels[l + 1]);
-        if (sm.post == 0) {
+        if (sm.post_at(l) == 0) {
             launch_prolong<T>(lv, L.agg, e, cur[l], b.scalars, gate, st);
             continue;
         }
         launch_prolong_smooth<T>(lv, L.agg, e, rhs_of[l], cur[l], other[l], omega, b.scalars, gate, st);
         std::swap(cur[l], other[l]);
-        for (int k = 1; k < sm.post; ++k) {
+        for (int k = 1; k < sm.post_at(l); ++k) {
             launch_smooth<T>(lv, rhs_of[l], cur[l], other[l], omega, b.scalars, gate, st);
             std::swap(cur[l], other[l]);
         }
@@ -533,6 +536,19 @@ template float* vcycle_first_target<float>(Batch&, float*);
 namespace {
 
 ReduceCtx reduce_ctx(Batch& b) { return ReduceCtx{b.partial, b.ticket, b.tile_begin, b.scalars}; }
+
+// What a recorded Krylov chunk depends on besides precision, method and length: the
+// per-level sweeps and launch shapes.
+std::vector<int> shape_of(const Batch& b) {
+    std::vector<int> shape;
+    for (std::size_t l = 0; l < b.levels.size(); ++l) {
+        shape.push_back(b.smoother.pre_at(l));
+        shape.push_back(b.smoother.post_at(l));
+        shape.push_back(b.levels[l].sets_stencil);
+        shape.push_back(b.levels[l].sets_vector);
+    }
+    return shape;
+}
 
 bool all_done(Batch& b, cudaStream_t st, bool outer) {
     InstanceScalars* host = b.pinned_scalars != nullptr ? b.pinned_scalars : b.host_scalars.data();
@@ -578,7 +594,7 @@ void krylov_chunk(Batch& b, int method, int count, T* rhs_unused, T* x, cudaStre
 // The chunk as a CUDA graph, recorded once per (precision, method, chunk, smoother).
 template <typename T>
 GraphEntry& chunk_graph(Batch& b, int method, int count, T* x, cudaStream_t st) {
-    const GraphKey key{static_cast<int>(sizeof(T)), method, count, b.smoother.pre, b.smoother.post, b.smoother.omega};
+    const GraphKey key{static_cast<int>(sizeof(T)), method, count, shape_of(b), b.smoother.omega};
     GraphEntry& g = b.graphs[key];
     if (g.exec != nullptr) return g;
     cudaGraph_t graph = nullptr;
@@ -666,10 +682,12 @@ PersistentArgs<T> persistent_args(Batch& b, const SolveOptions& opt, const doubl
     a.max_iterations = opt.max_iterations;
     a.max_refinements = opt.max_refinements;
     a.method = opt.method;
-    a.pre = b.smoother.pre;
-    a.post = b.smoother.post;
+    for (std::size_t l = 0; l < b.levels.size(); ++l) {
+        a.pre[l] = b.smoother.pre_at(l);
+        a.post[l] = b.smoother.post_at(l);
+        a.starts_in_x[l] = b.smoother.starts_in_x(l) ? 1 : 0;
+    }
     a.omega = static_cast<T>(b.smoother.omega);
-    a.starts_in_x = starts_in_x(b.smoother) ? 1 : 0;
     a.sync = PersistentSync{b.sync, b.sync + 1, b.sync + 2};
     return a;
 }

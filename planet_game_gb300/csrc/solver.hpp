@@ -35,6 +35,9 @@ std::unique_ptr<Batch> make_batch(const std::vector<Planet*>& planets);
 // creation; the solver then runs directly on the caller's stream.
 std::unique_ptr<Batch> make_batch_in(const std::vector<Planet*>& planets, void* arena, std::size_t arena_bytes);
 
+// Default tiles per thread of every level's launches (from its tile count).
+void default_launch_shapes(Batch& b);
+
 // The fine-level (padded) row base of planet i inside the batch.
 inline std::int64_t fine_base(const Batch& b, std::size_t i) { return b.fine_base[i]; }
 

@@ -1,0 +1,93 @@
+"""The per-level autotuner: launch shapes never change a result, tuned sweeps still meet
+the 1e-10 residual and 1e-12 closure gates, and a tuning carries over between batches of
+the same planets bit for bit."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def planets(meshes):
+    from planet_game_gb300 import workloads as W
+
+    specs = [(6, 8.1e6), (4, 3.3e6), (5, 6.0e6), (7, 5.0e6), (5, 4.1e6)]
+    ms = [meshes(l, r) for l, r in specs]
+    inputs = [W.step_inputs(m, seed=40 + i, edge_diffusivity=W.lognormal_edge_diffusivity(m.edge_count, 400 + i))
+              for i, m in enumerate(ms)]
+    return ms, inputs
+
+
+def step(batch, inputs, **options):
+    return batch.transport_step([i.t0 for i in inputs], [i.source for i in inputs], 4e7, inputs[0].dt,
+                                edge_conductance=[i.edge_conductance for i in inputs], **options)
+
+
+def test_autotune_meets_the_gates_and_carries_over(planets):
+    import planet_game_gb300 as pg
+
+    ms, inputs = planets
+    batch = pg.Batch(ms)
+    tuning = batch.autotune([i.t0 for i in inputs], [i.source for i in inputs], 4e7, inputs[0].dt,
+                            edge_conductance=[i.edge_conductance for i in inputs], precision="mixed")
+    depth = tuning["levels"]
+    assert depth == len(ms[3].level_rows)
+    assert all(1 <= p <= 8 for p in tuning["pre_sweeps"]) and all(0 <= p <= 8 for p in tuning["post_sweeps"])
+    assert set(tuning["stencil_tiles"]) <= {1, 2} and set(tuning["vector_tiles"]) <= {1, 4}
+    assert tuning["trial_solves"] >= 4 and tuning["tuned_solve_ms"] > 0
+    assert tuning["tuned_solve_ms"] <= 1.25 * tuning["default_solve_ms"]
+    assert batch.tuning["pre_sweeps"] == tuning["pre_sweeps"]
+    out, reps = step(batch, inputs, precision="mixed")
+    for r in reps:
+        assert r.status == 0 and r.relative_residual <= 1e-10 and r.closure <= 1e-12
+    # the same settings on a fresh batch of the same planets: identical results
+    other = pg.Batch(ms)
+    other.set_tuning(tuning)
+    out2, reps2 = step(other, inputs, precision="mixed")
+    for a, b, ra, rb in zip(out, out2, reps, reps2):
+        assert np.array_equal(a, b) and ra.iterations == rb.iterations
+
+
+def test_launch_shapes_never_change_results(planets):
+    import planet_game_gb300 as pg
+
+    ms, inputs = planets
+    batch = pg.Batch(ms)
+    base = batch.tuning
+    outs = []
+    for stencil, vector in ((1, 1), (2, 4), (2, 1), (1, 4)):
+        t = dict(base)
+        t["stencil_tiles"] = [stencil] * base["levels"]
+        t["vector_tiles"] = [vector] * base["levels"]
+        batch.set_tuning(t)
+        for precision in ("mixed", "fp64"):
+            out, reps = step(batch, inputs, precision=precision)
+            assert all(r.status == 0 for r in reps)
+            outs.append((precision, out))
+    for precision in ("mixed", "fp64"):
+        ref = [o for p, o in outs if p == precision]
+        for other in ref[1:]:
+            assert all(np.array_equal(a, b) for a, b in zip(ref[0], other))
+
+
+def test_clearing_a_tuning_restores_the_option_sweeps(planets):
+    import planet_game_gb300 as pg
+
+    ms, inputs = planets
+    plain = pg.Batch(ms)
+    ref, _ = step(plain, inputs, precision="mixed", pre_sweeps=1, post_sweeps=1, jacobi_omega=1.0)
+    batch = pg.Batch(ms)
+    t = batch.tuning
+    t["pre_sweeps"] = [3] * t["levels"]
+    t["post_sweeps"] = [3] * t["levels"]
+    batch.set_tuning(t)
+    tuned, reps = step(batch, inputs, precision="mixed", pre_sweeps=1, post_sweeps=1, jacobi_omega=1.0)
+    assert all(r.status == 0 for r in reps)
+    assert not all(np.array_equal(a, b) for a, b in zip(ref, tuned))     # the tuning took precedence
+    batch.set_tuning(None)
+    back, _ = step(batch, inputs, precision="mixed", pre_sweeps=1, post_sweeps=1, jacobi_omega=1.0)
+    assert all(np.array_equal(a, b) for a, b in zip(ref, back))
+    bad = dict(t)
+    bad["stencil_tiles"] = [3] * t["levels"]
+    with pytest.raises(ValueError, match="tile sets"):
+        batch.set_tuning(bad)
