@@ -359,7 +359,8 @@ def serving_point(args, dev, rate: float, count: int, population=None) -> dict:
         reqs = serve.make_requests(trace, pop, seed=args.seed + 2)
         if name.startswith("continuous"):
             srv = serve.Server(pop, budget_bytes=150e9, precision="mixed", **SOLVER_SERVE)
-            warm = serve.make_requests(trace[:40], pop, seed=args.seed + 3)   # build lanes, record graphs
+            srv.prepare()                                                      # admit and tune the lanes
+            warm = serve.make_requests(trace[:40], pop, seed=args.seed + 3)   # record graphs
             srv.run_trace(warm, realtime=False)
             srv.completed = 0
             try:

@@ -5,9 +5,10 @@
 //    CUDA events on the solve's stream; the faster shape is kept. Levels with fewer than
 //    two waves of tiles keep one tile per thread: there every block counts.
 // 2. Sweeps: whole solves of the batch's system are timed for a list of candidates
-//    (uniform pre/post sweeps and damping, then per-level variants of the coarse levels
-//    around the best); a candidate counts only if every planet meets its tolerance. Each
-//    candidate runs once untimed first (CUDA graph recording), then once timed.
+//    (uniform pre/post sweeps and damping; then, around the best, the coarse levels'
+//    sweeps, the fine level's sweeps, the damping); a candidate counts only if every
+//    planet meets its tolerance. Each candidate runs once untimed first (CUDA graph
+//    recording), then once timed.
 #include "autotune.hpp"
 
 #include "kernels.hpp"
@@ -206,16 +207,38 @@ Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x,
         const double ms = run(s);
         if (ms > 0.0 && (best_ms < 0.0 || ms < best_ms)) { best = s; best_ms = ms; }
     }
+
+    auto consider = [&](const Sweeps& s) {
+        const double ms = run(s);
+        if (ms > 0.0 && (best_ms < 0.0 || ms < best_ms)) { best = s; best_ms = ms; }
+    };
     if (depth > 1) {
-        const int coarse[][2] = {{1, 1}, {2, 2}, {3, 3}, {4, 4}};
+        // coarse levels (cheap, latency-bound sweeps) around the best uniform setting
+        const int coarse[][2] = {{1, 1}, {2, 2}, {3, 3}, {4, 4}, {6, 6}};
         const Sweeps base = best;
         for (const auto& c : coarse) {
             Sweeps s = base;
             for (std::size_t l = 1; l < depth; ++l) { s.pre[l] = c[0]; s.post[l] = c[1]; }
             if (s.pre == base.pre && s.post == base.post) continue;
-            const double ms = run(s);
-            if (ms > 0.0 && (best_ms < 0.0 || ms < best_ms)) { best = s; best_ms = ms; }
+            consider(s);
         }
+        // then the fine level with the best coarse setting
+        const int fine[][2] = {{1, 1}, {2, 2}, {1, 2}, {2, 1}};
+        const Sweeps with_coarse = best;
+        for (const auto& f : fine) {
+            Sweeps s = with_coarse;
+            s.pre[0] = f[0];
+            s.post[0] = f[1];
+            if (s.pre == with_coarse.pre && s.post == with_coarse.post) continue;
+            consider(s);
+        }
+    }
+    // damping around the best
+    for (double omega : {0.9, 1.0}) {
+        if (omega == best.omega) continue;
+        Sweeps s = best;
+        s.omega = omega;
+        consider(s);
     }
     if (best_ms < 0.0) {
         set_sweeps(b, before);

@@ -161,7 +161,7 @@ class Server:
     """The continuous-batching request loop (see the module docstring)."""
 
     def __init__(self, population, budget_bytes: float = 150e9, precision: str = "mixed", method: str = "bicgstab",
-                 device=None, keep_inputs: bool = False, **solver):
+                 device=None, keep_inputs: bool = False, autotune: bool = True, **solver):
         import torch
 
         self.population = population
@@ -177,6 +177,8 @@ class Server:
         self.errors: list[Exception] = []
         self.keep_inputs = keep_inputs
         self.evictions = 0
+        self.autotune = autotune
+        self.tunings: dict[int, dict] = {}     # per level, from the lane's first admission
         self.t_start = time.perf_counter()
 
     # -- admission ------------------------------------------------------------------------
@@ -205,9 +207,31 @@ class Server:
             self.lanes[level] = lane
             lane.thread.start()
         lane.batch = api.Batch([p.mesh for p in self.population[level]])
+        if self.autotune:
+            if level not in self.tunings:
+                self.tunings[level] = self._tune(lane.batch, level)
+            else:
+                lane.batch.set_tuning(self.tunings[level])
         lane.bytes = need
         self.resident_bytes += need
         return lane
+
+    def _tune(self, batch, level) -> dict:
+        """Per-level settings for a lane, from trial solves of a step of its planets."""
+        import torch
+
+        planets = self.population[level]
+        zeros = [torch.zeros_like(p.state) for p in planets]
+        return batch.autotune([p.state for p in planets], zeros, [p.heat_capacity for p in planets],
+                              [p.dt for p in planets], conductance=[p.conductance for p in planets],
+                              edge_conductance=[p.edge_conductance for p in planets], **self.options)
+
+    def prepare(self, levels=None):
+        """Admit (and tune) the lanes of `levels` ahead of traffic, as far as the budget allows."""
+        with self.lock:
+            for level in (levels if levels is not None else sorted(self.population)):
+                if self._admit(level) is None:
+                    break
 
     def submit(self, req: ServedRequest) -> bool:
         """Queue a request; False if its lane cannot be admitted yet (memory)."""

@@ -22,7 +22,7 @@ def test_served_results_equal_the_same_step_alone(population):
 
     trace = W.poisson_trace(120, 2000.0, seed=3, weights=((4, .4), (5, .4), (6, .2)), planets_per_level=3)
     reqs = serve.make_requests(trace, population, seed=4)
-    srv = serve.Server(population, precision="mixed", keep_inputs=True)
+    srv = serve.Server(population, precision="mixed", keep_inputs=True, autotune=False)
     try:
         srv.run_trace(reqs, realtime=True)
     finally:
@@ -37,6 +37,36 @@ def test_served_results_equal_the_same_step_alone(population):
         assert np.array_equal(alone, r.result)
     s = serve.summarize(reqs)
     assert s["ok"] == len(reqs) and s["p99_ms"] >= s["p50_ms"] > 0
+
+
+def test_tuned_lanes_equal_the_planet_alone_with_the_lane_tuning(population):
+    """Lanes autotune at admission; a result equals the planet stepped alone in a one-planet
+    batch that carries the lane's tuning."""
+    import planet_game_gb300 as pg
+    from planet_game_gb300 import serve
+    from planet_game_gb300 import workloads as W
+
+    trace = W.poisson_trace(60, 2000.0, seed=13, weights=((4, .4), (5, .4), (6, .2)), planets_per_level=3)
+    reqs = serve.make_requests(trace, population, seed=14)
+    srv = serve.Server(population, precision="mixed", keep_inputs=True)
+    srv.prepare()
+    assert set(srv.tunings) == {4, 5, 6}
+    try:
+        srv.run_trace(reqs, realtime=True)
+    finally:
+        srv.close()
+    assert all(r.status == 0 for r in reqs)
+    alone = {}
+    for r in reqs:
+        p = population[r.level][r.planet]
+        key = (r.level, r.planet)
+        if key not in alone:
+            alone[key] = pg.Batch([p.mesh])
+            alone[key].set_tuning(srv.tunings[r.level])
+        out, reps = alone[key].transport_step([r.t_in], [r.source], p.heat_capacity, p.dt, conductance=p.conductance,
+                                              edge_conductance=[p.edge_conductance], precision="mixed")
+        assert reps[0].status == 0
+        assert np.array_equal(out[0], r.result)
 
 
 def test_budget_admission_evicts_idle_lanes(population):
