@@ -254,26 +254,28 @@ def run_gb300(args, rank, world, local_rank):
     # profiled pass: the dominant kernel family timed with events on its stream
     import ctypes as C
 
-    ms, nl, nbytes = C.c_double(), C.c_uint64(), C.c_uint64()
-    prof_family = b"persistent" if args.schedule == "persistent" else b"smooth"
-    capi.check(lib.psgb_profile_begin(prof_family))
-    for _ in range(args.steps):
-        step(t0_d, s_d, out_d)
-    capi.check(lib.psgb_profile_end(C.byref(ms), C.byref(nl), C.byref(nbytes)))
     peak, peak_kind = peaks()
-    achieved = nbytes.value / (ms.value / 1e3) / 1e9 if ms.value > 0 else None
-    traffic = None
-    if TRAFFIC_FILE.exists():
-        t = json.loads(TRAFFIC_FILE.read_text()).get(args.workload)
-        if t:
-            traffic = t.get("dram_bytes_per_launch")
-    kernel = {b"smooth": "k_smooth (Jacobi sweep, all levels)",
-              b"persistent": "k_persistent_solve (whole refined solve, all levels)"}[prof_family]
-    roofline = {"bound": "hbm", "kernel": kernel, "achieved": achieved,
-                "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+    traffic_all = json.loads(TRAFFIC_FILE.read_text()) if TRAFFIC_FILE.exists() else {}
+
+    def profile_family(family: bytes, kernel: str) -> dict:
+        ms, nl, nbytes = C.c_double(), C.c_uint64(), C.c_uint64()
+        capi.check(lib.psgb_profile_begin(family))
+        for _ in range(args.steps):
+            step(t0_d, s_d, out_d)
+        capi.check(lib.psgb_profile_end(C.byref(ms), C.byref(nl), C.byref(nbytes)))
+        achieved = nbytes.value / (ms.value / 1e3) / 1e9 if ms.value > 0 else None
+        traffic = (traffic_all.get(args.workload) or {}).get(family.decode())
+        return {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
+                "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                 "launches": int(nl.value), "avg_launch_us": ms.value * 1e3 / max(1, nl.value),
-                "bytes_per_launch": nbytes.value / max(1, nl.value)}
+                "bytes_per_launch": nbytes.value / max(1, nl.value), "share_of_step": ms.value / args.steps / (elapsed * 1e3 / args.steps)}
+
+    if args.schedule == "persistent":
+        roofline = profile_family(b"persistent", "k_persistent_solve (whole refined solve; Jacobi-sweep bytes)")
+        roofline_coarse = None
+    else:
+        roofline = profile_family(b"smooth", "k_smooth / k_prolong_smooth / k_smooth_zero on the fine level")
+        roofline_coarse = profile_family(b"smooth_coarse", "k_smooth / k_prolong_smooth on the coarse levels")
 
     # the plain one-planet-at-a-time FP64 GPU drop-in on the same planets
     plain = None
@@ -327,6 +329,7 @@ def run_gb300(args, rank, world, local_rank):
             "e2e": e2e,
             "serving": serving,
             "roofline": roofline,
+            "roofline_coarse_sweeps": roofline_coarse,
             "cpu_baseline": cpu,
             "clocks": clock,
             "gpu_launches": int(launches),

@@ -235,6 +235,42 @@ int psgb_batch_transport_step_masked(psgb_batch* batch, const uint8_t* active, c
                                      double* const* transport_W_m2, psgb_step_report* reports, int memory,
                                      void* stream);
 
+/* The implicit transport solve with a general tile response: replaces
+ * solve_implicit_transport (heat_transport.cpp:595-772) with its ImplicitTransportSettings
+ * and ImplicitTransportResult (heat_transport.hpp:82-119). The response stays with the
+ * caller, as TransportResponse (heat_transport.hpp:78-80): for sources h (W/m^2) it
+ * writes the cell mean temperatures T(h) (K) and their slopes dT/dh (K m^2/W; 0 holds a
+ * cell); HOST arrays of `cells` values; a nonzero return aborts the solve. The two-point
+ * Laplacians and every linear Newton system run on the GPU (the system with `options`:
+ * precision, method, smoother; its tolerance and iteration cap come from `settings`).
+ * All arrays are HOST arrays in the planet's cell order; `latent_W_m2` may be NULL. */
+typedef int (*psgb_transport_response)(void* user, uint64_t cells, const double* source_W_m2, double* mean_K,
+                                       double* slope_K_m2_W);
+typedef struct psgb_transport_settings {
+    int max_newton_iterations;        /* 30 */
+    int max_line_search_halvings;     /* 12 */
+    double rounding_floor_W_m2;       /* 1e-3: a failed line search below this ends the solve */
+    int max_non_monotone_steps;       /* 4: full steps across kinks above it */
+    double max_non_monotone_growth;   /* 100: largest merit growth such a step may bring */
+    double newton_tolerance_W_m2;     /* 1e-6: stop at max |h - K lap T(h)| below this */
+    double cg_relative_tolerance;     /* 1e-6: inner (inexact) Newton solves */
+    int max_cg_iterations;            /* 2000 */
+} psgb_transport_settings;
+void psgb_transport_settings_default(psgb_transport_settings* out);
+typedef struct psgb_transport_result {
+    double consistency_residual_W_m2; /* max |H - h| at the last iterate */
+    int newton_iterations;
+    int cg_iterations;                /* Krylov iterations summed over Newton iterations */
+    double sum_W;                     /* sum A H: zero to rounding */
+    double absolute_sum_W;            /* sum A |H| */
+    double dissipation_W_K;           /* sum A H T <= 0 */
+} psgb_transport_result;
+int psgb_solve_implicit_transport(psgb_planet* planet, double conductance_W_K, const double* source_floor_W_m2,
+                                  psgb_transport_response response, void* user,
+                                  const psgb_transport_settings* settings, const psgb_solve_options* options,
+                                  const double* latent_W_m2, double* source_out_W_m2, double* mean_out_K,
+                                  psgb_transport_result* result);
+
 /* Per-level settings of a batch's solve. The reference has no counterpart (its smoother
  * is fixed, heat_transport.cpp:258-286); the autotuner picks them for the batch's GPU:
  * launch shapes (tiles per thread; never change a result) and damped-Jacobi sweeps per

@@ -50,6 +50,9 @@ def lib() -> C.CDLL:
         L.orc_bicgstab.restype = C.c_int
         L.orc_bicgstab.argtypes = [P, P, C.c_double, P, P, C.c_double, C.c_int, P]
         L.orc_solve_implicit_transport_linear.argtypes = [P, C.c_double, P, P, C.c_double, C.c_double, P, P, P]
+        L.orc_quartic_response.argtypes = [C.c_uint64, C.c_double, P, P, P, P]
+        L.orc_solve_implicit_transport_quartic.argtypes = [P, C.c_double, C.c_double, P, C.c_double, C.c_double, P,
+                                                           P, P, P]
         L.orc_transport_step.restype = C.c_int
         L.orc_transport_step.argtypes = [P, P, C.c_double, P, C.c_double, C.c_double, P, P, C.c_double, C.c_int,
                                          P, P, P, P]
@@ -117,6 +120,23 @@ class OracleMesh:
         lib().orc_solve_implicit_transport_linear(C.byref(self.graph), K, _p(base), _p(slope), cg_tol, newton_tol,
                                                   _p(mean), _p(src), _p(stats))
         return mean, src, stats
+
+    def solve_implicit_transport_quartic(self, K, a, b, cg_tol=1e-6, newton_tol=1e-6):
+        b = np.ascontiguousarray(b, np.float64)
+        floor, mean, src, stats = np.empty(self.n), np.empty(self.n), np.empty(self.n), np.empty(6)
+        lib().orc_solve_implicit_transport_quartic(C.byref(self.graph), K, a, _p(b), cg_tol, newton_tol, _p(floor),
+                                                   _p(mean), _p(src), _p(stats))
+        return floor, mean, src, stats
+
+
+def quartic_response(a, b, source):
+    """The quartic tile response of the reference's heat-transport test
+    (tests/unit/test_heat_transport.cpp:30-76): T and dT/dh per cell."""
+    b = np.ascontiguousarray(b, np.float64)
+    source = np.ascontiguousarray(source, np.float64)
+    mean, slope = np.empty(len(b)), np.empty(len(b))
+    lib().orc_quartic_response(len(b), a, _p(b), _p(source), _p(mean), _p(slope))
+    return mean, slope
 
 
 class OracleHierarchy:

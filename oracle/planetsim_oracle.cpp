@@ -607,25 +607,25 @@ int orc_bicgstab(void* hp, const orc_graph* g, double K, const double* slope, co
     return it;
 }
 
-// solve_implicit_transport (heat_transport.cpp:595-772) with a linear response
-// mean = base + slope h, floor = -inf. stats = {newton, cg, consistency, sum, abs, dissipation}.
-void orc_solve_implicit_transport_linear(const orc_graph* gp, double K, const double* base, const double* slope_in,
-                                         double cg_tol, double newton_tol, double* mean_out, double* source_out,
-                                         double* stats) {
-    const Graph g = graph_of(gp);
+}  // extern "C"
+
+namespace {
+
+// solve_implicit_transport (heat_transport.cpp:595-772) for a response(at, mean, slope)
+// and a per-cell floor. stats = {newton, cg, consistency, sum, abs, dissipation}.
+template <typename Response>
+void implicit_transport(const Graph& g, double K, Response&& response, const double* floor, double cg_tol,
+                        double newton_tol, double* mean_out, double* source_out, double* stats) {
     const std::size_t n = g.n;
     Hierarchy h = build(g);
     const int max_newton = 30, max_halvings = 12, max_non_monotone = 4;
     const double rounding_floor = 1e-3, max_growth = 100.0;
-    const double floor = -std::numeric_limits<double>::infinity();
     std::vector<double> source(n, 0.0), mean(n), slope(n), diff(n), resid(n), rhs(n), dmean, dsource(n), trial(n),
         tmean(n), tslope(n);
+    for (std::size_t c = 0; c < n; ++c) source[c] = std::max(0.0, floor[c]);
     auto evaluate = [&](const std::vector<double>& at, std::vector<double>& at_mean, std::vector<double>& at_slope,
                         std::vector<double>& at_resid) {
-        for (std::size_t c = 0; c < n; ++c) {
-            at_mean[c] = base[c] + slope_in[c] * at[c];
-            at_slope[c] = slope_in[c];
-        }
+        response(at, at_mean, at_slope);
         diffusion(g, K, at_mean.data(), diff.data());
         return block_sum(n, [&](std::size_t c) {
             at_resid[c] = at[c] - diff[c];
@@ -652,7 +652,7 @@ void orc_solve_implicit_transport_linear(const orc_graph* gp, double K, const do
         for (std::size_t c = 0; c < n; ++c) dsource[c] -= resid[c];
         double step = 1.0, trial_merit = 0.0;
         for (int halving = 0;; ++halving) {
-            for (std::size_t c = 0; c < n; ++c) trial[c] = std::max(source[c] + step * dsource[c], floor);
+            for (std::size_t c = 0; c < n; ++c) trial[c] = std::max(source[c] + step * dsource[c], floor[c]);
             std::vector<double> tresid(n, 0.0);
             trial_merit = evaluate(trial, tmean, tslope, tresid);
             if (trial_merit < merit) {
@@ -665,7 +665,7 @@ void orc_solve_implicit_transport_linear(const orc_graph* gp, double K, const do
                 } else {
                     ++non_monotone;
                     step = 1.0;
-                    for (std::size_t c = 0; c < n; ++c) trial[c] = std::max(source[c] + dsource[c], floor);
+                    for (std::size_t c = 0; c < n; ++c) trial[c] = std::max(source[c] + dsource[c], floor[c]);
                     trial_merit = evaluate(trial, tmean, tslope, tresid);
                     if (std::isfinite(trial_merit) && trial_merit <= max_growth * merit) resid = std::move(tresid);
                     else step = 0.0;
@@ -702,6 +702,79 @@ void orc_solve_implicit_transport_linear(const orc_graph* gp, double K, const do
     stats[3] = s;
     stats[4] = a;
     stats[5] = d;
+}
+
+// The quartic tile response of tests/unit/test_heat_transport.cpp:30-76: a x + r x^4 = b + h
+// per cell, r = 0.75 * 0.97 * sigma, root by the dry Newton of solve_column_surface
+// (sim/planet/surface/column_step.cpp:255-270: start at the smaller single-term root, at
+// most column_newton_iterations = 10 steps, stop once a step is within 4 eps of x); slope
+// dx/dh = 1 / (a + 4 r x^3) (column_step.cpp:273-276). Cells whose index is a multiple of
+// seven hold at 273.15 K with slope 0 when they would warm past it.
+void quartic_response(std::size_t n, double a, const double* b, const double* source, double* mean, double* slope) {
+    const double r = 0.75 * 0.97 * 5.670374419e-8;
+    for (std::size_t c = 0; c < n; ++c) {
+        const double rhs = b[c] + source[c];
+        double x = std::min(rhs / a, std::sqrt(std::sqrt(rhs / r)));
+        for (int it = 0; it < 10; ++it) {
+            const double x3 = x * x * x;
+            const double value = a * x + r * x3 * x - rhs;
+            const double d = a + 4.0 * r * x3;
+            const double step = value / d;
+            x -= step;
+            if (std::abs(step) <= 4.0 * std::numeric_limits<double>::epsilon() * x) break;
+        }
+        if (c % 7U == 0U && x > 273.15) {
+            mean[c] = 273.15;
+            slope[c] = 0.0;
+            continue;
+        }
+        mean[c] = x;
+        slope[c] = 1.0 / (a + 4.0 * r * x * x * x + 0.0);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+// The linear response mean = base + slope h with floor = -inf.
+void orc_solve_implicit_transport_linear(const orc_graph* gp, double K, const double* base, const double* slope_in,
+                                         double cg_tol, double newton_tol, double* mean_out, double* source_out,
+                                         double* stats) {
+    const Graph g = graph_of(gp);
+    const std::vector<double> floor(g.n, -std::numeric_limits<double>::infinity());
+    implicit_transport(
+        g, K,
+        [&](const std::vector<double>& at, std::vector<double>& mean, std::vector<double>& slope) {
+            for (std::size_t c = 0; c < g.n; ++c) {
+                mean[c] = base[c] + slope_in[c] * at[c];
+                slope[c] = slope_in[c];
+            }
+        },
+        floor.data(), cg_tol, newton_tol, mean_out, source_out, stats);
+}
+
+void orc_quartic_response(std::uint64_t n, double a, const double* b, const double* source, double* mean,
+                          double* slope) {
+    quartic_response(n, a, b, source, mean, slope);
+}
+
+// The quartic response with the test's floor (the source that puts a column at 100 K).
+void orc_solve_implicit_transport_quartic(const orc_graph* gp, double K, double a, const double* b, double cg_tol,
+                                          double newton_tol, double* floor_out, double* mean_out, double* source_out,
+                                          double* stats) {
+    const Graph g = graph_of(gp);
+    const double r = 0.75 * 0.97 * 5.670374419e-8;
+    for (std::size_t c = 0; c < g.n; ++c) {
+        const double x = 100.0;
+        floor_out[c] = a * x + r * x * x * x * x - b[c];
+    }
+    implicit_transport(
+        g, K,
+        [&](const std::vector<double>& at, std::vector<double>& mean, std::vector<double>& slope) {
+            quartic_response(g.n, a, b, at.data(), mean.data(), slope.data());
+        },
+        floor_out, cg_tol, newton_tol, mean_out, source_out, stats);
 }
 
 // The implicit sub-step with the linear column response, solved directly with the

@@ -22,6 +22,7 @@
 #include "sim/planet/orbit/climate_calendar.hpp"
 #include "sim/planet/orbit/substep_forcing.hpp"
 #include "sim/planet/planet_parameters.hpp"
+#include "sim/planet/surface/column_step.hpp"
 
 #include <cstdint>
 #include <cstring>
@@ -305,6 +306,69 @@ void refd_solve_linear(void* handle, double conductance, const double* base, con
     settings.newton_tolerance_W_m2 = newton_tolerance;
     const auto result = solve_implicit_transport(graph, conductance, floor, response, settings,
                                                  static_cast<std::size_t>(workers));
+    std::copy(result.mean_K.values().begin(), result.mean_K.values().end(), mean_out);
+    std::copy(result.source_W_m2.values().begin(), result.source_W_m2.values().end(), source_out);
+    stats[0] = result.newton_iterations;
+    stats[1] = result.cg_iterations;
+    stats[2] = result.consistency_residual_W_m2;
+    stats[3] = result.sum_W;
+    stats[4] = result.absolute_sum_W;
+    stats[5] = result.dissipation_W_K;
+}
+
+// ---- the nonlinear transport solve with the reference test's quartic response -----
+// The tile-like response of tests/unit/test_heat_transport.cpp:30-76: a x + r x^4 = b + h
+// per cell, solved by the reference's solve_column_surface; cells whose index is a
+// multiple of seven hold at 273.15 K (slope 0) when they would warm past it.
+static void quartic_response(std::size_t n, double a, const double* b, const Field2D<double>& source,
+                             Field2D<double>& mean, Field2D<double>& slope) {
+    const double radiative = 0.75 * 0.97 * stefan_boltzmann_W_m2_K4;
+    for (std::size_t cell = 0; cell < n; ++cell) {
+        ColumnSystem system;
+        system.a = a;
+        system.b = b[cell] + source[cell];
+        system.radiative = radiative;
+        const double x = solve_column_surface(system);
+        if (cell % 7U == 0U && x > 273.15) {
+            mean[cell] = 273.15;
+            slope[cell] = 0.0;
+            continue;
+        }
+        mean[cell] = x;
+        slope[cell] = system.slope_K_m2_W(x);
+    }
+}
+
+void refd_quartic_response(std::uint64_t n, double a, const double* b, const double* source, double* mean_out,
+                           double* slope_out) {
+    Field2D<double> h(copy_in(source, n)), mean(n, 0.0), slope(n, 0.0);
+    quartic_response(n, a, b, h, mean, slope);
+    std::copy(mean.values().begin(), mean.values().end(), mean_out);
+    std::copy(slope.values().begin(), slope.values().end(), slope_out);
+}
+
+// solve_implicit_transport with that response; the floor is the test's floor(): the
+// source that puts every column at 100 K.
+void refd_solve_quartic(void* handle, double a, double conductance, const double* b, double cg_tolerance,
+                        double newton_tolerance, std::uint64_t workers, double* floor_out, double* mean_out,
+                        double* source_out, double* stats) {
+    const auto& mesh = *static_cast<PlanetMesh*>(handle);
+    const auto graph = mesh_transport_graph(mesh);
+    const std::size_t n = mesh.cell_count();
+    const double radiative = 0.75 * 0.97 * stefan_boltzmann_W_m2_K4;
+    Field2D<double> floor(n, 0.0);
+    for (std::size_t cell = 0; cell < n; ++cell) {
+        const double x = 100.0;
+        floor[cell] = a * x + radiative * x * x * x * x - b[cell];
+    }
+    const TransportResponse response = [&](const Field2D<double>& source, Field2D<double>& mean,
+                                           Field2D<double>& slope) { quartic_response(n, a, b, source, mean, slope); };
+    ImplicitTransportSettings settings;
+    settings.cg_relative_tolerance = cg_tolerance;
+    settings.newton_tolerance_W_m2 = newton_tolerance;
+    const auto result = solve_implicit_transport(graph, conductance, floor, response, settings,
+                                                 static_cast<std::size_t>(workers));
+    std::copy(floor.values().begin(), floor.values().end(), floor_out);
     std::copy(result.mean_K.values().begin(), result.mean_K.values().end(), mean_out);
     std::copy(result.source_W_m2.values().begin(), result.source_W_m2.values().end(), source_out);
     stats[0] = result.newton_iterations;

@@ -17,8 +17,10 @@ from .api import (  # noqa: F401
     laplacian,
     make_icosphere,
     mesh_transport_graph,
+    solve_implicit_transport,
     solve_newton_system,
     solve_options,
+    transport_settings,
     transport_step,
 )
 from .capi import GB300Error  # noqa: F401

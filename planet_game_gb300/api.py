@@ -289,6 +289,66 @@ def solve_newton_system(mesh: PlanetMesh, conductance_W_K: float, slope, rhs, x0
 
 
 @dataclass
+class ImplicitTransportResult:
+    """ImplicitTransportResult (heat_transport.hpp:110-119)."""
+    source_W_m2: np.ndarray
+    mean_K: np.ndarray
+    consistency_residual_W_m2: float
+    newton_iterations: int
+    cg_iterations: int
+    sum_W: float
+    absolute_sum_W: float
+    dissipation_W_K: float
+
+
+def transport_settings(**kw) -> capi.TransportSettings:
+    s = capi.TransportSettings()
+    capi.load().psgb_transport_settings_default(C.byref(s))
+    for k, v in kw.items():
+        setattr(s, k, v)
+    return s
+
+
+def solve_implicit_transport(mesh: PlanetMesh, conductance_W_K: float, source_floor_W_m2, response,
+                             settings: dict | None = None, latent_W_m2=None, **options) -> ImplicitTransportResult:
+    """solve_implicit_transport (heat_transport.cpp:595-772) with a general response.
+
+    `response(source) -> (mean_K, slope_K_m2_W)` runs on the host (numpy arrays of the
+    cells); the Laplacians and the linear Newton systems run on the GPU with `options`
+    (precision, method, sweeps, schedule). Host arrays in and out."""
+    n = mesh.cell_count
+    floor = np.ascontiguousarray(source_floor_W_m2, dtype=np.float64)
+    latent = None if latent_W_m2 is None else np.ascontiguousarray(latent_W_m2, dtype=np.float64)
+    error: list[BaseException] = []
+
+    def trampoline(_user, cells, source, mean, slope):
+        try:
+            h = np.ctypeslib.as_array(source, shape=(cells,))
+            m, s = response(h.copy())
+            np.ctypeslib.as_array(mean, shape=(cells,))[:] = m
+            np.ctypeslib.as_array(slope, shape=(cells,))[:] = s
+            return 0
+        except BaseException as exc:   # reported after the call returns
+            error.append(exc)
+            return 1
+
+    callback = capi.TransportResponse(trampoline)
+    source_out = np.empty(n)
+    mean_out = np.empty(n)
+    res = capi.TransportResult()
+    st = transport_settings(**(settings or {}))
+    o = solve_options(**options)
+    code = capi.load().psgb_solve_implicit_transport(
+        mesh.handle, C.c_double(conductance_W_K), _ptr(floor), callback, None, C.byref(st), C.byref(o),
+        _ptr(latent) if latent is not None else None, _ptr(source_out), _ptr(mean_out), C.byref(res))
+    if error:
+        raise error[0]
+    _raise(code)
+    return ImplicitTransportResult(source_out, mean_out, res.consistency_residual_W_m2, res.newton_iterations,
+                                   res.cg_iterations, res.sum_W, res.absolute_sum_W, res.dissipation_W_K)
+
+
+@dataclass
 class StepResult:
     status: int
     refinements: int

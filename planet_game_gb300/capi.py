@@ -56,6 +56,24 @@ class SolveOptions(C.Structure):
 MAX_LEVELS = 12
 
 
+class TransportSettings(C.Structure):
+    _fields_ = [("max_newton_iterations", C.c_int), ("max_line_search_halvings", C.c_int),
+                ("rounding_floor_W_m2", C.c_double), ("max_non_monotone_steps", C.c_int),
+                ("max_non_monotone_growth", C.c_double), ("newton_tolerance_W_m2", C.c_double),
+                ("cg_relative_tolerance", C.c_double), ("max_cg_iterations", C.c_int)]
+
+
+class TransportResult(C.Structure):
+    _fields_ = [("consistency_residual_W_m2", C.c_double), ("newton_iterations", C.c_int),
+                ("cg_iterations", C.c_int), ("sum_W", C.c_double), ("absolute_sum_W", C.c_double),
+                ("dissipation_W_K", C.c_double)]
+
+
+# int response(void* user, uint64_t cells, const double* source, double* mean, double* slope)
+TransportResponse = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint64, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                C.POINTER(C.c_double))
+
+
 class Tuning(C.Structure):
     _fields_ = [("levels", C.c_uint32), ("pre_sweeps", C.c_int * MAX_LEVELS), ("post_sweeps", C.c_int * MAX_LEVELS),
                 ("stencil_tiles", C.c_int * MAX_LEVELS), ("vector_tiles", C.c_int * MAX_LEVELS),
@@ -122,6 +140,9 @@ _SIGNATURES = {
                                       C.c_int, P, C.POINTER(Tuning)]),
     "psgb_batch_get_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
     "psgb_batch_set_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
+    "psgb_transport_settings_default": (None, [C.POINTER(TransportSettings)]),
+    "psgb_solve_implicit_transport": (C.c_int, [P, C.c_double, P, TransportResponse, P, C.POINTER(TransportSettings),
+                                                C.POINTER(SolveOptions), P, P, P, C.POINTER(TransportResult)]),
     "psgb_column_radiation": (C.c_int, [C.c_uint32, C.c_uint32, C.POINTER(ColumnConstants), P, P, P, P, P, P, P,
                                         P, P, P, C.c_int, P]),
     "psgb_substep_mean_insolation": (C.c_int, [P, C.c_int64, P]),

@@ -56,6 +56,7 @@ struct LevelView {
     unsigned long long* bytes;        // algorithmic-byte counter while profiling, else null
     std::uint8_t sets_stencil;        // tiles per tile set of the stencil launches (1 or 2)
     std::uint8_t sets_vector;         // tiles per tile set of the vector launches (1 or 4)
+    std::uint8_t level;               // multigrid level (0: fine)
 };
 
 struct ReduceCtx {

@@ -248,6 +248,10 @@ __global__ void k_dense_solve(DenseTask<T> dense, const InstanceScalars* sc, int
 
 // ---- launchers -----------------------------------------------------------------
 
+// Jacobi sweeps are accounted as fine-level or coarse-level sweeps.
+template <typename T>
+inline int smooth_family(const LevelView<T>& lv) { return lv.level == 0 ? kFamSmooth : kFamSmoothCoarse; }
+
 void launch_assemble_transport(const LevelView<double>& fine, const double* w, const double* wsum,
                                const double* area, const double* slope, const double* conductance,
                                const double* edge_conductance, double* vd, cudaStream_t stream) {
@@ -279,7 +283,7 @@ void launch_dense_invert(const DenseView& dense, int level, const LevelView<doub
 template <typename T>
 void launch_smooth_zero(const LevelView<T>& lv, const T* b, T* x, T omega, const InstanceScalars* sc,
                         int gate, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamSmooth, stream,
+    PSGB_LAUNCH(smooth_family(lv), stream,
                 PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_smooth_zero<T, R>, ph::tile_sets(lv.tiles, R), kTile, stream,
                                                             lv, b, x, omega, sc, gate)));
 }
@@ -287,7 +291,7 @@ void launch_smooth_zero(const LevelView<T>& lv, const T* b, T* x, T omega, const
 template <typename T>
 void launch_smooth(const LevelView<T>& lv, const T* b, const T* x, T* y, T omega,
                    const InstanceScalars* sc, int gate, cudaStream_t stream, const DenseTask<T>& dense) {
-    PSGB_LAUNCH(kFamSmooth, stream,
+    PSGB_LAUNCH(smooth_family(lv), stream,
                 PSGB_STENCIL_SETS(lv.sets_stencil, PSGB_WIDTHS(lv.width,
                     launch_pdl(k_smooth<T, W, R>, ph::tile_sets(lv.tiles, R) + dense.count, kTile, stream, lv, b, x, y, omega,
                                sc, gate, dense))));
@@ -330,7 +334,7 @@ void launch_restrict_zero(const LevelView<T>& coarse, const std::uint32_t* membe
 template <typename T>
 void launch_prolong_smooth(const LevelView<T>& lv, const std::int32_t* agg, const T* e, const T* b, const T* x,
                            T* y, T omega, const InstanceScalars* sc, int gate, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamSmooth, stream,
+    PSGB_LAUNCH(smooth_family(lv), stream,
                 PSGB_STENCIL_SETS(lv.sets_stencil, PSGB_WIDTHS(lv.width,
                     launch_pdl(k_prolong_smooth<T, W, R>, ph::tile_sets(lv.tiles, R), kTile, stream, lv, agg, e, b, x, y, omega,
                                sc, gate))));

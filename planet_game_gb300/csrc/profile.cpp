@@ -26,7 +26,7 @@ constexpr std::size_t kMaxEvents = 1 << 16;
 
 const char* const kNames[kFamCount] = {"smooth", "residual", "restrict", "prolong", "dense", "krylov_spmv",
                                        "krylov_vector", "refine", "setup", "step", "operator", "column",
-                                       "persistent"};
+                                       "persistent", "smooth_coarse"};
 
 }  // namespace
 
@@ -44,7 +44,11 @@ namespace {
 unsigned long long* g_bytes_counter = nullptr;   // device, allocated by the first profile_begin
 }
 
-unsigned long long* profile_bytes_counter() { return profile_active() ? g_bytes_counter : nullptr; }
+unsigned long long* profile_bytes_counter(int level) {
+    const int f = g_profile.family;
+    const bool counted = f == kFamPersistent || (f == kFamSmooth && level == 0) || (f == kFamSmoothCoarse && level > 0);
+    return counted ? g_bytes_counter : nullptr;
+}
 
 std::uint64_t profile_bytes_exchange() {
     if (g_bytes_counter == nullptr) return 0;

@@ -13,7 +13,7 @@
 namespace psgb {
 
 enum KernelFamily : int {
-    kFamSmooth = 0,      // Jacobi sweeps (k_smooth, k_smooth_zero)
+    kFamSmooth = 0,      // fine-level Jacobi sweeps (k_smooth, k_smooth_zero, k_prolong_smooth)
     kFamResidual,        // V-cycle residual
     kFamRestrict,        // restriction
     kFamProlong,         // prolongation
@@ -26,6 +26,7 @@ enum KernelFamily : int {
     kFamOperator,        // finite-volume operators
     kFamColumn,          // column radiation
     kFamPersistent,      // the persistent cooperative solve (one launch per solve)
+    kFamSmoothCoarse,    // Jacobi sweeps of the coarse levels
     kFamCount
 };
 
@@ -46,9 +47,10 @@ bool profile_active();
 void set_capturing(bool on);
 void count_graph_kernels(std::uint64_t kernels);
 
-// Device counter of algorithmic bytes the solve phases move while a profile records
-// (null otherwise); allocated on the first profile_begin.
-unsigned long long* profile_bytes_counter();
+// Device counter of the algorithmic bytes that the Jacobi sweeps of multigrid level `level`
+// move, while a profile of their family records (null otherwise); allocated on the first
+// profile_begin.
+unsigned long long* profile_bytes_counter(int level);
 std::uint64_t profile_bytes_exchange();
 
 bool profile_begin(int family);

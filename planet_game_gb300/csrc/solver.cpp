@@ -365,11 +365,11 @@ std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* ar
 }  // namespace
 
 template <typename T>
-static LevelView<T> make_view(const BatchLevel& L, const T* vd, const T* inv) {
-    return LevelView<T>{L.rows,       L.width,      L.tiles,      L.col,
-                        vd,           inv,          L.tile_inst,  L.tile_rows,
-                        L.tile_sweep, L.tile_meta,  profile_bytes_counter(),
-                        L.sets_stencil, L.sets_vector};
+static LevelView<T> make_view(const BatchLevel& L, const T* vd, const T* inv, std::size_t level) {
+    return LevelView<T>{L.rows,         L.width,        L.tiles,      L.col,
+                        vd,             inv,            L.tile_inst,  L.tile_rows,
+                        L.tile_sweep,   L.tile_meta,    profile_bytes_counter(static_cast<int>(level)),
+                        L.sets_stencil, L.sets_vector,  static_cast<std::uint8_t>(level)};
 }
 
 StepView step_view(const Batch& b) {
@@ -380,12 +380,12 @@ StepView step_view(const Batch& b) {
 
 LevelView<double> view64(const Batch& b, std::size_t level) {
     const BatchLevel& L = b.levels[level];
-    return make_view<double>(L, L.vd64, L.inv64);
+    return make_view<double>(L, L.vd64, L.inv64, level);
 }
 
 LevelView<float> view32(const Batch& b, std::size_t level) {
     const BatchLevel& L = b.levels[level];
-    return make_view<float>(L, L.vd32, L.inv32);
+    return make_view<float>(L, L.vd32, L.inv32, level);
 }
 
 namespace {

@@ -58,7 +58,42 @@ def load(reference: Path) -> C.CDLL:
     R.refd_column_radiation.argtypes = [C.c_uint32, P, P, P, C.c_double, C.c_double, C.c_double, P, P, P, P, P, P]
     R.refd_insolation.argtypes = [P, C.c_int64, P]
     R.refd_insolation_nodes.argtypes = [C.c_int64, P]
+    R.refd_quartic_response.argtypes = [C.c_uint64, C.c_double, P, P, P, P]
+    R.refd_solve_quartic.argtypes = [P, C.c_double, C.c_double, P, C.c_double, C.c_double, C.c_uint64, P, P, P, P]
     return R
+
+
+def quartic_cases(R) -> None:
+    """The nonlinear transport solve with the reference test's quartic response
+    (tests/unit/test_heat_transport.cpp:30-76, 112-146) at L4: heat capacities of a month
+    and of ten minutes, the test's conductance and ten times it. The local forcings b put
+    each column's equilibrium between 200 and 320 K (seeded here instead of the test's
+    keyed random stream); a sample of response evaluations pins the response itself."""
+    m = R.refd_mesh_new(4, RADIUS)
+    cnt = np.zeros(4, np.uint64)
+    R.refd_mesh_counts(P_(m), p(cnt))
+    n = int(cnt[0])
+    rng = np.random.default_rng(20260930)
+    radiative = 0.75 * 0.97 * 5.670374419e-8
+    out = {}
+    for ia, a in enumerate((0.04 + 0.37, 1.0e5 / 600.0)):
+        target = 200.0 + 120.0 * rng.random(n)
+        b = a * target + radiative * target ** 4
+        out[f"b{ia}"] = b
+        out[f"a{ia}"] = a
+        h = rng.normal(0.0, 40.0, n)
+        mean, slope = np.empty(n), np.empty(n)
+        R.refd_quartic_response(n, a, p(b), p(h), p(mean), p(slope))
+        out[f"probe_source{ia}"], out[f"probe_mean{ia}"], out[f"probe_slope{ia}"] = h, mean, slope
+        for factor in (1.0, 10.0):
+            K = factor * 0.5 * RADIUS * RADIUS
+            floor, mean, src, stats = np.empty(n), np.empty(n), np.empty(n), np.empty(6)
+            R.refd_solve_quartic(m, a, K, p(b), 1e-6, 1e-6, 4, p(floor), p(mean), p(src), p(stats))
+            key = f"{ia}_{int(factor)}"
+            out[f"K{key}"], out[f"floor{key}"], out[f"mean{key}"] = K, floor, mean
+            out[f"source{key}"], out[f"stats{key}"] = src, stats
+    np.savez_compressed(HERE / "newton_quartic_L4.npz", **out)
+    R.refd_mesh_free(m)
 
 
 def mesh_arrays(R, m) -> dict:
@@ -247,4 +282,11 @@ def main(reference: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    reference = Path(args[0] if args else "/root/reference")
+    if "--quartic" in sys.argv:   # only the nonlinear-transport fixture
+        quartic_cases(load(reference))
+        print("quartic fixture written")
+    else:
+        main(reference)
+        quartic_cases(load(reference))

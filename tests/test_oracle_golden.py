@@ -111,3 +111,29 @@ def test_planted_oracle_mistake_is_caught(L4):
     a["edge_length_m"] = w
     bad = O.OracleMesh(a)
     assert not np.array_equal(bad.laplacian(g["x64"]), g["laplacian64"])
+
+
+@pytest.mark.parametrize("case", [0, 1])
+def test_quartic_response_bit_identical(case):
+    """The oracle's quartic tile response equals the reference's (solve_column_surface)."""
+    g = golden("newton_quartic_L4.npz")
+    mean, slope = O.quartic_response(float(g[f"a{case}"]), g[f"b{case}"], g[f"probe_source{case}"])
+    assert np.array_equal(mean, g[f"probe_mean{case}"])
+    assert np.array_equal(slope, g[f"probe_slope{case}"])
+
+
+@pytest.mark.parametrize("case,factor", [(0, 1), (0, 10), (1, 1), (1, 10)])
+def test_nonlinear_newton_driver_bit_identical(L4, case, factor):
+    """The oracle's restatement of solve_implicit_transport with the quartic response is
+    the reference's, bit for bit, and meets the reference test's gates
+    (test_heat_transport.cpp:140-144)."""
+    g = golden("newton_quartic_L4.npz")
+    key = f"{case}_{factor}"
+    floor, mean, src, stats = L4.solve_implicit_transport_quartic(float(g[f"K{key}"]), float(g[f"a{case}"]),
+                                                                  g[f"b{case}"])
+    assert np.array_equal(floor, g[f"floor{key}"])
+    assert np.array_equal(mean, g[f"mean{key}"])
+    assert np.array_equal(src, g[f"source{key}"])
+    assert np.array_equal(stats, g[f"stats{key}"])
+    assert stats[2] <= 1e-6 and abs(stats[3]) <= 1e-13 * stats[4] and stats[5] <= 0.0
+    assert np.all(mean[::7] <= 273.15)
