@@ -320,6 +320,9 @@ def run_gb300(args, rank, world, local_rank):
                 "planets": len(meshes), "cells": cells, "precision": prec, "krylov": "BiCGSTAB",
                 "smoother": smoother_desc(tuning), "tuning": tuning, "tolerance": 1e-10,
                 "krylov_iterations_per_step": sum(r.iterations for r in reps), "refinements_last_step": max(refinements),
+                "krylov_iterations_per_planet": {"min": min(r.iterations for r in reps),
+                                                 "median": float(np.median([r.iterations for r in reps])),
+                                                 "max": max(r.iterations for r in reps)},
                 "cell_iterations_per_s": statistics.mean(iters) * world / (elapsed / args.steps),
                 "l2": "working set larger than the 129 MB L2 (no flush needed)" if cells > 1_000_000 else
                       "working set may be L2 resident",

@@ -286,6 +286,7 @@ typedef struct psgb_tuning {
     double tuned_solve_ms;                /* autotune: trial solve with the chosen settings */
     double default_solve_ms;              /* autotune: trial solve with the settings before */
     int trial_solves;                     /* autotune: solves timed */
+    int coarse_tail_level;                /* levels from this one down run one block per planet; 0: none */
 } psgb_tuning;
 
 /* Times trial solves of one sub-step (the inputs as for psgb_batch_transport_step, every

@@ -417,7 +417,8 @@ def _tuning_dict(t) -> dict:
     return {"levels": n, "pre_sweeps": list(t.pre_sweeps[:n]), "post_sweeps": list(t.post_sweeps[:n]),
             "stencil_tiles": list(t.stencil_tiles[:n]), "vector_tiles": list(t.vector_tiles[:n]),
             "jacobi_omega": float(t.jacobi_omega), "tuned_solve_ms": float(t.tuned_solve_ms),
-            "default_solve_ms": float(t.default_solve_ms), "trial_solves": int(t.trial_solves)}
+            "default_solve_ms": float(t.default_solve_ms), "trial_solves": int(t.trial_solves),
+            "coarse_tail_level": int(t.coarse_tail_level)}
 
 
 class Batch:
@@ -483,6 +484,7 @@ class Batch:
             for l, v in enumerate(tuning[k]):
                 arr[l] = int(v)
         t.jacobi_omega = float(tuning["jacobi_omega"])
+        t.coarse_tail_level = int(tuning.get("coarse_tail_level", 0))
         _raise(capi.load().psgb_batch_set_tuning(self._h, C.byref(t)))
 
     def transport_step(self, t0, sources, heat_capacity, dt, conductance=None, edge_conductance=None,

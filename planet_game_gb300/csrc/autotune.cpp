@@ -99,6 +99,17 @@ void tune_shapes(Batch& b, cudaStream_t st) {
         }
         L.sets_vector = pick;
     }
+    // Where the coarse tail starts (or none): time whole V-cycles over every planet.
+    T* rhs = vecs_of<T>(b.levels[0]).rhs;
+    T* x = vecs_of<T>(b.levels[0]).x;
+    double best = -1.0;
+    int pick = b.tail_level;
+    for (int tail = 0; tail < static_cast<int>(b.levels.size()); ++tail) {
+        b.tail_level = tail;
+        const double ms = time_launches(st, [&] { vcycle<T>(b, rhs, x, kGateAlways, false, st); });
+        if (best < 0.0 || ms < best) { best = ms; pick = tail; }
+    }
+    b.tail_level = pick;
     PSGB_CUDA(cudaGetLastError());
 }
 
@@ -144,6 +155,7 @@ Tuning current_tuning(const Batch& b) {
         t.sets_vector.push_back(b.levels[l].sets_vector);
     }
     t.omega = b.smoother.omega;
+    t.tail_level = b.tail_level;
     return t;
 }
 
@@ -158,6 +170,8 @@ void apply_tuning(Batch& b, const Tuning& t) {
             throw std::invalid_argument("tuned tile sets must be 1 or 2 (stencil) and 1 or 4 (vector)");
     }
     if (!(t.omega > 0.0 && t.omega < 2.0)) throw std::invalid_argument("tuned damping must be in (0, 2)");
+    if (t.tail_level < 0 || static_cast<std::size_t>(t.tail_level) >= depth)
+        throw std::invalid_argument("the coarse tail level must be 0 (none) or a level below the fine one");
     for (std::size_t l = 0; l < depth; ++l) {
         b.levels[l].sets_stencil = t.sets_stencil[l];
         b.levels[l].sets_vector = t.sets_vector[l];
@@ -165,6 +179,7 @@ void apply_tuning(Batch& b, const Tuning& t) {
     b.smoother.level_pre = t.pre;
     b.smoother.level_post = t.post;
     b.smoother.omega = t.omega;
+    b.tail_level = t.tail_level;
     b.tuned = true;
 }
 
@@ -240,6 +255,20 @@ Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x,
         s.omega = omega;
         consider(s);
     }
+    // where the coarse tail starts, with the chosen sweeps (whole solves: the tail's cost
+    // depends on how many sweeps its levels run)
+    set_sweeps(b, best);
+    {
+        const int chosen = b.tail_level;
+        int pick = chosen;
+        for (int tail = 0; tail < static_cast<int>(depth); ++tail) {
+            if (tail == chosen) continue;
+            b.tail_level = tail;
+            const double ms = run(best);
+            if (ms > 0.0 && ms < best_ms) { best_ms = ms; pick = tail; }
+        }
+        b.tail_level = pick;
+    }
     if (best_ms < 0.0) {
         set_sweeps(b, before);
         throw std::runtime_error("autotune: no candidate met the tolerance on every planet");
@@ -253,6 +282,7 @@ Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x,
         result.sets_stencil.push_back(b.levels[l].sets_stencil);
         result.sets_vector.push_back(b.levels[l].sets_vector);
     }
+    result.tail_level = b.tail_level;
     result.tuned_ms = best_ms;
     return result;
 }

@@ -15,6 +15,7 @@ struct Tuning {
     std::vector<std::uint8_t> sets_stencil;        // per level: 1 or 2
     std::vector<std::uint8_t> sets_vector;         // per level: 1 or 4
     double omega = 0.8;
+    int tail_level = 0;                            // coarse tail from this level (0: none)
     double tuned_ms = 0.0;                         // trial solve with the chosen settings
     double default_ms = 0.0;                       // trial solve with the settings before tuning
     int trials = 0;                                // trial solves timed

@@ -703,6 +703,7 @@ void fill_tuning(const psgb::Tuning& t, psgb_tuning* out) {
     out->tuned_solve_ms = t.tuned_ms;
     out->default_solve_ms = t.default_ms;
     out->trial_solves = t.trials;
+    out->coarse_tail_level = t.tail_level;
 }
 
 }  // namespace
@@ -764,6 +765,7 @@ int psgb_batch_set_tuning(psgb_batch* h, const psgb_tuning* tuning) {
             t.sets_vector.push_back(static_cast<std::uint8_t>(tuning->vector_tiles[l]));
         }
         t.omega = tuning->jacobi_omega;
+        t.tail_level = tuning->coarse_tail_level;
         psgb::apply_tuning(b, t);
         return PSGB_OK;
     });

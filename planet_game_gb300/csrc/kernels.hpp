@@ -64,6 +64,7 @@ struct ReduceCtx {
     unsigned* ticket;                 // [instances]
     const std::uint32_t* tile_begin;  // [instances + 1] fine-level tile ranges
     InstanceScalars* sc;
+    std::uint32_t instances;
 };
 
 struct DenseView {

@@ -157,15 +157,51 @@ __device__ __forceinline__ bool finite(double v) { return isfinite(v); }
 // the sequentially consistent __threadfence(), which the reduction does not need.
 __device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 
-// Tile partial sums (in the tiles' precision A) to FP64 partials, one fence and one ticket
-// per run of the set's tiles that belong to one planet; the last tile set of a planet to
-// arrive (integer ticket, so arrival order never matters) sums that planet's partials in
-// tile order. fin[k]: lane 0 holds planet inst[k]'s sums in out[k * NQ + q].
-template <typename A, int NQ, int R>
+// How a reduction phase completes its planets' sums.
+//   kTicket:   after writing its tile partials, a tile set takes one ticket per run of
+//              its tiles that belong to one planet (release fence, integer atomic); the
+//              last tile set of a planet to arrive sums that planet's partials and
+//              performs the scalar step (the persistent solver: no launch boundary follows).
+//   kDeferred: tile sets only write their partials; a finish launch per planet sums them
+//              and performs the same step (the kernel schedule: no block waits on a ticket).
+// Both sum a planet's partials with sum_partials, so both give the same bits.
+enum Completion : int { kTicket = 0, kDeferred = 1 };
+
+// A planet's tile partials in tile order: lane l sums tiles begin + l, + 256, ... (four
+// loads in flight at a time), then the group's fixed tree; result in lane 0.
+template <int NQ>
+__device__ __forceinline__ void sum_partials(const ReduceCtx& ctx, int inst, int gid, int lane, double (&acc)[NQ]) {
+    const unsigned begin = ctx.tile_begin[inst], end = ctx.tile_begin[inst + 1];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) acc[q] = 0.0;
+    for (unsigned t0 = begin + lane; t0 < end; t0 += 4 * kTile) {
+        double p[4][NQ];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const unsigned t = t0 + u * kTile;
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) p[u][q] = t < end ? __ldcg(&ctx.partial[t * 8 + q]) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (t0 + u * kTile < end) {
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) acc[q] += p[u][q];
+            }
+        }
+    }
+    group_sum<double, NQ>(acc, gid, lane);
+}
+
+// Tile partial sums (in the tiles' precision A) to FP64 partials, then completion C.
+// fin[k]: (kTicket only) lane 0 holds planet inst[k]'s sums in out[k * NQ + q].
+template <typename A, int NQ, int R, int C>
 __device__ void tiles_reduce(A (&v)[R * NQ], const ReduceCtx& ctx, const TileSet<R>& ts, const bool (&on)[R],
                              double (&out)[R * NQ], bool (&fin)[R], int gid, int lane) {
     __shared__ int last[kGroups][R];
     group_sum<A, R * NQ>(v, gid, lane);
+#pragma unroll
+    for (int k = 0; k < R; ++k) fin[k] = false;
     if (lane == 0) {
 #pragma unroll
         for (int k = 0; k < R; ++k) {
@@ -173,56 +209,41 @@ __device__ void tiles_reduce(A (&v)[R * NQ], const ReduceCtx& ctx, const TileSet
 #pragma unroll
             for (int q = 0; q < NQ; ++q) ctx.partial[ts.tile[k] * 8 + q] = static_cast<double>(v[k * NQ + q]);
         }
-        fence_acq_rel_gpu();
-#pragma unroll
-        for (int k = 0; k < R; ++k) last[gid][k] = 0;
-        for (int k = 0; k < R;) {
-            if (!on[k]) { ++k; continue; }
-            int e = k + 1;
-            while (e < R && on[e] && ts.inst[e] == ts.inst[k]) ++e;
-            const int inst = ts.inst[k];
-            const unsigned n = ctx.tile_begin[inst + 1] - ctx.tile_begin[inst];
-            const unsigned add = static_cast<unsigned>(e - k);
-            const unsigned old = atomicAdd(&ctx.ticket[inst], add);
-            last[gid][k] = (old + add == n) ? 1 : 0;
-            k = e;
-        }
-        fence_acq_rel_gpu();
     }
-    group_sync(gid);
-#pragma unroll
-    for (int k = 0; k < R; ++k) {
-        fin[k] = false;
-        if (!last[gid][k]) continue;
-        fence_acq_rel_gpu();
-        const int inst = ts.inst[k];
-        const unsigned begin = ctx.tile_begin[inst], end = ctx.tile_begin[inst + 1];
-        double acc[NQ];
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) acc[q] = 0.0;
-        // partials of this lane's tiles, in tile order; four loads in flight at a time
-        for (unsigned t0 = begin + lane; t0 < end; t0 += 4 * kTile) {
-            double p[4][NQ];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const unsigned t = t0 + u * kTile;
-#pragma unroll
-                for (int q = 0; q < NQ; ++q) p[u][q] = t < end ? __ldcg(&ctx.partial[t * 8 + q]) : 0.0;
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                if (t0 + u * kTile < end) {
-#pragma unroll
-                    for (int q = 0; q < NQ; ++q) acc[q] += p[u][q];
-                }
-            }
-        }
-        group_sum<double, NQ>(acc, gid, lane);
+    if constexpr (C == kDeferred) {
+        return;
+    } else {
         if (lane == 0) {
-            ctx.ticket[inst] = 0;
+            fence_acq_rel_gpu();
+            bool any_last = false;
 #pragma unroll
-            for (int q = 0; q < NQ; ++q) out[k * NQ + q] = acc[q];
-            fin[k] = true;
+            for (int k = 0; k < R; ++k) last[gid][k] = 0;
+            for (int k = 0; k < R;) {
+                if (!on[k]) { ++k; continue; }
+                int e = k + 1;
+                while (e < R && on[e] && ts.inst[e] == ts.inst[k]) ++e;
+                const int inst = ts.inst[k];
+                const unsigned n = ctx.tile_begin[inst + 1] - ctx.tile_begin[inst];
+                const unsigned add = static_cast<unsigned>(e - k);
+                const unsigned old = atomicAdd(&ctx.ticket[inst], add);
+                last[gid][k] = (old + add == n) ? 1 : 0;
+                any_last = any_last || old + add == n;
+                k = e;
+            }
+            if (any_last) fence_acq_rel_gpu();   // acquire: the other tile sets' partials
+        }
+        group_sync(gid);
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            if (!last[gid][k]) continue;
+            double acc[NQ];
+            sum_partials<NQ>(ctx, ts.inst[k], gid, lane, acc);
+            if (lane == 0) {
+                ctx.ticket[ts.inst[k]] = 0;
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) out[k * NQ + q] = acc[q];
+                fin[k] = true;
+            }
         }
     }
 }
@@ -449,9 +470,169 @@ __device__ void dense_block(const DenseTask<T>& task, unsigned k, int lane, cons
     dense_row<T>(task.dense, blk.x, row, lane & 31, task.inv, task.b, task.x);
 }
 
+// ---- scalar steps: one planet, once its sums are complete (ticket or finish launch) ----
+
+__device__ inline void finish_bicg_init(InstanceScalars& s, const double* sum, double tol, int max_it) {
+    s.b_norm = sqrt(sum[0]);
+    s.target = fmax(tol * s.b_norm, 0.5 * s.outer_target);
+    s.rho = sum[0]; s.alpha = 1.0; s.omega = 1.0; s.beta = 0.0;
+    s.iterations = 0; s.half_done = 0; s.max_iterations = max_it; s.first = 1;
+    s.r_norm = s.b_norm;
+    s.status = !finite(s.b_norm) ? kNonFinite : (s.b_norm > 0.0 ? kRunning : kConverged);
+}
+
+// alpha = rho / (shadow . v)
+__device__ inline void finish_bicg_v(InstanceScalars& s, const double* sum) {
+    if (!finite(sum[0])) { s.status = kNonFinite; return; }
+    if (sum[0] == 0.0) { s.status = kBreakdown; return; }
+    s.alpha = s.rho / sum[0];
+}
+
+// ||s||: converged at s -> the iteration finishes with x += alpha p_hat.
+__device__ inline void finish_bicg_s(InstanceScalars& s, const double* sum) {
+    s.s_norm = sqrt(sum[0]);
+    s.iterations += 1;
+    if (!finite(s.s_norm)) { s.status = kNonFinite; return; }
+    if (s.s_norm <= s.target) s.half_done = 1;
+}
+
+// omega = (t.s) / (t.t)
+__device__ inline void finish_bicg_t(InstanceScalars& s, const double* sum) {
+    s.omega = sum[0] > 0.0 ? sum[1] / sum[0] : 0.0;
+    if (!finite(s.omega)) s.status = kNonFinite;
+}
+
+// ||r||, rho_next = shadow . r -> beta; a planet converged at s closes its iteration.
+__device__ inline void finish_bicg_x(InstanceScalars& s, const double* sum) {
+    if (s.half_done) {
+        s.r_norm = s.s_norm;
+        s.half_done = 0;
+        s.status = kConverged;
+        return;
+    }
+    s.r_norm = sqrt(sum[0]);
+    if (!finite(s.r_norm)) { s.status = kNonFinite; return; }
+    if (s.r_norm <= s.target) { s.status = kConverged; return; }
+    const double rho_next = sum[1];
+    if (rho_next == 0.0 || s.omega == 0.0) { s.status = kBreakdown; return; }
+    s.beta = rho_next / s.rho * (s.alpha / s.omega);
+    s.rho = rho_next;
+    if (s.iterations >= s.max_iterations) s.status = kCap;
+}
+
+__device__ inline void finish_pcg_init(InstanceScalars& s, const double* sum, double tol, int max_it) {
+    s.b_norm = sqrt(sum[0]);
+    s.target = fmax(tol * s.b_norm, 0.5 * s.outer_target);
+    s.r_norm = s.b_norm;
+    s.iterations = 0; s.half_done = 0; s.max_iterations = max_it; s.first = 1;
+    s.rho = 0.0; s.beta = 0.0; s.alpha = 0.0;
+    s.status = !finite(s.b_norm) ? kNonFinite : (s.b_norm > 0.0 ? kRunning : kConverged);
+}
+
+// rho = r.z, beta = rho / rho_old
+__device__ inline void finish_pcg_rz(InstanceScalars& s, const double* sum) {
+    if (!finite(sum[0])) { s.status = kNonFinite; return; }
+    if (!(sum[0] > 0.0)) { s.status = s.first ? kConverged : kBreakdown; return; }
+    s.beta = s.first ? 0.0 : sum[0] / s.rho;
+    s.rho = sum[0];
+    s.first = 0;
+}
+
+// alpha = rho / p.q
+__device__ inline void finish_pcg_q(InstanceScalars& s, const double* sum) {
+    if (!finite(sum[0])) { s.status = kNonFinite; return; }
+    if (!(sum[0] > 0.0)) { s.status = kBreakdown; return; }
+    s.alpha = s.rho / sum[0];
+}
+
+// ||r|| -> converged?
+__device__ inline void finish_pcg_xr(InstanceScalars& s, const double* sum) {
+    s.r_norm = sqrt(sum[0]);
+    s.iterations += 1;
+    if (!finite(s.r_norm)) { s.status = kNonFinite; return; }
+    if (s.r_norm <= s.target) { s.status = kConverged; return; }
+    if (s.iterations >= s.max_iterations) s.status = kCap;
+}
+
+__device__ inline void finish_outer_init(InstanceScalars& s, const double* sum, double tol) {
+    s.outer_b_norm = sqrt(sum[0]);
+    s.outer_target = tol * s.outer_b_norm;
+    s.tolerance = tol;
+    s.refinements = 0;
+    s.inner_total = 0;
+    s.outer_status = !finite(s.outer_b_norm) ? kNonFinite : kRunning;
+    s.status = kConverged;   // no inner solve runs until an inner init starts one
+}
+
+// ||b - A x|| in FP64 decides: converged, capped, or one more refinement.
+__device__ inline void finish_outer_residual(InstanceScalars& s, const double* sum, int max_refine) {
+    s.outer_r_norm = sqrt(sum[0]);
+    if (!finite(s.outer_r_norm)) { s.outer_status = kNonFinite; return; }
+    if (s.outer_r_norm <= s.outer_target || s.outer_b_norm == 0.0) {
+        s.outer_status = kConverged;
+        s.status = kConverged;
+        return;
+    }
+    if (s.refinements >= max_refine) { s.outer_status = kCap; s.status = kConverged; return; }
+    s.refinements += 1;
+}
+
+// ---- finish launches of the kernel schedule (kDeferred) --------------------------------------
+
+enum FinishKind : int {
+    kFinBicgInit, kFinBicgV, kFinBicgS, kFinBicgT, kFinBicgX,
+    kFinPcgInit, kFinPcgRz, kFinPcgQ, kFinPcgXr,
+    kFinOuterInit, kFinOuterResidual,
+};
+
+struct FinishParams {
+    double tol;
+    int max_it;
+    int max_refine;
+    const std::uint8_t* active;
+};
+
+template <int K>
+struct FinishSums {
+    static constexpr int value = (K == kFinBicgT || K == kFinBicgX) ? 2 : 1;
+};
+
+// The planets whose tiles took part in the reduction: the phase's own gate.
+template <int K>
+__device__ __forceinline__ bool finish_gate(const InstanceScalars& s, int inst, const FinishParams& p) {
+    if constexpr (K == kFinBicgInit || K == kFinPcgInit || K == kFinOuterResidual) return s.outer_status == kRunning;
+    else if constexpr (K == kFinOuterInit) return p.active == nullptr || p.active[inst] != 0;
+    else if constexpr (K == kFinBicgT) return s.status == kRunning && !s.half_done;
+    else return s.status == kRunning;
+}
+
+template <int K>
+__device__ __forceinline__ void finish_step(InstanceScalars& s, const double* sum, const FinishParams& p) {
+    if constexpr (K == kFinBicgInit) finish_bicg_init(s, sum, p.tol, p.max_it);
+    else if constexpr (K == kFinBicgV) finish_bicg_v(s, sum);
+    else if constexpr (K == kFinBicgS) finish_bicg_s(s, sum);
+    else if constexpr (K == kFinBicgT) finish_bicg_t(s, sum);
+    else if constexpr (K == kFinBicgX) finish_bicg_x(s, sum);
+    else if constexpr (K == kFinPcgInit) finish_pcg_init(s, sum, p.tol, p.max_it);
+    else if constexpr (K == kFinPcgRz) finish_pcg_rz(s, sum);
+    else if constexpr (K == kFinPcgQ) finish_pcg_q(s, sum);
+    else if constexpr (K == kFinPcgXr) finish_pcg_xr(s, sum);
+    else if constexpr (K == kFinOuterInit) finish_outer_init(s, sum, p.tol);
+    else finish_outer_residual(s, sum, p.max_refine);
+}
+
+// One planet per 256-thread block: its partials in tile order, then its scalar step.
+template <int K>
+__device__ void finish_planet(const ReduceCtx& ctx, int inst, int lane, const FinishParams& p) {
+    if (!finish_gate<K>(ctx.sc[inst], inst, p)) return;
+    double acc[FinishSums<K>::value];
+    sum_partials(ctx, inst, 0, lane, acc);
+    if (lane == 0) finish_step<K>(ctx.sc[inst], acc, p);
+}
+
 // ---- Krylov phases (fine level) ----------------------------------------------------------
 
-template <typename T, int R>
+template <typename T, int R, int C = kTicket>
 __device__ void bicg_init(const LevelView<T>& lv, int t0, int gid, int lane, const T* PSGB_PHASE_RESTRICT b, T* x, T* r,
                           T* shadow, T* p, T* v, const ReduceCtx& ctx, double tol, int max_it) {
     const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
@@ -471,17 +652,10 @@ __device__ void bicg_init(const LevelView<T>& lv, int t0, int gid, int lane, con
     }
     double out[R];
     bool fin[R];
-    tiles_reduce<T, 1, R>(q, ctx, ts, on, out, fin, gid, lane);
+    tiles_reduce<T, 1, R, C>(q, ctx, ts, on, out, fin, gid, lane);
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-        if (!fin[k]) continue;
-        InstanceScalars& s = ctx.sc[ts.inst[k]];
-        s.b_norm = sqrt(out[k]);
-        s.target = fmax(tol * s.b_norm, 0.5 * s.outer_target);
-        s.rho = out[k]; s.alpha = 1.0; s.omega = 1.0; s.beta = 0.0;
-        s.iterations = 0; s.half_done = 0; s.max_iterations = max_it; s.first = 1;
-        s.r_norm = s.b_norm;
-        s.status = !finite(s.b_norm) ? kNonFinite : (s.b_norm > 0.0 ? kRunning : kConverged);
+        if (fin[k]) finish_bicg_init(ctx.sc[ts.inst[k]], &out[k], tol, max_it);
     }
 }
 
@@ -512,7 +686,7 @@ __device__ void bicg_p(const LevelView<T>& lv, int t0, int lane, const T* PSGB_P
 }
 
 // out = A in; dot(shadow, out) -> alpha = rho / (shadow . v)
-template <typename T, int W, int R>
+template <typename T, int W, int R, int C = kTicket>
 __device__ void bicg_v(const LevelView<T>& lv, int t0, int gid, int lane, const T* PSGB_PHASE_RESTRICT in,
                        T* PSGB_PHASE_RESTRICT out, const T* PSGB_PHASE_RESTRICT shadow, const ReduceCtx& ctx) {
     const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
@@ -539,19 +713,15 @@ __device__ void bicg_v(const LevelView<T>& lv, int t0, int gid, int lane, const 
     }
     double sum[R];
     bool fin[R];
-    tiles_reduce<T, 1, R>(q, ctx, ts, on, sum, fin, gid, lane);
+    tiles_reduce<T, 1, R, C>(q, ctx, ts, on, sum, fin, gid, lane);
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-        if (!fin[k]) continue;
-        InstanceScalars& s = ctx.sc[ts.inst[k]];
-        if (!finite(sum[k])) { s.status = kNonFinite; continue; }
-        if (sum[k] == 0.0) { s.status = kBreakdown; continue; }
-        s.alpha = s.rho / sum[k];
+        if (fin[k]) finish_bicg_v(ctx.sc[ts.inst[k]], &sum[k]);
     }
 }
 
 // s = r - alpha v; ||s||: converged at s -> finish with x += alpha p_hat.
-template <typename T, int R>
+template <typename T, int R, int C = kTicket>
 __device__ void bicg_s(const LevelView<T>& lv, int t0, int gid, int lane, const T* PSGB_PHASE_RESTRICT r,
                        const T* PSGB_PHASE_RESTRICT v, T* PSGB_PHASE_RESTRICT s_out, T* xv, T omega_j, const ReduceCtx& ctx) {
     const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
@@ -578,20 +748,15 @@ __device__ void bicg_s(const LevelView<T>& lv, int t0, int gid, int lane, const 
     }
     double sum[R];
     bool fin[R];
-    tiles_reduce<T, 1, R>(q, ctx, ts, on, sum, fin, gid, lane);
+    tiles_reduce<T, 1, R, C>(q, ctx, ts, on, sum, fin, gid, lane);
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-        if (!fin[k]) continue;
-        InstanceScalars& s = ctx.sc[ts.inst[k]];
-        s.s_norm = sqrt(sum[k]);
-        s.iterations += 1;
-        if (!finite(s.s_norm)) { s.status = kNonFinite; continue; }
-        if (s.s_norm <= s.target) s.half_done = 1;
+        if (fin[k]) finish_bicg_s(ctx.sc[ts.inst[k]], &sum[k]);
     }
 }
 
 // t = A s_hat; (t.t, t.s) -> omega
-template <typename T, int W, int R>
+template <typename T, int W, int R, int C = kTicket>
 __device__ void bicg_t(const LevelView<T>& lv, int t0, int gid, int lane, const T* PSGB_PHASE_RESTRICT shat,
                        T* PSGB_PHASE_RESTRICT t, const T* PSGB_PHASE_RESTRICT s_vec, const ReduceCtx& ctx) {
     const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
@@ -622,20 +787,17 @@ __device__ void bicg_t(const LevelView<T>& lv, int t0, int gid, int lane, const 
     }
     double sum[2 * R];
     bool fin[R];
-    tiles_reduce<T, 2, R>(q, ctx, ts, on, sum, fin, gid, lane);
+    tiles_reduce<T, 2, R, C>(q, ctx, ts, on, sum, fin, gid, lane);
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-        if (!fin[k]) continue;
-        InstanceScalars& s = ctx.sc[ts.inst[k]];
-        s.omega = sum[2 * k] > 0.0 ? sum[2 * k + 1] / sum[2 * k] : 0.0;
-        if (!finite(s.omega)) s.status = kNonFinite;
+        if (fin[k]) finish_bicg_t(ctx.sc[ts.inst[k]], &sum[2 * k]);
     }
 }
 
 // x += alpha p_hat + omega s_hat; r = s - omega t; (r.r, shadow.r) -> next rho/beta.
 // A planet that converged at s (half_done) finishes with x += alpha p_hat instead; its
 // tiles still count through the reduction so that its last tile closes the iteration.
-template <typename T, int R>
+template <typename T, int R, int C = kTicket>
 __device__ void bicg_x(const LevelView<T>& lv, int t0, int gid, int lane, const T* PSGB_PHASE_RESTRICT phat,
                        const T* PSGB_PHASE_RESTRICT shat, const T* PSGB_PHASE_RESTRICT s_vec, const T* PSGB_PHASE_RESTRICT t,
                        T* x, T* r, const T* PSGB_PHASE_RESTRICT shadow, const ReduceCtx& ctx) {
@@ -676,29 +838,14 @@ __device__ void bicg_x(const LevelView<T>& lv, int t0, int gid, int lane, const 
     }
     double sum[2 * R];
     bool fin[R];
-    tiles_reduce<T, 2, R>(q, ctx, ts, on, sum, fin, gid, lane);
+    tiles_reduce<T, 2, R, C>(q, ctx, ts, on, sum, fin, gid, lane);
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-        if (!fin[k]) continue;
-        InstanceScalars& s = ctx.sc[ts.inst[k]];
-        if (s.half_done) {
-            s.r_norm = s.s_norm;
-            s.half_done = 0;
-            s.status = kConverged;
-            continue;
-        }
-        s.r_norm = sqrt(sum[2 * k]);
-        if (!finite(s.r_norm)) { s.status = kNonFinite; continue; }
-        if (s.r_norm <= s.target) { s.status = kConverged; continue; }
-        const double rho_next = sum[2 * k + 1];
-        if (rho_next == 0.0 || s.omega == 0.0) { s.status = kBreakdown; continue; }
-        s.beta = rho_next / s.rho * (s.alpha / s.omega);
-        s.rho = rho_next;
-        if (s.iterations >= s.max_iterations) s.status = kCap;
+        if (fin[k]) finish_bicg_x(ctx.sc[ts.inst[k]], &sum[2 * k]);
     }
 }
 
-template <typename T, int R>
+template <typename T, int R, int C = kTicket>
 __device__ void pcg_init(const LevelView<T>& lv, int t0, int gid, int lane, const T* PSGB_PHASE_RESTRICT b, T* x, T* r,
                          T* p, T* xv, T omega_j, const ReduceCtx& ctx, double tol, int max_it) {
     const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
@@ -719,22 +866,15 @@ __device__ void pcg_init(const LevelView<T>& lv, int t0, int gid, int lane, cons
     }
     double out[R];
     bool fin[R];
-    tiles_reduce<T, 1, R>(q, ctx, ts, on, out, fin, gid, lane);
+    tiles_reduce<T, 1, R, C>(q, ctx, ts, on, out, fin, gid, lane);
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-        if (!fin[k]) continue;
-        InstanceScalars& s = ctx.sc[ts.inst[k]];
-        s.b_norm = sqrt(out[k]);
-        s.target = fmax(tol * s.b_norm, 0.5 * s.outer_target);
-        s.r_norm = s.b_norm;
-        s.iterations = 0; s.half_done = 0; s.max_iterations = max_it; s.first = 1;
-        s.rho = 0.0; s.beta = 0.0; s.alpha = 0.0;
-        s.status = !finite(s.b_norm) ? kNonFinite : (s.b_norm > 0.0 ? kRunning : kConverged);
+        if (fin[k]) finish_pcg_init(ctx.sc[ts.inst[k]], &out[k], tol, max_it);
     }
 }
 
 // rho = r.z, beta = rho / rho_old
-template <typename T, int R>
+template <typename T, int R, int C = kTicket>
 __device__ void pcg_rz(const LevelView<T>& lv, int t0, int gid, int lane, const T* PSGB_PHASE_RESTRICT r,
                        const T* PSGB_PHASE_RESTRICT z, const ReduceCtx& ctx) {
     const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
@@ -750,16 +890,10 @@ __device__ void pcg_rz(const LevelView<T>& lv, int t0, int gid, int lane, const 
     }
     double sum[R];
     bool fin[R];
-    tiles_reduce<T, 1, R>(q, ctx, ts, on, sum, fin, gid, lane);
+    tiles_reduce<T, 1, R, C>(q, ctx, ts, on, sum, fin, gid, lane);
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-        if (!fin[k]) continue;
-        InstanceScalars& s = ctx.sc[ts.inst[k]];
-        if (!finite(sum[k])) { s.status = kNonFinite; continue; }
-        if (!(sum[k] > 0.0)) { s.status = s.first ? kConverged : kBreakdown; continue; }
-        s.beta = s.first ? 0.0 : sum[k] / s.rho;
-        s.rho = sum[k];
-        s.first = 0;
+        if (fin[k]) finish_pcg_rz(ctx.sc[ts.inst[k]], &sum[k]);
     }
 }
 
@@ -776,7 +910,7 @@ __device__ void pcg_p(const LevelView<T>& lv, int t0, int lane, const T* PSGB_PH
 }
 
 // q = A p; alpha = rho / p.q
-template <typename T, int W, int R>
+template <typename T, int W, int R, int C = kTicket>
 __device__ void pcg_q(const LevelView<T>& lv, int t0, int gid, int lane, const T* PSGB_PHASE_RESTRICT p,
                       T* PSGB_PHASE_RESTRICT q_out, const ReduceCtx& ctx) {
     const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
@@ -803,19 +937,15 @@ __device__ void pcg_q(const LevelView<T>& lv, int t0, int gid, int lane, const T
     }
     double sum[R];
     bool fin[R];
-    tiles_reduce<T, 1, R>(q, ctx, ts, on, sum, fin, gid, lane);
+    tiles_reduce<T, 1, R, C>(q, ctx, ts, on, sum, fin, gid, lane);
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-        if (!fin[k]) continue;
-        InstanceScalars& s = ctx.sc[ts.inst[k]];
-        if (!finite(sum[k])) { s.status = kNonFinite; continue; }
-        if (!(sum[k] > 0.0)) { s.status = kBreakdown; continue; }
-        s.alpha = s.rho / sum[k];
+        if (fin[k]) finish_pcg_q(ctx.sc[ts.inst[k]], &sum[k]);
     }
 }
 
 // x += alpha p; r -= alpha q; ||r|| -> converged?; first sweep of M r.
-template <typename T, int R>
+template <typename T, int R, int C = kTicket>
 __device__ void pcg_xr(const LevelView<T>& lv, int t0, int gid, int lane, const T* PSGB_PHASE_RESTRICT p,
                        const T* PSGB_PHASE_RESTRICT q_in, T* x, T* r, T* xv, T omega_j, const ReduceCtx& ctx) {
     const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
@@ -844,22 +974,16 @@ __device__ void pcg_xr(const LevelView<T>& lv, int t0, int gid, int lane, const 
     }
     double sum[R];
     bool fin[R];
-    tiles_reduce<T, 1, R>(q, ctx, ts, on, sum, fin, gid, lane);
+    tiles_reduce<T, 1, R, C>(q, ctx, ts, on, sum, fin, gid, lane);
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-        if (!fin[k]) continue;
-        InstanceScalars& s = ctx.sc[ts.inst[k]];
-        s.r_norm = sqrt(sum[k]);
-        s.iterations += 1;
-        if (!finite(s.r_norm)) { s.status = kNonFinite; continue; }
-        if (s.r_norm <= s.target) { s.status = kConverged; continue; }
-        if (s.iterations >= s.max_iterations) s.status = kCap;
+        if (fin[k]) finish_pcg_xr(ctx.sc[ts.inst[k]], &sum[k]);
     }
 }
 
 // ---- FP64 refinement ----------------------------------------------------------------------
 
-template <int R>
+template <int R, int C = kTicket>
 __device__ void outer_init(const LevelView<double>& lv, int t0, int gid, int lane, const double* PSGB_PHASE_RESTRICT b,
                            const ReduceCtx& ctx, double tol, const std::uint8_t* PSGB_PHASE_RESTRICT active) {
     const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
@@ -889,23 +1013,15 @@ __device__ void outer_init(const LevelView<double>& lv, int t0, int gid, int lan
     }
     double sum[R];
     bool fin[R];
-    tiles_reduce<double, 1, R>(q, ctx, ts, on, sum, fin, gid, lane);
+    tiles_reduce<double, 1, R, C>(q, ctx, ts, on, sum, fin, gid, lane);
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-        if (!fin[k]) continue;
-        InstanceScalars& s = ctx.sc[ts.inst[k]];
-        s.outer_b_norm = sqrt(sum[k]);
-        s.outer_target = tol * s.outer_b_norm;
-        s.tolerance = tol;
-        s.refinements = 0;
-        s.inner_total = 0;
-        s.outer_status = !finite(s.outer_b_norm) ? kNonFinite : kRunning;
-        s.status = kConverged;   // no inner solve runs until an inner init starts one
+        if (fin[k]) finish_outer_init(ctx.sc[ts.inst[k]], &sum[k], tol);
     }
 }
 
 // r = b - A x in FP64 (FP64 matrix), cast to the inner precision; ||r|| decides.
-template <typename TI, int W, int R>
+template <typename TI, int W, int R, int C = kTicket>
 __device__ void outer_residual(const LevelView<double>& lv, int t0, int gid, int lane, const double* PSGB_PHASE_RESTRICT b,
                                const double* PSGB_PHASE_RESTRICT x, double* PSGB_PHASE_RESTRICT r64, TI* PSGB_PHASE_RESTRICT rin,
                                const ReduceCtx& ctx, int max_refine) {
@@ -935,20 +1051,10 @@ __device__ void outer_residual(const LevelView<double>& lv, int t0, int gid, int
     }
     double sum[R];
     bool fin[R];
-    tiles_reduce<double, 1, R>(q, ctx, ts, on, sum, fin, gid, lane);
+    tiles_reduce<double, 1, R, C>(q, ctx, ts, on, sum, fin, gid, lane);
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-        if (!fin[k]) continue;
-        InstanceScalars& s = ctx.sc[ts.inst[k]];
-        s.outer_r_norm = sqrt(sum[k]);
-        if (!finite(s.outer_r_norm)) { s.outer_status = kNonFinite; continue; }
-        if (s.outer_r_norm <= s.outer_target || s.outer_b_norm == 0.0) {
-            s.outer_status = kConverged;
-            s.status = kConverged;
-            continue;
-        }
-        if (s.refinements >= max_refine) { s.outer_status = kCap; s.status = kConverged; continue; }
-        s.refinements += 1;
+        if (fin[k]) finish_outer_residual(ctx.sc[ts.inst[k]], &sum[k], max_refine);
     }
 }
 

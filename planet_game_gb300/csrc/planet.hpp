@@ -200,6 +200,10 @@ struct Batch {
     DenseCoarse dense;
     DeviceStore store;
     SmootherConfig smoother;
+    // Levels from tail_level down run as one block per planet (coarse_tail.hpp); 0: none.
+    int tail_level = 0;
+    int default_tail_level = 0;
+    std::uint32_t* tile_range = nullptr;   // [levels][instances][2]: first tile, tile count
     bool tuned = false;                // per-level settings from an autotune: the options' sweeps do not apply
     std::vector<std::int64_t> fine_base;      // fine-level row base per planet
     // fine-level graph data for assembly and the transport operator

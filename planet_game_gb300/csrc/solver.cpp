@@ -9,6 +9,7 @@
 #include "solver.hpp"
 
 #include "kernels.hpp"
+#include "coarse_tail.hpp"
 #include "krylov.hpp"
 #include "persistent.hpp"
 #include "profile.hpp"
@@ -25,6 +26,9 @@ namespace {
 // use multi-tile sets by default.
 constexpr std::uint32_t kSetsMinTiles = 2 * 8 * 152;
 
+// Levels whose planets hold at most this many rows each run in the coarse tail.
+constexpr std::uint32_t kTailRows = 4096;
+
 template <typename T>
 void upload_to(T* dst, const std::vector<T>& host) {
     if (!host.empty()) PSGB_CUDA(cudaMemcpy(dst, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice));
@@ -39,6 +43,7 @@ void default_launch_shapes(Batch& b) {
         L.sets_stencil = L.tiles >= kSetsMinTiles ? 2 : 1;
         L.sets_vector = L.tiles >= kSetsMinTiles ? 4 : 1;
     }
+    b.tail_level = b.default_tail_level;
 }
 
 std::unique_ptr<Planet> make_planet(std::uint32_t level, double radius_m) {
@@ -164,6 +169,24 @@ std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* ar
         if (l == 0) L.width = 6;
     }
     b.fine_base = b.levels[0].base;
+    // Per planet and level: its tile range; the coarse tail starts at the first level
+    // where no planet holds more than kTailRows rows.
+    {
+        std::vector<std::uint32_t> range(depth * I * 2, 0u);
+        for (std::size_t l = 0; l < depth; ++l) {
+            for (std::uint32_t i = 0; i < I; ++i) {
+                if (b.levels[l].base[i] < 0) continue;
+                range[(l * I + i) * 2] = static_cast<std::uint32_t>(b.levels[l].base[i] / kTileRows);
+                range[(l * I + i) * 2 + 1] = pad_rows(b.levels[l].count[i]) / kTileRows;
+            }
+        }
+        b.tile_range = b.store.upload(range);
+        for (std::size_t l = 1; l < depth && b.default_tail_level == 0; ++l) {
+            std::uint32_t most = 0;
+            for (std::uint32_t i = 0; i < I; ++i) most = std::max(most, b.levels[l].count[i]);
+            if (most <= kTailRows) b.default_tail_level = static_cast<int>(l);
+        }
+    }
     default_launch_shapes(b);
 
     // Tile metadata and ELL columns.
@@ -426,6 +449,36 @@ DenseTask<T> dense_task(Batch& b, std::size_t level, const T* rhs, T* x) {
     return DenseTask<T>{dense_view(b), D.d_blocks + begin, end - begin, Pick<T>::inv(D), rhs, x};
 }
 
+template <typename T>
+PersistentLevel<T> level_of(Batch& b, std::size_t l) {
+    BatchLevel& L = b.levels[l];
+    return PersistentLevel<T>{Pick<T>::view(b, l), Pick<T>::x(L), Pick<T>::y(L), Pick<T>::bvec(L), Pick<T>::r(L),
+                              L.member_offset, L.member, L.agg};
+}
+
+template <typename T>
+TailArgs<T> tail_args(Batch& b, int gate) {
+    TailArgs<T> a{};
+    const std::size_t depth = b.levels.size();
+    if (depth > static_cast<std::size_t>(kMaxLevels)) throw std::logic_error("coarse tail: hierarchy deeper than 12 levels");
+    for (std::size_t l = 0; l < depth; ++l) {
+        a.level[l] = level_of<T>(b, l);
+        a.pre[l] = b.smoother.pre_at(l);
+        a.post[l] = b.smoother.post_at(l);
+        a.starts_in_x[l] = b.smoother.starts_in_x(l) ? 1 : 0;
+    }
+    a.tile_range = b.tile_range;
+    a.first = b.tail_level;
+    a.depth = static_cast<int>(depth);
+    a.instances = b.instances;
+    a.dense = dense_view(b);
+    a.dense_inv = Pick<T>::inv(b.dense);
+    a.omega = static_cast<T>(b.smoother.omega);
+    a.sc = b.scalars;
+    a.gate = gate;
+    return a;
+}
+
 }  // namespace
 
 void assemble_transport(Batch& b, const double* slope, const double* conductance,
@@ -484,10 +537,14 @@ void vcycle(Batch& b, const T* rhs, T* x, int gate, bool first_sweep_done, cudaS
         other[l] = sm.starts_in_x(l) ? Y : X;
         rhs_of[l] = (l == 0) ? rhs : Pick<T>::bvec(L);
     }
+    // Levels from `tail` down run as one block per planet (0: none).
+    const std::size_t tail =
+        (b.tail_level > 0 && static_cast<std::size_t>(b.tail_level) < depth) ? static_cast<std::size_t>(b.tail_level) : 0;
+    const std::size_t down_end = tail != 0 ? tail : depth - 1;
     // Planets whose only level is the fine one: dense solve there.
     if (b.dense_at[0]) launch_dense_solve<T>(dense_task<T>(b, 0, rhs, x), b.scalars, gate, st);
     // Down: pre-smoothing, residual, restriction fused with the next level's first sweep.
-    for (std::size_t l = 0; l + 1 < depth; ++l) {
+    for (std::size_t l = 0; l < down_end; ++l) {
         const LevelView<T> lv = Pick<T>::view(b, l);
         BatchLevel& L = b.levels[l];
         // Planets whose coarsest level is this one (l >= 1) solve it in extra blocks of the
@@ -506,12 +563,13 @@ void vcycle(Batch& b, const T* rhs, T* x, int gate, bool first_sweep_done, cudaS
         launch_restrict_zero<T>(cv, L.member_offset, L.member, Pick<T>::r(L), Pick<T>::bvec(C), cur[l + 1], omega,
                                 b.scalars, gate, st);
         // The deepest level has no smoothing launch: its dense solves run on their own.
-        if (l + 2 == depth && b.dense_at[l + 1]) {
+        if (tail == 0 && l + 2 == depth && b.dense_at[l + 1]) {
             launch_dense_solve<T>(dense_task<T>(b, l + 1, Pick<T>::bvec(C), Pick<T>::x(C)), b.scalars, gate, st);
         }
     }
+    if (tail != 0) launch_coarse_tail<T>(tail_args<T>(b, gate), st);
     // Up: prolongation fused with the first post-smoothing sweep.
-    for (std::size_t l = depth - 1; l-- > 0;) {
+    for (std::size_t l = tail != 0 ? tail : depth - 1; l-- > 0;) {
         const LevelView<T> lv = Pick<T>::view(b, l);
         BatchLevel& L = b.levels[l];
         const T* e = Pick<T>::x(b.levels[l + 1]);
@@ -535,7 +593,7 @@ template float* vcycle_first_target<float>(Batch&, float*);
 
 namespace {
 
-ReduceCtx reduce_ctx(Batch& b) { return ReduceCtx{b.partial, b.ticket, b.tile_begin, b.scalars}; }
+ReduceCtx reduce_ctx(Batch& b) { return ReduceCtx{b.partial, b.ticket, b.tile_begin, b.scalars, b.instances}; }
 
 // What a recorded Krylov chunk depends on besides precision, method and length: the
 // per-level sweeps and launch shapes.
@@ -547,6 +605,7 @@ std::vector<int> shape_of(const Batch& b) {
         shape.push_back(b.levels[l].sets_stencil);
         shape.push_back(b.levels[l].sets_vector);
     }
+    shape.push_back(b.tail_level);
     return shape;
 }
 
@@ -659,9 +718,7 @@ PersistentArgs<T> persistent_args(Batch& b, const SolveOptions& opt, const doubl
     PersistentArgs<T> a{};
     a.depth = static_cast<int>(b.levels.size());
     for (std::size_t l = 0; l < b.levels.size(); ++l) {
-        BatchLevel& L = b.levels[l];
-        a.level[l] = PersistentLevel<T>{Pick<T>::view(b, l), Pick<T>::x(L), Pick<T>::y(L), Pick<T>::bvec(L),
-                                        Pick<T>::r(L), L.member_offset, L.member, L.agg};
+        a.level[l] = level_of<T>(b, l);
         a.dense_at[l] = b.dense_at[l] ? 1 : 0;
     }
     a.dense = dense_view(b);

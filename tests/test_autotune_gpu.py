@@ -91,3 +91,26 @@ def test_clearing_a_tuning_restores_the_option_sweeps(planets):
     bad["stencil_tiles"] = [3] * t["levels"]
     with pytest.raises(ValueError, match="tile sets"):
         batch.set_tuning(bad)
+
+
+def test_coarse_tail_never_changes_results(planets):
+    """The coarse levels run as one block per planet from any tail level, or grid-wide:
+    the same phases in the same order per planet, so every result is bit-identical."""
+    import planet_game_gb300 as pg
+
+    ms, inputs = planets
+    batch = pg.Batch(ms)
+    base = batch.tuning
+    assert base["coarse_tail_level"] >= 1              # chosen by the planets' level sizes
+    for precision, method in (("mixed", "bicgstab"), ("fp64", "pcg")):
+        outs = []
+        for tail in range(base["levels"]):
+            t = dict(base)
+            t["coarse_tail_level"] = tail
+            batch.set_tuning(t)
+            out, reps = step(batch, inputs, precision=precision, method=method)
+            assert all(r.status == 0 for r in reps)
+            outs.append((out, [r.iterations for r in reps]))
+        for out, its in outs[1:]:
+            assert its == outs[0][1]
+            assert all(np.array_equal(a, b) for a, b in zip(outs[0][0], out))
