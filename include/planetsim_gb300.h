@@ -183,6 +183,8 @@ typedef struct psgb_step_params {
     double dt_s;                 /* dt */
     double conductance_W_K;      /* K (used when edge_conductance is NULL) */
     const double* edge_conductance; /* optional, per undirected edge [edges], W/K; HOST */
+    int edge_conductance_stored;    /* nonzero: the per-edge conductance stored with
+                                       psgb_batch_set_edge_conductance (edge_conductance NULL) */
 } psgb_step_params;
 
 typedef struct psgb_step_report {
@@ -270,6 +272,11 @@ int psgb_solve_implicit_transport(psgb_planet* planet, double conductance_W_K, c
                                   const psgb_transport_settings* settings, const psgb_solve_options* options,
                                   const double* latent_W_m2, double* source_out_W_m2, double* mean_out_K,
                                   psgb_transport_result* result);
+
+/* Stores per-edge conductances with a batch (HOST arrays, one per planet, [edges] W/K;
+ * NULL entries clear a planet's): steps whose params set edge_conductance_stored use them
+ * without passing (and without the library comparing) the arrays on every call. */
+int psgb_batch_set_edge_conductance(psgb_batch* batch, const double* const* edge_conductance);
 
 /* Per-level settings of a batch's solve. The reference has no counterpart (its smoother
  * is fixed, heat_transport.cpp:258-286); the autotuner picks them for the batch's GPU:

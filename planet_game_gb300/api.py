@@ -366,9 +366,15 @@ def _step_result(r: capi.StepReport) -> StepResult:
 
 
 def step_params(heat_capacity_J_m2_K: float, dt_s: float, conductance_W_K: float = 0.0,
-                edge_conductance: np.ndarray | None = None) -> capi.StepParams:
-    p = capi.StepParams(heat_capacity_J_m2_K, dt_s, conductance_W_K, None)
-    if edge_conductance is not None:
+                edge_conductance=None) -> capi.StepParams:
+    """`edge_conductance`: None (uniform K), an array per undirected edge, or "stored"
+    (the batch's stored array, Batch.set_edge_conductance)."""
+    p = capi.StepParams(heat_capacity_J_m2_K, dt_s, conductance_W_K, None, 0)
+    if isinstance(edge_conductance, str):
+        if edge_conductance != "stored":
+            raise ValueError("edge_conductance must be an array, None or 'stored'")
+        p.edge_conductance_stored = 1
+    elif edge_conductance is not None:
         arr = np.ascontiguousarray(edge_conductance, dtype=np.float64)
         p.edge_conductance = arr.ctypes.data
         p._keep = arr  # keep the host array alive with the struct
@@ -448,10 +454,19 @@ class Batch:
             p = step_params(heat_capacity[i] if np.ndim(heat_capacity) else heat_capacity,
                             dt[i] if np.ndim(dt) else dt,
                             (conductance[i] if np.ndim(conductance) else conductance) if conductance is not None else 0.0,
-                            edge_conductance[i] if edge_conductance is not None else None)
+                            edge_conductance if isinstance(edge_conductance, str)
+                            else (edge_conductance[i] if edge_conductance is not None else None))
             params._keep.append(p)
             params[i] = p
         return params
+
+    def set_edge_conductance(self, edge_conductance) -> None:
+        """Store per-edge conductances with the batch (one array per planet, None clears);
+        steps then pass edge_conductance="stored"."""
+        n = len(self.meshes)
+        keep = [None if e is None else np.ascontiguousarray(e, dtype=np.float64) for e in edge_conductance]
+        arr = (C.c_void_p * n)(*[None if e is None else e.ctypes.data for e in keep])
+        _raise(capi.load().psgb_batch_set_edge_conductance(self._h, arr))
 
     def autotune(self, t0, sources, heat_capacity, dt, conductance=None, edge_conductance=None, **options) -> dict:
         """Pick per-level launch shapes and sweeps by timing trial solves of this sub-step;

@@ -88,7 +88,7 @@ class SolveReport(C.Structure):
 
 class StepParams(C.Structure):
     _fields_ = [("heat_capacity_J_m2_K", C.c_double), ("dt_s", C.c_double), ("conductance_W_K", C.c_double),
-                ("edge_conductance", C.c_void_p)]
+                ("edge_conductance", C.c_void_p), ("edge_conductance_stored", C.c_int)]
 
 
 class StepReport(C.Structure):
@@ -139,6 +139,7 @@ _SIGNATURES = {
     "psgb_batch_autotune": (C.c_int, [P, C.POINTER(StepParams), C.POINTER(SolveOptions), C.POINTER(P), C.POINTER(P),
                                       C.c_int, P, C.POINTER(Tuning)]),
     "psgb_batch_get_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
+    "psgb_batch_set_edge_conductance": (C.c_int, [P, C.POINTER(P)]),
     "psgb_batch_set_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
     "psgb_transport_settings_default": (None, [C.POINTER(TransportSettings)]),
     "psgb_solve_implicit_transport": (C.c_int, [P, C.c_double, P, TransportResponse, P, C.POINTER(TransportSettings),

@@ -167,30 +167,51 @@ void scatter_edge_conductance(const psgb::Planet& p, const double* per_edge, std
 // ones the current matrix was built from.
 void assemble_step_matrix(psgb::Batch& b, const psgb_step_params* params, cudaStream_t st) {
     const std::uint32_t I = b.instances;
+    if (b.assembled_edges.size() != I) b.assembled_edges.assign(I, {});
+    if (b.stored_edges.size() != I) {
+        b.stored_edges.assign(I, {});
+        b.stored_generation.assign(I, 0);
+    }
+    // The matrix depends on C, dt, K and the per-edge conductances: scalars and the
+    // conductance source go into a key; arrays passed in are compared with the ones the
+    // current matrix was built from (no copy unless they changed); stored arrays by
+    // their generation.
     std::vector<double> key;
+    std::vector<const double*> edges(I, nullptr);
     bool per_edge = false;
     for (std::uint32_t i = 0; i < I; ++i) {
         const psgb_step_params& p = params[i];
         require(p.heat_capacity_J_m2_K > 0.0 && std::isfinite(p.heat_capacity_J_m2_K), "heat capacity must be finite and positive");
         require(p.dt_s > 0.0 && std::isfinite(p.dt_s), "time step must be finite and positive");
-        if (p.edge_conductance == nullptr) {
+        if (p.edge_conductance_stored) {
+            require(p.edge_conductance == nullptr, "edge_conductance must be NULL when the stored conductance is used");
+            require(!b.stored_edges[i].empty(), "no per-edge conductance is stored for this planet");
+            edges[i] = b.stored_edges[i].data();
+        } else {
+            edges[i] = p.edge_conductance;
+        }
+        if (edges[i] == nullptr) {
             require(p.conductance_W_K > 0.0 && std::isfinite(p.conductance_W_K), "transport conductance must be finite and positive");
         }
+        per_edge = per_edge || edges[i] != nullptr;
         key.push_back(p.heat_capacity_J_m2_K);
         key.push_back(p.dt_s);
-        key.push_back(p.edge_conductance == nullptr ? p.conductance_W_K : -1.0);
-        if (p.edge_conductance != nullptr) {
-            per_edge = true;
-            const std::size_t e = b.planets[i]->mesh.edges;
-            key.insert(key.end(), p.edge_conductance, p.edge_conductance + e);
-        }
+        key.push_back(edges[i] == nullptr ? p.conductance_W_K : -1.0);
+        key.push_back(p.edge_conductance_stored ? static_cast<double>(b.stored_generation[i]) : -1.0);
     }
-    if (b.matrix_ready && key == b.assembled_key) return;
+    bool same = b.matrix_ready && key == b.assembled_key;
+    for (std::uint32_t i = 0; same && i < I; ++i) {
+        if (edges[i] == nullptr || params[i].edge_conductance_stored) continue;
+        const std::size_t e = b.planets[i]->mesh.edges;
+        same = b.assembled_edges[i].size() == e &&
+               std::memcmp(b.assembled_edges[i].data(), edges[i], e * sizeof(double)) == 0;
+    }
+    if (same) return;
     const std::size_t P0 = b.levels[0].rows;
     std::vector<double> slope_of(I), conductance(I);
     for (std::uint32_t i = 0; i < I; ++i) {
         slope_of[i] = params[i].dt_s / params[i].heat_capacity_J_m2_K;
-        conductance[i] = params[i].edge_conductance == nullptr ? params[i].conductance_W_K : 0.0;
+        conductance[i] = edges[i] == nullptr ? params[i].conductance_W_K : 0.0;
     }
     PSGB_CUDA(cudaMemcpyAsync(b.slope_of, slope_of.data(), I * sizeof(double), cudaMemcpyHostToDevice, st));
     PSGB_CUDA(cudaMemcpyAsync(b.conductance, conductance.data(), I * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -199,8 +220,8 @@ void assemble_step_matrix(psgb::Batch& b, const psgb_step_params* params, cudaSt
         if (b.edge_g == nullptr) b.edge_g = b.store.alloc<double>(6 * P0);
         std::vector<double> g(6 * P0, 0.0);
         for (std::uint32_t i = 0; i < I; ++i) {
-            if (params[i].edge_conductance != nullptr) {
-                scatter_edge_conductance(*b.planets[i], params[i].edge_conductance, b.fine_base[i], P0, g);
+            if (edges[i] != nullptr) {
+                scatter_edge_conductance(*b.planets[i], edges[i], b.fine_base[i], P0, g);
             } else {
                 const psgb::HostMesh& m = b.planets[i]->mesh;
                 for (std::size_t c = 0; c < m.cells; ++c)
@@ -222,6 +243,13 @@ void assemble_step_matrix(psgb::Batch& b, const psgb_step_params* params, cudaSt
     psgb::prepare_levels(b, st);
     PSGB_CUDA(cudaStreamSynchronize(st));
     b.assembled_key = key;
+    for (std::uint32_t i = 0; i < I; ++i) {
+        if (edges[i] != nullptr && !params[i].edge_conductance_stored) {
+            b.assembled_edges[i].assign(edges[i], edges[i] + b.planets[i]->mesh.edges);
+        } else {
+            b.assembled_edges[i].clear();
+        }
+    }
     b.step_edge_conductance = edge_g;
 }
 
@@ -735,6 +763,30 @@ int psgb_batch_autotune(psgb_batch* h, const psgb_step_params* params, const psg
         psgb::launch_step_rhs(step_view(b), b.t0, b.src, b.bb, b.tmp, b.xr, st);
         const psgb::Tuning t = psgb::autotune(b, opt, b.bb, b.tmp2, st);
         if (out != nullptr) fill_tuning(t, out);
+        return PSGB_OK;
+    });
+}
+
+int psgb_batch_set_edge_conductance(psgb_batch* h, const double* const* edge_conductance) {
+    return guarded([&] {
+        require(h != nullptr && edge_conductance != nullptr, "null argument");
+        psgb::Batch& b = *h->batch;
+        if (b.stored_edges.size() != b.instances) {
+            b.stored_edges.assign(b.instances, {});
+            b.stored_generation.assign(b.instances, 0);
+        }
+        for (std::uint32_t i = 0; i < b.instances; ++i) {
+            const double* e = edge_conductance[i];
+            if (e == nullptr) {
+                b.stored_edges[i].clear();
+            } else {
+                const std::size_t n = b.planets[i]->mesh.edges;
+                for (std::size_t k = 0; k < n; ++k)
+                    require(std::isfinite(e[k]) && e[k] >= 0.0, "edge conductances must be finite and non-negative");
+                b.stored_edges[i].assign(e, e + n);
+            }
+            ++b.stored_generation[i];
+        }
         return PSGB_OK;
     });
 }

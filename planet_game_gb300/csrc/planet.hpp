@@ -251,7 +251,10 @@ struct Batch {
     double* csr_values = nullptr;      // one-planet batches: set_matrix staging
     std::uint32_t* csr_offset = nullptr;   // one-planet batches: the graph's CSR offsets
     // the parameters the current matrix was assembled with
-    std::vector<double> assembled_key;
+    std::vector<double> assembled_key;                  // C, dt, K and the conductance source per planet
+    std::vector<std::vector<double>> assembled_edges;   // per planet: per-edge conductance passed in (empty: none)
+    std::vector<std::vector<double>> stored_edges;      // per planet: set with psgb_batch_set_edge_conductance
+    std::vector<std::uint64_t> stored_generation;       // per planet: bumped on every set
     std::uint64_t assembled_bytes_hint = 0;
     ~Batch() {
         for (auto& g : graphs) cudaGraphExecDestroy(g.second.exec);

@@ -99,6 +99,7 @@ class _Lane:
         self.level = level
         self.planets = server.population[level]
         self.batch = None
+        self.edge_conductance = None        # "stored" once the lane's batch holds the planets' arrays
         self.bytes = 0
         self.pending: dict[int, collections.deque] = collections.defaultdict(collections.deque)
         self.cv = threading.Condition(server.lock)
@@ -120,7 +121,7 @@ class _Lane:
             outs, reps = self.batch.transport_step(
                 t0, src, [p.heat_capacity for p in self.planets], [p.dt for p in self.planets],
                 conductance=[p.conductance for p in self.planets],
-                edge_conductance=[p.edge_conductance for p in self.planets], active=active, **self.server.options)
+                edge_conductance=self.edge_conductance, active=active, **self.server.options)
             for i, r in reqs.items():
                 if self.server.keep_inputs:
                     r.t_in = self.planets[i].state.cpu().numpy()
@@ -207,6 +208,11 @@ class Server:
             self.lanes[level] = lane
             lane.thread.start()
         lane.batch = api.Batch([p.mesh for p in self.population[level]])
+        edges = [p.edge_conductance for p in self.population[level]]
+        lane.edge_conductance = None
+        if any(e is not None for e in edges):
+            lane.batch.set_edge_conductance(edges)
+            lane.edge_conductance = "stored"
         if self.autotune:
             if level not in self.tunings:
                 self.tunings[level] = self._tune(lane.batch, level)
@@ -224,7 +230,7 @@ class Server:
         zeros = [torch.zeros_like(p.state) for p in planets]
         return batch.autotune([p.state for p in planets], zeros, [p.heat_capacity for p in planets],
                               [p.dt for p in planets], conductance=[p.conductance for p in planets],
-                              edge_conductance=[p.edge_conductance for p in planets], **self.options)
+                              edge_conductance=self.lanes[level].edge_conductance, **self.options)
 
     def prepare(self, levels=None):
         """Admit (and tune) the lanes of `levels` ahead of traffic, as far as the budget allows."""
