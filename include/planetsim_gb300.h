@@ -294,6 +294,8 @@ typedef struct psgb_tuning {
     double default_solve_ms;              /* autotune: trial solve with the settings before */
     int trial_solves;                     /* autotune: solves timed */
     int coarse_tail_level;                /* levels from this one down run one block per planet; 0: none */
+    int block_sweeps[PSGB_MAX_LEVELS];    /* per level: Jacobi sweeps per smoothing launch, each tile in shared
+                                             memory with its neighbours in other tiles held (1..8; 1 = plain) */
 } psgb_tuning;
 
 /* Times trial solves of one sub-step (the inputs as for psgb_batch_transport_step, every

@@ -424,7 +424,7 @@ def _tuning_dict(t) -> dict:
             "stencil_tiles": list(t.stencil_tiles[:n]), "vector_tiles": list(t.vector_tiles[:n]),
             "jacobi_omega": float(t.jacobi_omega), "tuned_solve_ms": float(t.tuned_solve_ms),
             "default_solve_ms": float(t.default_solve_ms), "trial_solves": int(t.trial_solves),
-            "coarse_tail_level": int(t.coarse_tail_level)}
+            "coarse_tail_level": int(t.coarse_tail_level), "block_sweeps": list(t.block_sweeps[:n])}
 
 
 class Batch:
@@ -494,9 +494,9 @@ class Batch:
             return
         t = capi.Tuning()
         t.levels = len(tuning["pre_sweeps"])
-        for k in ("pre_sweeps", "post_sweeps", "stencil_tiles", "vector_tiles"):
+        for k in ("pre_sweeps", "post_sweeps", "stencil_tiles", "vector_tiles", "block_sweeps"):
             arr = getattr(t, k)
-            for l, v in enumerate(tuning[k]):
+            for l, v in enumerate(tuning.get(k, [1] * t.levels)):
                 arr[l] = int(v)
         t.jacobi_omega = float(tuning["jacobi_omega"])
         t.coarse_tail_level = int(tuning.get("coarse_tail_level", 0))

@@ -116,11 +116,13 @@ void tune_shapes(Batch& b, cudaStream_t st) {
 struct Sweeps {
     std::vector<int> pre, post;
     double omega;
+    std::vector<int> inner;   // empty: one sweep per launch everywhere
 };
 
 void set_sweeps(Batch& b, const Sweeps& s) {
     b.smoother.level_pre = s.pre;
     b.smoother.level_post = s.post;
+    b.smoother.level_inner = s.inner;
     b.smoother.omega = s.omega;
 }
 
@@ -151,6 +153,7 @@ Tuning current_tuning(const Batch& b) {
     for (std::size_t l = 0; l < b.levels.size(); ++l) {
         t.pre.push_back(b.smoother.pre_at(l));
         t.post.push_back(b.smoother.post_at(l));
+        t.inner.push_back(b.smoother.inner_at(l));
         t.sets_stencil.push_back(b.levels[l].sets_stencil);
         t.sets_vector.push_back(b.levels[l].sets_vector);
     }
@@ -161,8 +164,11 @@ Tuning current_tuning(const Batch& b) {
 
 void apply_tuning(Batch& b, const Tuning& t) {
     const std::size_t depth = b.levels.size();
-    if (t.pre.size() != depth || t.post.size() != depth || t.sets_stencil.size() != depth || t.sets_vector.size() != depth)
+    if (t.pre.size() != depth || t.post.size() != depth || t.sets_stencil.size() != depth || t.sets_vector.size() != depth ||
+        (!t.inner.empty() && t.inner.size() != depth))
         throw std::invalid_argument("tuning levels do not match the batch");
+    for (int k : t.inner)
+        if (k < 1 || k > 8) throw std::invalid_argument("block-local sweeps must be 1..8");
     for (std::size_t l = 0; l < depth; ++l) {
         if (t.pre[l] < 1 || t.pre[l] > 8 || t.post[l] < 0 || t.post[l] > 8)
             throw std::invalid_argument("tuned sweeps must be 1..8 (pre) and 0..8 (post)");
@@ -178,6 +184,7 @@ void apply_tuning(Batch& b, const Tuning& t) {
     }
     b.smoother.level_pre = t.pre;
     b.smoother.level_post = t.post;
+    b.smoother.level_inner = t.inner;
     b.smoother.omega = t.omega;
     b.tail_level = t.tail_level;
     b.tuned = true;
@@ -186,6 +193,7 @@ void apply_tuning(Batch& b, const Tuning& t) {
 void clear_tuning(Batch& b) {
     b.smoother.level_pre.clear();
     b.smoother.level_post.clear();
+    b.smoother.level_inner.clear();
     default_launch_shapes(b);
     b.tuned = false;
 }
@@ -197,7 +205,7 @@ Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x,
     Tuning result;
     // Settings before tuning: the reference point.
     const Sweeps before{std::vector<int>(depth, b.smoother.pre_at(0)), std::vector<int>(depth, b.smoother.post_at(0)),
-                        b.smoother.omega};
+                        b.smoother.omega, {}};
     set_sweeps(b, before);
     default_launch_shapes(b);
     trial(b, opt, rhs, x, rows, st, result.trials);
@@ -218,7 +226,7 @@ Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x,
     const struct { int pre, post; double omega; } uniform[] = {
         {1, 1, 1.0}, {1, 1, 0.8}, {2, 2, 1.0}, {2, 1, 0.9}, {1, 2, 0.9}, {3, 3, 0.8}};
     for (const auto& u : uniform) {
-        const Sweeps s{std::vector<int>(depth, u.pre), std::vector<int>(depth, u.post), u.omega};
+        const Sweeps s{std::vector<int>(depth, u.pre), std::vector<int>(depth, u.post), u.omega, {}};
         const double ms = run(s);
         if (ms > 0.0 && (best_ms < 0.0 || ms < best_ms)) { best = s; best_ms = ms; }
     }
@@ -245,6 +253,17 @@ Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x,
             s.pre[0] = f[0];
             s.post[0] = f[1];
             if (s.pre == with_coarse.pre && s.post == with_coarse.post) continue;
+            consider(s);
+        }
+    }
+    // block-local sweeps on the coarse levels: several Jacobi sweeps per launch
+    if (depth > 1) {
+        const int block[][3] = {{2, 2, 2}, {2, 2, 3}, {2, 2, 4}, {3, 3, 2}, {3, 3, 3}};
+        const Sweeps base = best;
+        for (const auto& c : block) {
+            Sweeps s = base;
+            s.inner.assign(depth, 1);
+            for (std::size_t l = 1; l < depth; ++l) { s.pre[l] = c[0]; s.post[l] = c[1]; s.inner[l] = c[2]; }
             consider(s);
         }
     }
@@ -277,6 +296,7 @@ Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x,
     b.tuned = true;
     result.pre = best.pre;
     result.post = best.post;
+    result.inner = best.inner.empty() ? std::vector<int>(depth, 1) : best.inner;
     result.omega = best.omega;
     for (std::size_t l = 0; l < depth; ++l) {
         result.sets_stencil.push_back(b.levels[l].sets_stencil);

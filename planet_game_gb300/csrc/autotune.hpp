@@ -12,6 +12,7 @@ namespace psgb {
 
 struct Tuning {
     std::vector<int> pre, post;                    // sweeps per level
+    std::vector<int> inner;                        // block-local sweeps per smoothing launch, per level
     std::vector<std::uint8_t> sets_stencil;        // per level: 1 or 2
     std::vector<std::uint8_t> sets_vector;         // per level: 1 or 4
     double omega = 0.8;

@@ -726,6 +726,7 @@ void fill_tuning(const psgb::Tuning& t, psgb_tuning* out) {
         out->post_sweeps[l] = t.post[l];
         out->stencil_tiles[l] = t.sets_stencil[l];
         out->vector_tiles[l] = t.sets_vector[l];
+        out->block_sweeps[l] = l < t.inner.size() ? t.inner[l] : 1;
     }
     out->jacobi_omega = t.omega;
     out->tuned_solve_ms = t.tuned_ms;
@@ -815,6 +816,7 @@ int psgb_batch_set_tuning(psgb_batch* h, const psgb_tuning* tuning) {
             t.post.push_back(tuning->post_sweeps[l]);
             t.sets_stencil.push_back(static_cast<std::uint8_t>(tuning->stencil_tiles[l]));
             t.sets_vector.push_back(static_cast<std::uint8_t>(tuning->vector_tiles[l]));
+            t.inner.push_back(tuning->block_sweeps[l] == 0 ? 1 : tuning->block_sweeps[l]);
         }
         t.omega = tuning->jacobi_omega;
         t.tail_level = tuning->coarse_tail_level;

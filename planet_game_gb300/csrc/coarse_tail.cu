@@ -58,8 +58,14 @@ __global__ void __launch_bounds__(1024, 1) k_coarse_tail(const __grid_constant__
         TailPair<T> p = tail_pair(a, l);
         for (int k = 1; k < a.pre[l]; ++k) {
             tail_widths(lv.width, [&](auto W) {
-                PSGB_PLANET_TILES(a, l, inst, gid)
-                    ph::smooth<T, decltype(W)::value, 1>(lv, tile, lane, L.b, p.first, p.second, omega, a.sc, a.gate);
+                if (a.inner[l] > 1) {
+                    PSGB_PLANET_TILES(a, l, inst, gid)
+                        ph::smooth_block<T, decltype(W)::value>(lv, tile, gid, lane, L.b, p.first, p.second, omega,
+                                                                a.inner[l], a.sc, a.gate);
+                } else {
+                    PSGB_PLANET_TILES(a, l, inst, gid)
+                        ph::smooth<T, decltype(W)::value, 1>(lv, tile, lane, L.b, p.first, p.second, omega, a.sc, a.gate);
+                }
             });
             __syncthreads();
             T* t = p.first; p.first = p.second; p.second = t;
@@ -104,8 +110,14 @@ __global__ void __launch_bounds__(1024, 1) k_coarse_tail(const __grid_constant__
         { T* t = p.first; p.first = p.second; p.second = t; }
         for (int k = 1; k < a.post[l]; ++k) {
             tail_widths(lv.width, [&](auto W) {
-                PSGB_PLANET_TILES(a, l, inst, gid)
-                    ph::smooth<T, decltype(W)::value, 1>(lv, tile, lane, L.b, p.first, p.second, omega, a.sc, a.gate);
+                if (a.inner[l] > 1) {
+                    PSGB_PLANET_TILES(a, l, inst, gid)
+                        ph::smooth_block<T, decltype(W)::value>(lv, tile, gid, lane, L.b, p.first, p.second, omega,
+                                                                a.inner[l], a.sc, a.gate);
+                } else {
+                    PSGB_PLANET_TILES(a, l, inst, gid)
+                        ph::smooth<T, decltype(W)::value, 1>(lv, tile, lane, L.b, p.first, p.second, omega, a.sc, a.gate);
+                }
             });
             __syncthreads();
             T* t = p.first; p.first = p.second; p.second = t;

@@ -24,7 +24,7 @@ struct TailArgs {
     unsigned instances;
     DenseView dense;
     const T* dense_inv;
-    int pre[kMaxLevels], post[kMaxLevels];
+    int pre[kMaxLevels], post[kMaxLevels], inner[kMaxLevels];
     unsigned char starts_in_x[kMaxLevels];
     T omega;
     const InstanceScalars* sc;

@@ -110,9 +110,11 @@ void launch_dense_invert(const DenseView& dense, int level, const LevelView<doub
 template <typename T>
 void launch_smooth_zero(const LevelView<T>& lv, const T* b, T* x, T omega, const InstanceScalars* sc,
                         int gate, cudaStream_t stream);
+// `inner` > 1: block-local sweeps (each tile `inner` Jacobi sweeps in one launch).
 template <typename T>
 void launch_smooth(const LevelView<T>& lv, const T* b, const T* x, T* y, T omega,
-                   const InstanceScalars* sc, int gate, cudaStream_t stream, const DenseTask<T>& dense = {});
+                   const InstanceScalars* sc, int gate, cudaStream_t stream, const DenseTask<T>& dense = {},
+                   int inner = 1);
 template <typename T>
 void launch_residual(const LevelView<T>& lv, const T* b, const T* x, T* r, const InstanceScalars* sc,
                      int gate, cudaStream_t stream, const DenseTask<T>& dense = {});

@@ -183,6 +183,17 @@ __global__ void k_smooth(LevelView<T> lv, const T* __restrict__ b, const T* __re
     ph::smooth<T, W, R>(lv, blockIdx.x * R, threadIdx.x, b, x, y, omega, sc, gate);
 }
 
+template <typename T, int W>
+__global__ void k_smooth_block(LevelView<T> lv, const T* __restrict__ b, const T* __restrict__ x, T* __restrict__ y,
+                               T omega, int inner, const InstanceScalars* sc, int gate, DenseTask<T> dense) {
+    pdl_begin();
+    if (blockIdx.x >= lv.tiles) {
+        ph::dense_block<T>(dense, blockIdx.x - lv.tiles, threadIdx.x, sc, gate);
+        return;
+    }
+    ph::smooth_block<T, W>(lv, blockIdx.x, 0, threadIdx.x, b, x, y, omega, inner, sc, gate);
+}
+
 template <typename T, int W, int R>
 __global__ void k_residual(LevelView<T> lv, const T* __restrict__ b, const T* __restrict__ x, T* __restrict__ r,
                            const InstanceScalars* sc, int gate, DenseTask<T> dense) {
@@ -290,7 +301,13 @@ void launch_smooth_zero(const LevelView<T>& lv, const T* b, T* x, T omega, const
 
 template <typename T>
 void launch_smooth(const LevelView<T>& lv, const T* b, const T* x, T* y, T omega,
-                   const InstanceScalars* sc, int gate, cudaStream_t stream, const DenseTask<T>& dense) {
+                   const InstanceScalars* sc, int gate, cudaStream_t stream, const DenseTask<T>& dense, int inner) {
+    if (inner > 1) {
+        PSGB_LAUNCH(smooth_family(lv), stream,
+                    PSGB_WIDTHS(lv.width, launch_pdl(k_smooth_block<T, W>, lv.tiles + dense.count, kTile, stream, lv, b, x, y,
+                                                     omega, inner, sc, gate, dense)));
+        return;
+    }
     PSGB_LAUNCH(smooth_family(lv), stream,
                 PSGB_STENCIL_SETS(lv.sets_stencil, PSGB_WIDTHS(lv.width,
                     launch_pdl(k_smooth<T, W, R>, ph::tile_sets(lv.tiles, R) + dense.count, kTile, stream, lv, b, x, y, omega,
@@ -358,7 +375,7 @@ void launch_dense_solve(const DenseTask<T>& dense, const InstanceScalars* sc, in
     template void launch_smooth_zero<T>(const LevelView<T>&, const T*, T*, T, const InstanceScalars*, \
                                         int, cudaStream_t);                                           \
     template void launch_smooth<T>(const LevelView<T>&, const T*, const T*, T*, T,                     \
-                                   const InstanceScalars*, int, cudaStream_t, const DenseTask<T>&);   \
+                                   const InstanceScalars*, int, cudaStream_t, const DenseTask<T>&, int); \
     template void launch_residual<T>(const LevelView<T>&, const T*, const T*, T*,                      \
                                      const InstanceScalars*, int, cudaStream_t, const DenseTask<T>&); \
     template void launch_spmv<T>(const LevelView<T>&, const T*, T*, cudaStream_t);                     \

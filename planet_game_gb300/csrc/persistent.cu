@@ -179,7 +179,13 @@ __device__ bool vcycle(const Args<T>& a, const T* rhs, T* x, int gate) {
             if (dense) dense_phase<T>(a, l, L.b, L.x, gate);
             dense = false;
             with_width(lv.width, [&](auto W) {
-                PSGB_SETS(lv, G) ph::smooth<T, decltype(W)::value, kPR>(lv, t0, G.lane, b, p.first, p.second, omega, a.sc, gate);
+                if (a.inner[l] > 1) {
+                    for (int tile = G.first; tile < static_cast<int>(lv.tiles); tile += G.stride)
+                        ph::smooth_block<T, decltype(W)::value>(lv, tile, G.gid, G.lane, b, p.first, p.second, omega,
+                                                                a.inner[l], a.sc, gate);
+                } else {
+                    PSGB_SETS(lv, G) ph::smooth<T, decltype(W)::value, kPR>(lv, t0, G.lane, b, p.first, p.second, omega, a.sc, gate);
+                }
             });
             PSGB_BARRIER(a);
             T* t = p.first; p.first = p.second; p.second = t;
@@ -218,7 +224,13 @@ __device__ bool vcycle(const Args<T>& a, const T* rhs, T* x, int gate) {
         { T* t = p.first; p.first = p.second; p.second = t; }
         for (int k = 1; k < a.post[l]; ++k) {
             with_width(lv.width, [&](auto W) {
-                PSGB_SETS(lv, G) ph::smooth<T, decltype(W)::value, kPR>(lv, t0, G.lane, b, p.first, p.second, omega, a.sc, gate);
+                if (a.inner[l] > 1) {
+                    for (int tile = G.first; tile < static_cast<int>(lv.tiles); tile += G.stride)
+                        ph::smooth_block<T, decltype(W)::value>(lv, tile, G.gid, G.lane, b, p.first, p.second, omega,
+                                                                a.inner[l], a.sc, gate);
+                } else {
+                    PSGB_SETS(lv, G) ph::smooth<T, decltype(W)::value, kPR>(lv, t0, G.lane, b, p.first, p.second, omega, a.sc, gate);
+                }
             });
             PSGB_BARRIER(a);
             T* t = p.first; p.first = p.second; p.second = t;

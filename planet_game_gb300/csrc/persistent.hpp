@@ -56,6 +56,7 @@ struct PersistentArgs {
     int max_refinements;
     int method;                         // psgb::Method
     int pre[kMaxLevels], post[kMaxLevels];   // sweeps per level
+    int inner[kMaxLevels];                   // block-local sweeps per smoothing pass
     unsigned char starts_in_x[kMaxLevels];   // the level's first sweep writes x (sweep parity)
     T omega;
     PersistentSync sync;

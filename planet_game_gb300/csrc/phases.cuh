@@ -321,6 +321,59 @@ __device__ void smooth(const LevelView<T>& lv, int t0, int lane, const T* PSGB_P
     }
 }
 
+// Block-local Jacobi: `inner` damped sweeps of one tile in one call, the tile's own rows
+// updated in shared memory between sweeps and its neighbours in other tiles held at x
+// (loaded once). One inner sweep is exactly `smooth` (same terms, same order). Several
+// smooth the tile's error like that many sweeps at the cost of one pass over HBM; the
+// error between tiles is left to the next launch or the coarser levels. The tile-level
+// counterpart of the reference's block-hybrid smoother (heat_transport.cpp:258-286), with
+// Jacobi instead of sequential Gauss-Seidel inside the block.
+template <typename T, int W>
+__device__ void smooth_block(const LevelView<T>& lv, int tile, int gid, int lane, const T* PSGB_PHASE_RESTRICT b,
+                             const T* PSGB_PHASE_RESTRICT x, T* PSGB_PHASE_RESTRICT y, T omega, int inner,
+                             const InstanceScalars* sc, int gate) {
+    __shared__ T xs[kGroups][kTile];
+    const TileSet<1> ts = tile_set<1>(lv.tile_meta, lv.tiles, tile);
+    if (!ts.sweep[0] || !gate_open(sc, ts.inst[0], gate)) return;
+    const std::uint32_t P = lv.rows;
+    const int row = ts.tile[0] * kTile + lane;
+    const int first = ts.tile[0] * kTile;
+    const bool live = lane < ts.rows[0];
+    // the row's couplings: within the tile (index into xs) or frozen at x
+    T a[W], h[W];
+    int local[W];
+    T bv = T(0), inv = T(0), xo = T(0);
+    if (live) {
+        bv = b[row];
+        inv = lv.inv[row];
+        xo = x[row];
+#pragma unroll
+        for (int j = 0; j < W; ++j) {
+            const int c = lv.col[j * P + row];
+            a[j] = lv.vd[j * P + row];
+            local[j] = (c >= first && c < first + kTile) ? c - first : -1;
+            h[j] = local[j] < 0 ? x[c] : T(0);
+        }
+    }
+    xs[gid][lane] = xo;
+    group_sync(gid);
+    for (int sweep = 0; sweep < inner; ++sweep) {
+        T out = xo;
+        if (live) {
+            T s = bv;
+#pragma unroll
+            for (int j = 0; j < W; ++j) s -= a[j] * (local[j] >= 0 ? xs[gid][local[j]] : h[j]);
+            out = xo + omega * (inv * s - xo);
+        }
+        group_sync(gid);
+        xs[gid][lane] = out;
+        xo = out;
+        group_sync(gid);
+    }
+    count_bytes(lv.bytes, lane, static_cast<unsigned long long>(ts.rows[0]) * (4ull * W + sizeof(T) * (W + 4ull)));
+    if (live) y[row] = xo;
+}
+
 // r = b - A x
 template <typename T, int W, int R>
 __device__ void residual(const LevelView<T>& lv, int t0, int lane, const T* PSGB_PHASE_RESTRICT b,

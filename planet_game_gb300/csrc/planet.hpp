@@ -186,8 +186,10 @@ struct SmootherConfig {
     int pre = 2, post = 2;             // damped Jacobi sweeps on every level ...
     double omega = 0.8;                // damping factor
     std::vector<int> level_pre, level_post;   // ... unless set per level (a tuning)
+    std::vector<int> level_inner;             // per level: block-local sweeps per smoothing launch (1: plain Jacobi)
     int pre_at(std::size_t l) const { return l < level_pre.size() ? level_pre[l] : pre; }
     int post_at(std::size_t l) const { return l < level_post.size() ? level_post[l] : post; }
+    int inner_at(std::size_t l) const { return l < level_inner.size() ? level_inner[l] : 1; }
     // The first (zero-start) sweep of level l writes x when the level's sweep count after
     // it is even, so that its last sweep ends in x.
     bool starts_in_x(std::size_t l) const { return ((pre_at(l) - 1 + post_at(l)) % 2) == 0; }

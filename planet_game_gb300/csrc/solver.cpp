@@ -465,6 +465,7 @@ TailArgs<T> tail_args(Batch& b, int gate) {
         a.level[l] = level_of<T>(b, l);
         a.pre[l] = b.smoother.pre_at(l);
         a.post[l] = b.smoother.post_at(l);
+        a.inner[l] = b.smoother.inner_at(l);
         a.starts_in_x[l] = b.smoother.starts_in_x(l) ? 1 : 0;
     }
     a.tile_range = b.tile_range;
@@ -553,7 +554,7 @@ void vcycle(Batch& b, const T* rhs, T* x, int gate, bool first_sweep_done, cudaS
         if (l > 0 && b.dense_at[l]) dense = dense_task<T>(b, l, Pick<T>::bvec(L), Pick<T>::x(L));
         if (l == 0 && !first_sweep_done) launch_smooth_zero<T>(lv, rhs_of[l], cur[l], omega, b.scalars, gate, st);
         for (int k = 1; k < sm.pre_at(l); ++k) {
-            launch_smooth<T>(lv, rhs_of[l], cur[l], other[l], omega, b.scalars, gate, st, dense);
+            launch_smooth<T>(lv, rhs_of[l], cur[l], other[l], omega, b.scalars, gate, st, dense, sm.inner_at(l));
             dense = DenseTask<T>{};
             std::swap(cur[l], other[l]);
         }
@@ -580,7 +581,7 @@ void vcycle(Batch& b, const T* rhs, T* x, int gate, bool first_sweep_done, cudaS
         launch_prolong_smooth<T>(lv, L.agg, e, rhs_of[l], cur[l], other[l], omega, b.scalars, gate, st);
         std::swap(cur[l], other[l]);
         for (int k = 1; k < sm.post_at(l); ++k) {
-            launch_smooth<T>(lv, rhs_of[l], cur[l], other[l], omega, b.scalars, gate, st);
+            launch_smooth<T>(lv, rhs_of[l], cur[l], other[l], omega, b.scalars, gate, st, DenseTask<T>{}, sm.inner_at(l));
             std::swap(cur[l], other[l]);
         }
     }
@@ -602,6 +603,7 @@ std::vector<int> shape_of(const Batch& b) {
     for (std::size_t l = 0; l < b.levels.size(); ++l) {
         shape.push_back(b.smoother.pre_at(l));
         shape.push_back(b.smoother.post_at(l));
+        shape.push_back(b.smoother.inner_at(l));
         shape.push_back(b.levels[l].sets_stencil);
         shape.push_back(b.levels[l].sets_vector);
     }
@@ -742,6 +744,7 @@ PersistentArgs<T> persistent_args(Batch& b, const SolveOptions& opt, const doubl
     for (std::size_t l = 0; l < b.levels.size(); ++l) {
         a.pre[l] = b.smoother.pre_at(l);
         a.post[l] = b.smoother.post_at(l);
+        a.inner[l] = b.smoother.inner_at(l);
         a.starts_in_x[l] = b.smoother.starts_in_x(l) ? 1 : 0;
     }
     a.omega = static_cast<T>(b.smoother.omega);
