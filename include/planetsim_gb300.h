@@ -76,6 +76,7 @@ typedef struct psgb_planet_info {
     uint32_t levels;             /* multigrid levels (the last one is solved densely) */
     uint32_t level_rows[8];      /* rows per multigrid level */
     uint64_t device_bytes;       /* HBM held by the planet (mesh + its solo batch) */
+    uint64_t fine_cells;         /* agglomerated planets: cells of the fine mesh; 0 otherwise */
 } psgb_planet_info;
 int psgb_planet_info_get(const psgb_planet* planet, psgb_planet_info* out);
 
@@ -103,6 +104,35 @@ typedef struct psgb_mesh_view {
     const double* graph_weight_sum; /* [cells] */
 } psgb_mesh_view;
 int psgb_planet_mesh_view(const psgb_planet* planet, psgb_mesh_view* out);
+
+/* The transport one mesh level coarser, as the reference's production path runs it:
+ * agglomerated_transport_graph / agglomerated_mesh (heat_transport.cpp:456-543). The
+ * planet's nodes are the cells of the level-1 mesh (its mesh view), each taking the
+ * summed areas of the fine cells nearest to it; every transport entry point
+ * (diffusion source, set_matrix, solves, steps, batches) then works on that graph.
+ * Level 0: the mesh itself. */
+int psgb_planet_create_agglomerated(uint32_t level, double radius_m, psgb_planet** out);
+/* Host views of the transport graph (valid while the planet lives): node areas, CSR
+ * offsets [nodes + 1], neighbours, weights l/d and their sums per node. */
+typedef struct psgb_graph_view {
+    const double* area_m2;
+    const uint32_t* offset;
+    const uint32_t* neighbour;
+    const double* weight;
+    const double* weight_sum;
+} psgb_graph_view;
+int psgb_planet_graph_view(const psgb_planet* planet, psgb_graph_view* out);
+/* Agglomerated planets: the node of every fine cell ([fine_cells], HOST). */
+int psgb_planet_group_of_cell(const psgb_planet* planet, uint32_t* out);
+/* Agglomerated planets, the production response's two sides (surface_energy.cpp:
+ * 1285-1296 and 1583/1595): the nodes' area-weighted means of fine-cell fields
+ * (sum over each node's fine cells in cell order of A_cell v_cell, over the node's
+ * area; bit-identical to that loop), for one field or two (fine_b and node_b both
+ * NULL or both set); and every fine cell taking its node's value. */
+int psgb_group_mean(psgb_planet* planet, const double* fine_a, const double* fine_b, double* node_a,
+                    double* node_b, int memory, void* stream);
+int psgb_group_scatter(psgb_planet* planet, const double* node_value, double* fine_value, int memory,
+                       void* stream);
 
 /* Integer structure of one multigrid level (heat_transport.cpp:54-66): CSR
  * offsets [rows + 1] and columns, aggregate of each row ([rows], none on the

@@ -82,8 +82,10 @@ class OracleMesh:
         self.n = n
         self.offset = np.append(a["edge_offset"], np.uint32(len(a["neighbor"]))).astype(np.uint32)
         self.neighbour = a["neighbor"].astype(np.uint32)
+        # the transport graph's node areas: the cells' own, or an agglomeration's sums
+        a.setdefault("graph_area_m2", a["area_m2"])
         self.graph = Graph(n, _p(self.offset), _p(self.neighbour), _p(a["graph_weight"]), _p(a["graph_weight_sum"]),
-                           _p(a["area_m2"]))
+                           _p(a["graph_area_m2"]))
         self.mesh = Mesh(n, len(a["edge_length_m"]), _p(a["edge_offset"]), _p(a["edge_count"]), _p(a["neighbor"]),
                          _p(a["edge"]), _p(a["normal_east"]), _p(a["normal_north"]), _p(a["edge_first"]),
                          _p(a["edge_length_m"]), _p(a["edge_distance_m"]), _p(a["area_m2"]))

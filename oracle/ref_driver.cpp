@@ -146,6 +146,31 @@ void refd_graph(void* handle, double* area, std::uint64_t* offset, std::uint64_t
     }
 }
 
+// ---- agglomerated graph: agglomerated_transport_graph (heat_transport.cpp:467-539) ----
+void refd_agglomeration_counts(void* handle, std::uint64_t* counts) {
+    const std::vector<std::size_t>* groups = nullptr;
+    const auto& graph = agglomerated_transport_graph(*static_cast<PlanetMesh*>(handle), groups);
+    counts[0] = graph.size();
+    counts[1] = graph.neighbour.size();
+    counts[2] = groups->size();
+}
+
+void refd_agglomeration(void* handle, double* area, std::uint64_t* offset, std::uint64_t* neighbour,
+                        double* weight, double* weight_sum, std::uint64_t* group_of_cell) {
+    const std::vector<std::size_t>* groups = nullptr;
+    const auto& graph = agglomerated_transport_graph(*static_cast<PlanetMesh*>(handle), groups);
+    for (std::size_t i = 0; i < graph.size(); ++i) {
+        area[i] = graph.area_m2[i];
+        weight_sum[i] = graph.weight_sum[i];
+    }
+    for (std::size_t i = 0; i < graph.offset.size(); ++i) offset[i] = graph.offset[i];
+    for (std::size_t k = 0; k < graph.neighbour.size(); ++k) {
+        neighbour[k] = graph.neighbour[k];
+        weight[k] = graph.weight[k];
+    }
+    for (std::size_t c = 0; c < groups->size(); ++c) group_of_cell[c] = (*groups)[c];
+}
+
 // ---- hierarchy: build_hierarchy (heat_transport.cpp:175-200) --------------
 void* refd_hierarchy_new(void* handle) {
     const auto graph = mesh_transport_graph(*static_cast<PlanetMesh*>(handle));
@@ -363,6 +388,60 @@ void refd_solve_quartic(void* handle, double a, double conductance, const double
     }
     const TransportResponse response = [&](const Field2D<double>& source, Field2D<double>& mean,
                                            Field2D<double>& slope) { quartic_response(n, a, b, source, mean, slope); };
+    ImplicitTransportSettings settings;
+    settings.cg_relative_tolerance = cg_tolerance;
+    settings.newton_tolerance_W_m2 = newton_tolerance;
+    const auto result = solve_implicit_transport(graph, conductance, floor, response, settings,
+                                                 static_cast<std::size_t>(workers));
+    std::copy(floor.values().begin(), floor.values().end(), floor_out);
+    std::copy(result.mean_K.values().begin(), result.mean_K.values().end(), mean_out);
+    std::copy(result.source_W_m2.values().begin(), result.source_W_m2.values().end(), source_out);
+    stats[0] = result.newton_iterations;
+    stats[1] = result.cg_iterations;
+    stats[2] = result.consistency_residual_W_m2;
+    stats[3] = result.sum_W;
+    stats[4] = result.absolute_sum_W;
+    stats[5] = result.dissipation_W_K;
+}
+
+// The same solve on the agglomerated graph of a fine mesh, as the production step runs it
+// (surface_energy.cpp:1219-1300, 1589-1597): each fine cell answers the quartic at its
+// group's source, a group's mean and slope are the area-weighted means of its cells'
+// (summed in cell order, over the group's area); the floor of a group is the largest of
+// its cells' floors. Outputs per group.
+void refd_solve_quartic_agglomerated(void* handle, double a, double conductance, const double* b_fine,
+                                     double cg_tolerance, double newton_tolerance, std::uint64_t workers,
+                                     double* floor_out, double* mean_out, double* source_out, double* stats) {
+    const auto& mesh = *static_cast<PlanetMesh*>(handle);
+    const std::vector<std::size_t>* group_map = nullptr;
+    const TransportGraph& graph = agglomerated_transport_graph(mesh, group_map);
+    const std::vector<std::size_t>& group_of_cell = *group_map;
+    const std::size_t cells = mesh.cell_count(), groups = graph.size();
+    const double radiative = 0.75 * 0.97 * stefan_boltzmann_W_m2_K4;
+    Field2D<double> floor(groups, -std::numeric_limits<double>::infinity());
+    for (std::size_t cell = 0; cell < cells; ++cell) {
+        const double x = 100.0;
+        double& f = floor[group_of_cell[cell]];
+        f = std::max(f, a * x + radiative * x * x * x * x - b_fine[cell]);
+    }
+    std::vector<std::vector<std::size_t>> members(groups);
+    for (std::size_t cell = 0; cell < cells; ++cell) members[group_of_cell[cell]].push_back(cell);
+    Field2D<double> cell_source(cells, 0.0), cell_mean(cells, 0.0), cell_slope(cells, 0.0);
+    const TransportResponse response = [&](const Field2D<double>& source, Field2D<double>& mean,
+                                           Field2D<double>& slope) {
+        for (std::size_t cell = 0; cell < cells; ++cell) cell_source[cell] = source[group_of_cell[cell]];
+        quartic_response(cells, a, b_fine, cell_source, cell_mean, cell_slope);
+        for (std::size_t group = 0; group < groups; ++group) {
+            double air = 0.0, air_slope = 0.0;
+            for (const std::size_t cell : members[group]) {
+                const double area = mesh.cells()[cell].area_m2;
+                air += area * cell_mean[cell];
+                air_slope += area * cell_slope[cell];
+            }
+            mean[group] = air / graph.area_m2[group];
+            slope[group] = air_slope / graph.area_m2[group];
+        }
+    };
     ImplicitTransportSettings settings;
     settings.cg_relative_tolerance = cg_tolerance;
     settings.newton_tolerance_W_m2 = newton_tolerance;

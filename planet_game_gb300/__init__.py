@@ -9,11 +9,14 @@ from .api import (  # noqa: F401
     GraphMultigrid,
     PlanetMesh,
     TransportGraph,
+    agglomerated_transport_graph,
     column_constants,
     column_radiation,
     diffusion_source,
     divergence,
     gradient,
+    group_mean,
+    group_scatter,
     laplacian,
     make_icosphere,
     mesh_transport_graph,

@@ -88,15 +88,19 @@ class PlanetMesh:
     the device copy is uploaded on first GPU use.
     """
 
-    def __init__(self, level: int, radius_m: float):
+    def __init__(self, level: int, radius_m: float, agglomerated: bool = False):
         lib = capi.load()
         h = C.c_void_p()
-        _raise(lib.psgb_planet_create(C.c_uint32(level), C.c_double(radius_m), C.byref(h)))
+        create = lib.psgb_planet_create_agglomerated if agglomerated else lib.psgb_planet_create
+        _raise(create(C.c_uint32(level), C.c_double(radius_m), C.byref(h)))
         self._h = h
-        self.subdivision = int(level)
+        self.agglomerated = bool(agglomerated)
+        # the mesh the transport runs on: one level coarser when agglomerated
+        self.subdivision = max(int(level) - 1, 0) if agglomerated else int(level)
         self.radius_m = float(radius_m)
         info = capi.PlanetInfo()
         _raise(lib.psgb_planet_info_get(h, C.byref(info)))
+        self.fine_cell_count = int(info.fine_cells)
         self.cell_count = int(info.cells)
         self.edge_count = int(info.edges)
         self.directed_edge_count = int(info.directed_edges)
@@ -143,7 +147,21 @@ class PlanetMesh:
             "corner_unit": _view(v.corner_unit, np.float64, 3 * k).reshape(k, 3),
             "graph_weight": _view(v.graph_weight, np.float64, d),
             "graph_weight_sum": _view(v.graph_weight_sum, np.float64, n),
+            "graph_area_m2": self._graph_area(),
         }
+
+    def _graph_area(self) -> np.ndarray:
+        g = capi.GraphView()
+        _raise(capi.load().psgb_planet_graph_view(self._h, C.byref(g)))
+        return _view(g.area_m2, np.float64, self.cell_count)
+
+    def group_of_cell(self) -> np.ndarray:
+        """Agglomerated planets: the transport node of every fine cell."""
+        if not self.agglomerated:
+            raise ValueError("not an agglomerated planet")
+        out = np.empty(self.fine_cell_count, dtype=np.uint32)
+        _raise(capi.load().psgb_planet_group_of_cell(self._h, _ptr(out)))
+        return out
 
     def hierarchy_level(self, level: int) -> dict[str, np.ndarray]:
         sizes = (C.c_uint64 * 4)()
@@ -167,6 +185,15 @@ def make_icosphere(subdivision: int, radius_m: float) -> PlanetMesh:
     return PlanetMesh(subdivision, radius_m)
 
 
+def agglomerated_transport_graph(subdivision: int, radius_m: float) -> PlanetMesh:
+    """The transport of a level-`subdivision` planet one mesh level coarser, as the
+    reference's production path runs it (agglomerated_transport_graph, heat_transport.cpp:
+    456-539): every fine cell joins the nearest cell of the coarser mesh, nodes take their
+    fine cells' summed areas. The returned planet's cells are those nodes; its
+    group_of_cell() maps fine cells onto them."""
+    return PlanetMesh(subdivision, radius_m, agglomerated=True)
+
+
 @dataclass
 class TransportGraph:
     """CSR transport graph of a mesh (heat_transport.hpp:27-36)."""
@@ -185,7 +212,7 @@ class TransportGraph:
 def mesh_transport_graph(mesh: PlanetMesh) -> TransportGraph:
     a = mesh.arrays()
     offset = np.append(a["edge_offset"].astype(np.uint64), np.uint64(mesh.directed_edge_count))
-    return TransportGraph(mesh, a["area_m2"], offset, a["neighbor"].astype(np.uint64), a["graph_weight"],
+    return TransportGraph(mesh, a["graph_area_m2"], offset, a["neighbor"].astype(np.uint64), a["graph_weight"],
                           a["graph_weight_sum"])
 
 
@@ -219,6 +246,32 @@ def diffusion_source(mesh: PlanetMesh, conductance_W_K: float, temperature_K):
     mem, st = _memory_of(temperature_K, out)
     _raise(capi.load().psgb_diffusion_source(mesh.handle, C.c_double(conductance_W_K), _ptr(temperature_K),
                                              _ptr(out), mem, st))
+    return out
+
+
+def group_mean(planet: PlanetMesh, fine_a, fine_b=None):
+    """Agglomerated planets: the nodes' area-weighted means of fine-cell fields, as the
+    production response forms a group's air temperature and slope (surface_energy.cpp:
+    1285-1296). Returns one array, or two when `fine_b` is given."""
+    if len(fine_a) != planet.fine_cell_count or (fine_b is not None and len(fine_b) != planet.fine_cell_count):
+        raise ValueError("fine-cell field does not match the planet's fine mesh")
+    out_a = _empty_like(fine_a, (planet.cell_count,))
+    out_b = None if fine_b is None else _empty_like(fine_b, (planet.cell_count,))
+    mem, st = _memory_of(fine_a, fine_b, out_a)
+    nil = C.c_void_p(None)
+    _raise(capi.load().psgb_group_mean(planet.handle, _ptr(fine_a), nil if fine_b is None else _ptr(fine_b),
+                                       _ptr(out_a), nil if out_b is None else _ptr(out_b), mem, st))
+    return out_a if fine_b is None else (out_a, out_b)
+
+
+def group_scatter(planet: PlanetMesh, node_value):
+    """Agglomerated planets: every fine cell takes its node's value (the transport
+    applied per fine cell, surface_energy.cpp:1583, 1595)."""
+    if len(node_value) != planet.cell_count:
+        raise ValueError("node field does not match the planet's transport graph")
+    out = _empty_like(node_value, (planet.fine_cell_count,))
+    mem, st = _memory_of(node_value, out)
+    _raise(capi.load().psgb_group_scatter(planet.handle, _ptr(node_value), _ptr(out), mem, st))
     return out
 
 

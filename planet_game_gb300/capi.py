@@ -36,7 +36,11 @@ SCHEDULE_PERSISTENT = 2
 class PlanetInfo(C.Structure):
     _fields_ = [("cells", C.c_uint64), ("edges", C.c_uint64), ("directed_edges", C.c_uint64),
                 ("corners", C.c_uint64), ("levels", C.c_uint32), ("level_rows", C.c_uint32 * 8),
-                ("device_bytes", C.c_uint64)]
+                ("device_bytes", C.c_uint64), ("fine_cells", C.c_uint64)]
+
+
+class GraphView(C.Structure):
+    _fields_ = [(name, C.c_void_p) for name in ("area_m2", "offset", "neighbour", "weight", "weight_sum")]
 
 
 class MeshView(C.Structure):
@@ -108,6 +112,11 @@ _SIGNATURES = {
     "psgb_last_error": (C.c_char_p, []),
     "psgb_abi_version": (C.c_int, []),
     "psgb_planet_create": (C.c_int, [C.c_uint32, C.c_double, C.POINTER(P)]),
+    "psgb_planet_create_agglomerated": (C.c_int, [C.c_uint32, C.c_double, C.POINTER(P)]),
+    "psgb_planet_graph_view": (C.c_int, [P, C.POINTER(GraphView)]),
+    "psgb_planet_group_of_cell": (C.c_int, [P, P]),
+    "psgb_group_mean": (C.c_int, [P, P, P, P, P, C.c_int, P]),
+    "psgb_group_scatter": (C.c_int, [P, P, P, C.c_int, P]),
     "psgb_planet_destroy": (None, [P]),
     "psgb_planet_info_get": (C.c_int, [P, C.POINTER(PlanetInfo)]),
     "psgb_planet_mesh_view": (C.c_int, [P, C.POINTER(MeshView)]),

@@ -63,7 +63,7 @@ const psgb::DevMesh& device_mesh(psgb_planet* h) {
 // Device staging buffers of max(P, edges) doubles each.
 double* stage(psgb_planet* h, int index) {
     const psgb::DevMesh& d = device_mesh(h);
-    const std::size_t len = std::max<std::size_t>(d.p, d.edges);
+    const std::size_t len = std::max<std::size_t>(std::max<std::size_t>(d.p, d.edges), d.fine_cells);
     while (static_cast<int>(h->stage.size()) <= index) h->stage.push_back(h->stage_store.alloc<double>(len));
     h->stage_len = len;
     return h->stage[index];
@@ -307,15 +307,53 @@ void psgb_solve_options_default(psgb_solve_options* out) {
     out->schedule = PSGB_SCHEDULE_AUTO;
 }
 
+namespace {
+std::uint64_t next_planet_serial() {
+    static std::atomic<std::uint64_t> serials{0};
+    return ++serials;
+}
+}  // namespace
+
 int psgb_planet_create(uint32_t level, double radius_m, psgb_planet** out) {
     return guarded([&] {
         require(out != nullptr, "output handle pointer is null");
         *out = nullptr;
-        static std::atomic<std::uint64_t> serials{0};
         auto h = std::make_unique<psgb_planet>();
         h->planet = psgb::make_planet(level, radius_m);
-        h->serial = ++serials;
+        h->serial = next_planet_serial();
         *out = h.release();
+        return PSGB_OK;
+    });
+}
+
+int psgb_planet_create_agglomerated(uint32_t level, double radius_m, psgb_planet** out) {
+    return guarded([&] {
+        require(out != nullptr, "output handle pointer is null");
+        *out = nullptr;
+        auto h = std::make_unique<psgb_planet>();
+        h->planet = psgb::make_planet(level, radius_m, true);
+        h->serial = next_planet_serial();
+        *out = h.release();
+        return PSGB_OK;
+    });
+}
+
+int psgb_planet_graph_view(const psgb_planet* h, psgb_graph_view* out) {
+    return guarded([&] {
+        require(h != nullptr && out != nullptr, "null argument");
+        const psgb::TransportGraph& g = h->planet->graph;
+        *out = psgb_graph_view{g.area_m2.data(), g.offset.data(), g.neighbour.data(), g.weight.data(),
+                               g.weight_sum.data()};
+        return PSGB_OK;
+    });
+}
+
+int psgb_planet_group_of_cell(const psgb_planet* h, uint32_t* out) {
+    return guarded([&] {
+        require(h != nullptr && out != nullptr, "null argument");
+        const auto& g = h->planet->group_of_cell;
+        require(!g.empty(), "not an agglomerated planet");
+        std::copy(g.begin(), g.end(), out);
         return PSGB_OK;
     });
 }
@@ -334,6 +372,7 @@ int psgb_planet_info_get(const psgb_planet* h, psgb_planet_info* out) {
         out->levels = static_cast<uint32_t>(p.hierarchy.levels.size());
         for (std::size_t l = 0; l < p.hierarchy.levels.size() && l < 8; ++l) out->level_rows[l] = p.hierarchy.levels[l].size;
         out->device_bytes = p.store.bytes() + (p.solo ? p.solo->store.bytes() : 0) + h->stage_store.bytes();
+        out->fine_cells = p.group_of_cell.size();
         return PSGB_OK;
     });
 }
@@ -485,6 +524,65 @@ int psgb_diffusion_source(psgb_planet* h, double conductance_W_K, const double* 
         PSGB_CUDA(cudaGetLastError());
         if (memory == PSGB_MEMORY_HOST) {
             copy_out(source_W_m2, out, d.n * 8, memory, st);
+            PSGB_CUDA(cudaStreamSynchronize(st));
+        }
+        return PSGB_OK;
+    });
+}
+
+int psgb_group_mean(psgb_planet* h, const double* fine_a, const double* fine_b, double* node_a, double* node_b,
+                    int memory, void* stream) {
+    return guarded([&] {
+        require(h != nullptr && fine_a != nullptr && node_a != nullptr, "null argument");
+        require((fine_b == nullptr) == (node_b == nullptr), "second field: both pointers or neither");
+        require(!h->planet->group_of_cell.empty(), "not an agglomerated planet");
+        require_memory(memory);
+        const psgb::DevMesh& d = device_mesh(h);
+        cudaStream_t st = as_stream(stream);
+        const double *a = fine_a, *b = fine_b;
+        double *ma = node_a, *mb = node_b;
+        if (memory == PSGB_MEMORY_HOST) {
+            double* sa = stage(h, 0);
+            copy_in(sa, fine_a, std::size_t(d.fine_cells) * 8, memory, st);
+            a = sa;
+            ma = stage(h, 2);
+            if (fine_b != nullptr) {
+                double* sb = stage(h, 1);
+                copy_in(sb, fine_b, std::size_t(d.fine_cells) * 8, memory, st);
+                b = sb;
+                mb = stage(h, 3);
+            }
+        }
+        psgb::launch_group_mean(d, a, b, ma, mb, st);
+        PSGB_CUDA(cudaGetLastError());
+        if (memory == PSGB_MEMORY_HOST) {
+            copy_out(node_a, ma, std::size_t(d.n) * 8, memory, st);
+            if (node_b != nullptr) copy_out(node_b, mb, std::size_t(d.n) * 8, memory, st);
+            PSGB_CUDA(cudaStreamSynchronize(st));
+        }
+        return PSGB_OK;
+    });
+}
+
+int psgb_group_scatter(psgb_planet* h, const double* node_value, double* fine_value, int memory, void* stream) {
+    return guarded([&] {
+        require(h != nullptr && node_value != nullptr && fine_value != nullptr, "null argument");
+        require(!h->planet->group_of_cell.empty(), "not an agglomerated planet");
+        require_memory(memory);
+        const psgb::DevMesh& d = device_mesh(h);
+        cudaStream_t st = as_stream(stream);
+        const double* in = node_value;
+        double* out = fine_value;
+        if (memory == PSGB_MEMORY_HOST) {
+            double* s = stage(h, 0);
+            copy_in(s, node_value, std::size_t(d.n) * 8, memory, st);
+            in = s;
+            out = stage(h, 1);
+        }
+        psgb::launch_group_scatter(d, in, out, st);
+        PSGB_CUDA(cudaGetLastError());
+        if (memory == PSGB_MEMORY_HOST) {
+            copy_out(fine_value, out, std::size_t(d.fine_cells) * 8, memory, st);
             PSGB_CUDA(cudaStreamSynchronize(st));
         }
         return PSGB_OK;

@@ -136,9 +136,9 @@ int psgb_solve_implicit_transport(psgb_planet* planet, double conductance_W_K, c
         if (psgb_planet_info_get(planet, &info) != PSGB_OK) throw std::runtime_error(psgb_last_error());
         const std::size_t n = info.cells;
         std::vector<double> area(n);
-        {
-            psgb_mesh_view view{};
-            if (psgb_planet_mesh_view(planet, &view) != PSGB_OK) throw std::runtime_error(psgb_last_error());
+        {   // the transport graph's node areas (an agglomeration's summed fine areas)
+            psgb_graph_view view{};
+            if (psgb_planet_graph_view(planet, &view) != PSGB_OK) throw std::runtime_error(psgb_last_error());
             std::copy(view.area_m2, view.area_m2 + n, area.begin());
         }
         Solver s{planet, n, conductance_W_K, area, source_floor_W_m2, latent_W_m2, response, user, {}, std::vector<double>(n)};

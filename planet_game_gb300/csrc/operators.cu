@@ -49,6 +49,33 @@ __global__ void k_diffusion_source(std::uint32_t n, std::uint32_t P, const std::
     out[c] = __ddiv_rn(dmul(conductance, sum), area[c]);
 }
 
+// A node's area-weighted mean of its fine cells' values, summed over the members in cell
+// order and divided by the node's area (surface_energy.cpp:1285-1296); two fields at once
+// (mean and slope of a response), the second optional.
+__global__ void k_group_mean(std::uint32_t n, const std::uint32_t* __restrict__ member_offset,
+                             const std::uint32_t* __restrict__ member, const double* __restrict__ fine_area,
+                             const double* __restrict__ graph_area, const double* __restrict__ a,
+                             const double* __restrict__ b, double* __restrict__ mean_a, double* __restrict__ mean_b) {
+    const std::uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    double sa = 0.0, sb = 0.0;
+    for (std::uint32_t k = member_offset[g]; k < member_offset[g + 1]; ++k) {
+        const std::uint32_t c = member[k];
+        const double area = fine_area[c];
+        sa = dadd(sa, dmul(area, a[c]));
+        if (b != nullptr) sb = dadd(sb, dmul(area, b[c]));
+    }
+    mean_a[g] = __ddiv_rn(sa, graph_area[g]);
+    if (b != nullptr) mean_b[g] = __ddiv_rn(sb, graph_area[g]);
+}
+
+// Every fine cell takes its node's value (surface_energy.cpp:1583, 1595).
+__global__ void k_group_scatter(std::uint32_t fine_cells, const std::uint32_t* __restrict__ group_of_cell,
+                                const double* __restrict__ node_value, double* __restrict__ out) {
+    const std::uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < fine_cells) out[c] = node_value[group_of_cell[c]];
+}
+
 template <typename T>
 __global__ void k_gradient(std::uint32_t n, std::uint32_t P, const std::int32_t* __restrict__ nbr,
                            const std::uint8_t* __restrict__ degree, const double* __restrict__ dist,
@@ -213,7 +240,17 @@ void launch_divergence(const DevMesh& m, const T* flux, T* out, cudaStream_t st)
 }
 void launch_diffusion_source(const DevMesh& m, double conductance, const double* t, double* out,
                              cudaStream_t st) {
-    PSGB_LAUNCH(kFamOperator, st, k_diffusion_source<<<(m.n + 255) / 256, 256, 0, st>>>(m.n, m.p, m.nbr, m.w, m.area, conductance, t, out));
+    PSGB_LAUNCH(kFamOperator, st, k_diffusion_source<<<(m.n + 255) / 256, 256, 0, st>>>(m.n, m.p, m.nbr, m.w, m.graph_area, conductance, t, out));
+}
+
+void launch_group_mean(const DevMesh& m, const double* a, const double* b, double* mean_a, double* mean_b,
+                       cudaStream_t st) {
+    PSGB_LAUNCH(kFamOperator, st, k_group_mean<<<(m.n + 255) / 256, 256, 0, st>>>(m.n, m.member_offset, m.member, m.fine_area,
+                                                                               m.graph_area, a, b, mean_a, mean_b));
+}
+void launch_group_scatter(const DevMesh& m, const double* node_value, double* out, cudaStream_t st) {
+    PSGB_LAUNCH(kFamOperator, st, k_group_scatter<<<(m.fine_cells + 255) / 256, 256, 0, st>>>(m.fine_cells, m.group_of_cell,
+                                                                                           node_value, out));
 }
 
 template void launch_laplacian<float>(const DevMesh&, const float*, float*, cudaStream_t);

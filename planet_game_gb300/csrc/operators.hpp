@@ -11,6 +11,11 @@ template <typename T>
 void launch_gradient(const DevMesh& m, const T* in, T* east, T* north, cudaStream_t st);
 template <typename T>
 void launch_divergence(const DevMesh& m, const T* flux, T* out, cudaStream_t st);
+// Agglomerated planets: node means of fine-cell fields (b, mean_b may be null) and fine
+// cells taking their node's value.
+void launch_group_mean(const DevMesh& m, const double* a, const double* b, double* mean_a, double* mean_b,
+                       cudaStream_t st);
+void launch_group_scatter(const DevMesh& m, const double* node_value, double* out, cudaStream_t st);
 void launch_diffusion_source(const DevMesh& m, double conductance, const double* t, double* out,
                              cudaStream_t st);
 

@@ -104,14 +104,25 @@ struct DevMesh {
     double* dist = nullptr;            // [6][P] centroid distance; 1 in padding slots
     float* ne = nullptr;               // [6][P] FP32 outward normal (east)
     float* nn = nullptr;               // [6][P] FP32 outward normal (north)
-    double* area = nullptr;            // [P]; 1 in padding rows
+    double* area = nullptr;            // [P] mesh cell areas; 1 in padding rows
+    double* graph_area = nullptr;      // [P] the transport graph's node areas (differ when agglomerated)
     double* gm = nullptr;              // [4][P] m_ee, m_en, m_nn, det of the LSQ gradient
     double* edge_length = nullptr;     // [E]
+    // agglomerated planets: fine cells -> nodes
+    std::uint32_t fine_cells = 0;
+    std::uint32_t* group_of_cell = nullptr;   // [fine cells]
+    std::uint32_t* member_offset = nullptr;   // [n + 1]: each node's fine cells ...
+    std::uint32_t* member = nullptr;          // ... in cell order
+    double* fine_area = nullptr;              // [fine cells]
 };
 
 struct Planet {
-    HostMesh mesh;
-    TransportGraph graph;
+    HostMesh mesh;                     // for an agglomerated planet: the mesh one level coarser
+    TransportGraph graph;              // ... and its graph with the groups' summed fine areas
+    std::vector<std::uint32_t> group_of_cell;   // agglomerated planets: fine cell -> node
+    std::vector<std::uint32_t> member_offset, member;   // ... each node's fine cells in cell order
+    std::vector<double> fine_area_m2;  // ... the fine cells' areas
+    std::size_t fine_cells = 0;        // agglomerated planets: cells of the fine mesh
     HostHierarchy hierarchy;
     DevMesh dev;
     DeviceStore store;

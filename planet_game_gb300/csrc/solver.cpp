@@ -10,6 +10,7 @@
 
 #include "kernels.hpp"
 #include "coarse_tail.hpp"
+#include "host/agglomerate.hpp"
 #include "krylov.hpp"
 #include "persistent.hpp"
 #include "profile.hpp"
@@ -46,10 +47,33 @@ void default_launch_shapes(Batch& b) {
     b.tail_level = b.default_tail_level;
 }
 
-std::unique_ptr<Planet> make_planet(std::uint32_t level, double radius_m) {
+std::unique_ptr<Planet> make_planet(std::uint32_t level, double radius_m, bool agglomerated) {
     auto planet = std::make_unique<Planet>();
-    planet->mesh = build_icosphere(level, radius_m);
-    planet->graph = transport_graph(planet->mesh);
+    if (agglomerated && level > 0) {
+        // The transport one level coarser: the coarse mesh's graph, nodes taking the
+        // areas of the fine cells that join them (heat_transport.cpp:467-512).
+        const HostMesh fine = build_icosphere(level, radius_m);
+        planet->mesh = build_icosphere(level - 1, radius_m);
+        planet->graph = transport_graph(planet->mesh);
+        Agglomeration agg = agglomerate(fine, planet->mesh);
+        planet->graph.area_m2 = std::move(agg.area_m2);
+        planet->group_of_cell = std::move(agg.group_of_cell);
+        planet->member_offset = std::move(agg.member_offset);
+        planet->member = std::move(agg.member);
+        planet->fine_area_m2 = std::move(agg.fine_area_m2);
+        planet->fine_cells = fine.cells;
+    } else {
+        planet->mesh = build_icosphere(level, radius_m);
+        planet->graph = transport_graph(planet->mesh);
+        if (agglomerated) {   // level 0: the mesh itself
+            Agglomeration agg = identity_agglomeration(planet->mesh);
+            planet->group_of_cell = std::move(agg.group_of_cell);
+            planet->member_offset = std::move(agg.member_offset);
+            planet->member = std::move(agg.member);
+            planet->fine_area_m2 = std::move(agg.fine_area_m2);
+            planet->fine_cells = planet->mesh.cells;
+        }
+    }
     planet->hierarchy = build_hierarchy(planet->graph);
     for (const auto& lv : planet->hierarchy.levels) {
         if (lv.width > 16) throw std::logic_error("hierarchy level wider than 16");
@@ -110,6 +134,18 @@ void upload_planet(Planet& planet_ref) {
     d.ne = planet->store.upload(ne);
     d.nn = planet->store.upload(nn);
     d.area = planet->store.upload(area);
+    {
+        std::vector<double> graph_area(P, 1.0);
+        for (std::size_t c = 0; c < m.cells; ++c) graph_area[c] = planet->graph.area_m2[c];
+        d.graph_area = planet->store.upload(graph_area);
+    }
+    if (!planet->group_of_cell.empty()) {
+        d.fine_cells = static_cast<std::uint32_t>(planet->fine_cells);
+        d.group_of_cell = planet->store.upload(planet->group_of_cell);
+        d.member_offset = planet->store.upload(planet->member_offset);
+        d.member = planet->store.upload(planet->member);
+        d.fine_area = planet->store.upload(planet->fine_area_m2);
+    }
     d.gm = planet->store.upload(gm);
     d.edge_length = planet->store.upload(m.edge_length_m);
     planet->uploaded = true;

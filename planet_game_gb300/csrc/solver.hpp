@@ -25,7 +25,8 @@ struct SolveOptions {
 };
 
 // Host-side mesh, graph and hierarchy; no device memory is touched.
-std::unique_ptr<Planet> make_planet(std::uint32_t level, double radius_m);
+// `agglomerated`: the transport graph one mesh level coarser (agglomerated_transport_graph).
+std::unique_ptr<Planet> make_planet(std::uint32_t level, double radius_m, bool agglomerated = false);
 // Uploads the operator geometry to HBM (idempotent).
 void upload_planet(Planet& planet);
 

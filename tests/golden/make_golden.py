@@ -60,7 +60,53 @@ def load(reference: Path) -> C.CDLL:
     R.refd_insolation_nodes.argtypes = [C.c_int64, P]
     R.refd_quartic_response.argtypes = [C.c_uint64, C.c_double, P, P, P, P]
     R.refd_solve_quartic.argtypes = [P, C.c_double, C.c_double, P, C.c_double, C.c_double, C.c_uint64, P, P, P, P]
+    R.refd_agglomeration_counts.argtypes = [P, P]
+    R.refd_agglomeration.argtypes = [P, P, P, P, P, P, P]
+    R.refd_solve_quartic_agglomerated.argtypes = [P, C.c_double, C.c_double, P, C.c_double, C.c_double, C.c_uint64,
+                                                  P, P, P, P]
     return R
+
+
+AGGLOMERATION_LEVELS = (0, 1, 3, 5)
+
+
+def agglomeration_cases(R) -> None:
+    """The agglomerated transport graph (heat_transport.cpp:456-539): for each fine level,
+    the reference's group of every fine cell and the coarse graph (areas, CSR, weights).
+    Integer maps in full; the L5 graph's doubles in full as well (2,562 nodes)."""
+    out = {}
+    for level in AGGLOMERATION_LEVELS:
+        m = P(R.refd_mesh_new(level, RADIUS))
+        counts = np.zeros(3, dtype=np.uint64)
+        R.refd_agglomeration_counts(m, p(counts))
+        n, d, f = (int(c) for c in counts)
+        area, wsum = np.empty(n), np.empty(n)
+        off, nb = np.empty(n + 1, dtype=np.uint64), np.empty(d, dtype=np.uint64)
+        w, groups = np.empty(d), np.empty(f, dtype=np.uint64)
+        R.refd_agglomeration(m, p(area), p(off), p(nb), p(w), p(wsum), p(groups))
+        R.refd_mesh_free(m)
+        out.update({f"area{level}": area, f"offset{level}": off.astype(np.uint32),
+                    f"neighbour{level}": nb.astype(np.uint32), f"weight{level}": w,
+                    f"weight_sum{level}": wsum, f"group{level}": groups.astype(np.uint32)})
+    # The production pattern at L5: the quartic response per fine cell at its group's
+    # source, group means over the cells, the reference's solve on the agglomerated graph.
+    m = P(R.refd_mesh_new(5, RADIUS))
+    cnt = np.zeros(4, np.uint64)
+    R.refd_mesh_counts(m, p(cnt))
+    cells, groups = int(cnt[0]), len(out["area5"])
+    rng = np.random.default_rng(20261203)
+    radiative = 0.75 * 0.97 * 5.670374419e-8
+    a = 0.04 + 0.37
+    target = 200.0 + 120.0 * rng.random(cells)
+    out["qa"], out["qb"] = a, a * target + radiative * target ** 4
+    for factor in (1, 10):
+        K = factor * 0.5 * RADIUS * RADIUS
+        floor, mean, src, stats = np.empty(groups), np.empty(groups), np.empty(groups), np.empty(6)
+        R.refd_solve_quartic_agglomerated(m, a, K, p(out["qb"]), 1e-6, 1e-6, 4, p(floor), p(mean), p(src), p(stats))
+        out.update({f"qK{factor}": K, f"qfloor{factor}": floor, f"qmean{factor}": mean, f"qsource{factor}": src,
+                    f"qstats{factor}": stats})
+    R.refd_mesh_free(m)
+    np.savez_compressed(HERE / "agglomeration.npz", levels=np.array(AGGLOMERATION_LEVELS), **out)
 
 
 def quartic_cases(R) -> None:
@@ -287,6 +333,10 @@ if __name__ == "__main__":
     if "--quartic" in sys.argv:   # only the nonlinear-transport fixture
         quartic_cases(load(reference))
         print("quartic fixture written")
+    elif "--agglomeration" in sys.argv:   # only the agglomerated-graph fixture
+        agglomeration_cases(load(reference))
+        print("agglomeration fixture written")
     else:
         main(reference)
         quartic_cases(load(reference))
+        agglomeration_cases(load(reference))
