@@ -275,7 +275,9 @@ int psgb_batch_transport_step_masked(psgb_batch* batch, const uint8_t* active, c
  * cell); HOST arrays of `cells` values; a nonzero return aborts the solve. The two-point
  * Laplacians and every linear Newton system run on the GPU (the system with `options`:
  * precision, method, smoother; its tolerance and iteration cap come from `settings`).
- * All arrays are HOST arrays in the planet's cell order; `latent_W_m2` may be NULL. */
+ * All arrays are HOST arrays in the planet's cell order; `latent_W_m2` may be NULL.
+ * The Newton iterate lives in device memory; each evaluation copies h to the host and
+ * T, dT/dh back (pinned buffers). */
 typedef int (*psgb_transport_response)(void* user, uint64_t cells, const double* source_W_m2, double* mean_K,
                                        double* slope_K_m2_W);
 typedef struct psgb_transport_settings {
@@ -302,6 +304,43 @@ int psgb_solve_implicit_transport(psgb_planet* planet, double conductance_W_K, c
                                   const psgb_transport_settings* settings, const psgb_solve_options* options,
                                   const double* latent_W_m2, double* source_out_W_m2, double* mean_out_K,
                                   psgb_transport_result* result);
+
+/* The same solve with the response on the GPU: the whole Newton iteration (response,
+ * Laplacians, merit sums, line search trials, linear systems) stays in device memory;
+ * the host reads two scalars per evaluation (the merit sum A F^2 and max |F|) to take
+ * the line search's decisions. The response is called on the host with DEVICE arrays of
+ * `cells` values and the solve's stream, and enqueues its work on that stream. The
+ * floor, latent heat and outputs are HOST or DEVICE arrays as `memory` says. */
+typedef int (*psgb_device_response)(void* user, uint64_t cells, const double* source_W_m2, double* mean_K,
+                                    double* slope_K_m2_W, void* stream);
+int psgb_solve_implicit_transport_device(psgb_planet* planet, double conductance_W_K,
+                                         const double* source_floor_W_m2, psgb_device_response response,
+                                         void* user, const psgb_transport_settings* settings,
+                                         const psgb_solve_options* options, const double* latent_W_m2,
+                                         double* source_out_W_m2, double* mean_out_K,
+                                         psgb_transport_result* result, int memory, void* stream);
+
+/* The quartic column response of the reference's transport test (test_heat_transport.cpp:
+ * 30-76) as a GPU kernel: per cell the root x of a x + r x^4 = b + h by
+ * solve_column_surface's Newton without evaporation (column_step.cpp:254-270; bit-
+ * identical), slope 1/(a + 4 r x^3); cells whose index is a multiple of hold_stride are
+ * held at hold_K (slope 0) when they would pass it (hold_stride 0: none). `b` is a
+ * DEVICE array of `cells` values. With `planet` set (an agglomerated planet), the cells
+ * are its FINE cells: h is scattered from the nodes, the quartic runs per fine cell and
+ * the nodes take the area-weighted means (surface_energy.cpp:1240-1296); `scratch` is
+ * DEVICE memory of 2 fine-cell arrays. */
+typedef struct psgb_quartic_response {
+    double a;
+    double radiative;          /* r; the test's 0.75 * 0.97 * sigma */
+    const double* b;
+    uint32_t hold_stride;      /* the test's 7 */
+    double hold_K;             /* the test's 273.15 */
+    psgb_planet* planet;       /* NULL: per node */
+    double* scratch;
+} psgb_quartic_response;
+/* psgb_device_response with user = psgb_quartic_response*. */
+int psgb_quartic_device_response(void* user, uint64_t cells, const double* source_W_m2, double* mean_K,
+                                 double* slope_K_m2_W, void* stream);
 
 /* Stores per-edge conductances with a batch (HOST arrays, one per planet, [edges] W/K;
  * NULL entries clear a planet's): steps whose params set edge_conductance_stored use them

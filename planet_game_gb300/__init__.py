@@ -8,6 +8,7 @@ from .api import (  # noqa: F401
     Batch,
     GraphMultigrid,
     PlanetMesh,
+    QuarticResponse,
     TransportGraph,
     agglomerated_transport_graph,
     column_constants,
@@ -19,6 +20,7 @@ from .api import (  # noqa: F401
     group_scatter,
     laplacian,
     make_icosphere,
+    quartic_response,
     mesh_transport_graph,
     solve_implicit_transport,
     solve_newton_system,

@@ -366,10 +366,25 @@ def solve_implicit_transport(mesh: PlanetMesh, conductance_W_K: float, source_fl
                              settings: dict | None = None, latent_W_m2=None, **options) -> ImplicitTransportResult:
     """solve_implicit_transport (heat_transport.cpp:595-772) with a general response.
 
-    `response(source) -> (mean_K, slope_K_m2_W)` runs on the host (numpy arrays of the
-    cells); the Laplacians and the linear Newton systems run on the GPU with `options`
-    (precision, method, sweeps, schedule). Host arrays in and out."""
+    `response` is either
+    - a host callable `response(source) -> (mean_K, slope_K_m2_W)` on numpy arrays of
+      the cells (copied across once per evaluation), or
+    - a device response: a `QuarticResponse`, or `device=True` with a callable
+      `response(cells, source, mean, slope, stream)` on device pointers;
+    the Newton iterate, the Laplacians and the linear Newton systems (with `options`:
+    precision, method, sweeps, schedule) stay on the GPU either way. The floor, latent
+    heat and results are numpy arrays, or CUDA tensors on a device response."""
     n = mesh.cell_count
+    if isinstance(response, QuarticResponse) or options.pop("device", False):
+        floor = source_floor_W_m2 if _is_torch(source_floor_W_m2) else np.ascontiguousarray(source_floor_W_m2,
+                                                                                          dtype=np.float64)
+        latent = latent_W_m2
+        if latent is not None and not _is_torch(latent):
+            latent = np.ascontiguousarray(latent, dtype=np.float64)
+        if latent is not None and _is_torch(latent) != _is_torch(floor):
+            raise ValueError("pass the floor and the latent heat both as numpy arrays or both as CUDA tensors")
+        return _solve_device(mesh, conductance_W_K, floor, response, transport_settings(**(settings or {})),
+                             solve_options(**options), latent)
     floor = np.ascontiguousarray(source_floor_W_m2, dtype=np.float64)
     latent = None if latent_W_m2 is None else np.ascontiguousarray(latent_W_m2, dtype=np.float64)
     error: list[BaseException] = []
@@ -396,6 +411,98 @@ def solve_implicit_transport(mesh: PlanetMesh, conductance_W_K: float, source_fl
         _ptr(latent) if latent is not None else None, _ptr(source_out), _ptr(mean_out), C.byref(res))
     if error:
         raise error[0]
+    _raise(code)
+    return ImplicitTransportResult(source_out, mean_out, res.consistency_residual_W_m2, res.newton_iterations,
+                                   res.cg_iterations, res.sum_W, res.absolute_sum_W, res.dissipation_W_K)
+
+
+STEFAN_BOLTZMANN_W_M2_K4 = 5.670374419e-8
+
+
+@dataclass
+class QuarticResponse:
+    """The quartic column response of the reference's transport test (test_heat_transport.
+    cpp:30-76) evaluated on the GPU: per cell the root of a x + r x^4 = b + h, cells whose
+    index is a multiple of `hold_stride` held at `hold_K` when they would pass it. With
+    `fine=True` (an agglomerated planet) `b` is per FINE cell: each fine cell answers at
+    its node's source and the nodes take the area-weighted means, as the production step
+    forms a group's response (surface_energy.cpp:1240-1296)."""
+
+    a: float
+    b: object
+    radiative: float = 0.75 * 0.97 * STEFAN_BOLTZMANN_W_M2_K4
+    hold_stride: int = 7
+    hold_K: float = 273.15
+    fine: bool = False
+
+
+def quartic_response(q: QuarticResponse, source):
+    """The per-cell quartic response on the GPU: (T, dT/dh) for sources h (CUDA tensors)."""
+    import torch
+
+    if q.fine:
+        raise ValueError("the fine-cell response runs inside a solve on an agglomerated planet")
+    h = torch.as_tensor(source, dtype=torch.float64, device="cuda").contiguous()
+    b = torch.as_tensor(q.b, dtype=torch.float64, device="cuda").contiguous()
+    if b.numel() != h.numel():
+        raise ValueError("the quartic's b does not match the sources")
+    mean, slope = torch.empty_like(h), torch.empty_like(h)
+    cq = capi.QuarticResponse(q.a, q.radiative, b.data_ptr(), q.hold_stride, q.hold_K, None, None)
+    _raise(capi.load().psgb_quartic_device_response(C.byref(cq), C.c_uint64(h.numel()), C.c_void_p(h.data_ptr()),
+                                                    C.c_void_p(mean.data_ptr()), C.c_void_p(slope.data_ptr()),
+                                                    C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    return mean, slope
+
+
+def _solve_device(mesh: PlanetMesh, conductance_W_K: float, floor, response, st, o, latent):
+    """The device-resident Newton solve; `response` a QuarticResponse or a callable
+    (cells, source, mean, slope, stream) on device pointers."""
+    import torch
+
+    n = mesh.cell_count
+    keep = []
+    if isinstance(response, QuarticResponse):
+        cells = mesh.fine_cell_count if response.fine else n
+        if response.fine and not mesh.agglomerated:
+            raise ValueError("a fine-cell response needs an agglomerated planet")
+        b = torch.as_tensor(response.b, dtype=torch.float64, device="cuda").contiguous()
+        if b.numel() != cells:
+            raise ValueError("the quartic's b does not match the cells")
+        scratch = torch.empty(2 * cells if response.fine else 1, dtype=torch.float64, device="cuda")
+        q = capi.QuarticResponse(response.a, response.radiative, b.data_ptr(), response.hold_stride, response.hold_K,
+                                 mesh.handle.value if response.fine else None, scratch.data_ptr())
+        keep += [b, scratch, q]
+        fn = C.cast(capi.load().psgb_quartic_device_response, C.c_void_p)
+        user = C.cast(C.pointer(q), C.c_void_p)
+    else:
+        error: list[BaseException] = []
+
+        def trampoline(_user, cells, source, mean, slope, stream):
+            try:
+                response(int(cells), source, mean, slope, stream)
+                return 0
+            except BaseException as exc:   # reported after the call returns
+                error.append(exc)
+                return 1
+
+        cb = capi.DeviceResponse(trampoline)
+        keep += [cb, error]
+        fn = C.cast(cb, C.c_void_p)
+        user = None
+    on_device = _is_torch(floor)
+    if on_device:
+        source_out = torch.empty(n, dtype=torch.float64, device=floor.device)
+        mean_out = torch.empty(n, dtype=torch.float64, device=floor.device)
+        mem, stream = capi.MEMORY_DEVICE, C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    else:
+        source_out, mean_out = np.empty(n), np.empty(n)
+        mem, stream = capi.MEMORY_HOST, C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    res = capi.TransportResult()
+    code = capi.load().psgb_solve_implicit_transport_device(
+        mesh.handle, C.c_double(conductance_W_K), _ptr(floor), fn, user, C.byref(st), C.byref(o),
+        _ptr(latent) if latent is not None else None, _ptr(source_out), _ptr(mean_out), C.byref(res), mem, stream)
+    if not isinstance(response, QuarticResponse) and keep[1]:
+        raise keep[1][0]
     _raise(code)
     return ImplicitTransportResult(source_out, mean_out, res.consistency_residual_W_m2, res.newton_iterations,
                                    res.cg_iterations, res.sum_W, res.absolute_sum_W, res.dissipation_W_K)

@@ -28,10 +28,11 @@ ORACLE_LIB = ORACLE_DIR / "lib" / "libplanetsim_oracle.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 
-CU_SOURCES = ["multigrid.cu", "krylov.cu", "operators.cu", "column.cu", "noalloc.cu", "persistent.cu", "coarse_tail.cu"]
-CPP_SOURCES = ["solver.cpp", "autotune.cpp", "capi.cpp", "newton.cpp", "profile.cpp", "host/icosphere.cpp", "host/agglomerate.cpp", "host/hierarchy.cpp", "host/insolation.cpp"]
+CU_SOURCES = ["multigrid.cu", "krylov.cu", "operators.cu", "column.cu", "noalloc.cu", "persistent.cu", "coarse_tail.cu",
+              "newton.cu"]
+CPP_SOURCES = ["solver.cpp", "autotune.cpp", "capi.cpp", "profile.cpp", "host/icosphere.cpp", "host/agglomerate.cpp", "host/hierarchy.cpp", "host/insolation.cpp"]
 # Files compiled without FMA contraction (reference operation order).
-NO_FMAD = {"column.cu"}
+NO_FMAD = {"column.cu", "newton.cu"}
 
 
 def _nvcc() -> str:

@@ -76,6 +76,13 @@ class TransportResult(C.Structure):
 # int response(void* user, uint64_t cells, const double* source, double* mean, double* slope)
 TransportResponse = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint64, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                 C.POINTER(C.c_double))
+# psgb_device_response: (user, cells, source, mean, slope, stream), device pointers
+DeviceResponse = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p)
+
+
+class QuarticResponse(C.Structure):
+    _fields_ = [("a", C.c_double), ("radiative", C.c_double), ("b", C.c_void_p), ("hold_stride", C.c_uint32),
+                ("hold_K", C.c_double), ("planet", C.c_void_p), ("scratch", C.c_void_p)]
 
 
 class Tuning(C.Structure):
@@ -153,6 +160,10 @@ _SIGNATURES = {
     "psgb_transport_settings_default": (None, [C.POINTER(TransportSettings)]),
     "psgb_solve_implicit_transport": (C.c_int, [P, C.c_double, P, TransportResponse, P, C.POINTER(TransportSettings),
                                                 C.POINTER(SolveOptions), P, P, P, C.POINTER(TransportResult)]),
+    "psgb_solve_implicit_transport_device": (C.c_int, [P, C.c_double, P, P, P, C.POINTER(TransportSettings),
+                                                       C.POINTER(SolveOptions), P, P, P, C.POINTER(TransportResult),
+                                                       C.c_int, P]),
+    "psgb_quartic_device_response": (C.c_int, [P, C.c_uint64, P, P, P, P]),
     "psgb_column_radiation": (C.c_int, [C.c_uint32, C.c_uint32, C.POINTER(ColumnConstants), P, P, P, P, P, P, P,
                                         P, P, P, C.c_int, P]),
     "psgb_substep_mean_insolation": (C.c_int, [P, C.c_int64, P]),

@@ -11,6 +11,30 @@
 #include <string>
 #include <vector>
 
+namespace psgb {
+
+// Page-locked host doubles (the Newton solve's copies of h, T and dT/dh).
+class PinnedDoubles {
+  public:
+    PinnedDoubles() = default;
+    PinnedDoubles(const PinnedDoubles&) = delete;
+    PinnedDoubles& operator=(const PinnedDoubles&) = delete;
+    ~PinnedDoubles() {
+        if (p_ != nullptr) cudaFreeHost(p_);
+    }
+    void reset(std::size_t count) {
+        if (p_ != nullptr) cudaFreeHost(p_);
+        p_ = nullptr;
+        PSGB_CUDA(cudaMallocHost(reinterpret_cast<void**>(&p_), count * sizeof(double)));
+    }
+    double* data() const { return p_; }
+
+  private:
+    double* p_ = nullptr;
+};
+
+}  // namespace psgb
+
 struct psgb_planet {
     std::unique_ptr<psgb::Planet> planet;
     // lazily created device staging for host-memory calls
@@ -18,6 +42,10 @@ struct psgb_planet {
     std::vector<double*> stage;
     std::size_t stage_len = 0;
     std::uint64_t serial = 0;   // unique per planet for the life of the process
+    // the implicit transport solve's device vectors and pinned host copies
+    psgb::DeviceStore newton_store;
+    std::vector<double*> newton;
+    psgb::PinnedDoubles newton_pinned;
 };
 
 struct psgb_batch {

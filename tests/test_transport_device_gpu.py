@@ -1,0 +1,119 @@
+"""The implicit transport solve with the response on the GPU (the whole Newton iteration in
+device memory), against the reference's own solves (golden vectors from the reference,
+tests/golden/make_golden.py):
+
+- the quartic response kernel reproduces the reference's roots and slopes bit for bit
+  (solve_column_surface's Newton without FMA, the reference test's hold rule);
+- the solve with that response meets the reference test's gates and matches the
+  reference's solve to 1e-5 K / 1e-3 W/m^2 (both stop at 1e-6 W/m^2), for the test's
+  four cases, in FP64 and with the FP32 inner solve;
+- on an agglomerated L5 planet with the response per fine cell and group means on the
+  GPU, it matches the reference's production-pattern solve to the same bars;
+- a device callback (torch on the device pointers) gives the same bits as the same
+  response through the host callback."""
+import numpy as np
+import pytest
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+SETTINGS = {"cg_relative_tolerance": 1e-6, "newton_tolerance_W_m2": 1e-6}
+
+
+def test_quartic_kernel_bit_identical_to_the_reference():
+    import planet_game_gb300 as pg
+
+    g = golden("newton_quartic_L4.npz")
+    for case in (0, 1):
+        q = pg.QuarticResponse(float(g[f"a{case}"]), g[f"b{case}"])
+        mean, slope = pg.quartic_response(q, g[f"probe_source{case}"])
+        assert np.array_equal(mean.cpu().numpy(), g[f"probe_mean{case}"])
+        assert np.array_equal(slope.cpu().numpy(), g[f"probe_slope{case}"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("case,factor", [(0, 1), (0, 10), (1, 1), (1, 10)])
+def test_device_quartic_solve_matches_the_reference(meshes, case, factor, precision):
+    import planet_game_gb300 as pg
+
+    g = golden("newton_quartic_L4.npz")
+    key = f"{case}_{factor}"
+    m = meshes(4)
+    q = pg.QuarticResponse(float(g[f"a{case}"]), g[f"b{case}"])
+    r = pg.solve_implicit_transport(m, float(g[f"K{key}"]), g[f"floor{key}"], q, settings=SETTINGS,
+                                    precision=precision)
+    assert r.consistency_residual_W_m2 <= 1e-6
+    assert abs(r.sum_W) <= 1e-13 * r.absolute_sum_W and r.dissipation_W_K <= 0.0
+    assert np.all(r.mean_K[::7] <= 273.15)
+    assert np.max(np.abs(r.mean_K - g[f"mean{key}"])) <= 1e-5
+    assert np.max(np.abs(r.source_W_m2 - g[f"source{key}"])) <= 1e-3
+    assert abs(r.newton_iterations - g[f"stats{key}"][0]) <= 2
+
+
+@pytest.mark.parametrize("factor", [1, 10])
+def test_device_fine_response_on_the_agglomerated_graph(factor):
+    import torch
+
+    import planet_game_gb300 as pg
+
+    g = golden("agglomeration.npz")
+    p = pg.agglomerated_transport_graph(5, 6.371e6)
+    q = pg.QuarticResponse(float(g["qa"]), g["qb"], fine=True)
+    floor = torch.as_tensor(g[f"qfloor{factor}"], device="cuda")
+    r = pg.solve_implicit_transport(p, float(g[f"qK{factor}"]), floor, q, settings=SETTINGS, precision="mixed")
+    mean, source = r.mean_K.cpu().numpy(), r.source_W_m2.cpu().numpy()
+    assert r.consistency_residual_W_m2 <= 1e-6
+    assert abs(r.sum_W) <= 1e-13 * r.absolute_sum_W and r.dissipation_W_K <= 0.0
+    assert np.max(np.abs(mean - g[f"qmean{factor}"])) <= 1e-5
+    assert np.max(np.abs(source - g[f"qsource{factor}"])) <= 1e-3
+
+
+class _DeviceArray:
+    """A raw device pointer as a CUDA array (for torch.as_tensor, no copy)."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr, False), "version": 3,
+                                         "stream": None}
+
+
+def test_device_callback_equals_host_callback(meshes):
+    import torch
+
+    import planet_game_gb300 as pg
+
+    g = golden("newton_L4.npz")
+    m = meshes(4)
+    base, slope = g["base"], g["slope"]
+    floor = np.full(m.cell_count, -np.inf)
+    host = pg.solve_implicit_transport(m, float(g["conductance"]), floor,
+                                       lambda h: (base + slope * h, slope.copy()), settings=SETTINGS)
+    base_d, slope_d = torch.as_tensor(base, device="cuda"), torch.as_tensor(slope, device="cuda")
+    calls = []
+
+    def response(cells, source, mean, slope_out, stream):
+        calls.append(cells)
+        h = torch.as_tensor(_DeviceArray(source, cells), device="cuda")
+        torch.as_tensor(_DeviceArray(mean, cells), device="cuda").copy_(base_d + slope_d * h)
+        torch.as_tensor(_DeviceArray(slope_out, cells), device="cuda").copy_(slope_d)
+
+    dev = pg.solve_implicit_transport(m, float(g["conductance"]), floor, response, settings=SETTINGS, device=True)
+    assert calls and all(c == m.cell_count for c in calls)
+    assert dev.newton_iterations == host.newton_iterations
+    assert np.array_equal(dev.mean_K, host.mean_K) and np.array_equal(dev.source_W_m2, host.source_W_m2)
+
+
+def test_device_callback_errors_reach_the_caller(meshes):
+    import planet_game_gb300 as pg
+
+    class Boom(RuntimeError):
+        pass
+
+    def failing(*_):
+        raise Boom("tile solve failed")
+
+    m = meshes(4)
+    with pytest.raises(Boom):
+        pg.solve_implicit_transport(m, 1e12, np.zeros(m.cell_count), failing, device=True)
+    with pytest.raises(ValueError):
+        pg.solve_implicit_transport(m, 1e12, np.zeros(m.cell_count), pg.QuarticResponse(0.41, np.ones(5)))
