@@ -342,6 +342,86 @@ typedef struct psgb_quartic_response {
 int psgb_quartic_device_response(void* user, uint64_t cells, const double* source_W_m2, double* mean_K,
                                  double* slope_K_m2_W, void* stream);
 
+/* ---- non-symmetric solves: heat_transport.hpp:140-238, incomplete_lu.hpp:14-43 ---- */
+
+/* IncompleteLU (incomplete_lu.hpp:14-43): block ILU(0) of diagonal * scale + off on a
+ * CSR pattern (row i's off-diagonal columns neighbour[offset[i] .. offset[i + 1])),
+ * blocks of rows [block_start[b], block_start[b + 1]) factored on their own. HOST arrays;
+ * factored on the GPU at creation, level-scheduled inside each block, bit-identical to
+ * the reference's factor. PSGB_ERR_BREAKDOWN on a zero pivot (the reference's
+ * std::runtime_error). */
+typedef struct psgb_incomplete_lu psgb_incomplete_lu;
+int psgb_incomplete_lu_create(uint32_t rows, const uint32_t* offset, const uint32_t* neighbour,
+                              const double* diagonal, const double* off, const uint32_t* block_start,
+                              uint32_t blocks, double diagonal_scale, psgb_incomplete_lu** out);
+/* IncompleteLU::solve: x <- (LU)^-1 x. */
+int psgb_incomplete_lu_solve(psgb_incomplete_lu* lu, double* x, int memory, void* stream);
+void psgb_incomplete_lu_destroy(psgb_incomplete_lu* lu);
+
+/* AdvectionDiffusion (heat_transport.hpp:140-166): per CSR entry of the planet's graph
+ * the eddies' conductance G (W/K, symmetric) and per layer the mass leaving across the
+ * face (kg/s, layer-major, antisymmetric); c_p; per node the eddies' latent heat E
+ * (W/m^2) or NULL. Arrays HOST or DEVICE with the call's `memory`. */
+typedef struct psgb_advection_diffusion {
+    uint32_t layers;
+    const double* conductance_W_K;
+    const double* outflow_kg_s;
+    double heat_capacity_J_kg_K;      /* 1004.64 */
+    const double* eddy_latent_W_m2;
+} psgb_advection_diffusion;
+
+/* advection_diffusion_source (heat_transport.hpp:168-175): H_eddy and H_advective per
+ * node for given theta_c and s_l (layer-major); bit-identical. */
+int psgb_advection_diffusion_source(psgb_planet* planet, const psgb_advection_diffusion* transport,
+                                    const double* mean_K, const double* energy_J_kg, double* eddy_W_m2,
+                                    double* advective_W_m2, int memory, void* stream);
+
+/* solve_implicit_tracer (heat_transport.hpp:198-238): the layers' mixing ratios
+ * (layer-major, layers x nodes) carried implicitly by the advective fluxes (upwind), the
+ * eddies and the vertical fluxes that close each layer's divergence; BiCGSTAB with the
+ * stacked system's block ILU(0) on the GPU; the flux form of the solution. */
+typedef struct psgb_tracer_result {
+    int iterations;
+    double relative_residual;
+    double clipped_kg;
+    double column_divergence_kg_s;
+} psgb_tracer_result;
+int psgb_solve_implicit_tracer(psgb_planet* planet, const psgb_advection_diffusion* transport,
+                               const double* layer_mass_kg, const double* tracer, double dt_s,
+                               double relative_tolerance, int max_iterations, double* tracer_out,
+                               psgb_tracer_result* result, int memory, void* stream);
+
+/* solve_implicit_advection_diffusion (heat_transport.hpp:240-248): Newton on h with
+ * h = H(theta_c(h), s(h)), the line search of the implicit transport solve; the Newton
+ * system J = I - dH/dh on the graph's pattern solved by BiCGSTAB preconditioned with the
+ * V-cycle of the eddies' symmetric part, then the block ILU(0) of J on what is left.
+ * The response (AdvectionResponse, heat_transport.hpp:170-173) gives theta_c, its slope,
+ * and per layer s_l and ds_l/dh (layer-major): on the host (HOST arrays) or on the GPU
+ * (DEVICE arrays, enqueued on `stream`); give exactly one. `initial_source_W_m2` (may be
+ * NULL) starts the iteration (ImplicitTransportSettings::initial_source_W_m2). */
+typedef int (*psgb_advection_response)(void* user, uint64_t nodes, uint32_t layers, const double* source_W_m2,
+                                       double* mean_K, double* slope_K_m2_W, double* energy_J_kg,
+                                       double* energy_slope_J_kg_m2_W);
+typedef int (*psgb_device_advection_response)(void* user, uint64_t nodes, uint32_t layers,
+                                              const double* source_W_m2, double* mean_K, double* slope_K_m2_W,
+                                              double* energy_J_kg, double* energy_slope_J_kg_m2_W, void* stream);
+typedef struct psgb_advection_result {
+    double consistency_residual_W_m2;
+    int newton_iterations;
+    int linear_iterations;
+    double sum_W;
+    double absolute_sum_W;
+    double eddy_absolute_sum_W;
+    double advective_absolute_sum_W;
+} psgb_advection_result;
+int psgb_solve_implicit_advection_diffusion(psgb_planet* planet, const psgb_advection_diffusion* transport,
+                                            const double* source_floor_W_m2, const double* initial_source_W_m2,
+                                            psgb_advection_response host_response,
+                                            psgb_device_advection_response device_response, void* user,
+                                            const psgb_transport_settings* settings, double* source_out_W_m2,
+                                            double* mean_out_K, double* energy_out_J_kg,
+                                            psgb_advection_result* result, int memory, void* stream);
+
 /* Stores per-edge conductances with a batch (HOST arrays, one per planet, [edges] W/K;
  * NULL entries clear a planet's): steps whose params set edge_conductance_stored use them
  * without passing (and without the library comparing) the arrays on every call. */

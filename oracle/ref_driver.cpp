@@ -14,6 +14,7 @@
 
 #include "sim/planet/surface/heat_transport.cpp"
 
+#include "sim/core/math/incomplete_lu.hpp"
 #include "sim/planet/atmosphere/atmosphere.hpp"
 #include "sim/planet/atmosphere/atmosphere_column.hpp"
 #include "sim/planet/atmosphere/saturation.hpp"
@@ -456,6 +457,125 @@ void refd_solve_quartic_agglomerated(void* handle, double a, double conductance,
     stats[3] = result.sum_W;
     stats[4] = result.absolute_sum_W;
     stats[5] = result.dissipation_W_K;
+}
+
+// ---- non-symmetric solves (heat_transport.cpp:774-1318, incomplete_lu.cpp) --------
+namespace {
+
+const TransportGraph& graph_of(void* handle, int agglomerated, TransportGraph& own) {
+    const auto& mesh = *static_cast<PlanetMesh*>(handle);
+    if (agglomerated != 0) {
+        const std::vector<std::size_t>* groups = nullptr;
+        return agglomerated_transport_graph(mesh, groups);
+    }
+    own = mesh_transport_graph(mesh);
+    return own;
+}
+
+AdvectionDiffusion transport_of(const TransportGraph& graph, std::uint64_t layers, const double* conductance,
+                                const double* outflow, const double* latent, double heat_capacity) {
+    AdvectionDiffusion t;
+    t.layers = layers;
+    t.conductance_W_K.assign(conductance, conductance + graph.neighbour.size());
+    t.outflow_kg_s.assign(outflow, outflow + layers * graph.neighbour.size());
+    t.heat_capacity_J_kg_K = heat_capacity;
+    if (latent != nullptr) t.eddy_latent_W_m2.assign(latent, latent + graph.size());
+    return t;
+}
+
+}  // namespace
+
+// IncompleteLU with blocks, then solve(x) in place.
+void refd_incomplete_lu(std::uint64_t rows, const std::uint64_t* offset, const std::uint64_t* neighbour,
+                        const double* diagonal, const double* off, const std::uint64_t* block_start,
+                        std::uint64_t blocks, double scale, double* x) {
+    std::vector<std::size_t> o(offset, offset + rows + 1), nb(neighbour, neighbour + offset[rows]),
+        bs(block_start, block_start + blocks + 1);
+    const IncompleteLU lu(o, nb, std::vector<double>(diagonal, diagonal + rows),
+                          std::vector<double>(off, off + offset[rows]), bs, scale, 1U);
+    std::vector<double> v(x, x + rows);
+    lu.solve(v);
+    std::copy(v.begin(), v.end(), x);
+}
+
+void refd_advection_source(void* handle, int agglomerated, std::uint64_t layers, const double* conductance,
+                           const double* outflow, const double* latent, double heat_capacity, const double* mean,
+                           const double* energy, double* eddy_out, double* advective_out) {
+    TransportGraph own;
+    const TransportGraph& graph = graph_of(handle, agglomerated, own);
+    const auto t = transport_of(graph, layers, conductance, outflow, latent, heat_capacity);
+    Field2D<double> m(copy_in(mean, graph.size())), eddy, advective;
+    advection_diffusion_source(graph, t, m, copy_in(energy, layers * graph.size()), eddy, advective);
+    std::copy(eddy.values().begin(), eddy.values().end(), eddy_out);
+    std::copy(advective.values().begin(), advective.values().end(), advective_out);
+}
+
+// solve_implicit_tracer; stats: iterations, relative residual, clipped, column divergence.
+void refd_tracer(void* handle, int agglomerated, std::uint64_t layers, const double* conductance,
+                 const double* outflow, double heat_capacity, const double* mass, const double* tracer, double dt,
+                 double tolerance, std::uint64_t workers, double* tracer_out, double* stats) {
+    TransportGraph own;
+    const TransportGraph& graph = graph_of(handle, agglomerated, own);
+    const auto t = transport_of(graph, layers, conductance, outflow, nullptr, heat_capacity);
+    const auto r = solve_implicit_tracer(graph, t, std::span<const double>(mass, graph.size()),
+                                         copy_in(tracer, layers * graph.size()), dt, tolerance, 2'000,
+                                         static_cast<std::size_t>(workers));
+    std::copy(r.tracer.begin(), r.tracer.end(), tracer_out);
+    stats[0] = r.iterations;
+    stats[1] = r.relative_residual;
+    stats[2] = r.clipped_kg;
+    stats[3] = r.column_divergence_kg_s;
+}
+
+// solve_implicit_advection_diffusion with the column of test_advection_diffusion.cpp:
+// a x + r x^4 = b + h (solve_column_surface), s_l = c_p x (1 + eps_l) + phi_l. Stats:
+// newton, linear iterations, consistency, sum, absolute, eddy absolute, advective absolute.
+void refd_advection_solve(void* handle, int agglomerated, std::uint64_t layers, const double* conductance,
+                          const double* outflow, const double* latent, double heat_capacity, double a,
+                          const double* b, const double* epsilon, const double* geopotential, const double* floor,
+                          double cg_tolerance, double newton_tolerance, std::uint64_t workers, double* source_out,
+                          double* mean_out, double* energy_out, double* stats) {
+    TransportGraph own;
+    const TransportGraph& graph = graph_of(handle, agglomerated, own);
+    const auto t = transport_of(graph, layers, conductance, outflow, latent, heat_capacity);
+    const std::size_t nodes = graph.size();
+    const double radiative = 0.75 * 0.97 * stefan_boltzmann_W_m2_K4;
+    const AdvectionResponse column = [&](const Field2D<double>& source, Field2D<double>& mean,
+                                         Field2D<double>& slope, std::vector<double>& energy,
+                                         std::vector<double>& energy_slope) {
+        mean = Field2D<double>(nodes, 0.0);
+        slope = Field2D<double>(nodes, 0.0);
+        energy.assign(layers * nodes, 0.0);
+        energy_slope.assign(layers * nodes, 0.0);
+        for (std::size_t i = 0; i < nodes; ++i) {
+            ColumnSystem system;
+            system.a = a;
+            system.b = b[i] + source[i];
+            system.radiative = radiative;
+            const double x = solve_column_surface(system);
+            mean[i] = x;
+            slope[i] = system.slope_K_m2_W(x);
+            for (std::size_t l = 0; l < layers; ++l) {
+                energy[l * nodes + i] = heat_capacity * x * (1.0 + epsilon[l]) + geopotential[l];
+                energy_slope[l * nodes + i] = heat_capacity * slope[i] * (1.0 + epsilon[l]);
+            }
+        }
+    };
+    ImplicitTransportSettings settings;
+    settings.cg_relative_tolerance = cg_tolerance;
+    settings.newton_tolerance_W_m2 = newton_tolerance;
+    const auto r = solve_implicit_advection_diffusion(graph, t, Field2D<double>(copy_in(floor, nodes)), column,
+                                                      settings, static_cast<std::size_t>(workers));
+    std::copy(r.source_W_m2.values().begin(), r.source_W_m2.values().end(), source_out);
+    std::copy(r.mean_K.values().begin(), r.mean_K.values().end(), mean_out);
+    std::copy(r.energy_J_kg.begin(), r.energy_J_kg.end(), energy_out);
+    stats[0] = r.newton_iterations;
+    stats[1] = r.linear_iterations;
+    stats[2] = r.consistency_residual_W_m2;
+    stats[3] = r.sum_W;
+    stats[4] = r.absolute_sum_W;
+    stats[5] = r.eddy_absolute_sum_W;
+    stats[6] = r.advective_absolute_sum_W;
 }
 
 // ---- the assembled SPD system by the reference's own PCG + SGS V-cycle ------

@@ -29,3 +29,10 @@ from .api import (  # noqa: F401
     transport_step,
 )
 from .capi import GB300Error  # noqa: F401
+from .nonsym import (  # noqa: F401
+    AdvectionDiffusion,
+    IncompleteLU,
+    advection_diffusion_source,
+    solve_implicit_advection_diffusion,
+    solve_implicit_tracer,
+)

@@ -80,6 +80,29 @@ TransportResponse = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint64, C.POINTER(C.c_d
 DeviceResponse = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p)
 
 
+class AdvectionDiffusion(C.Structure):
+    _fields_ = [("layers", C.c_uint32), ("conductance_W_K", C.c_void_p), ("outflow_kg_s", C.c_void_p),
+                ("heat_capacity_J_kg_K", C.c_double), ("eddy_latent_W_m2", C.c_void_p)]
+
+
+class TracerResult(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("relative_residual", C.c_double), ("clipped_kg", C.c_double),
+                ("column_divergence_kg_s", C.c_double)]
+
+
+class AdvectionResult(C.Structure):
+    _fields_ = [("consistency_residual_W_m2", C.c_double), ("newton_iterations", C.c_int),
+                ("linear_iterations", C.c_int), ("sum_W", C.c_double), ("absolute_sum_W", C.c_double),
+                ("eddy_absolute_sum_W", C.c_double), ("advective_absolute_sum_W", C.c_double)]
+
+
+# psgb_advection_response (host arrays) and psgb_device_advection_response (device pointers)
+AdvectionResponse = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint64, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                C.c_void_p, C.c_void_p)
+DeviceAdvectionResponse = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint64, C.c_uint32, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p)
+
+
 class QuarticResponse(C.Structure):
     _fields_ = [("a", C.c_double), ("radiative", C.c_double), ("b", C.c_void_p), ("hold_stride", C.c_uint32),
                 ("hold_K", C.c_double), ("planet", C.c_void_p), ("scratch", C.c_void_p)]
@@ -164,6 +187,15 @@ _SIGNATURES = {
                                                        C.POINTER(SolveOptions), P, P, P, C.POINTER(TransportResult),
                                                        C.c_int, P]),
     "psgb_quartic_device_response": (C.c_int, [P, C.c_uint64, P, P, P, P]),
+    "psgb_incomplete_lu_create": (C.c_int, [C.c_uint32, P, P, P, P, P, C.c_uint32, C.c_double, C.POINTER(P)]),
+    "psgb_incomplete_lu_solve": (C.c_int, [P, P, C.c_int, P]),
+    "psgb_incomplete_lu_destroy": (None, [P]),
+    "psgb_advection_diffusion_source": (C.c_int, [P, C.POINTER(AdvectionDiffusion), P, P, P, P, C.c_int, P]),
+    "psgb_solve_implicit_tracer": (C.c_int, [P, C.POINTER(AdvectionDiffusion), P, P, C.c_double, C.c_double, C.c_int,
+                                             P, C.POINTER(TracerResult), C.c_int, P]),
+    "psgb_solve_implicit_advection_diffusion": (C.c_int, [P, C.POINTER(AdvectionDiffusion), P, P, P, P, P,
+                                                          C.POINTER(TransportSettings), P, P, P,
+                                                          C.POINTER(AdvectionResult), C.c_int, P]),
     "psgb_column_radiation": (C.c_int, [C.c_uint32, C.c_uint32, C.POINTER(ColumnConstants), P, P, P, P, P, P, P,
                                         P, P, P, C.c_int, P]),
     "psgb_substep_mean_insolation": (C.c_int, [P, C.c_int64, P]),

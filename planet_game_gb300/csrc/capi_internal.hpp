@@ -13,6 +13,13 @@
 
 namespace psgb {
 
+struct NonsymContext;   // the non-symmetric solves' per-planet structures (nonsym.cu)
+
+// A numerical breakdown reported as PSGB_ERR_BREAKDOWN (a zero ILU pivot).
+struct Breakdown : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
 // Page-locked host doubles (the Newton solve's copies of h, T and dT/dh).
 class PinnedDoubles {
   public:
@@ -46,6 +53,7 @@ struct psgb_planet {
     psgb::DeviceStore newton_store;
     std::vector<double*> newton;
     psgb::PinnedDoubles newton_pinned;
+    std::shared_ptr<psgb::NonsymContext> nonsym;
 };
 
 struct psgb_batch {
@@ -65,6 +73,8 @@ int guarded(F&& body) {
         return body();
     } catch (const std::invalid_argument& e) {
         return fail(PSGB_ERR_INVALID_ARGUMENT, e.what());
+    } catch (const psgb::Breakdown& e) {
+        return fail(PSGB_ERR_BREAKDOWN, e.what());
     } catch (const std::bad_alloc& e) {
         return fail(PSGB_ERR_OUT_OF_MEMORY, e.what());
     } catch (const psgb::CudaError& e) {

@@ -62,6 +62,13 @@ def load(reference: Path) -> C.CDLL:
     R.refd_solve_quartic.argtypes = [P, C.c_double, C.c_double, P, C.c_double, C.c_double, C.c_uint64, P, P, P, P]
     R.refd_agglomeration_counts.argtypes = [P, P]
     R.refd_agglomeration.argtypes = [P, P, P, P, P, P, P]
+    R.refd_graph.argtypes = [P, P, P, P, P, P]
+    R.refd_incomplete_lu.argtypes = [C.c_uint64, P, P, P, P, P, C.c_uint64, C.c_double, P]
+    R.refd_advection_source.argtypes = [P, C.c_int, C.c_uint64, P, P, P, C.c_double, P, P, P, P]
+    R.refd_tracer.argtypes = [P, C.c_int, C.c_uint64, P, P, C.c_double, P, P, C.c_double, C.c_double, C.c_uint64,
+                              P, P]
+    R.refd_advection_solve.argtypes = [P, C.c_int, C.c_uint64, P, P, P, C.c_double, C.c_double, P, P, P, P,
+                                       C.c_double, C.c_double, C.c_uint64, P, P, P, P]
     R.refd_solve_quartic_agglomerated.argtypes = [P, C.c_double, C.c_double, P, C.c_double, C.c_double, C.c_uint64,
                                                   P, P, P, P]
     return R
@@ -107,6 +114,174 @@ def agglomeration_cases(R) -> None:
                     f"qstats{factor}": stats})
     R.refd_mesh_free(m)
     np.savez_compressed(HERE / "agglomeration.npz", levels=np.array(AGGLOMERATION_LEVELS), **out)
+
+
+def ref_graph(R, m, agglomerated: bool) -> dict:
+    """The reference's transport graph of mesh handle `m` (its own, or its agglomeration)."""
+    if agglomerated:
+        counts = np.zeros(3, dtype=np.uint64)
+        R.refd_agglomeration_counts(m, p(counts))
+        n, d, f = (int(c) for c in counts)
+    else:
+        cnt = np.zeros(4, np.uint64)
+        R.refd_mesh_counts(m, p(cnt))
+        n, d = int(cnt[0]), int(cnt[2])
+    area, wsum = np.empty(n), np.empty(n)
+    off, nb, w = np.empty(n + 1, dtype=np.uint64), np.empty(d, dtype=np.uint64), np.empty(d)
+    if agglomerated:
+        groups = np.empty(f, dtype=np.uint64)
+        R.refd_agglomeration(m, p(area), p(off), p(nb), p(w), p(wsum), p(groups))
+    else:
+        R.refd_graph(m, p(area), p(off), p(nb), p(w), p(wsum))
+    return {"area": area, "offset": off, "neighbour": nb, "weight": w}
+
+
+def reverse_entries(g: dict) -> np.ndarray:
+    off, nb = g["offset"], g["neighbour"]
+    rev = np.empty(len(nb), dtype=np.int64)
+    for a in range(len(off) - 1):
+        for k in range(off[a], off[a + 1]):
+            b = nb[k]
+            row = nb[off[b]:off[b + 1]]
+            rev[k] = off[b] + int(np.nonzero(row == a)[0][0])
+    return rev
+
+
+def column_free_fluxes(g: dict, layers: int, scale: float, rng) -> np.ndarray:
+    """Antisymmetric layer fluxes summing to zero over each face's column (the bottom
+    layer's flux returns in the others), as test_advection_diffusion.cpp:47-70 builds."""
+    assert layers == 3
+    off, nb = g["offset"], g["neighbour"]
+    E = len(nb)
+    rev = reverse_entries(g)
+    out = np.zeros(layers * E)
+    for a in range(len(off) - 1):
+        for k in range(off[a], off[a + 1]):
+            if a < nb[k]:
+                f = scale * (2.0 * rng.random() - 1.0)
+                split = rng.random()
+                flux = [f, -split * f, -(1.0 - split) * f]
+                for l in range(layers):
+                    out[l * E + k] = flux[l]
+                    out[l * E + rev[k]] = -flux[l]
+    return out
+
+
+def noisy_fluxes(g: dict, layers: int, scale: float, divergent: bool, rng) -> np.ndarray:
+    """Antisymmetric per-face layer fluxes of about `scale`, with or without column
+    divergence (test_tracer_transport.cpp:33-60's construction, seeded numpy draws)."""
+    off, nb = g["offset"], g["neighbour"]
+    E = len(nb)
+    rev = reverse_entries(g)
+    out = np.zeros(layers * E)
+    for a in range(len(off) - 1):
+        for k in range(off[a], off[a + 1]):
+            if a < nb[k]:
+                flow = scale * (2.0 * rng.random(layers) - 1.0)
+                if not divergent:
+                    flow = flow - flow.mean()
+                for l in range(layers):
+                    out[l * E + k] = flow[l]
+                    out[l * E + rev[k]] = -flow[l]
+    return out
+
+
+NONSYM_CP = 1004.64
+
+
+def upper_entries(g: dict) -> np.ndarray:
+    """The CSR entries a -> b with a < b, in CSR order: one per face."""
+    off, nb = g["offset"], g["neighbour"]
+    rows = np.repeat(np.arange(len(off) - 1), np.diff(off.astype(np.int64)))
+    return np.nonzero(rows < nb.astype(np.int64))[0]
+
+
+def half_fluxes(g: dict, flows: np.ndarray, layers: int) -> np.ndarray:
+    """The antisymmetric flows on the faces' a < b entries only ([layers][faces])."""
+    E = len(g["neighbour"])
+    return flows.reshape(layers, E)[:, upper_entries(g)].copy()
+
+
+def nonsym_cases(R) -> None:
+    """The non-symmetric solves of the reference (heat_transport.cpp:774-1318) and its
+    block ILU(0) (incomplete_lu.cpp), on the L3 mesh graph, the L3 mesh's agglomerated
+    graph and the L4 mesh graph; inputs are seeded numpy draws shaped like the
+    reference's tests (test_tracer_transport.cpp, test_advection_diffusion.cpp)."""
+    rng = np.random.default_rng(20261204)
+    out = {}
+    m3 = P(R.refd_mesh_new(3, RADIUS))
+    g3, g3a = ref_graph(R, m3, False), ref_graph(R, m3, True)
+    # block ILU(0) on the L3 graph with a non-symmetric diagonally dominant matrix
+    n4 = len(g3["area"])
+    diag = 6.0 + 4.0 * rng.random(n4)
+    offv = -rng.random(len(g3["neighbour"]))
+    blocks = np.array(list(range(0, n4, 256)) + [n4], dtype=np.uint64)
+    x = rng.standard_normal(n4)
+    y = x.copy()
+    R.refd_incomplete_lu(n4, p(g3["offset"]), p(g3["neighbour"]), p(diag), p(offv), p(blocks), len(blocks) - 1, 1.0,
+                         p(y))
+    out.update(ilu_diag=diag, ilu_off=offv, ilu_blocks=blocks.astype(np.uint32), ilu_x=x, ilu_y=y)
+    # advection-diffusion source on the L3 graph
+    n3, L = len(g3["area"]), 3
+    K = 0.5 * RADIUS * RADIUS
+    cond = K * g3["weight"]
+    flux = column_free_fluxes(g3, L, 5.0e9, rng)   # also the coupled solves' fluxes, below
+    mean = 250.0 + 50.0 * rng.random(n3)
+    energy = 2.5e5 + 1.0e5 * rng.random(L * n3)
+    latent = rng.normal(0.0, 3.0, n3)
+    for tag, lat in (("dry", None), ("latent", latent)):
+        eddy, adv = np.empty(n3), np.empty(n3)
+        R.refd_advection_source(m3, 0, L, p(cond), p(flux), None if lat is None else p(lat), NONSYM_CP, p(mean),
+                                p(energy), p(eddy), p(adv))
+        out[f"src_eddy_{tag}"], out[f"src_adv_{tag}"] = eddy, adv
+    out.update(flux=half_fluxes(g3, flux, L), src_mean=mean, src_energy=energy, src_latent=latent)
+    # the tracer on the agglomerated L3 graph (3 layers) and the L4 graph (2 layers)
+    month = 2.63e6
+    for tag, (m, g, agg, layers, scale, eddy_g, divergent) in {
+            "bal": (m3, g3a, 1, 3, 2e9, 2e8, False), "div": (m3, g3a, 1, 3, 2e9, 2e8, True),
+            "eddy": (m3, g3a, 1, 2, 0.0, 1e13, False), "l3": (m3, g3, 0, 2, 5e9, 5e8, True)}.items():
+        n = len(g["area"])
+        E = len(g["neighbour"])
+        flows = noisy_fluxes(g, layers, scale, divergent, rng) if scale > 0 else np.zeros(layers * E)
+        conductance = np.full(E, eddy_g)
+        mass = g["area"] * 100000.0 / (9.81 * layers)
+        tracer = 0.01 * (1.0 + (2.0 * rng.random(layers * n) - 1.0)) + np.where(np.arange(layers * n) % 17 == 0, 0.0,
+                                                                               1e-6)
+        res, stats = np.empty(layers * n), np.empty(4)
+        R.refd_tracer(m, agg, layers, p(conductance), p(flows), NONSYM_CP, p(mass), p(tracer), month, 1e-12, 1,
+                      p(res), p(stats))
+        out.update({f"tr_{tag}_layers": layers, f"tr_{tag}_agg": agg, f"tr_{tag}_eddy": eddy_g,
+                    f"tr_{tag}_flux": half_fluxes(g, flows, layers), f"tr_{tag}_in": tracer, f"tr_{tag}_out": res,
+                    f"tr_{tag}_stats": stats})
+    # the coupled solve on the L3 graph: pure diffusion, advection, advection with latent heat
+    a = 3.0e5 / (30.0 * 86400.0)
+    radiative = 0.75 * 0.97 * 5.670374419e-8
+    target = 200.0 + 120.0 * rng.random(n3)
+    b = a * target + radiative * target ** 4
+    floor = a * 100.0 + radiative * 100.0 ** 4 - b
+    eps, phi = np.array([0.0, -0.08, -0.16]), np.array([3.0e4, 4.5e4, 7.0e4])
+    out.update(ad_a=a, ad_b=b, ad_floor=floor, ad_eps=eps, ad_phi=phi)
+    for tag, scale, with_latent in (("diff", 0.0, False), ("adv", 5.0e9, False), ("lat", 5.0e9, True)):
+        flows = flux if scale > 0 else np.zeros(L * len(g3["neighbour"]))
+        lat = None
+        if with_latent:
+            rnd = rng.random(n3)
+            lat = np.zeros(n3)
+            for i in range(n3):
+                water = 0.0
+                for k in range(g3["offset"][i], g3["offset"][i + 1]):
+                    j = g3["neighbour"][k]
+                    water += cond[k] / (NONSYM_CP * L) * 1e-3 * (rnd[j] - rnd[i])
+                lat[i] = 2.501e6 * water / g3["area"][i]
+        src, mn, en, stats = np.empty(n3), np.empty(n3), np.empty(L * n3), np.empty(7)
+        R.refd_advection_solve(m3, 0, L, p(cond), p(flows), None if lat is None else p(lat), NONSYM_CP, a, p(b),
+                               p(eps), p(phi), p(floor), 1e-6, 1e-6, 1, p(src), p(mn), p(en), p(stats))
+        out.update({f"ad_{tag}_source": src, f"ad_{tag}_mean": mn, f"ad_{tag}_energy": en,
+                    f"ad_{tag}_stats": stats})
+        if lat is not None:
+            out[f"ad_{tag}_latent"] = lat
+    R.refd_mesh_free(m3)
+    np.savez_compressed(HERE / "nonsym.npz", **out)
 
 
 def quartic_cases(R) -> None:
@@ -336,7 +511,11 @@ if __name__ == "__main__":
     elif "--agglomeration" in sys.argv:   # only the agglomerated-graph fixture
         agglomeration_cases(load(reference))
         print("agglomeration fixture written")
+    elif "--nonsym" in sys.argv:   # only the non-symmetric solves' fixture
+        nonsym_cases(load(reference))
+        print("nonsym fixture written")
     else:
         main(reference)
         quartic_cases(load(reference))
         agglomeration_cases(load(reference))
+        nonsym_cases(load(reference))
