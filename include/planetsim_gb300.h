@@ -494,6 +494,10 @@ int psgb_profile_end(double* total_ms, uint64_t* launches, uint64_t* swept_bytes
  * (compute_substep_mean_insolation, sim/planet/orbit/substep_forcing.cpp:102-127),
  * computed on the host; cells floats. */
 int psgb_substep_mean_insolation(const psgb_planet* planet, int64_t substep, float* out);
+/* The same on the GPU: the sub-step's 16 orbit nodes on the host, the per-cell
+ * quadrature in a kernel; `out` [cells] FP32, HOST or DEVICE per `memory`. Within one
+ * FP32 ulp of the reference (CUDA's acos/sin against the host library's). */
+int psgb_substep_mean_insolation_gpu(psgb_planet* planet, int64_t substep, float* out, int memory, void* stream);
 
 #ifdef __cplusplus
 }

@@ -175,6 +175,15 @@ class PlanetMesh:
             "target": _view(ptrs[3].value or 0, np.int64, nt) if nt else np.empty(0, np.int64),
         }
 
+    def substep_mean_insolation_gpu(self, substep: int = 0, out=None):
+        """The sub-step-mean insolation computed on the GPU (numpy out, or a float32
+        CUDA tensor `out` filled in place on the current stream)."""
+        if out is None:
+            out = np.empty(self.cell_count, dtype=np.float32)
+        mem, st = _memory_of(out)
+        _raise(capi.load().psgb_substep_mean_insolation_gpu(self._h, C.c_int64(substep), _ptr(out), mem, st))
+        return out
+
     def substep_mean_insolation(self, substep: int = 0) -> np.ndarray:
         out = np.empty(self.cell_count, dtype=np.float32)
         _raise(capi.load().psgb_substep_mean_insolation(self._h, C.c_int64(substep), _ptr(out)))

@@ -199,6 +199,7 @@ _SIGNATURES = {
     "psgb_column_radiation": (C.c_int, [C.c_uint32, C.c_uint32, C.POINTER(ColumnConstants), P, P, P, P, P, P, P,
                                         P, P, P, C.c_int, P]),
     "psgb_substep_mean_insolation": (C.c_int, [P, C.c_int64, P]),
+    "psgb_substep_mean_insolation_gpu": (C.c_int, [P, C.c_int64, P, C.c_int, P]),
     "psgb_launch_count": (C.c_uint64, []),
     "psgb_profile_begin": (C.c_int, [C.c_char_p]),
     "psgb_profile_end": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),

@@ -1003,6 +1003,24 @@ int psgb_profile_end(double* total_ms, uint64_t* launches, uint64_t* swept_bytes
     });
 }
 
+int psgb_substep_mean_insolation_gpu(psgb_planet* h, int64_t substep, float* out, int memory, void* stream) {
+    return guarded([&] {
+        require(h != nullptr && out != nullptr, "null argument");
+        require_memory(memory);
+        const psgb::DevMesh& d = device_mesh(h);
+        cudaStream_t st = as_stream(stream);
+        const psgb::InsolationNodes nodes = psgb::substep_forcing_nodes(substep);
+        float* o = memory == PSGB_MEMORY_DEVICE ? out : reinterpret_cast<float*>(stage(h, 0));
+        psgb::launch_substep_insolation(d, nodes, o, st);
+        PSGB_CUDA(cudaGetLastError());
+        if (memory == PSGB_MEMORY_HOST) {
+            PSGB_CUDA(cudaMemcpyAsync(out, o, std::size_t(d.n) * sizeof(float), cudaMemcpyDeviceToHost, st));
+            PSGB_CUDA(cudaStreamSynchronize(st));
+        }
+        return PSGB_OK;
+    });
+}
+
 int psgb_substep_mean_insolation(const psgb_planet* h, int64_t substep, float* out) {
     return guarded([&] {
         require(h != nullptr && out != nullptr, "null argument");

@@ -64,9 +64,7 @@ void gauss_legendre(std::array<double, 16>& x, std::array<double, 16>& w) {
     }
 }
 
-struct Node {
-    double weight, sin_dec, cos_dec, flux;
-};
+using Node = InsolationNode;
 
 Node orbit_at(const Orbit& o, double t, double weight) {
     const double mean = wrap(o.initial_orbital_phase_rad + kTwoPi * std::fmod(t, o.orbital_period_s) / o.orbital_period_s);
@@ -117,7 +115,7 @@ double daily_mean(double sl, double cl, double sd, double cd, double flux) {
 
 }  // namespace
 
-void substep_mean_insolation(const HostMesh& mesh, std::int64_t substep, float* out) {
+InsolationNodes substep_forcing_nodes(std::int64_t substep) {
     const Orbit o;
     const double per_year = 12.0;
     auto begin_tick = [&](std::int64_t k) {
@@ -129,14 +127,19 @@ void substep_mean_insolation(const HostMesh& mesh, std::int64_t substep, float* 
     const double span = t1 - t0;
     std::array<double, 16> gx{}, gw{};
     gauss_legendre(gx, gw);
-    std::array<Node, 16> nodes{};
-    for (int i = 0; i < 16; ++i) nodes[i] = orbit_at(o, t0 + 0.5 * span * (1.0 + gx[i]), 0.5 * gw[i]);
+    InsolationNodes nodes{};
+    for (int i = 0; i < 16; ++i) nodes.node[i] = orbit_at(o, t0 + 0.5 * span * (1.0 + gx[i]), 0.5 * gw[i]);
+    return nodes;
+}
+
+void substep_mean_insolation(const HostMesh& mesh, std::int64_t substep, float* out) {
+    const InsolationNodes nodes = substep_forcing_nodes(substep);
     for (std::size_t c = 0; c < mesh.cells; ++c) {
         const double x = mesh.center[3 * c], y = mesh.center[3 * c + 1], z = mesh.center[3 * c + 2];
         const double sl = z;
         const double cl = std::sqrt(x * x + y * y);
         double mean = 0.0;
-        for (const Node& n : nodes) mean += n.weight * daily_mean(sl, cl, n.sin_dec, n.cos_dec, n.flux);
+        for (const Node& n : nodes.node) mean += n.weight * daily_mean(sl, cl, n.sin_dec, n.cos_dec, n.flux);
         out[c] = static_cast<float>(mean);
     }
 }

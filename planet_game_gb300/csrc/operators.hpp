@@ -1,9 +1,13 @@
 // Host launchers of the finite-volume operator and transport-step kernels (operators.cu).
 #pragma once
 
+#include "host/insolation.hpp"
 #include "planet.hpp"
 
 namespace psgb {
+
+// Sub-step-mean insolation per cell (insolation.cu), FP32 out.
+void launch_substep_insolation(const DevMesh& m, const InsolationNodes& nodes, float* out, cudaStream_t st);
 
 template <typename T>
 void launch_laplacian(const DevMesh& m, const T* in, T* out, cudaStream_t st);

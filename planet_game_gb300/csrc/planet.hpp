@@ -108,6 +108,7 @@ struct DevMesh {
     double* graph_area = nullptr;      // [P] the transport graph's node areas (differ when agglomerated)
     double* gm = nullptr;              // [4][P] m_ee, m_en, m_nn, det of the LSQ gradient
     double* edge_length = nullptr;     // [E]
+    double* latitude = nullptr;        // [2][P] sin and cos of the cell centre's latitude
     // agglomerated planets: fine cells -> nodes
     std::uint32_t fine_cells = 0;
     std::uint32_t* group_of_cell = nullptr;   // [fine cells]

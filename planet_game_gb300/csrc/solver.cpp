@@ -16,6 +16,7 @@
 #include "profile.hpp"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <stdexcept>
 
@@ -147,6 +148,15 @@ void upload_planet(Planet& planet_ref) {
         d.fine_area = planet->store.upload(planet->fine_area_m2);
     }
     d.gm = planet->store.upload(gm);
+    {   // sin(lat) = z, cos(lat) = sqrt(x^2 + y^2) as the reference forms them
+        std::vector<double> latitude(2 * P, 0.0);
+        for (std::size_t c = 0; c < m.cells; ++c) {
+            const double x = m.center[3 * c], y = m.center[3 * c + 1];
+            latitude[c] = m.center[3 * c + 2];
+            latitude[P + c] = std::sqrt(x * x + y * y);
+        }
+        d.latitude = planet->store.upload(latitude);
+    }
     d.edge_length = planet->store.upload(m.edge_length_m);
     planet->uploaded = true;
 }

@@ -125,3 +125,29 @@ def test_device_pointer_path_matches_host_path(meshes):
     e, n = pg.gradient(m, f32)
     e_h, n_h = pg.gradient(m, phi.astype(np.float32))
     assert np.array_equal(e.cpu().numpy(), e_h) and np.array_equal(n.cpu().numpy(), n_h)
+
+
+@pytest.mark.parametrize("substep", [0, 5])
+def test_insolation_kernel_matches_the_reference(meshes, substep):
+    """The sub-step-mean insolation kernel: within one FP32 ulp of the reference at L4
+    (sub-step 0, golden) and of the host restatement (another sub-step); zero only where
+    the host's is."""
+    m = meshes(4)
+    gpu = m.substep_mean_insolation_gpu(substep)
+    host = m.substep_mean_insolation(substep)
+    ulp = np.spacing(np.abs(host).astype(np.float32))
+    assert np.all(np.abs(gpu - host) <= ulp)
+    assert np.array_equal(gpu == 0.0, host == 0.0)
+    if substep == 0:
+        ref = golden("insolation_L4.npz")["insolation"]
+        assert np.all(np.abs(gpu - ref) <= np.spacing(np.abs(ref).astype(np.float32)))
+
+
+def test_insolation_kernel_on_device_memory(meshes):
+    import torch
+
+    m = meshes(6)
+    out = torch.empty(m.cell_count, dtype=torch.float32, device="cuda")
+    m.substep_mean_insolation_gpu(3, out)
+    host = m.substep_mean_insolation(3)
+    assert np.all(np.abs(out.cpu().numpy() - host) <= np.spacing(np.abs(host).astype(np.float32)))
