@@ -506,7 +506,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=["batch", "l8", "serve"], default="batch")
-    ap.add_argument("--serve-rate", type=float, default=1000.0)
+    ap.add_argument("--serve-rate", type=float, default=5000.0)
     ap.add_argument("--serve-requests", type=int, default=2000)
     ap.add_argument("--skip-serve", action="store_true")
     ap.add_argument("--seed", type=int, default=2026)

@@ -445,6 +445,9 @@ typedef struct psgb_tuning {
     int coarse_tail_level;                /* levels from this one down run one block per planet; 0: none */
     int block_sweeps[PSGB_MAX_LEVELS];    /* per level: Jacobi sweeps per smoothing launch, each tile in shared
                                              memory with its neighbours in other tiles held (1..8; 1 = plain) */
+    int coarse_tail_single;               /* 0: a large planet's tail runs on several co-resident blocks
+                                             (cooperative launch, per-planet barriers); 1: one block each */
+    uint32_t coarse_tail_blocks;          /* out: blocks of the tail launch (0: no tail) */
 } psgb_tuning;
 
 /* Times trial solves of one sub-step (the inputs as for psgb_batch_transport_step, every

@@ -159,6 +159,10 @@ Tuning current_tuning(const Batch& b) {
     }
     t.omega = b.smoother.omega;
     t.tail_level = b.tail_level;
+    t.tail_spread = b.tail_spread;
+    t.tail_blocks = b.tail_level == 0 ? 0u
+                    : (b.tail_spread && b.tail_cta_at[b.tail_level] != nullptr) ? b.tail_ctas_at[b.tail_level]
+                                                                                 : b.instances;
     return t;
 }
 
@@ -187,6 +191,7 @@ void apply_tuning(Batch& b, const Tuning& t) {
     b.smoother.level_inner = t.inner;
     b.smoother.omega = t.omega;
     b.tail_level = t.tail_level;
+    b.tail_spread = t.tail_spread;
     b.tuned = true;
 }
 
@@ -258,13 +263,28 @@ Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x,
     }
     // block-local sweeps on the coarse levels: several Jacobi sweeps per launch
     if (depth > 1) {
-        const int block[][3] = {{2, 2, 2}, {2, 2, 3}, {2, 2, 4}, {3, 3, 2}, {3, 3, 3}};
+        // (pre launches + 1, post launches + 1, sweeps per launch): fewer, longer launches
+        // trade the latency of a launch against tile-local coupling
+        const int block[][3] = {{2, 2, 2}, {2, 2, 3}, {2, 2, 4}, {3, 3, 2}, {3, 3, 3},
+                                {2, 2, 6}, {2, 2, 8}, {2, 1, 6}, {2, 1, 8}};
         const Sweeps base = best;
         for (const auto& c : block) {
             Sweeps s = base;
             s.inner.assign(depth, 1);
             for (std::size_t l = 1; l < depth; ++l) { s.pre[l] = c[0]; s.post[l] = c[1]; s.inner[l] = c[2]; }
             consider(s);
+        }
+        // then the levels below the first coarse one on their own: the smallest levels
+        // are pure latency, fewer launches may beat more smoothing there
+        if (depth > 2 && !best.inner.empty()) {
+            const int deep[][3] = {{1, 1, 1}, {2, 1, 8}, {2, 2, 8}};
+            const Sweeps with_first = best;
+            for (const auto& c : deep) {
+                Sweeps s = with_first;
+                for (std::size_t l = 2; l < depth; ++l) { s.pre[l] = c[0]; s.post[l] = c[1]; s.inner[l] = c[2]; }
+                if (s.pre == with_first.pre && s.post == with_first.post && s.inner == with_first.inner) continue;
+                consider(s);
+            }
         }
     }
     // damping around the best
@@ -279,14 +299,20 @@ Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x,
     set_sweeps(b, best);
     {
         const int chosen = b.tail_level;
+        const bool chosen_spread = b.tail_spread;
         int pick = chosen;
+        bool pick_spread = chosen_spread;
         for (int tail = 0; tail < static_cast<int>(depth); ++tail) {
-            if (tail == chosen) continue;
-            b.tail_level = tail;
-            const double ms = run(best);
-            if (ms > 0.0 && ms < best_ms) { best_ms = ms; pick = tail; }
+            for (bool spread : {true, false}) {
+                if ((tail == chosen && spread == chosen_spread) || (tail == 0 && !spread)) continue;
+                b.tail_level = tail;
+                b.tail_spread = spread;
+                const double ms = run(best);
+                if (ms > 0.0 && ms < best_ms) { best_ms = ms; pick = tail; pick_spread = spread; }
+            }
         }
         b.tail_level = pick;
+        b.tail_spread = pick_spread;
     }
     if (best_ms < 0.0) {
         set_sweeps(b, before);
@@ -303,6 +329,7 @@ Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x,
         result.sets_vector.push_back(b.levels[l].sets_vector);
     }
     result.tail_level = b.tail_level;
+    result.tail_spread = b.tail_spread;
     result.tuned_ms = best_ms;
     return result;
 }

@@ -17,6 +17,8 @@ struct Tuning {
     std::vector<std::uint8_t> sets_vector;         // per level: 1 or 4
     double omega = 0.8;
     int tail_level = 0;                            // coarse tail from this level (0: none)
+    bool tail_spread = true;                       // several blocks per large planet in the tail
+    unsigned tail_blocks = 0;                      // blocks of the tail launch (out; 0: no tail)
     double tuned_ms = 0.0;                         // trial solve with the chosen settings
     double default_ms = 0.0;                       // trial solve with the settings before tuning
     int trials = 0;                                // trial solves timed

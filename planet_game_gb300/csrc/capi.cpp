@@ -831,6 +831,8 @@ void fill_tuning(const psgb::Tuning& t, psgb_tuning* out) {
     out->default_solve_ms = t.default_ms;
     out->trial_solves = t.trials;
     out->coarse_tail_level = t.tail_level;
+    out->coarse_tail_single = t.tail_spread ? 0 : 1;
+    out->coarse_tail_blocks = t.tail_blocks;
 }
 
 }  // namespace
@@ -918,6 +920,7 @@ int psgb_batch_set_tuning(psgb_batch* h, const psgb_tuning* tuning) {
         }
         t.omega = tuning->jacobi_omega;
         t.tail_level = tuning->coarse_tail_level;
+        t.tail_spread = tuning->coarse_tail_single == 0;
         psgb::apply_tuning(b, t);
         return PSGB_OK;
     });

@@ -1,12 +1,17 @@
-// The coarse tail of the V-cycle (see coarse_tail.hpp): one block of four 256-thread tile
-// groups per planet. The block walks its planet's tiles of each level (group g takes
-// tiles g, g + 4, ...), calls the shared per-tile phases, and meets at a block barrier
-// between phases; the dense coarsest solve uses the block's 32 warps, one row each.
+// The coarse tail of the V-cycle (see coarse_tail.hpp): blocks of four 256-thread tile
+// groups. A planet's groups walk its tiles of each level (group g of G takes tiles g,
+// g + G, ...), call the shared per-tile phases, and meet at a barrier between phases (a
+// block barrier, or with several blocks per planet a per-planet barrier in global
+// memory); the dense coarsest solve gives one row to each of the planet's warps.
 #define PSGB_PHASE_RESTRICT
 #include "coarse_tail.hpp"
 #include "phases.cuh"
+#include "planet.hpp"
 #include "profile.hpp"
 
+#include <algorithm>
+#include <stdexcept>
+#include <string>
 #include <type_traits>
 
 namespace psgb {
@@ -35,20 +40,82 @@ __device__ __forceinline__ TailPair<T> tail_pair(const TailArgs<T>& a, int l) {
     return a.starts_in_x[l] ? TailPair<T>{X, Y} : TailPair<T>{Y, X};
 }
 
-// The planet's tiles of level l, split over the block's four groups.
-#define PSGB_PLANET_TILES(a, l, inst, gid)                                                      \
-    for (int tile = static_cast<int>((a).tile_range[((l) * (a).instances + (inst)) * 2]) + (gid), \
-             tile_end = static_cast<int>((a).tile_range[((l) * (a).instances + (inst)) * 2] +    \
-                                         (a).tile_range[((l) * (a).instances + (inst)) * 2 + 1]); \
-         tile < tile_end; tile += ph::kGroups)
+// The planet's tiles of level l, split over its `groups` tile groups (this one: `group`).
+#define PSGB_PLANET_TILES(a, l, inst, group)                                                        \
+    for (int tile = static_cast<int>((a).tile_range[((l) * (a).instances + (inst)) * 2]) + (group),   \
+             tile_end = static_cast<int>((a).tile_range[((l) * (a).instances + (inst)) * 2] +        \
+                                         (a).tile_range[((l) * (a).instances + (inst)) * 2 + 1]);     \
+         tile < tile_end; tile += groups)
 
-template <typename T>
+constexpr unsigned long long kTailBarrierTimeoutNs = 2000000000ull;   // 2 s
+constexpr unsigned kTailSpinLimit = 1u << 26;
+
+__device__ __forceinline__ unsigned ld_volatile_u(const unsigned* p) { return *reinterpret_cast<const volatile unsigned*>(p); }
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// The `size` blocks of planet `inst` meet (sense by generation: the last to arrive resets
+// the count and advances the generation). Every wait is bounded; past its limit the
+// error flag is set and every block of the launch stops at its next barrier.
+__device__ bool planet_barrier(unsigned* barrier, unsigned* error, unsigned instances, int inst, int size) {
+    __shared__ int stop;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned* count = barrier + inst;
+        unsigned* gen = barrier + instances + inst;
+        const unsigned g = ld_volatile_u(gen);
+        __threadfence();
+        const unsigned arrived = atomicAdd(count, 1u);
+        if (arrived == static_cast<unsigned>(size) - 1u) {
+            atomicExch(count, 0u);
+            __threadfence();
+            atomicAdd(gen, 1u);
+        } else {
+            const unsigned long long start = global_ns();
+            unsigned spins = 0;
+            while (ld_volatile_u(gen) == g) {
+                if (ld_volatile_u(error) != 0u) break;
+                ++spins;
+                if (spins > kTailSpinLimit || ((spins & 1023u) == 0u && global_ns() - start > kTailBarrierTimeoutNs)) {
+                    atomicExch(error, 1u);
+                    break;
+                }
+                if (spins > 256u) __nanosleep(32);
+            }
+        }
+        __threadfence();
+        stop = ld_volatile_u(error) != 0u;
+    }
+    __syncthreads();
+    return stop == 0;
+}
+
+template <typename T, bool Multi>
 __global__ void __launch_bounds__(1024, 1) k_coarse_tail(const __grid_constant__ TailArgs<T> a) {
     pdl_begin();
-    const int inst = static_cast<int>(blockIdx.x);
+    int inst = static_cast<int>(blockIdx.x), rank = 0, size = 1;
+    if (Multi) {
+        const std::uint32_t w = a.cta[blockIdx.x];
+        inst = static_cast<int>(w & 0xFFFFu);
+        rank = static_cast<int>((w >> 16) & 0xFFu);
+        size = static_cast<int>(w >> 24);
+    }
     const int gid = static_cast<int>(threadIdx.x >> 8), lane = static_cast<int>(threadIdx.x & 255);
+    const int group = rank * ph::kGroups + gid, groups = size * ph::kGroups;
     const int coarsest = a.dense.level[inst];
     if (coarsest < a.first || !ph::gate_open(a.sc, inst, a.gate)) return;
+    // between phases: the block, or all of the planet's blocks
+#define PSGB_TAIL_SYNC()                                                                   \
+    do {                                                                                   \
+        if (Multi) {                                                                       \
+            if (!planet_barrier(a.barrier, a.error, a.instances, inst, size)) return;      \
+        } else {                                                                           \
+            __syncthreads();                                                               \
+        }                                                                                  \
+    } while (0)
     const T omega = a.omega;
     // Down: the level's remaining pre-sweeps (its first sweep came with the restriction
     // into it), residual, restriction fused with the next level's first sweep.
@@ -59,35 +126,35 @@ __global__ void __launch_bounds__(1024, 1) k_coarse_tail(const __grid_constant__
         for (int k = 1; k < a.pre[l]; ++k) {
             tail_widths(lv.width, [&](auto W) {
                 if (a.inner[l] > 1) {
-                    PSGB_PLANET_TILES(a, l, inst, gid)
+                    PSGB_PLANET_TILES(a, l, inst, group)
                         ph::smooth_block<T, decltype(W)::value>(lv, tile, gid, lane, L.b, p.first, p.second, omega,
                                                                 a.inner[l], a.sc, a.gate);
                 } else {
-                    PSGB_PLANET_TILES(a, l, inst, gid)
+                    PSGB_PLANET_TILES(a, l, inst, group)
                         ph::smooth<T, decltype(W)::value, 1>(lv, tile, lane, L.b, p.first, p.second, omega, a.sc, a.gate);
                 }
             });
-            __syncthreads();
+            PSGB_TAIL_SYNC();
             T* t = p.first; p.first = p.second; p.second = t;
         }
         tail_widths(lv.width, [&](auto W) {
-            PSGB_PLANET_TILES(a, l, inst, gid)
+            PSGB_PLANET_TILES(a, l, inst, group)
                 ph::residual<T, decltype(W)::value, 1>(lv, tile, lane, L.b, p.first, L.r, a.sc, a.gate);
         });
-        __syncthreads();
+        PSGB_TAIL_SYNC();
         const PersistentLevel<T>& C = a.level[l + 1];
         const TailPair<T> pc = tail_pair(a, l + 1);
-        PSGB_PLANET_TILES(a, l + 1, inst, gid)
+        PSGB_PLANET_TILES(a, l + 1, inst, group)
             ph::restrict_zero<T, 1>(C.view, tile, lane, L.member_offset, L.member, L.r, C.b, pc.first, omega, a.sc, a.gate);
-        __syncthreads();
+        PSGB_TAIL_SYNC();
     }
     // The planet's coarsest level: x = A^-1 b, one warp per row.
     {
         const int n = static_cast<int>(a.dense.size[inst]);
         const PersistentLevel<T>& L = a.level[coarsest];
-        for (int row = static_cast<int>(threadIdx.x >> 5); row < n; row += 32)
+        for (int row = rank * 32 + static_cast<int>(threadIdx.x >> 5); row < n; row += 32 * size)
             ph::dense_row<T>(a.dense, inst, row, static_cast<int>(threadIdx.x & 31), a.dense_inv, L.b, L.x);
-        __syncthreads();
+        PSGB_TAIL_SYNC();
     }
     // Up: prolongation fused with the first post-sweep, then the remaining post-sweeps.
     for (int l = coarsest - 1; l >= a.first; --l) {
@@ -97,39 +164,92 @@ __global__ void __launch_bounds__(1024, 1) k_coarse_tail(const __grid_constant__
         TailPair<T> p = tail_pair(a, l);
         if ((a.pre[l] - 1) & 1) { T* t = p.first; p.first = p.second; p.second = t; }   // where the down sweeps ended
         if (a.post[l] == 0) {
-            PSGB_PLANET_TILES(a, l, inst, gid) ph::prolong<T, 1>(lv, tile, lane, L.agg, e, p.first, a.sc, a.gate);
-            __syncthreads();
+            PSGB_PLANET_TILES(a, l, inst, group) ph::prolong<T, 1>(lv, tile, lane, L.agg, e, p.first, a.sc, a.gate);
+            PSGB_TAIL_SYNC();
             continue;
         }
         tail_widths(lv.width, [&](auto W) {
-            PSGB_PLANET_TILES(a, l, inst, gid)
+            PSGB_PLANET_TILES(a, l, inst, group)
                 ph::prolong_smooth<T, decltype(W)::value, 1>(lv, tile, lane, L.agg, e, L.b, p.first, p.second, omega, a.sc,
                                                              a.gate);
         });
-        __syncthreads();
+        PSGB_TAIL_SYNC();
         { T* t = p.first; p.first = p.second; p.second = t; }
         for (int k = 1; k < a.post[l]; ++k) {
             tail_widths(lv.width, [&](auto W) {
                 if (a.inner[l] > 1) {
-                    PSGB_PLANET_TILES(a, l, inst, gid)
+                    PSGB_PLANET_TILES(a, l, inst, group)
                         ph::smooth_block<T, decltype(W)::value>(lv, tile, gid, lane, L.b, p.first, p.second, omega,
                                                                 a.inner[l], a.sc, a.gate);
                 } else {
-                    PSGB_PLANET_TILES(a, l, inst, gid)
+                    PSGB_PLANET_TILES(a, l, inst, group)
                         ph::smooth<T, decltype(W)::value, 1>(lv, tile, lane, L.b, p.first, p.second, omega, a.sc, a.gate);
                 }
             });
-            __syncthreads();
+            PSGB_TAIL_SYNC();
             T* t = p.first; p.first = p.second; p.second = t;
         }
     }
+#undef PSGB_TAIL_SYNC
 }
 
 }  // namespace
 
+std::vector<std::uint32_t> tail_blocks(const std::vector<std::uint32_t>& rows, unsigned budget) {
+    const std::size_t I = rows.size();
+    std::vector<unsigned> size(I, 1);
+    if (I > 0xFFFFu) throw std::logic_error("coarse tail: too many planets for per-planet blocks");
+    unsigned used = static_cast<unsigned>(I);
+    while (used < budget) {
+        std::size_t best = I;
+        double most = 0.0;
+        for (std::size_t i = 0; i < I; ++i) {
+            const double per = static_cast<double>(rows[i]) / size[i];
+            if (size[i] < 16 && per > most) { most = per; best = i; }
+        }
+        if (best == I || most <= 2048.0) break;   // a block covers up to 2048 rows well
+        ++size[best];
+        ++used;
+    }
+    std::vector<std::uint32_t> cta;
+    for (std::size_t i = 0; i < I; ++i)
+        for (unsigned r = 0; r < size[i]; ++r) cta.push_back(static_cast<std::uint32_t>(i) | (r << 16) | (size[i] << 24));
+    return cta;
+}
+
+unsigned tail_block_budget() {
+    int device = 0, coop = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&device) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device) != cudaSuccess || coop == 0) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_coarse_tail<float, true>, 1024, 0) != cudaSuccess)
+        return 0;
+    int per_sm64 = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm64, k_coarse_tail<double, true>, 1024, 0) != cudaSuccess)
+        return 0;
+    return static_cast<unsigned>(sms * std::min(per_sm, per_sm64));
+}
+
 template <typename T>
 void launch_coarse_tail(const TailArgs<T>& args, cudaStream_t st) {
-    PSGB_LAUNCH(kFamSmoothCoarse, st, launch_pdl(k_coarse_tail<T>, args.instances, 1024, st, args));
+    if (args.cta == nullptr) {
+        PSGB_LAUNCH(kFamSmoothCoarse, st, launch_pdl(k_coarse_tail<T, false>, args.instances, 1024, st, args));
+        return;
+    }
+    // Cooperative: every block co-resident (checked by the runtime), no early start.
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(args.ctas);
+    cfg.blockDim = dim3(1024);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    PSGB_LAUNCH(kFamSmoothCoarse, st, {
+        const cudaError_t e = cudaLaunchKernelEx(&cfg, k_coarse_tail<T, true>, args);
+        if (e != cudaSuccess) throw std::runtime_error(std::string("coarse tail launch: ") + cudaGetErrorString(e));
+    });
 }
 
 template void launch_coarse_tail<float>(const TailArgs<float>&, cudaStream_t);

@@ -1,9 +1,11 @@
 // The coarse tail of the V-cycle: from a level down to every planet's coarsest level and
-// back up, one 1024-thread block per planet. Below the tail level every planet's level
-// holds a few thousand rows at most, where a launch per phase costs more than the phase:
-// the block runs all of its planet's sweeps, residuals, restrictions, the dense coarsest
-// solve and the prolongations with block barriers in between. Each phase is the same
-// per-tile code as the grid-wide V-cycle, so the result is identical.
+// back up. Below the tail level every planet's level holds few rows, where a launch per
+// phase costs more than the phase: the planet's blocks run all of its sweeps, residuals,
+// restrictions, the dense coarsest solve and the prolongations with barriers in between.
+// Either one 1024-thread block per planet (block barriers), or a cooperative launch in
+// which each planet owns 1 to 16 co-resident blocks in proportion to its rows at the tail
+// level, meeting at a per-planet barrier in global memory (bounded waits). Each phase is
+// the same per-tile code as the grid-wide V-cycle, so the result is identical.
 #pragma once
 
 #include "kernels.hpp"
@@ -12,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <vector>
 
 namespace psgb {
 
@@ -29,7 +32,20 @@ struct TailArgs {
     T omega;
     const InstanceScalars* sc;
     int gate;
+    // per-planet blocks (null: one block per planet)
+    const std::uint32_t* cta;   // per block: planet | rank << 16 | size << 24
+    unsigned ctas;
+    unsigned* barrier;          // [2][instances]: arrivals, generation
+    unsigned* error;            // set when a barrier wait runs past its limit
 };
+
+// Blocks per planet for a tail from `level`: `rows[i]` its rows there, `budget` blocks
+// that can be co-resident; each planet gets at least one, the rest go to the planet with
+// the most rows per block (at most 16 each). Returns the packed per-block words.
+std::vector<std::uint32_t> tail_blocks(const std::vector<std::uint32_t>& rows, unsigned budget);
+
+// Co-resident 1024-thread tail blocks on this device (0: no cooperative launch).
+unsigned tail_block_budget();
 
 template <typename T>
 void launch_coarse_tail(const TailArgs<T>& args, cudaStream_t st);

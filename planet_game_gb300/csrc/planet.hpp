@@ -217,6 +217,12 @@ struct Batch {
     // Levels from tail_level down run as one block per planet (coarse_tail.hpp); 0: none.
     int tail_level = 0;
     int default_tail_level = 0;
+    // Several co-resident blocks per large planet in the tail (cooperative launch): per
+    // tail level the packed per-block words and their count (null: one block per planet).
+    bool tail_spread = true;
+    std::vector<std::uint32_t*> tail_cta_at;
+    std::vector<unsigned> tail_ctas_at;
+    unsigned* tail_barrier = nullptr;  // [2][instances]
     std::uint32_t* tile_range = nullptr;   // [levels][instances][2]: first tile, tile count
     bool tuned = false;                // per-level settings from an autotune: the options' sweeps do not apply
     std::vector<std::int64_t> fine_base;      // fine-level row base per planet
@@ -240,7 +246,7 @@ struct Batch {
     unsigned* ticket = nullptr;        // [instances]
     std::uint32_t* tile_begin = nullptr;  // [instances + 1] fine-level tile ranges
     InstanceScalars* scalars = nullptr;   // [instances]
-    unsigned* sync = nullptr;          // [3] grid-barrier state of the persistent solve
+    unsigned* sync = nullptr;          // [4] grid-barrier state of the persistent solve; [3]: tail barrier error
     std::vector<InstanceScalars> host_scalars;
     InstanceScalars* pinned_scalars = nullptr;   // pinned host mirror
     bool matrix_ready = false;

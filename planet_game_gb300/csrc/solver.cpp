@@ -407,6 +407,26 @@ std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* ar
     PSGB_CUDA(cudaMemset(b.ticket, 0, I * sizeof(unsigned)));
     b.sync = b.store.alloc<unsigned>(4);
     PSGB_CUDA(cudaMemset(b.sync, 0, 4 * sizeof(unsigned)));
+    // The coarse tail's blocks per planet for every possible tail level, laid out now so
+    // that no allocation happens while a stream records (one block each where the
+    // device cannot hold every planet's blocks at once).
+    {
+        const unsigned budget = tail_block_budget();
+        b.tail_cta_at.assign(depth, nullptr);
+        b.tail_ctas_at.assign(depth, 0u);
+        for (std::size_t l = 1; l < depth && budget >= I; ++l) {
+            std::vector<std::uint32_t> rows(I, 0);
+            for (std::uint32_t i = 0; i < I; ++i)
+                if (b.levels[l].base[i] >= 0) rows[i] = b.levels[l].count[i];
+            const std::vector<std::uint32_t> cta = tail_blocks(rows, budget);
+            if (cta.size() > I) {
+                b.tail_cta_at[l] = b.store.upload(cta);
+                b.tail_ctas_at[l] = static_cast<unsigned>(cta.size());
+            }
+        }
+        b.tail_barrier = b.store.alloc<unsigned>(2 * std::size_t(I));
+        PSGB_CUDA(cudaMemset(b.tail_barrier, 0, 2 * std::size_t(I) * sizeof(unsigned)));
+    }
     b.tile_begin = b.store.upload(tile_begin);
     b.scalars = b.store.alloc<InstanceScalars>(I);
     PSGB_CUDA(cudaMemset(b.scalars, 0, I * sizeof(InstanceScalars)));
@@ -523,6 +543,13 @@ TailArgs<T> tail_args(Batch& b, int gate) {
     a.omega = static_cast<T>(b.smoother.omega);
     a.sc = b.scalars;
     a.gate = gate;
+    // Per-planet blocks in proportion to the planets' rows at the tail level.
+    if (b.tail_spread && b.tail_cta_at[b.tail_level] != nullptr) {
+        a.cta = b.tail_cta_at[b.tail_level];
+        a.ctas = b.tail_ctas_at[b.tail_level];
+        a.barrier = b.tail_barrier;
+        a.error = b.sync + 3;
+    }
     return a;
 }
 
@@ -654,6 +681,7 @@ std::vector<int> shape_of(const Batch& b) {
         shape.push_back(b.levels[l].sets_vector);
     }
     shape.push_back(b.tail_level);
+    shape.push_back(b.tail_spread ? 1 : 0);
     return shape;
 }
 
@@ -853,13 +881,20 @@ void solve(Batch& b, const SolveOptions& opt, const double* rhs, double* x, cuda
     }
     InstanceScalars* host = b.pinned_scalars != nullptr ? b.pinned_scalars : b.host_scalars.data();
     PSGB_CUDA(cudaMemcpyAsync(host, b.scalars, b.instances * sizeof(InstanceScalars), cudaMemcpyDeviceToHost, st));
-    unsigned barrier_error = 0;
-    if (persistent) {
-        PSGB_CUDA(cudaMemcpyAsync(&barrier_error, b.sync + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    unsigned barrier_error[2] = {0, 0};
+    const bool spread_tail = !persistent && b.tail_level > 0 && b.tail_spread && b.tail_cta_at[b.tail_level] != nullptr;
+    if (persistent || spread_tail) {
+        PSGB_CUDA(cudaMemcpyAsync(barrier_error, b.sync + 2, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     }
     PSGB_CUDA(cudaStreamSynchronize(st));
-    if (barrier_error != 0) {
+    if (barrier_error[0] != 0) {
         throw std::runtime_error("persistent solve: a grid-barrier wait ran past its iteration limit");
+    }
+    if (barrier_error[1] != 0) {
+        // the per-planet barriers' state is unknown after a timeout: start them afresh
+        PSGB_CUDA(cudaMemset(b.tail_barrier, 0, 2 * std::size_t(b.instances) * sizeof(unsigned)));
+        PSGB_CUDA(cudaMemset(b.sync + 3, 0, sizeof(unsigned)));
+        throw std::runtime_error("coarse tail: a per-planet barrier wait ran past its limit");
     }
     if (host != b.host_scalars.data()) {
         std::memcpy(b.host_scalars.data(), host, b.instances * sizeof(InstanceScalars));

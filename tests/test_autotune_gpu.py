@@ -141,3 +141,25 @@ def test_block_sweeps_are_schedule_independent(planets):
     for out, its in runs[1:]:
         assert its == runs[0][1]
         assert all(np.array_equal(a, b) for a, b in zip(runs[0][0], out))
+
+
+def test_spread_coarse_tail_equals_single_block_tail(planets):
+    """Large planets' tails on several co-resident blocks (per-planet barriers) give the
+    same bits as one block per planet and as no tail, in both precisions."""
+    import planet_game_gb300 as pg
+
+    ms, inputs = planets
+    batch = pg.Batch(ms)
+    t = batch.tuning
+    for precision, method in (("mixed", "bicgstab"), ("fp64", "pcg")):
+        runs = []
+        for tail, single in ((0, 0), (1, 1), (1, 0), (2, 0)):
+            t["coarse_tail_level"], t["coarse_tail_single"] = tail, single
+            batch.set_tuning(t)
+            out, reps = step(batch, inputs, precision=precision, method=method)
+            assert all(r.status == 0 for r in reps)
+            runs.append((out, [r.iterations for r in reps], batch.tuning["coarse_tail_blocks"]))
+        assert runs[2][2] > len(ms)            # the L7 and L6 planets took several blocks
+        for out, its, _ in runs[1:]:
+            assert its == runs[0][1]
+            assert all(np.array_equal(a, b) for a, b in zip(runs[0][0], out))
