@@ -292,7 +292,9 @@ __device__ void smooth_zero(const LevelView<T>& lv, int t0, int lane, const T* P
     }
 }
 
-// Damped Jacobi sweep: y = x + omega (D^-1 (b - O x) - x).
+// Damped Jacobi sweep: y = x + omega (D^-1 (b - O x) - x); undamped (omega = 1, a
+// uniform branch) y = D^-1 (b - O x), which neither reads x at the row nor spends the two
+// FP64 operations of the damping.
 template <typename T, int W, int R>
 __device__ void smooth(const LevelView<T>& lv, int t0, int lane, const T* PSGB_PHASE_RESTRICT b,
                        const T* PSGB_PHASE_RESTRICT x, T* PSGB_PHASE_RESTRICT y, T omega, const InstanceScalars* sc,
@@ -310,8 +312,12 @@ __device__ void smooth(const LevelView<T>& lv, int t0, int lane, const T* PSGB_P
         T s = b[row];
 #pragma unroll
         for (int j = 0; j < W; ++j) s -= lv.vd[j * P + row] * x[lv.col[j * P + row]];
-        const T xo = x[row];
-        out[k] = xo + omega * (lv.inv[row] * s - xo);
+        if (omega == T(1)) {
+            out[k] = lv.inv[row] * s;
+        } else {
+            const T xo = x[row];
+            out[k] = xo + omega * (lv.inv[row] * s - xo);
+        }
     }
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -363,7 +369,7 @@ __device__ void smooth_block(const LevelView<T>& lv, int tile, int gid, int lane
             T s = bv;
 #pragma unroll
             for (int j = 0; j < W; ++j) s -= a[j] * (local[j] >= 0 ? xs[gid][local[j]] : h[j]);
-            out = xo + omega * (inv * s - xo);
+            out = omega == T(1) ? inv * s : xo + omega * (inv * s - xo);
         }
         group_sync(gid);
         xs[gid][lane] = out;
@@ -477,8 +483,12 @@ __device__ void prolong_smooth(const LevelView<T>& lv, int t0, int lane, const s
             const int c = lv.col[j * P + row];
             s -= lv.vd[j * P + row] * (x[c] + e[agg[c]]);
         }
-        const T xo = x[row] + e[agg[row]];
-        out[k] = xo + omega * (lv.inv[row] * s - xo);
+        if (omega == T(1)) {
+            out[k] = lv.inv[row] * s;
+        } else {
+            const T xo = x[row] + e[agg[row]];
+            out[k] = xo + omega * (lv.inv[row] * s - xo);
+        }
     }
 #pragma unroll
     for (int k = 0; k < R; ++k) {

@@ -16,6 +16,7 @@
 #include "profile.hpp"
 
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 #include <cstring>
 #include <stdexcept>
@@ -647,8 +648,18 @@ void vcycle(Batch& b, const T* rhs, T* x, int gate, bool first_sweep_done, cudaS
         const LevelView<T> lv = Pick<T>::view(b, l);
         BatchLevel& L = b.levels[l];
         const T* e = Pick<T>::x(b.levels[l + 1]);
-        if (sm.post_at(l) == 0) {
+        // FP64 on the fine level: the fused prolongation adds the correction to every
+        // neighbour it reads (7 more FP64 additions a row), and GB300's FP64 pipe, not
+        // HBM, would bound the sweep; add it once in its own pass instead (same sums,
+        // same bits). FP32 and the latency-bound coarse levels keep the fused launch.
+        const bool split = std::is_same<T, double>::value && l == 0;
+        if (sm.post_at(l) == 0 || split) {
             launch_prolong<T>(lv, L.agg, e, cur[l], b.scalars, gate, st);
+            for (int k = 0; k < sm.post_at(l); ++k) {
+                launch_smooth<T>(lv, rhs_of[l], cur[l], other[l], omega, b.scalars, gate, st, DenseTask<T>{},
+                                 sm.inner_at(l));
+                std::swap(cur[l], other[l]);
+            }
             continue;
         }
         launch_prolong_smooth<T>(lv, L.agg, e, rhs_of[l], cur[l], other[l], omega, b.scalars, gate, st);
