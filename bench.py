@@ -425,6 +425,110 @@ def run_serve_sweep(args, rank, local_rank):
                       "higher_is_better": True, "data": "synthetic", "sweep": points}))
 
 
+# ---- the rows that widen the hot path -------------------------------------------------------
+
+class _DeviceArray:
+    """A raw device pointer as a CUDA array (torch.as_tensor without a copy)."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr, False), "version": 3,
+                                         "stream": None}
+
+
+def _median_ms(fn, repeats: int = 5) -> float:
+    import statistics
+
+    import torch
+
+    fn()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(repeats):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        times.append((time.perf_counter() - t) * 1e3)
+    return statistics.median(times)
+
+
+def run_next(args, rank, local_rank):
+    """GPU timings of the widened rows on the cases oracle/time_reference.py times with the
+    reference's CPU code (same shapes, same seeds): the implicit tracer on the L7 mesh's
+    agglomerated graph (10 layers), the transport step on the L8 mesh's agglomerated graph,
+    the L8 sub-step-mean insolation, the coupled advection-diffusion solve on the L6 graph
+    (3 layers, the reference test's column on the GPU). Host arrays in and out (as the
+    reference's calls), device-resident where noted. One JSON line."""
+    import torch
+
+    import planet_game_gb300 as pg
+    from planet_game_gb300 import workloads as W
+
+    if rank != 0:
+        return
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    R, CP = W.EARTH_RADIUS, 1004.64
+    out = {"metric": "ms per call of the widened rows (median of 5)", "unit": "ms", "n_gpus": 1, "data": "synthetic"}
+    # tracer
+    p7 = pg.agglomerated_transport_graph(7, R)
+    g7 = pg.mesh_transport_graph(p7)
+    n7, layers = p7.cell_count, 10
+    flux = W.antisymmetric_layer_fluxes(g7.offset, g7.neighbour, layers, 2e9, seed=71, column_balanced=False)
+    cond = np.full(len(g7.neighbour), 2e8)
+    mass = g7.area_m2 * 100000.0 / (9.81 * layers)
+    tracer = W.tracer_field(layers * n7, seed=72)
+    tr_h = pg.AdvectionDiffusion(layers, cond, flux, CP)
+    res = {}
+    out["tracer_ms"] = _median_ms(lambda: res.update(r=pg.solve_implicit_tracer(p7, tr_h, mass, tracer, 2.63e6)))
+    out["tracer_iterations"] = res["r"].iterations
+    out["tracer_rows"] = layers * n7
+    tr_d = pg.AdvectionDiffusion(layers, torch.as_tensor(cond, device=dev), torch.as_tensor(flux, device=dev), CP)
+    mass_d, tracer_d = torch.as_tensor(mass, device=dev), torch.as_tensor(tracer, device=dev)
+    out["tracer_resident_ms"] = _median_ms(lambda: pg.solve_implicit_tracer(p7, tr_d, mass_d, tracer_d, 2.63e6))
+    # agglomerated transport step (plain FP64 and mixed)
+    p8 = pg.agglomerated_transport_graph(8, R)
+    t0, source = W.agglomerated_step_inputs(p8.cell_count, seed=81)
+    for prec in ("fp64", "mixed"):
+        rep = {}
+        out[f"agglomerated_{prec}_ms"] = _median_ms(lambda: rep.update(r=pg.transport_step(
+            p8, t0, source, W.HEAT_CAPACITY, W.SUBSTEP_S, W.HEAT_CAPACITY * W.DIFFUSIVITY, precision=prec)[2]))
+        out[f"agglomerated_{prec}_iterations"] = rep["r"].iterations
+    out["agglomerated_nodes"] = p8.cell_count
+    # insolation at L8
+    m8 = pg.make_icosphere(8, R)
+    ins = torch.empty(m8.cell_count, dtype=torch.float32, device=dev)
+    out["insolation_resident_ms"] = _median_ms(lambda: m8.substep_mean_insolation_gpu(0, ins))
+    out["insolation_ms"] = _median_ms(lambda: m8.substep_mean_insolation_gpu(0))
+    # coupled advection-diffusion on the L6 graph, the column on the GPU
+    m6 = pg.make_icosphere(6, R)
+    g6 = pg.mesh_transport_graph(m6)
+    n6 = m6.cell_count
+    flux6 = W.antisymmetric_layer_fluxes(g6.offset, g6.neighbour, 3, 5e9, seed=61, column_balanced=True)
+    cond6 = 0.5 * R * R * g6.weight
+    a, radiative = 3.0e5 / (30.0 * 86400.0), 0.75 * 0.97 * pg.api.STEFAN_BOLTZMANN_W_M2_K4
+    b, floor = W.quartic_column(a, radiative, n6, seed=62)
+    eps = torch.tensor([0.0, -0.08, -0.16], dtype=torch.float64, device=dev)[:, None]
+    phi = torch.tensor([3.0e4, 4.5e4, 7.0e4], dtype=torch.float64, device=dev)[:, None]
+    q = pg.QuarticResponse(a, torch.as_tensor(b, device=dev), radiative, hold_stride=0)
+
+    def column(nodes, nl, src, mean, slope, energy, energy_slope, stream):
+        h = torch.as_tensor(_DeviceArray(src, nodes), device=dev)
+        x, s = pg.quartic_response(q, h)
+        torch.as_tensor(_DeviceArray(mean, nodes), device=dev).copy_(x)
+        torch.as_tensor(_DeviceArray(slope, nodes), device=dev).copy_(s)
+        torch.as_tensor(_DeviceArray(energy, nodes * nl), device=dev).view(nl, nodes).copy_(CP * x * (1.0 + eps) + phi)
+        torch.as_tensor(_DeviceArray(energy_slope, nodes * nl), device=dev).view(nl, nodes).copy_(CP * s * (1.0 + eps))
+
+    tr6 = pg.AdvectionDiffusion(3, cond6, flux6, CP)
+    settings = {"cg_relative_tolerance": 1e-6, "newton_tolerance_W_m2": 1e-6}
+    ad = {}
+    out["advection_ms"] = _median_ms(lambda: ad.update(r=pg.solve_implicit_advection_diffusion(
+        m6, tr6, floor, column, settings=settings, device=True)))
+    out["advection_newton"], out["advection_linear"] = ad["r"].newton_iterations, ad["r"].linear_iterations
+    print(json.dumps(out))
+
+
 # ---- CPU baseline and the reference arm ------------------------------------------------------
 
 def _oracle_solve(payload):
@@ -505,7 +609,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["batch", "l8", "serve"], default="batch")
+    ap.add_argument("--workload", choices=["batch", "l8", "serve", "next"], default="batch")
     ap.add_argument("--serve-rate", type=float, default=5000.0)
     ap.add_argument("--serve-requests", type=int, default=2000)
     ap.add_argument("--skip-serve", action="store_true")
@@ -528,6 +632,9 @@ def main():
         return
     if args.workload == "serve":
         run_serve_sweep(args, rank, local_rank)
+        return
+    if args.workload == "next":
+        run_next(args, rank, local_rank)
         return
     run_gb300(args, rank, world, local_rank)
 

@@ -485,6 +485,34 @@ AdvectionDiffusion transport_of(const TransportGraph& graph, std::uint64_t layer
 
 }  // namespace
 
+// solve_implicit_transport with the linear response mean = base + slope h on the mesh's
+// agglomerated graph (heat_transport.cpp:456-539, 595-772); nodes of the coarser mesh.
+void refd_solve_linear_agglomerated(void* handle, double conductance, const double* base, const double* slope,
+                                    double cg_tolerance, double newton_tolerance, std::uint64_t workers,
+                                    double* mean_out, double* source_out, double* stats) {
+    TransportGraph own;
+    const TransportGraph& graph = graph_of(handle, 1, own);
+    const std::size_t n = graph.size();
+    const TransportResponse response = [&](const Field2D<double>& source, Field2D<double>& mean,
+                                           Field2D<double>& slope_out) {
+        for (std::size_t cell = 0; cell < n; ++cell) {
+            mean[cell] = base[cell] + slope[cell] * source[cell];
+            slope_out[cell] = slope[cell];
+        }
+    };
+    const Field2D<double> floor(n, -std::numeric_limits<double>::infinity());
+    ImplicitTransportSettings settings;
+    settings.cg_relative_tolerance = cg_tolerance;
+    settings.newton_tolerance_W_m2 = newton_tolerance;
+    const auto result = solve_implicit_transport(graph, conductance, floor, response, settings,
+                                                 static_cast<std::size_t>(workers));
+    std::copy(result.mean_K.values().begin(), result.mean_K.values().end(), mean_out);
+    std::copy(result.source_W_m2.values().begin(), result.source_W_m2.values().end(), source_out);
+    stats[0] = result.newton_iterations;
+    stats[1] = result.cg_iterations;
+    stats[2] = result.consistency_residual_W_m2;
+}
+
 // IncompleteLU with blocks, then solve(x) in place.
 void refd_incomplete_lu(std::uint64_t rows, const std::uint64_t* offset, const std::uint64_t* neighbour,
                         const double* diagonal, const double* off, const std::uint64_t* block_start,

@@ -296,3 +296,59 @@ def poisson_trace(count: int, rate_per_s: float, seed: int, weights=((4, .30), (
     pl = rng.integers(0, planets_per_level, count)
     t = np.cumsum(gaps)
     return [Request(float(t[i]), int(lv[i]), int(pl[i])) for i in range(count)]
+
+
+# ---- non-symmetric transport cases (tracer, coupled advection-diffusion) -----------------
+
+def reverse_entries(offset: np.ndarray, neighbour: np.ndarray) -> np.ndarray:
+    """For every CSR entry a -> b, the entry b -> a."""
+    offset = offset.astype(np.int64)
+    neighbour = neighbour.astype(np.int64)
+    rows = np.repeat(np.arange(len(offset) - 1), np.diff(offset))
+    # entries sorted by (row, neighbour) and by (neighbour, row) pair up one to one
+    forward = np.lexsort((neighbour, rows))
+    backward = np.lexsort((rows, neighbour))
+    rev = np.empty(len(neighbour), dtype=np.int64)
+    rev[forward] = backward
+    return rev
+
+
+def antisymmetric_layer_fluxes(offset, neighbour, layers: int, scale: float, seed: int,
+                               column_balanced: bool = True) -> np.ndarray:
+    """Layer mass fluxes per CSR entry (kg/s, layer-major) of about `scale`, antisymmetric
+    per face; with `column_balanced` each face's column sums to zero (the shape of the
+    reference's transport tests, test_tracer_transport.cpp:33-60)."""
+    offset = offset.astype(np.int64)
+    neighbour = neighbour.astype(np.int64)
+    rows = np.repeat(np.arange(len(offset) - 1), np.diff(offset))
+    upper = np.nonzero(rows < neighbour)[0]
+    rev = reverse_entries(offset, neighbour)
+    rng = np.random.default_rng(seed)
+    flow = scale * (2.0 * rng.random((layers, len(upper))) - 1.0)
+    if column_balanced:
+        flow -= flow.mean(axis=0, keepdims=True)
+    out = np.zeros((layers, len(neighbour)))
+    out[:, upper] = flow
+    out[:, rev[upper]] = -flow
+    return out.ravel()
+
+
+def agglomerated_step_inputs(nodes: int, seed: int) -> tuple[np.ndarray, np.ndarray]:
+    """T0 = 288 + N(0, 0.5) K and S = N(0, 50) W/m^2 per node: the transport step on an
+    agglomerated graph (nodes of the coarser mesh)."""
+    rng = np.random.default_rng(seed)
+    return 288.0 + rng.normal(0.0, 0.5, nodes), rng.normal(0.0, 50.0, nodes)
+
+
+def tracer_field(count: int, seed: int) -> np.ndarray:
+    """Positive mixing ratios around 0.01 (layer-major)."""
+    return 0.01 * (1.0 + 0.5 * np.random.default_rng(seed).standard_normal(count) ** 2)
+
+
+def quartic_column(a: float, radiative: float, nodes: int, seed: int) -> tuple[np.ndarray, np.ndarray]:
+    """The reference test's quartic column (test_heat_transport.cpp:58-76): forcings b
+    putting each column's equilibrium between 200 and 320 K, and the floor of sources
+    that keeps every column at or above 100 K."""
+    target = 200.0 + 120.0 * np.random.default_rng(seed).random(nodes)
+    b = a * target + radiative * target ** 4
+    return b, a * 100.0 + radiative * 100.0 ** 4 - b
