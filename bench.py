@@ -470,6 +470,14 @@ def run_next(args, rank, local_rank):
     dev = torch.device("cuda", local_rank)
     R, CP = W.EARTH_RADIUS, 1004.64
     out = {"metric": "ms per call of the widened rows (median of 5)", "unit": "ms", "n_gpus": 1, "data": "synthetic"}
+    # the mesh builder (host, all cores): the first L8 mesh of the process, then another radius
+    t = time.perf_counter()
+    pg.make_icosphere(8, R)
+    out["mesh_l8_first_ms"] = (time.perf_counter() - t) * 1e3
+    t = time.perf_counter()
+    pg.make_icosphere(8, 0.5 * R)
+    out["mesh_l8_radius_ms"] = (time.perf_counter() - t) * 1e3
+    out["host_cores"] = os.cpu_count()
     # tracer
     p7 = pg.agglomerated_transport_graph(7, R)
     g7 = pg.mesh_transport_graph(p7)

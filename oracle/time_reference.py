@@ -94,6 +94,9 @@ def main(reference: Path, workers: int) -> None:
 
     R = load(reference)
     out = {"workers": workers, "host": os.uname().machine}
+    t = time.perf_counter()
+    R.refd_mesh_free(P(R.refd_mesh_new(8, RADIUS)))   # make_icosphere (single-threaded in the reference)
+    out["mesh_l8_ms"] = (time.perf_counter() - t) * 1e3
     # tracer: agglomerated L7 graph, 10 layers
     m7 = P(R.refd_mesh_new(7, RADIUS))
     g = graph(R, m7, True)

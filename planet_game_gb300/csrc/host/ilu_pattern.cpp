@@ -112,6 +112,39 @@ IluPattern ilu_pattern(const std::vector<std::uint32_t>& offset, const std::vect
     p.upper = schedule(block_start, false, [&](std::uint32_t i, auto&& f) {
         for (std::uint32_t q = p.diagonal[i] + 1; q < p.start[i + 1]; ++q) f(p.column[q]);
     });
+    // Records for the shared-memory solve, if every block and row fit it.
+    bool fits = true;
+    for (std::uint32_t b = 0; b < p.blocks; ++b)
+        fits = fits && block_start[b + 1] - block_start[b] <= kIluSharedRows;
+    for (std::uint32_t i = 0; i < p.rows && fits; ++i)
+        fits = p.diagonal[i] - p.start[i] <= static_cast<std::uint32_t>(kIluRecord) &&
+               p.start[i + 1] - p.diagonal[i] - 1 <= static_cast<std::uint32_t>(kIluRecord);
+    if (fits) {
+        for (int part = 0; part < 2; ++part) {
+            LevelSchedule& s = part == 0 ? p.lower : p.upper;
+            s.rec_row.resize(p.rows);
+            s.rec_count.resize(p.rows);
+            s.rec_col.assign(std::size_t(p.rows) * kIluRecord, 0);
+            s.rec_q.assign(std::size_t(p.rows) * kIluRecord, 0);
+            for (std::uint32_t b = 0; b < p.blocks; ++b) {
+                for (std::uint32_t lv = s.block_level[b]; lv < s.block_level[b + 1]; ++lv) {
+                    s.widest = std::max(s.widest, s.level_start[lv + 1] - s.level_start[lv]);
+                    for (std::uint32_t idx = s.level_start[lv]; idx < s.level_start[lv + 1]; ++idx) {
+                        const std::uint32_t i = s.order[idx];
+                        const std::uint32_t first = block_start[b];
+                        const std::uint32_t q0 = part == 0 ? p.start[i] : p.diagonal[i] + 1;
+                        const std::uint32_t q1 = part == 0 ? p.diagonal[i] : p.start[i + 1];
+                        s.rec_row[idx] = static_cast<std::uint16_t>(i - first);
+                        s.rec_count[idx] = static_cast<std::uint8_t>(q1 - q0);
+                        for (std::uint32_t q = q0; q < q1; ++q) {
+                            s.rec_col[std::size_t(idx) * kIluRecord + (q - q0)] = static_cast<std::uint16_t>(p.column[q] - first);
+                            s.rec_q[std::size_t(idx) * kIluRecord + (q - q0)] = q;
+                        }
+                    }
+                }
+            }
+        }
+    }
     return p;
 }
 

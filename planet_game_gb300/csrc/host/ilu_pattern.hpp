@@ -20,7 +20,19 @@ struct LevelSchedule {
     std::vector<std::uint32_t> block_level;   // [blocks + 1]: each block's levels
     std::vector<std::uint32_t> level_start;   // [levels + 1]: each level's rows in `order`
     std::vector<std::uint32_t> order;         // [rows]
+    // The triangular solve's records in `order`'s order, for a solve with the block's x
+    // in shared memory: the row and its (at most kIluRecord) couplings of this triangle as
+    // block-local indices, and the positions of their values in the factor (packed next
+    // to the record after each factorisation). Empty when a block is too large for it.
+    std::vector<std::uint16_t> rec_row;       // [rows]
+    std::vector<std::uint8_t> rec_count;      // [rows]
+    std::vector<std::uint16_t> rec_col;       // [rows][kIluRecord]
+    std::vector<std::uint32_t> rec_q;         // [rows][kIluRecord]
+    std::uint32_t widest = 0;                 // most rows in one level
 };
+
+constexpr int kIluRecord = 8;
+constexpr std::uint32_t kIluSharedRows = 4096;   // block rows the shared-memory solve takes
 
 struct IluPattern {
     std::uint32_t rows = 0, blocks = 0;

@@ -113,6 +113,102 @@ __global__ void __launch_bounds__(kIluThreads) k_ilu_solve(IluView v, double* __
     }
 }
 
+// The triangular solves with the block's x in shared memory and per-level records (the
+// row, its couplings' block-local columns and their factor values packed next to them):
+// a thread owns one row of a level, loads the next level's record before the current
+// level's barrier, so a level costs a barrier and shared-memory reads rather than a chain
+// of dependent global loads. Same terms in the same order as k_ilu_solve: same bits.
+struct IluRecords {
+    const std::uint16_t* row;
+    const std::uint8_t* count;
+    const std::uint16_t* col;      // [rows][8]
+    const std::uint32_t* q;        // [rows][8]: value positions
+    double* val;                   // [rows][8]: packed values
+    const std::uint32_t* dq;       // upper: the row's diagonal position
+    double* dval;                  // upper: the diagonal value
+    const std::uint32_t* block;    // [blocks + 1] levels
+    const std::uint32_t* level;    // [levels + 1]
+};
+
+struct IluShared {
+    IluRecords lo, up;
+    const std::uint32_t* block_start;   // [blocks + 1] rows
+};
+
+__global__ void k_ilu_pack(std::uint32_t rows, IluShared s, const double* __restrict__ value) {
+    const std::uint32_t idx = blockIdx.x * kThreads + threadIdx.x;
+    if (idx >= rows) return;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        s.lo.val[idx * 8 + k] = k < s.lo.count[idx] ? value[s.lo.q[idx * 8 + k]] : 0.0;
+        s.up.val[idx * 8 + k] = k < s.up.count[idx] ? value[s.up.q[idx * 8 + k]] : 0.0;
+    }
+    s.up.dval[idx] = value[s.up.dq[idx]];
+}
+
+struct Rec {
+    int row, count;
+    std::uint16_t col[8];
+    double val[8];
+    double diag;
+};
+
+__device__ __forceinline__ Rec load_rec(const IluRecords& r, std::uint32_t lv, bool upper) {
+    Rec x;
+    x.row = -1;
+    x.count = 0;
+    x.diag = 1.0;
+    const std::uint32_t idx = r.level[lv] + threadIdx.x;
+    if (idx < r.level[lv + 1]) {
+        x.row = r.row[idx];
+        x.count = r.count[idx];
+        const uint4 c = *reinterpret_cast<const uint4*>(r.col + std::size_t(idx) * 8);
+        const std::uint16_t* cc = reinterpret_cast<const std::uint16_t*>(&c);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x.col[k] = cc[k];
+        const double2* v = reinterpret_cast<const double2*>(r.val + std::size_t(idx) * 8);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const double2 d = v[k];
+            x.val[2 * k] = d.x;
+            x.val[2 * k + 1] = d.y;
+        }
+        if (upper) x.diag = r.dval[idx];
+    }
+    return x;
+}
+
+constexpr unsigned kIluSharedThreads = 512;   // the widest level the shared-memory solve takes
+
+__global__ void __launch_bounds__(kIluSharedThreads, 1) k_ilu_solve_shared(IluShared s, double* __restrict__ x) {
+    extern __shared__ double xs[];
+    const std::uint32_t b = blockIdx.x;
+    const std::uint32_t first = s.block_start[b], n = s.block_start[b + 1] - first;
+    for (std::uint32_t r = threadIdx.x; r < n; r += blockDim.x) xs[r] = x[first + r];
+    __syncthreads();
+    for (int part = 0; part < 2; ++part) {
+        const bool upper = part == 1;
+        const IluRecords& R = upper ? s.up : s.lo;
+        const std::uint32_t lv0 = R.block[b], lv1 = R.block[b + 1];
+        const Rec none{-1, 0, {}, {}, 1.0};
+        // the next level's record loads while this level computes and meets
+        Rec cur = lv0 < lv1 ? load_rec(R, lv0, upper) : none;
+        for (std::uint32_t lv = lv0; lv < lv1; ++lv) {
+            const Rec next = lv + 1 < lv1 ? load_rec(R, lv + 1, upper) : none;
+            if (cur.row >= 0) {
+                double sum = xs[cur.row];
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    if (k < cur.count) sum -= cur.val[k] * xs[cur.col[k]];
+                xs[cur.row] = upper ? sum / cur.diag : sum;
+            }
+            __syncthreads();
+            cur = next;
+        }
+    }
+    for (std::uint32_t r = threadIdx.x; r < n; r += blockDim.x) x[first + r] = xs[r];
+}
+
 }  // namespace
 
 // A block ILU(0) structure on the device, its values refactored per matrix.
@@ -135,6 +231,45 @@ class DeviceIlu {
         v_.value = store_.alloc<double>(p.column.size());
         v_.flag = store_.alloc<int>(1);
         v_.rows = p.rows;
+        // the shared-memory solve, when the pattern has its records and a level fits a block
+        const std::uint32_t widest = std::max(p.lower.widest, p.upper.widest);
+        if (!p.lower.rec_row.empty() && widest <= kIluSharedThreads) {
+            auto records = [&](const LevelSchedule& sch, bool upper) {
+                IluRecords r{};
+                r.row = store_.upload(sch.rec_row);
+                r.count = store_.upload(sch.rec_count);
+                r.col = store_.upload(sch.rec_col);
+                r.q = store_.upload(sch.rec_q);
+                r.val = store_.alloc<double>(sch.rec_q.size());
+                r.block = upper ? v_.up_block : v_.lo_block;
+                r.level = upper ? v_.up_level : v_.lo_level;
+                if (upper) {
+                    std::vector<std::uint32_t> dq(p.rows);
+                    for (std::uint32_t idx = 0; idx < p.rows; ++idx) dq[idx] = p.diagonal[sch.order[idx]];
+                    r.dq = store_.upload(dq);
+                    r.dval = store_.alloc<double>(p.rows);
+                }
+                return r;
+            };
+            shared_.lo = records(p.lower, false);
+            shared_.up = records(p.upper, true);
+            std::uint32_t most = 0;
+            std::vector<std::uint32_t> starts(p.blocks + 1, 0);
+            for (std::uint32_t b = 0; b < p.blocks; ++b) {
+                // block b's rows: the lower schedule lists them level by level
+                const std::uint32_t lv0 = p.lower.block_level[b], lv1 = p.lower.block_level[b + 1];
+                const std::uint32_t count = lv1 > lv0 ? p.lower.level_start[lv1] - p.lower.level_start[lv0] : 0;
+                starts[b + 1] = starts[b] + count;
+                most = std::max(most, count);
+            }
+            shared_.block_start = store_.upload(starts);
+            shared_threads_ = std::max(32u, (widest + 31) / 32 * 32);
+            shared_bytes_ = std::max<std::size_t>(8, std::size_t(most) * sizeof(double));
+            use_shared_ = shared_bytes_ <= 48 * 1024 ||
+                          cudaFuncSetAttribute(k_ilu_solve_shared, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               static_cast<int>(shared_bytes_)) == cudaSuccess;
+            cudaGetLastError();
+        }
     }
 
     // Factors diag * scale + off (CSR entries as the pattern's source); throws Breakdown
@@ -145,6 +280,10 @@ class DeviceIlu {
         PSGB_CHECK_LAUNCH();
         k_ilu_factor<<<blocks_, kIluThreads, 0, st>>>(v_);
         PSGB_CHECK_LAUNCH();
+        if (use_shared_) {
+            k_ilu_pack<<<blocks_of(rows_), kThreads, 0, st>>>(rows_, shared_, v_.value);
+            PSGB_CHECK_LAUNCH();
+        }
         int flag = 0;
         PSGB_CUDA(cudaMemcpyAsync(&flag, v_.flag, sizeof(int), cudaMemcpyDeviceToHost, st));
         PSGB_CUDA(cudaStreamSynchronize(st));
@@ -152,7 +291,11 @@ class DeviceIlu {
     }
 
     void solve(double* x, cudaStream_t st) const {
-        k_ilu_solve<<<blocks_, kIluThreads, 0, st>>>(v_, x);
+        if (use_shared_) {
+            k_ilu_solve_shared<<<blocks_, shared_threads_, shared_bytes_, st>>>(shared_, x);
+        } else {
+            k_ilu_solve<<<blocks_, kIluThreads, 0, st>>>(v_, x);
+        }
         PSGB_CHECK_LAUNCH();
     }
 
@@ -162,21 +305,32 @@ class DeviceIlu {
     DeviceStore store_;
     IluView v_{};
     std::uint32_t rows_, blocks_;
+    IluShared shared_{};
+    bool use_shared_ = false;
+    unsigned shared_threads_ = 0;
+    std::size_t shared_bytes_ = 0;
 };
 
 namespace {
 
 // ---- reductions and BiCGSTAB -------------------------------------------------------
 
+// Fixed-order block sum (256 threads): a butterfly in each warp, then one over the eight
+// warp sums; the same bits on every run.
 __device__ double tree_sum(double v, double* sh) {
     const int t = threadIdx.x;
-    sh[t] = v;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((t & 31) == 0) sh[t >> 5] = v;
     __syncthreads();
-    for (int s = kThreads / 2; s > 0; s >>= 1) {
-        if (t < s) sh[t] = sh[t] + sh[t + s];
-        __syncthreads();
+    double r = (t & 31) < kThreads / 32 ? sh[t & 31] : 0.0;
+    if (t < 32) {
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+        if (t == 0) sh[32] = r;
     }
-    const double r = sh[0];
+    __syncthreads();
+    r = sh[32];
     __syncthreads();
     return r;
 }
@@ -255,14 +409,33 @@ __global__ void k_bicg_xr(std::uint32_t n, double* __restrict__ x, double* __res
     }
 }
 
-// y = diag x + off x over a CSR pattern (the reference's apply, its order).
-__global__ void k_csr_apply(std::uint32_t n, const std::uint32_t* __restrict__ offset,
-                            const std::uint32_t* __restrict__ neighbour, const double* __restrict__ diag,
-                            const double* __restrict__ off, const double* __restrict__ x, double* __restrict__ y) {
+
+// y = diag x + off x (the reference's apply) on an ELL copy of the off-diagonals (slot-major,
+// coalesced): slot j of row r is CSR entry offset[r] + j, so the terms add in the same
+// order, the same bits.
+struct Ell {
+    std::uint32_t rows, width;
+    const std::uint8_t* degree;     // [rows]
+    const std::uint32_t* col;       // [width][rows]
+};
+
+__global__ void k_csr_to_ell(Ell e, const std::uint32_t* __restrict__ offset, const double* __restrict__ off,
+                             double* __restrict__ val) {
     const std::uint32_t r = blockIdx.x * kThreads + threadIdx.x;
-    if (r >= n) return;
+    if (r >= e.rows) return;
+    const std::uint32_t first = offset[r], deg = e.degree[r];
+    for (std::uint32_t j = 0; j < e.width; ++j) val[std::size_t(j) * e.rows + r] = j < deg ? off[first + j] : 0.0;
+}
+
+__global__ void k_ell_apply(Ell e, const double* __restrict__ val, const double* __restrict__ diag,
+                            const double* __restrict__ x, double* __restrict__ y) {
+    const std::uint32_t r = blockIdx.x * kThreads + threadIdx.x;
+    if (r >= e.rows) return;
+    const std::uint32_t deg = e.degree[r];
     double sum = diag[r] * x[r];
-    for (std::uint32_t k = offset[r]; k < offset[r + 1]; ++k) sum += off[k] * x[neighbour[k]];
+    for (std::uint32_t j = 0; j < e.width; ++j) {
+        if (j < deg) sum += val[std::size_t(j) * e.rows + r] * x[e.col[std::size_t(j) * e.rows + r]];
+    }
     y[r] = sum;
 }
 
@@ -667,6 +840,7 @@ __global__ void __launch_bounds__(kThreads) k_tracer_flux_form(GraphView g, Tran
 struct NonsymContext {
     DeviceStore store;
     GraphView graph{};
+    Ell graph_ell{};
     std::uint32_t* face_order = nullptr;
     std::uint32_t* lower_count = nullptr;
     std::uint32_t* reverse = nullptr;
@@ -674,12 +848,30 @@ struct NonsymContext {
     struct StackedSystem {
         DeviceStore store;
         Stacked view{};
+        Ell ell{};
         std::unique_ptr<DeviceIlu> ilu;
     };
     std::map<std::uint32_t, std::unique_ptr<StackedSystem>> stacked;
 };
 
 namespace {
+
+// The ELL shape of a CSR pattern (columns slot-major, degrees), in `store`.
+Ell ell_of(DeviceStore& store, const std::vector<std::uint32_t>& offset, const std::vector<std::uint32_t>& neighbour) {
+    Ell e{};
+    e.rows = static_cast<std::uint32_t>(offset.size() - 1);
+    for (std::uint32_t r = 0; r < e.rows; ++r) e.width = std::max(e.width, offset[r + 1] - offset[r]);
+    if (e.width > 255) throw std::logic_error("non-symmetric solve: a row with more than 255 couplings");
+    std::vector<std::uint8_t> degree(e.rows);
+    std::vector<std::uint32_t> col(std::size_t(e.width) * e.rows, 0);
+    for (std::uint32_t r = 0; r < e.rows; ++r) {
+        degree[r] = static_cast<std::uint8_t>(offset[r + 1] - offset[r]);
+        for (std::uint32_t j = 0; j < degree[r]; ++j) col[std::size_t(j) * e.rows + r] = neighbour[offset[r] + j];
+    }
+    e.degree = store.upload(degree);
+    e.col = store.upload(col);
+    return e;
+}
 
 NonsymContext& context(psgb_planet* h) {
     if (h->nonsym) return *h->nonsym;
@@ -719,6 +911,7 @@ NonsymContext& context(psgb_planet* h) {
     c->face_order = c->store.upload(order);
     c->lower_count = c->store.upload(lower);
     c->graph_ilu = std::make_unique<DeviceIlu>(ilu_pattern(g.offset, g.neighbour, fixed_blocks(n, 1)));
+    c->graph_ell = ell_of(c->store, g.offset, g.neighbour);
     h->nonsym = c;
     return *c;
 }
@@ -749,6 +942,7 @@ NonsymContext::StackedSystem& stacked_system(psgb_planet* h, std::uint32_t layer
     s->view.offset = s->store.upload(offset);
     s->view.neighbour = s->store.upload(neighbour);
     s->ilu = std::make_unique<DeviceIlu>(ilu_pattern(offset, neighbour, fixed_blocks(n, layers)));
+    s->ell = ell_of(s->store, offset, neighbour);
     auto& ref = *s;
     c.stacked.emplace(layers, std::move(s));
     return ref;
@@ -929,8 +1123,11 @@ int psgb_solve_implicit_tracer(psgb_planet* planet, const psgb_advection_diffusi
                                                               c0, diagonal, off, rhs, start);
         PSGB_CHECK_LAUNCH();
         S.ilu->factor(diagonal, off, 1.0, st);
+        double* off_ell = w.alloc<double>(std::size_t(S.ell.width) * rows);
+        psgb::k_csr_to_ell<<<gr, psgb::kThreads, 0, st>>>(S.ell, S.view.offset, off, off_ell);
+        PSGB_CHECK_LAUNCH();
         const psgb::Op apply = [&](const double* x, double* y) {
-            psgb::k_csr_apply<<<gr, psgb::kThreads, 0, st>>>(urows, S.view.offset, S.view.neighbour, diagonal, off, x, y);
+            psgb::k_ell_apply<<<gr, psgb::kThreads, 0, st>>>(S.ell, off_ell, diagonal, x, y);
             PSGB_CHECK_LAUNCH();
         };
         const psgb::Op precondition = [&](const double* x, double* y) {
@@ -1065,8 +1262,9 @@ int psgb_solve_implicit_advection_diffusion(psgb_planet* planet, const psgb_adve
         evaluate(current);
         psgb_advection_result out{};
         int non_monotone = 0;
+        double* off_ell = w.alloc<double>(std::size_t(c.graph_ell.width) * n);
         const psgb::Op apply = [&](const double* x, double* y) {
-            psgb::k_csr_apply<<<gn, psgb::kThreads, 0, st>>>(n, g.offset, g.neighbour, diagonal, off, x, y);
+            psgb::k_ell_apply<<<gn, psgb::kThreads, 0, st>>>(c.graph_ell, off_ell, diagonal, x, y);
             PSGB_CHECK_LAUNCH();
         };
         // The V-cycle of A theta'^-1 + K on A x, divided by theta', then the block ILU of J
@@ -1092,6 +1290,8 @@ int psgb_solve_implicit_advection_diffusion(psgb_planet* planet, const psgb_adve
                                                                      sym_off);
             PSGB_CHECK_LAUNCH();
             c.graph_ilu->factor(diagonal, off, 1.0, st);
+            psgb::k_csr_to_ell<<<gn, psgb::kThreads, 0, st>>>(c.graph_ell, g.offset, off, off_ell);
+            PSGB_CHECK_LAUNCH();
             if (psgb_multigrid_set_matrix(planet, sym_diagonal, sym_off, PSGB_MEMORY_DEVICE, st) != PSGB_OK)
                 throw std::runtime_error(psgb_last_error());
             out.linear_iterations += psgb::bicgstab(n, apply, precondition, rhs, delta, settings.cg_relative_tolerance,
