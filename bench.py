@@ -162,6 +162,8 @@ def make_workload(kind: str, seed: int):
 def smoother_desc(tuning) -> str:
     if tuning is None:
         return "damped Jacobi 2+2 on every level, omega 0.8 (untuned)"
+    if isinstance(tuning, list):
+        return " | ".join(f"lane {k}: {smoother_desc(t)}" for k, t in enumerate(tuning))
     per = ", ".join(f"L{l}: {a}+{b}" for l, (a, b) in enumerate(zip(tuning["pre_sweeps"], tuning["post_sweeps"])))
     return f"damped Jacobi, autotuned sweeps per level ({per}), omega {tuning['jacobi_omega']}"
 
@@ -188,7 +190,9 @@ def run_gb300(args, rank, world, local_rank):
     meshes = [m for m, _ in planets]
     cells = sum(m.cell_count for m in meshes)
     prec = precision_for(args.workload)
-    batch = pg.Batch(meshes)
+    # the planets of the mix's highest level in a lane of their own (pg.default_lanes):
+    # they need the most Krylov iterations, and the lanes run side by side
+    batch = pg.LaneBatch(meshes)
     t0_d = [torch.from_numpy(inp.t0).to(dev) for _, inp in planets]
     s_d = [torch.from_numpy(inp.source).to(dev) for _, inp in planets]
     out_d = [torch.empty_like(t) for t in t0_d]
@@ -269,10 +273,12 @@ def run_gb300(args, rank, world, local_rank):
 
     def profile_family(family: bytes, kernel: str) -> dict:
         ms, nl, nbytes = C.c_double(), C.c_uint64(), C.c_uint64()
+        batch.concurrent = False      # one launch at a time between a family's events
         capi.check(lib.psgb_profile_begin(family))
         for _ in range(args.steps):
             step(t0_d, s_d, out_d)
         capi.check(lib.psgb_profile_end(C.byref(ms), C.byref(nl), C.byref(nbytes)))
+        batch.concurrent = True
         achieved = nbytes.value / (ms.value / 1e3) / 1e9 if ms.value > 0 else None
         traffic = (traffic_all.get(args.workload) or {}).get(family.decode())
         return {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
@@ -328,6 +334,7 @@ def run_gb300(args, rank, world, local_rank):
                              "diffusivity, one batched sub-step per step" if args.workload == "batch"
                              else "one L8 planet (655,362 cells), plain FP64 drop-in solve"),
                 "planets": len(meshes), "cells": cells, "precision": prec, "krylov": "BiCGSTAB",
+                "lanes": [sorted({meshes[i].subdivision for i in lane}) for lane in batch.lanes],
                 "smoother": smoother_desc(tuning), "tuning": tuning, "tolerance": 1e-10,
                 "krylov_iterations_per_step": sum(r.iterations for r in reps), "refinements_last_step": max(refinements),
                 "krylov_iterations_per_planet": {"min": min(r.iterations for r in reps),

@@ -7,6 +7,8 @@ reference's C++ operator and solver API over it.
 from .api import (  # noqa: F401
     Batch,
     GraphMultigrid,
+    LaneBatch,
+    default_lanes,
     PlanetMesh,
     QuarticResponse,
     TransportGraph,

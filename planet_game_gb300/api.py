@@ -698,6 +698,99 @@ class Batch:
         return out, [_step_result(r) for r in reps]
 
 
+def default_lanes(meshes: list[PlanetMesh]) -> list[list[int]]:
+    """The highest level's planets apart from the others when a mix spans three or more
+    levels (they need the most Krylov iterations); otherwise one lane."""
+    levels = [m.subdivision for m in meshes]
+    if len(set(levels)) < 3:
+        return [list(range(len(meshes)))]
+    top = max(levels)
+    return [[i for i, l in enumerate(levels) if l != top], [i for i, l in enumerate(levels) if l == top]]
+
+
+class LaneBatch:
+    """Planets in several batches ("lanes") solved side by side on one GPU, one host thread
+    per lane.
+
+    A batch solves its planets in lockstep: every Krylov iteration runs every level's
+    launches until its slowest planet converges, and the coarse levels' launches cost their
+    latency however few planets are still running. Planets that converge much more slowly
+    than the rest therefore run better in a lane of their own, concurrently with the
+    others. `lanes`: lists of planet indices covering every planet once (default:
+    `default_lanes`). The same calls as `Batch`, with per-lane tunings."""
+
+    def __init__(self, meshes: list[PlanetMesh], lanes: list[list[int]] | None = None):
+        from concurrent.futures import ThreadPoolExecutor
+
+        self.meshes = list(meshes)
+        self.lanes = [list(l) for l in (lanes if lanes is not None else default_lanes(self.meshes))]
+        if sorted(i for l in self.lanes for i in l) != list(range(len(self.meshes))) or any(not l for l in self.lanes):
+            raise ValueError("lanes must cover every planet exactly once")
+        self.batches = [Batch([self.meshes[i] for i in lane]) for lane in self.lanes]
+        self._pool = ThreadPoolExecutor(max_workers=len(self.lanes) - 1) if len(self.lanes) > 1 else None
+        self.concurrent = True    # False: the lanes one after another (e.g. while a profile records)
+
+    def close(self) -> None:
+        if self._pool is not None:
+            self._pool.shutdown()
+            self._pool = None
+
+    def _pick(self, value, lane):
+        """A per-planet list restricted to a lane; scalars, None and "stored" pass through."""
+        if value is None or isinstance(value, str):
+            return value
+        if isinstance(value, (list, tuple)) or np.ndim(value) > 0:
+            return [value[i] for i in lane]
+        return value
+
+    def _run(self, fn):
+        """fn(k) for every lane k, lanes 1.. on worker threads, lane 0 here."""
+        if self._pool is None or not self.concurrent:
+            return [fn(k) for k in range(len(self.lanes))]
+        futures = [self._pool.submit(fn, k) for k in range(1, len(self.lanes))]
+        first = fn(0)
+        return [first] + [f.result() for f in futures]
+
+    def set_edge_conductance(self, edge_conductance) -> None:
+        for lane, b in zip(self.lanes, self.batches):
+            b.set_edge_conductance(self._pick(edge_conductance, lane))
+
+    def autotune(self, t0, sources, heat_capacity, dt, conductance=None, edge_conductance=None, **options) -> list:
+        """Each lane tuned on its own (one after another, so the trial timings are clean)."""
+        return [b.autotune(self._pick(t0, lane), self._pick(sources, lane), self._pick(heat_capacity, lane),
+                           self._pick(dt, lane), conductance=self._pick(conductance, lane),
+                           edge_conductance=self._pick(edge_conductance, lane), **options)
+                for lane, b in zip(self.lanes, self.batches)]
+
+    @property
+    def tuning(self) -> list:
+        return [b.tuning for b in self.batches]
+
+    def set_tuning(self, tunings) -> None:
+        for b, t in zip(self.batches, tunings if tunings is not None else [None] * len(self.batches)):
+            b.set_tuning(t)
+
+    def transport_step(self, t0, sources, heat_capacity, dt, conductance=None, edge_conductance=None,
+                       out=None, transport_out=None, active=None, **options):
+        """One sub-step of every planet, the lanes concurrently; results in planet order."""
+        n = len(self.meshes)
+
+        def lane_step(k):
+            lane = self.lanes[k]
+            return self.batches[k].transport_step(
+                self._pick(t0, lane), self._pick(sources, lane), self._pick(heat_capacity, lane),
+                self._pick(dt, lane), conductance=self._pick(conductance, lane),
+                edge_conductance=self._pick(edge_conductance, lane), out=self._pick(out, lane),
+                transport_out=self._pick(transport_out, lane), active=self._pick(active, lane), **options)
+
+        results = self._run(lane_step)
+        outs, reps = [None] * n, [None] * n
+        for lane, (o, r) in zip(self.lanes, results):
+            for j, i in enumerate(lane):
+                outs[i], reps[i] = o[j], r[j]
+        return outs, reps
+
+
 # ---- column radiation ----------------------------------------------------------------
 
 def column_constants(**kw) -> capi.ColumnConstants:

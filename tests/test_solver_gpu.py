@@ -273,3 +273,26 @@ def test_stored_edge_conductance_equals_passed_arrays(meshes):
     out_d, _ = passed.transport_step([i.t0 for i in inputs], [i.source for i in inputs], 4e7, inputs[0].dt,
                                      edge_conductance=[2.0 * i.edge_conductance for i in inputs], precision="mixed")
     assert all(np.array_equal(a, b) for a, b in zip(out_c, out_d))
+
+
+def test_lane_batch_equals_one_batch(meshes):
+    """Planets split into lanes solved side by side give each planet the bits of the
+    one-batch solve (every result is the planet's own, whatever batch it is in)."""
+    import planet_game_gb300 as pg
+    from planet_game_gb300 import workloads as W
+
+    specs = [(4, 3.3e6), (6, 8.1e6), (5, 6.0e6), (7, 5.0e6), (3, 7.0e6), (7, 4.4e6)]
+    ms = [meshes(l, r) for l, r in specs]
+    inputs = [W.step_inputs(m, seed=60 + i, edge_diffusivity=W.lognormal_edge_diffusivity(m.edge_count, 600 + i))
+              for i, m in enumerate(ms)]
+    lanes = pg.LaneBatch(ms)
+    assert sorted(map(sorted, lanes.lanes)) == [[0, 1, 2, 4], [3, 5]]   # the L7 planets apart
+    one = pg.Batch(ms)
+    args = ([i.t0 for i in inputs], [i.source for i in inputs], 4e7, inputs[0].dt)
+    kw = dict(edge_conductance=[i.edge_conductance for i in inputs], precision="mixed")
+    a, ra = lanes.transport_step(*args, **kw)
+    b, rb = one.transport_step(*args, **kw)
+    for x, y, p, q in zip(a, b, ra, rb):
+        assert p.status == 0 and p.iterations == q.iterations
+        assert np.array_equal(x, y)
+    lanes.close()
