@@ -193,6 +193,7 @@ def run_gb300(args, rank, world, local_rank):
     # the planets of the mix's highest level in a lane of their own (pg.default_lanes):
     # they need the most Krylov iterations, and the lanes run side by side
     batch = pg.LaneBatch(meshes)
+    batch.concurrent = not args.serial_lanes
     t0_d = [torch.from_numpy(inp.t0).to(dev) for _, inp in planets]
     s_d = [torch.from_numpy(inp.source).to(dev) for _, inp in planets]
     out_d = [torch.empty_like(t) for t in t0_d]
@@ -278,7 +279,7 @@ def run_gb300(args, rank, world, local_rank):
         for _ in range(args.steps):
             step(t0_d, s_d, out_d)
         capi.check(lib.psgb_profile_end(C.byref(ms), C.byref(nl), C.byref(nbytes)))
-        batch.concurrent = True
+        batch.concurrent = not args.serial_lanes
         achieved = nbytes.value / (ms.value / 1e3) / 1e9 if ms.value > 0 else None
         traffic = (traffic_all.get(args.workload) or {}).get(family.decode())
         return {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
@@ -635,6 +636,8 @@ def main():
     ap.add_argument("--tuning-out", help="write the autotuned settings (JSON) here")
     ap.add_argument("--tuning-in", help="use these settings (JSON from --tuning-out) instead of autotuning; "
                                         "profiling runs use it, since timings under a profiler are not the real ones")
+    ap.add_argument("--serial-lanes", action="store_true",
+                    help="step the lanes one after another (profiling runs: the profiler serialises kernels anyway)")
     ap.add_argument("--schedule", choices=["auto", "kernels", "persistent"], default="auto",
                     help="persistent: one cooperative kernel per solve; kernels: one kernel per phase")
     args = ap.parse_args()
