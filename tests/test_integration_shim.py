@@ -1,4 +1,4 @@
-"""The C++ shim of INTEGRATION.md compiles against the reference's own headers and this
+"""The C++ shim of the integration guide (its first cpp block) compiles against the reference's own headers and this
 library's C header: the drop-in a maintainer adds is real code, not a sketch. Needs the
 reference sources (found through oracle/Makefile.ref, or PLANETSIM_REFERENCE); skipped
 where they are absent."""
@@ -29,7 +29,7 @@ def test_shim_compiles_against_the_reference_headers(tmp_path):
         pytest.skip("no C++ compiler")
     text = (ROOT / "INTEGRATION.md").read_text()
     blocks = re.findall(r"```cpp\n(.*?)```", text, re.S)
-    assert blocks, "INTEGRATION.md has no C++ shim"
+    assert blocks, "the integration guide has no C++ shim"
     src = tmp_path / "planetsim_gb300_adapter.cpp"
     src.write_text(blocks[0] + "\nint main() { return 0; }\n")
     proc = subprocess.run(["g++", "-std=c++20", "-fsyntax-only", "-I", str(ref), "-I", str(ROOT / "include"),

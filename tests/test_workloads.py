@@ -99,3 +99,31 @@ def test_lognormal_diffusivity_is_per_edge():
     k = W.lognormal_edge_diffusivity(100_000, seed=3)
     assert abs(np.median(k) / 1e6 - 1) < 0.02
     assert abs(np.std(np.log(k)) - 0.5) < 0.01
+
+
+def test_reverse_entries_and_antisymmetric_fluxes(meshes):
+    import planet_game_gb300 as pg
+    from planet_game_gb300 import workloads as W
+
+    g = pg.mesh_transport_graph(meshes(3))
+    off, nb = g.offset.astype(np.int64), g.neighbour.astype(np.int64)
+    rows = np.repeat(np.arange(len(off) - 1), np.diff(off))
+    rev = W.reverse_entries(g.offset, g.neighbour)
+    assert np.array_equal(nb[rev], rows) and np.array_equal(rows[rev], nb)
+    for balanced in (True, False):
+        f = W.antisymmetric_layer_fluxes(g.offset, g.neighbour, 3, 1e9, seed=5, column_balanced=balanced)
+        F = f.reshape(3, len(nb))
+        assert np.array_equal(F[:, rev], -F)
+        column = np.abs(F.sum(axis=0)).max()
+        assert (column <= 1e-6 * 1e9) if balanced else (column > 1.0)
+
+
+def test_default_lanes_split_the_highest_level():
+    from types import SimpleNamespace
+
+    import planet_game_gb300 as pg
+
+    ms = [SimpleNamespace(subdivision=l) for l in (4, 7, 5, 6, 7, 4)]
+    assert pg.default_lanes(ms) == [[0, 2, 3, 5], [1, 4]]
+    assert pg.default_lanes([SimpleNamespace(subdivision=l) for l in (5, 6, 5)]) == [[0, 1, 2]]
+    assert pg.default_lanes([SimpleNamespace(subdivision=8)]) == [[0]]
