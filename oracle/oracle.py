@@ -64,6 +64,15 @@ def lib() -> C.CDLL:
         for name in ("orc_gradient_f64", "orc_gradient_f32"):
             getattr(L, name).argtypes = [P, P, P, P]
         L.orc_diffusion_source.argtypes = [P, C.c_double, P, P]
+        L.orc_ilu_new.restype = P
+        L.orc_ilu_new.argtypes = [C.c_uint64, P, P, P, P, P, C.c_uint64, C.c_double]
+        L.orc_ilu_zero_pivot.restype = C.c_int
+        L.orc_ilu_zero_pivot.argtypes = [P]
+        L.orc_ilu_solve.argtypes = [P, C.c_uint64, P]
+        L.orc_ilu_free.argtypes = [P]
+        L.orc_advection_source.argtypes = [C.c_uint64, P, P, P, C.c_uint64, P, P, P, P, P, P, P]
+        L.orc_solve_implicit_tracer.argtypes = [C.c_uint64, P, P, C.c_uint64, P, P, C.c_double, P, P, C.c_double,
+                                                C.c_double, C.c_int, P, P]
         _lib = L
     return _lib
 
@@ -218,3 +227,58 @@ def column_radiation(constants, temperature, humidity, cloud, ts, ps):
 
 def saturation_specific_humidity(t, p):
     return lib().orc_saturation_specific_humidity(float(t), float(p))
+
+
+# ---- non-symmetric transport (nonsym_oracle.cpp) ------------------------------------
+
+def _u32(a):
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+class OracleIlu:
+    """IncompleteLU (incomplete_lu.cpp:33-152): block ILU(0), factored at construction."""
+
+    def __init__(self, offset, neighbour, diagonal, off, block_start, scale: float = 1.0):
+        self._keep = [_u32(offset), _u32(neighbour), _f64(diagonal), _f64(off), _u32(block_start)]
+        o, nb, d, f, bs = self._keep
+        self.rows = len(d)
+        self._h = C.c_void_p(lib().orc_ilu_new(self.rows, _p(o), _p(nb), _p(d), _p(f), _p(bs), len(bs) - 1, scale))
+        self.zero_pivot = bool(lib().orc_ilu_zero_pivot(self._h))
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().orc_ilu_free(self._h)
+            self._h = None
+
+    def solve(self, x):
+        y = np.array(x, dtype=np.float64, copy=True)
+        lib().orc_ilu_solve(self._h, self.rows, _p(y))
+        return y
+
+
+def advection_source(offset, neighbour, area, layers, conductance, outflow, latent, mean, energy):
+    """advection_diffusion_source (heat_transport.cpp:774-815): (H_eddy, H_advective)."""
+    o, nb = _u32(offset), _u32(neighbour)
+    n = len(o) - 1
+    eddy, adv = np.empty(n), np.empty(n)
+    lib().orc_advection_source(n, _p(o), _p(nb), _p(_f64(area)), layers, _p(_f64(conductance)),
+                               _p(_f64(outflow)), _p(_f64(latent)), _p(_f64(mean)), _p(_f64(energy)), _p(eddy),
+                               _p(adv))
+    return eddy, adv
+
+
+def solve_implicit_tracer(offset, neighbour, layers, conductance, outflow, heat_capacity, layer_mass, tracer, dt,
+                          tolerance=1e-12, max_iterations=2000):
+    """solve_implicit_tracer (heat_transport.cpp:901-1081): the new tracer (layer-major) and
+    (iterations, relative residual, clipped kg, column divergence)."""
+    o, nb = _u32(offset), _u32(neighbour)
+    n = len(o) - 1
+    keep = [_f64(conductance), _f64(outflow), _f64(layer_mass), _f64(tracer)]
+    out, stats = np.empty(layers * n), np.empty(4)
+    lib().orc_solve_implicit_tracer(n, _p(o), _p(nb), layers, _p(keep[0]), _p(keep[1]), heat_capacity, _p(keep[2]),
+                                    _p(keep[3]), dt, tolerance, max_iterations, _p(out), _p(stats))
+    return out, stats

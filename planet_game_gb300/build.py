@@ -99,11 +99,11 @@ def build_library(force: bool = False, verbose_ptxas: bool = False) -> Path:
 
 def build_oracle(force: bool = False) -> Path:
     """Compile the CPU oracle (test infrastructure) into oracle/lib/."""
-    src = ORACLE_DIR / "planetsim_oracle.cpp"
+    srcs = [ORACLE_DIR / "planetsim_oracle.cpp", ORACLE_DIR / "nonsym_oracle.cpp"]
     ORACLE_LIB.parent.mkdir(parents=True, exist_ok=True)
-    if force or _stale(ORACLE_LIB, [src]):
+    if force or _stale(ORACLE_LIB, srcs):
         tmp = ORACLE_LIB.with_suffix(".so.tmp")
-        _run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-pthread", str(src),
+        _run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-pthread", *map(str, srcs),
               "-o", str(tmp)])
         os.replace(tmp, ORACLE_LIB)
     return ORACLE_LIB

@@ -137,3 +137,59 @@ def test_nonlinear_newton_driver_bit_identical(L4, case, factor):
     assert np.array_equal(stats, g[f"stats{key}"])
     assert stats[2] <= 1e-6 and abs(stats[3]) <= 1e-13 * stats[4] and stats[5] <= 0.0
     assert np.all(mean[::7] <= 273.15)
+
+
+# ---- the non-symmetric pieces against the reference (tests/golden/nonsym.npz) ---------
+
+def _graph(planet):
+    import planet_game_gb300 as pg
+
+    g = pg.mesh_transport_graph(planet)
+    return g.offset, g.neighbour, g.area_m2, g.weight
+
+
+def _full_fluxes(offset, neighbour, half, layers):
+    from planet_game_gb300 import workloads as W
+
+    off, nb = offset.astype(np.int64), neighbour.astype(np.int64)
+    rows = np.repeat(np.arange(len(off) - 1), np.diff(off))
+    upper = np.nonzero(rows < nb)[0]
+    rev = W.reverse_entries(offset, neighbour)
+    out = np.zeros((layers, len(nb)))
+    out[:, upper] = half
+    out[:, rev[upper]] = -half
+    return out.ravel()
+
+
+def test_oracle_block_ilu_bit_identical_to_the_reference(meshes):
+    g = golden("nonsym.npz")
+    off, nb, _, _ = _graph(meshes(3))
+    lu = O.OracleIlu(off, nb, g["ilu_diag"], g["ilu_off"], g["ilu_blocks"])
+    assert not lu.zero_pivot
+    assert np.array_equal(lu.solve(g["ilu_x"]), g["ilu_y"])
+
+
+def test_oracle_advection_source_bit_identical_to_the_reference(meshes):
+    g = golden("nonsym.npz")
+    off, nb, area, weight = _graph(meshes(3))
+    flux = _full_fluxes(off, nb, g["flux"], 3)
+    for tag, latent in (("dry", None), ("latent", g["src_latent"])):
+        eddy, adv = O.advection_source(off, nb, area, 3, 0.5 * 6.371e6 ** 2 * weight, flux, latent, g["src_mean"],
+                                       g["src_energy"])
+        assert np.array_equal(eddy, g[f"src_eddy_{tag}"]) and np.array_equal(adv, g[f"src_adv_{tag}"])
+
+
+@pytest.mark.parametrize("tag", ["bal", "div", "eddy", "l3"])
+def test_oracle_tracer_bit_identical_to_the_reference(meshes, tag):
+    import planet_game_gb300 as pg
+
+    g = golden("nonsym.npz")
+    layers = int(g[f"tr_{tag}_layers"])
+    planet = pg.agglomerated_transport_graph(3, 6.371e6) if int(g[f"tr_{tag}_agg"]) else meshes(3)
+    off, nb, area, _ = _graph(planet)
+    flux = _full_fluxes(off, nb, g[f"tr_{tag}_flux"], layers)
+    cond = np.full(len(nb), float(g[f"tr_{tag}_eddy"]))
+    mass = area * 100000.0 / (9.81 * layers)
+    out, stats = O.solve_implicit_tracer(off, nb, layers, cond, flux, 1004.64, mass, g[f"tr_{tag}_in"], 2.63e6)
+    assert np.array_equal(out, g[f"tr_{tag}_out"])
+    assert np.array_equal(stats, g[f"tr_{tag}_stats"])
