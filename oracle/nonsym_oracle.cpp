@@ -6,10 +6,14 @@
 //   advection_diffusion_source     sim/planet/surface/heat_transport.cpp:774-815
 //   right-preconditioned BiCGSTAB  sim/planet/surface/heat_transport.cpp:823-897
 //   solve_implicit_tracer          sim/planet/surface/heat_transport.cpp:901-1081
+//   solve_implicit_advection_diffusion  sim/planet/surface/heat_transport.cpp:1083-1318, with the
+//                                  column of tests/unit/test_advection_diffusion.cpp:73-104
 // Same operations in the same order, sums over the reference's deterministic blocks
 // (sequential inside a block, then the blocks in order), -ffp-contract=off: the results
 // are the reference's bits. Parity pinning: tests/test_oracle_golden.py checks each entry
 // point against the reference's own outputs (tests/golden/nonsym.npz).
+#include "oracle_abi.hpp"
+
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -310,6 +314,184 @@ void orc_solve_implicit_tracer(std::uint64_t nodes, const std::uint32_t* offset,
     stats[1] = rhs_norm > 0.0 ? std::sqrt(residual_norm / rhs_norm) : 0.0;
     stats[2] = clipped;
     stats[3] = column_divergence;
+}
+
+
+// solve_implicit_advection_diffusion with the reference test's column: a x + r x^4 = b + h
+// (solve_column_surface's dry Newton, column_step.cpp:254-276), s_l = c_p x (1 + eps_l) +
+// phi_l. stats: newton, linear iterations, consistency, sum, absolute, eddy absolute,
+// advective absolute.
+void orc_solve_implicit_advection_diffusion(const orc_graph* gp, std::uint64_t layers, const double* conductance,
+                                            const double* outflow, const double* latent, double heat_capacity,
+                                            double a, const double* b, const double* epsilon,
+                                            const double* geopotential, const double* floor, double cg_tolerance,
+                                            double newton_tolerance, double* source_out, double* mean_out,
+                                            double* energy_out, double* stats) {
+    const std::size_t n = gp->n, entries = gp->offset[n], L = layers;
+    const std::uint32_t* offset = gp->offset;
+    const std::uint32_t* neighbour = gp->neighbour;
+    const double* area = gp->area;
+    const double radiative = 0.75 * 0.97 * 5.670374419e-8;
+    struct Iterate {
+        std::vector<double> source, mean, slope, energy, energy_slope, residual;
+        double merit = 0.0;
+    };
+    const auto respond = [&](Iterate& at) {
+        at.mean.assign(n, 0.0);
+        at.slope.assign(n, 0.0);
+        at.energy.assign(L * n, 0.0);
+        at.energy_slope.assign(L * n, 0.0);
+        for (std::size_t i = 0; i < n; ++i) {
+            const double rhs = b[i] + at.source[i];
+            double x = std::min(rhs / a, std::sqrt(std::sqrt(rhs / radiative)));
+            for (int it = 0; it < 10; ++it) {
+                const double x3 = x * x * x;
+                const double value = a * x + radiative * x3 * x - rhs;
+                const double slope = a + 4.0 * radiative * x3;
+                const double step = value / slope;
+                x -= step;
+                if (std::abs(step) <= 4.0 * std::numeric_limits<double>::epsilon() * x) break;
+            }
+            at.mean[i] = x;
+            at.slope[i] = 1.0 / (a + 4.0 * radiative * x * x * x + 0.0);
+            for (std::size_t l = 0; l < L; ++l) {
+                at.energy[l * n + i] = heat_capacity * x * (1.0 + epsilon[l]) + geopotential[l];
+                at.energy_slope[l * n + i] = heat_capacity * at.slope[i] * (1.0 + epsilon[l]);
+            }
+        }
+    };
+    std::vector<double> eddy(n, 0.0), advective(n, 0.0);
+    const auto source_of = [&](const Iterate& at) {
+        orc_advection_source(n, offset, neighbour, area, L, conductance, outflow, latent, at.mean.data(),
+                             at.energy.data(), eddy.data(), advective.data());
+    };
+    const auto evaluate = [&](Iterate& at) {
+        respond(at);
+        source_of(at);
+        at.residual.assign(n, 0.0);
+        double merit = 0.0;
+        for (std::size_t begin = 0; begin < n; begin += 256) {
+            double part = 0.0;
+            for (std::size_t i = begin; i < std::min(n, begin + 256); ++i) {
+                at.residual[i] = at.source[i] - (eddy[i] + advective[i]);
+                part += area[i] * at.residual[i] * at.residual[i];
+            }
+            merit = merit + part;
+        }
+        at.merit = merit;
+    };
+    const auto max_abs = [&](const std::vector<double>& v) {
+        double largest = 0.0;
+        for (const double x : v) largest = std::max(largest, std::abs(x));
+        return largest;
+    };
+    Iterate current, trial;
+    current.source.assign(n, 0.0);
+    for (std::size_t i = 0; i < n; ++i) current.source[i] = std::max(0.0, floor[i]);
+    evaluate(current);
+    std::vector<std::uint32_t> blocks{0};
+    for (std::size_t begin = 0; begin < n; begin += 256) blocks.push_back(static_cast<std::uint32_t>(std::min(n, begin + 256)));
+    std::vector<double> diagonal(n, 0.0), off(entries, 0.0), sym_diag(n, 0.0), sym_off(entries, 0.0), rhs(n, 0.0),
+        delta(n, 0.0), scaled(n, 0.0), leftover(n, 0.0);
+    void* multigrid = orc_hierarchy_new(gp);
+    int newton = 0, linear = 0, non_monotone = 0;
+    const int max_newton = 30, max_halvings = 12, max_non_monotone = 4, max_cg = 2000;
+    const double rounding_floor = 1e-3, max_growth = 100.0;
+    for (int iteration = 0; iteration < max_newton; ++iteration) {
+        if (max_abs(current.residual) <= newton_tolerance) break;
+        for (std::size_t i = 0; i < n; ++i) {
+            const double inverse_area = 1.0 / area[i];
+            double own = 0.0;
+            for (std::size_t k = offset[i]; k < offset[i + 1]; ++k) {
+                const std::size_t j = neighbour[k];
+                const double g = conductance[k];
+                own -= g * current.slope[i];
+                double nb = g * current.slope[j];
+                for (std::size_t l = 0; l < L; ++l) {
+                    const double out = outflow[l * entries + k];
+                    if (out > 0.0) {
+                        own -= out * current.energy_slope[l * n + i];
+                    } else {
+                        nb -= out * current.energy_slope[l * n + j];
+                    }
+                }
+                off[k] = -nb * inverse_area;
+            }
+            diagonal[i] = 1.0 - own * inverse_area;
+            rhs[i] = -current.residual[i];
+        }
+        const Ilu factor(n, offset, neighbour, diagonal.data(), off.data(), blocks.data(), blocks.size() - 1, 1.0);
+        const auto apply = [&](const std::vector<double>& x, std::vector<double>& y) {
+            for (std::size_t i = 0; i < n; ++i) {
+                double sum = diagonal[i] * x[i];
+                for (std::size_t k = offset[i]; k < offset[i + 1]; ++k) sum += off[k] * x[neighbour[k]];
+                y[i] = sum;
+            }
+        };
+        for (std::size_t i = 0; i < n; ++i) {
+            double sum = 0.0;
+            for (std::size_t k = offset[i]; k < offset[i + 1]; ++k) {
+                sum += conductance[k];
+                sym_off[k] = -conductance[k];
+            }
+            sym_diag[i] = area[i] / std::max(current.slope[i], 1.0e-12) + sum;
+        }
+        orc_hierarchy_set_matrix(multigrid, sym_diag.data(), sym_off.data());
+        const auto precondition = [&](const std::vector<double>& x, std::vector<double>& y) {
+            for (std::size_t i = 0; i < n; ++i) scaled[i] = area[i] * x[i];
+            y.assign(n, 0.0);
+            orc_vcycle_sgs(multigrid, scaled.data(), y.data());
+            for (std::size_t i = 0; i < n; ++i) y[i] /= std::max(current.slope[i], 1.0e-12);
+            apply(y, leftover);
+            for (std::size_t i = 0; i < n; ++i) leftover[i] = x[i] - leftover[i];
+            factor.solve(leftover);
+            for (std::size_t i = 0; i < n; ++i) y[i] += leftover[i];
+        };
+        linear += bicgstab(n, 256, apply, precondition, rhs, delta, cg_tolerance, max_cg);
+        double step = 1.0;
+        bool accepted = false;
+        for (int halving = 0;; ++halving) {
+            trial.source.assign(n, 0.0);
+            for (std::size_t i = 0; i < n; ++i) trial.source[i] = std::max(current.source[i] + step * delta[i], floor[i]);
+            evaluate(trial);
+            if (trial.merit < current.merit) {
+                accepted = true;
+                break;
+            }
+            if (halving == max_halvings) {
+                if (max_abs(current.residual) > rounding_floor && non_monotone < max_non_monotone) {
+                    ++non_monotone;
+                    for (std::size_t i = 0; i < n; ++i) trial.source[i] = std::max(current.source[i] + delta[i], floor[i]);
+                    evaluate(trial);
+                    accepted = std::isfinite(trial.merit) && trial.merit <= max_growth * current.merit;
+                }
+                break;
+            }
+            step *= 0.5;
+        }
+        if (!accepted) break;
+        std::swap(current, trial);
+        ++newton;
+    }
+    orc_hierarchy_free(multigrid);
+    source_of(current);
+    double sum = 0.0, absolute = 0.0, eddy_absolute = 0.0, advective_absolute = 0.0;
+    for (std::size_t i = 0; i < n; ++i) {
+        source_out[i] = eddy[i] + advective[i];
+        sum += area[i] * source_out[i];
+        absolute += area[i] * std::abs(source_out[i]);
+        eddy_absolute += area[i] * std::abs(eddy[i]);
+        advective_absolute += area[i] * std::abs(advective[i]);
+    }
+    std::copy(current.mean.begin(), current.mean.end(), mean_out);
+    std::copy(current.energy.begin(), current.energy.end(), energy_out);
+    stats[0] = newton;
+    stats[1] = linear;
+    stats[2] = max_abs(current.residual);
+    stats[3] = sum;
+    stats[4] = absolute;
+    stats[5] = eddy_absolute;
+    stats[6] = advective_absolute;
 }
 
 }  // extern "C"

@@ -73,6 +73,8 @@ def lib() -> C.CDLL:
         L.orc_advection_source.argtypes = [C.c_uint64, P, P, P, C.c_uint64, P, P, P, P, P, P, P]
         L.orc_solve_implicit_tracer.argtypes = [C.c_uint64, P, P, C.c_uint64, P, P, C.c_double, P, P, C.c_double,
                                                 C.c_double, C.c_int, P, P]
+        L.orc_solve_implicit_advection_diffusion.argtypes = [P, C.c_uint64, P, P, P, C.c_double, C.c_double, P, P,
+                                                             P, P, C.c_double, C.c_double, P, P, P, P]
         _lib = L
     return _lib
 
@@ -282,3 +284,18 @@ def solve_implicit_tracer(offset, neighbour, layers, conductance, outflow, heat_
     lib().orc_solve_implicit_tracer(n, _p(o), _p(nb), layers, _p(keep[0]), _p(keep[1]), heat_capacity, _p(keep[2]),
                                     _p(keep[3]), dt, tolerance, max_iterations, _p(out), _p(stats))
     return out, stats
+
+
+def solve_implicit_advection_diffusion(om: "OracleMesh", layers, conductance, outflow, latent, heat_capacity, a, b,
+                                       epsilon, geopotential, floor, cg_tolerance=1e-6, newton_tolerance=1e-6):
+    """solve_implicit_advection_diffusion (heat_transport.cpp:1083-1318) with the reference
+    test's column (test_advection_diffusion.cpp:73-104): (H, theta, s, stats), stats =
+    (newton, linear, consistency, sum, absolute, eddy absolute, advective absolute)."""
+    n = om.n
+    keep = [_f64(conductance), _f64(outflow), _f64(latent), _f64(b), _f64(epsilon), _f64(geopotential), _f64(floor)]
+    src, mean, energy, stats = np.empty(n), np.empty(n), np.empty(layers * n), np.empty(7)
+    lib().orc_solve_implicit_advection_diffusion(C.byref(om.graph), layers, _p(keep[0]), _p(keep[1]), _p(keep[2]),
+                                                 heat_capacity, a, _p(keep[3]), _p(keep[4]), _p(keep[5]),
+                                                 _p(keep[6]), cg_tolerance, newton_tolerance, _p(src), _p(mean),
+                                                 _p(energy), _p(stats))
+    return src, mean, energy, stats

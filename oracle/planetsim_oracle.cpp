@@ -24,6 +24,8 @@
 //   BiCGSTAB                     sim/planet/surface/heat_transport.cpp:823-897
 //   column radiation             sim/planet/atmosphere/atmosphere_column.hpp:39-143, 589-634
 //   saturation                   sim/planet/atmosphere/saturation.cpp:9-54
+#include "oracle_abi.hpp"
+
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -431,15 +433,6 @@ double saturation_vapour_pressure(double t) {
 }  // namespace
 
 extern "C" {
-
-struct orc_graph {
-    std::uint64_t n;
-    const std::uint32_t* offset;
-    const std::uint32_t* neighbour;
-    const double* weight;
-    const double* weight_sum;
-    const double* area;
-};
 
 struct orc_mesh {
     std::uint64_t cells, edges;

@@ -101,7 +101,7 @@ def build_oracle(force: bool = False) -> Path:
     """Compile the CPU oracle (test infrastructure) into oracle/lib/."""
     srcs = [ORACLE_DIR / "planetsim_oracle.cpp", ORACLE_DIR / "nonsym_oracle.cpp"]
     ORACLE_LIB.parent.mkdir(parents=True, exist_ok=True)
-    if force or _stale(ORACLE_LIB, srcs):
+    if force or _stale(ORACLE_LIB, srcs + [ORACLE_DIR / "oracle_abi.hpp"]):
         tmp = ORACLE_LIB.with_suffix(".so.tmp")
         _run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-pthread", *map(str, srcs),
               "-o", str(tmp)])

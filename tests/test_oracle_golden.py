@@ -193,3 +193,18 @@ def test_oracle_tracer_bit_identical_to_the_reference(meshes, tag):
     out, stats = O.solve_implicit_tracer(off, nb, layers, cond, flux, 1004.64, mass, g[f"tr_{tag}_in"], 2.63e6)
     assert np.array_equal(out, g[f"tr_{tag}_out"])
     assert np.array_equal(stats, g[f"tr_{tag}_stats"])
+
+
+@pytest.mark.parametrize("tag", ["diff", "adv", "lat"])
+def test_oracle_advection_diffusion_bit_identical_to_the_reference(meshes, tag):
+    g = golden("nonsym.npz")
+    m = meshes(3)
+    off, nb, area, weight = _graph(m)
+    flux = _full_fluxes(off, nb, g["flux"], 3) if tag != "diff" else np.zeros(3 * len(nb))
+    om = O.OracleMesh(m.arrays())
+    src, mean, energy, stats = O.solve_implicit_advection_diffusion(
+        om, 3, 0.5 * 6.371e6 ** 2 * weight, flux, g["ad_lat_latent"] if tag == "lat" else None, 1004.64,
+        float(g["ad_a"]), g["ad_b"], g["ad_eps"], g["ad_phi"], g["ad_floor"])
+    assert np.array_equal(stats, g[f"ad_{tag}_stats"])
+    assert np.array_equal(src, g[f"ad_{tag}_source"]) and np.array_equal(mean, g[f"ad_{tag}_mean"])
+    assert np.array_equal(energy, g[f"ad_{tag}_energy"])
