@@ -10,7 +10,10 @@ vectors from the reference, tests/golden/make_golden.py --nonsym):
   field (both solve to a 1e-12 relative residual, reduced in a different order);
 - solve_implicit_advection_diffusion on the L3 graph (diffusion only, advection, advection
   with latent heat): the reference test's gates and the reference's H to 1e-5 W/m^2
-  (both stop at 1e-6 W/m^2); a device response gives the host response's bits."""
+  (both stop at 1e-6 W/m^2); a device response gives the host response's bits;
+- at L5 (tracer on the agglomerated graph with 6 layers, the coupled solve on the mesh
+  graph) against the oracle's restatements, themselves pinned bit-for-bit to the
+  reference."""
 import numpy as np
 import pytest
 
@@ -187,3 +190,46 @@ def test_invalid_inputs_are_refused(planets):
         pg.solve_implicit_advection_diffusion(p, tr, g["ad_floor"], lambda h: column(g, h))
     with pytest.raises(ValueError):
         pg.solve_implicit_tracer(p, tr, np.ones(p.cell_count + 1), np.zeros(3 * p.cell_count), 1.0)
+
+
+def test_tracer_and_coupled_solve_against_the_oracle_at_l5():
+    """Larger cases against the oracle's restatement (pinned bit-for-bit to the reference):
+    the tracer on the L5 mesh's agglomerated graph with 6 layers, the coupled solve on the
+    L5 graph; the tracer field to 1e-9, the coupled H to 1e-5 W/m^2."""
+    import planet_game_gb300 as pg
+    from oracle import oracle as O
+    from planet_game_gb300 import workloads as W
+
+    p = pg.agglomerated_transport_graph(5, RADIUS)
+    g = pg.mesh_transport_graph(p)
+    layers = 6
+    flux = W.antisymmetric_layer_fluxes(g.offset, g.neighbour, layers, 2e9, seed=51, column_balanced=False)
+    cond = np.full(len(g.neighbour), 2e8)
+    mass = g.area_m2 * 100000.0 / (9.81 * layers)
+    c0 = W.tracer_field(layers * p.cell_count, seed=52)
+    r = pg.solve_implicit_tracer(p, pg.AdvectionDiffusion(layers, cond, flux, CP), mass, c0, 2.63e6)
+    ref, stats = O.solve_implicit_tracer(g.offset, g.neighbour, layers, cond, flux, CP, mass, c0, 2.63e6)
+    assert r.relative_residual <= 1e-10 and stats[1] <= 1e-10
+    assert np.max(np.abs(r.tracer - ref)) <= 1e-9 * np.max(np.abs(ref))
+
+    m = pg.make_icosphere(5, RADIUS)
+    g5 = pg.mesh_transport_graph(m)
+    flux5 = W.antisymmetric_layer_fluxes(g5.offset, g5.neighbour, 3, 5e9, seed=53, column_balanced=True)
+    cond5 = 0.5 * RADIUS * RADIUS * g5.weight
+    a, radiative = 3.0e5 / (30.0 * 86400.0), 0.75 * 0.97 * 5.670374419e-8
+    b, floor = W.quartic_column(a, radiative, m.cell_count, seed=54)
+    eps, phi = np.array([0.0, -0.08, -0.16]), np.array([3.0e4, 4.5e4, 7.0e4])
+
+    def column(h):
+        q = pg.QuarticResponse(a, b, radiative, hold_stride=0)
+        x, s = (v.cpu().numpy() for v in pg.quartic_response(q, h))
+        return x, s, np.concatenate([CP * x * (1.0 + e) + f for e, f in zip(eps, phi)]), \
+            np.concatenate([CP * s * (1.0 + e) for e in eps])
+
+    settings = {"cg_relative_tolerance": 1e-6, "newton_tolerance_W_m2": 1e-6}
+    got = pg.solve_implicit_advection_diffusion(m, pg.AdvectionDiffusion(3, cond5, flux5, CP), floor, column,
+                                                settings=settings)
+    src, _, _, ostats = O.solve_implicit_advection_diffusion(O.OracleMesh(m.arrays()), 3, cond5, flux5, None, CP, a,
+                                                             b, eps, phi, floor)
+    assert got.consistency_residual_W_m2 <= 1e-6 and ostats[2] <= 1e-6
+    assert np.max(np.abs(got.source_W_m2 - src)) <= 1e-5
