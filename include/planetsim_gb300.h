@@ -14,6 +14,13 @@
  * Each entry point names the reference interface it replaces; the C++ shim that
  * re-exports those interfaces with their original signatures is described with the
  * library's integration notes.
+ *
+ * Threads: different planets and different batches may be used from different host
+ * threads at once (each owns its device memory and private stream); calls on one planet,
+ * or on one batch, must not overlap.
+ *
+ * ABI version 2: psgb_planet_info and psgb_tuning grew fields (fine_cells; the coarse
+ * tail's spread and block count).
  */
 #ifndef PLANETSIM_GB300_H
 #define PLANETSIM_GB300_H
@@ -25,7 +32,7 @@
 extern "C" {
 #endif
 
-#define PSGB_ABI_VERSION 1
+#define PSGB_ABI_VERSION 2
 
 /* status codes */
 #define PSGB_OK 0

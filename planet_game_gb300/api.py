@@ -731,9 +731,18 @@ class LaneBatch:
         self.concurrent = True    # False: the lanes one after another (e.g. while a profile records)
 
     def close(self) -> None:
-        if self._pool is not None:
+        if getattr(self, "_pool", None) is not None:
             self._pool.shutdown()
             self._pool = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        self.close()
 
     def _pick(self, value, lane):
         """A per-planet list restricted to a lane; scalars, None and "stored" pass through."""
