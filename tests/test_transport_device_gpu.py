@@ -10,7 +10,9 @@ tests/golden/make_golden.py):
 - on an agglomerated L5 planet with the response per fine cell and group means on the
   GPU, it matches the reference's production-pattern solve to the same bars;
 - a device callback (torch on the device pointers) gives the same bits as the same
-  response through the host callback."""
+  response through the host callback;
+- the reference's P2 energy-balance gate (steady response ratio with and without
+  transport against lambda / (lambda + 6 D)), within 2% at L5."""
 import numpy as np
 import pytest
 
@@ -117,3 +119,34 @@ def test_device_callback_errors_reach_the_caller(meshes):
         pg.solve_implicit_transport(m, 1e12, np.zeros(m.cell_count), failing, device=True)
     with pytest.raises(ValueError):
         pg.solve_implicit_transport(m, 1e12, np.zeros(m.cell_count), pg.QuarticResponse(0.41, np.ones(5)))
+
+
+@pytest.mark.parametrize("D", [0.5, 2.0])
+def test_p2_response_matches_the_energy_balance_model(meshes, D):
+    """The reference's V4 gate restated for the transport solve (test_heat_transport_planet.cpp:
+    136-194): the steady response of quartic columns (a x + r x^4 = b + h around 250 K) to a
+    2% P2 anomaly of their forcing, with transport of conductance K = D R^2 and without, has
+    the amplitude ratio of the linear energy balance, lambda / (lambda + 6 D), lambda =
+    a + 4 r T0^3 (North, 1975): within 2% at L5 and closer than at L3."""
+    import planet_game_gb300 as pg
+
+    R, r, a, T0, anomaly = 6.371e6, 0.75 * 0.97 * 5.670374419e-8, 0.41, 250.0, 0.02
+    lam = a + 4.0 * r * T0 ** 3
+    expected = lam / (lam + 6.0 * D)
+    errors = []
+    for level in (3, 4, 5):
+        m = meshes(level)
+        arr = m.arrays()
+        mu = arr["center"][:, 2]
+        p2 = 0.5 * (3.0 * mu * mu - 1.0)
+        area = arr["area_m2"]
+        b = (a * T0 + r * T0 ** 4) * (1.0 + anomaly * p2)
+        q = pg.QuarticResponse(a, b, r, hold_stride=0)
+        alone = pg.quartic_response(q, np.zeros(m.cell_count))[0].cpu().numpy()
+        floor = a * 100.0 + r * 100.0 ** 4 - b
+        res = pg.solve_implicit_transport(m, D * R * R, floor, q, precision="fp64",
+                                          settings={"cg_relative_tolerance": 1e-10, "newton_tolerance_W_m2": 1e-9})
+        assert res.consistency_residual_W_m2 <= 1e-9
+        amplitude = lambda t: np.sum(area * t * p2) / np.sum(area * p2 * p2)   # noqa: E731
+        errors.append(abs(amplitude(res.mean_K) / amplitude(alone) - expected) / expected)
+    assert errors[-1] <= 0.02 and errors[-1] < errors[0]
