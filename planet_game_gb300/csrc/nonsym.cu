@@ -1057,9 +1057,10 @@ int psgb_advection_diffusion_source(psgb_planet* planet, const psgb_advection_di
                                     const double* mean_K, const double* energy_J_kg, double* eddy_W_m2,
                                     double* advective_W_m2, int memory, void* stream) {
     return guarded([&] {
-        psgb::require(planet != nullptr && mean_K != nullptr && (energy_J_kg != nullptr || transport->layers == 0) &&
-                          eddy_W_m2 != nullptr && advective_W_m2 != nullptr,
+        psgb::require(planet != nullptr && transport != nullptr && mean_K != nullptr && eddy_W_m2 != nullptr &&
+                          advective_W_m2 != nullptr,
                       "null argument");
+        psgb::require(energy_J_kg != nullptr || transport->layers == 0, "null argument");
         psgb::require_memory(memory);
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         psgb::NonsymContext& c = psgb::context(planet);

@@ -23,6 +23,10 @@ def _u32(a):
     return np.ascontiguousarray(a, dtype=np.uint32)
 
 
+def _count(a) -> int:
+    return int(a.numel()) if _is_torch(a) else int(np.size(a))
+
+
 class IncompleteLU:
     """Block ILU(0) of diagonal * scale + off (incomplete_lu.hpp:14-43), factored on the
     GPU at construction; `solve(x)` returns (LU)^-1 x. `offset`/`neighbour`: the
@@ -73,6 +77,14 @@ class AdvectionDiffusion:
     eddy_latent_W_m2: np.ndarray | None = None
     _keep: list = field(default_factory=list, repr=False)
 
+    def check(self, planet: PlanetMesh) -> None:
+        """The arrays' sizes against the planet's graph (the C ABI takes bare pointers)."""
+        entries, nodes = planet.directed_edge_count, planet.cell_count
+        if self.layers < 0 or _count(self.conductance_W_K) != entries or \
+                _count(self.outflow_kg_s) != self.layers * entries or \
+                (self.eddy_latent_W_m2 is not None and _count(self.eddy_latent_W_m2) != nodes):
+            raise ValueError("advection-diffusion inputs do not match the graph")
+
     def c_struct(self) -> capi.AdvectionDiffusion:
         g, o = _f64(self.conductance_W_K), _f64(self.outflow_kg_s)
         e = None if self.eddy_latent_W_m2 is None else _f64(self.eddy_latent_W_m2)
@@ -103,8 +115,11 @@ def _empty(transport: AdvectionDiffusion, n: int):
 def advection_diffusion_source(planet: PlanetMesh, transport: AdvectionDiffusion, mean_K, energy_J_kg):
     """advection_diffusion_source (heat_transport.hpp:168-175): (H_eddy, H_advective)."""
     n = planet.cell_count
+    transport.check(planet)
     ts = transport.c_struct()
     m, e = _f64(mean_K), _f64(energy_J_kg)
+    if _count(m) != n or _count(e) != transport.layers * n:
+        raise ValueError("advection-diffusion inputs do not match the graph")
     eddy, adv = _empty(transport, n), _empty(transport, n)
     mem, st = _memory(transport)
     _raise(capi.load().psgb_advection_diffusion_source(planet.handle, C.byref(ts), _ptr(m), _ptr(e), _ptr(eddy),
@@ -127,9 +142,10 @@ def solve_implicit_tracer(planet: PlanetMesh, transport: AdvectionDiffusion, lay
                           relative_tolerance: float = 1e-12, max_iterations: int = 2000) -> TracerTransportResult:
     """solve_implicit_tracer (heat_transport.hpp:222-226): tracer layer-major."""
     n = planet.cell_count
+    transport.check(planet)
     ts = transport.c_struct()
     mass, c0 = _f64(layer_mass_kg), _f64(tracer)
-    if len(mass) != n or len(c0) != transport.layers * n:
+    if _count(mass) != n or _count(c0) != transport.layers * n:
         raise ValueError("tracer transport inputs do not match the graph")
     out = _empty(transport, transport.layers * n)
     res = capi.TracerResult()
@@ -167,9 +183,12 @@ def solve_implicit_advection_diffusion(planet: PlanetMesh, transport: AdvectionD
     `response(nodes, layers, source, mean, slope, energy, energy_slope, stream)` on
     device pointers, enqueuing its work on `stream`."""
     n, L = planet.cell_count, transport.layers
+    transport.check(planet)
     ts = transport.c_struct()
     floor = _f64(source_floor_W_m2)
     initial = None if initial_source_W_m2 is None else _f64(initial_source_W_m2)
+    if _count(floor) != n or (initial is not None and _count(initial) != n):
+        raise ValueError("advection-diffusion inputs do not match the graph")
     if _is_torch(floor) != transport.on_device() or (initial is not None and _is_torch(initial) != _is_torch(floor)):
         raise ValueError("pass every array as numpy or every array as CUDA tensors")
     error: list[BaseException] = []

@@ -70,3 +70,24 @@ def test_level0_is_the_mesh_itself(planets, meshes):
 def test_plain_planet_has_no_groups(meshes):
     with pytest.raises(ValueError):
         meshes(2).group_of_cell()
+
+
+def test_nonsymmetric_inputs_are_checked_before_the_library(planets):
+    """The C ABI takes bare pointers: the Python layer refuses arrays of the wrong size."""
+    import numpy as np
+
+    import planet_game_gb300 as pg
+
+    p = planets[3]
+    E, n = p.directed_edge_count, p.cell_count
+    good = pg.AdvectionDiffusion(2, np.ones(E), np.zeros(2 * E))
+    good.check(p)
+    for bad in (pg.AdvectionDiffusion(2, np.ones(E - 1), np.zeros(2 * E)),
+                pg.AdvectionDiffusion(2, np.ones(E), np.zeros(E)),
+                pg.AdvectionDiffusion(2, np.ones(E), np.zeros(2 * E), eddy_latent_W_m2=np.zeros(n + 1))):
+        with pytest.raises(ValueError):
+            bad.check(p)
+    with pytest.raises(ValueError):
+        pg.solve_implicit_tracer(p, good, np.ones(n), np.ones(2 * n - 1), 1.0)
+    with pytest.raises(ValueError):
+        pg.advection_diffusion_source(p, good, np.ones(n), np.ones(n))
