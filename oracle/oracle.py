@@ -64,6 +64,8 @@ def lib() -> C.CDLL:
         for name in ("orc_gradient_f64", "orc_gradient_f32"):
             getattr(L, name).argtypes = [P, P, P, P]
         L.orc_diffusion_source.argtypes = [P, C.c_double, P, P]
+        L.orc_solve_implicit_transport_group_quartic.argtypes = [P, C.c_uint64, P, P, C.c_double, C.c_double, P, P,
+                                                                 C.c_double, C.c_double, P, P, P]
         L.orc_ilu_new.restype = P
         L.orc_ilu_new.argtypes = [C.c_uint64, P, P, P, P, P, C.c_uint64, C.c_double]
         L.orc_ilu_zero_pivot.restype = C.c_int
@@ -132,6 +134,18 @@ class OracleMesh:
         mean, src, stats = np.empty(self.n), np.empty(self.n), np.empty(6)
         lib().orc_solve_implicit_transport_linear(C.byref(self.graph), K, _p(base), _p(slope), cg_tol, newton_tol,
                                                   _p(mean), _p(src), _p(stats))
+        return mean, src, stats
+
+    def solve_implicit_transport_group_quartic(self, group_of_cell, fine_area, K, a, b_fine, floor, cg_tol=1e-6,
+                                               newton_tol=1e-6):
+        """The production group response on an agglomerated graph (this mesh's arrays carry
+        the groups' areas as `graph_area_m2`): (mean, source, stats) per group."""
+        keep = [np.ascontiguousarray(group_of_cell, np.uint32), np.ascontiguousarray(fine_area, np.float64),
+                np.ascontiguousarray(b_fine, np.float64), np.ascontiguousarray(floor, np.float64)]
+        mean, src, stats = np.empty(self.n), np.empty(self.n), np.empty(6)
+        lib().orc_solve_implicit_transport_group_quartic(C.byref(self.graph), len(keep[0]), _p(keep[0]), _p(keep[1]),
+                                                         K, a, _p(keep[2]), _p(keep[3]), cg_tol, newton_tol,
+                                                         _p(mean), _p(src), _p(stats))
         return mean, src, stats
 
     def solve_implicit_transport_quartic(self, K, a, b, cg_tol=1e-6, newton_tol=1e-6):

@@ -770,6 +770,37 @@ void orc_solve_implicit_transport_quartic(const orc_graph* gp, double K, double 
         floor_out, cg_tol, newton_tol, mean_out, source_out, stats);
 }
 
+// The same solve on an agglomerated graph with the production group response
+// (surface_energy.cpp:1240-1296): every fine cell answers the quartic at its group's source
+// (the hold rule on the fine cell's index), a group takes the area-weighted means of its
+// cells (summed in cell order) over the group's area. `floor` per group.
+void orc_solve_implicit_transport_group_quartic(const orc_graph* gp, std::uint64_t fine_cells,
+                                                const std::uint32_t* group_of_cell, const double* fine_area,
+                                                double K, double a, const double* b_fine, const double* floor,
+                                                double cg_tol, double newton_tol, double* mean_out,
+                                                double* source_out, double* stats) {
+    const Graph g = graph_of(gp);
+    std::vector<double> floor_v(floor, floor + g.n), h_fine(fine_cells), mean_f(fine_cells), slope_f(fine_cells),
+        air(g.n), air_slope(g.n);
+    implicit_transport(
+        g, K,
+        [&](const std::vector<double>& at, std::vector<double>& mean, std::vector<double>& slope) {
+            for (std::size_t c = 0; c < fine_cells; ++c) h_fine[c] = at[group_of_cell[c]];
+            quartic_response(fine_cells, a, b_fine, h_fine.data(), mean_f.data(), slope_f.data());
+            std::fill(air.begin(), air.end(), 0.0);
+            std::fill(air_slope.begin(), air_slope.end(), 0.0);
+            for (std::size_t c = 0; c < fine_cells; ++c) {
+                air[group_of_cell[c]] += fine_area[c] * mean_f[c];
+                air_slope[group_of_cell[c]] += fine_area[c] * slope_f[c];
+            }
+            for (std::size_t n = 0; n < g.n; ++n) {
+                mean[n] = air[n] / g.area[n];
+                slope[n] = air_slope[n] / g.area[n];
+            }
+        },
+        floor_v.data(), cg_tol, newton_tol, mean_out, source_out, stats);
+}
+
 // The implicit sub-step with the linear column response, solved directly with the
 // reference PCG: (A/s + K L) T = (A/s) T0 + A S, s = dt/C; then H = flux form of T and
 // T_new = T0 + s (S + H). sums = {sum A H, sum A|H|, sum A H T, sum A S, sum A|S|,

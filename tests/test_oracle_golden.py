@@ -208,3 +208,19 @@ def test_oracle_advection_diffusion_bit_identical_to_the_reference(meshes, tag):
     assert np.array_equal(stats, g[f"ad_{tag}_stats"])
     assert np.array_equal(src, g[f"ad_{tag}_source"]) and np.array_equal(mean, g[f"ad_{tag}_mean"])
     assert np.array_equal(energy, g[f"ad_{tag}_energy"])
+
+
+@pytest.mark.parametrize("factor", [1, 10])
+def test_oracle_group_response_solve_bit_identical_to_the_reference(meshes, factor):
+    """The production pattern on the L5 agglomeration (fine-cell quartic at the group's
+    source, group means, the nonlinear solve) against the reference's own solve."""
+    import planet_game_gb300 as pg
+
+    g = golden("agglomeration.npz")
+    p = pg.agglomerated_transport_graph(5, 6.371e6)
+    om = O.OracleMesh(p.arrays())
+    mean, src, stats = om.solve_implicit_transport_group_quartic(
+        p.group_of_cell(), meshes(5).arrays()["area_m2"], float(g[f"qK{factor}"]), float(g["qa"]), g["qb"],
+        g[f"qfloor{factor}"])
+    assert np.array_equal(mean, g[f"qmean{factor}"]) and np.array_equal(src, g[f"qsource{factor}"])
+    assert np.array_equal(stats, g[f"qstats{factor}"])
