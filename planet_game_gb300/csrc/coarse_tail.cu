@@ -195,27 +195,6 @@ __global__ void __launch_bounds__(1024, 1) k_coarse_tail(const __grid_constant__
 
 }  // namespace
 
-std::vector<std::uint32_t> tail_blocks(const std::vector<std::uint32_t>& rows, unsigned budget) {
-    const std::size_t I = rows.size();
-    std::vector<unsigned> size(I, 1);
-    if (I > 0xFFFFu) throw std::logic_error("coarse tail: too many planets for per-planet blocks");
-    unsigned used = static_cast<unsigned>(I);
-    while (used < budget) {
-        std::size_t best = I;
-        double most = 0.0;
-        for (std::size_t i = 0; i < I; ++i) {
-            const double per = static_cast<double>(rows[i]) / size[i];
-            if (size[i] < 16 && per > most) { most = per; best = i; }
-        }
-        if (best == I || most <= 2048.0) break;   // a block covers up to 2048 rows well
-        ++size[best];
-        ++used;
-    }
-    std::vector<std::uint32_t> cta;
-    for (std::size_t i = 0; i < I; ++i)
-        for (unsigned r = 0; r < size[i]; ++r) cta.push_back(static_cast<std::uint32_t>(i) | (r << 16) | (size[i] << 24));
-    return cta;
-}
 
 unsigned tail_block_budget() {
     int device = 0, coop = 0, sms = 0, per_sm = 0;

@@ -8,6 +8,7 @@
 // the same per-tile code as the grid-wide V-cycle, so the result is identical.
 #pragma once
 
+#include "coarse_tail_blocks.hpp"
 #include "kernels.hpp"
 #include "persistent.hpp"
 
@@ -38,11 +39,6 @@ struct TailArgs {
     unsigned* barrier;          // [2][instances]: arrivals, generation
     unsigned* error;            // set when a barrier wait runs past its limit
 };
-
-// Blocks per planet for a tail from `level`: `rows[i]` its rows there, `budget` blocks
-// that can be co-resident; each planet gets at least one, the rest go to the planet with
-// the most rows per block (at most 16 each). Returns the packed per-block words.
-std::vector<std::uint32_t> tail_blocks(const std::vector<std::uint32_t>& rows, unsigned budget);
 
 // Co-resident 1024-thread tail blocks on this device (0: no cooperative launch).
 unsigned tail_block_budget();
