@@ -22,7 +22,7 @@ from __future__ import annotations
 import collections
 import threading
 import time
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 
 import numpy as np
 
