@@ -464,7 +464,6 @@ class Scalars {
         PSGB_CUDA(cudaStreamSynchronize(st));
         return {host_.data()[0], q > 1 ? host_.data()[1] : 0.0};
     }
-    const double* host() const { return host_.data(); }
 
   private:
     unsigned blocks_;
