@@ -114,6 +114,22 @@ def agglomeration_cases(R) -> None:
                     f"qstats{factor}": stats})
     R.refd_mesh_free(m)
     np.savez_compressed(HERE / "agglomeration.npz", levels=np.array(AGGLOMERATION_LEVELS), **out)
+    # L6-L8 as SHA-256 digests of the same arrays (groups as uint32, CSR as uint32, doubles)
+    digests = {}
+    for level in (6, 7, 8):
+        m = P(R.refd_mesh_new(level, RADIUS))
+        counts = np.zeros(3, dtype=np.uint64)
+        R.refd_agglomeration_counts(m, p(counts))
+        n, d, f = (int(c) for c in counts)
+        area, wsum = np.empty(n), np.empty(n)
+        off, nb = np.empty(n + 1, dtype=np.uint64), np.empty(d, dtype=np.uint64)
+        w, groups = np.empty(d), np.empty(f, dtype=np.uint64)
+        R.refd_agglomeration(m, p(area), p(off), p(nb), p(w), p(wsum), p(groups))
+        R.refd_mesh_free(m)
+        digests[str(level)] = {"group": sha(groups.astype(np.uint32)), "area": sha(area),
+                               "offset": sha(off.astype(np.uint32)), "neighbour": sha(nb.astype(np.uint32)),
+                               "weight": sha(w), "weight_sum": sha(wsum), "nodes": n}
+    (HERE / "agglomeration_sha256.json").write_text(json.dumps(digests, indent=1, sort_keys=True))
 
 
 def ref_graph(R, m, agglomerated: bool) -> dict:

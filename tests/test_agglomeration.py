@@ -1,7 +1,8 @@
 """The agglomerated transport graph against the reference's (golden vectors from
 agglomerated_transport_graph, heat_transport.cpp:456-539): the group of every fine cell,
 the coarse graph's CSR and weights, and the groups' summed areas, bit for bit at L0, L1,
-L3 and L5; plus the reference test's own checks (test_heat_transport.cpp:173-211):
+L3 and L5 and through SHA-256 digests of the same arrays at L6-L8; plus the reference
+test's own checks (test_heat_transport.cpp:173-211):
 every cell covered once, areas summing to the sphere's to 1e-12, symmetric positive
 weights, about four cells per group. Host-built, no GPU."""
 import numpy as np
@@ -91,3 +92,25 @@ def test_nonsymmetric_inputs_are_checked_before_the_library(planets):
         pg.solve_implicit_tracer(p, good, np.ones(n), np.ones(2 * n - 1), 1.0)
     with pytest.raises(ValueError):
         pg.advection_diffusion_source(p, good, np.ones(n), np.ones(n))
+
+
+@pytest.mark.parametrize("level", [6, 7, 8])
+def test_large_agglomerations_match_the_reference_digests(level):
+    """L6-L8 (the sizes the workloads use) against SHA-256 digests of the reference's
+    groups, graph and areas (tests/golden/agglomeration_sha256.json)."""
+    import hashlib
+    import json
+    from pathlib import Path
+
+    import planet_game_gb300 as pg
+
+    want = json.loads((Path(__file__).parent / "golden" / "agglomeration_sha256.json").read_text())[str(level)]
+    sha = lambda a: hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()   # noqa: E731
+    p = pg.agglomerated_transport_graph(level, 6.371e6)
+    g = pg.mesh_transport_graph(p)
+    assert p.cell_count == want["nodes"]
+    assert sha(p.group_of_cell()) == want["group"]
+    assert sha(g.area_m2) == want["area"]
+    assert sha(g.offset.astype(np.uint32)) == want["offset"]
+    assert sha(g.neighbour.astype(np.uint32)) == want["neighbour"]
+    assert sha(g.weight) == want["weight"] and sha(g.weight_sum) == want["weight_sum"]
