@@ -1,6 +1,9 @@
 """The multi-replica path of bench.py on CPU: two ranks over gloo (one process each),
 the timing barrier, the max over ranks, and the reference arm run by rank 0 alone. The
 path has no data-path collective: replicas solve their own planets."""
+import contextlib
+import io
+import json
 import multiprocessing as mp
 import os
 import socket
@@ -33,8 +36,10 @@ def _rank(rank: int, world: int, port: int, out):
     class Args:
         workload, seed, steps, warmup = "batch", 1, 1, 1
 
-    skipped = bench.run_reference(Args, r, w) is None if r != 0 else True
-    out.put((r, w, local, slowest, skipped))
+    printed = io.StringIO()
+    with contextlib.redirect_stdout(printed):
+        bench.run_reference(Args, r, w)
+    out.put((r, w, local, slowest, printed.getvalue()))
     dist.destroy_process_group()
 
 
@@ -52,4 +57,12 @@ def test_two_gloo_ranks_time_the_slowest_rank():
     results = sorted(out.get(timeout=5) for _ in procs)
     assert [r[:3] for r in results] == [(0, 2, 0), (1, 2, 1)]
     assert all(r[3] == 1.5 for r in results)          # value uses the slowest rank's time
-    assert all(r[4] for r in results)                 # the reference arm: rank 1 does no work
+    assert results[1][4] == ""                        # the reference arm: rank 1 does no work
+    line = json.loads(results[0][4])                  # rank 0 prints the one line of the contract
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in line
+    assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
+    assert line["cpu_baseline"]["value"] == line["value"] == line["e2e"]["value"]
+    assert line["e2e"]["h2d_bytes_per_step"] == line["e2e"]["d2h_bytes_per_step"] == 0
+    assert line["config"]["planets"] == 64 and line["config"]["cells"] == 2252928
