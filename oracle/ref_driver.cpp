@@ -25,6 +25,7 @@
 #include "sim/planet/planet_parameters.hpp"
 #include "sim/planet/surface/column_step.hpp"
 
+#include <chrono>
 #include <cstdint>
 #include <cstring>
 #include <limits>
@@ -624,6 +625,28 @@ int refd_pcg(void* handle, double conductance, const double* slope, const double
                                                static_cast<std::size_t>(workers));
     std::copy(x.values().begin(), x.values().end(), x_out);
     return iterations;
+}
+
+// The same solve with the graph and hierarchy built before the clock starts: seconds of
+// solve_newton_system alone (matrix values, Galerkin coarsening, coarse factor and PCG).
+double refd_pcg_seconds(void* handle, double conductance, const double* slope, const double* rhs,
+                        double relative_tolerance, int max_iterations, std::uint64_t workers, double* x_out,
+                        int* iterations) {
+    const auto& mesh = *static_cast<PlanetMesh*>(handle);
+    const auto graph = mesh_transport_graph(mesh);
+    const std::size_t n = mesh.cell_count();
+    std::vector<Level> levels = build_hierarchy(graph, n);
+    Field2D<double> s(copy_in(slope, n));
+    Field2D<double> b(copy_in(rhs, n));
+    Field2D<double> x;
+    ImplicitTransportSettings settings;
+    settings.cg_relative_tolerance = relative_tolerance;
+    settings.max_cg_iterations = max_iterations;
+    const auto start = std::chrono::steady_clock::now();
+    *iterations = solve_newton_system(graph, conductance, s, b, levels, x, settings, static_cast<std::size_t>(workers));
+    const double seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - start).count();
+    std::copy(x.values().begin(), x.values().end(), x_out);
+    return seconds;
 }
 
 // ---- column radiation (atmosphere_column.hpp:85-143, 599-634) ---------------

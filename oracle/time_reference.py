@@ -16,6 +16,14 @@ planet_game_gb300.workloads with the same seeds):
   agglomerated solve_implicit_transport, linear response, the L8 mesh's agglomerated graph
                (163,842 nodes), to a 1e-10 relative residual
 Prints one JSON line: per case the median of 3 timed calls (after one warm-up), in ms.
+
+    python oracle/time_reference.py /path/to/planet_game --headline
+
+instead times the headline solve one core at a time: every planet of the 64-planet mix
+(16 x L4, 24 x L5, 16 x L6, 8 x L7) solved to a 1e-10 relative residual by the reference's
+solve_newton_system (PCG + SGS V-cycle, worker_count 1) and by the oracle's restatement
+that bench.py's reference arm runs, on the same matrix (the planet's median conductance:
+the reference's API takes one conductance per graph), the clock around the solve alone.
 Oracle infrastructure: never imported by the product."""
 from __future__ import annotations
 
@@ -58,6 +66,8 @@ def load(reference: Path) -> C.CDLL:
                                        C.c_double, C.c_double, C.c_uint64, P, P, P, P]
     R.refd_insolation.argtypes = [P, C.c_int64, P]
     R.refd_solve_linear_agglomerated.argtypes = [P, C.c_double, P, P, C.c_double, C.c_double, C.c_uint64, P, P, P]
+    R.refd_pcg_seconds.restype = C.c_double
+    R.refd_pcg_seconds.argtypes = [P, C.c_double, P, P, C.c_double, C.c_int, C.c_uint64, P, P]
     return R
 
 
@@ -144,9 +154,50 @@ def main(reference: Path, workers: int) -> None:
     print(json.dumps(out))
 
 
+def headline(reference: Path) -> None:
+    """The reference's PCG against the oracle's restatement of it, one core, per planet."""
+    import planet_game_gb300 as pg
+    from oracle import oracle as O
+    from planet_game_gb300 import workloads as W
+
+    R = load(reference)
+    ref_s, port_s, ref_it, port_it, worst = 0.0, 0.0, 0, 0, 0.0
+    specs = W.planet_mix(2026)
+    for spec in specs:
+        mesh = pg.make_icosphere(spec.level, spec.radius)
+        inp = W.step_inputs(mesh, spec.seed)
+        arrays = mesh.arrays()
+        n = mesh.cell_count
+        s = inp.dt / inp.heat_capacity
+        area = arrays["area_m2"]
+        slope, rhs = np.full(n, s), area / s * inp.t0 + area * inp.source
+        m = P(R.refd_mesh_new(spec.level, spec.radius))
+        x_ref, it = np.empty(n), C.c_int(0)
+        best = min(R.refd_pcg_seconds(m, inp.conductance, p(slope), p(rhs), 1e-10, 2000, 1, p(x_ref), C.byref(it))
+                   for _ in range(3))
+        R.refd_mesh_free(m)
+        h = O.OracleHierarchy(O.OracleMesh(arrays))
+        times = []
+        for _ in range(3):
+            t = time.perf_counter()
+            x_port, port = h.pcg(inp.conductance, slope, rhs, 1e-10, 2000)
+            times.append(time.perf_counter() - t)
+        ref_s, port_s = ref_s + best, port_s + min(times)
+        ref_it, port_it = ref_it + it.value, port_it + port
+        worst = max(worst, float(np.max(np.abs(x_port - x_ref)) / np.max(np.abs(x_ref))))
+    print(json.dumps({"host": os.uname().machine, "planets": len(specs), "reference_s": ref_s, "port_s": port_s,
+                      "port_over_reference": port_s / ref_s, "reference_pcg_iterations": ref_it,
+                      "port_pcg_iterations": port_it, "max_relative_difference": worst,
+                      "reference_substeps_per_s_one_core": len(specs) / ref_s,
+                      "port_substeps_per_s_one_core": len(specs) / port_s}))
+
+
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     workers = os.cpu_count() or 1
     if "--workers" in sys.argv:
         workers = int(sys.argv[sys.argv.index("--workers") + 1])
-    main(Path(args[0] if args else "/root/reference"), workers)
+    if "--headline" in sys.argv:
+        headline(Path(args[0] if args else "/root/reference"))
+    else:
+        main(Path(args[0] if args else "/root/reference"), workers)
