@@ -162,6 +162,7 @@ def headline(reference: Path) -> None:
 
     R = load(reference)
     ref_s, port_s, ref_it, port_it, worst = 0.0, 0.0, 0, 0, 0.0
+    per_level: dict[str, list[float]] = {}
     specs = W.planet_mix(2026)
     for spec in specs:
         mesh = pg.make_icosphere(spec.level, spec.radius)
@@ -183,13 +184,17 @@ def headline(reference: Path) -> None:
             x_port, port = h.pcg(inp.conductance, slope, rhs, 1e-10, 2000)
             times.append(time.perf_counter() - t)
         ref_s, port_s = ref_s + best, port_s + min(times)
+        lv = per_level.setdefault(f"L{spec.level}", [0.0, 0.0])
+        lv[0] += best
+        lv[1] += min(times)
         ref_it, port_it = ref_it + it.value, port_it + port
         worst = max(worst, float(np.max(np.abs(x_port - x_ref)) / np.max(np.abs(x_ref))))
     print(json.dumps({"host": os.uname().machine, "planets": len(specs), "reference_s": ref_s, "port_s": port_s,
                       "port_over_reference": port_s / ref_s, "reference_pcg_iterations": ref_it,
                       "port_pcg_iterations": port_it, "max_relative_difference": worst,
                       "reference_substeps_per_s_one_core": len(specs) / ref_s,
-                      "port_substeps_per_s_one_core": len(specs) / port_s}))
+                      "port_substeps_per_s_one_core": len(specs) / port_s,
+                      "per_level_reference_port_s": per_level}))
 
 
 if __name__ == "__main__":
