@@ -103,33 +103,34 @@ Incidence incidence(std::size_t vertices, const std::vector<Face>& faces) {
 }
 
 // Lloyd relaxation towards the centroidal tessellation, as the reference's
-// Jacobi-style update (icosphere.cpp:92-118), with its per-vertex sum order.
+// Jacobi-style update (icosphere.cpp:92-118), with its per-vertex sum order. Each
+// iteration computes the faces' circumcentres, then every vertex sums the two
+// area-weighted centroids of each incident face's corner (faces in ascending order,
+// "next" neighbour before "previous") from the old positions into a second buffer.
 void lloyd(std::vector<V3>& v, const std::vector<Face>& faces, std::uint32_t iterations) {
     const Incidence inc = incidence(v.size(), faces);
-    std::vector<V3> contrib(faces.size() * 6);
+    std::vector<V3> centre(faces.size()), next(v.size());
     for (std::uint32_t it = 0; it < iterations; ++it) {
         parallel_for(faces.size(), [&](std::size_t f) {
             const Face& face = faces[f];
-            const V3 cc = circumcentre(v[face[0]], v[face[1]], v[face[2]]);
-            for (std::size_t c = 0; c < 3; ++c) {
-                const V3& gen = v[face[c]];
-                const V3* around[2] = {&v[face[(c + 1) % 3]], &v[face[(c + 2) % 3]]};
-                for (std::size_t k = 0; k < 2; ++k) {
-                    const V3 mid = unit(add(gen, *around[k]));
-                    const double area = triangle_area_unit(gen, mid, cc);
-                    contrib[f * 6 + c * 2 + k] = scale(unit(add(add(gen, mid), cc)), area);
-                }
-            }
+            centre[f] = circumcentre(v[face[0]], v[face[1]], v[face[2]]);
         });
         parallel_for(v.size(), [&](std::size_t vertex) {
+            const V3& gen = v[vertex];
             V3 sum{0.0, 0.0, 0.0};
             for (std::uint32_t k = inc.offset[vertex]; k < inc.offset[vertex + 1]; ++k) {
-                const std::size_t base = std::size_t(inc.face[k]) * 6 + std::size_t(inc.slot[k]) * 2;
-                sum = add(sum, contrib[base]);
-                sum = add(sum, contrib[base + 1]);
+                const Face& face = faces[inc.face[k]];
+                const V3& cc = centre[inc.face[k]];
+                const std::size_t c = inc.slot[k];
+                for (std::size_t side = 1; side <= 2; ++side) {
+                    const V3 mid = unit(add(gen, v[face[(c + side) % 3]]));
+                    const double area = triangle_area_unit(gen, mid, cc);
+                    sum = add(sum, scale(unit(add(add(gen, mid), cc)), area));
+                }
             }
-            v[vertex] = unit(sum);
+            next[vertex] = unit(sum);
         });
+        v.swap(next);
     }
 }
 
@@ -138,52 +139,70 @@ struct UnitMesh {
     std::vector<Face> faces;
 };
 
-UnitMesh subdivide_and_relax(std::uint32_t level) {
-    UnitMesh u;
-    u.vertices = icosahedron_vertices();
-    u.faces = icosahedron_faces();
+// One level finer: every face split in four at its edges' normalised midpoints (a
+// midpoint is numbered when first met, faces in order), then the Lloyd relaxation.
+void subdivide_and_relax(UnitMesh& u) {
     std::vector<V3>& vert = u.vertices;
     std::vector<Face>& faces = u.faces;
-    for (std::uint32_t l = 0; l < level; ++l) {
-        std::unordered_map<std::uint64_t, std::uint32_t> midpoints;
-        midpoints.reserve(faces.size() * 2);
-        auto midpoint = [&](std::uint32_t a, std::uint32_t b) {
-            const std::uint64_t key = (std::uint64_t(std::min(a, b)) << 32) | std::max(a, b);
-            auto it = midpoints.find(key);
-            if (it != midpoints.end()) return it->second;
-            const auto index = static_cast<std::uint32_t>(vert.size());
-            vert.push_back(unit(add(vert[a], vert[b])));
-            midpoints.emplace(key, index);
-            return index;
-        };
-        std::vector<Face> next;
-        next.reserve(faces.size() * 4);
-        for (const auto& f : faces) {
-            const auto e01 = midpoint(f[0], f[1]);
-            const auto e12 = midpoint(f[1], f[2]);
-            const auto e20 = midpoint(f[2], f[0]);
-            next.push_back({f[0], e01, e20});
-            next.push_back({f[1], e12, e01});
-            next.push_back({f[2], e20, e12});
-            next.push_back({e01, e12, e20});
-        }
-        faces.swap(next);
-        lloyd(vert, faces, lloyd_iterations);
+    std::unordered_map<std::uint64_t, std::uint32_t> midpoints;
+    midpoints.reserve(faces.size() * 2);
+    auto midpoint = [&](std::uint32_t a, std::uint32_t b) {
+        const std::uint64_t key = (std::uint64_t(std::min(a, b)) << 32) | std::max(a, b);
+        auto it = midpoints.find(key);
+        if (it != midpoints.end()) return it->second;
+        const auto index = static_cast<std::uint32_t>(vert.size());
+        vert.push_back(unit(add(vert[a], vert[b])));
+        midpoints.emplace(key, index);
+        return index;
+    };
+    std::vector<Face> next;
+    next.reserve(faces.size() * 4);
+    for (const auto& f : faces) {
+        const auto e01 = midpoint(f[0], f[1]);
+        const auto e12 = midpoint(f[1], f[2]);
+        const auto e20 = midpoint(f[2], f[0]);
+        next.push_back({f[0], e01, e20});
+        next.push_back({f[1], e12, e01});
+        next.push_back({f[2], e20, e12});
+        next.push_back({e01, e12, e20});
     }
-    return u;
+    faces.swap(next);
+    lloyd(vert, faces, lloyd_iterations);
 }
 
+// The relaxed unit mesh of `level`, built once per process from the finest level
+// already built below it; every level passed on the way is kept too (a level's mesh
+// depends only on the level, so an L8 build leaves L1-L7 ready).
 const UnitMesh& relaxed_unit_mesh(std::uint32_t level) {
     static std::mutex mutex;
     static std::map<std::uint32_t, std::unique_ptr<UnitMesh>> cache;
     std::unique_lock<std::mutex> lock(mutex);
-    auto& entry = cache[level];
-    if (!entry) {
-        lock.unlock();
-        auto built = std::make_unique<UnitMesh>(subdivide_and_relax(level));
-        lock.lock();
-        if (!entry) entry = std::move(built);
+    if (const auto hit = cache.find(level); hit != cache.end()) return *hit->second;
+    UnitMesh u;
+    std::uint32_t from = 0;
+    if (auto below = cache.lower_bound(level); below != cache.begin()) {
+        --below;
+        u = *below->second;
+        from = below->first;
+    } else {
+        u.vertices = icosahedron_vertices();
+        u.faces = icosahedron_faces();
     }
+    lock.unlock();
+    for (std::uint32_t l = from; l < level; ++l) {
+        subdivide_and_relax(u);
+        if (l + 1 < level) {
+            auto copy = std::make_unique<UnitMesh>(u);
+            lock.lock();
+            auto& entry = cache[l + 1];
+            if (!entry) entry = std::move(copy);
+            lock.unlock();
+        }
+    }
+    auto built = std::make_unique<UnitMesh>(std::move(u));
+    lock.lock();
+    auto& entry = cache[level];
+    if (!entry) entry = std::move(built);
     return *entry;
 }
 
