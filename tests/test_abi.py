@@ -81,3 +81,20 @@ def test_hierarchy_view_without_gpu(meshes):
     lv = m.hierarchy_level(0)
     assert len(lv["aggregate"]) == 10242 and lv["aggregate"].max() == 641
     assert len(m.hierarchy_level(2)["aggregate"]) == 0
+
+
+def test_missing_library_fails_loudly():
+    """Without the built library every entry point raises: there is no CPU fallback."""
+    import subprocess
+    import sys
+
+    code = ("import pathlib, planet_game_gb300 as pg\n"
+            "from planet_game_gb300 import capi\n"
+            "capi.LIBRARY = pathlib.Path('/nonexistent/libplanetsim_gb300.so')\n"
+            "capi._lib = None\n"
+            "try:\n"
+            "    pg.make_icosphere(2, 6.371e6)\n"
+            "except FileNotFoundError as e:\n"
+            "    print('refused:', e)\n")
+    out = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0 and out.stdout.startswith("refused:"), out.stdout + out.stderr
