@@ -73,4 +73,12 @@ void launch_persistent(const PersistentArgs<T>& args, cudaStream_t st, bool seri
 // True when the persistent kernel fits one block per SM on the current device.
 bool persistent_supported();
 
+// The kernel's own entry points (instantiated for float and double, one translation
+// unit each): co-resident 1024-thread blocks per SM, and the cooperative launch of
+// `blocks` blocks on `st`.
+template <typename T>
+int persistent_kernel_blocks_per_sm();
+template <typename T>
+void persistent_kernel_launch(const PersistentArgs<T>& args, unsigned blocks, cudaStream_t st);
+
 }  // namespace psgb
