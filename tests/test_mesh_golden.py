@@ -79,3 +79,22 @@ def test_invalid_mesh_arguments():
         pg.make_icosphere(3, float("nan"))
     with pytest.raises(ValueError):
         pg.make_icosphere(40, 6.371e6)
+
+
+@pytest.mark.parametrize("level", [4, 5, 6])
+def test_integer_structure_depends_on_the_level_only(level):
+    """The hierarchy is built from unit conductances: its integer structure (columns,
+    aggregates, targets) and the graph's CSR are the same for every radius of a level,
+    while the geometric weights differ in the last bits."""
+    import planet_game_gb300 as pg
+
+    ms = [pg.make_icosphere(level, r) for r in (3.1e6, 6.371e6, 8.9e6)]
+    for m in ms[1:]:
+        assert m.level_rows == ms[0].level_rows
+        for i in range(len(m.level_rows)):
+            a, b = ms[0].hierarchy_level(i), m.hierarchy_level(i)
+            for key in ("offset", "column", "aggregate", "target"):
+                assert np.array_equal(a[key], b[key]), (level, i, key)
+        ga, gb = pg.mesh_transport_graph(ms[0]), pg.mesh_transport_graph(m)
+        assert np.array_equal(ga.offset, gb.offset) and np.array_equal(ga.neighbour, gb.neighbour)
+        assert np.allclose(ga.weight, gb.weight, rtol=1e-15, atol=0)
