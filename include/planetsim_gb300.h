@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define PSGB_ABI_VERSION 2
+#define PSGB_ABI_VERSION 3
 
 /* status codes */
 #define PSGB_OK 0
@@ -44,6 +44,7 @@ extern "C" {
 #define PSGB_ERR_CUDA 6
 #define PSGB_ERR_LOGIC 7            /* std::logic_error in the reference */
 #define PSGB_ERR_BUDGET 8           /* admission refused by the HBM budget */
+#define PSGB_ERR_TIMEOUT 9          /* a wait ran out before the request finished */
 
 #define PSGB_MEMORY_HOST 0
 #define PSGB_MEMORY_DEVICE 1
@@ -508,6 +509,55 @@ int psgb_substep_mean_insolation(const psgb_planet* planet, int64_t substep, flo
  * quadrature in a kernel; `out` [cells] FP32, HOST or DEVICE per `memory`. Within one
  * FP32 ulp of the reference (CUDA's acos/sin against the host library's). */
 int psgb_substep_mean_insolation_gpu(psgb_planet* planet, int64_t substep, float* out, int memory, void* stream);
+
+/* ---- the serving loop (no counterpart in the reference: it steps one planet per call)
+ * A continuous-batching request loop for implicit heat-transport sub-steps of registered
+ * planets of uneven mesh levels. Planets of one mesh level form a lane: while admitted,
+ * the lane's batch (mesh, hierarchy, matrix) and its planets' temperatures stay in device
+ * memory, and a worker thread steps, in rounds, the oldest queued request of every planet
+ * of the lane together (psgb_batch_transport_step_masked); requests arriving during a
+ * round join the next one, and the lanes' rounds overlap on the GPU. Lanes are admitted
+ * against a device-memory budget: the least recently used idle lanes are evicted first
+ * (their temperatures copied back to the host), or the lane waits until one goes idle; a
+ * lane larger than the budget fails its requests with PSGB_ERR_BUDGET. A request's new
+ * temperature is the step from the planet's state after its earlier requests. */
+typedef struct psgb_server psgb_server;
+
+typedef struct psgb_server_config {
+    double budget_bytes;          /* device memory for resident lanes */
+    double bytes_per_cell;        /* a resident lane's estimate per cell (<= 0: 700) */
+    psgb_solve_options options;   /* every step's solve */
+    int autotune;                 /* nonzero: tune each lane at its first admission (psgb_batch_autotune),
+                                     reapplied at later admissions */
+    int device;                   /* CUDA device of the lanes */
+} psgb_server_config;
+
+typedef struct psgb_server_stats {
+    uint64_t submitted, completed, failed, rounds, evictions, admissions;
+    uint64_t resident_bytes;
+    uint32_t resident_lanes, planets;
+    double p50_ms, p99_ms;        /* submit-to-done latency of the completed requests */
+} psgb_server_stats;
+
+int psgb_server_create(const psgb_server_config* config, psgb_server** out);
+/* Stops the lanes after their running round; requests still queued fail. */
+void psgb_server_destroy(psgb_server* server);
+/* Registers a planet (before its level's first request): mesh level and radius, its step
+ * parameters (params->edge_conductance: optional HOST array per undirected edge), its
+ * initial temperature (HOST, cells). */
+int psgb_server_add_planet(psgb_server* server, uint32_t level, double radius_m, const psgb_step_params* params,
+                           const double* t0_K, uint32_t* planet_out);
+/* Queues one sub-step of `planet` with this source (HOST, cells; copied). */
+int psgb_server_submit(psgb_server* server, uint32_t planet, const double* source_W_m2, uint64_t* request_out);
+/* Waits for a request (timeout_s < 0: no limit). Returns its status (PSGB_OK, a solve
+ * status, PSGB_ERR_BUDGET, ...) and, once finished, forgets it after copying the new
+ * temperature (t_new_K, HOST, cells; may be NULL) and the report (may be NULL);
+ * PSGB_ERR_TIMEOUT while it is still queued or running. Every request is waited on once. */
+int psgb_server_wait(psgb_server* server, uint64_t request, double timeout_s, double* t_new_K,
+                     psgb_step_report* report);
+/* The planet's temperature after its finished requests (HOST, cells). */
+int psgb_server_state(psgb_server* server, uint32_t planet, double* t_K);
+int psgb_server_stats_get(psgb_server* server, psgb_server_stats* out);
 
 #ifdef __cplusplus
 }

@@ -19,6 +19,7 @@ ERR_NON_FINITE = 5
 ERR_CUDA = 6
 ERR_LOGIC = 7
 ERR_BUDGET = 8
+ERR_TIMEOUT = 9
 
 MEMORY_HOST = 0
 MEMORY_DEVICE = 1
@@ -131,6 +132,17 @@ class StepReport(C.Structure):
                 ("dissipation_W_K", C.c_double), ("closure", C.c_double)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("budget_bytes", C.c_double), ("bytes_per_cell", C.c_double), ("options", SolveOptions),
+                ("autotune", C.c_int), ("device", C.c_int)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(name, C.c_uint64) for name in (
+        "submitted", "completed", "failed", "rounds", "evictions", "admissions", "resident_bytes")] + [
+        ("resident_lanes", C.c_uint32), ("planets", C.c_uint32), ("p50_ms", C.c_double), ("p99_ms", C.c_double)]
+
+
 class ColumnConstants(C.Structure):
     _fields_ = [(name, C.c_double) for name in (
         "dry_optical_depth", "vapour_absorption_m2_kg", "in_cloud_water_path_kg_m2", "effective_radius_m",
@@ -201,6 +213,14 @@ _SIGNATURES = {
                                         P, P, P, C.c_int, P]),
     "psgb_substep_mean_insolation": (C.c_int, [P, C.c_int64, P]),
     "psgb_substep_mean_insolation_gpu": (C.c_int, [P, C.c_int64, P, C.c_int, P]),
+    "psgb_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(P)]),
+    "psgb_server_destroy": (None, [P]),
+    "psgb_server_add_planet": (C.c_int, [P, C.c_uint32, C.c_double, C.POINTER(StepParams), P,
+                                         C.POINTER(C.c_uint32)]),
+    "psgb_server_submit": (C.c_int, [P, C.c_uint32, P, C.POINTER(C.c_uint64)]),
+    "psgb_server_wait": (C.c_int, [P, C.c_uint64, C.c_double, P, C.POINTER(StepReport)]),
+    "psgb_server_state": (C.c_int, [P, C.c_uint32, P]),
+    "psgb_server_stats_get": (C.c_int, [P, C.POINTER(ServerStats)]),
     "psgb_launch_count": (C.c_uint64, []),
     "psgb_profile_begin": (C.c_int, [C.c_char_p]),
     "psgb_profile_end": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
