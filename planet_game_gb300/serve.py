@@ -16,6 +16,9 @@ or the request waits until memory frees up.
 
 The comparator (`OneAtATime`) serves the same trace with the plain drop-in: one request
 at a time, each planet solved alone in plain FP64.
+
+`NativeServer` is the library's own loop (psgb_server_*): the same policy with the lanes and
+their worker threads in C++, host arrays in and out.
 """
 from __future__ import annotations
 
@@ -26,7 +29,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from . import api
+from . import api, capi
 from . import workloads as W
 
 
@@ -278,6 +281,85 @@ class Server:
                 lane.cv.notify_all()
         for lane in self.lanes.values():
             lane.thread.join(timeout=30)
+
+
+class NativeServer:
+    """The library's serving loop (psgb_server_*): register planets, submit sub-steps,
+    wait for their new temperatures. Lanes per mesh level, resident under `budget_bytes`
+    of device memory; `solver` as for `api.solve_options`."""
+
+    def __init__(self, budget_bytes: float = 150e9, precision: str = "mixed", method: str = "bicgstab",
+                 autotune: bool = True, device: int = 0, bytes_per_cell: float = 700.0, **solver):
+        import ctypes as C
+
+        self._C = C
+        self._lib = capi.load()
+        cfg = capi.ServerConfig()
+        cfg.budget_bytes, cfg.bytes_per_cell = float(budget_bytes), float(bytes_per_cell)
+        cfg.options = api.solve_options(precision=precision, method=method, **solver)
+        cfg.autotune, cfg.device = int(bool(autotune)), int(device)
+        handle = C.c_void_p()
+        capi.check(self._lib.psgb_server_create(C.byref(cfg), C.byref(handle)))
+        self._h = handle
+        self._cells: dict[int, int] = {}
+
+    def add_planet(self, level: int, radius_m: float, heat_capacity: float, dt: float, conductance: float, t0_K,
+                   edge_conductance=None) -> int:
+        """Registers a planet (before its level's first request); returns its id."""
+        C = self._C
+        t0 = np.ascontiguousarray(t0_K, dtype=np.float64)
+        edges = None if edge_conductance is None else np.ascontiguousarray(edge_conductance, dtype=np.float64)
+        cells = 10 * 4 ** int(level) + 2   # the icosphere's cells at this level
+        if t0.size != cells:
+            raise ValueError("the initial temperature does not match the level's cells")
+        params = capi.StepParams(heat_capacity, dt, conductance, None if edges is None else edges.ctypes.data, 0)
+        pid = C.c_uint32()
+        capi.check(self._lib.psgb_server_add_planet(self._h, level, radius_m, C.byref(params),
+                                                    t0.ctypes.data_as(C.c_void_p), C.byref(pid)))
+        self._cells[pid.value] = cells
+        return pid.value
+
+    def submit(self, planet: int, source_W_m2) -> int:
+        C = self._C
+        src = np.ascontiguousarray(source_W_m2, dtype=np.float64)
+        if src.size != self._cells.get(planet, -1):
+            raise ValueError("unknown planet or a source of the wrong size")
+        rid = C.c_uint64()
+        capi.check(self._lib.psgb_server_submit(self._h, planet, src.ctypes.data_as(C.c_void_p), C.byref(rid)))
+        return rid.value
+
+    def wait(self, request: int, planet: int, timeout_s: float = -1.0):
+        """(new temperature, report) of a request of `planet`; raises GB300Error on failure."""
+        C = self._C
+        out = np.empty(self._cells[planet])
+        rep = capi.StepReport()
+        capi.check(self._lib.psgb_server_wait(self._h, request, timeout_s, out.ctypes.data_as(C.c_void_p),
+                                              C.byref(rep)))
+        return out, rep
+
+    def state(self, planet: int) -> np.ndarray:
+        out = np.empty(self._cells[planet])
+        capi.check(self._lib.psgb_server_state(self._h, planet, out.ctypes.data_as(self._C.c_void_p)))
+        return out
+
+    def stats(self) -> dict:
+        st = capi.ServerStats()
+        capi.check(self._lib.psgb_server_stats_get(self._h, self._C.byref(st)))
+        return {name: getattr(st, name) for name, _ in capi.ServerStats._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            self._lib.psgb_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        self.close()
 
 
 class OneAtATime:

@@ -5,8 +5,9 @@
   steps every planet of a lane with queued work; lanes step side by side), the memory
   budget (least recently used idle lane evicted with its states copied back; a lane larger
   than the budget refused), failures reported per request, timeouts and shutdown;
-- the C entry points: argument checks, and a lane that cannot reach a GPU failing its
-  requests with the CUDA status instead of hanging."""
+- the C entry points and their Python wrapper (serve.NativeServer): argument checks, and a
+  lane that cannot reach a GPU failing its requests with the CUDA status instead of
+  hanging."""
 import ctypes as C
 import shutil
 import subprocess
@@ -95,3 +96,21 @@ def test_server_without_a_gpu_fails_requests_cleanly():
         assert (stats.submitted, stats.failed, stats.completed, stats.resident_lanes) == (1, 1, 0, 0)
     finally:
         lib.psgb_server_destroy(srv)
+
+
+def test_python_wrapper_of_the_native_server():
+    from planet_game_gb300 import capi
+    from planet_game_gb300.serve import NativeServer
+
+    with NativeServer(budget_bytes=1e9, autotune=False) as srv:
+        t0 = np.linspace(250.0, 300.0, 162)
+        pid = srv.add_planet(2, 6.371e6, 4e7, 2.6e6, 4e13, t0)
+        assert np.array_equal(srv.state(pid), t0)
+        with pytest.raises(ValueError):
+            srv.add_planet(2, 6.371e6, 4e7, 2.6e6, 4e13, t0[:-1])
+        with pytest.raises(ValueError):
+            srv.submit(pid, np.zeros(10))
+        with pytest.raises(capi.GB300Error):
+            srv.add_planet(2, 6.371e6, 4e7, 0.0, 4e13, t0)
+        stats = srv.stats()
+        assert stats["planets"] == 1 and stats["submitted"] == 0
