@@ -264,6 +264,48 @@ void timeouts_and_close() {
     CHECK(bad_budget);
 }
 
+// Four producer threads submit to their own planets of four levels under a budget for two
+// lanes: lanes come and go while requests arrive; every request still sees its planet's
+// earlier requests, in order.
+void concurrent_producers_under_a_tight_budget() {
+    Counters c;
+    Server s(std::make_unique<FakeBackend>(c, 10), 2 * 3 * 16 * 10 + 5, map_error);   // two lanes of 3 x 16 cells
+    std::vector<std::uint32_t> ids;
+    for (std::uint32_t level : {3u, 4u, 5u, 6u})
+        for (int k = 0; k < 3; ++k) ids.push_back(s.add_planet(planet(level, 16, 100.0 * level)));
+    const int per_planet = 20;
+    std::vector<std::vector<std::uint64_t>> reqs(ids.size());
+    std::vector<std::thread> producers;
+    for (int t = 0; t < 4; ++t) {
+        producers.emplace_back([&, t] {
+            for (int k = 0; k < per_planet; ++k)
+                for (std::size_t p = static_cast<std::size_t>(t); p < ids.size(); p += 4) {
+                    std::vector<double> src(16, 1.0 + k + p);
+                    reqs[p].push_back(s.submit(ids[p], src.data()));
+                    if ((k + p) % 5 == 0) std::this_thread::sleep_for(std::chrono::microseconds(300));
+                }
+        });
+    }
+    for (auto& th : producers) th.join();
+    for (std::size_t p = 0; p < ids.size(); ++p) {
+        double expect = 100.0 * (3 + p / 3);
+        for (int k = 0; k < per_planet; ++k) {
+            std::vector<double> out(16);
+            std::string msg;
+            CHECK(s.wait(reqs[p][k], 30.0, out.data(), nullptr, msg) == PSGB_OK);
+            expect += 0.5 * (1.0 + k + p);
+            CHECK(out[7] == expect);
+        }
+        std::vector<double> now(16);
+        s.state(ids[p], now.data());
+        CHECK(now[0] == expect);
+    }
+    const Stats st = s.stats();
+    CHECK(st.completed == ids.size() * per_planet && st.failed == 0);
+    CHECK(st.evictions > 0 && st.resident_lanes <= 2);
+    CHECK(static_cast<double>(st.resident_bytes) <= 2 * 3 * 16 * 10 + 5);
+}
+
 }  // namespace
 
 int main() {
@@ -271,6 +313,7 @@ int main() {
     budget_eviction_and_refusal();
     failures_are_reported();
     timeouts_and_close();
+    concurrent_producers_under_a_tight_budget();
     if (failures == 0) std::printf("OK\n");
     return failures == 0 ? 0 : 1;
 }
