@@ -56,6 +56,52 @@ class GpuLane final : public Lane {
     GpuLane(const psgb_server_config& cfg, std::uint32_t level, const std::vector<PlanetRecord*>& planets,
             Tunings& tunings)
         : options_(cfg.options) {
+        try {
+            build(cfg, level, planets, tunings);
+        } catch (...) {
+            release();   // a partly built lane frees what it holds
+            throw;
+        }
+    }
+
+    ~GpuLane() override { release(); }
+
+    GpuLane(const GpuLane&) = delete;
+    GpuLane& operator=(const GpuLane&) = delete;
+
+    void step(const std::vector<std::uint8_t>& active, const std::vector<const double*>& sources,
+              const std::vector<double*>& results, std::vector<psgb_step_report>& reports) override {
+        const std::size_t n = cells_.size();
+        std::vector<const double*> t0(n), src(n);
+        std::vector<double*> t_new(n);
+        for (std::size_t i = 0; i < n; ++i) {
+            t0[i] = states_ + offset_[i];
+            t_new[i] = states_ + offset_[i];
+            src[i] = sources_ + offset_[i];
+            if (active[i])
+                PSGB_CUDA(cudaMemcpyAsync(sources_ + offset_[i], sources[i], cells_[i] * sizeof(double),
+                                          cudaMemcpyHostToDevice, stream_));
+        }
+        const int status = psgb_batch_transport_step_masked(batch_, active.data(), params_.data(), &options_, t0.data(),
+                                                            src.data(), t_new.data(), nullptr, reports.data(),
+                                                            PSGB_MEMORY_DEVICE, stream_);
+        if (status != PSGB_OK && !solve_status(status)) throw StatusError(status, psgb_last_error());
+        for (std::size_t i = 0; i < n; ++i)
+            if (active[i])
+                PSGB_CUDA(cudaMemcpyAsync(results[i], states_ + offset_[i], cells_[i] * sizeof(double),
+                                          cudaMemcpyDeviceToHost, stream_));
+        PSGB_CUDA(cudaStreamSynchronize(stream_));
+    }
+
+    void read_state(std::size_t i, double* out) override {
+        PSGB_CUDA(cudaMemcpyAsync(out, states_ + offset_[i], cells_[i] * sizeof(double), cudaMemcpyDeviceToHost,
+                                  stream_));
+        PSGB_CUDA(cudaStreamSynchronize(stream_));
+    }
+
+  private:
+    void build(const psgb_server_config& cfg, std::uint32_t level, const std::vector<PlanetRecord*>& planets,
+               Tunings& tunings) {
         const std::size_t n = planets.size();
         std::vector<psgb_planet*> handles(n);
         std::size_t total = 0;
@@ -114,48 +160,17 @@ class GpuLane final : public Lane {
         PSGB_CUDA(cudaStreamSynchronize(stream_));
     }
 
-    ~GpuLane() override {
+    void release() noexcept {
         if (stream_ != nullptr) cudaStreamSynchronize(stream_);
         if (batch_ != nullptr) psgb_batch_destroy(batch_);
         if (states_ != nullptr) cudaFree(states_);
         if (sources_ != nullptr) cudaFree(sources_);
         if (stream_ != nullptr) cudaStreamDestroy(stream_);
+        batch_ = nullptr;
+        states_ = sources_ = nullptr;
+        stream_ = nullptr;
     }
 
-    GpuLane(const GpuLane&) = delete;
-    GpuLane& operator=(const GpuLane&) = delete;
-
-    void step(const std::vector<std::uint8_t>& active, const std::vector<const double*>& sources,
-              const std::vector<double*>& results, std::vector<psgb_step_report>& reports) override {
-        const std::size_t n = cells_.size();
-        std::vector<const double*> t0(n), src(n);
-        std::vector<double*> t_new(n);
-        for (std::size_t i = 0; i < n; ++i) {
-            t0[i] = states_ + offset_[i];
-            t_new[i] = states_ + offset_[i];
-            src[i] = sources_ + offset_[i];
-            if (active[i])
-                PSGB_CUDA(cudaMemcpyAsync(sources_ + offset_[i], sources[i], cells_[i] * sizeof(double),
-                                          cudaMemcpyHostToDevice, stream_));
-        }
-        const int status = psgb_batch_transport_step_masked(batch_, active.data(), params_.data(), &options_, t0.data(),
-                                                            src.data(), t_new.data(), nullptr, reports.data(),
-                                                            PSGB_MEMORY_DEVICE, stream_);
-        if (status != PSGB_OK && !solve_status(status)) throw StatusError(status, psgb_last_error());
-        for (std::size_t i = 0; i < n; ++i)
-            if (active[i])
-                PSGB_CUDA(cudaMemcpyAsync(results[i], states_ + offset_[i], cells_[i] * sizeof(double),
-                                          cudaMemcpyDeviceToHost, stream_));
-        PSGB_CUDA(cudaStreamSynchronize(stream_));
-    }
-
-    void read_state(std::size_t i, double* out) override {
-        PSGB_CUDA(cudaMemcpyAsync(out, states_ + offset_[i], cells_[i] * sizeof(double), cudaMemcpyDeviceToHost,
-                                  stream_));
-        PSGB_CUDA(cudaStreamSynchronize(stream_));
-    }
-
-  private:
     psgb_solve_options options_;
     psgb_batch* batch_ = nullptr;
     cudaStream_t stream_ = nullptr;
