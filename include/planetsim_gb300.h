@@ -519,8 +519,9 @@ int psgb_substep_mean_insolation_gpu(psgb_planet* planet, int64_t substep, float
  * round join the next one, and the lanes' rounds overlap on the GPU. Lanes are admitted
  * against a device-memory budget: the least recently used idle lanes are evicted first
  * (their temperatures copied back to the host), or the lane waits until one goes idle; a
- * lane larger than the budget fails its requests with PSGB_ERR_BUDGET. A request's new
- * temperature is the step from the planet's state after its earlier requests. */
+ * lane larger than the budget fails its requests with PSGB_ERR_BUDGET. Under memory
+ * pressure lanes take turns (yield_after_s). A request's new temperature is the step from
+ * the planet's state after its earlier requests. */
 typedef struct psgb_server psgb_server;
 
 typedef struct psgb_server_config {
@@ -530,6 +531,8 @@ typedef struct psgb_server_config {
     int autotune;                 /* nonzero: tune each lane at its first admission (psgb_batch_autotune),
                                      reapplied at later admissions */
     int device;                   /* CUDA device of the lanes */
+    double yield_after_s;         /* a lane waiting for memory this long makes the resident lanes
+                                     that stepped since take turns with it (<= 0: 0.25 s) */
 } psgb_server_config;
 
 typedef struct psgb_server_stats {

@@ -134,7 +134,7 @@ class StepReport(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("budget_bytes", C.c_double), ("bytes_per_cell", C.c_double), ("options", SolveOptions),
-                ("autotune", C.c_int), ("device", C.c_int)]
+                ("autotune", C.c_int), ("device", C.c_int), ("yield_after_s", C.c_double)]
 
 
 class ServerStats(C.Structure):

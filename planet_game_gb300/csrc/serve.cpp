@@ -245,8 +245,10 @@ int psgb_server_create(const psgb_server_config* config, psgb_server** out) {
         auto backend = std::make_unique<psgb::serve::GpuBackend>(*config);
         auto h = std::make_unique<psgb_server>();
         h->backend = backend.get();
+        require(std::isfinite(config->yield_after_s), "the yield delay must be finite");
+        const double yield_after = config->yield_after_s > 0.0 ? config->yield_after_s : 0.25;
         h->server = std::make_unique<psgb::serve::Server>(std::move(backend), config->budget_bytes,
-                                                          psgb::serve::map_error);
+                                                          psgb::serve::map_error, yield_after);
         *out = h.release();
         return PSGB_OK;
     });

@@ -13,10 +13,32 @@ bool Server::LaneState::has_work() const {
     return false;
 }
 
-Server::Server(std::unique_ptr<Backend> backend, double budget_bytes, ErrorMapper mapper)
-    : backend_(std::move(backend)), budget_(budget_bytes), mapper_(mapper), start_(std::chrono::steady_clock::now()) {
+Server::Server(std::unique_ptr<Backend> backend, double budget_bytes, ErrorMapper mapper, double yield_after_s)
+    : backend_(std::move(backend)),
+      budget_(budget_bytes),
+      mapper_(mapper),
+      yield_after_s_(yield_after_s),
+      start_(std::chrono::steady_clock::now()) {
     if (!backend_ || mapper_ == nullptr) throw std::invalid_argument("serve: null backend or error mapper");
     if (!(budget_bytes > 0.0)) throw std::invalid_argument("serve: the memory budget must be positive");
+    if (!(yield_after_s >= 0.0)) throw std::invalid_argument("serve: the yield delay must be non-negative");
+}
+
+bool Server::yields_to(const LaneState* o, const LaneState* waiter, double now) const {
+    return waiter != o && waiter->waiting_since_s >= 0.0 && now - waiter->waiting_since_s >= yield_after_s_ &&
+           o->last_used_s >= waiter->waiting_since_s;
+}
+
+const Server::LaneState* Server::starving_waiter(const LaneState* o, double now) const {
+    for (const auto& [level, w] : lanes_)
+        if (yields_to(o, w.get(), now)) return w.get();
+    return nullptr;
+}
+
+void Server::stop_waiting(LaneState* L) {
+    if (L->waiting_since_s < 0.0) return;
+    L->waiting_since_s = -1.0;
+    for (auto& [level, lane] : lanes_) lane->cv.notify_all();   // lanes that yielded to it resume
 }
 
 Server::~Server() {
@@ -206,31 +228,43 @@ bool Server::admit(LaneState* L, std::unique_lock<std::mutex>& lock) {
     } catch (...) {
         std::string message;
         const int status = mapper_(std::current_exception(), message);
+        stop_waiting(L);
         fail_queued(L, status, message);
         return false;
     }
     if (static_cast<double>(need) > budget_) {
+        stop_waiting(L);
         fail_queued(L, PSGB_ERR_BUDGET, "serve: the lane's device memory exceeds the budget");
         return false;
     }
-    // the least recently used idle lanes go until the new one fits
+    // idle lanes go first (least recently used first), then lanes yielding to this one
+    const double now = now_s();
     std::vector<LaneState*> victims;
     std::uint64_t freed = 0;
     while (static_cast<double>(resident_bytes_ - freed + need) > budget_) {
         LaneState* victim = nullptr;
+        bool victim_idle = false;
         for (auto& [level, other] : lanes_) {
             LaneState* o = other.get();
-            if (o == L || o->phase != Phase::Resident || o->busy || o->has_work()) continue;
+            if (o == L || o->phase != Phase::Resident || o->busy) continue;
+            const bool idle = !o->has_work();
+            if (!idle && !yields_to(o, L, now)) continue;
             if (std::find(victims.begin(), victims.end(), o) != victims.end()) continue;
-            if (victim == nullptr || o->last_used_s < victim->last_used_s) victim = o;
+            if (victim == nullptr || (idle && !victim_idle) ||
+                (idle == victim_idle && o->last_used_s < victim->last_used_s)) {
+                victim = o;
+                victim_idle = idle;
+            }
         }
-        if (victim == nullptr) {   // every resident lane is busy: wait for one to go idle
-            memory_cv_.wait(lock);
+        if (victim == nullptr) {   // every resident lane is busy: wait for one to go idle or yield
+            if (L->waiting_since_s < 0.0) L->waiting_since_s = now;
+            memory_cv_.wait_for(lock, std::chrono::duration<double>(std::max(yield_after_s_, 1e-3)));
             return false;
         }
         victims.push_back(victim);
         freed += victim->bytes;
     }
+    stop_waiting(L);
     for (LaneState* v : victims) v->phase = Phase::Evicting;
     L->phase = Phase::Admitting;
     lock.unlock();
@@ -297,6 +331,11 @@ void Server::run_lane(LaneState* L) {
         }
         if (L->phase == Phase::Absent) {
             admit(L, lock);
+            continue;
+        }
+        if (starving_waiter(L, now_s()) != nullptr) {   // make way: stay idle until evicted or no longer asked
+            memory_cv_.notify_all();
+            L->cv.wait_for(lock, std::chrono::duration<double>(std::max(yield_after_s_, 1e-3)));
             continue;
         }
         // one round: the oldest request of every planet with queued work

@@ -11,8 +11,12 @@
 // Admission is bounded by a device-memory budget: a lane with queued requests that is not
 // resident reserves its estimated bytes, evicting the least recently used idle lanes
 // (resident, not stepping, nothing queued) first, or waits until a lane goes idle. A lane
-// whose own estimate exceeds the budget fails its requests with PSGB_ERR_BUDGET. An
-// evicted lane's states are copied back to the host first, so no sub-step is lost.
+// that has waited longer than `yield_after_s` makes the resident lanes that stepped since
+// it began waiting yield after their running round, so that under memory pressure the
+// lanes take turns instead of a busy lane holding the memory for as long as its requests
+// keep coming. A lane whose own estimate exceeds the budget fails its requests with
+// PSGB_ERR_BUDGET. An evicted lane's states are copied back to the host first, so no
+// sub-step is lost.
 //
 // The device side is behind Backend/Lane (serve.cpp runs them on the GPU through the batch
 // entry points; the host tests use a fake), so this file has no CUDA code.
@@ -85,7 +89,7 @@ using ErrorMapper = int (*)(std::exception_ptr error, std::string& message);
 
 class Server {
   public:
-    Server(std::unique_ptr<Backend> backend, double budget_bytes, ErrorMapper mapper);
+    Server(std::unique_ptr<Backend> backend, double budget_bytes, ErrorMapper mapper, double yield_after_s = 0.25);
     ~Server();   // stops the lanes after their current round; queued requests fail
     Server(const Server&) = delete;
     Server& operator=(const Server&) = delete;
@@ -125,6 +129,7 @@ class Server {
         bool busy = false;        // a round (or a state read) is using the resident lane
         std::uint64_t bytes = 0;  // reserved while resident
         double last_used_s = 0.0;
+        double waiting_since_s = -1.0;   // waiting for memory since (negative: not waiting)
         std::condition_variable cv;
         std::thread thread;
         bool has_work() const;
@@ -135,10 +140,16 @@ class Server {
     void fail_queued(LaneState* lane, int status, const std::string& message);
     void complete(const std::vector<std::shared_ptr<Request>>& round, int status, const std::string& message);
     double now_s() const;
+    // True when resident lane `o` must make way for lane `waiter` (waiting long enough, and
+    // `o` has stepped since it began waiting).
+    bool yields_to(const LaneState* o, const LaneState* waiter, double now) const;
+    const LaneState* starving_waiter(const LaneState* o, double now) const;
+    void stop_waiting(LaneState* lane);
 
     std::unique_ptr<Backend> backend_;
     const double budget_;
     ErrorMapper mapper_;
+    const double yield_after_s_;
     std::mutex mu_;
     std::condition_variable done_cv_, memory_cv_;
     std::vector<std::unique_ptr<PlanetRecord>> planets_;   // stable addresses for the lanes

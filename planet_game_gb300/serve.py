@@ -289,7 +289,8 @@ class NativeServer:
     of device memory; `solver` as for `api.solve_options`."""
 
     def __init__(self, budget_bytes: float = 150e9, precision: str = "mixed", method: str = "bicgstab",
-                 autotune: bool = True, device: int = 0, bytes_per_cell: float = 700.0, **solver):
+                 autotune: bool = True, device: int = 0, bytes_per_cell: float = 700.0, yield_after_s: float = 0.25,
+                 **solver):
         import ctypes as C
 
         self._C = C
@@ -297,7 +298,7 @@ class NativeServer:
         cfg = capi.ServerConfig()
         cfg.budget_bytes, cfg.bytes_per_cell = float(budget_bytes), float(bytes_per_cell)
         cfg.options = api.solve_options(precision=precision, method=method, **solver)
-        cfg.autotune, cfg.device = int(bool(autotune)), int(device)
+        cfg.autotune, cfg.device, cfg.yield_after_s = int(bool(autotune)), int(device), float(yield_after_s)
         handle = C.c_void_p()
         capi.check(self._lib.psgb_server_create(C.byref(cfg), C.byref(handle)))
         self._h = handle

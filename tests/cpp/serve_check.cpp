@@ -306,6 +306,34 @@ void concurrent_producers_under_a_tight_budget() {
     CHECK(static_cast<double>(st.resident_bytes) <= 2 * 3 * 16 * 10 + 5);
 }
 
+// A budget for one lane and two busy levels: past the yield delay the resident lane makes
+// way after its round, so the lanes take turns (with their states) instead of the second
+// waiting until the first has drained its queue.
+void lanes_take_turns_under_pressure() {
+    Counters c;
+    Server s(std::make_unique<FakeBackend>(c, 1), 8 + 4, map_error, 0.010);   // one lane of 8 cells
+    const std::uint32_t a = s.add_planet(planet(4, 8, 10.0));
+    const std::uint32_t b = s.add_planet(planet(5, 8, 20.0));
+    const int n = 40;   // 40 rounds of 3 ms per lane
+    std::vector<double> one(8, 1.0);
+    std::vector<std::uint64_t> ra, rb;
+    for (int k = 0; k < n; ++k) ra.push_back(s.submit(a, one.data()));
+    std::this_thread::sleep_for(std::chrono::milliseconds(2));   // a is resident and busy
+    for (int k = 0; k < n; ++k) rb.push_back(s.submit(b, one.data()));
+    std::string msg;
+    std::vector<double> out(8);
+    CHECK(s.wait(rb.front(), 30.0, out.data(), nullptr, msg) == PSGB_OK && out[0] == 20.5);
+    // b's first request finished while a still had work queued
+    CHECK(s.wait(ra.back(), 0.0, nullptr, nullptr, msg) == PSGB_ERR_TIMEOUT);
+    for (int k = 0; k < n; ++k) {
+        CHECK(s.wait(ra[k], 30.0, out.data(), nullptr, msg) == PSGB_OK && out[3] == 10.0 + 0.5 * (k + 1));
+        if (k > 0) CHECK(s.wait(rb[k], 30.0, out.data(), nullptr, msg) == PSGB_OK && out[3] == 20.0 + 0.5 * (k + 1));
+    }
+    const Stats st = s.stats();
+    CHECK(st.evictions >= 2 && st.failed == 0 && st.completed == 2 * n);
+    CHECK(static_cast<double>(st.resident_bytes) <= 12.0 && c.lanes_alive.load() == 1);
+}
+
 }  // namespace
 
 int main() {
@@ -314,6 +342,7 @@ int main() {
     failures_are_reported();
     timeouts_and_close();
     concurrent_producers_under_a_tight_budget();
+    lanes_take_turns_under_pressure();
     if (failures == 0) std::printf("OK\n");
     return failures == 0 ? 0 : 1;
 }
