@@ -4,7 +4,8 @@
   (tests/cpp/serve_check.cpp): per-planet request order, continuous batching (one round
   steps every planet of a lane with queued work; lanes step side by side), the memory
   budget (least recently used idle lane evicted with its states copied back; a lane larger
-  than the budget refused), failures reported per request, timeouts and shutdown;
+  than the budget refused; lanes taking turns when one waits for memory), concurrent
+  producers, failures reported per request, timeouts and shutdown;
 - the C entry points and their Python wrapper (serve.NativeServer): argument checks, and a
   lane that cannot reach a GPU failing its requests with the CUDA status instead of
   hanging."""
