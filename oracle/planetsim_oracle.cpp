@@ -82,6 +82,8 @@ struct Level {
 
 struct Hierarchy {
     std::vector<Level> levels;
+    // per-level scratch of the SGS V-cycle (one solve at a time per hierarchy)
+    mutable std::vector<std::vector<double>> prev, rhs, sol;
     // exported copies for the C ABI
     std::vector<std::vector<std::uint32_t>> x_off, x_col, x_agg;
     std::vector<std::vector<std::int64_t>> x_tgt;
@@ -228,7 +230,8 @@ void set_values(Hierarchy& h) {
 }
 
 // Symmetric block-hybrid Gauss-Seidel half sweep (heat_transport.cpp:258-286).
-void gauss_seidel(const Level& L, const std::vector<double>& b, std::vector<double>& x, bool forward, bool blocked) {
+void gauss_seidel(const Level& L, const std::vector<double>& b, std::vector<double>& x, bool forward, bool blocked,
+                  std::vector<double>& prev) {
     if (!blocked) {
         for (std::size_t s = 0; s < L.size; ++s) {
             const std::size_t r = forward ? s : L.size - 1 - s;
@@ -238,7 +241,7 @@ void gauss_seidel(const Level& L, const std::vector<double>& b, std::vector<doub
         }
         return;
     }
-    const std::vector<double> prev = x;
+    prev.assign(x.begin(), x.end());
     for (std::size_t b0 = 0; b0 < L.size; b0 += kBlock) {
         const std::size_t b1 = std::min(L.size, b0 + kBlock);
         for (std::size_t s = 0; s < b1 - b0; ++s) {
@@ -259,20 +262,25 @@ void vcycle_sgs(const Hierarchy& h, std::size_t l, const std::vector<double>& b,
         chol_solve(L, b, x);
         return;
     }
+    if (h.prev.size() != h.levels.size()) {
+        h.prev.resize(h.levels.size());
+        h.rhs.resize(h.levels.size());
+        h.sol.resize(h.levels.size());
+    }
     x.assign(L.size, 0.0);
-    gauss_seidel(L, b, x, true, l == 0);
-    std::vector<double> r(L.size, 0.0);
+    gauss_seidel(L, b, x, true, l == 0, h.prev[l]);
+    // residual and restriction: the coarse sums take the residuals in ascending row order
+    std::vector<double>& bc = h.rhs[l + 1];
+    bc.assign(h.levels[l + 1].size, 0.0);
     for (std::size_t i = 0; i < L.size; ++i) {
         double v = b[i] - L.diag[i] * x[i];
         for (std::size_t k = L.off[i]; k < L.off[i + 1]; ++k) v -= L.val[k] * x[L.col[k]];
-        r[i] = v;
+        bc[L.agg[i]] += v;
     }
-    std::vector<double> bc(h.levels[l + 1].size, 0.0);
-    for (std::size_t i = 0; i < L.size; ++i) bc[L.agg[i]] += r[i];
-    std::vector<double> xc;
+    std::vector<double>& xc = h.sol[l + 1];
     vcycle_sgs(h, l + 1, bc, xc);
     for (std::size_t i = 0; i < L.size; ++i) x[i] += xc[L.agg[i]];
-    gauss_seidel(L, b, x, false, l == 0);
+    gauss_seidel(L, b, x, false, l == 0, h.prev[l]);
 }
 
 // The GB300 V-cycle's algorithm: damped Jacobi (pre sweeps from zero, post sweeps),
