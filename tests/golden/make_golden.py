@@ -218,7 +218,7 @@ def half_fluxes(g: dict, flows: np.ndarray, layers: int) -> np.ndarray:
     return flows.reshape(layers, E)[:, upper_entries(g)].copy()
 
 
-def nonsym_cases(R) -> None:
+def nonsym_cases(R, write: bool = True) -> dict:
     """The non-symmetric solves of the reference (heat_transport.cpp:774-1318) and its
     block ILU(0) (incomplete_lu.cpp), on the L3 mesh graph, the L3 mesh's agglomerated
     graph and the L4 mesh graph; inputs are seeded numpy draws shaped like the
@@ -297,10 +297,12 @@ def nonsym_cases(R) -> None:
         if lat is not None:
             out[f"ad_{tag}_latent"] = lat
     R.refd_mesh_free(m3)
-    np.savez_compressed(HERE / "nonsym.npz", **out)
+    if write:
+        np.savez_compressed(HERE / "nonsym.npz", **out)
+    return out
 
 
-def quartic_cases(R) -> None:
+def quartic_cases(R, write: bool = True) -> dict:
     """The nonlinear transport solve with the reference test's quartic response
     (tests/unit/test_heat_transport.cpp:30-76, 112-146) at L4: heat capacities of a month
     and of ten minutes, the test's conductance and ten times it. The local forcings b put
@@ -329,8 +331,10 @@ def quartic_cases(R) -> None:
             key = f"{ia}_{int(factor)}"
             out[f"K{key}"], out[f"floor{key}"], out[f"mean{key}"] = K, floor, mean
             out[f"source{key}"], out[f"stats{key}"] = src, stats
-    np.savez_compressed(HERE / "newton_quartic_L4.npz", **out)
+    if write:
+        np.savez_compressed(HERE / "newton_quartic_L4.npz", **out)
     R.refd_mesh_free(m)
+    return out
 
 
 def mesh_arrays(R, m) -> dict:

@@ -2,7 +2,9 @@
 sources are present, its code (compiled where it lies by oracle/Makefile.ref, driven by
 oracle/ref_driver.cpp through tests/golden/make_golden.py's loader) is run again and must
 give the committed values bit for bit: the L0-L2 meshes' arrays, the L3-L8 meshes' and
-hierarchies' digests, and the agglomerated graphs at L0/L1/L3/L5 and their L6-L8 digests.
+hierarchies' digests, the agglomerated graphs at L0/L1/L3/L5 and their L6-L8 digests, the
+non-symmetric solves' fixture (block ILU(0), advection source, tracer, coupled solve) and
+the quartic-response transport solves.
 Skipped where the reference is absent (the GPU host)."""
 import importlib.util
 import json
@@ -97,3 +99,13 @@ def test_agglomeration_digest_at_l6_is_the_reference_one(maker):
     assert len(fresh["area"]) == want["nodes"]
     for key, value in fresh.items():
         assert mg.sha(value) == want[key], key
+
+
+@pytest.mark.parametrize("name,fixture", [("nonsym_cases", "nonsym.npz"), ("quartic_cases", "newton_quartic_L4.npz")])
+def test_solve_fixtures_are_the_reference_ones(maker, name, fixture):
+    mg, R = maker
+    fresh = getattr(mg, name)(R, write=False)
+    committed = golden(fixture)
+    assert sorted(fresh) == sorted(committed.files)
+    for key, value in fresh.items():
+        assert np.array_equal(np.asarray(value), committed[key]), key
