@@ -382,8 +382,17 @@ def hierarchy(R, m) -> list[dict]:
     return out
 
 
-def main(reference: Path) -> None:
+def main(reference: Path, write: bool = True) -> dict:
+    """Every fixture below; written to tests/golden/ when `write`, returned either way
+    (file name -> arrays, or the digests' dictionary for golden.json)."""
     R = load(reference)
+    made: dict = {}
+
+    def save(name: str, **arrays):
+        made[name] = arrays
+        if write:
+            np.savez_compressed(HERE / name, **arrays)
+
     rng = np.random.default_rng(20261203)
     meta = {"radius_m": RADIUS, "mesh_sha256": {}, "hierarchy_sha256": {}}
 
@@ -393,7 +402,7 @@ def main(reference: Path) -> None:
         a = mesh_arrays(R, m)
         meta["mesh_sha256"][str(level)] = {k: sha(v) for k, v in a.items()}
         if level <= 2:
-            np.savez_compressed(HERE / f"mesh_L{level}.npz", **a)
+            save(f"mesh_L{level}.npz", **a)
         if level >= 3:
             hl = hierarchy(R, m)
             meta["hierarchy_sha256"][str(level)] = [{k: sha(v) for k, v in lv.items()} | {"rows": int(len(lv["offset"]) - 1)}
@@ -421,7 +430,7 @@ def main(reference: Path) -> None:
     ds = np.empty(n)
     R.refd_diffusion_source(m, 4e13, p(t), p(ds))
     out.update({"temperature": t, "diffusion_source": ds, "conductance": 4e13})
-    np.savez_compressed(HERE / "operators_L4.npz", **out)
+    save("operators_L4.npz", **out)
 
     # ---- Newton driver with a linear response at L4 (test_heat_transport.cpp:80-107 style)
     base = 250.0 + 50.0 * rng.random(n)
@@ -429,7 +438,7 @@ def main(reference: Path) -> None:
     K = 0.5 * RADIUS * RADIUS
     mean, src, stats = np.empty(n), np.empty(n), np.empty(6)
     R.refd_solve_linear(m, K, p(base), p(slope), 1e-6, 1e-6, 4, p(mean), p(src), p(stats))
-    np.savez_compressed(HERE / "newton_L4.npz", base=base, slope=slope, conductance=K, cg_tolerance=1e-6,
+    save("newton_L4.npz", base=base, slope=slope, conductance=K, cg_tolerance=1e-6,
                         newton_tolerance=1e-6, mean=mean, source=src, stats=stats)
 
     # insolation at L4 (substep_forcing.cpp) and its nodes
@@ -437,7 +446,7 @@ def main(reference: Path) -> None:
     R.refd_insolation(m, 0, p(ins))
     nodes = np.empty(80)
     R.refd_insolation_nodes(0, p(nodes))
-    np.savez_compressed(HERE / "insolation_L4.npz", insolation=ins, nodes=nodes.reshape(16, 5))
+    save("insolation_L4.npz", insolation=ins, nodes=nodes.reshape(16, 5))
     R.refd_mesh_free(m)
 
     # ---- multigrid + PCG at L5 with the heat-step matrix ---------------------------------
@@ -474,7 +483,7 @@ def main(reference: Path) -> None:
     R.refd_hierarchy_free(h)
     x = np.empty(n)
     it = R.refd_pcg(m, K, p(s), p(rhs), 1e-12, 2000, 1, p(x))
-    np.savez_compressed(HERE / "heatstep_L5.npz", t0=t0, source=S, insolation=ins, heat_capacity=C_heat,
+    save("heatstep_L5.npz", t0=t0, source=S, insolation=ins, heat_capacity=C_heat,
                         diffusivity=kappa, dt=dt, rhs=rhs, vcycle_rhs=vrhs, vcycle_out=vout, pcg_x=x,
                         pcg_iterations=it, pcg_tolerance=1e-12, **galerkin)
     R.refd_mesh_free(m)
@@ -510,16 +519,19 @@ def main(reference: Path) -> None:
         col_out.update({f"temperature{N}": temp, f"humidity{N}": q, f"cloud_water{N}": ql, f"surface_temperature{N}": ts,
                         f"surface_pressure{N}": ps, f"emissivity{N}": eps, f"absorbed{N}": absb, f"fraction{N}": fr,
                         f"reflectance{N}": refl, f"scalars{N}": sc})
-    np.savez_compressed(HERE / "column.npz", **col_out)
+    save("column.npz", **col_out)
 
     # ---- saturation (saturation.cpp) ------------------------------------------------------
     T = np.linspace(180.0, 320.0, 57)
     Pp = np.array([5e3, 2e4, 5e4, 8e4, 1e5])
     qs = np.array([[R.refd_saturation_specific_humidity(tt, pp) for pp in Pp] for tt in T])
-    np.savez_compressed(HERE / "saturation.npz", temperature=T, pressure=Pp, qsat=qs)
+    save("saturation.npz", temperature=T, pressure=Pp, qsat=qs)
 
-    (HERE / "golden.json").write_text(json.dumps(meta, indent=1, sort_keys=True))
-    print("golden fixtures written")
+    made["golden.json"] = meta
+    if write:
+        (HERE / "golden.json").write_text(json.dumps(meta, indent=1, sort_keys=True))
+        print("golden fixtures written")
+    return made
 
 
 if __name__ == "__main__":

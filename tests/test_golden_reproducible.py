@@ -3,8 +3,10 @@ sources are present, its code (compiled where it lies by oracle/Makefile.ref, dr
 oracle/ref_driver.cpp through tests/golden/make_golden.py's loader) is run again and must
 give the committed values bit for bit: the L0-L2 meshes' arrays, the L3-L8 meshes' and
 hierarchies' digests, the agglomerated graphs at L0/L1/L3/L5 and their L6-L8 digests, the
-non-symmetric solves' fixture (block ILU(0), advection source, tracer, coupled solve) and
-the quartic-response transport solves.
+non-symmetric solves' fixture (block ILU(0), advection source, tracer, coupled solve), the
+quartic-response transport solves, and every fixture of the main set (operators, the
+linear Newton solve, insolation, the L5 heat step with its Galerkin values, V-cycle and PCG,
+column radiation, saturation, the digests).
 Skipped where the reference is absent (the GPU host)."""
 import importlib.util
 import json
@@ -109,3 +111,15 @@ def test_solve_fixtures_are_the_reference_ones(maker, name, fixture):
     assert sorted(fresh) == sorted(committed.files)
     for key, value in fresh.items():
         assert np.array_equal(np.asarray(value), committed[key]), key
+
+
+def test_main_fixtures_are_the_reference_ones(maker):
+    mg, R = maker
+    ref = _reference()
+    made = mg.main(ref, write=False)
+    assert made.pop("golden.json") == golden("golden.json")
+    for name, arrays in made.items():
+        committed = golden(name)
+        assert sorted(arrays) == sorted(committed.files), name
+        for key, value in arrays.items():
+            assert np.array_equal(np.asarray(value), committed[key]), (name, key)
