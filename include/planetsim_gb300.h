@@ -20,7 +20,10 @@
  * or on one batch, must not overlap.
  *
  * ABI version 2: psgb_planet_info and psgb_tuning grew fields (fine_cells; the coarse
- * tail's spread and block count).
+ * tail's spread and block count). Version 3: the serving loop (psgb_server_*) and
+ * PSGB_ERR_TIMEOUT.
+ *
+ * A server's calls may come from any thread; its lanes step on threads of their own.
  */
 #ifndef PLANETSIM_GB300_H
 #define PLANETSIM_GB300_H
