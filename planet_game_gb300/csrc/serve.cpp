@@ -270,15 +270,16 @@ int psgb_server_add_planet(psgb_server* server, uint32_t level, double radius_m,
         const int status = psgb_planet_create(level, radius_m, &raw);
         if (status != PSGB_OK) return psgb::capi::fail(status, psgb_last_error());
         std::unique_ptr<psgb_planet, void (*)(psgb_planet*)> handle(raw, psgb_planet_destroy);
-        const psgb::Planet& p = *raw->planet;
+        psgb_planet_info info{};
+        if (psgb_planet_info_get(raw, &info) != PSGB_OK) return psgb::capi::fail(PSGB_ERR_LOGIC, psgb_last_error());
         psgb::serve::PlanetRecord rec;
         rec.level = level;
-        rec.cells = static_cast<std::uint32_t>(p.mesh.cells);
+        rec.cells = static_cast<std::uint32_t>(info.cells);
         rec.heat_capacity_J_m2_K = params->heat_capacity_J_m2_K;
         rec.dt_s = params->dt_s;
         rec.conductance_W_K = params->conductance_W_K;
         if (params->edge_conductance != nullptr) {
-            rec.edge_conductance.assign(params->edge_conductance, params->edge_conductance + p.mesh.edges);
+            rec.edge_conductance.assign(params->edge_conductance, params->edge_conductance + info.edges);
             for (double e : rec.edge_conductance)
                 require(std::isfinite(e) && e >= 0.0, "edge conductances must be finite and non-negative");
         }

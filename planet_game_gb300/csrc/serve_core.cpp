@@ -194,9 +194,10 @@ void Server::complete(const std::vector<std::shared_ptr<Request>>& round, int st
     const double t = now_s();
     for (const auto& r : round) {
         if (!r) continue;
-        if (status != PSGB_OK) {
+        if (status != PSGB_OK) {   // the round failed: no new temperature
             r->status = status;
             r->message = message;
+            r->result.clear();
         } else {
             r->status = r->report.solve.status;
         }

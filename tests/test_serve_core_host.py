@@ -6,10 +6,16 @@
   budget (least recently used idle lane evicted with its states copied back; a lane larger
   than the budget refused; lanes taking turns when one waits for memory), concurrent
   producers, failures reported per request, timeouts and shutdown;
+- its device side (serve.cpp) with the CUDA runtime and the batch entry points replaced by
+  host stand-ins (tests/cpp/serve_gpu_lane_check.cpp): the lanes' layout of states and
+  sources, stored per-edge conductances, tuning once per level and reused after eviction,
+  states surviving eviction, per-request solve statuses, failed rounds keeping the state,
+  and everything freed with the server;
 - the C entry points and their Python wrapper (serve.NativeServer): argument checks, and a
   lane that cannot reach a GPU failing its requests with the CUDA status instead of
   hanging."""
 import ctypes as C
+import os
 import shutil
 import subprocess
 from pathlib import Path
@@ -26,6 +32,21 @@ def test_serving_loop_host_logic(tmp_path):
     exe = tmp_path / "serve_check"
     csrc = ROOT / "planet_game_gb300" / "csrc"
     subprocess.run(["g++", "-std=c++17", "-O1", "-pthread", "-I", str(csrc), str(ROOT / "tests" / "cpp" / "serve_check.cpp"),
+                    str(csrc / "serve_core.cpp"), "-o", str(exe)], check=True, capture_output=True, text=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0 and out.stdout.strip() == "OK", out.stdout + out.stderr
+
+
+def test_serving_loop_device_side_with_host_stand_ins(tmp_path):
+    if shutil.which("g++") is None:
+        pytest.skip("no C++ compiler")
+    cuda_include = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "include"
+    if not (cuda_include / "cuda_runtime.h").exists():
+        pytest.skip("no CUDA headers")
+    exe = tmp_path / "serve_gpu_lane_check"
+    csrc = ROOT / "planet_game_gb300" / "csrc"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-pthread", "-I", str(csrc), "-I", str(cuda_include),
+                    str(ROOT / "tests" / "cpp" / "serve_gpu_lane_check.cpp"), str(csrc / "serve.cpp"),
                     str(csrc / "serve_core.cpp"), "-o", str(exe)], check=True, capture_output=True, text=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert out.returncode == 0 and out.stdout.strip() == "OK", out.stdout + out.stderr
