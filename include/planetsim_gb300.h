@@ -564,6 +564,8 @@ int psgb_server_wait(psgb_server* server, uint64_t request, double timeout_s, do
 /* The planet's temperature after its finished requests (HOST, cells). */
 int psgb_server_state(psgb_server* server, uint32_t planet, double* t_K);
 int psgb_server_stats_get(psgb_server* server, psgb_server_stats* out);
+/* Forgets the counts and latencies so far (after a warm-up); resident lanes stay. */
+int psgb_server_stats_reset(psgb_server* server);
 
 #ifdef __cplusplus
 }

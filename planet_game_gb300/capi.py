@@ -221,6 +221,7 @@ _SIGNATURES = {
     "psgb_server_wait": (C.c_int, [P, C.c_uint64, C.c_double, P, C.POINTER(StepReport)]),
     "psgb_server_state": (C.c_int, [P, C.c_uint32, P]),
     "psgb_server_stats_get": (C.c_int, [P, C.POINTER(ServerStats)]),
+    "psgb_server_stats_reset": (C.c_int, [P]),
     "psgb_launch_count": (C.c_uint64, []),
     "psgb_profile_begin": (C.c_int, [C.c_char_p]),
     "psgb_profile_end": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),

@@ -333,4 +333,12 @@ int psgb_server_stats_get(psgb_server* server, psgb_server_stats* out) {
     });
 }
 
+int psgb_server_stats_reset(psgb_server* server) {
+    return guarded([&] {
+        require(server != nullptr, "null argument");
+        server->server->reset_stats();
+        return PSGB_OK;
+    });
+}
+
 }  // extern "C"

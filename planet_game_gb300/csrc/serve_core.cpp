@@ -179,6 +179,12 @@ Stats Server::stats() {
     return s;
 }
 
+void Server::reset_stats() {
+    std::lock_guard<std::mutex> lock(mu_);
+    counts_ = Stats{};
+    latencies_ms_.clear();
+}
+
 void Server::fail_queued(LaneState* L, int status, const std::string& message) {
     std::vector<std::shared_ptr<Request>> failed;
     for (auto& q : L->queue) {

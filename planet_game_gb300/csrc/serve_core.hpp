@@ -105,6 +105,8 @@ class Server {
     // The planet's temperature after its completed requests (waits for a running round).
     void state(std::uint32_t planet, double* out);
     Stats stats();
+    // Forgets the counts and latencies so far (e.g. after a warm-up); resident lanes stay.
+    void reset_stats();
     std::uint32_t cells(std::uint32_t planet);
 
   private:

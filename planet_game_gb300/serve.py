@@ -348,6 +348,9 @@ class NativeServer:
         capi.check(self._lib.psgb_server_stats_get(self._h, self._C.byref(st)))
         return {name: getattr(st, name) for name, _ in capi.ServerStats._fields_}
 
+    def reset_stats(self) -> None:
+        capi.check(self._lib.psgb_server_stats_reset(self._h))
+
     def close(self) -> None:
         if getattr(self, "_h", None) is not None:
             self._lib.psgb_server_destroy(self._h)

@@ -167,6 +167,9 @@ void continuous_batching_and_order() {
     CHECK(c.max_round_size.load() == 3);             // a round steps every planet of its level with work
     CHECK(c.max_concurrent.load() >= 2);             // lanes stepped side by side
     CHECK(st.p99_ms >= st.p50_ms && st.p50_ms > 0.0);
+    s.reset_stats();
+    const Stats zero = s.stats();
+    CHECK(zero.submitted == 0 && zero.completed == 0 && zero.p50_ms == 0.0 && zero.resident_lanes == 3);
     std::string msg;
     bool unknown_refused = false;
     try {

@@ -136,3 +136,4 @@ def test_python_wrapper_of_the_native_server():
             srv.add_planet(2, 6.371e6, 4e7, 0.0, 4e13, t0)
         stats = srv.stats()
         assert stats["planets"] == 1 and stats["submitted"] == 0
+        srv.reset_stats()
