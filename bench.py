@@ -403,7 +403,55 @@ def serving_point(args, dev, rate: float, count: int, population=None) -> dict:
         out[name] = summary
     a, b = out["continuous_batching_mixed"], out["one_at_a_time_fp64"]
     out["speedup_sub_steps_per_s"] = a["sub_steps_per_s"] / b["sub_steps_per_s"]
+    if getattr(args, "native_serve", False):
+        out["continuous_batching_native"] = native_serving_point(args, dev, rate, count)
     return out
+
+
+def native_serving_point(args, dev, rate: float, count: int) -> dict:
+    """The same trace through the library's own serving loop (psgb_server_*): lanes and
+    their threads in C++, host arrays in and out; latency from submission to completion as
+    the loop records it, after a warm-up that admits and tunes every lane."""
+    from planet_game_gb300 import serve
+    from planet_game_gb300 import workloads as W
+
+    pop = build_serve_population(dev)
+    trace = W.poisson_trace(count, rate, seed=args.seed + 1, planets_per_level=max(SERVE_POPULATION.values()))
+    trace = [W.Request(r.arrival_s, r.level, r.planet % SERVE_POPULATION[r.level]) for r in trace]
+    reqs = serve.make_requests(trace, pop, seed=args.seed + 2)
+    warm = serve.make_requests(trace[:40], pop, seed=args.seed + 3)
+    srv = serve.NativeServer(budget_bytes=150e9, precision="mixed", **SOLVER_SERVE)
+    try:
+        ids = {}
+        for level, planets in pop.items():
+            for i, p in enumerate(planets):
+                ids[(level, i)] = srv.add_planet(level, p.radius, p.heat_capacity, p.dt, p.conductance,
+                                                 p.state.cpu().numpy(), p.edge_conductance)
+        for level in pop:   # admit and tune every lane
+            pid = ids[(level, 0)]
+            srv.wait(srv.submit(pid, np.zeros(pop[level][0].mesh.cell_count)), pid)
+        for r in warm:
+            pid = ids[(r.level, r.planet)]
+            srv.wait(srv.submit(pid, r.source), pid)
+        srv.reset_stats()
+        t_start = time.perf_counter()
+        pending = []
+        for r in reqs:
+            delay = r.arrival_s - (time.perf_counter() - t_start)
+            if delay > 0:
+                time.sleep(delay)
+            pid = ids[(r.level, r.planet)]
+            pending.append((r, srv.submit(pid, r.source), pid))
+        for r, rid, pid in pending:
+            r.result, rep = srv.wait(rid, pid)
+            r.status = rep.solve.status
+        elapsed = time.perf_counter() - t_start
+        stats = srv.stats()
+    finally:
+        srv.close()
+    return {"requests": count, "sub_steps_per_s": count / elapsed, "p50_ms": stats["p50_ms"],
+            "p99_ms": stats["p99_ms"], "ok": int(sum(r.status == 0 for r in reqs)),
+            "latency": "submission to completion, recorded by the loop"}
 
 
 SOLVER_SERVE = dict(method="bicgstab", tolerance=1e-10, inner_tolerance=1e-4, poll=4)
@@ -633,6 +681,8 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=5000.0)
     ap.add_argument("--serve-requests", type=int, default=2000)
     ap.add_argument("--skip-serve", action="store_true")
+    ap.add_argument("--native-serve", action="store_true",
+                    help="serving: also run the trace through the library's own loop (psgb_server_*)")
     ap.add_argument("--seed", type=int, default=2026)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-plain", action="store_true")
