@@ -242,14 +242,19 @@ int psgb_transport_step(psgb_planet* planet, const psgb_step_params* params,
                         void* stream);
 
 /* The same step, allocating nothing (no counterpart in the reference). For callers that
- * may not call cudaMalloc or any other allocating CUDA routine while they run (a fixed
- * memory budget, code around stream capture or in a latency-critical loop where an
- * allocation could synchronise the device): all solver workspace lives in one static
- * 8 MiB device array of this library, which every GPU that loads the library holds until
- * the process exits. DEVICE pointers only, ordered on `stream`. Planets of at most 10,242
- * cells (a level-5 mesh); larger ones fail with PSGB_ERR_INVALID_ARGUMENT. The first call
- * on a device looks up that array's device address; make it before any stream capture.
- * Calls share the array: calls that overlap on the GPU race, serialise them. */
+ * may not call cudaMalloc or any other allocating CUDA routine while they run: a loop
+ * with a fixed memory budget reserved up front, a host that lends the library a GPU under
+ * a hard memory cap, a plugin host whose allocator owns the device memory. All solver
+ * workspace lives in one static 8 MiB device array of this library, which every GPU that
+ * loads the library holds until the process exits. DEVICE pointers only, ordered on
+ * `stream`; the call waits for `stream` before it returns. Planets of at most 10,242
+ * cells (a level-5 mesh); larger ones fail with PSGB_ERR_INVALID_ARGUMENT, and so does
+ * edge_conductance_stored (pass the per-edge array instead). The first call on a device
+ * looks up that array's device address; make it before any stream capture. CUDA loads
+ * kernels lazily by default, so make one warm-up call per precision (or set
+ * CUDA_MODULE_LOADING=EAGER) before relying on the no-allocation property. Calls share
+ * the array and it keeps the last call's contents: calls that overlap on the GPU race,
+ * serialise them. */
 int psgb_transport_step_noalloc(psgb_planet* planet, const psgb_step_params* params,
                                 const psgb_solve_options* options, const double* t0_K,
                                 const double* source_W_m2, double* t_new_K, double* transport_W_m2,
@@ -564,7 +569,10 @@ int psgb_server_wait(psgb_server* server, uint64_t request, double timeout_s, do
 /* The planet's temperature after its finished requests (HOST, cells). */
 int psgb_server_state(psgb_server* server, uint32_t planet, double* t_K);
 int psgb_server_stats_get(psgb_server* server, psgb_server_stats* out);
-/* Forgets the counts and latencies so far (after a warm-up); resident lanes stay. */
+/* Forgets the counts and latencies so far (after a warm-up); resident lanes stay. Call
+ * it while the server is idle (every submitted request waited on): a request still queued
+ * or running when it resets completes into the new counts without being counted as
+ * submitted there. */
 int psgb_server_stats_reset(psgb_server* server);
 
 #ifdef __cplusplus

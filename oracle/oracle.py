@@ -77,12 +77,42 @@ def lib() -> C.CDLL:
                                                 C.c_double, C.c_int, P, P]
         L.orc_solve_implicit_advection_diffusion.argtypes = [P, C.c_uint64, P, P, P, C.c_double, C.c_double, P, P,
                                                              P, P, C.c_double, C.c_double, P, P, P, P]
+        L.orc_icosphere_counts.restype = C.c_int
+        L.orc_icosphere_counts.argtypes = [C.c_uint32, P, P, P]
+        L.orc_icosphere.restype = C.c_int
+        L.orc_icosphere.argtypes = [C.c_uint32, C.c_double] + [P] * 19
         _lib = L
     return _lib
 
 
 def _p(a):
     return C.c_void_p(a.ctypes.data) if a is not None else C.c_void_p(None)
+
+
+def icosphere(level: int, radius_m: float) -> dict:
+    """The reference's make_icosphere(level, radius_m) and its transport graph, built by the
+    oracle's own restatement (mesh_oracle.cpp): the same keys as the product mesh's arrays()."""
+    n, e, k = C.c_uint64(), C.c_uint64(), C.c_uint64()
+    if lib().orc_icosphere_counts(level, C.byref(n), C.byref(e), C.byref(k)) != 0:
+        raise ValueError(f"oracle mesh: level {level}")
+    n, e, k = n.value, e.value, k.value
+    d = 2 * e
+    out = {
+        "center": np.empty((n, 3)), "east": np.empty((n, 3)), "north": np.empty((n, 3)), "area_m2": np.empty(n),
+        "source_vertex": np.empty(n, np.uint32), "edge_offset": np.empty(n, np.uint32),
+        "edge_count": np.empty(n, np.uint8), "neighbor": np.empty(d, np.uint32), "edge": np.empty(d, np.uint32),
+        "corner": np.empty(d, np.uint32), "normal_east": np.empty(d, np.float32),
+        "normal_north": np.empty(d, np.float32), "edge_first": np.empty(e, np.uint32),
+        "edge_second": np.empty(e, np.uint32), "edge_length_m": np.empty(e), "edge_distance_m": np.empty(e),
+        "corner_unit": np.empty((k, 3)), "graph_weight": np.empty(d), "graph_weight_sum": np.empty(n),
+    }
+    order = ["center", "east", "north", "area_m2", "source_vertex", "edge_offset", "edge_count", "neighbor", "edge",
+             "corner", "normal_east", "normal_north", "edge_first", "edge_second", "edge_length_m",
+             "edge_distance_m", "corner_unit", "graph_weight", "graph_weight_sum"]
+    if lib().orc_icosphere(level, float(radius_m), *[_p(out[name]) for name in order]) != 0:
+        raise ValueError(f"oracle mesh: level {level}, radius {radius_m}")
+    out["graph_area_m2"] = out["area_m2"]
+    return out
 
 
 class OracleMesh:

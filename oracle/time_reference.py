@@ -202,7 +202,13 @@ if __name__ == "__main__":
     workers = os.cpu_count() or 1
     if "--workers" in sys.argv:
         workers = int(sys.argv[sys.argv.index("--workers") + 1])
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+    from oracle.build import reference_root
+
+    reference = reference_root(args[0] if args else None)
+    if reference is None:
+        raise SystemExit("name the reference checkout: time_reference.py <path> (or set PLANETSIM_REFERENCE)")
     if "--headline" in sys.argv:
-        headline(Path(args[0] if args else "/root/reference"))
+        headline(reference)
     else:
-        main(Path(args[0] if args else "/root/reference"), workers)
+        main(reference, workers)

@@ -574,8 +574,18 @@ def transport_step_noalloc(mesh: PlanetMesh, t0_K, source_W_m2, heat_capacity_J_
         raise ValueError("the no-allocation step takes CUDA tensors")
     import torch
 
-    t_new = torch.empty_like(t0_K)
-    h = torch.empty_like(t0_K)
+    n = mesh.cell_count
+    current = torch.device("cuda", torch.cuda.current_device())
+    for name, t in (("t0_K", t0_K), ("source_W_m2", source_W_m2)):
+        if t.dtype != torch.float64 or t.numel() != n or not t.is_contiguous():
+            raise ValueError(f"{name} must be a contiguous float64 tensor of {n} cells "
+                             f"(got {t.dtype}, {t.numel()} elements)")
+        if t.device != current:
+            raise ValueError(f"{name} is on {t.device}; the no-allocation step runs on the current device {current}")
+    if isinstance(edge_conductance, str):
+        raise ValueError("the no-allocation step has no stored per-edge conductance: pass the array")
+    t_new = torch.empty(n, dtype=torch.float64, device=current)
+    h = torch.empty(n, dtype=torch.float64, device=current)
     params = step_params(heat_capacity_J_m2_K, dt_s, conductance_W_K, edge_conductance)
     o = solve_options(**options)
     rep = capi.StepReport()

@@ -1,11 +1,10 @@
-"""In-tree build of the GB300 library and of the CPU oracle.
+"""In-tree build of the GB300 library.
 
 ``build_library()`` compiles the CUDA kernels for sm_103a with nvcc and the host
 C++ (mesh builder, hierarchy, C-ABI) with g++ under ``-ffp-contract=off``, then links
-``planet_game_gb300/lib/libplanetsim_gb300.so``. ``build_oracle()`` compiles
-``oracle/planetsim_oracle.cpp`` into ``oracle/lib/libplanetsim_oracle.so``. Both are
-incremental (a target is rebuilt when any of its sources is newer) and compile their
-translation units in parallel. No cmake, no torch extension machinery.
+``planet_game_gb300/lib/libplanetsim_gb300.so``. It is incremental (a target is rebuilt
+when any of its sources is newer) and compiles its translation units in parallel. No
+cmake, no torch extension machinery. (The checker's own build is ``oracle/build.py``.)
 """
 from __future__ import annotations
 
@@ -22,8 +21,6 @@ CSRC = PKG / "csrc"
 LIB_DIR = PKG / "lib"
 OBJ_DIR = PKG / "lib" / "obj"
 LIBRARY = LIB_DIR / "libplanetsim_gb300.so"
-ORACLE_DIR = ROOT / "oracle"
-ORACLE_LIB = ORACLE_DIR / "lib" / "libplanetsim_oracle.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
@@ -97,27 +94,6 @@ def build_library(force: bool = False, verbose_ptxas: bool = False) -> Path:
         _run([_nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart", "-lpthread"])
         os.replace(tmp, LIBRARY)
     return LIBRARY
-
-
-def build_oracle(force: bool = False) -> Path:
-    """Compile the CPU oracle (test infrastructure) into oracle/lib/."""
-    srcs = [ORACLE_DIR / "planetsim_oracle.cpp", ORACLE_DIR / "nonsym_oracle.cpp"]
-    ORACLE_LIB.parent.mkdir(parents=True, exist_ok=True)
-    if force or _stale(ORACLE_LIB, srcs + [ORACLE_DIR / "oracle_abi.hpp"]):
-        tmp = ORACLE_LIB.with_suffix(".so.tmp")
-        _run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-pthread", *map(str, srcs),
-              "-o", str(tmp)])
-        os.replace(tmp, ORACLE_LIB)
-    return ORACLE_LIB
-
-
-def build_reference_driver(reference: Path = Path("/root/reference")) -> Path | None:
-    """Compile the reference's own sources into oracle/_ref/ when they are present."""
-    if not (reference / "sim").is_dir():
-        return None
-    _run(["make", "-s", "-f", str(ORACLE_DIR / "Makefile.ref"), f"REF={reference}",
-          f"OUT={ORACLE_DIR / '_ref'}", f"-j{os.cpu_count() or 4}", "-C", str(ROOT)])
-    return ORACLE_DIR / "_ref" / "libref_driver.so"
 
 
 if __name__ == "__main__":

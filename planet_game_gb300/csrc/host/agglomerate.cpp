@@ -4,6 +4,7 @@
 #include "agglomerate.hpp"
 
 #include <stdexcept>
+#include <string>
 
 namespace psgb {
 
@@ -34,33 +35,46 @@ Agglomeration identity_agglomeration(const HostMesh& mesh) {
     return out;
 }
 
+// The coarse node nearest to `point` (largest dot product of unit centres), found by
+// descending from `start`: move to the best of the current node's neighbours while one
+// beats it strictly, the first of equals winning. Consecutive fine cells lie close
+// together, so starting at the previous cell's node makes the descent short; the start
+// and the strict test decide between equidistant nodes exactly as the reference's walk
+// (heat_transport.cpp:483-500) does.
+std::size_t descend_to_nearest(const HostMesh& coarse, std::size_t start, const double* point) {
+    std::size_t at = start;
+    for (;;) {
+        const double here = dot3(point, &coarse.center[3 * at]);
+        double better = here;
+        std::size_t next = at;
+        const std::uint32_t* ring = &coarse.nb_cell[coarse.edge_offset[at]];
+        for (std::uint32_t k = 0; k < coarse.edge_count[at]; ++k) {
+            const double d = dot3(point, &coarse.center[3 * ring[k]]);
+            if (d > better) {
+                better = d;
+                next = ring[k];
+            }
+        }
+        if (next == at) return at;
+        at = next;
+    }
+}
+
 Agglomeration agglomerate(const HostMesh& fine, const HostMesh& coarse) {
     Agglomeration out;
     out.group_of_cell.resize(fine.cells);
     out.area_m2.assign(coarse.cells, 0.0);
-    std::size_t guess = 0;
+    std::size_t node = 0;
     for (std::size_t cell = 0; cell < fine.cells; ++cell) {
-        const double* centre = &fine.center[3 * cell];
-        for (;;) {
-            std::size_t best = guess;
-            double best_dot = dot3(centre, &coarse.center[3 * guess]);
-            const std::uint32_t begin = coarse.edge_offset[guess];
-            for (std::uint32_t k = 0; k < coarse.edge_count[guess]; ++k) {
-                const std::size_t other = coarse.nb_cell[begin + k];
-                const double value = dot3(centre, &coarse.center[3 * other]);
-                if (value > best_dot) {
-                    best_dot = value;
-                    best = other;
-                }
-            }
-            if (best == guess) break;
-            guess = best;
-        }
-        out.group_of_cell[cell] = static_cast<std::uint32_t>(guess);
-        out.area_m2[guess] += fine.area_m2[cell];
+        node = descend_to_nearest(coarse, node, &fine.center[3 * cell]);
+        out.group_of_cell[cell] = static_cast<std::uint32_t>(node);
+        out.area_m2[node] += fine.area_m2[cell];
     }
-    for (double area : out.area_m2) {
-        if (!(area > 0.0)) throw std::logic_error("a coarse transport cell received no fine cell");
+    for (std::size_t g = 0; g < coarse.cells; ++g) {
+        if (!(out.area_m2[g] > 0.0)) {
+            throw std::logic_error("agglomeration: coarse node " + std::to_string(g) + " of " +
+                                   std::to_string(coarse.cells) + " gathered no fine cell");
+        }
     }
     out.fine_area_m2 = fine.area_m2;
     list_members(out, coarse.cells);

@@ -1,87 +1,120 @@
-// Host-side aggregation hierarchy: structure bit-identical to the reference's
-// build_hierarchy (sim/planet/surface/heat_transport.cpp:73-200).
+// Host-side aggregation hierarchy. Its integer structure must equal the one the
+// reference's build_hierarchy produces (sim/planet/surface/heat_transport.cpp:73-200),
+// so the rules below are the reference's; the code is organised around claims,
+// coupling pairs and per-aggregate member lists instead.
 //
-// aggregate_rows (:73-108): greedy pass in row order - a free row whose
-// neighbours are all free seeds an aggregate with them; leftovers join their
-// strongest (most negative off-diagonal) aggregated neighbour, else form their own.
-// coarsen_pattern (:113-154): coarse columns sorted and unique per coarse row;
-// every fine off-diagonal lands on a coarse off-diagonal or the diagonal.
-// coarsen_values (:157-171): values summed in fine-row order.
+// Aggregation rule (:73-108): walking rows in order, a row whose whole neighbourhood is
+// still unclaimed claims it as a new aggregate. Rows left over are then visited in order;
+// each joins the aggregate of the neighbour it is most strongly coupled to (largest
+// -a_ij, strictly above zero, the first such neighbour on ties, claims made earlier in
+// this second walk included), or opens an aggregate of its own.
+// Coarse pattern (:113-154): the coarse row of an aggregate couples to every other
+// aggregate one of its members touches, columns in ascending order; each fine
+// off-diagonal lands on one coarse off-diagonal, or on the coarse diagonal when both ends
+// share an aggregate. Galerkin values (:157-171): summed in fine-row order.
 #include "hierarchy.hpp"
 
 #include <algorithm>
-#include <limits>
+#include <cstdint>
 #include <stdexcept>
+#include <utility>
 
 namespace psgb {
 namespace {
 
-constexpr std::uint32_t unassigned = std::numeric_limits<std::uint32_t>::max();
+constexpr std::int64_t kUnclaimed = -1;
 
-std::vector<std::uint32_t> aggregate_rows(const HostLevel& level, std::uint32_t& count) {
-    std::vector<std::uint32_t> agg(level.size, unassigned);
-    count = 0;
+// Aggregate of every row of `level`; `aggregates` receives their number.
+std::vector<std::uint32_t> claim_aggregates(const HostLevel& level, std::uint32_t& aggregates) {
+    std::vector<std::int64_t> owner(level.size, kUnclaimed);
+    std::int64_t opened = 0;
+    const auto neighbours = [&](std::uint32_t row) {
+        return std::make_pair(level.column.begin() + level.offset[row], level.column.begin() + level.offset[row + 1]);
+    };
+    // first walk: seeds with their whole neighbourhood
     for (std::uint32_t row = 0; row < level.size; ++row) {
-        bool free = agg[row] == unassigned;
-        for (std::uint32_t k = level.offset[row]; free && k < level.offset[row + 1]; ++k) {
-            free = agg[level.column[k]] == unassigned;
-        }
-        if (!free) continue;
-        agg[row] = count;
-        for (std::uint32_t k = level.offset[row]; k < level.offset[row + 1]; ++k) {
-            agg[level.column[k]] = count;
-        }
-        ++count;
+        const auto [first, last] = neighbours(row);
+        const bool untouched = owner[row] == kUnclaimed &&
+                               std::all_of(first, last, [&](std::uint32_t c) { return owner[c] == kUnclaimed; });
+        if (!untouched) continue;
+        owner[row] = opened;
+        std::for_each(first, last, [&](std::uint32_t c) { owner[c] = opened; });
+        ++opened;
     }
+    // second walk: leftovers follow their strongest claimed coupling
     for (std::uint32_t row = 0; row < level.size; ++row) {
-        if (agg[row] != unassigned) continue;
-        double strongest = 0.0;
+        if (owner[row] != kUnclaimed) continue;
+        double pull = 0.0;
+        std::int64_t chosen = kUnclaimed;
         for (std::uint32_t k = level.offset[row]; k < level.offset[row + 1]; ++k) {
-            const std::uint32_t other = level.column[k];
-            if (agg[other] != unassigned && -level.value[k] > strongest) {
-                strongest = -level.value[k];
-                agg[row] = agg[other];
-            }
+            const std::int64_t there = owner[level.column[k]];
+            const double coupling = -level.value[k];
+            if (there == kUnclaimed || !(coupling > pull)) continue;
+            pull = coupling;
+            chosen = there;
         }
-        if (agg[row] == unassigned) agg[row] = count++;
+        owner[row] = chosen != kUnclaimed ? chosen : opened++;
     }
-    return agg;
+    aggregates = static_cast<std::uint32_t>(opened);
+    return std::vector<std::uint32_t>(owner.begin(), owner.end());
+}
+
+// Fine rows of each aggregate, ascending: offsets [aggregates + 1] and rows.
+void members_of(const std::vector<std::uint32_t>& aggregate, std::uint32_t aggregates,
+                std::vector<std::uint32_t>& start, std::vector<std::uint32_t>& rows) {
+    start.assign(aggregates + 1, 0);
+    for (std::uint32_t a : aggregate) ++start[a + 1];
+    for (std::uint32_t a = 0; a < aggregates; ++a) start[a + 1] += start[a];
+    rows.resize(aggregate.size());
+    std::vector<std::uint32_t> fill(start.begin(), start.end() - 1);
+    for (std::uint32_t r = 0; r < aggregate.size(); ++r) rows[fill[aggregate[r]]++] = r;
 }
 
 HostLevel coarsen_pattern(HostLevel& fine) {
-    std::uint32_t count = 0;
-    fine.aggregate = aggregate_rows(fine, count);
+    std::uint32_t aggregates = 0;
+    fine.aggregate = claim_aggregates(fine, aggregates);
+    const std::vector<std::uint32_t>& agg = fine.aggregate;
     HostLevel coarse;
-    coarse.size = count;
-    std::vector<std::vector<std::uint32_t>> columns(count);
+    coarse.size = aggregates;
+    // every coupling between two different aggregates, as (from, to) pairs, sorted and
+    // unique: the coarse CSR in row order with ascending columns
+    std::vector<std::pair<std::uint32_t, std::uint32_t>> couplings;
+    couplings.reserve(fine.column.size());
     for (std::uint32_t row = 0; row < fine.size; ++row) {
-        const std::uint32_t a = fine.aggregate[row];
         for (std::uint32_t k = fine.offset[row]; k < fine.offset[row + 1]; ++k) {
-            const std::uint32_t b = fine.aggregate[fine.column[k]];
-            if (b != a) columns[a].push_back(b);
+            if (agg[fine.column[k]] != agg[row]) couplings.emplace_back(agg[row], agg[fine.column[k]]);
         }
     }
-    coarse.offset.assign(count + 1, 0);
-    for (std::uint32_t row = 0; row < count; ++row) {
-        auto& entries = columns[row];
-        std::sort(entries.begin(), entries.end());
-        entries.erase(std::unique(entries.begin(), entries.end()), entries.end());
-        coarse.column.insert(coarse.column.end(), entries.begin(), entries.end());
-        coarse.offset[row + 1] = static_cast<std::uint32_t>(coarse.column.size());
-        coarse.width = std::max<std::uint32_t>(coarse.width, static_cast<std::uint32_t>(entries.size()));
+    std::sort(couplings.begin(), couplings.end());
+    couplings.erase(std::unique(couplings.begin(), couplings.end()), couplings.end());
+    coarse.offset.assign(aggregates + 1, 0);
+    coarse.column.resize(couplings.size());
+    for (std::size_t e = 0; e < couplings.size(); ++e) {
+        ++coarse.offset[couplings[e].first + 1];
+        coarse.column[e] = couplings[e].second;
     }
-    coarse.diagonal.assign(count, 0.0);
+    for (std::uint32_t a = 0; a < aggregates; ++a) {
+        coarse.width = std::max(coarse.width, coarse.offset[a + 1]);
+        coarse.offset[a + 1] += coarse.offset[a];
+    }
+    coarse.diagonal.assign(aggregates, 0.0);
     coarse.value.assign(coarse.column.size(), 0.0);
+    // where each fine off-diagonal lands: per aggregate, its coarse columns' positions
+    // marked in a scratch row, read back by every member's entries
     fine.target.assign(fine.column.size(), -1);
-    for (std::uint32_t row = 0; row < fine.size; ++row) {
-        const std::uint32_t a = fine.aggregate[row];
-        for (std::uint32_t k = fine.offset[row]; k < fine.offset[row + 1]; ++k) {
-            const std::uint32_t b = fine.aggregate[fine.column[k]];
-            if (b == a) continue;
-            const auto first = coarse.column.begin() + coarse.offset[a];
-            const auto last = coarse.column.begin() + coarse.offset[a + 1];
-            fine.target[k] = std::lower_bound(first, last, b) - coarse.column.begin();
+    std::vector<std::uint32_t> start, rows;
+    members_of(agg, aggregates, start, rows);
+    std::vector<std::int64_t> position(aggregates, -1);
+    for (std::uint32_t a = 0; a < aggregates; ++a) {
+        for (std::uint32_t e = coarse.offset[a]; e < coarse.offset[a + 1]; ++e) position[coarse.column[e]] = e;
+        for (std::uint32_t m = start[a]; m < start[a + 1]; ++m) {
+            const std::uint32_t row = rows[m];
+            for (std::uint32_t k = fine.offset[row]; k < fine.offset[row + 1]; ++k) {
+                const std::uint32_t to = agg[fine.column[k]];
+                if (to != a) fine.target[k] = position[to];
+            }
         }
+        for (std::uint32_t e = coarse.offset[a]; e < coarse.offset[a + 1]; ++e) position[coarse.column[e]] = -1;
     }
     return coarse;
 }

@@ -1,10 +1,9 @@
 // A transport step that allocates nothing: psgb_transport_step_noalloc.
 //
 // Who needs it: callers that must not call cudaMalloc (or any other allocating CUDA
-// routine) while they run - for example a simulation loop with a fixed, pre-reserved
-// memory budget that may not grow, code running where an allocation could implicitly
-// synchronise the device (around stream capture, inside a latency-critical frame), or a
-// host that hands this library a GPU it shares under a hard memory cap. The regular
+// routine) while they run - a simulation loop that reserved a fixed memory budget up
+// front and may not grow it, a host that lends this library a GPU it shares under a hard
+// memory cap, or a plugin host whose own allocator owns the device memory. The regular
 // entry points allocate a planet's device workspace on first use; this one never does.
 //
 // How: every device array the solver needs (matrix hierarchy, Krylov and V-cycle
@@ -15,8 +14,16 @@
 // that device current, looks the address up with cudaGetSymbolAddress and caches it; make
 // that first call before any stream capture. Planets of at most kNoAllocMaxCells cells
 // (10,242: a level-5 mesh) fit; larger ones are rejected with PSGB_ERR_INVALID_ARGUMENT.
-// No graphs, streams, events or pinned buffers are created: the work runs on the
-// caller's stream and the scalars come back through pageable copies.
+// A per-edge conductance passed with the call is laid into the same array; the stored
+// conductance of a batch (psgb_batch_set_edge_conductance) does not exist here and is
+// rejected. No graphs, streams, events or pinned buffers are created: the work runs on
+// the caller's stream, and the call waits for that stream before it returns (the solver's
+// scalars come back through pageable copies).
+//
+// CUDA loads kernels lazily by default: the first call on a device, and the first call
+// of each precision, load their kernels and map the array. Make one warm-up call per
+// precision (or run with CUDA_MODULE_LOADING=EAGER) before relying on the no-allocation
+// property.
 //
 // The array is shared by every call on a device and keeps the last call's contents;
 // the step clears what must start at zero (reduction tickets, solver state) itself.
@@ -70,6 +77,10 @@ extern "C" int psgb_transport_step_noalloc(psgb_planet* planet, const psgb_step_
     return guarded([&] {
         if (planet == nullptr || params == nullptr || t0_K == nullptr || source_W_m2 == nullptr || t_new_K == nullptr) {
             throw std::invalid_argument("null argument");
+        }
+        if (params->edge_conductance_stored) {
+            throw std::invalid_argument("psgb_transport_step_noalloc has no stored per-edge conductance: pass the "
+                                        "array in edge_conductance");
         }
         const std::uint64_t cells = planet->planet->mesh.cells;
         if (cells > kNoAllocMaxCells) {

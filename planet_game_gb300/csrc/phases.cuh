@@ -493,7 +493,9 @@ __device__ void prolong_smooth(const LevelView<T>& lv, int t0, int lane, const s
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         if (!on[k]) continue;
-        count_bytes(lv.bytes, lane, static_cast<unsigned long long>(ts.rows[k]) * (8ull * W + sizeof(T) * (W + 4ull) + 4ull));
+        // each vector once: col, values, inv, b, x, y and the row's aggregate index (the
+        // neighbours' x and agg are gathers of vectors already counted; e is 1/16 of a row)
+        count_bytes(lv.bytes, lane, static_cast<unsigned long long>(ts.rows[k]) * (4ull * W + sizeof(T) * (W + 4ull) + 4ull));
         if (lane < ts.rows[k]) y[ts.tile[k] * kTile + lane] = out[k];
     }
 }

@@ -106,6 +106,7 @@ class Server {
     void state(std::uint32_t planet, double* out);
     Stats stats();
     // Forgets the counts and latencies so far (e.g. after a warm-up); resident lanes stay.
+    // Meant for an idle server: a request in flight completes into the new counts.
     void reset_stats();
     std::uint32_t cells(std::uint32_t planet);
 

@@ -349,6 +349,7 @@ class NativeServer:
         return {name: getattr(st, name) for name, _ in capi.ServerStats._fields_}
 
     def reset_stats(self) -> None:
+        """Forget the counts and latencies so far; call it while no request is in flight."""
         capi.check(self._lib.psgb_server_stats_reset(self._h))
 
     def close(self) -> None:

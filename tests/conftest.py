@@ -23,10 +23,11 @@ def pytest_configure(config):
 @pytest.fixture(scope="session", autouse=True)
 def built():
     """Compile the library and the oracle in-tree (incremental)."""
+    from oracle import build as oracle_build
     from planet_game_gb300 import build
 
     build.build_library()
-    build.build_oracle()
+    oracle_build.build_oracle()
     yield
 
 

@@ -536,7 +536,12 @@ def main(reference: Path, write: bool = True) -> dict:
 
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    reference = Path(args[0] if args else "/root/reference")
+    sys.path.insert(0, str(ROOT))
+    from oracle.build import reference_root
+
+    reference = reference_root(args[0] if args else None)
+    if reference is None:
+        raise SystemExit("name the reference checkout: make_golden.py <path> (or set PLANETSIM_REFERENCE)")
     if "--quartic" in sys.argv:   # only the nonlinear-transport fixture
         quartic_cases(load(reference))
         print("quartic fixture written")

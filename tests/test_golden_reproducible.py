@@ -23,9 +23,9 @@ ROOT = Path(__file__).resolve().parents[1]
 
 
 def _reference() -> Path | None:
-    m = re.search(r"^REF \?= (\S+)$", (ROOT / "oracle" / "Makefile.ref").read_text(), re.M)
-    ref = Path(m.group(1)) if m else None
-    return ref if ref is not None and (ref / "sim" / "planet" / "surface" / "heat_transport.cpp").exists() else None
+    from oracle.build import reference_root
+
+    return reference_root()
 
 
 @pytest.fixture(scope="module")
