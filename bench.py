@@ -8,17 +8,29 @@ FP32 multigrid-preconditioned BiCGSTAB inside FP64 iterative refinement to a 1e-
 relative residual, all 64 planets solved together in the concatenated block layout. A
 step is one sub-step of every planet; the metric is sub-steps/s (planets x steps / s).
 
-`--workload l8` times the L8 plain-FP64 drop-in solve (one planet) instead.
+Reported beside it, in the same JSON line:
+* `e2e`: the same through the C-ABI with host buffers, copies inside the timed region;
+* `reassembled`: the same with the matrix, its Galerkin coarse values and the coarsest
+  inverses assembled again on every step (the timed step otherwise reuses them while C,
+  dt and the conductances are unchanged);
+* `oracle_error`: every planet's T and H against the oracle (the reference's FP64 PCG +
+  SGS V-cycle solve, restated) on the same inputs;
+* `plain_fp64_one_at_a_time`: the same planets solved one per call in plain FP64, tuned
+  per level as the batch is (and untuned);
+* `serving`: the served workload (a Poisson trace over L4-L8) swept over offered rates
+  50 -> 5000 requests/s through the continuous-batching loop and the tuned plain FP64
+  one-at-a-time comparator, with p50/p99 latency; `headline_served` is its saturated point;
+* `roofline` (the fine-level Jacobi sweeps) and `kernels` (every profiled kernel family:
+  algorithmic GB/s from bytes counted on the device over CUDA-event kernel time);
+* `cpu_baseline`: the oracle's port of the reference's solve on one host core.
 
-Reported beside it, in the same JSON line: the plain one-planet-at-a-time FP64 GPU
-solve of the same planets (the drop-in comparator), the end-to-end rate through the
-C-ABI with host buffers, the dominant kernel's roofline (CUDA events on its launching
-stream during a profiled pass over the same steps, algorithmic bytes counted on the
-device), a CPU baseline (the oracle's port of the reference's FP64 PCG solve, one
-host core, a bounded sample) and the SM clocks sampled during the timed region.
+Other workloads: `l8` (one L8 planet, plain FP64), `l8rhs` (one L8 planet with 32 right-hand
+sides, plain FP64 and mixed, in one multi-RHS block), `ops` (the L6 operator sweep, L6 solve
+and 10-layer column radiation), `serve` (the serving sweep alone), `next` (the widened rows).
 
-`--impl reference` times the reference algorithm on the host cores instead (the oracle
-port, all cores, one process per core), on the same workload, metric and unit.
+`--impl reference` times the reference algorithm on the host cores instead (the oracle's
+port, all cores, one process per core) on the same workload, metric and unit; it builds
+its planets with the oracle's own mesh builder, without the product library.
 
 Multi-GPU (`torchrun ... --gpus N`): planets are independent, so every rank solves its
 own replica of the workload with no data-path collective ("replicas only"); the value
@@ -139,14 +151,21 @@ def peaks() -> tuple[float, str]:
 
 # ---- workloads ---------------------------------------------------------------------------------
 
+WORKLOAD_NAMES = {
+    "batch": "64 uneven planets (16xL4, 24xL5, 16xL6, 8xL7; 2,252,928 cells), per-edge lognormal diffusivity, "
+             "one batched sub-step per step",
+    "l8": "one L8 planet (655,362 cells), plain FP64 drop-in solve",
+}
+
+
 def make_workload(kind: str, seed: int):
-    """Planets and their inputs (host numpy)."""
+    """Planets and their inputs (host numpy), meshes from the product's builder."""
     import planet_game_gb300 as pg
     from planet_game_gb300 import workloads as W
 
     planets = []
     if kind == "batch":
-        for i, spec in enumerate(W.planet_mix(seed)):
+        for spec in W.planet_mix(seed):
             m = pg.make_icosphere(spec.level, spec.radius)
             kappa = W.lognormal_edge_diffusivity(m.edge_count, spec.seed)
             inp = W.step_inputs(m, spec.seed, edge_diffusivity=kappa)
@@ -157,6 +176,29 @@ def make_workload(kind: str, seed: int):
     else:
         raise SystemExit(f"unknown workload {kind}")
     return planets
+
+
+def oracle_workload(kind: str, seed: int):
+    """The same planets and inputs built by the oracle alone (its restatement of the
+    reference's mesh builder and sub-step insolation, the reference's own orbit nodes from
+    the committed fixture): the CPU arms never load the product library."""
+    from oracle import oracle as O
+    from planet_game_gb300 import workloads as W   # numpy only: no library is loaded
+
+    nodes = np.load(ROOT / "tests" / "golden" / "insolation_L4.npz")["nodes"]
+    out = []
+    if kind == "batch":
+        for spec in W.planet_mix(seed):
+            a = O.icosphere(spec.level, spec.radius)
+            kappa = W.lognormal_edge_diffusivity(len(a["edge_length_m"]), spec.seed)
+            out.append((a, W.step_inputs_from(a["center"], O.substep_mean_insolation(a["center"], nodes), spec.seed,
+                                              kappa)))
+    elif kind == "l8":
+        a = O.icosphere(8, W.EARTH_RADIUS)
+        out.append((a, W.step_inputs_from(a["center"], O.substep_mean_insolation(a["center"], nodes), seed)))
+    else:
+        raise SystemExit(f"unknown workload {kind}")
+    return out
 
 
 def smoother_desc(tuning) -> str:
@@ -173,6 +215,11 @@ def precision_for(kind: str) -> str:
 
 
 SOLVER = dict(method="bicgstab", tolerance=1e-10, inner_tolerance=1e-4, poll=4)
+
+
+def static_config(kind: str, planets: int, cells: int) -> dict:
+    """The workload's description, the same in both arms' lines."""
+    return {"workload": WORKLOAD_NAMES[kind], "planets": planets, "cells": cells, "tolerance": 1e-10}
 
 
 # ---- the GB300 arm ---------------------------------------------------------------------------------
@@ -206,9 +253,9 @@ def run_gb300(args, rank, world, local_rank):
         edge_g = "stored"
     lib = capi.load()
 
-    def step(t0, src, out):
+    def step(t0, src, out, h=None):
         _, reps = batch.transport_step(t0, src, heat, dt, conductance=cond, edge_conductance=edge_g, out=out,
-                                       precision=prec, **SOLVER)
+                                       transport_out=h, precision=prec, **SOLVER)
         return reps
 
     # per-level launch shapes and sweeps picked by the autotuner (setup, not timed)
@@ -228,25 +275,30 @@ def run_gb300(args, rank, world, local_rank):
     if bad:
         raise SystemExit(f"solve failed its gates: {bad[0]}")
 
-    # timed region: inputs resident in HBM
-    stream = torch.cuda.current_stream()
-    launches0 = lib.psgb_launch_count()
-    with ClockSampler(local_rank) as clocks:
+    def timed(steps: int):
+        """`steps` steps bracketed by a barrier and device synchronisation, CUDA events on
+        the stream the steps are ordered on; max over ranks."""
+        stream = torch.cuda.current_stream()
         barrier(dist)
         torch.cuda.synchronize()
         start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         start.record(stream)
-        iters = []
-        for _ in range(args.steps):
+        its = []
+        for _ in range(steps):
             torch.cuda.nvtx.range_push("timed_step")     # ncu --nvtx-include "timed_step/" selects these launches
-            reps = step(t0_d, s_d, out_d)
+            r = step(t0_d, s_d, out_d)
             torch.cuda.nvtx.range_pop()
-            iters.append(sum(r.iterations * m.cell_count for r, m in zip(reps, meshes)))
+            its.append(sum(x.iterations * m.cell_count for x, m in zip(r, meshes)))
         end.record(stream)
         torch.cuda.synchronize()
         barrier(dist)
+        return max_over_ranks(start.elapsed_time(end) / 1e3, dist, dev), r, its
+
+    # timed region: inputs resident in HBM
+    launches0 = lib.psgb_launch_count()
+    with ClockSampler(local_rank) as clocks:
+        elapsed, reps, iters = timed(args.steps)
     launches = lib.psgb_launch_count() - launches0
-    elapsed = max_over_ranks(start.elapsed_time(end) / 1e3, dist, dev)
     units = len(meshes) * args.steps * world
     value = units / elapsed
     clock = clocks.summary()
@@ -266,7 +318,26 @@ def run_gb300(args, rank, world, local_rank):
     e2e = {"value": units / e2e_elapsed, "unit": "sub-steps/s", "h2d_bytes_per_step": cells * 16,
            "d2h_bytes_per_step": cells * 8}
 
-    # profiled pass: the dominant kernel family timed with events on its stream
+    # the same steps with the matrix assembled again every step (as the reference does)
+    batch.set_reassembly(True)
+    step(t0_d, s_d, out_d)
+    re_elapsed, re_reps, _ = timed(args.steps)
+    batch.set_reassembly(False)
+    reassembled = {"value": units / re_elapsed, "unit": "sub-steps/s", "ms_per_step": re_elapsed * 1e3 / args.steps,
+                   "what": "every step assembles the fine matrix from C, dt and the per-edge conductances, the "
+                           "Galerkin values of every coarse level and the coarsest levels' inverses on the device; "
+                           "the headline steps reuse them while those parameters are unchanged",
+                   "same_iterations": [r.iterations for r in re_reps] == [r.iterations for r in reps]}
+
+    # every planet's result against the oracle (FP64 PCG + SGS V-cycle, tight tolerance)
+    oracle_error = None
+    if rank == 0 and not args.skip_cpu:
+        h_d = [torch.empty_like(t) for t in t0_d]
+        step(t0_d, s_d, out_d, h_d)
+        torch.cuda.synchronize()
+        oracle_error = oracle_errors(planets, [o.cpu().numpy() for o in out_d], [h.cpu().numpy() for h in h_d])
+
+    # profiled pass: kernel families timed with events on their stream, bytes counted on the device
     import ctypes as C
 
     peak, peak_kind = peaks()
@@ -280,43 +351,49 @@ def run_gb300(args, rank, world, local_rank):
             step(t0_d, s_d, out_d)
         capi.check(lib.psgb_profile_end(C.byref(ms), C.byref(nl), C.byref(nbytes)))
         batch.concurrent = not args.serial_lanes
-        achieved = nbytes.value / (ms.value / 1e3) / 1e9 if ms.value > 0 else None
+        achieved = nbytes.value / (ms.value / 1e3) / 1e9 if ms.value > 0 and nbytes.value > 0 else None
         traffic = (traffic_all.get(args.workload) or {}).get(family.decode())
         return {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
                 "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                "traffic_source": "ncu dram__bytes per launch of this family, profiles/launches_*.md (constant)"
+                                  if traffic is not None else None,
                 "launches": int(nl.value), "avg_launch_us": ms.value * 1e3 / max(1, nl.value),
-                "bytes_per_launch": nbytes.value / max(1, nl.value), "share_of_step": ms.value / args.steps / (elapsed * 1e3 / args.steps)}
+                "bytes_per_launch": nbytes.value / max(1, nl.value),
+                "share_of_step": ms.value / args.steps / (elapsed * 1e3 / args.steps)}
 
+    kernels = {}
     if args.schedule == "persistent":
         roofline = profile_family(b"persistent", "k_persistent_solve (whole refined solve; Jacobi-sweep bytes)")
-        roofline_coarse = None
     else:
         roofline = profile_family(b"smooth", "k_smooth / k_prolong_smooth / k_smooth_zero on the fine level")
-        roofline_coarse = profile_family(b"smooth_coarse", "k_smooth / k_prolong_smooth on the coarse levels")
+        for fam, desc in PROFILED_FAMILIES:
+            kernels[fam] = profile_family(fam.encode(), desc)
 
     # the plain one-planet-at-a-time FP64 GPU drop-in on the same planets
     plain = None
     if rank == 0 and not args.skip_plain:
-        for i, (m, inp) in enumerate(planets):   # warm the solo batches
-            pg.transport_step(m, t0_d[i], s_d[i], inp.heat_capacity, inp.dt, inp.conductance,
-                              edge_conductance=inp.edge_conductance, precision="fp64", **SOLVER)
-        torch.cuda.synchronize()
-        tp = time.perf_counter()
-        plain_iters = 0
-        for i, (m, inp) in enumerate(planets):
-            _, _, r = pg.transport_step(m, t0_d[i], s_d[i], inp.heat_capacity, inp.dt, inp.conductance,
-                                        edge_conductance=inp.edge_conductance, precision="fp64", **SOLVER)
-            plain_iters += r.iterations
-            if r.status != 0:
-                raise SystemExit(f"plain FP64 solve failed: {r}")
-        torch.cuda.synchronize()
-        plain = {"value": len(planets) / (time.perf_counter() - tp), "unit": "sub-steps/s",
-                 "krylov_iterations": plain_iters, "solver": "FP64 AMG-BiCGSTAB, one planet per call"}
+        plain = plain_comparator(planets, t0_d, s_d, torch)
 
-    serving = serving_point(args, dev, rate=args.serve_rate, count=args.serve_requests) \
-        if (rank == 0 and not args.skip_serve) else None
+    serving = serving_sweep(args, dev) if (rank == 0 and not args.skip_serve) else None
     cpu = cpu_baseline(planets, args) if (rank == 0 and not args.skip_cpu) else None
     if rank == 0:
+        config = static_config(args.workload, len(meshes), cells)
+        config.update({
+            "precision": prec, "krylov": "BiCGSTAB", "parallelism": f"replicas x{world}",
+            "lanes": [sorted({meshes[i].subdivision for i in lane}) for lane in batch.lanes],
+            "smoother": smoother_desc(tuning), "tuning": tuning,
+            "krylov_iterations_per_step": sum(r.iterations for r in reps), "refinements_last_step": max(refinements),
+            "krylov_iterations_per_planet": {"min": min(r.iterations for r in reps),
+                                             "median": float(np.median([r.iterations for r in reps])),
+                                             "max": max(r.iterations for r in reps)},
+            "cell_iterations_per_s": statistics.mean(iters) * world / (elapsed / args.steps),
+            "l2": "working set larger than the 129 MB L2 (no flush needed)" if cells > 1_000_000 else
+                  "working set may be L2 resident",
+            "matrix": "assembled once and reused while C, dt and the conductances are unchanged (as in a run of "
+                      "sub-steps with constant coefficients); `reassembled` times the same steps assembling it "
+                      "every step",
+            "plain_fp64_one_at_a_time": plain,
+        })
         line = {
             "metric": "sub-steps/s at 1e-10 relative residual",
             "value": value,
@@ -330,27 +407,14 @@ def run_gb300(args, rank, world, local_rank):
             "vs_baseline": None,
             "dtype": "f32 inner, f64 refinement" if prec == "mixed" else "f64",
             "data": "synthetic",
-            "config": {
-                "workload": ("64 uneven planets (16xL4, 24xL5, 16xL6, 8xL7; 2,252,928 cells), per-edge lognormal "
-                             "diffusivity, one batched sub-step per step" if args.workload == "batch"
-                             else "one L8 planet (655,362 cells), plain FP64 drop-in solve"),
-                "planets": len(meshes), "cells": cells, "precision": prec, "krylov": "BiCGSTAB",
-                "lanes": [sorted({meshes[i].subdivision for i in lane}) for lane in batch.lanes],
-                "smoother": smoother_desc(tuning), "tuning": tuning, "tolerance": 1e-10,
-                "krylov_iterations_per_step": sum(r.iterations for r in reps), "refinements_last_step": max(refinements),
-                "krylov_iterations_per_planet": {"min": min(r.iterations for r in reps),
-                                                 "median": float(np.median([r.iterations for r in reps])),
-                                                 "max": max(r.iterations for r in reps)},
-                "cell_iterations_per_s": statistics.mean(iters) * world / (elapsed / args.steps),
-                "l2": "working set larger than the 129 MB L2 (no flush needed)" if cells > 1_000_000 else
-                      "working set may be L2 resident",
-                "plain_fp64_one_at_a_time": plain,
-                "parallelism": f"replicas x{world}",
-            },
+            "config": config,
             "e2e": e2e,
+            "reassembled": reassembled,
+            "oracle_error": oracle_error,
+            "headline_served": serving.get("headline") if serving else None,
             "serving": serving,
             "roofline": roofline,
-            "roofline_coarse_sweeps": roofline_coarse,
+            "kernels": kernels,
             "cpu_baseline": cpu,
             "clocks": clock,
             "gpu_launches": int(launches),
@@ -360,51 +424,160 @@ def run_gb300(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+# Kernel families profiled beside the headline roofline (psgb_profile_begin names).
+PROFILED_FAMILIES = (
+    ("smooth_coarse", "k_smooth / k_smooth_block / k_prolong_smooth on the coarse levels"),
+    ("residual", "k_residual, fine level"),
+    ("residual_coarse", "k_residual, coarse levels"),
+    ("restrict", "k_restrict_zero from the fine level"),
+    ("restrict_coarse", "k_restrict_zero between coarse levels"),
+    ("dense", "k_dense_solve (coarsest levels)"),
+    ("krylov_spmv", "k_bicg_v / k_bicg_t (SpMV with fused dots)"),
+    ("krylov_vector", "k_bicg_init / p / s / x (vector updates with fused dots)"),
+    ("refine", "k_outer_init / residual / update (FP64 refinement)"),
+    ("step", "k_step_rhs / k_step_finish (right-hand side, flux form, closure sums)"),
+)
+
+
+def plain_comparator(planets, t0_d, s_d, torch) -> dict:
+    """The planets one per call in plain FP64: tuned once per level (api.TunedSolo), and
+    through the untuned single-planet entry point."""
+    import planet_game_gb300 as pg
+
+    out = {"unit": "sub-steps/s", "solver": "FP64 AMG-BiCGSTAB, one planet per call"}
+    solo = pg.TunedSolo(precision="fp64", **SOLVER)
+    for name, fn in (
+        ("untuned", lambda i, m, inp: pg.transport_step(m, t0_d[i], s_d[i], inp.heat_capacity, inp.dt,
+                                                        inp.conductance, edge_conductance=inp.edge_conductance,
+                                                        precision="fp64", **SOLVER)[2]),
+        ("tuned", lambda i, m, inp: solo.step(m, t0_d[i], s_d[i], inp.heat_capacity, inp.dt, inp.conductance,
+                                              edge_conductance=inp.edge_conductance)[1]),
+    ):
+        for i, (m, inp) in enumerate(planets):   # warm: batches, tunings, graphs
+            fn(i, m, inp)
+        torch.cuda.synchronize()
+        tp = time.perf_counter()
+        its = 0
+        for i, (m, inp) in enumerate(planets):
+            r = fn(i, m, inp)
+            its += r.iterations
+            if r.status != 0:
+                raise SystemExit(f"plain FP64 solve failed: {r}")
+        torch.cuda.synchronize()
+        out[name] = {"value": len(planets) / (time.perf_counter() - tp), "krylov_iterations": its}
+    out["value"] = out["tuned"]["value"]
+    out["tunings_per_level"] = {f"L{k[0]}": smoother_desc(t) for k, t in solo.tunings.items()}
+    return out
+
+
+def oracle_errors(planets, t_gpu, h_gpu) -> dict:
+    """Max |T_gpu - T_oracle| and |H_gpu - H_oracle| over every planet, the oracle (the
+    reference's FP64 PCG + SGS V-cycle solve, restated) to a 1e-13 relative residual on
+    the same inputs, its solves spread over the host cores (spawned processes)."""
+    import multiprocessing as mp
+
+    payloads = [(m.arrays(), inp_dict(inp), inp.edge_conductance, 1e-13) for m, inp in planets]
+    with mp.get_context("spawn").Pool(processes=max(1, min(len(payloads), os.cpu_count() or 1))) as pool:
+        results = pool.map(_oracle_solve_full, payloads, chunksize=1)
+    rows = []
+    for (m, _), tg, hg, (tn, h) in zip(planets, t_gpu, h_gpu, results):
+        rows.append((m.subdivision, float(np.max(np.abs(tg - tn))), float(np.max(np.abs(tn))),
+                     float(np.max(np.abs(hg - h))), float(np.max(np.abs(h)))))
+    worst = max(range(len(rows)), key=lambda k: rows[k][1])
+    per_level = {}
+    for lvl, dt_, _, dh, _ in rows:
+        e = per_level.setdefault(f"L{lvl}", {"max_abs_T_K": 0.0, "max_abs_H_W_m2": 0.0})
+        e["max_abs_T_K"] = max(e["max_abs_T_K"], dt_)
+        e["max_abs_H_W_m2"] = max(e["max_abs_H_W_m2"], dh)
+    return {"planets": len(rows), "oracle": "FP64 PCG + SGS V-cycle (the reference's solve, restated), relative "
+                                            "residual 1e-13, same inputs",
+            "max_abs_T_K": max(r[1] for r in rows), "max_rel_T": max(r[1] / r[2] for r in rows),
+            "max_abs_H_W_m2": max(r[3] for r in rows), "max_rel_H": max(r[3] / r[4] for r in rows),
+            "worst_planet": {"index": worst, "level": rows[worst][0], "abs_T_K": rows[worst][1]},
+            "per_level": per_level}
+
+
 # ---- serving ------------------------------------------------------------------------------------
 
 SERVE_POPULATION = {4: 16, 5: 16, 6: 16, 7: 8, 8: 4}
+SERVE_RATES = (50.0, 200.0, 1000.0, 5000.0)
+SOLVER_SERVE = dict(method="bicgstab", tolerance=1e-10, inner_tolerance=1e-4, poll=4)
 
 
-def serving_point(args, dev, rate: float, count: int, population=None) -> dict:
-    """A seeded Poisson trace of `count` requests over L4-L8 (30/30/20/15/5 %) at `rate`
-    requests/s, served by the continuous-batching loop (mixed precision) and by the plain
-    FP64 one-at-a-time drop-in, with p50/p99 latency from arrival to result on the host."""
+def build_serve_population(dev):
+    from planet_game_gb300 import serve
+
+    pop = {}
+    for level, n in SERVE_POPULATION.items():
+        pop.update(serve.build_population(n, levels=(level,), seed=100 + level, device=dev))
+    return pop
+
+
+def serve_trace(args, rate: float, count: int):
+    from planet_game_gb300 import workloads as W
+
+    trace = W.poisson_trace(count, rate, seed=args.seed + 1, planets_per_level=max(SERVE_POPULATION.values()))
+    return [W.Request(r.arrival_s, r.level, r.planet % SERVE_POPULATION[r.level]) for r in trace]
+
+
+def requests_at(args, rate: float) -> int:
+    """2,000 requests a point, fewer at the lowest rate (500 at 50 requests/s: 10 s of
+    offered traffic, where both arms keep up and only the latency differs)."""
+    return min(args.serve_requests, max(500, int(10 * rate)))
+
+
+def serving_sweep(args, dev, rates=SERVE_RATES) -> dict:
+    """A seeded Poisson trace over L4-L8 (30/30/20/15/5 %) at each offered rate, served by
+    the continuous-batching loop (mixed precision, lanes tuned at admission) and by the
+    plain FP64 one-at-a-time comparator (one-planet batches tuned per level); latency from
+    arrival to result on the host. Both arms see the same requests and sources."""
     import torch
 
     from planet_game_gb300 import serve
-    from planet_game_gb300 import workloads as W
 
-    out = {"requests": count, "offered_per_s": rate, "population": {f"L{k}": v for k, v in SERVE_POPULATION.items()},
-           "budget_gb": 150}
-    for name in ("continuous_batching_mixed", "one_at_a_time_fp64"):
-        pop = build_serve_population(dev)
-        trace = W.poisson_trace(count, rate, seed=args.seed + 1, planets_per_level=max(SERVE_POPULATION.values()))
-        trace = [W.Request(r.arrival_s, r.level, r.planet % SERVE_POPULATION[r.level]) for r in trace]
-        reqs = serve.make_requests(trace, pop, seed=args.seed + 2)
-        if name.startswith("continuous"):
-            srv = serve.Server(pop, budget_bytes=150e9, precision="mixed", **SOLVER_SERVE)
-            srv.prepare()                                                      # admit and tune the lanes
-            warm = serve.make_requests(trace[:40], pop, seed=args.seed + 3)   # record graphs
-            srv.run_trace(warm, realtime=False)
+    out = {"population": {f"L{k}": v for k, v in SERVE_POPULATION.items()}, "budget_gb": 150,
+           "latency": "arrival to result on the host (host source in, host temperature out)", "points": []}
+    pop_b = build_serve_population(dev)
+    pop_o = build_serve_population(dev)
+    srv = serve.Server(pop_b, budget_bytes=150e9, precision="mixed", **SOLVER_SERVE)
+    one = serve.OneAtATime(pop_o, tuned=True, **SOLVER_SERVE)
+    try:
+        srv.prepare()                                    # admit and tune every lane
+        for planets in pop_o.values():                   # one-planet batches and per-level tunings
+            for p in planets:
+                zero = torch.zeros_like(p.state)
+                one.solo.batch_of(p.mesh, p.state, zero, p.heat_capacity, p.dt, p.conductance, p.edge_conductance)
+        warm = serve_trace(args, 5000.0, 60)
+        srv.run_trace(serve.make_requests(warm, pop_b, seed=args.seed + 3), realtime=False)   # record graphs
+        one.run_trace(serve.make_requests(warm, pop_o, seed=args.seed + 3), realtime=False)
+        for rate in rates:
+            count = requests_at(args, rate)
+            trace = serve_trace(args, rate, count)
+            reqs_b = serve.make_requests(trace, pop_b, seed=args.seed + 2)
             srv.completed = 0
-            try:
-                srv.run_trace(reqs, realtime=True)
-            finally:
-                srv.close()
-        else:
-            srv = serve.OneAtATime(pop, **SOLVER_SERVE)
-            warm = serve.make_requests(trace[:40], pop, seed=args.seed + 3)
-            srv.run_trace(warm, realtime=False)
-            srv.run_trace(reqs, realtime=True)
-        torch.cuda.synchronize()
-        summary = serve.summarize(reqs)
-        if summary["ok"] != count:
-            raise SystemExit(f"serving: {count - summary['ok']} requests failed")
-        out[name] = summary
-    a, b = out["continuous_batching_mixed"], out["one_at_a_time_fp64"]
-    out["speedup_sub_steps_per_s"] = a["sub_steps_per_s"] / b["sub_steps_per_s"]
+            srv.run_trace(reqs_b, realtime=True)
+            reqs_o = serve.make_requests(trace, pop_o, seed=args.seed + 2)
+            one.run_trace(reqs_o, realtime=True)
+            torch.cuda.synchronize()
+            a, b = serve.summarize(reqs_b), serve.summarize(reqs_o)
+            if a["ok"] != count or b["ok"] != count:
+                raise SystemExit(f"serving at {rate}/s: {count - a['ok']} + {count - b['ok']} requests failed")
+            out["points"].append({"offered_per_s": rate, "requests": count, "continuous_batching_mixed": a,
+                                  "one_at_a_time_fp64_tuned": b,
+                                  "speedup_sub_steps_per_s": a["sub_steps_per_s"] / b["sub_steps_per_s"]})
+    finally:
+        srv.close()
     if getattr(args, "native_serve", False):
-        out["continuous_batching_native"] = native_serving_point(args, dev, rate, count)
+        out["continuous_batching_native"] = native_serving_point(args, dev, rates[-1], requests_at(args, rates[-1]))
+    top = out["points"][-1]
+    out["headline"] = {"offered_per_s": top["offered_per_s"], "requests": top["requests"],
+                       "served_sub_steps_per_s": top["continuous_batching_mixed"]["sub_steps_per_s"],
+                       "plain_fp64_tuned_sub_steps_per_s": top["one_at_a_time_fp64_tuned"]["sub_steps_per_s"],
+                       "ratio": top["speedup_sub_steps_per_s"], "target_ratio": 5.0,
+                       "p50_ms": top["continuous_batching_mixed"]["p50_ms"],
+                       "p99_ms": top["continuous_batching_mixed"]["p99_ms"],
+                       "plain_p50_ms": top["one_at_a_time_fp64_tuned"]["p50_ms"],
+                       "plain_p99_ms": top["one_at_a_time_fp64_tuned"]["p99_ms"]}
     return out
 
 
@@ -413,13 +586,10 @@ def native_serving_point(args, dev, rate: float, count: int) -> dict:
     their threads in C++, host arrays in and out; latency from submission to completion as
     the loop records it, after a warm-up that admits and tunes every lane."""
     from planet_game_gb300 import serve
-    from planet_game_gb300 import workloads as W
 
     pop = build_serve_population(dev)
-    trace = W.poisson_trace(count, rate, seed=args.seed + 1, planets_per_level=max(SERVE_POPULATION.values()))
-    trace = [W.Request(r.arrival_s, r.level, r.planet % SERVE_POPULATION[r.level]) for r in trace]
-    reqs = serve.make_requests(trace, pop, seed=args.seed + 2)
-    warm = serve.make_requests(trace[:40], pop, seed=args.seed + 3)
+    reqs = serve.make_requests(serve_trace(args, rate, count), pop, seed=args.seed + 2)
+    warm = serve.make_requests(serve_trace(args, 5000.0, 60), pop, seed=args.seed + 3)
     srv = serve.NativeServer(budget_bytes=150e9, precision="mixed", **SOLVER_SERVE)
     try:
         ids = {}
@@ -449,36 +619,23 @@ def native_serving_point(args, dev, rate: float, count: int) -> dict:
         stats = srv.stats()
     finally:
         srv.close()
-    return {"requests": count, "sub_steps_per_s": count / elapsed, "p50_ms": stats["p50_ms"],
+    return {"requests": count, "offered_per_s": rate, "sub_steps_per_s": count / elapsed, "p50_ms": stats["p50_ms"],
             "p99_ms": stats["p99_ms"], "ok": int(sum(r.status == 0 for r in reqs)),
             "latency": "submission to completion, recorded by the loop"}
 
 
-SOLVER_SERVE = dict(method="bicgstab", tolerance=1e-10, inner_tolerance=1e-4, poll=4)
-
-
-def build_serve_population(dev):
-    from planet_game_gb300 import serve
-
-    pop = {}
-    for level, n in SERVE_POPULATION.items():
-        pop.update(serve.build_population(n, levels=(level,), seed=100 + level, device=dev))
-    return pop
-
-
 def run_serve_sweep(args, rank, local_rank):
-    """The full offered-rate sweep (50 -> 5000 requests/s), one JSON line."""
+    """The serving sweep alone, one JSON line."""
     import torch
 
     if rank != 0:
         return
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    points = [serving_point(args, dev, rate, args.serve_requests) for rate in (50.0, 200.0, 1000.0, 5000.0)]
-    best = max(points, key=lambda p: p["continuous_batching_mixed"]["sub_steps_per_s"])
+    sweep = serving_sweep(args, dev)
     print(json.dumps({"metric": "served sub-steps/s and p50/p99 at 1e-10 relative residual", "unit": "sub-steps/s",
-                      "value": best["continuous_batching_mixed"]["sub_steps_per_s"], "n_gpus": 1,
-                      "higher_is_better": True, "data": "synthetic", "sweep": points}))
+                      "value": sweep["headline"]["served_sub_steps_per_s"], "n_gpus": 1, "higher_is_better": True,
+                      "data": "synthetic", "serving": sweep}))
 
 
 # ---- the rows that widen the hot path -------------------------------------------------------
@@ -593,10 +750,171 @@ def run_next(args, rank, local_rank):
     print(json.dumps(out))
 
 
+# ---- config 1: operators, L6 solve, column radiation ---------------------------------------------
+
+def _event_median_us(fn, flush, reps: int = 7) -> float:
+    """Median device time of fn() in microseconds, CUDA events on the current stream, the
+    L2 flushed (a write of a buffer larger than L2) before every timed launch."""
+    import torch
+
+    stream = torch.cuda.current_stream()
+    fn()
+    times = []
+    for _ in range(reps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b) * 1e3)
+    return float(statistics.median(times))
+
+
+def operator_bytes(a: dict) -> dict:
+    """Algorithmic FP64 bytes per cell of the operator kernels, each array counted once:
+    Laplacian: columns 24, weights 48, area 8, field 8, out 8; gradient: columns 24,
+    degree 1, distances 48, FP32 normals 48, the 2x2 normal matrix 32, field 8, out 16;
+    divergence: edge ids 24, orientation and degree 2, area 8, out 8, and per undirected
+    edge its flux and length (16 B, E/N of them per cell)."""
+    n, e = len(a["area_m2"]), len(a["edge_length_m"])
+    return {"laplacian": 96.0, "gradient": 177.0, "divergence": 42.0 + 16.0 * e / n}
+
+
+def run_ops(args, rank, local_rank):
+    """The L6 operator sweep on 8 seeded fields (sums of real spherical harmonics l <= 16):
+    gradient, divergence of the exact edge-normal flux of the gradient, Laplacian; then the
+    config-0 implicit solve on L6 in plain FP64; then column radiation over 10 layers for
+    every L6 cell. Each kernel's time (CUDA events, L2 flushed before every launch),
+    algorithmic GB/s and fraction of the measured HBM bandwidth, its error against the
+    analytic fields and against the oracle, and the oracle's time on one host core. The
+    operator kernels are also timed on the L8 mesh (655,362 cells), whose arrays exceed
+    what a flushed L2 would hide."""
+    import torch
+
+    import planet_game_gb300 as pg
+    from oracle import oracle as O
+    from planet_game_gb300 import workloads as W
+
+    if rank != 0:
+        return
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    peak, peak_kind = peaks()
+    flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)      # 256 MB > L2
+    R = W.EARTH_RADIUS
+    out = {"metric": "config 1 (L6 operator sweep, L6 solve, 10-layer column radiation)", "n_gpus": 1,
+           "data": "synthetic", "peak_GBs": peak, "peak_kind": peak_kind,
+           "timing": "median of 7 launches, CUDA events, L2 flushed before each"}
+
+    def rel_l2(x, y, w):
+        return float(np.sqrt(np.sum(w * (x - y) ** 2) / np.sum(w * y ** 2)))
+
+    for level in (6, 8):
+        m = pg.make_icosphere(level, R)
+        a = m.arrays()
+        om = O.OracleMesh(a)
+        per_cell = operator_bytes(a)
+        n = m.cell_count
+        fields = [W.harmonic_field(a, R, 16, seed) for seed in range(8 if level == 6 else 1)]
+        res = {"cells": n, "fields": len(fields), "kernels": {}}
+        x_d = [torch.from_numpy(F.value).to(dev) for F in fields]
+        f_d = [torch.from_numpy(F.edge_flux).to(dev) for F in fields]
+        kern = {
+            "laplacian": lambda k: pg.laplacian(m, x_d[k]),
+            "gradient": lambda k: pg.gradient(m, x_d[k]),
+            "divergence": lambda k: pg.divergence(m, f_d[k]),
+        }
+        for name, fn in kern.items():
+            us = statistics.median(_event_median_us(lambda: fn(k), flush) for k in range(len(fields)))
+            gbs = per_cell[name] * n / (us * 1e-6) / 1e9
+            res["kernels"][name] = {"us": us, "bytes_per_cell": per_cell[name], "achieved_GBs": gbs,
+                                    "frac": gbs / peak}
+        if level == 6:
+            w = a["area_m2"]
+            errs = {"laplacian_vs_oracle": 0.0, "gradient_vs_oracle": 0.0, "divergence_vs_oracle": 0.0,
+                    "laplacian_vs_analytic_rel_l2": 0.0, "gradient_vs_analytic_rel_l2": 0.0,
+                    "divergence_vs_analytic_rel_l2": 0.0}
+            cpu_s = 0.0
+            for k, F in enumerate(fields):
+                lap = pg.laplacian(m, x_d[k]).cpu().numpy()
+                ge, gn = (t.cpu().numpy() for t in pg.gradient(m, x_d[k]))
+                div = pg.divergence(m, f_d[k]).cpu().numpy()
+                t = time.perf_counter()
+                lo, (eo, no), do = om.laplacian(F.value), om.gradient(F.value), om.divergence(F.edge_flux)
+                cpu_s += time.perf_counter() - t
+                errs["laplacian_vs_oracle"] = max(errs["laplacian_vs_oracle"], float(np.max(np.abs(lap - lo)) / np.max(np.abs(lo))))
+                errs["gradient_vs_oracle"] = max(errs["gradient_vs_oracle"], float(max(np.max(np.abs(ge - eo)), np.max(np.abs(gn - no))) / np.max(np.abs(eo))))
+                errs["divergence_vs_oracle"] = max(errs["divergence_vs_oracle"], float(np.max(np.abs(div - do)) / np.max(np.abs(do))))
+                errs["laplacian_vs_analytic_rel_l2"] = max(errs["laplacian_vs_analytic_rel_l2"], rel_l2(lap, F.laplacian, w))
+                errs["gradient_vs_analytic_rel_l2"] = max(errs["gradient_vs_analytic_rel_l2"],
+                                                          rel_l2(ge, F.east, w), rel_l2(gn, F.north, w))
+                errs["divergence_vs_analytic_rel_l2"] = max(errs["divergence_vs_analytic_rel_l2"], rel_l2(div, F.laplacian, w))
+            res["errors"] = errs
+            gpu_us = sum(v["us"] for v in res["kernels"].values()) * len(fields)
+            res["cpu_baseline"] = {"seconds": cpu_s, "cores": 1, "kind": "port",
+                                   "sample": "the oracle's gradient, divergence and Laplacian of the 8 fields"}
+            res["gpu_over_cpu"] = cpu_s / (gpu_us * 1e-6)
+        out[f"operators_L{level}"] = res
+
+    # the config-0 solve on L6, plain FP64, one planet per call (tuned)
+    m = pg.make_icosphere(6, R)
+    inp = W.step_inputs(m, args.seed)
+    t0, src = torch.from_numpy(inp.t0).to(dev), torch.from_numpy(inp.source).to(dev)
+    solo = pg.TunedSolo(precision="fp64", **SOLVER)
+    rep = {}
+    ms = _median_ms(lambda: rep.update(r=solo.step(m, t0, src, inp.heat_capacity, inp.dt, inp.conductance)))
+    t_new = rep["r"][0].cpu().numpy()
+    om = O.OracleMesh(m.arrays())
+    tight = O.OracleHierarchy(om).transport_step(inp.conductance, inp.heat_capacity, inp.dt, inp.t0, inp.source,
+                                                 tol=1e-13)
+    t = time.perf_counter()
+    base = O.OracleHierarchy(om).transport_step(inp.conductance, inp.heat_capacity, inp.dt, inp.t0, inp.source,
+                                                tol=1e-10)
+    cpu_s = time.perf_counter() - t
+    r = rep["r"][1]
+    out["solve_L6"] = {"ms": ms, "iterations": r.iterations, "relative_residual": r.relative_residual,
+                       "closure": r.closure, "max_abs_T_vs_oracle_K": float(np.max(np.abs(t_new - tight["t_new"]))),
+                       "cpu_baseline": {"seconds": cpu_s, "cores": 1, "kind": "port", "pcg_iterations": base["iterations"]},
+                       "gpu_over_cpu": cpu_s / (ms * 1e-3)}
+
+    # column radiation over 10 layers for every L6 cell
+    col = W.column_profiles(inp.t0, 10, seed=args.seed)
+    k = pg.column_constants(**W.EARTH_COLUMN)
+    ins = [torch.from_numpy(np.ascontiguousarray(v)).to(dev) for v in
+           (col.temperature, col.humidity, col.cloud_water, col.surface_temperature, col.surface_pressure)]
+    res = {}
+    us = _event_median_us(lambda: res.update(o=pg.column_radiation(k, *ins)), flush)
+    n = m.cell_count
+    per_cell = (7 * 10 + 7) * 8.0
+    gbs = per_cell * n / (us * 1e-6) / 1e9
+    got = [o.cpu().numpy() for o in res["o"]]
+    t = time.perf_counter()
+    ref = O.column_radiation(W.column_constant_vector(), col.temperature, col.humidity, col.cloud_water,
+                             col.surface_temperature, col.surface_pressure)
+    cpu_s = time.perf_counter() - t
+    rel = max(float(np.max(np.abs(g - r_) / np.maximum(np.abs(r_), 1e-300))) for g, r_ in zip(got, ref))
+    out["column_L6"] = {"cells": n, "layers": 10, "us": us, "bytes_per_cell": per_cell, "achieved_GBs": gbs,
+                        "frac": gbs / peak, "max_rel_vs_oracle": rel,
+                        "cpu_baseline": {"seconds": cpu_s, "cores": 1, "kind": "port"},
+                        "gpu_over_cpu": cpu_s / (us * 1e-6)}
+    print(json.dumps(out))
+
+
+# ---- config 2: one L8 planet, 32 right-hand sides --------------------------------------------------
+
+def run_l8rhs(args, rank, local_rank):
+    raise SystemExit("the multi-RHS block solve is not built yet")
+
+
 # ---- CPU baseline and the reference arm ------------------------------------------------------
 
-def _oracle_solve(payload):
-    """One planet's sub-step by the oracle's port of the reference (FP64 PCG + SGS V-cycle)."""
+def inp_dict(inp) -> dict:
+    return {"conductance": inp.conductance, "heat_capacity": inp.heat_capacity, "dt": inp.dt, "t0": inp.t0,
+            "source": inp.source}
+
+
+def _oracle_run(payload):
     arrays, inp, edge_g, tol = payload
     from oracle import oracle as O
 
@@ -605,21 +923,27 @@ def _oracle_solve(payload):
     t = time.perf_counter()
     out = h.transport_step(inp["conductance"], inp["heat_capacity"], inp["dt"], inp["t0"], inp["source"], tol=tol,
                            edge_g=None if edge_g is None else om.directed_conductance(edge_g))
-    return time.perf_counter() - t, out["iterations"]
+    return time.perf_counter() - t, out
 
 
-def _payload(m, inp):
-    return (m.arrays(), {"conductance": inp.conductance, "heat_capacity": inp.heat_capacity, "dt": inp.dt,
-                         "t0": inp.t0, "source": inp.source}, inp.edge_conductance, 1e-10)
+def _oracle_solve(payload):
+    """One planet's sub-step by the oracle's port of the reference (FP64 PCG + SGS V-cycle):
+    its time and PCG iterations."""
+    dt, out = _oracle_run(payload)
+    return dt, out["iterations"]
+
+
+def _oracle_solve_full(payload):
+    """The same, returning the new temperature and the transport H."""
+    _, out = _oracle_run(payload)
+    return out["t_new"], out["transport"]
 
 
 def cpu_baseline(planets, args):
     """A bounded sample on one host core: every planet of the mix once (about 10-30 s)."""
-    from oracle import oracle as O  # noqa: F401  (the checker; timed here as the CPU baseline)
-
     total, iters = 0.0, 0
     for m, inp in planets:
-        dt, it = _oracle_solve(_payload(m, inp))
+        dt, it = _oracle_solve((m.arrays(), inp_dict(inp), inp.edge_conductance, 1e-10))
         total += dt
         iters += it
     return {"value": len(planets) / total, "unit": "sub-steps/s", "cores": 1, "kind": "port",
@@ -630,12 +954,18 @@ def cpu_baseline(planets, args):
 
 
 def run_reference(args, rank, world):
+    """The reference's algorithm (the oracle's port) on all host cores, one process per core,
+    every planet of the workload per step. Inputs are built by the oracle itself (its
+    restatement of the mesh builder and insolation): this arm loads no product library."""
     if rank != 0:
         return
     import multiprocessing as mp
 
-    planets = make_workload(args.workload, args.seed)
-    payloads = [_payload(m, inp) for m, inp in planets]
+    if args.workload not in WORKLOAD_NAMES:
+        print(json.dumps({"impl": "reference", "unavailable": f"no CPU reference arm for workload {args.workload}"}))
+        return
+    planets = oracle_workload(args.workload, args.seed)
+    payloads = [(a, inp_dict(inp), inp.edge_conductance, 1e-10) for a, inp in planets]
     cores = os.cpu_count() or 1
     ctx = mp.get_context("spawn")
     with ctx.Pool(processes=cores) as pool:
@@ -646,6 +976,9 @@ def run_reference(args, rank, world):
             results = pool.map(_oracle_solve, payloads, chunksize=1)
         elapsed = time.perf_counter() - t
     value = len(planets) * args.steps / elapsed
+    cells = sum(len(a["area_m2"]) for a, _ in planets)
+    config = static_config(args.workload, len(planets), cells)
+    config["pcg_iterations"] = sum(r[1] for r in results)
     line = {
         "impl": "reference",
         "metric": "sub-steps/s at 1e-10 relative residual",
@@ -660,12 +993,12 @@ def run_reference(args, rank, world):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": "same planets and inputs as the GB300 arm", "planets": len(planets),
-                   "cells": sum(m.cell_count for m, _ in planets), "pcg_iterations": sum(r[1] for r in results)},
+        "config": config,
         "cpu_baseline": {"value": value, "unit": "sub-steps/s", "cores": cores, "kind": "port",
                          "sample": "every planet of the workload per step, one process per core (the oracle's "
                                    "restatement of the reference's FP64 PCG + SGS solve: bit-identical solutions, "
-                                   "within 1% of the reference's own speed where both compile)"},
+                                   "within 1% of the reference's own speed where both compile); planets built by "
+                                   "the oracle's restatement of the reference's mesh builder"},
         "e2e": {"value": value, "unit": "sub-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -677,9 +1010,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["batch", "l8", "serve", "next"], default="batch")
-    ap.add_argument("--serve-rate", type=float, default=5000.0)
-    ap.add_argument("--serve-requests", type=int, default=2000)
+    ap.add_argument("--workload", choices=["batch", "l8", "l8rhs", "ops", "serve", "next"], default="batch")
+    ap.add_argument("--serve-requests", type=int, default=2000, help="requests per offered rate (fewer at 50/s)")
     ap.add_argument("--skip-serve", action="store_true")
     ap.add_argument("--native-serve", action="store_true",
                     help="serving: also run the trace through the library's own loop (psgb_server_*)")
@@ -707,6 +1039,12 @@ def main():
         return
     if args.workload == "next":
         run_next(args, rank, local_rank)
+        return
+    if args.workload == "ops":
+        run_ops(args, rank, local_rank)
+        return
+    if args.workload == "l8rhs":
+        run_l8rhs(args, rank, local_rank)
         return
     run_gb300(args, rank, world, local_rank)
 

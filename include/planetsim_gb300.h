@@ -443,6 +443,14 @@ int psgb_solve_implicit_advection_diffusion(psgb_planet* planet, const psgb_adve
  * without passing (and without the library comparing) the arrays on every call. */
 int psgb_batch_set_edge_conductance(psgb_batch* batch, const double* const* edge_conductance);
 
+/* Nonzero: every step of the batch assembles its matrix again on the device (the fine
+ * matrix from the staged C, dt and conductances, the Galerkin values of every coarse
+ * level, the coarsest levels' inverses), as the reference does on every call of
+ * solve_implicit_transport (heat_transport.cpp:613); zero (the default): the assembled
+ * matrix is reused while C, dt and the conductances are unchanged. Results are the same
+ * either way. */
+int psgb_batch_set_reassembly(psgb_batch* batch, int every_step);
+
 /* Per-level settings of a batch's solve. The reference has no counterpart (its smoother
  * is fixed, heat_transport.cpp:258-286); the autotuner picks them for the batch's GPU:
  * launch shapes (tiles per thread; never change a result) and damped-Jacobi sweeps per

@@ -293,3 +293,48 @@ int orc_icosphere(std::uint32_t level, double radius_m, double* center, double* 
 }
 
 }  // extern "C"
+
+// ---- the sub-step-mean insolation of the benchmark's source term -----------------------
+//
+// compute_substep_mean_insolation (sim/planet/orbit/substep_forcing.cpp:102-127) with
+// daily_mean_insolation_W_m2 (:35-56): per cell, the weighted sum over the sub-step's 16
+// orbit nodes of the daily-mean insolation at the cell's latitude (sin = z, cos =
+// sqrt(x^2 + y^2) of its unit centre), stored in FP32. The nodes (weight, sin and cos of
+// the declination, incident flux) are the reference's own for the sub-step, passed in.
+namespace {
+
+double daily_mean(double sin_lat, double cos_lat, double sin_dec, double cos_dec, double flux) {
+    const double pi = 3.14159265358979323846;
+    const double a = sin_lat * sin_dec;
+    const double b = cos_lat * cos_dec;
+    double h = 0.0;
+    if (b <= 0.0) {
+        h = a > 0.0 ? pi : 0.0;
+    } else {
+        const double c = -a / b;
+        if (c <= -1.0) {
+            h = pi;
+        } else if (c < 1.0) {
+            h = std::acos(c);
+        }
+    }
+    const double value = flux / pi * (h * a + b * std::sin(h));
+    return std::max(0.0, value);
+}
+
+}  // namespace
+
+extern "C" void orc_substep_mean_insolation(std::uint64_t cells, const double* center, const double* weight,
+                                            const double* sin_dec, const double* cos_dec, const double* flux,
+                                            std::uint32_t nodes, float* out) {
+    for (std::uint64_t c = 0; c < cells; ++c) {
+        const double x = center[3 * c], y = center[3 * c + 1], z = center[3 * c + 2];
+        const double sin_lat = z;
+        const double cos_lat = std::sqrt(x * x + y * y);
+        double mean = 0.0;
+        for (std::uint32_t k = 0; k < nodes; ++k) {
+            mean += weight[k] * daily_mean(sin_lat, cos_lat, sin_dec[k], cos_dec[k], flux[k]);
+        }
+        out[c] = static_cast<float>(mean);
+    }
+}

@@ -81,6 +81,7 @@ def lib() -> C.CDLL:
         L.orc_icosphere_counts.argtypes = [C.c_uint32, P, P, P]
         L.orc_icosphere.restype = C.c_int
         L.orc_icosphere.argtypes = [C.c_uint32, C.c_double] + [P] * 19
+        L.orc_substep_mean_insolation.argtypes = [C.c_uint64, P, P, P, P, P, C.c_uint32, P]
         _lib = L
     return _lib
 
@@ -112,6 +113,18 @@ def icosphere(level: int, radius_m: float) -> dict:
     if lib().orc_icosphere(level, float(radius_m), *[_p(out[name]) for name in order]) != 0:
         raise ValueError(f"oracle mesh: level {level}, radius {radius_m}")
     out["graph_area_m2"] = out["area_m2"]
+    return out
+
+
+def substep_mean_insolation(center, nodes) -> np.ndarray:
+    """The reference's sub-step-mean insolation per cell (FP32), from unit cell centres
+    [n, 3] and the sub-step's orbit nodes [16, 5] (time, weight, sin and cos of the
+    declination, incident flux: the reference's substep_forcing_nodes)."""
+    c = np.ascontiguousarray(center, dtype=np.float64)
+    nd = np.ascontiguousarray(nodes, dtype=np.float64)
+    cols = [np.ascontiguousarray(nd[:, j]) for j in (1, 2, 3, 4)]
+    out = np.empty(len(c), dtype=np.float32)
+    lib().orc_substep_mean_insolation(len(c), _p(c), *[_p(x) for x in cols], len(nd), _p(out))
     return out
 
 

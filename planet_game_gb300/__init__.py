@@ -12,6 +12,7 @@ from .api import (  # noqa: F401
     PlanetMesh,
     QuarticResponse,
     TransportGraph,
+    TunedSolo,
     agglomerated_transport_graph,
     column_constants,
     column_radiation,

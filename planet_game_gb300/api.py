@@ -648,6 +648,12 @@ class Batch:
         arr = (C.c_void_p * n)(*[None if e is None else e.ctypes.data for e in keep])
         _raise(capi.load().psgb_batch_set_edge_conductance(self._h, arr))
 
+    def set_reassembly(self, every_step: bool) -> None:
+        """True: every step assembles the matrix, its Galerkin coarse values and the coarsest
+        inverses again on the device (as the reference does per call); False (default):
+        the assembled matrix is reused while C, dt and the conductances are unchanged."""
+        _raise(capi.load().psgb_batch_set_reassembly(self._h, 1 if every_step else 0))
+
     def autotune(self, t0, sources, heat_capacity, dt, conductance=None, edge_conductance=None, **options) -> dict:
         """Pick per-level launch shapes and sweeps by timing trial solves of this sub-step;
         the batch keeps them (see `tuning`). Nothing is written back."""
@@ -706,6 +712,53 @@ class Batch:
         if code not in (capi.OK, capi.ERR_NOT_CONVERGED, capi.ERR_BREAKDOWN):
             _raise(code)
         return out, [_step_result(r) for r in reps]
+
+
+class TunedSolo:
+    """Planets stepped one per call, each in a one-planet batch of its own - the drop-in
+    solve of a single planet - with the launch shapes and damped-Jacobi sweeps autotuned
+    once per mesh level (on the first planet of the level stepped) and reused for every
+    other planet of that level. The plain one-planet-at-a-time FP64 comparator of the
+    benchmark and of the serving comparator, tuned as the batched solves are.
+
+    A planet's per-edge conductance is stored with its batch on its first step; later
+    steps of the planet use that array."""
+
+    def __init__(self, precision: str = "fp64", autotune: bool = True, **solver):
+        self.options = dict(solver, precision=precision)
+        self.autotune = autotune
+        self._batches: dict[int, tuple] = {}
+        self.tunings: dict[tuple, dict] = {}
+
+    def batch_of(self, mesh: PlanetMesh, t0, source, heat_capacity, dt, conductance, edge_conductance=None):
+        key = id(mesh)
+        entry = self._batches.get(key)
+        if entry is None:
+            b = Batch([mesh])
+            stored = None
+            if edge_conductance is not None:
+                b.set_edge_conductance([edge_conductance])
+                stored = "stored"
+            entry = (mesh, b, stored)
+            self._batches[key] = entry
+            if self.autotune:
+                level = (mesh.subdivision, mesh.agglomerated)
+                if level not in self.tunings:
+                    self.tunings[level] = b.autotune([t0], [source], [heat_capacity], [dt], conductance=[conductance],
+                                                     edge_conductance=stored, **self.options)
+                else:
+                    b.set_tuning(self.tunings[level])
+        return entry[1], entry[2]
+
+    def step(self, mesh: PlanetMesh, t0, source, heat_capacity, dt, conductance, edge_conductance=None,
+             out=None, transport_out=None):
+        """One sub-step of one planet: (t_new, report)."""
+        b, stored = self.batch_of(mesh, t0, source, heat_capacity, dt, conductance, edge_conductance)
+        outs, reps = b.transport_step([t0], [source], [heat_capacity], [dt], conductance=[conductance],
+                                      edge_conductance=stored, out=None if out is None else [out],
+                                      transport_out=None if transport_out is None else [transport_out],
+                                      **self.options)
+        return outs[0], reps[0]
 
 
 def default_lanes(meshes: list[PlanetMesh]) -> list[list[int]]:
@@ -784,6 +837,10 @@ class LaneBatch:
     @property
     def tuning(self) -> list:
         return [b.tuning for b in self.batches]
+
+    def set_reassembly(self, every_step: bool) -> None:
+        for b in self.batches:
+            b.set_reassembly(every_step)
 
     def set_tuning(self, tunings) -> None:
         for b, t in zip(self.batches, tunings if tunings is not None else [None] * len(self.batches)):

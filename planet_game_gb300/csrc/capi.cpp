@@ -206,6 +206,13 @@ void assemble_step_matrix(psgb::Batch& b, const psgb_step_params* params, cudaSt
         same = b.assembled_edges[i].size() == e &&
                std::memcmp(b.assembled_edges[i].data(), edges[i], e * sizeof(double)) == 0;
     }
+    if (same && b.reassemble) {
+        // the parameters are staged on the device already: the device part of the
+        // assembly again (fine matrix, Galerkin values, coarsest inverses)
+        psgb::assemble_transport(b, b.slope_field, b.conductance, b.step_edge_conductance, st);
+        psgb::prepare_levels(b, st);
+        return;
+    }
     if (same) return;
     const std::size_t P0 = b.levels[0].rows;
     std::vector<double> slope_of(I), conductance(I);
@@ -232,14 +239,15 @@ void assemble_step_matrix(psgb::Batch& b, const psgb_step_params* params, cudaSt
         PSGB_CUDA(cudaStreamSynchronize(st));
         edge_g = b.edge_g;
     }
-    // slope field (dt/C per cell of every planet) in b.tmp2
+    // slope field (dt/C per cell of every planet), kept for reassembly
     std::vector<double> slope(P0, 1.0);
     for (std::uint32_t i = 0; i < I; ++i) {
         const std::size_t n = b.planets[i]->mesh.cells;
         for (std::size_t c = 0; c < n; ++c) slope[b.fine_base[i] + c] = slope_of[i];
     }
-    PSGB_CUDA(cudaMemcpyAsync(b.tmp2, slope.data(), P0 * sizeof(double), cudaMemcpyHostToDevice, st));
-    psgb::assemble_transport(b, b.tmp2, b.conductance, edge_g, st);
+    if (b.slope_field == nullptr) b.slope_field = b.store.alloc<double>(P0);
+    PSGB_CUDA(cudaMemcpyAsync(b.slope_field, slope.data(), P0 * sizeof(double), cudaMemcpyHostToDevice, st));
+    psgb::assemble_transport(b, b.slope_field, b.conductance, edge_g, st);
     psgb::prepare_levels(b, st);
     PSGB_CUDA(cudaStreamSynchronize(st));
     b.assembled_key = key;
@@ -864,6 +872,14 @@ int psgb_batch_autotune(psgb_batch* h, const psgb_step_params* params, const psg
         psgb::launch_step_rhs(step_view(b), b.t0, b.src, b.bb, b.tmp, b.xr, st);
         const psgb::Tuning t = psgb::autotune(b, opt, b.bb, b.tmp2, st);
         if (out != nullptr) fill_tuning(t, out);
+        return PSGB_OK;
+    });
+}
+
+int psgb_batch_set_reassembly(psgb_batch* h, int every_step) {
+    return guarded([&] {
+        require(h != nullptr, "null argument");
+        h->batch->reassemble = every_step != 0;
         return PSGB_OK;
     });
 }

@@ -86,6 +86,7 @@ struct DenseTask {
     const T* inv;
     const T* b;
     T* x;
+    unsigned long long* bytes = nullptr;   // algorithmic-byte counter while profiling, else null
 };
 
 // ---- multigrid.cu ---------------------------------------------------------

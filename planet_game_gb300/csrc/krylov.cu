@@ -145,66 +145,66 @@ __global__ void k_outer_account(InstanceScalars* sc, std::uint32_t instances) {
 template <typename T>
 void KrylovLaunch<T>::bicg_init(const LevelView<T>& lv, const T* b, T* x, T* r, T* shadow, T* p, T* v,
                                 const ReduceCtx& ctx, double tol, int max_it, cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_bicg_init<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, b, x, r, shadow, p, v, ctx, tol, max_it)));
+    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_bicg_init<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamKrylovVector), b, x, r, shadow, p, v, ctx, tol, max_it)));
     launch_finish<ph::kFinBicgInit>(kFamKrylovVector, ctx, st, ph::FinishParams{tol, max_it, 0, nullptr});
 }
 template <typename T>
 void KrylovLaunch<T>::bicg_p(const LevelView<T>& lv, const T* r, const T* v, T* p, T* xv, T omega_j,
                              const InstanceScalars* sc, cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_bicg_p<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, r, v, p, xv, omega_j, sc)));
+    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_bicg_p<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamKrylovVector), r, v, p, xv, omega_j, sc)));
 }
 template <typename T>
 void KrylovLaunch<T>::bicg_v(const LevelView<T>& lv, const T* in, T* out, const T* shadow,
                              const ReduceCtx& ctx, cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovSpmv, st, PSGB_WIDTHS(lv.width, PSGB_STENCIL_SETS(lv.sets_stencil, launch_pdl(k_bicg_v<T, W, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, in, out, shadow, ctx))));
+    PSGB_LAUNCH(kFamKrylovSpmv, st, PSGB_WIDTHS(lv.width, PSGB_STENCIL_SETS(lv.sets_stencil, launch_pdl(k_bicg_v<T, W, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamKrylovSpmv), in, out, shadow, ctx))));
     launch_finish<ph::kFinBicgV>(kFamKrylovSpmv, ctx, st);
 }
 template <typename T>
 void KrylovLaunch<T>::bicg_s(const LevelView<T>& lv, const T* r, const T* v, T* s, T* xv, T omega_j,
                              const ReduceCtx& ctx, cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_bicg_s<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, r, v, s, xv, omega_j, ctx)));
+    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_bicg_s<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamKrylovVector), r, v, s, xv, omega_j, ctx)));
     launch_finish<ph::kFinBicgS>(kFamKrylovVector, ctx, st);
 }
 template <typename T>
 void KrylovLaunch<T>::bicg_t(const LevelView<T>& lv, const T* shat, T* t, const T* s,
                              const ReduceCtx& ctx, cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovSpmv, st, PSGB_WIDTHS(lv.width, PSGB_STENCIL_SETS(lv.sets_stencil, launch_pdl(k_bicg_t<T, W, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, shat, t, s, ctx))));
+    PSGB_LAUNCH(kFamKrylovSpmv, st, PSGB_WIDTHS(lv.width, PSGB_STENCIL_SETS(lv.sets_stencil, launch_pdl(k_bicg_t<T, W, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamKrylovSpmv), shat, t, s, ctx))));
     launch_finish<ph::kFinBicgT>(kFamKrylovSpmv, ctx, st);
 }
 template <typename T>
 void KrylovLaunch<T>::bicg_x(const LevelView<T>& lv, const T* phat, const T* shat, const T* s,
                              const T* t, T* x, T* r, const T* shadow, const ReduceCtx& ctx,
                              cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_bicg_x<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, phat, shat, s, t, x, r, shadow, ctx)));
+    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_bicg_x<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamKrylovVector), phat, shat, s, t, x, r, shadow, ctx)));
     launch_finish<ph::kFinBicgX>(kFamKrylovVector, ctx, st);
 }
 template <typename T>
 void KrylovLaunch<T>::pcg_init(const LevelView<T>& lv, const T* b, T* x, T* r, T* p, T* xv, T omega_j,
                                const ReduceCtx& ctx, double tol, int max_it, cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_pcg_init<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, b, x, r, p, xv, omega_j, ctx, tol, max_it)));
+    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_pcg_init<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamKrylovVector), b, x, r, p, xv, omega_j, ctx, tol, max_it)));
     launch_finish<ph::kFinPcgInit>(kFamKrylovVector, ctx, st, ph::FinishParams{tol, max_it, 0, nullptr});
 }
 template <typename T>
 void KrylovLaunch<T>::pcg_rz(const LevelView<T>& lv, const T* r, const T* z, const ReduceCtx& ctx,
                              cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_pcg_rz<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, r, z, ctx)));
+    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_pcg_rz<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamKrylovVector), r, z, ctx)));
     launch_finish<ph::kFinPcgRz>(kFamKrylovVector, ctx, st);
 }
 template <typename T>
 void KrylovLaunch<T>::pcg_p(const LevelView<T>& lv, const T* z, T* p, const InstanceScalars* sc,
                             cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_pcg_p<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, z, p, sc)));
+    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_pcg_p<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamKrylovVector), z, p, sc)));
 }
 template <typename T>
 void KrylovLaunch<T>::pcg_q(const LevelView<T>& lv, const T* p, T* q, const ReduceCtx& ctx,
                             cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovSpmv, st, PSGB_WIDTHS(lv.width, PSGB_STENCIL_SETS(lv.sets_stencil, launch_pdl(k_pcg_q<T, W, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, p, q, ctx))));
+    PSGB_LAUNCH(kFamKrylovSpmv, st, PSGB_WIDTHS(lv.width, PSGB_STENCIL_SETS(lv.sets_stencil, launch_pdl(k_pcg_q<T, W, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamKrylovSpmv), p, q, ctx))));
     launch_finish<ph::kFinPcgQ>(kFamKrylovSpmv, ctx, st);
 }
 template <typename T>
 void KrylovLaunch<T>::pcg_xr(const LevelView<T>& lv, const T* p, const T* q, T* x, T* r, T* xv,
                              T omega_j, const ReduceCtx& ctx, cudaStream_t st) {
-    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_pcg_xr<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, p, q, x, r, xv, omega_j, ctx)));
+    PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_pcg_xr<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamKrylovVector), p, q, x, r, xv, omega_j, ctx)));
     launch_finish<ph::kFinPcgXr>(kFamKrylovVector, ctx, st);
 }
 
@@ -213,14 +213,14 @@ template struct KrylovLaunch<double>;
 
 void launch_outer_init(const LevelView<double>& lv, const double* b, const ReduceCtx& ctx, double tol,
                        int max_refine, const std::uint8_t* active, cudaStream_t st) {
-    PSGB_LAUNCH(kFamRefine, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_outer_init<R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, b, ctx, tol, max_refine, active)));
+    PSGB_LAUNCH(kFamRefine, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_outer_init<R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamRefine), b, ctx, tol, max_refine, active)));
     launch_finish<ph::kFinOuterInit>(kFamRefine, ctx, st, ph::FinishParams{tol, 0, max_refine, active});
 }
 
 template <typename TI>
 void launch_outer_residual(const LevelView<double>& lv, const double* b, const double* x, double* r64,
                            TI* rin, const ReduceCtx& ctx, int max_refine, cudaStream_t st) {
-    PSGB_LAUNCH(kFamRefine, st, PSGB_WIDTHS(lv.width, PSGB_STENCIL_SETS(lv.sets_stencil, launch_pdl(k_outer_residual<TI, W, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, b, x, r64, rin, ctx, max_refine))));
+    PSGB_LAUNCH(kFamRefine, st, PSGB_WIDTHS(lv.width, PSGB_STENCIL_SETS(lv.sets_stencil, launch_pdl(k_outer_residual<TI, W, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamRefine), b, x, r64, rin, ctx, max_refine))));
     launch_finish<ph::kFinOuterResidual>(kFamRefine, ctx, st, ph::FinishParams{0.0, 0, max_refine, nullptr});
 }
 
@@ -228,7 +228,7 @@ template <typename TI>
 void launch_outer_update(const LevelView<double>& lv, const TI* delta, double* x, InstanceScalars* sc,
                          std::uint32_t instances, cudaStream_t st) {
     PSGB_LAUNCH(kFamRefine, st, launch_pdl(k_outer_account, (instances + 127) / 128, 128, st, sc, instances));
-    PSGB_LAUNCH(kFamRefine, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_outer_update<TI, R>, ph::tile_sets(lv.tiles, R), kTile, st, lv, delta, x, sc)));
+    PSGB_LAUNCH(kFamRefine, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_outer_update<TI, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamRefine), delta, x, sc)));
 }
 
 template void launch_outer_residual<float>(const LevelView<double>&, const double*, const double*, double*,

@@ -259,9 +259,17 @@ __global__ void k_dense_solve(DenseTask<T> dense, const InstanceScalars* sc, int
 
 // ---- launchers -----------------------------------------------------------------
 
-// Jacobi sweeps are accounted as fine-level or coarse-level sweeps.
+// Jacobi sweeps, residuals and prolongations are accounted as fine-level or coarse-level
+// launches; a restriction by the level it restricts onto (level 1: from the fine level).
 template <typename T>
 inline int smooth_family(const LevelView<T>& lv) { return lv.level == 0 ? kFamSmooth : kFamSmoothCoarse; }
+template <typename T>
+inline int residual_family(const LevelView<T>& lv) { return lv.level == 0 ? kFamResidual : kFamResidualCoarse; }
+template <typename T>
+inline int restrict_family(const LevelView<T>& coarse) { return coarse.level <= 1 ? kFamRestrict : kFamRestrictCoarse; }
+template <typename T>
+inline int prolong_family(const LevelView<T>& lv) { return lv.level == 0 ? kFamProlong : kFamProlongCoarse; }
+
 
 void launch_assemble_transport(const LevelView<double>& fine, const double* w, const double* wsum,
                                const double* area, const double* slope, const double* conductance,
@@ -296,7 +304,7 @@ void launch_smooth_zero(const LevelView<T>& lv, const T* b, T* x, T omega, const
                         int gate, cudaStream_t stream) {
     PSGB_LAUNCH(smooth_family(lv), stream,
                 PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_smooth_zero<T, R>, ph::tile_sets(lv.tiles, R), kTile, stream,
-                                                            lv, b, x, omega, sc, gate)));
+                                                            counted(lv, smooth_family(lv)), b, x, omega, sc, gate)));
 }
 
 template <typename T>
@@ -304,48 +312,50 @@ void launch_smooth(const LevelView<T>& lv, const T* b, const T* x, T* y, T omega
                    const InstanceScalars* sc, int gate, cudaStream_t stream, const DenseTask<T>& dense, int inner) {
     if (inner > 1) {
         PSGB_LAUNCH(smooth_family(lv), stream,
-                    PSGB_WIDTHS(lv.width, launch_pdl(k_smooth_block<T, W>, lv.tiles + dense.count, kTile, stream, lv, b, x, y,
-                                                     omega, inner, sc, gate, dense)));
+                    PSGB_WIDTHS(lv.width, launch_pdl(k_smooth_block<T, W>, lv.tiles + dense.count, kTile, stream,
+                                                     counted(lv, smooth_family(lv)), b, x, y, omega, inner, sc, gate,
+                                                     dense)));
         return;
     }
     PSGB_LAUNCH(smooth_family(lv), stream,
                 PSGB_STENCIL_SETS(lv.sets_stencil, PSGB_WIDTHS(lv.width,
-                    launch_pdl(k_smooth<T, W, R>, ph::tile_sets(lv.tiles, R) + dense.count, kTile, stream, lv, b, x, y, omega,
-                               sc, gate, dense))));
+                    launch_pdl(k_smooth<T, W, R>, ph::tile_sets(lv.tiles, R) + dense.count, kTile, stream,
+                               counted(lv, smooth_family(lv)), b, x, y, omega, sc, gate, dense))));
 }
 
 template <typename T>
 void launch_residual(const LevelView<T>& lv, const T* b, const T* x, T* r, const InstanceScalars* sc,
                      int gate, cudaStream_t stream, const DenseTask<T>& dense) {
-    PSGB_LAUNCH(kFamResidual, stream,
+    PSGB_LAUNCH(residual_family(lv), stream,
                 PSGB_STENCIL_SETS(lv.sets_stencil, PSGB_WIDTHS(lv.width,
-                    launch_pdl(k_residual<T, W, R>, ph::tile_sets(lv.tiles, R) + dense.count, kTile, stream, lv, b, x, r, sc,
-                               gate, dense))));
+                    launch_pdl(k_residual<T, W, R>, ph::tile_sets(lv.tiles, R) + dense.count, kTile, stream,
+                               counted(lv, residual_family(lv)), b, x, r, sc, gate, dense))));
 }
 
 template <typename T>
 void launch_spmv(const LevelView<T>& lv, const T* x, T* y, cudaStream_t stream) {
     PSGB_LAUNCH(kFamKrylovSpmv, stream,
                 PSGB_STENCIL_SETS(lv.sets_stencil, PSGB_WIDTHS(lv.width,
-                    launch_pdl(k_spmv<T, W, R>, ph::tile_sets(lv.tiles, R), kTile, stream, lv, x, y))));
+                    launch_pdl(k_spmv<T, W, R>, ph::tile_sets(lv.tiles, R), kTile, stream, counted(lv, kFamKrylovSpmv),
+                               x, y))));
 }
 
 template <typename T>
 void launch_restrict(const LevelView<T>& coarse, const std::uint32_t* member_offset,
                      const std::uint32_t* member, const T* r, T* bc, const InstanceScalars* sc,
                      int gate, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamRestrict, stream,
-                launch_pdl(k_restrict<T>, ph::tile_sets(coarse.tiles, ph::kRowsCoarse), kTile, stream, coarse, member_offset,
-                           member, r, bc, sc, gate));
+    PSGB_LAUNCH(restrict_family(coarse), stream,
+                launch_pdl(k_restrict<T>, ph::tile_sets(coarse.tiles, ph::kRowsCoarse), kTile, stream,
+                           counted(coarse, restrict_family(coarse)), member_offset, member, r, bc, sc, gate));
 }
 
 template <typename T>
 void launch_restrict_zero(const LevelView<T>& coarse, const std::uint32_t* member_offset,
                           const std::uint32_t* member, const T* r, T* bc, T* xc, T omega,
                           const InstanceScalars* sc, int gate, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamRestrict, stream,
-                launch_pdl(k_restrict_zero<T>, ph::tile_sets(coarse.tiles, ph::kRowsCoarse), kTile, stream, coarse,
-                           member_offset, member, r, bc, xc, omega, sc, gate));
+    PSGB_LAUNCH(restrict_family(coarse), stream,
+                launch_pdl(k_restrict_zero<T>, ph::tile_sets(coarse.tiles, ph::kRowsCoarse), kTile, stream,
+                           counted(coarse, restrict_family(coarse)), member_offset, member, r, bc, xc, omega, sc, gate));
 }
 
 template <typename T>
@@ -353,22 +363,24 @@ void launch_prolong_smooth(const LevelView<T>& lv, const std::int32_t* agg, cons
                            T* y, T omega, const InstanceScalars* sc, int gate, cudaStream_t stream) {
     PSGB_LAUNCH(smooth_family(lv), stream,
                 PSGB_STENCIL_SETS(lv.sets_stencil, PSGB_WIDTHS(lv.width,
-                    launch_pdl(k_prolong_smooth<T, W, R>, ph::tile_sets(lv.tiles, R), kTile, stream, lv, agg, e, b, x, y, omega,
-                               sc, gate))));
+                    launch_pdl(k_prolong_smooth<T, W, R>, ph::tile_sets(lv.tiles, R), kTile, stream,
+                               counted(lv, smooth_family(lv)), agg, e, b, x, y, omega, sc, gate))));
 }
 
 template <typename T>
 void launch_prolong(const LevelView<T>& fine, const std::int32_t* agg, const T* xc, T* x,
                     const InstanceScalars* sc, int gate, cudaStream_t stream) {
-    PSGB_LAUNCH(kFamProlong, stream,
+    PSGB_LAUNCH(prolong_family(fine), stream,
                 PSGB_VECTOR_SETS(fine.sets_vector, launch_pdl(k_prolong<T, R>, ph::tile_sets(fine.tiles, R), kTile, stream,
-                                                              fine, agg, xc, x, sc, gate)));
+                                                              counted(fine, prolong_family(fine)), agg, xc, x, sc, gate)));
 }
 
 template <typename T>
 void launch_dense_solve(const DenseTask<T>& dense, const InstanceScalars* sc, int gate, cudaStream_t stream) {
     if (dense.count == 0) return;
-    PSGB_LAUNCH(kFamDense, stream, launch_pdl(k_dense_solve<T>, dense.count, 256, stream, dense, sc, gate));
+    DenseTask<T> task = dense;
+    task.bytes = profile_bytes_for(kFamDense);
+    PSGB_LAUNCH(kFamDense, stream, launch_pdl(k_dense_solve<T>, dense.count, 256, stream, task, sc, gate));
 }
 
 #define PSGB_INSTANTIATE(T)                                                                           \

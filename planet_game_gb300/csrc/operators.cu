@@ -131,9 +131,11 @@ __global__ void k_step_rhs(std::uint32_t rows, const std::int32_t* __restrict__ 
                            const std::int32_t* __restrict__ tile_rows, const double* __restrict__ area,
                            const double* __restrict__ slope_of, const double* __restrict__ t0,
                            const double* __restrict__ src, double* __restrict__ rhs,
-                           double* __restrict__ slope, double* __restrict__ x0) {
+                           double* __restrict__ slope, double* __restrict__ x0, unsigned long long* bytes) {
     const int tile = blockIdx.x;
     const int row = tile * kTile + threadIdx.x;
+    // area, T0, S in; rhs, slope, x0 out
+    if (bytes != nullptr && threadIdx.x == 0) atomicAdd(bytes, 48ull * static_cast<unsigned>(tile_rows[tile]));
     if (threadIdx.x >= tile_rows[tile]) {
         rhs[row] = 0.0;
         slope[row] = 1.0;
@@ -159,10 +161,13 @@ __global__ void k_step_finish(std::uint32_t P, const std::int32_t* __restrict__ 
                               const double* __restrict__ slope_of, const double* __restrict__ t,
                               const double* __restrict__ t0, const double* __restrict__ src,
                               double* __restrict__ h_out, double* __restrict__ t_new,
-                              double* __restrict__ partial) {
+                              double* __restrict__ partial, unsigned long long* bytes) {
     const int tile = blockIdx.x;
     const int row = tile * kTile + threadIdx.x;
     const int inst = tile_inst[tile];
+    // columns, weights (and per-entry conductances), area, T, T0, S in; H, T_new out
+    if (bytes != nullptr && threadIdx.x == 0)
+        atomicAdd(bytes, (edge_conductance != nullptr ? 168ull : 120ull) * static_cast<unsigned>(tile_rows[tile]));
     double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     if (threadIdx.x < tile_rows[tile]) {
         const double own = t[row];
@@ -263,14 +268,14 @@ template void launch_divergence<double>(const DevMesh&, const double*, double*, 
 void launch_step_rhs(const StepView& v, const double* t0, const double* src, double* rhs, double* slope,
                      double* x0, cudaStream_t st) {
     PSGB_LAUNCH(kFamStep, st, k_step_rhs<<<v.tiles, kTile, 0, st>>>(v.rows, v.tile_inst, v.tile_rows, v.area, v.slope_of, t0, src,
-                                          rhs, slope, x0));
+                                          rhs, slope, x0, v.bytes));
 }
 
 void launch_step_finish(const StepView& v, const double* t, const double* t0, const double* src,
                         double* h, double* t_new, double* partial, double* sums, cudaStream_t st) {
     PSGB_LAUNCH(kFamStep, st, k_step_finish<<<v.tiles, kTile, 0, st>>>(v.rows, v.tile_inst, v.tile_rows, v.nbr, v.w, v.area,
                                              v.conductance, v.edge_conductance, v.slope_of, t, t0, src, h,
-                                             t_new, partial));
+                                             t_new, partial, v.bytes));
     PSGB_LAUNCH(kFamStep, st, k_sum_tiles<<<v.instances, 32, 0, st>>>(v.instances, v.tile_begin, partial, 6, sums));
 }
 

@@ -35,6 +35,7 @@ struct StepView {
     const double* conductance;          // [instances]
     const double* edge_conductance;     // [6][P] or null
     const double* slope_of;             // [instances] dt / C
+    unsigned long long* bytes;          // algorithmic-byte counter while the step family is profiled
 };
 
 // Held rows (slope <= 0) solve x = 0, as the reference masks their residual

@@ -20,6 +20,7 @@
 
 #include "common.cuh"
 #include "kernels.hpp"
+#include "profile.hpp"
 
 #include <stdexcept>
 
@@ -70,6 +71,21 @@ __device__ __forceinline__ void group_sync(int gid) {
 
 __device__ __forceinline__ void count_bytes(unsigned long long* counter, int lane, unsigned long long bytes) {
     if (counter != nullptr && lane == 0 && bytes != 0) atomicAdd(counter, bytes);
+}
+
+// A per-thread byte count summed over each warp (every lane of the warp calls it).
+__device__ __forceinline__ void count_bytes_warp(unsigned long long* counter, unsigned bytes) {
+    if (counter == nullptr) return;
+    const unsigned s = __reduce_add_sync(0xffffffffu, bytes);
+    if ((threadIdx.x & 31) == 0 && s != 0) atomicAdd(counter, static_cast<unsigned long long>(s));
+}
+
+// The view of one launch: its family's byte counter while a profile of it records.
+template <typename T>
+inline LevelView<T> counted(const LevelView<T>& lv, int family) {
+    LevelView<T> v = lv;
+    v.bytes = profile_bytes_for(family);
+    return v;
 }
 
 // Sum of N values over the 256 threads of a group, each value in its own fixed tree
@@ -129,6 +145,17 @@ __device__ __forceinline__ TileSet<R> tile_set(const std::uint32_t* meta, unsign
         s.sweep[k] = valid && (w[k] >> 31) != 0u;
     }
     return s;
+}
+
+// Algorithmic bytes of the open tiles of a tile set: `per_row` times their valid rows.
+template <int R>
+__device__ __forceinline__ void count_rows(unsigned long long* counter, int lane, const TileSet<R>& ts,
+                                           const bool (&on)[R], unsigned long long per_row) {
+    if (counter == nullptr || lane != 0) return;
+    unsigned long long rows = 0;
+#pragma unroll
+    for (int k = 0; k < R; ++k) rows += on[k] ? static_cast<unsigned long long>(ts.rows[k]) : 0ull;
+    if (rows != 0) atomicAdd(counter, rows * per_row);
 }
 
 template <int R>
@@ -401,7 +428,9 @@ __device__ void residual(const LevelView<T>& lv, int t0, int lane, const T* PSGB
     }
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-        if (on[k] && lane < ts.rows[k]) r[ts.tile[k] * kTile + lane] = out[k];
+        if (!on[k]) continue;
+        count_bytes(lv.bytes, lane, static_cast<unsigned long long>(ts.rows[k]) * (4ull * W + sizeof(T) * (W + 4ull)));
+        if (lane < ts.rows[k]) r[ts.tile[k] * kTile + lane] = out[k];
     }
 }
 
@@ -421,6 +450,7 @@ __device__ void spmv(const LevelView<T>& lv, int t0, int lane, const T* PSGB_PHA
     }
 #pragma unroll
     for (int k = 0; k < R; ++k) {
+        count_bytes(lv.bytes, lane, static_cast<unsigned long long>(ts.rows[k]) * (4ull * W + sizeof(T) * (W + 3ull)));
         if (lane < ts.rows[k]) y[ts.tile[k] * kTile + lane] = out[k];
     }
 }
@@ -438,14 +468,19 @@ __device__ void restrict_zero(const LevelView<T>& coarse, int t0, int lane, cons
 #pragma unroll
     for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && gate_open(sc, ts.inst[k], gate);
     if (!any_of(on)) return;
+    unsigned moved = 0;
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         if (!on[k] || lane >= ts.rows[k]) continue;
         const int row = ts.tile[k] * kTile + lane;
-        const T s = member_sum(member, moff[row], moff[row + 1], r);
+        const std::uint32_t k0 = moff[row], k1 = moff[row + 1];
+        const T s = member_sum(member, k0, k1, r);
         bc[row] = s;
         if (ts.sweep[k]) xc[row] = omega * coarse.inv[row] * s;
+        // offsets, members and their residuals, 1/diag, b_c and x_c
+        moved += 4u + (k1 - k0) * (4u + static_cast<unsigned>(sizeof(T))) + 3u * static_cast<unsigned>(sizeof(T));
     }
+    count_bytes_warp(coarse.bytes, moved);
 }
 
 template <typename T, int R>
@@ -453,12 +488,16 @@ __device__ void restrict_only(const LevelView<T>& coarse, int t0, int lane, cons
                               const std::uint32_t* PSGB_PHASE_RESTRICT member, const T* PSGB_PHASE_RESTRICT r,
                               T* PSGB_PHASE_RESTRICT bc, const InstanceScalars* sc, int gate) {
     const TileSet<R> ts = tile_set<R>(coarse.tile_meta, coarse.tiles, t0);
+    unsigned moved = 0;
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         if (lane >= ts.rows[k] || !gate_open(sc, ts.inst[k], gate)) continue;
         const int row = ts.tile[k] * kTile + lane;
-        bc[row] = member_sum(member, moff[row], moff[row + 1], r);
+        const std::uint32_t k0 = moff[row], k1 = moff[row + 1];
+        bc[row] = member_sum(member, k0, k1, r);
+        moved += 4u + (k1 - k0) * (4u + static_cast<unsigned>(sizeof(T))) + static_cast<unsigned>(sizeof(T));
     }
+    count_bytes_warp(coarse.bytes, moved);
 }
 
 // Prolongation fused with the first post-smoothing sweep: with x' = x + e[agg] (formed on
@@ -506,7 +545,10 @@ __device__ void prolong(const LevelView<T>& lv, int t0, int lane, const std::int
     const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-        if (lane >= ts.rows[k] || !ts.sweep[k] || !gate_open(sc, ts.inst[k], gate)) continue;
+        if (!ts.sweep[k] || !gate_open(sc, ts.inst[k], gate)) continue;
+        // agg, x read and written (the coarse correction is 1/16 of a row)
+        count_bytes(lv.bytes, lane, static_cast<unsigned long long>(ts.rows[k]) * (4ull + 2ull * sizeof(T)));
+        if (lane >= ts.rows[k]) continue;
         const int row = ts.tile[k] * kTile + lane;
         x[row] += xc[agg[row]];
     }
@@ -533,6 +575,9 @@ __device__ void dense_block(const DenseTask<T>& task, unsigned k, int lane, cons
     const int row = blk.y + (lane >> 5);
     if (row >= static_cast<int>(task.dense.size[blk.x])) return;
     dense_row<T>(task.dense, blk.x, row, lane & 31, task.inv, task.b, task.x);
+    // the inverse's row and the solution's entry (b is read from cache by every row)
+    if (task.bytes != nullptr && (lane & 31) == 0)
+        atomicAdd(task.bytes, static_cast<unsigned long long>(task.dense.size[blk.x] + 1) * sizeof(T));
 }
 
 // ---- scalar steps: one planet, once its sums are complete (ticket or finish launch) ----
@@ -705,6 +750,7 @@ __device__ void bicg_init(const LevelView<T>& lv, int t0, int gid, int lane, con
 #pragma unroll
     for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && ctx.sc[ts.inst[k]].outer_status == kRunning;
     if (!any_of(on)) return;
+    count_rows<R>(lv.bytes, lane, ts, on, 6ull * sizeof(T));
     T q[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -733,6 +779,7 @@ __device__ void bicg_p(const LevelView<T>& lv, int t0, int lane, const T* PSGB_P
 #pragma unroll
     for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && running(sc[ts.inst[k]]);
     if (!any_of(on)) return;
+    count_rows<R>(lv.bytes, lane, ts, on, 6ull * sizeof(T));
     T pv[R], zv[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -759,6 +806,7 @@ __device__ void bicg_v(const LevelView<T>& lv, int t0, int gid, int lane, const 
 #pragma unroll
     for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && running(ctx.sc[ts.inst[k]]);
     if (!any_of(on)) return;
+    count_rows<R>(lv.bytes, lane, ts, on, 4ull * W + sizeof(T) * (W + 4ull));
     const std::uint32_t P = lv.rows;
     T q[R], y[R];
 #pragma unroll
@@ -794,6 +842,7 @@ __device__ void bicg_s(const LevelView<T>& lv, int t0, int gid, int lane, const 
 #pragma unroll
     for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && running(ctx.sc[ts.inst[k]]);
     if (!any_of(on)) return;
+    count_rows<R>(lv.bytes, lane, ts, on, 5ull * sizeof(T));
     T q[R], sv[R], zv[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -832,6 +881,7 @@ __device__ void bicg_t(const LevelView<T>& lv, int t0, int gid, int lane, const 
         on[k] = ts.rows[k] > 0 && running(sc) && !sc.half_done;
     }
     if (!any_of(on)) return;
+    count_rows<R>(lv.bytes, lane, ts, on, 4ull * W + sizeof(T) * (W + 4ull));
     const std::uint32_t P = lv.rows;
     T q[2 * R], y[R];
 #pragma unroll
@@ -875,6 +925,7 @@ __device__ void bicg_x(const LevelView<T>& lv, int t0, int gid, int lane, const 
         half[k] = sc.half_done != 0;
     }
     if (!any_of(on)) return;
+    count_rows<R>(lv.bytes, lane, ts, on, 8ull * sizeof(T));
     T q[2 * R], xv[R], rv[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -918,6 +969,7 @@ __device__ void pcg_init(const LevelView<T>& lv, int t0, int gid, int lane, cons
 #pragma unroll
     for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && ctx.sc[ts.inst[k]].outer_status == kRunning;
     if (!any_of(on)) return;
+    count_rows<R>(lv.bytes, lane, ts, on, 5ull * sizeof(T));
     T q[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -947,6 +999,7 @@ __device__ void pcg_rz(const LevelView<T>& lv, int t0, int gid, int lane, const 
 #pragma unroll
     for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && running(ctx.sc[ts.inst[k]]);
     if (!any_of(on)) return;
+    count_rows<R>(lv.bytes, lane, ts, on, 2ull * sizeof(T));
     T q[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -966,9 +1019,13 @@ template <typename T, int R>
 __device__ void pcg_p(const LevelView<T>& lv, int t0, int lane, const T* PSGB_PHASE_RESTRICT z, T* p,
                       const InstanceScalars* sc) {
     const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
+    bool on[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && running(sc[ts.inst[k]]);
+    count_rows<R>(lv.bytes, lane, ts, on, 3ull * sizeof(T));   // z, p; p
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-        if (lane >= ts.rows[k] || !running(sc[ts.inst[k]])) continue;
+        if (lane >= ts.rows[k] || !on[k]) continue;
         const int row = ts.tile[k] * kTile + lane;
         p[row] = z[row] + T(sc[ts.inst[k]].beta) * p[row];
     }
@@ -983,6 +1040,7 @@ __device__ void pcg_q(const LevelView<T>& lv, int t0, int gid, int lane, const T
 #pragma unroll
     for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && running(ctx.sc[ts.inst[k]]);
     if (!any_of(on)) return;
+    count_rows<R>(lv.bytes, lane, ts, on, 4ull * W + sizeof(T) * (W + 3ull));
     const std::uint32_t P = lv.rows;
     T q[R], y[R];
 #pragma unroll
@@ -1018,6 +1076,7 @@ __device__ void pcg_xr(const LevelView<T>& lv, int t0, int gid, int lane, const 
 #pragma unroll
     for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && running(ctx.sc[ts.inst[k]]);
     if (!any_of(on)) return;
+    count_rows<R>(lv.bytes, lane, ts, on, 8ull * sizeof(T));
     T q[R], xn[R], rn[R], zn[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -1070,6 +1129,7 @@ __device__ void outer_init(const LevelView<double>& lv, int t0, int gid, int lan
         }
     }
     if (!any_of(on)) return;
+    count_rows<R>(lv.bytes, lane, ts, on, 8ull);
     double q[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -1095,6 +1155,7 @@ __device__ void outer_residual(const LevelView<double>& lv, int t0, int gid, int
 #pragma unroll
     for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && ctx.sc[ts.inst[k]].outer_status == kRunning;
     if (!any_of(on)) return;
+    count_rows<R>(lv.bytes, lane, ts, on, 4ull * W + 8ull * (W + 4ull) + sizeof(TI));
     const std::uint32_t P = lv.rows;
     double q[R], rv[R];
 #pragma unroll
@@ -1128,9 +1189,13 @@ template <typename TI, int R>
 __device__ void outer_update(const LevelView<double>& lv, int t0, int lane, const TI* PSGB_PHASE_RESTRICT delta, double* x,
                              const InstanceScalars* sc) {
     const TileSet<R> ts = tile_set<R>(lv.tile_meta, lv.tiles, t0);
+    bool on[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && sc[ts.inst[k]].outer_status == kRunning;
+    count_rows<R>(lv.bytes, lane, ts, on, 16ull + sizeof(TI));   // delta, x; x
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-        if (lane >= ts.rows[k] || sc[ts.inst[k]].outer_status != kRunning) continue;
+        if (lane >= ts.rows[k] || !on[k]) continue;
         const int row = ts.tile[k] * kTile + lane;
         x[row] += static_cast<double>(delta[row]);
     }
@@ -1143,4 +1208,7 @@ __device__ inline void outer_account(InstanceScalars& s) {
 }
 
 }  // namespace ph
+
+using ph::counted;
+
 }  // namespace psgb

@@ -267,6 +267,8 @@ struct Batch {
     std::vector<std::uint8_t> host_active;
     bool active_mask = false;          // some planet is left out of the current step
     double* edge_g = nullptr;          // [6][P0] per-entry conductance (lazily)
+    double* slope_field = nullptr;     // [P0] dt / C per row of the assembled matrix (lazily)
+    bool reassemble = false;           // assemble on every step, even with unchanged parameters
     const double* step_edge_conductance = nullptr;   // edge_g when the matrix uses it
     double* csr_values = nullptr;      // one-planet batches: set_matrix staging
     std::uint32_t* csr_offset = nullptr;   // one-planet batches: the graph's CSR offsets

@@ -17,16 +17,27 @@ struct Profile {
     std::mutex mu;
     std::atomic<int> family{-1};
     std::vector<cudaEvent_t> start, stop;
-    std::size_t used = 0;
+    std::size_t used = 0;          // event pairs handed out
     std::uint64_t launches = 0;
-    bool pending = false;
+    std::uint64_t generation = 0;  // bumped by every profile_begin
 } g_profile;
+
+// The event pair a thread's launch_begin handed out, closed by the same thread's
+// launch_end: two host threads launching the same family (lanes stepped side by side)
+// each time their own launch.
+struct PendingSlot {
+    std::size_t index = 0;
+    std::uint64_t generation = 0;
+    bool open = false;
+};
+thread_local PendingSlot t_pending;
 
 constexpr std::size_t kMaxEvents = 1 << 16;
 
 const char* const kNames[kFamCount] = {"smooth", "residual", "restrict", "prolong", "dense", "krylov_spmv",
                                        "krylov_vector", "refine", "setup", "step", "operator", "column",
-                                       "persistent", "smooth_coarse"};
+                                       "persistent", "smooth_coarse", "residual_coarse", "restrict_coarse",
+                                       "prolong_coarse"};
 
 }  // namespace
 
@@ -44,10 +55,8 @@ namespace {
 unsigned long long* g_bytes_counter = nullptr;   // device, allocated by the first profile_begin
 }
 
-unsigned long long* profile_bytes_counter(int level) {
-    const int f = g_profile.family;
-    const bool counted = f == kFamPersistent || (f == kFamSmooth && level == 0) || (f == kFamSmoothCoarse && level > 0);
-    return counted ? g_bytes_counter : nullptr;
+unsigned long long* profile_bytes_for(int family) {
+    return g_profile.family == family ? g_bytes_counter : nullptr;
 }
 
 std::uint64_t profile_bytes_exchange() {
@@ -72,18 +81,18 @@ void launch_begin(int family, cudaStream_t st) {
         g_profile.start.push_back(a);
         g_profile.stop.push_back(b);
     }
+    t_pending = PendingSlot{g_profile.used, g_profile.generation, true};
     cudaEventRecord(g_profile.start[g_profile.used], st);
-    g_profile.pending = true;
+    ++g_profile.used;
 }
 
 void launch_end(int family, cudaStream_t st) {
-    if (g_capturing || g_profile.family != family) return;
+    if (g_capturing || g_profile.family != family || !t_pending.open) return;
     std::lock_guard<std::mutex> lock(g_profile.mu);
-    if (!g_profile.pending) return;
-    cudaEventRecord(g_profile.stop[g_profile.used], st);
-    ++g_profile.used;
+    t_pending.open = false;
+    if (t_pending.generation != g_profile.generation || g_profile.family != family) return;
+    cudaEventRecord(g_profile.stop[t_pending.index], st);
     ++g_profile.launches;
-    g_profile.pending = false;
 }
 
 std::uint64_t launches_total() {
@@ -104,7 +113,7 @@ bool profile_begin(int family) {
     g_profile.family = family;
     g_profile.used = 0;
     g_profile.launches = 0;
-    g_profile.pending = false;
+    ++g_profile.generation;
     return true;
 }
 
@@ -112,6 +121,8 @@ bool profile_end(double* total_ms, std::uint64_t* launches) {
     std::lock_guard<std::mutex> lock(g_profile.mu);
     if (g_profile.family < 0) return false;
     double sum = 0.0;
+    // every slot handed out was closed by its launch_end (launches complete before a
+    // profile ends: the caller synchronises its steps first)
     for (std::size_t i = 0; i < g_profile.used; ++i) {
         cudaEventSynchronize(g_profile.stop[i]);
         float ms = 0.0F;
@@ -120,6 +131,7 @@ bool profile_end(double* total_ms, std::uint64_t* launches) {
     *total_ms = sum;
     *launches = g_profile.launches;
     g_profile.family = -1;
+    ++g_profile.generation;
     return true;
 }
 

@@ -27,6 +27,9 @@ enum KernelFamily : int {
     kFamColumn,          // column radiation
     kFamPersistent,      // the persistent cooperative solve (one launch per solve)
     kFamSmoothCoarse,    // Jacobi sweeps of the coarse levels
+    kFamResidualCoarse,  // V-cycle residual of the coarse levels
+    kFamRestrictCoarse,  // restriction onto a level below the first coarse one
+    kFamProlongCoarse,   // prolongation onto a coarse level
     kFamCount
 };
 
@@ -47,10 +50,11 @@ bool profile_active();
 void set_capturing(bool on);
 void count_graph_kernels(std::uint64_t kernels);
 
-// Device counter of the algorithmic bytes that the Jacobi sweeps of multigrid level `level`
-// move, while a profile of their family records (null otherwise); allocated on the first
-// profile_begin.
-unsigned long long* profile_bytes_counter(int level);
+// Device counter of the algorithmic bytes that the kernels of `family` move (each vector a
+// kernel touches counted once per active row), while a profile of that family records;
+// null otherwise. Allocated on the first profile_begin. Launchers pass it in the views of
+// their launches.
+unsigned long long* profile_bytes_for(int family);
 std::uint64_t profile_bytes_exchange();
 
 bool profile_begin(int family);

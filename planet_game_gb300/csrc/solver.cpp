@@ -458,14 +458,14 @@ template <typename T>
 static LevelView<T> make_view(const BatchLevel& L, const T* vd, const T* inv, std::size_t level) {
     return LevelView<T>{L.rows,         L.width,        L.tiles,      L.col,
                         vd,             inv,            L.tile_inst,  L.tile_rows,
-                        L.tile_sweep,   L.tile_meta,    profile_bytes_counter(static_cast<int>(level)),
+                        L.tile_sweep,   L.tile_meta,    nullptr,
                         L.sets_stencil, L.sets_vector,  static_cast<std::uint8_t>(level)};
 }
 
 StepView step_view(const Batch& b) {
     const BatchLevel& F = b.levels[0];
     return StepView{F.rows, F.tiles, b.instances, F.tile_inst, F.tile_rows, b.tile_begin, F.col, b.w, b.area,
-                    b.conductance, b.step_edge_conductance, b.slope_of};
+                    b.conductance, b.step_edge_conductance, b.slope_of, profile_bytes_for(kFamStep)};
 }
 
 LevelView<double> view64(const Batch& b, std::size_t level) {
@@ -530,6 +530,7 @@ TailArgs<T> tail_args(Batch& b, int gate) {
     if (depth > static_cast<std::size_t>(kMaxLevels)) throw std::logic_error("coarse tail: hierarchy deeper than 12 levels");
     for (std::size_t l = 0; l < depth; ++l) {
         a.level[l] = level_of<T>(b, l);
+        a.level[l].view.bytes = profile_bytes_for(kFamSmoothCoarse);
         a.pre[l] = b.smoother.pre_at(l);
         a.post[l] = b.smoother.post_at(l);
         a.inner[l] = b.smoother.inner_at(l);
@@ -808,6 +809,7 @@ PersistentArgs<T> persistent_args(Batch& b, const SolveOptions& opt, const doubl
         a.level[l] = level_of<T>(b, l);
         a.dense_at[l] = b.dense_at[l] ? 1 : 0;
     }
+    for (std::size_t l = 0; l < b.levels.size(); ++l) a.level[l].view.bytes = profile_bytes_for(kFamPersistent);
     a.dense = dense_view(b);
     a.dense_inv = Pick<T>::inv(b.dense);
     a.dense_blocks = b.dense.d_blocks;

@@ -369,14 +369,17 @@ class NativeServer:
 
 class OneAtATime:
     """The comparator: requests in arrival order, one at a time, plain FP64, each planet
-    solved alone through the single-planet entry point."""
+    solved alone. `tuned` (default): each planet in a one-planet batch with the launch
+    shapes and sweeps autotuned once per mesh level (api.TunedSolo), as the batched lanes
+    are tuned; otherwise the single-planet entry point with the untuned defaults."""
 
-    def __init__(self, population, device=None, **solver):
+    def __init__(self, population, device=None, tuned: bool = True, **solver):
         import torch
 
         self.population = population
         self.device = device or torch.device("cuda", 0)
         self.options = {"method": "bicgstab", **solver, "precision": "fp64"}
+        self.solo = api.TunedSolo(**self.options) if tuned else None
 
     def run_trace(self, requests: list[ServedRequest], realtime: bool = True):
         import torch
@@ -389,8 +392,12 @@ class OneAtATime:
                     time.sleep(delay)
             p = self.population[r.level][r.planet]
             src = torch.from_numpy(r.source).to(self.device)
-            out, _, rep = api.transport_step(p.mesh, p.state, src, p.heat_capacity, p.dt, p.conductance,
-                                             edge_conductance=p.edge_conductance, **self.options)
+            if self.solo is not None:
+                out, rep = self.solo.step(p.mesh, p.state, src, p.heat_capacity, p.dt, p.conductance,
+                                          edge_conductance=p.edge_conductance)
+            else:
+                out, _, rep = api.transport_step(p.mesh, p.state, src, p.heat_capacity, p.dt, p.conductance,
+                                                 edge_conductance=p.edge_conductance, **self.options)
             p.state = out
             r.result = out.cpu().numpy()
             r.status = rep.status

@@ -62,10 +62,16 @@ class StepInputs:
 
 def step_inputs(mesh, seed: int, edge_diffusivity: np.ndarray | None = None) -> StepInputs:
     """Inputs of one sub-step on `mesh` (a planet_game_gb300 PlanetMesh)."""
+    return step_inputs_from(mesh.arrays()["center"], mesh.substep_mean_insolation(0), seed, edge_diffusivity)
+
+
+def step_inputs_from(center: np.ndarray, insolation: np.ndarray, seed: int,
+                     edge_diffusivity: np.ndarray | None = None) -> StepInputs:
+    """The same from the cells' unit centres and the sub-step-0 mean insolation (any mesh
+    builder that gives the reference's mesh gives the same inputs)."""
     rng = np.random.default_rng(seed)
-    a = mesh.arrays()
-    t0 = initial_temperature(a["center"], rng)
-    s = source_term(mesh.substep_mean_insolation(0), t0)
+    t0 = initial_temperature(center, rng)
+    s = source_term(insolation, t0)
     g = None if edge_diffusivity is None else HEAT_CAPACITY * edge_diffusivity
     return StepInputs(t0, s, HEAT_CAPACITY, SUBSTEP_S, HEAT_CAPACITY * DIFFUSIVITY, g)
 

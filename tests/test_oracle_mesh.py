@@ -42,3 +42,12 @@ def test_oracle_mesh_is_the_product_mesh_at_another_radius(meshes):
     b = meshes(4, 4.2e6).arrays()
     for key in a:
         assert np.array_equal(a[key], b[key]), key
+
+
+def test_oracle_insolation_is_the_reference_one():
+    from oracle import oracle as O
+
+    ref = golden("insolation_L4.npz")
+    mine = O.substep_mean_insolation(O.icosphere(4, 6.371e6)["center"], ref["nodes"])
+    assert mine.dtype == ref["insolation"].dtype
+    assert np.array_equal(mine, ref["insolation"])

@@ -1,6 +1,7 @@
 """The continuous-batching request loop: every served result equals the same step run
-alone (bit for bit: planets never influence each other in a batch), lanes overlap, and
-HBM-budget admission evicts idle lanes without losing requests."""
+alone (bit for bit: planets never influence each other in a batch) and the oracle's solve
+of the same step, lanes overlap, and HBM-budget admission evicts idle lanes without losing
+requests."""
 import numpy as np
 import pytest
 
@@ -37,6 +38,33 @@ def test_served_results_equal_the_same_step_alone(population):
         assert np.array_equal(alone, r.result)
     s = serve.summarize(reqs)
     assert s["ok"] == len(reqs) and s["p99_ms"] >= s["p50_ms"] > 0
+
+
+def test_served_results_against_the_oracle(population):
+    """Every result of a short trace through the tuned lanes against the oracle (the
+    reference's FP64 PCG + SGS V-cycle solve, restated) from the same state and source."""
+    from oracle import oracle as O
+    from planet_game_gb300 import serve
+    from planet_game_gb300 import workloads as W
+
+    trace = W.poisson_trace(40, 2000.0, seed=31, weights=((4, .4), (5, .4), (6, .2)), planets_per_level=3)
+    reqs = serve.make_requests(trace, population, seed=32)
+    srv = serve.Server(population, precision="mixed", keep_inputs=True)
+    try:
+        srv.run_trace(reqs, realtime=True)
+    finally:
+        srv.close()
+    assert all(r.status == 0 for r in reqs)
+    oracles = {}
+    for r in reqs:
+        p = population[r.level][r.planet]
+        if (r.level, r.planet) not in oracles:
+            om = O.OracleMesh(p.mesh.arrays())
+            oracles[(r.level, r.planet)] = (om, O.OracleHierarchy(om))
+        om, h = oracles[(r.level, r.planet)]
+        ref = h.transport_step(0.0, p.heat_capacity, p.dt, r.t_in, r.source, tol=1e-13,
+                               edge_g=om.directed_conductance(p.edge_conductance))
+        assert np.max(np.abs(r.result - ref["t_new"])) <= 2e-6
 
 
 def test_tuned_lanes_equal_the_planet_alone_with_the_lane_tuning(population):

@@ -150,6 +150,27 @@ def test_per_edge_conductance_matches_oracle(meshes):
     assert np.max(np.abs(t_new - ref["t_new"])) <= 2e-6
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_l7_planet_with_per_edge_conductance_against_the_oracle(meshes, precision):
+    """The largest planets of the batched workload: an L7 mesh (163,842 cells) with per-edge
+    lognormal diffusivity, against the oracle's FP64 PCG + SGS solve of the same inputs."""
+    import planet_game_gb300 as pg
+    from planet_game_gb300 import workloads as W
+
+    m = meshes(7, 5.3e6)
+    kappa = W.lognormal_edge_diffusivity(m.edge_count, seed=77)
+    inp = W.step_inputs(m, seed=78, edge_diffusivity=kappa)
+    t_new, H, rep = pg.transport_step(m, inp.t0, inp.source, inp.heat_capacity, inp.dt,
+                                      edge_conductance=inp.edge_conductance, precision=precision)
+    assert rep.status == 0 and rep.relative_residual <= 1e-10 and rep.closure <= 1e-12
+    assert abs(rep.sum_W) <= 1e-13 * rep.absolute_sum_W
+    om = O.OracleMesh(m.arrays())
+    ref = O.OracleHierarchy(om).transport_step(0.0, inp.heat_capacity, inp.dt, inp.t0, inp.source, tol=1e-13,
+                                               edge_g=om.directed_conductance(inp.edge_conductance))
+    assert np.max(np.abs(t_new - ref["t_new"])) <= 2e-6
+    assert np.max(np.abs(H - ref["transport"])) <= 2e-6 * inp.heat_capacity / inp.dt
+
+
 def test_batch_equals_solo_bit_for_bit(meshes):
     """Each result is the same alone and in the mix (uneven levels, radii, conductances)."""
     import planet_game_gb300 as pg
