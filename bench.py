@@ -752,7 +752,10 @@ def run_next(args, rank, local_rank):
 
 # ---- config 1: operators, L6 solve, column radiation ---------------------------------------------
 
-def _event_median_us(fn, flush, reps: int = 7) -> float:
+OPS_REPS = 7
+
+
+def _event_median_us(fn, flush, reps: int | None = None) -> float:
     """Median device time of fn() in microseconds, CUDA events on the current stream, the
     L2 flushed (a write of a buffer larger than L2) before every timed launch."""
     import torch
@@ -760,7 +763,7 @@ def _event_median_us(fn, flush, reps: int = 7) -> float:
     stream = torch.cuda.current_stream()
     fn()
     times = []
-    for _ in range(reps):
+    for _ in range(reps or OPS_REPS):
         flush.zero_()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
@@ -779,6 +782,37 @@ def operator_bytes(a: dict) -> dict:
     edge its flux and length (16 B, E/N of them per cell)."""
     n, e = len(a["area_m2"]), len(a["edge_length_m"])
     return {"laplacian": 96.0, "gradient": 177.0, "divergence": 42.0 + 16.0 * e / n}
+
+
+def column_point(args, m, flush, peak, dev) -> dict:
+    """Column radiation over 10 layers (1000 -> 100 hPa) for every cell of `m`: time,
+    algorithmic GB/s ((7N + 7) x 8 B a column at N = 10), error against the oracle's N-layer
+    restatement and the oracle's one-core time."""
+    import torch
+
+    import planet_game_gb300 as pg
+    from oracle import oracle as O
+    from planet_game_gb300 import workloads as W
+
+    inp = W.step_inputs(m, args.seed)
+    col = W.column_profiles(inp.t0, 10, seed=args.seed)
+    k = pg.column_constants(**W.EARTH_COLUMN)
+    ins = [torch.from_numpy(np.ascontiguousarray(v)).to(dev) for v in
+           (col.temperature, col.humidity, col.cloud_water, col.surface_temperature, col.surface_pressure)]
+    res = {}
+    us = _event_median_us(lambda: res.update(o=pg.column_radiation(k, *ins)), flush)
+    n = m.cell_count
+    per_cell = (7 * 10 + 7) * 8.0
+    gbs = per_cell * n / (us * 1e-6) / 1e9
+    got = [o.cpu().numpy() for o in res["o"]]
+    t = time.perf_counter()
+    ref = O.column_radiation(W.column_constant_vector(), col.temperature, col.humidity, col.cloud_water,
+                             col.surface_temperature, col.surface_pressure)
+    cpu_s = time.perf_counter() - t
+    rel = max(float(np.max(np.abs(g - r_) / np.maximum(np.abs(r_), 1e-300))) for g, r_ in zip(got, ref))
+    return {"cells": n, "layers": 10, "us": us, "bytes_per_cell": per_cell, "achieved_GBs": gbs,
+            "frac": gbs / peak, "max_rel_vs_oracle": rel,
+            "cpu_baseline": {"seconds": cpu_s, "cores": 1, "kind": "port"}, "gpu_over_cpu": cpu_s / (us * 1e-6)}
 
 
 def run_ops(args, rank, local_rank):
@@ -810,7 +844,7 @@ def run_ops(args, rank, local_rank):
     def rel_l2(x, y, w):
         return float(np.sqrt(np.sum(w * (x - y) ** 2) / np.sum(w * y ** 2)))
 
-    for level in (6, 8):
+    for level in args.ops_levels:
         m = pg.make_icosphere(level, R)
         a = m.arrays()
         om = O.OracleMesh(a)
@@ -857,6 +891,11 @@ def run_ops(args, rank, local_rank):
             res["gpu_over_cpu"] = cpu_s / (gpu_us * 1e-6)
         out[f"operators_L{level}"] = res
 
+        # column radiation over 10 layers for every cell of this level
+        out[f"column_L{level}"] = column_point(args, m, flush, peak, dev)
+    if 6 not in args.ops_levels:
+        print(json.dumps(out))
+        return
     # the config-0 solve on L6, plain FP64, one planet per call (tuned)
     m = pg.make_icosphere(6, R)
     inp = W.step_inputs(m, args.seed)
@@ -878,33 +917,98 @@ def run_ops(args, rank, local_rank):
                        "cpu_baseline": {"seconds": cpu_s, "cores": 1, "kind": "port", "pcg_iterations": base["iterations"]},
                        "gpu_over_cpu": cpu_s / (ms * 1e-3)}
 
-    # column radiation over 10 layers for every L6 cell
-    col = W.column_profiles(inp.t0, 10, seed=args.seed)
-    k = pg.column_constants(**W.EARTH_COLUMN)
-    ins = [torch.from_numpy(np.ascontiguousarray(v)).to(dev) for v in
-           (col.temperature, col.humidity, col.cloud_water, col.surface_temperature, col.surface_pressure)]
-    res = {}
-    us = _event_median_us(lambda: res.update(o=pg.column_radiation(k, *ins)), flush)
-    n = m.cell_count
-    per_cell = (7 * 10 + 7) * 8.0
-    gbs = per_cell * n / (us * 1e-6) / 1e9
-    got = [o.cpu().numpy() for o in res["o"]]
-    t = time.perf_counter()
-    ref = O.column_radiation(W.column_constant_vector(), col.temperature, col.humidity, col.cloud_water,
-                             col.surface_temperature, col.surface_pressure)
-    cpu_s = time.perf_counter() - t
-    rel = max(float(np.max(np.abs(g - r_) / np.maximum(np.abs(r_), 1e-300))) for g, r_ in zip(got, ref))
-    out["column_L6"] = {"cells": n, "layers": 10, "us": us, "bytes_per_cell": per_cell, "achieved_GBs": gbs,
-                        "frac": gbs / peak, "max_rel_vs_oracle": rel,
-                        "cpu_baseline": {"seconds": cpu_s, "cores": 1, "kind": "port"},
-                        "gpu_over_cpu": cpu_s / (us * 1e-6)}
     print(json.dumps(out))
 
 
 # ---- config 2: one L8 planet, 32 right-hand sides --------------------------------------------------
 
 def run_l8rhs(args, rank, local_rank):
-    raise SystemExit("the multi-RHS block solve is not built yet")
+    """One L8 planet (655,362 cells), 32 sub-steps with sources S_j = S + N(0, 5^2) W/m^2,
+    solved as one block (psgb_transport_step_multi: every sweep reads the matrix once for
+    all 32) in plain FP64 (variant A) and FP32 inner + FP64 refinement (variant B), beside
+    the same 32 sub-steps one per call through the plain FP64 drop-in; each sub-step's error
+    against the FP64 CPU oracle (PCG + SGS V-cycle to 1e-13, all host cores), refinement
+    counts and inner iterations, the block's fine-level sweep bytes per second."""
+    import ctypes as C
+
+    import torch
+
+    import planet_game_gb300 as pg
+    from oracle import oracle as O
+    from planet_game_gb300 import capi
+    from planet_game_gb300 import workloads as W
+
+    if rank != 0:
+        return
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    rhs = 32
+    m = pg.make_icosphere(8, W.EARTH_RADIUS)
+    inp = W.step_inputs(m, args.seed)
+    sources = W.perturbed_sources(inp.source, rhs, seed=args.seed + 1)
+    t0 = torch.from_numpy(inp.t0).to(dev)
+    src = [torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in sources]
+    lib = capi.load()
+    peak, peak_kind = peaks()
+    out = {"metric": "sub-steps/s of 32 sub-steps of one L8 planet at 1e-10 relative residual", "unit": "sub-steps/s",
+           "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "data": "synthetic", "higher_is_better": True,
+           "config": {"workload": "one L8 planet (655,362 cells), 32 right-hand sides S + N(0, 5^2) W/m^2",
+                      "cells": m.cell_count, "rhs": rhs, "tolerance": 1e-10, "krylov": "BiCGSTAB",
+                      "smoother": "damped Jacobi 2+2, omega 0.8 (untuned)"}}
+    results = {}
+    for name, precision in (("A_fp64", "fp64"), ("B_mixed", "mixed")):
+        step = lambda: pg.transport_step_multi(m, t0, src, inp.heat_capacity, inp.dt, inp.conductance,
+                                               precision=precision, **SOLVER)
+        for _ in range(args.warmup):
+            t_new, _, reps = step()
+        stream = torch.cuda.current_stream()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(args.steps):
+            t_new, _, reps = step()
+        b.record(stream)
+        torch.cuda.synchronize()
+        sec = a.elapsed_time(b) / 1e3
+        ms, nl, nbytes = C.c_double(), C.c_uint64(), C.c_uint64()
+        capi.check(lib.psgb_profile_begin(b"smooth"))
+        step()
+        capi.check(lib.psgb_profile_end(C.byref(ms), C.byref(nl), C.byref(nbytes)))
+        achieved = nbytes.value / (ms.value / 1e3) / 1e9 if ms.value > 0 else None
+        results[name] = [x.cpu().numpy() for x in t_new]
+        out[name] = {"value": rhs * args.steps / sec, "ms_per_block": sec * 1e3 / args.steps,
+                     "refinements": sorted({r.refinements for r in reps}),
+                     "inner_iterations": {"min": min(r.iterations for r in reps), "max": max(r.iterations for r in reps)},
+                     "max_relative_residual": max(r.relative_residual for r in reps),
+                     "max_closure": max(r.closure for r in reps), "status_ok": all(r.status == 0 for r in reps),
+                     "roofline_fine_sweeps": {"bound": "hbm", "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
+                                              "unit": "GB/s", "frac": achieved / peak if achieved else None,
+                                              "launches": int(nl.value), "bytes_per_launch": nbytes.value / max(1, nl.value),
+                                              "bytes": "matrix and indices once per row, the 32 right-hand sides' vectors"}}
+    # the same 32 sub-steps one per call through the plain FP64 drop-in
+    for _ in range(2):
+        pg.transport_step(m, t0, src[0], inp.heat_capacity, inp.dt, inp.conductance, precision="fp64", **SOLVER)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for j in range(rhs):
+        pg.transport_step(m, t0, src[j], inp.heat_capacity, inp.dt, inp.conductance, precision="fp64", **SOLVER)
+    torch.cuda.synchronize()
+    out["one_at_a_time_fp64"] = {"value": rhs / (time.perf_counter() - t), "unit": "sub-steps/s"}
+    out["value"] = out["B_mixed"]["value"]
+    out["speedup_block_mixed_vs_one_at_a_time"] = out["B_mixed"]["value"] / out["one_at_a_time_fp64"]["value"]
+    out["speedup_block_fp64_vs_one_at_a_time"] = out["A_fp64"]["value"] / out["one_at_a_time_fp64"]["value"]
+    if not args.skip_cpu:
+        t = time.perf_counter()
+        refs = O.transport_steps(m.arrays(), inp.conductance, inp.heat_capacity, inp.dt, [inp.t0] * rhs,
+                                 [np.ascontiguousarray(x) for x in sources], tol=1e-13)
+        cpu_s = time.perf_counter() - t
+        for name in ("A_fp64", "B_mixed"):
+            errs = [float(np.max(np.abs(results[name][j] - refs[j][0]))) for j in range(rhs)]
+            out[name]["oracle_error"] = {"max_abs_T_K": max(errs), "per_rhs_max_abs_T_K": errs}
+        out["cpu_baseline"] = {"value": rhs / cpu_s, "unit": "sub-steps/s", "cores": os.cpu_count(), "kind": "port",
+                               "sample": "the 32 sub-steps by the oracle (FP64 PCG + SGS V-cycle) to 1e-13, one "
+                                         "process per core", "pcg_iterations": [r[2] for r in refs]}
+    print(json.dumps(out))
 
 
 # ---- CPU baseline and the reference arm ------------------------------------------------------
@@ -1012,6 +1116,9 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=["batch", "l8", "l8rhs", "ops", "serve", "next"], default="batch")
     ap.add_argument("--serve-requests", type=int, default=2000, help="requests per offered rate (fewer at 50/s)")
+    ap.add_argument("--ops-levels", type=int, nargs="+", default=[6, 8],
+                    help="ops workload: mesh levels of the operator and column timings (the L6 solve runs with 6)")
+    ap.add_argument("--ops-reps", type=int, default=7, help="ops workload: timed launches per kernel (median)")
     ap.add_argument("--skip-serve", action="store_true")
     ap.add_argument("--native-serve", action="store_true",
                     help="serving: also run the trace through the library's own loop (psgb_server_*)")
@@ -1041,6 +1148,8 @@ def main():
         run_next(args, rank, local_rank)
         return
     if args.workload == "ops":
+        global OPS_REPS
+        OPS_REPS = args.ops_reps
         run_ops(args, rank, local_rank)
         return
     if args.workload == "l8rhs":

@@ -260,6 +260,23 @@ int psgb_transport_step_noalloc(psgb_planet* planet, const psgb_step_params* par
                                 const double* source_W_m2, double* t_new_K, double* transport_W_m2,
                                 psgb_step_report* report, void* stream);
 
+/* Up to 32 sub-steps of ONE planet with the same parameters (C, dt, conductances),
+ * solved together as one block: replaces `count` calls of solve_implicit_transport
+ * (heat_transport.cpp:595-772) that share the planet's matrix and differ in their
+ * states and sources (ensembles, perturbed sources). The vectors of all sub-steps are
+ * interleaved so that every sweep reads the matrix and its column indices once for all
+ * of them. Sub-step j takes t0_K[j] and source_W_m2[j] and writes t_new_K[j] (and
+ * transport_W_m2[j] when that array and its entry are not NULL) and reports[j]; each
+ * equals psgb_transport_step of that sub-step alone bit for bit (untuned, or under the
+ * same tuning without block-local sweeps, which the block solve does not apply).
+ * BiCGSTAB only; per-edge conductance as an array (not stored). HOST or DEVICE arrays
+ * per `memory`; returns the first failing sub-step's status. */
+int psgb_transport_step_multi(psgb_planet* planet, const psgb_step_params* params,
+                              const psgb_solve_options* options, uint32_t count, const double* const* t0_K,
+                              const double* const* source_W_m2, double* const* t_new_K,
+                              double* const* transport_W_m2, psgb_step_report* reports, int memory,
+                              void* stream);
+
 /* ---- batches: many planets of uneven levels solved together -------------------
  * Concatenated block layout (each planet padded to 256-row tiles), per-planet
  * convergence masks, one stream of launches for all planets. */

@@ -356,3 +356,41 @@ def solve_implicit_advection_diffusion(om: "OracleMesh", layers, conductance, ou
                                                  _p(keep[6]), cg_tolerance, newton_tolerance, _p(src), _p(mean),
                                                  _p(energy), _p(stats))
     return src, mean, energy, stats
+
+
+# ---- many sub-steps of one planet, spread over the host cores -----------------------------
+
+_WORKER: dict = {}
+_GRAPH_KEYS = ("area_m2", "edge_offset", "edge_count", "neighbor", "edge", "normal_east", "normal_north",
+               "edge_first", "edge_length_m", "edge_distance_m", "graph_weight", "graph_weight_sum", "graph_area_m2")
+
+
+def _worker_init(path, K, C_heat, dt, edge_g):
+    z = np.load(path)
+    om = OracleMesh({k: z[k] for k in z.files})
+    _WORKER.update(om=om, h=OracleHierarchy(om), K=K, C=C_heat, dt=dt,
+                   g=None if edge_g is None else om.directed_conductance(edge_g))
+
+
+def _worker_step(job):
+    t0, src, tol = job
+    w = _WORKER
+    r = w["h"].transport_step(w["K"], w["C"], w["dt"], t0, src, tol=tol, edge_g=w["g"])
+    return r["t_new"], r["transport"], r["iterations"]
+
+
+def transport_steps(arrays: dict, K, C_heat, dt, t0s, sources, tol=1e-13, edge_g=None, processes=None):
+    """Sub-steps (t0s[j], sources[j]) of one planet by the oracle, each process of a spawned
+    pool holding the planet's hierarchy: [(t_new, transport, iterations)] in order."""
+    import multiprocessing as mp
+    import os
+    import tempfile
+
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "graph.npz")
+        a = dict(arrays)
+        a.setdefault("graph_area_m2", a["area_m2"])
+        np.savez(path, **{k: a[k] for k in _GRAPH_KEYS})
+        n = processes or max(1, min(len(sources), os.cpu_count() or 1))
+        with mp.get_context("spawn").Pool(n, initializer=_worker_init, initargs=(path, K, C_heat, dt, edge_g)) as pool:
+            return pool.map(_worker_step, [(t0s[j], sources[j], tol) for j in range(len(sources))], chunksize=1)

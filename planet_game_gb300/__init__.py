@@ -30,6 +30,7 @@ from .api import (  # noqa: F401
     solve_options,
     transport_settings,
     transport_step,
+    transport_step_multi,
 )
 from .capi import GB300Error  # noqa: F401
 from .nonsym import (  # noqa: F401

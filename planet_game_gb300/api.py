@@ -566,6 +566,34 @@ def transport_step(mesh: PlanetMesh, t0_K, source_W_m2, heat_capacity_J_m2_K: fl
     return t_new, h, _step_result(rep)
 
 
+def transport_step_multi(mesh: PlanetMesh, t0_K, sources_W_m2, heat_capacity_J_m2_K: float, dt_s: float,
+                         conductance_W_K: float = 0.0, edge_conductance=None, transport=False, **options):
+    """Up to 32 sub-steps of one planet with the same parameters, solved as one block
+    (psgb_transport_step_multi): `t0_K` one state for every sub-step or a list of them,
+    `sources_W_m2` a list of sources (numpy or CUDA tensors). Returns the new states (a
+    list), the transports (a list, or None unless `transport`) and the reports; each
+    sub-step's result equals transport_step of that sub-step alone bit for bit."""
+    count = len(sources_W_m2)
+    if not 1 <= count <= 32:
+        raise ValueError("a block holds 1 to 32 sub-steps")
+    t0s = list(t0_K) if isinstance(t0_K, (list, tuple)) else [t0_K] * count
+    if len(t0s) != count:
+        raise ValueError("one initial state, or one per sub-step")
+    outs = [_empty_like(t0s[j], (mesh.cell_count,)) for j in range(count)]
+    hs = [_empty_like(t0s[j], (mesh.cell_count,)) for j in range(count)] if transport else None
+    params = step_params(heat_capacity_J_m2_K, dt_s, conductance_W_K, edge_conductance)
+    o = solve_options(**options)
+    mem, st = _memory_of(*t0s, *sources_W_m2, *outs)
+    arrs = lambda xs: (C.c_void_p * count)(*[_ptr(x).value for x in xs])
+    reps = (capi.StepReport * count)()
+    code = capi.load().psgb_transport_step_multi(mesh.handle, C.byref(params), C.byref(o), count, arrs(t0s),
+                                                 arrs(sources_W_m2), arrs(outs), arrs(hs) if hs else None, reps,
+                                                 mem, st)
+    if code not in (capi.OK, capi.ERR_NOT_CONVERGED, capi.ERR_BREAKDOWN):
+        _raise(code)
+    return outs, hs, [_step_result(r) for r in reps]
+
+
 def transport_step_noalloc(mesh: PlanetMesh, t0_K, source_W_m2, heat_capacity_J_m2_K: float, dt_s: float,
                            conductance_W_K: float = 0.0, edge_conductance=None, **options):
     """The transport step through the entry point that allocates nothing (CUDA tensors

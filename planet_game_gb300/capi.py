@@ -179,6 +179,9 @@ _SIGNATURES = {
                                       C.POINTER(StepReport), C.c_int, P]),
     "psgb_transport_step_noalloc": (C.c_int, [P, C.POINTER(StepParams), C.POINTER(SolveOptions), P, P, P, P,
                                               C.POINTER(StepReport), P]),
+    "psgb_transport_step_multi": (C.c_int, [P, C.POINTER(StepParams), C.POINTER(SolveOptions), C.c_uint32,
+                                            C.POINTER(P), C.POINTER(P), C.POINTER(P), C.POINTER(P),
+                                            C.POINTER(StepReport), C.c_int, P]),
     "psgb_batch_create": (C.c_int, [C.POINTER(P), C.c_uint32, C.POINTER(P)]),
     "psgb_batch_destroy": (None, [P]),
     "psgb_batch_set_reassembly": (C.c_int, [P, C.c_int]),

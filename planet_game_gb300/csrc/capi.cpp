@@ -720,6 +720,78 @@ int psgb_transport_step(psgb_planet* h, const psgb_step_params* params, const ps
     });
 }
 
+int psgb_transport_step_multi(psgb_planet* h, const psgb_step_params* params, const psgb_solve_options* options,
+                              uint32_t count, const double* const* t0_K, const double* const* source_W_m2,
+                              double* const* t_new_K, double* const* transport_W_m2, psgb_step_report* reports,
+                              int memory, void* stream) {
+    return guarded([&] {
+        require(h != nullptr && params != nullptr && t0_K != nullptr && source_W_m2 != nullptr && t_new_K != nullptr,
+                "null argument");
+        require(count >= 1 && count <= static_cast<uint32_t>(psgb::mr::kRhs),
+                "a block holds 1 to 32 right-hand sides");
+        require_memory(memory);
+        require(!params->edge_conductance_stored, "the block step takes per-edge conductances as an array");
+        for (uint32_t j = 0; j < count; ++j) {
+            require(t0_K[j] != nullptr && source_W_m2[j] != nullptr && t_new_K[j] != nullptr, "null array in the block");
+        }
+        const psgb::SolveOptions opt = to_options(options);
+        require(opt.method == psgb::kBiCGSTAB, "the multi-right-hand-side block solve runs BiCGSTAB");
+        psgb::Batch& b = solo(h);
+        apply_smoother(b, options);
+        cudaStream_t st = as_stream(stream);
+        assemble_step_matrix(b, params, st);
+        if (!h->multi) h->multi = std::make_unique<psgb::mr::Space>();
+        psgb::mr::Space& sp = *h->multi;
+        psgb::mr::prepare(b, sp, opt);
+        const std::uint32_t n = static_cast<std::uint32_t>(h->planet->mesh.cells);
+        const std::uint32_t P0 = b.levels[0].rows;
+        // the sub-steps' T0 and S on the device: the caller's arrays, or staged host copies
+        std::vector<const double*> in(2 * psgb::mr::kRhs, nullptr);
+        if (memory == PSGB_MEMORY_HOST) {
+            while (h->multi_stage.size() < 2 * count) h->multi_stage.push_back(sp.store.alloc<double>(P0));
+            for (uint32_t j = 0; j < count; ++j) {
+                copy_in(h->multi_stage[2 * j], t0_K[j], n * 8, memory, st);
+                copy_in(h->multi_stage[2 * j + 1], source_W_m2[j], n * 8, memory, st);
+                in[j] = h->multi_stage[2 * j];
+                in[psgb::mr::kRhs + j] = h->multi_stage[2 * j + 1];
+            }
+        } else {
+            for (uint32_t j = 0; j < count; ++j) {
+                in[j] = t0_K[j];
+                in[psgb::mr::kRhs + j] = source_W_m2[j];
+            }
+        }
+        PSGB_CUDA(cudaMemcpyAsync(sp.pointers, in.data(), in.size() * sizeof(const double*), cudaMemcpyHostToDevice, st));
+        psgb::mr::load(n, P0, static_cast<int>(count), sp.pointers, sp.pointers + psgb::mr::kRhs, b.area,
+                       params->dt_s / params->heat_capacity_J_m2_K, sp.bb, sp.xr, st);
+        psgb::mr::solve(b, sp, opt, st);
+        // the flux form of every solved temperature, with the single step's kernels
+        const psgb::StepView v = psgb::step_view(b);
+        int worst = PSGB_OK;
+        for (uint32_t j = 0; j < count; ++j) {
+            psgb::mr::take(P0, static_cast<int>(j), sp.xr, b.xr, st);
+            psgb::launch_step_finish(v, b.xr, in[j], in[psgb::mr::kRhs + j], b.hout, b.tnew, b.partial, b.sums, st);
+            copy_out(t_new_K[j], b.tnew, n * 8, memory, st);
+            if (transport_W_m2 != nullptr && transport_W_m2[j] != nullptr) {
+                copy_out(transport_W_m2[j], b.hout, n * 8, memory, st);
+            }
+            double sums[8];
+            PSGB_CUDA(cudaMemcpyAsync(sums, b.sums, sizeof(sums), cudaMemcpyDeviceToHost, st));
+            PSGB_CUDA(cudaStreamSynchronize(st));
+            psgb_step_report local;
+            fill_report(sp.host[j], &local.solve);
+            local.sum_W = sums[0];
+            local.absolute_sum_W = sums[1];
+            local.dissipation_W_K = sums[2];
+            local.closure = sums[4] > 0.0 ? std::fabs(sums[5] - sums[3]) / sums[4] : std::fabs(sums[5] - sums[3]);
+            if (reports != nullptr) reports[j] = local;
+            if (local.solve.status != PSGB_OK && worst == PSGB_OK) worst = local.solve.status;
+        }
+        if (worst != PSGB_OK) g_last_error = status_message(worst);
+        return worst;
+    });
+}
+
 int psgb_batch_create(psgb_planet* const* planets, uint32_t count, psgb_batch** out) {
     return guarded([&] {
         require(planets != nullptr && out != nullptr && count > 0, "a batch needs planets");

@@ -2,6 +2,7 @@
 #pragma once
 
 #include "../../include/planetsim_gb300.h"
+#include "multirhs.hpp"
 #include "solver.hpp"
 
 #include <cstdint>
@@ -54,6 +55,9 @@ struct psgb_planet {
     std::vector<double*> newton;
     psgb::PinnedDoubles newton_pinned;
     std::shared_ptr<psgb::NonsymContext> nonsym;
+    // the multi-right-hand-side block solve's workspace and host-input staging
+    std::unique_ptr<psgb::mr::Space> multi;
+    std::vector<double*> multi_stage;
 };
 
 struct psgb_batch {

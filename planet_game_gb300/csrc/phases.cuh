@@ -177,6 +177,11 @@ __device__ __forceinline__ bool gate_open(const InstanceScalars* sc, int inst, i
 
 __device__ __forceinline__ bool running(const InstanceScalars& s) { return s.status == kRunning; }
 
+// A dot-product term, rounded on its own (never fused into the reduction's first add), so
+// that every layout that sums the same terms in the same tree gets the same bits.
+__device__ __forceinline__ float prod(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double prod(double a, double b) { return __dmul_rn(a, b); }
+
 __device__ __forceinline__ bool finite(double v) { return isfinite(v); }
 
 // Release/acquire fence at GPU scope: orders this thread's partial stores before its
@@ -759,7 +764,7 @@ __device__ void bicg_init(const LevelView<T>& lv, int t0, int gid, int lane, con
         const int row = ts.tile[k] * kTile + lane;
         const T bv = b[row];
         x[row] = T(0); r[row] = bv; shadow[row] = bv; p[row] = T(0); v[row] = T(0);
-        q[k] = bv * bv;
+        q[k] = prod(bv, bv);
     }
     double out[R];
     bool fin[R];
@@ -816,7 +821,7 @@ __device__ void bicg_v(const LevelView<T>& lv, int t0, int gid, int lane, const 
 #pragma unroll
         for (int j = 0; j < W; ++j) s += lv.vd[j * P + row] * in[lv.col[j * P + row]];
         y[k] = s;
-        q[k] = shadow[row] * s;
+        q[k] = prod(shadow[row], s);
     }
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -857,7 +862,7 @@ __device__ void bicg_s(const LevelView<T>& lv, int t0, int gid, int lane, const 
         if (!on[k] || lane >= ts.rows[k]) continue;
         const int row = ts.tile[k] * kTile + lane;
         s_out[row] = sv[k];
-        q[k] = sv[k] * sv[k];
+        q[k] = prod(sv[k], sv[k]);
         if (ts.sweep[k]) xv[row] = zv[k];
     }
     double sum[R];
@@ -891,8 +896,8 @@ __device__ void bicg_t(const LevelView<T>& lv, int t0, int gid, int lane, const 
 #pragma unroll
         for (int j = 0; j < W; ++j) s += lv.vd[j * P + row] * shat[lv.col[j * P + row]];
         y[k] = s;
-        q[2 * k] = s * s;
-        q[2 * k + 1] = s * s_vec[row];
+        q[2 * k] = prod(s, s);
+        q[2 * k + 1] = prod(s, s_vec[row]);
     }
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -939,8 +944,8 @@ __device__ void bicg_x(const LevelView<T>& lv, int t0, int gid, int lane, const 
             xv[k] = x[row] + (alpha * phat[row] + omega * shat[row]);
             rv[k] = s_vec[row] - omega * t[row];
         }
-        q[2 * k] = rv[k] * rv[k];
-        q[2 * k + 1] = shadow[row] * rv[k];
+        q[2 * k] = prod(rv[k], rv[k]);
+        q[2 * k + 1] = prod(shadow[row], rv[k]);
     }
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -979,7 +984,7 @@ __device__ void pcg_init(const LevelView<T>& lv, int t0, int gid, int lane, cons
         const T bv = b[row];
         x[row] = T(0); r[row] = bv; p[row] = T(0);
         if (ts.sweep[k]) xv[row] = omega_j * lv.inv[row] * bv;
-        q[k] = bv * bv;
+        q[k] = prod(bv, bv);
     }
     double out[R];
     bool fin[R];
@@ -1004,7 +1009,7 @@ __device__ void pcg_rz(const LevelView<T>& lv, int t0, int gid, int lane, const 
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int row = ts.tile[k] * kTile + lane;
-        q[k] = (on[k] && lane < ts.rows[k]) ? r[row] * z[row] : T(0);
+        q[k] = (on[k] && lane < ts.rows[k]) ? prod(r[row], z[row]) : T(0);
     }
     double sum[R];
     bool fin[R];
@@ -1050,7 +1055,7 @@ __device__ void pcg_q(const LevelView<T>& lv, int t0, int gid, int lane, const T
 #pragma unroll
         for (int j = 0; j < W; ++j) s += lv.vd[j * P + row] * p[lv.col[j * P + row]];
         y[k] = s;
-        q[k] = p[row] * s;
+        q[k] = prod(p[row], s);
     }
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -1093,7 +1098,7 @@ __device__ void pcg_xr(const LevelView<T>& lv, int t0, int gid, int lane, const 
         const int row = ts.tile[k] * kTile + lane;
         x[row] = xn[k];
         r[row] = rn[k];
-        q[k] = rn[k] * rn[k];
+        q[k] = prod(rn[k], rn[k]);
         if (ts.sweep[k]) xv[row] = zn[k];
     }
     double sum[R];
@@ -1173,7 +1178,7 @@ __device__ void outer_residual(const LevelView<double>& lv, int t0, int gid, int
         const int row = ts.tile[k] * kTile + lane;
         r64[row] = rv[k];
         rin[row] = static_cast<TI>(rv[k]);
-        q[k] = rv[k] * rv[k];
+        q[k] = prod(rv[k], rv[k]);
     }
     double sum[R];
     bool fin[R];
