@@ -487,7 +487,8 @@ typedef struct psgb_tuning {
     int block_sweeps[PSGB_MAX_LEVELS];    /* per level: Jacobi sweeps per smoothing launch, each tile in shared
                                              memory with its neighbours in other tiles held (1..8; 1 = plain) */
     int coarse_tail_single;               /* 0: a large planet's tail runs on several co-resident blocks
-                                             (cooperative launch, per-planet barriers); 1: one block each */
+                                             (cooperative launch, per-planet barriers); 1: one block each;
+                                             2: one block each with the tail levels' vectors in shared memory */
     uint32_t coarse_tail_blocks;          /* out: blocks of the tail launch (0: no tail) */
 } psgb_tuning;
 

@@ -160,7 +160,8 @@ Tuning current_tuning(const Batch& b) {
     t.omega = b.smoother.omega;
     t.tail_level = b.tail_level;
     t.tail_spread = b.tail_spread;
-    t.tail_blocks = b.tail_level == 0 ? 0u
+    t.tail_shared = b.tail_shared;
+    t.tail_blocks = b.tail_level == 0 ? 0u : b.tail_shared ? b.instances
                     : (b.tail_spread && b.tail_cta_at[b.tail_level] != nullptr) ? b.tail_ctas_at[b.tail_level]
                                                                                  : b.instances;
     return t;
@@ -192,6 +193,7 @@ void apply_tuning(Batch& b, const Tuning& t) {
     b.smoother.omega = t.omega;
     b.tail_level = t.tail_level;
     b.tail_spread = t.tail_spread;
+    b.tail_shared = t.tail_shared;
     b.tuned = true;
 }
 
@@ -298,21 +300,29 @@ Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x,
     // depends on how many sweeps its levels run)
     set_sweeps(b, best);
     {
+        // modes: 0 spread over co-resident blocks, 1 one block per planet, 2 one block per
+        // planet with the levels' vectors in shared memory
+        const auto mode_of = [&] { return b.tail_shared ? 2 : (b.tail_spread ? 0 : 1); };
+        const auto set_mode = [&](int mode) {
+            b.tail_shared = mode == 2;
+            b.tail_spread = mode == 0;
+        };
         const int chosen = b.tail_level;
-        const bool chosen_spread = b.tail_spread;
-        int pick = chosen;
-        bool pick_spread = chosen_spread;
+        const int chosen_mode = mode_of();
+        int pick = chosen, pick_mode = chosen_mode;
+        const bool mixed = opt.precision == kMixed;
         for (int tail = 0; tail < static_cast<int>(depth); ++tail) {
-            for (bool spread : {true, false}) {
-                if ((tail == chosen && spread == chosen_spread) || (tail == 0 && !spread)) continue;
+            for (int mode : {0, 1, 2}) {
+                if ((tail == chosen && mode == chosen_mode) || (tail == 0 && mode != 0)) continue;
+                if (mode == 2 && !(mixed ? tail_fits_shared<float>(b, tail) : tail_fits_shared<double>(b, tail))) continue;
                 b.tail_level = tail;
-                b.tail_spread = spread;
+                set_mode(mode);
                 const double ms = run(best);
-                if (ms > 0.0 && ms < best_ms) { best_ms = ms; pick = tail; pick_spread = spread; }
+                if (ms > 0.0 && ms < best_ms) { best_ms = ms; pick = tail; pick_mode = mode; }
             }
         }
         b.tail_level = pick;
-        b.tail_spread = pick_spread;
+        set_mode(pick_mode);
     }
     if (best_ms < 0.0) {
         set_sweeps(b, before);
@@ -330,6 +340,7 @@ Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x,
     }
     result.tail_level = b.tail_level;
     result.tail_spread = b.tail_spread;
+    result.tail_shared = b.tail_shared;
     result.tuned_ms = best_ms;
     return result;
 }

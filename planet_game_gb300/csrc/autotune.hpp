@@ -18,6 +18,7 @@ struct Tuning {
     double omega = 0.8;
     int tail_level = 0;                            // coarse tail from this level (0: none)
     bool tail_spread = true;                       // several blocks per large planet in the tail
+    bool tail_shared = false;                      // one block per planet, the tail levels' vectors in shared memory
     unsigned tail_blocks = 0;                      // blocks of the tail launch (out; 0: no tail)
     double tuned_ms = 0.0;                         // trial solve with the chosen settings
     double default_ms = 0.0;                       // trial solve with the settings before tuning

@@ -93,16 +93,9 @@ __device__ bool planet_barrier(unsigned* barrier, unsigned* error, unsigned inst
     return stop == 0;
 }
 
+// The tail's phases for planet `inst` (block `rank` of its `size` blocks).
 template <typename T, bool Multi>
-__global__ void __launch_bounds__(1024, 1) k_coarse_tail(const __grid_constant__ TailArgs<T> a) {
-    pdl_begin();
-    int inst = static_cast<int>(blockIdx.x), rank = 0, size = 1;
-    if (Multi) {
-        const std::uint32_t w = a.cta[blockIdx.x];
-        inst = static_cast<int>(w & 0xFFFFu);
-        rank = static_cast<int>((w >> 16) & 0xFFu);
-        size = static_cast<int>(w >> 24);
-    }
+__device__ __forceinline__ void tail_body(const TailArgs<T>& a, int inst, int rank, int size) {
     const int gid = static_cast<int>(threadIdx.x >> 8), lane = static_cast<int>(threadIdx.x & 255);
     const int group = rank * ph::kGroups + gid, groups = size * ph::kGroups;
     const int coarsest = a.dense.level[inst];
@@ -193,6 +186,74 @@ __global__ void __launch_bounds__(1024, 1) k_coarse_tail(const __grid_constant__
 #undef PSGB_TAIL_SYNC
 }
 
+template <typename T, bool Multi>
+__global__ void __launch_bounds__(1024, 1) k_coarse_tail(const __grid_constant__ TailArgs<T> a) {
+    pdl_begin();
+    int inst = static_cast<int>(blockIdx.x), rank = 0, size = 1;
+    if (Multi) {
+        const std::uint32_t w = a.cta[blockIdx.x];
+        inst = static_cast<int>(w & 0xFFFFu);
+        rank = static_cast<int>((w >> 16) & 0xFFu);
+        size = static_cast<int>(w >> 24);
+    }
+    tail_body<T, Multi>(a, inst, rank, size);
+}
+
+// One block per planet with the tail levels' vectors (x, y, b, r of every level from the
+// tail level down) in shared memory: every phase's gathers, restrictions and prolongations
+// then read shared memory, and only the matrix streams from L2. The level pointers of a
+// copy of the arguments are rebased onto the planet's slices (vector[row] of a global row
+// lands in the slice), so the phases run unchanged and give the same bits. In: the tail
+// level's right-hand side and the iterate of its zero-start sweep; out: its final iterate.
+template <typename T>
+__global__ void __launch_bounds__(1024, 1) k_coarse_tail_shared(const __grid_constant__ TailArgs<T> a) {
+    pdl_begin();
+    const int inst = static_cast<int>(blockIdx.x);
+    const int coarsest = a.dense.level[inst];
+    if (coarsest < a.first || !ph::gate_open(a.sc, inst, a.gate)) return;
+    extern __shared__ __align__(16) unsigned char tail_shared_bytes[];
+    __shared__ TailArgs<T> la;
+    __shared__ unsigned total;
+    T* vec = reinterpret_cast<T*>(tail_shared_bytes);
+    if (threadIdx.x == 0) {
+        la = a;
+        std::size_t off = 0;
+        for (int l = a.first; l <= coarsest; ++l) {
+            const std::size_t base = std::size_t(a.tile_range[(l * a.instances + inst) * 2]) * kTile;
+            const std::size_t rows = std::size_t(a.tile_range[(l * a.instances + inst) * 2 + 1]) * kTile;
+            T* slice = vec + off;
+            la.level[l].x = slice - base;
+            la.level[l].y = slice + rows - base;
+            la.level[l].b = slice + 2 * rows - base;
+            la.level[l].r = slice + 3 * rows - base;
+            off += 4 * rows;
+        }
+        total = static_cast<unsigned>(off);
+    }
+    __syncthreads();
+    for (unsigned i = threadIdx.x; i < total; i += blockDim.x) vec[i] = T(0);
+    __syncthreads();
+    const int first = a.first;
+    const int t0 = static_cast<int>(a.tile_range[(first * a.instances + inst) * 2]);
+    const int nt = static_cast<int>(a.tile_range[(first * a.instances + inst) * 2 + 1]);
+    {
+        const T* gx = tail_pair(a, first).first;
+        T* sx = tail_pair(la, first).first;
+        for (int row = t0 * kTile + static_cast<int>(threadIdx.x); row < (t0 + nt) * kTile; row += blockDim.x) {
+            la.level[first].b[row] = a.level[first].b[row];
+            sx[row] = gx[row];
+        }
+    }
+    __syncthreads();
+    tail_body<T, false>(la, inst, 0, 1);
+    __syncthreads();
+    for (int t = t0; t < t0 + nt; ++t) {
+        const int rows = static_cast<int>((a.level[first].view.tile_meta[t] >> 22) & 0x1FFu);
+        const int row = t * kTile + static_cast<int>(threadIdx.x);
+        if (static_cast<int>(threadIdx.x) < rows) a.level[first].x[row] = la.level[first].x[row];
+    }
+}
+
 }  // namespace
 
 
@@ -209,8 +270,43 @@ unsigned tail_block_budget() {
     return static_cast<unsigned>(sms * std::min(per_sm, per_sm64));
 }
 
+unsigned tail_shared_max_bytes() {
+    int device = 0, optin = 0;
+    if (cudaGetDevice(&device) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess) return 0;
+    // room for the kernel's static shared memory (its argument copy and phase scratch)
+    const unsigned reserve = 16u << 10;
+    return optin > static_cast<int>(reserve) ? static_cast<unsigned>(optin) - reserve : 0u;
+}
+
 template <typename T>
 void launch_coarse_tail(const TailArgs<T>& args, cudaStream_t st) {
+    if (args.shared_rows != 0) {
+        const std::size_t bytes = std::size_t(4) * args.shared_rows * sizeof(T);
+        static const unsigned limit = tail_shared_max_bytes();
+        if (bytes > limit) throw std::logic_error("coarse tail: the levels do not fit in shared memory");
+        static bool opted = false;
+        if (!opted) {
+            PSGB_CUDA(cudaFuncSetAttribute(k_coarse_tail_shared<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(limit)));
+            opted = true;
+        }
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(args.instances);
+        cfg.blockDim = dim3(1024);
+        cfg.dynamicSmemBytes = bytes;
+        cfg.stream = st;
+        cfg.attrs = attr;
+        cfg.numAttrs = args.instances <= kPdlMaxBlocks ? 1 : 0;
+        PSGB_LAUNCH(kFamSmoothCoarse, st, {
+            const cudaError_t e = cudaLaunchKernelEx(&cfg, k_coarse_tail_shared<T>, args);
+            if (e != cudaSuccess) throw std::runtime_error(std::string("coarse tail launch: ") + cudaGetErrorString(e));
+        });
+        return;
+    }
     if (args.cta == nullptr) {
         PSGB_LAUNCH(kFamSmoothCoarse, st, launch_pdl(k_coarse_tail<T, false>, args.instances, 1024, st, args));
         return;

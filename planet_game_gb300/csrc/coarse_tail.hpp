@@ -38,10 +38,15 @@ struct TailArgs {
     unsigned ctas;
     unsigned* barrier;          // [2][instances]: arrivals, generation
     unsigned* error;            // set when a barrier wait runs past its limit
+    // one block per planet with the tail levels' vectors in shared memory: the largest
+    // planet's padded rows summed over the tail levels (0: vectors in global memory)
+    unsigned shared_rows;
 };
 
 // Co-resident 1024-thread tail blocks on this device (0: no cooperative launch).
 unsigned tail_block_budget();
+// Dynamic shared memory a shared-memory tail block may take on this device.
+unsigned tail_shared_max_bytes();
 
 template <typename T>
 void launch_coarse_tail(const TailArgs<T>& args, cudaStream_t st);

@@ -22,12 +22,18 @@ namespace psgb {
 namespace {
 
 // One 256-thread block per tile: the shared phases of phases.cuh.
+//
+// Reductions complete by ticket: the last tile set of a planet to write its partials sums
+// them and performs the scalar step in the same launch (one launch per phase; the
+// planets' finishes run in parallel inside it). kDeferred would instead add a per-planet
+// finish launch after each reducing phase; both give the same bits.
+constexpr int kCompletion = ph::kTicket;
 
 template <typename T, int R>
 __global__ void k_bicg_init(LevelView<T> lv, const T* __restrict__ b, T* x, T* r, T* shadow, T* p, T* v,
                             ReduceCtx ctx, double tol, int max_it) {
     pdl_begin();
-    ph::bicg_init<T, R, ph::kDeferred>(lv, blockIdx.x * R, 0, threadIdx.x, b, x, r, shadow, p, v, ctx, tol, max_it);
+    ph::bicg_init<T, R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, b, x, r, shadow, p, v, ctx, tol, max_it);
 }
 
 template <typename T, int R>
@@ -41,21 +47,21 @@ template <typename T, int W, int R>
 __global__ void k_bicg_v(LevelView<T> lv, const T* __restrict__ in, T* __restrict__ out, const T* __restrict__ shadow,
                          ReduceCtx ctx) {
     pdl_begin();
-    ph::bicg_v<T, W, R, ph::kDeferred>(lv, blockIdx.x * R, 0, threadIdx.x, in, out, shadow, ctx);
+    ph::bicg_v<T, W, R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, in, out, shadow, ctx);
 }
 
 template <typename T, int R>
 __global__ void k_bicg_s(LevelView<T> lv, const T* __restrict__ r, const T* __restrict__ v, T* __restrict__ s_out,
                          T* xv, T omega_j, ReduceCtx ctx) {
     pdl_begin();
-    ph::bicg_s<T, R, ph::kDeferred>(lv, blockIdx.x * R, 0, threadIdx.x, r, v, s_out, xv, omega_j, ctx);
+    ph::bicg_s<T, R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, r, v, s_out, xv, omega_j, ctx);
 }
 
 template <typename T, int W, int R>
 __global__ void k_bicg_t(LevelView<T> lv, const T* __restrict__ shat, T* __restrict__ t, const T* __restrict__ s_vec,
                          ReduceCtx ctx) {
     pdl_begin();
-    ph::bicg_t<T, W, R, ph::kDeferred>(lv, blockIdx.x * R, 0, threadIdx.x, shat, t, s_vec, ctx);
+    ph::bicg_t<T, W, R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, shat, t, s_vec, ctx);
 }
 
 template <typename T, int R>
@@ -63,20 +69,20 @@ __global__ void k_bicg_x(LevelView<T> lv, const T* __restrict__ phat, const T* _
                          const T* __restrict__ s_vec, const T* __restrict__ t, T* x, T* r,
                          const T* __restrict__ shadow, ReduceCtx ctx) {
     pdl_begin();
-    ph::bicg_x<T, R, ph::kDeferred>(lv, blockIdx.x * R, 0, threadIdx.x, phat, shat, s_vec, t, x, r, shadow, ctx);
+    ph::bicg_x<T, R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, phat, shat, s_vec, t, x, r, shadow, ctx);
 }
 
 template <typename T, int R>
 __global__ void k_pcg_init(LevelView<T> lv, const T* __restrict__ b, T* x, T* r, T* p, T* xv, T omega_j,
                            ReduceCtx ctx, double tol, int max_it) {
     pdl_begin();
-    ph::pcg_init<T, R, ph::kDeferred>(lv, blockIdx.x * R, 0, threadIdx.x, b, x, r, p, xv, omega_j, ctx, tol, max_it);
+    ph::pcg_init<T, R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, b, x, r, p, xv, omega_j, ctx, tol, max_it);
 }
 
 template <typename T, int R>
 __global__ void k_pcg_rz(LevelView<T> lv, const T* __restrict__ r, const T* __restrict__ z, ReduceCtx ctx) {
     pdl_begin();
-    ph::pcg_rz<T, R, ph::kDeferred>(lv, blockIdx.x * R, 0, threadIdx.x, r, z, ctx);
+    ph::pcg_rz<T, R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, r, z, ctx);
 }
 
 template <typename T, int R>
@@ -88,14 +94,14 @@ __global__ void k_pcg_p(LevelView<T> lv, const T* __restrict__ z, T* p, const In
 template <typename T, int W, int R>
 __global__ void k_pcg_q(LevelView<T> lv, const T* __restrict__ p, T* __restrict__ q_out, ReduceCtx ctx) {
     pdl_begin();
-    ph::pcg_q<T, W, R, ph::kDeferred>(lv, blockIdx.x * R, 0, threadIdx.x, p, q_out, ctx);
+    ph::pcg_q<T, W, R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, p, q_out, ctx);
 }
 
 template <typename T, int R>
 __global__ void k_pcg_xr(LevelView<T> lv, const T* __restrict__ p, const T* __restrict__ q_in, T* x, T* r, T* xv,
                          T omega_j, ReduceCtx ctx) {
     pdl_begin();
-    ph::pcg_xr<T, R, ph::kDeferred>(lv, blockIdx.x * R, 0, threadIdx.x, p, q_in, x, r, xv, omega_j, ctx);
+    ph::pcg_xr<T, R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, p, q_in, x, r, xv, omega_j, ctx);
 }
 
 template <int R>
@@ -103,14 +109,14 @@ __global__ void k_outer_init(LevelView<double> lv, const double* __restrict__ b,
                              int max_refine, const std::uint8_t* __restrict__ active) {
     pdl_begin();
     static_cast<void>(max_refine);
-    ph::outer_init<R, ph::kDeferred>(lv, blockIdx.x * R, 0, threadIdx.x, b, ctx, tol, active);
+    ph::outer_init<R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, b, ctx, tol, active);
 }
 
 template <typename TI, int W, int R>
 __global__ void k_outer_residual(LevelView<double> lv, const double* __restrict__ b, const double* __restrict__ x,
                                  double* __restrict__ r64, TI* __restrict__ rin, ReduceCtx ctx, int max_refine) {
     pdl_begin();
-    ph::outer_residual<TI, W, R, ph::kDeferred>(lv, blockIdx.x * R, 0, threadIdx.x, b, x, r64, rin, ctx, max_refine);
+    ph::outer_residual<TI, W, R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, b, x, r64, rin, ctx, max_refine);
 }
 
 template <typename TI, int R>
@@ -146,7 +152,7 @@ template <typename T>
 void KrylovLaunch<T>::bicg_init(const LevelView<T>& lv, const T* b, T* x, T* r, T* shadow, T* p, T* v,
                                 const ReduceCtx& ctx, double tol, int max_it, cudaStream_t st) {
     PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_bicg_init<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamKrylovVector), b, x, r, shadow, p, v, ctx, tol, max_it)));
-    launch_finish<ph::kFinBicgInit>(kFamKrylovVector, ctx, st, ph::FinishParams{tol, max_it, 0, nullptr});
+    if constexpr (kCompletion == ph::kDeferred) launch_finish<ph::kFinBicgInit>(kFamKrylovVector, ctx, st, ph::FinishParams{tol, max_it, 0, nullptr});
 }
 template <typename T>
 void KrylovLaunch<T>::bicg_p(const LevelView<T>& lv, const T* r, const T* v, T* p, T* xv, T omega_j,
@@ -157,38 +163,38 @@ template <typename T>
 void KrylovLaunch<T>::bicg_v(const LevelView<T>& lv, const T* in, T* out, const T* shadow,
                              const ReduceCtx& ctx, cudaStream_t st) {
     PSGB_LAUNCH(kFamKrylovSpmv, st, PSGB_WIDTHS(lv.width, PSGB_STENCIL_SETS(lv.sets_stencil, launch_pdl(k_bicg_v<T, W, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamKrylovSpmv), in, out, shadow, ctx))));
-    launch_finish<ph::kFinBicgV>(kFamKrylovSpmv, ctx, st);
+    if constexpr (kCompletion == ph::kDeferred) launch_finish<ph::kFinBicgV>(kFamKrylovSpmv, ctx, st);
 }
 template <typename T>
 void KrylovLaunch<T>::bicg_s(const LevelView<T>& lv, const T* r, const T* v, T* s, T* xv, T omega_j,
                              const ReduceCtx& ctx, cudaStream_t st) {
     PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_bicg_s<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamKrylovVector), r, v, s, xv, omega_j, ctx)));
-    launch_finish<ph::kFinBicgS>(kFamKrylovVector, ctx, st);
+    if constexpr (kCompletion == ph::kDeferred) launch_finish<ph::kFinBicgS>(kFamKrylovVector, ctx, st);
 }
 template <typename T>
 void KrylovLaunch<T>::bicg_t(const LevelView<T>& lv, const T* shat, T* t, const T* s,
                              const ReduceCtx& ctx, cudaStream_t st) {
     PSGB_LAUNCH(kFamKrylovSpmv, st, PSGB_WIDTHS(lv.width, PSGB_STENCIL_SETS(lv.sets_stencil, launch_pdl(k_bicg_t<T, W, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamKrylovSpmv), shat, t, s, ctx))));
-    launch_finish<ph::kFinBicgT>(kFamKrylovSpmv, ctx, st);
+    if constexpr (kCompletion == ph::kDeferred) launch_finish<ph::kFinBicgT>(kFamKrylovSpmv, ctx, st);
 }
 template <typename T>
 void KrylovLaunch<T>::bicg_x(const LevelView<T>& lv, const T* phat, const T* shat, const T* s,
                              const T* t, T* x, T* r, const T* shadow, const ReduceCtx& ctx,
                              cudaStream_t st) {
     PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_bicg_x<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamKrylovVector), phat, shat, s, t, x, r, shadow, ctx)));
-    launch_finish<ph::kFinBicgX>(kFamKrylovVector, ctx, st);
+    if constexpr (kCompletion == ph::kDeferred) launch_finish<ph::kFinBicgX>(kFamKrylovVector, ctx, st);
 }
 template <typename T>
 void KrylovLaunch<T>::pcg_init(const LevelView<T>& lv, const T* b, T* x, T* r, T* p, T* xv, T omega_j,
                                const ReduceCtx& ctx, double tol, int max_it, cudaStream_t st) {
     PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_pcg_init<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamKrylovVector), b, x, r, p, xv, omega_j, ctx, tol, max_it)));
-    launch_finish<ph::kFinPcgInit>(kFamKrylovVector, ctx, st, ph::FinishParams{tol, max_it, 0, nullptr});
+    if constexpr (kCompletion == ph::kDeferred) launch_finish<ph::kFinPcgInit>(kFamKrylovVector, ctx, st, ph::FinishParams{tol, max_it, 0, nullptr});
 }
 template <typename T>
 void KrylovLaunch<T>::pcg_rz(const LevelView<T>& lv, const T* r, const T* z, const ReduceCtx& ctx,
                              cudaStream_t st) {
     PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_pcg_rz<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamKrylovVector), r, z, ctx)));
-    launch_finish<ph::kFinPcgRz>(kFamKrylovVector, ctx, st);
+    if constexpr (kCompletion == ph::kDeferred) launch_finish<ph::kFinPcgRz>(kFamKrylovVector, ctx, st);
 }
 template <typename T>
 void KrylovLaunch<T>::pcg_p(const LevelView<T>& lv, const T* z, T* p, const InstanceScalars* sc,
@@ -199,13 +205,13 @@ template <typename T>
 void KrylovLaunch<T>::pcg_q(const LevelView<T>& lv, const T* p, T* q, const ReduceCtx& ctx,
                             cudaStream_t st) {
     PSGB_LAUNCH(kFamKrylovSpmv, st, PSGB_WIDTHS(lv.width, PSGB_STENCIL_SETS(lv.sets_stencil, launch_pdl(k_pcg_q<T, W, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamKrylovSpmv), p, q, ctx))));
-    launch_finish<ph::kFinPcgQ>(kFamKrylovSpmv, ctx, st);
+    if constexpr (kCompletion == ph::kDeferred) launch_finish<ph::kFinPcgQ>(kFamKrylovSpmv, ctx, st);
 }
 template <typename T>
 void KrylovLaunch<T>::pcg_xr(const LevelView<T>& lv, const T* p, const T* q, T* x, T* r, T* xv,
                              T omega_j, const ReduceCtx& ctx, cudaStream_t st) {
     PSGB_LAUNCH(kFamKrylovVector, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_pcg_xr<T, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamKrylovVector), p, q, x, r, xv, omega_j, ctx)));
-    launch_finish<ph::kFinPcgXr>(kFamKrylovVector, ctx, st);
+    if constexpr (kCompletion == ph::kDeferred) launch_finish<ph::kFinPcgXr>(kFamKrylovVector, ctx, st);
 }
 
 template struct KrylovLaunch<float>;
@@ -214,14 +220,14 @@ template struct KrylovLaunch<double>;
 void launch_outer_init(const LevelView<double>& lv, const double* b, const ReduceCtx& ctx, double tol,
                        int max_refine, const std::uint8_t* active, cudaStream_t st) {
     PSGB_LAUNCH(kFamRefine, st, PSGB_VECTOR_SETS(lv.sets_vector, launch_pdl(k_outer_init<R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamRefine), b, ctx, tol, max_refine, active)));
-    launch_finish<ph::kFinOuterInit>(kFamRefine, ctx, st, ph::FinishParams{tol, 0, max_refine, active});
+    if constexpr (kCompletion == ph::kDeferred) launch_finish<ph::kFinOuterInit>(kFamRefine, ctx, st, ph::FinishParams{tol, 0, max_refine, active});
 }
 
 template <typename TI>
 void launch_outer_residual(const LevelView<double>& lv, const double* b, const double* x, double* r64,
                            TI* rin, const ReduceCtx& ctx, int max_refine, cudaStream_t st) {
     PSGB_LAUNCH(kFamRefine, st, PSGB_WIDTHS(lv.width, PSGB_STENCIL_SETS(lv.sets_stencil, launch_pdl(k_outer_residual<TI, W, R>, ph::tile_sets(lv.tiles, R), kTile, st, counted(lv, kFamRefine), b, x, r64, rin, ctx, max_refine))));
-    launch_finish<ph::kFinOuterResidual>(kFamRefine, ctx, st, ph::FinishParams{0.0, 0, max_refine, nullptr});
+    if constexpr (kCompletion == ph::kDeferred) launch_finish<ph::kFinOuterResidual>(kFamRefine, ctx, st, ph::FinishParams{0.0, 0, max_refine, nullptr});
 }
 
 template <typename TI>

@@ -220,6 +220,10 @@ struct Batch {
     // Several co-resident blocks per large planet in the tail (cooperative launch): per
     // tail level the packed per-block words and their count (null: one block per planet).
     bool tail_spread = true;
+    // One block per planet with the tail levels' vectors in shared memory (wins over spread);
+    // per tail level the largest planet's padded rows summed down to its coarsest level.
+    bool tail_shared = false;
+    std::vector<unsigned> tail_rows_at;
     std::vector<std::uint32_t*> tail_cta_at;
     std::vector<unsigned> tail_ctas_at;
     unsigned* tail_barrier = nullptr;  // [2][instances]

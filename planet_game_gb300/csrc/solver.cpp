@@ -425,6 +425,15 @@ std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* ar
                 b.tail_ctas_at[l] = static_cast<unsigned>(cta.size());
             }
         }
+        // the shared-memory tail's rows per tail level (largest planet)
+        b.tail_rows_at.assign(depth, 0u);
+        for (std::size_t l = 1; l < depth; ++l) {
+            for (std::uint32_t i = 0; i < I; ++i) {
+                unsigned rows = 0;
+                for (std::size_t k = l; k < depth && b.levels[k].base[i] >= 0; ++k) rows += pad_rows(b.levels[k].count[i]);
+                b.tail_rows_at[l] = std::max(b.tail_rows_at[l], rows);
+            }
+        }
         b.tail_barrier = b.store.alloc<unsigned>(2 * std::size_t(I));
         PSGB_CUDA(cudaMemset(b.tail_barrier, 0, 2 * std::size_t(I) * sizeof(unsigned)));
     }
@@ -461,6 +470,15 @@ static LevelView<T> make_view(const BatchLevel& L, const T* vd, const T* inv, st
                         L.tile_sweep,   L.tile_meta,    nullptr,
                         L.sets_stencil, L.sets_vector,  static_cast<std::uint8_t>(level)};
 }
+
+template <typename T>
+bool tail_fits_shared(const Batch& b, int level) {
+    if (level <= 0 || static_cast<std::size_t>(level) >= b.tail_rows_at.size()) return false;
+    static const unsigned limit = tail_shared_max_bytes();
+    return std::size_t(4) * b.tail_rows_at[level] * sizeof(T) <= limit;
+}
+template bool tail_fits_shared<float>(const Batch&, int);
+template bool tail_fits_shared<double>(const Batch&, int);
 
 StepView step_view(const Batch& b) {
     const BatchLevel& F = b.levels[0];
@@ -545,6 +563,11 @@ TailArgs<T> tail_args(Batch& b, int gate) {
     a.omega = static_cast<T>(b.smoother.omega);
     a.sc = b.scalars;
     a.gate = gate;
+    a.shared_rows = 0;
+    if (b.tail_shared && tail_fits_shared<T>(b, b.tail_level)) {
+        a.shared_rows = b.tail_rows_at[b.tail_level];
+        return a;
+    }
     // Per-planet blocks in proportion to the planets' rows at the tail level.
     if (b.tail_spread && b.tail_cta_at[b.tail_level] != nullptr) {
         a.cta = b.tail_cta_at[b.tail_level];
@@ -694,6 +717,7 @@ std::vector<int> shape_of(const Batch& b) {
     }
     shape.push_back(b.tail_level);
     shape.push_back(b.tail_spread ? 1 : 0);
+    shape.push_back(b.tail_shared ? 1 : 0);
     return shape;
 }
 
@@ -895,7 +919,9 @@ void solve(Batch& b, const SolveOptions& opt, const double* rhs, double* x, cuda
     InstanceScalars* host = b.pinned_scalars != nullptr ? b.pinned_scalars : b.host_scalars.data();
     PSGB_CUDA(cudaMemcpyAsync(host, b.scalars, b.instances * sizeof(InstanceScalars), cudaMemcpyDeviceToHost, st));
     unsigned barrier_error[2] = {0, 0};
-    const bool spread_tail = !persistent && b.tail_level > 0 && b.tail_spread && b.tail_cta_at[b.tail_level] != nullptr;
+    const bool spread_tail = !persistent && b.tail_level > 0 && b.tail_spread && b.tail_cta_at[b.tail_level] != nullptr &&
+                             !(b.tail_shared && (opt.precision == kMixed ? tail_fits_shared<float>(b, b.tail_level)
+                                                                          : tail_fits_shared<double>(b, b.tail_level)));
     if (persistent || spread_tail) {
         PSGB_CUDA(cudaMemcpyAsync(barrier_error, b.sync + 2, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     }

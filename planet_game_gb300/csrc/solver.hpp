@@ -67,4 +67,8 @@ void solve(Batch& b, const SolveOptions& opt, const double* rhs, double* x, cuda
 // The fine level of a batch as the transport-step kernels see it.
 StepView step_view(const Batch& b);
 
+// The levels from `level` down fit the shared-memory coarse tail in precision T.
+template <typename T>
+bool tail_fits_shared(const Batch& b, int level);
+
 }  // namespace psgb

@@ -163,3 +163,29 @@ def test_spread_coarse_tail_equals_single_block_tail(planets):
         for out, its, _ in runs[1:]:
             assert its == runs[0][1]
             assert all(np.array_equal(a, b) for a, b in zip(runs[0][0], out))
+
+
+def test_shared_memory_coarse_tail_equals_no_tail(planets):
+    """The tail with its levels' vectors in shared memory (one block per planet) gives the
+    same bits as no tail at every tail level that fits, with plain and block-local sweeps,
+    in both precisions."""
+    import planet_game_gb300 as pg
+
+    ms, inputs = planets
+    batch = pg.Batch(ms)
+    t = batch.tuning
+    depth = t["levels"]
+    for block in (1, 4):
+        t["block_sweeps"] = [1] + [block] * (depth - 1)
+        for precision, method in (("mixed", "bicgstab"), ("fp64", "pcg")):
+            runs = []
+            for tail, mode in [(0, 0)] + [(l, 2) for l in range(1, depth)]:
+                t["coarse_tail_level"], t["coarse_tail_single"] = tail, mode
+                batch.set_tuning(t)
+                out, reps = step(batch, inputs, precision=precision, method=method)
+                for r in reps:
+                    assert r.status == 0 and r.relative_residual <= 1e-10
+                runs.append((out, [r.iterations for r in reps]))
+            for out, its in runs[1:]:
+                assert its == runs[0][1]
+                assert all(np.array_equal(a, b) for a, b in zip(runs[0][0], out))
