@@ -270,27 +270,38 @@ unsigned tail_block_budget() {
     return static_cast<unsigned>(sms * std::min(per_sm, per_sm64));
 }
 
+template <typename T>
 unsigned tail_shared_max_bytes() {
-    int device = 0, optin = 0;
-    if (cudaGetDevice(&device) != cudaSuccess) return 0;
-    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess) return 0;
-    // room for the kernel's static shared memory (its argument copy and phase scratch)
-    const unsigned reserve = 16u << 10;
-    return optin > static_cast<int>(reserve) ? static_cast<unsigned>(optin) - reserve : 0u;
+    // the block's opt-in shared memory less the kernel's static shared memory (its copy of
+    // the arguments, the block-local sweeps' tiles); the kernel is opted in to it once
+    static const unsigned limit = [] {
+        int device = 0, optin = 0;
+        cudaFuncAttributes fa{};
+        if (cudaGetDevice(&device) != cudaSuccess ||
+            cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess ||
+            cudaFuncGetAttributes(&fa, k_coarse_tail_shared<T>) != cudaSuccess) {
+            cudaGetLastError();
+            return 0u;
+        }
+        const long room = static_cast<long>(optin) - static_cast<long>(fa.sharedSizeBytes);
+        if (room <= 0) return 0u;
+        if (cudaFuncSetAttribute(k_coarse_tail_shared<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(room)) != cudaSuccess) {
+            cudaGetLastError();
+            return 0u;
+        }
+        return static_cast<unsigned>(room);
+    }();
+    return limit;
 }
+template unsigned tail_shared_max_bytes<float>();
+template unsigned tail_shared_max_bytes<double>();
 
 template <typename T>
 void launch_coarse_tail(const TailArgs<T>& args, cudaStream_t st) {
     if (args.shared_rows != 0) {
         const std::size_t bytes = std::size_t(4) * args.shared_rows * sizeof(T);
-        static const unsigned limit = tail_shared_max_bytes();
-        if (bytes > limit) throw std::logic_error("coarse tail: the levels do not fit in shared memory");
-        static bool opted = false;
-        if (!opted) {
-            PSGB_CUDA(cudaFuncSetAttribute(k_coarse_tail_shared<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           static_cast<int>(limit)));
-            opted = true;
-        }
+        if (bytes > tail_shared_max_bytes<T>()) throw std::logic_error("coarse tail: the levels do not fit in shared memory");
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
         attr[0].val.programmaticStreamSerializationAllowed = 1;

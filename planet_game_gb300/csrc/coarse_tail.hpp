@@ -45,7 +45,8 @@ struct TailArgs {
 
 // Co-resident 1024-thread tail blocks on this device (0: no cooperative launch).
 unsigned tail_block_budget();
-// Dynamic shared memory a shared-memory tail block may take on this device.
+// Dynamic shared memory a shared-memory tail block may take on this device (0: none).
+template <typename T>
 unsigned tail_shared_max_bytes();
 
 template <typename T>

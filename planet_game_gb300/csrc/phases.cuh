@@ -88,16 +88,64 @@ inline LevelView<T> counted(const LevelView<T>& lv, int family) {
     return v;
 }
 
+// The warp sums of N values (N a power of two, at most 32) by recursive halving: at the
+// exchanges with lane offsets 16, 8, ... while a lane holds several values, the lanes with
+// that offset bit clear keep the first half of their values and the others the second
+// half, each adding its partner's copy of what it keeps; once one value is left, plain
+// butterfly steps. Every value is combined with the same partner at every step as in a
+// butterfly of its own (warp_sum), so each total has warp_sum's bits, for N values at the
+// cost of about N - 1 + log2(32 / N) additions a lane instead of 5 N. On return `mine` is
+// the total of value `q`; `owner` is true in the lowest lane holding it.
+template <typename A, int N>
+__device__ __forceinline__ void warp_sum_halving(const A (&v)[N], int l32, A& mine, int& q, bool& owner) {
+    static_assert(N >= 1 && N <= 32 && (N & (N - 1)) == 0, "a power of two, at most 32");
+    A cur[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) cur[i] = v[i];
+    int held = 0;        // index of the first value this lane holds
+    unsigned mask = 0;   // lane bits that chose a half
+#pragma unroll
+    for (int step = 0; step < 5; ++step) {
+        const int o = 16 >> step;
+        const int m = (N >> step) > 1 ? (N >> step) : 1;   // values held before this step
+        if (m > 1) {
+            const int h = m / 2;
+            const bool upper = (l32 & o) != 0;
+#pragma unroll
+            for (int i = 0; i < h; ++i) {
+                const A send = upper ? cur[i] : cur[h + i];
+                const A keep = upper ? cur[h + i] : cur[i];
+                cur[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+            }
+            if (upper) held += h;
+            mask |= static_cast<unsigned>(o);
+        } else {
+            cur[0] += __shfl_xor_sync(0xffffffffu, cur[0], o);
+        }
+    }
+    mine = cur[0];
+    q = held;
+    owner = (static_cast<unsigned>(l32) & ~mask) == 0u;
+}
+
 // Sum of N values over the 256 threads of a group, each value in its own fixed tree
 // (warp butterflies, then the eight warp sums in order); results in lane 0.
 template <typename A, int N>
 __device__ __forceinline__ void group_sum(A (&v)[N], int gid, int lane) {
     __shared__ A scratch[kGroups][N][8];
     const int w = lane >> 5;
+    if constexpr (N == 1 || N == 2 || N == 4 || N == 8) {
+        A mine;
+        int q;
+        bool owner;
+        warp_sum_halving<A, N>(v, lane & 31, mine, q, owner);
+        if (owner) scratch[gid][q][w] = mine;
+    } else {
 #pragma unroll
-    for (int q = 0; q < N; ++q) {
-        const A s = warp_sum(v[q]);
-        if ((lane & 31) == 0) scratch[gid][q][w] = s;
+        for (int q = 0; q < N; ++q) {
+            const A s = warp_sum(v[q]);
+            if ((lane & 31) == 0) scratch[gid][q][w] = s;
+        }
     }
     group_sync(gid);
     if (lane == 0) {

@@ -474,8 +474,7 @@ static LevelView<T> make_view(const BatchLevel& L, const T* vd, const T* inv, st
 template <typename T>
 bool tail_fits_shared(const Batch& b, int level) {
     if (level <= 0 || static_cast<std::size_t>(level) >= b.tail_rows_at.size()) return false;
-    static const unsigned limit = tail_shared_max_bytes();
-    return std::size_t(4) * b.tail_rows_at[level] * sizeof(T) <= limit;
+    return std::size_t(4) * b.tail_rows_at[level] * sizeof(T) <= tail_shared_max_bytes<T>();
 }
 template bool tail_fits_shared<float>(const Batch&, int);
 template bool tail_fits_shared<double>(const Batch&, int);
