@@ -23,11 +23,15 @@ namespace {
 
 // One 256-thread block per tile: the shared phases of phases.cuh.
 //
-// Reductions complete by ticket: the last tile set of a planet to write its partials sums
-// them and performs the scalar step in the same launch (one launch per phase; the
-// planets' finishes run in parallel inside it). kDeferred would instead add a per-planet
-// finish launch after each reducing phase; both give the same bits.
-constexpr int kCompletion = ph::kTicket;
+// Reductions complete in a per-planet finish launch after each reducing phase (kDeferred).
+// Completing them by ticket instead (the last tile set of a planet to write its partials
+// sums them and performs the scalar step in the reducing launch) gives the same bits and
+// one launch fewer per reduction, but measured on GB300 it nearly doubled the reducing
+// kernels' time (BiCGSTAB products 10 -> 20 us on the 64-planet workload, 20 -> 32 us at
+// L8): the fences and tickets of every tile set and the last tile set's sum sit on the
+// kernel's critical path, where a separate small launch overlaps its start with the
+// previous kernel's drain.
+constexpr int kCompletion = ph::kDeferred;
 
 template <typename T, int R>
 __global__ void k_bicg_init(LevelView<T> lv, const T* __restrict__ b, T* x, T* r, T* shadow, T* p, T* v,
