@@ -88,6 +88,32 @@ __device__ __forceinline__ void count(unsigned long long* counter, unsigned long
     if (counter != nullptr && threadIdx.x == 0 && bytes != 0) atomicAdd(counter, bytes);
 }
 
+// A tile's 256 rows of a level's matrix (columns, off-diagonal values, optionally the
+// diagonal and its inverse) staged in shared memory with coalesced loads, thread t taking
+// row t: the warps' row loops then read their rows' columns and values there (broadcast)
+// and go to global memory only for the right-hand sides' vectors, one dependent round
+// trip per group of rows instead of two.
+template <typename T, int W, bool Diag, bool Inv>
+struct TileRows {
+    int col[W][kTile];
+    T val[W + (Diag ? 1 : 0)][kTile];
+    T inv[Inv ? kTile : 1];
+};
+
+template <typename T, int W, bool Diag, bool Inv>
+__device__ __forceinline__ void stage_rows(const LevelView<T>& L, int tile, TileRows<T, W, Diag, Inv>& m) {
+    const std::uint32_t P = L.rows;
+    const int t = threadIdx.x, row = tile * kTile + t;
+#pragma unroll
+    for (int j = 0; j < W; ++j) {
+        m.col[j][t] = L.col[j * P + row];
+        m.val[j][t] = L.vd[j * P + row];
+    }
+    if constexpr (Diag) m.val[W][t] = L.vd[W * P + row];
+    if constexpr (Inv) m.inv[t] = L.inv[row];
+    __syncthreads();
+}
+
 // ---- V-cycle ----------------------------------------------------------------------------
 
 template <typename T>
@@ -116,22 +142,23 @@ __global__ void k_smooth(LevelView<T> L, const T* __restrict__ b, const T* __res
     const int tile = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const TileInfo ti = tile_info(L.tile_meta, tile);
     if (!ti.sweep) return;
-    const std::uint32_t P = L.rows;
+    __shared__ TileRows<T, W, false, true> m;
+    stage_rows(L, tile, m);
     count(L.bytes, static_cast<unsigned long long>(ti.rows) * (4ull * W + sizeof(T) * (W + 1ull) + 3ull * kRhs * sizeof(T)));
     if (!ph::gate_open(sc, lane, gate)) return;
     for (int g = 0; g < 8; ++g) {
         T out[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            const int row = tile * kTile + local_row(warp, g, i);
+            const int local = local_row(warp, g, i), row = tile * kTile + local;
             T s = b[at(row, lane)];
 #pragma unroll
-            for (int j = 0; j < W; ++j) s -= L.vd[j * P + row] * x[at(L.col[j * P + row], lane)];
+            for (int j = 0; j < W; ++j) s -= m.val[j][local] * x[at(m.col[j][local], lane)];
             if (omega == T(1)) {
-                out[i] = L.inv[row] * s;
+                out[i] = m.inv[local] * s;
             } else {
                 const T xo = x[at(row, lane)];
-                out[i] = xo + omega * (L.inv[row] * s - xo);
+                out[i] = xo + omega * (m.inv[local] * s - xo);
             }
         }
 #pragma unroll
@@ -149,17 +176,18 @@ __global__ void k_residual(LevelView<T> L, const T* __restrict__ b, const T* __r
     const int tile = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const TileInfo ti = tile_info(L.tile_meta, tile);
     if (!ti.sweep) return;
-    const std::uint32_t P = L.rows;
+    __shared__ TileRows<T, W, true, false> m;
+    stage_rows(L, tile, m);
     count(L.bytes, static_cast<unsigned long long>(ti.rows) * (4ull * W + sizeof(T) * (W + 1ull) + 3ull * kRhs * sizeof(T)));
     if (!ph::gate_open(sc, lane, gate)) return;
     for (int g = 0; g < 8; ++g) {
         T out[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            const int row = tile * kTile + local_row(warp, g, i);
-            T s = b[at(row, lane)] - L.vd[W * P + row] * x[at(row, lane)];
+            const int local = local_row(warp, g, i), row = tile * kTile + local;
+            T s = b[at(row, lane)] - m.val[W][local] * x[at(row, lane)];
 #pragma unroll
-            for (int j = 0; j < W; ++j) s -= L.vd[j * P + row] * x[at(L.col[j * P + row], lane)];
+            for (int j = 0; j < W; ++j) s -= m.val[j][local] * x[at(m.col[j][local], lane)];
             out[i] = s;
         }
 #pragma unroll
@@ -211,25 +239,26 @@ __global__ void k_prolong_smooth(LevelView<T> L, const std::int32_t* __restrict_
     const int tile = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const TileInfo ti = tile_info(L.tile_meta, tile);
     if (!ti.sweep) return;
-    const std::uint32_t P = L.rows;
+    __shared__ TileRows<T, W, false, true> m;
+    stage_rows(L, tile, m);
     count(L.bytes, static_cast<unsigned long long>(ti.rows) * (4ull * W + sizeof(T) * (W + 1ull) + 4ull + 3ull * kRhs * sizeof(T)));
     if (!ph::gate_open(sc, lane, gate)) return;
     for (int g = 0; g < 8; ++g) {
         T out[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            const int row = tile * kTile + local_row(warp, g, i);
+            const int local = local_row(warp, g, i), row = tile * kTile + local;
             T s = b[at(row, lane)];
 #pragma unroll
             for (int j = 0; j < W; ++j) {
-                const int c = L.col[j * P + row];
-                s -= L.vd[j * P + row] * (x[at(c, lane)] + e[at(agg[c], lane)]);
+                const int c = m.col[j][local];
+                s -= m.val[j][local] * (x[at(c, lane)] + e[at(agg[c], lane)]);
             }
             if (omega == T(1)) {
-                out[i] = L.inv[row] * s;
+                out[i] = m.inv[local] * s;
             } else {
                 const T xo = x[at(row, lane)] + e[at(agg[row], lane)];
-                out[i] = xo + omega * (L.inv[row] * s - xo);
+                out[i] = xo + omega * (m.inv[local] * s - xo);
             }
         }
 #pragma unroll
@@ -349,7 +378,8 @@ __global__ void k_bicg_v(LevelView<T> L, const T* __restrict__ in, T* __restrict
     pdl_begin();
     const int tile = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const TileInfo ti = tile_info(L.tile_meta, tile);
-    const std::uint32_t P = L.rows;
+    __shared__ TileRows<T, W, true, false> m;
+    stage_rows(L, tile, m);
     const bool on = ti.rows > 0 && ph::running(ctx.sc[lane]);
     count(L.bytes, static_cast<unsigned long long>(ti.rows) * (4ull * W + sizeof(T) * (W + 1ull) + 3ull * kRhs * sizeof(T)));
     T run[8];
@@ -358,9 +388,9 @@ __global__ void k_bicg_v(LevelView<T> L, const T* __restrict__ in, T* __restrict
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             const int local = local_row(warp, g, i), row = tile * kTile + local;
-            T s = L.vd[W * P + row] * in[at(row, lane)];
+            T s = m.val[W][local] * in[at(row, lane)];
 #pragma unroll
-            for (int j = 0; j < W; ++j) s += L.vd[j * P + row] * in[at(L.col[j * P + row], lane)];
+            for (int j = 0; j < W; ++j) s += m.val[j][local] * in[at(m.col[j][local], lane)];
             q[i] = ph::prod(shadow[at(row, lane)], s);
             const bool store = on && local < ti.rows;
             if (store) out[at(row, lane)] = s;
@@ -409,7 +439,8 @@ __global__ void k_bicg_t(LevelView<T> L, const T* __restrict__ shat, T* __restri
     pdl_begin();
     const int tile = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const TileInfo ti = tile_info(L.tile_meta, tile);
-    const std::uint32_t P = L.rows;
+    __shared__ TileRows<T, W, true, false> m;
+    stage_rows(L, tile, m);
     const bool on = ti.rows > 0 && ph::running(ctx.sc[lane]) && !ctx.sc[lane].half_done;
     count(L.bytes, static_cast<unsigned long long>(ti.rows) * (4ull * W + sizeof(T) * (W + 1ull) + 3ull * kRhs * sizeof(T)));
     T run0[8], run1[8];
@@ -418,9 +449,9 @@ __global__ void k_bicg_t(LevelView<T> L, const T* __restrict__ shat, T* __restri
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             const int local = local_row(warp, g, i), row = tile * kTile + local;
-            T s = L.vd[W * P + row] * shat[at(row, lane)];
+            T s = m.val[W][local] * shat[at(row, lane)];
 #pragma unroll
-            for (int j = 0; j < W; ++j) s += L.vd[j * P + row] * shat[at(L.col[j * P + row], lane)];
+            for (int j = 0; j < W; ++j) s += m.val[j][local] * shat[at(m.col[j][local], lane)];
             q0[i] = ph::prod(s, s);
             q1[i] = ph::prod(s, s_vec[at(row, lane)]);
             const bool store = on && local < ti.rows;
@@ -506,7 +537,8 @@ __global__ void k_outer_residual(LevelView<double> L, const double* __restrict__
     pdl_begin();
     const int tile = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const TileInfo ti = tile_info(L.tile_meta, tile);
-    const std::uint32_t P = L.rows;
+    __shared__ TileRows<double, W, true, false> m;
+    stage_rows(L, tile, m);
     const bool on = ti.rows > 0 && ctx.sc[lane].outer_status == kRunning;
     count(L.bytes, static_cast<unsigned long long>(ti.rows) * (4ull * W + 8ull * (W + 1ull) + kRhs * (24ull + sizeof(TI))));
     double run[8];
@@ -514,10 +546,10 @@ __global__ void k_outer_residual(LevelView<double> L, const double* __restrict__
         double q[4], rv[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            const int row = tile * kTile + local_row(warp, g, i);
-            double s = b[at(row, lane)] - L.vd[W * P + row] * x[at(row, lane)];
+            const int local = local_row(warp, g, i), row = tile * kTile + local;
+            double s = b[at(row, lane)] - m.val[W][local] * x[at(row, lane)];
 #pragma unroll
-            for (int j = 0; j < W; ++j) s -= L.vd[j * P + row] * x[at(L.col[j * P + row], lane)];
+            for (int j = 0; j < W; ++j) s -= m.val[j][local] * x[at(m.col[j][local], lane)];
             rv[i] = s;
         }
 #pragma unroll
