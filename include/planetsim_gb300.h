@@ -21,7 +21,9 @@
  *
  * ABI version 2: psgb_planet_info and psgb_tuning grew fields (fine_cells; the coarse
  * tail's spread and block count). Version 3: the serving loop (psgb_server_*) and
- * PSGB_ERR_TIMEOUT.
+ * PSGB_ERR_TIMEOUT. Version 4: the block step of one planet (psgb_transport_step_multi),
+ * per-step reassembly (psgb_batch_set_reassembly), coarse_tail_single = 2 (the
+ * shared-memory coarse tail).
  *
  * A server's calls may come from any thread; its lanes step on threads of their own.
  */
@@ -35,7 +37,7 @@
 extern "C" {
 #endif
 
-#define PSGB_ABI_VERSION 3
+#define PSGB_ABI_VERSION 4
 
 /* status codes */
 #define PSGB_OK 0
