@@ -23,7 +23,8 @@
  * tail's spread and block count). Version 3: the serving loop (psgb_server_*) and
  * PSGB_ERR_TIMEOUT. Version 4: the block step of one planet (psgb_transport_step_multi),
  * per-step reassembly (psgb_batch_set_reassembly), coarse_tail_single = 2 (the
- * shared-memory coarse tail).
+ * shared-memory coarse tail). Version 5: coarse_tail_single = 3 and psgb_tuning's
+ * coarse_tail_cluster (the coarse tail on a thread-block cluster per planet).
  *
  * A server's calls may come from any thread; its lanes step on threads of their own.
  */
@@ -37,7 +38,7 @@
 extern "C" {
 #endif
 
-#define PSGB_ABI_VERSION 4
+#define PSGB_ABI_VERSION 5
 
 /* status codes */
 #define PSGB_OK 0
@@ -490,8 +491,12 @@ typedef struct psgb_tuning {
                                              memory with its neighbours in other tiles held (1..8; 1 = plain) */
     int coarse_tail_single;               /* 0: a large planet's tail runs on several co-resident blocks
                                              (cooperative launch, per-planet barriers); 1: one block each;
-                                             2: one block each with the tail levels' vectors in shared memory */
-    uint32_t coarse_tail_blocks;          /* out: blocks of the tail launch (0: no tail) */
+                                             2: one block each with the tail levels' vectors in shared memory;
+                                             3: a thread-block cluster each (coarse_tail_cluster blocks) with
+                                             the vectors in the cluster's distributed shared memory */
+    uint32_t coarse_tail_blocks;          /* out: blocks of the tail launch last built under these settings
+                                             (before one: the launch they ask for; 0: no tail) */
+    uint32_t coarse_tail_cluster;         /* coarse_tail_single = 3: blocks per planet's cluster, 2, 4 or 8 */
 } psgb_tuning;
 
 /* Times trial solves of one sub-step (the inputs as for psgb_batch_transport_step, every

@@ -161,7 +161,12 @@ Tuning current_tuning(const Batch& b) {
     t.tail_level = b.tail_level;
     t.tail_spread = b.tail_spread;
     t.tail_shared = b.tail_shared;
-    t.tail_blocks = b.tail_level == 0 ? 0u : b.tail_shared ? b.instances
+    t.tail_cluster = b.tail_cluster;
+    // the tail launch last built, else the one the settings ask for
+    t.tail_blocks = b.tail_level == 0             ? 0u
+                    : b.tail_launch_blocks != 0   ? b.tail_launch_blocks
+                    : b.tail_cluster != 0         ? b.instances * b.tail_cluster
+                    : b.tail_shared               ? b.instances
                     : (b.tail_spread && b.tail_cta_at[b.tail_level] != nullptr) ? b.tail_ctas_at[b.tail_level]
                                                                                  : b.instances;
     return t;
@@ -183,6 +188,8 @@ void apply_tuning(Batch& b, const Tuning& t) {
     if (!(t.omega > 0.0 && t.omega < 2.0)) throw std::invalid_argument("tuned damping must be in (0, 2)");
     if (t.tail_level < 0 || static_cast<std::size_t>(t.tail_level) >= depth)
         throw std::invalid_argument("the coarse tail level must be 0 (none) or a level below the fine one");
+    if (t.tail_cluster != 0 && t.tail_cluster != 2 && t.tail_cluster != 4 && t.tail_cluster != 8)
+        throw std::invalid_argument("the coarse tail's cluster must be 0 (none), 2, 4 or 8 blocks");
     for (std::size_t l = 0; l < depth; ++l) {
         b.levels[l].sets_stencil = t.sets_stencil[l];
         b.levels[l].sets_vector = t.sets_vector[l];
@@ -194,6 +201,8 @@ void apply_tuning(Batch& b, const Tuning& t) {
     b.tail_level = t.tail_level;
     b.tail_spread = t.tail_spread;
     b.tail_shared = t.tail_shared;
+    b.tail_cluster = t.tail_cluster;
+    b.tail_launch_blocks = 0;
     b.tuned = true;
 }
 
@@ -301,20 +310,30 @@ Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x,
     set_sweeps(b, best);
     {
         // modes: 0 spread over co-resident blocks, 1 one block per planet, 2 one block per
-        // planet with the levels' vectors in shared memory
-        const auto mode_of = [&] { return b.tail_shared ? 2 : (b.tail_spread ? 0 : 1); };
+        // planet with the levels' vectors in shared memory, 3/4/5 a cluster of 2/4/8 blocks
+        // per planet with the vectors in its distributed shared memory
+        const auto mode_of = [&] {
+            if (b.tail_cluster != 0) return b.tail_cluster == 2 ? 3 : (b.tail_cluster == 4 ? 4 : 5);
+            return b.tail_shared ? 2 : (b.tail_spread ? 0 : 1);
+        };
         const auto set_mode = [&](int mode) {
             b.tail_shared = mode == 2;
             b.tail_spread = mode == 0;
+            b.tail_cluster = mode >= 3 ? 1u << (mode - 2) : 0u;
+            b.tail_launch_blocks = 0;
         };
         const int chosen = b.tail_level;
         const int chosen_mode = mode_of();
         int pick = chosen, pick_mode = chosen_mode;
         const bool mixed = opt.precision == kMixed;
         for (int tail = 0; tail < static_cast<int>(depth); ++tail) {
-            for (int mode : {0, 1, 2}) {
+            for (int mode : {0, 1, 2, 3, 4, 5}) {
                 if ((tail == chosen && mode == chosen_mode) || (tail == 0 && mode != 0)) continue;
                 if (mode == 2 && !(mixed ? tail_fits_shared<float>(b, tail) : tail_fits_shared<double>(b, tail))) continue;
+                const unsigned cluster = mode >= 3 ? 1u << (mode - 2) : 0u;
+                if (mode >= 3 && !(mixed ? tail_fits_cluster<float>(b, tail, cluster)
+                                         : tail_fits_cluster<double>(b, tail, cluster)))
+                    continue;
                 b.tail_level = tail;
                 set_mode(mode);
                 const double ms = run(best);
@@ -341,6 +360,7 @@ Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x,
     result.tail_level = b.tail_level;
     result.tail_spread = b.tail_spread;
     result.tail_shared = b.tail_shared;
+    result.tail_cluster = b.tail_cluster;
     result.tuned_ms = best_ms;
     return result;
 }

@@ -19,6 +19,8 @@ struct Tuning {
     int tail_level = 0;                            // coarse tail from this level (0: none)
     bool tail_spread = true;                       // several blocks per large planet in the tail
     bool tail_shared = false;                      // one block per planet, the tail levels' vectors in shared memory
+    unsigned tail_cluster = 0;                     // blocks of a cluster per planet (2, 4, 8; 0: none), vectors in
+                                                   // the cluster's distributed shared memory
     unsigned tail_blocks = 0;                      // blocks of the tail launch (out; 0: no tail)
     double tuned_ms = 0.0;                         // trial solve with the chosen settings
     double default_ms = 0.0;                       // trial solve with the settings before tuning

@@ -911,8 +911,9 @@ void fill_tuning(const psgb::Tuning& t, psgb_tuning* out) {
     out->default_solve_ms = t.default_ms;
     out->trial_solves = t.trials;
     out->coarse_tail_level = t.tail_level;
-    out->coarse_tail_single = t.tail_shared ? 2 : (t.tail_spread ? 0 : 1);
+    out->coarse_tail_single = t.tail_cluster != 0 ? 3 : t.tail_shared ? 2 : (t.tail_spread ? 0 : 1);
     out->coarse_tail_blocks = t.tail_blocks;
+    out->coarse_tail_cluster = t.tail_cluster;
 }
 
 }  // namespace
@@ -1008,9 +1009,15 @@ int psgb_batch_set_tuning(psgb_batch* h, const psgb_tuning* tuning) {
         }
         t.omega = tuning->jacobi_omega;
         t.tail_level = tuning->coarse_tail_level;
-        require(tuning->coarse_tail_single >= 0 && tuning->coarse_tail_single <= 2, "coarse_tail_single must be 0, 1 or 2");
+        require(tuning->coarse_tail_single >= 0 && tuning->coarse_tail_single <= 3,
+                "coarse_tail_single must be 0, 1, 2 or 3");
         t.tail_spread = tuning->coarse_tail_single == 0;
         t.tail_shared = tuning->coarse_tail_single == 2;
+        if (tuning->coarse_tail_single == 3) {
+            const std::uint32_t c = tuning->coarse_tail_cluster;
+            require(c == 2 || c == 4 || c == 8, "coarse_tail_cluster must be 2, 4 or 8 blocks");
+            t.tail_cluster = c;
+        }
         psgb::apply_tuning(b, t);
         return PSGB_OK;
     });

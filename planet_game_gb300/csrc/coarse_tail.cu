@@ -299,6 +299,10 @@ template unsigned tail_shared_max_bytes<double>();
 
 template <typename T>
 void launch_coarse_tail(const TailArgs<T>& args, cudaStream_t st) {
+    if (args.cluster != 0) {
+        launch_coarse_cluster<T>(args, st);
+        return;
+    }
     if (args.shared_rows != 0) {
         const std::size_t bytes = std::size_t(4) * args.shared_rows * sizeof(T);
         if (bytes > tail_shared_max_bytes<T>()) throw std::logic_error("coarse tail: the levels do not fit in shared memory");

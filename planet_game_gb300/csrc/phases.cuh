@@ -414,11 +414,19 @@ __device__ void smooth(const LevelView<T>& lv, int t0, int lane, const T* PSGB_P
 // error between tiles is left to the next launch or the coarser levels. The tile-level
 // counterpart of the reference's block-hybrid smoother (heat_transport.cpp:258-286), with
 // Jacobi instead of sequential Gauss-Seidel inside the block.
+// The block-local sweeps' tiles, one per tile group: a single array per element type,
+// whichever ELL widths a kernel instantiates the sweep for.
+template <typename T>
+__device__ __forceinline__ T (*tile_buffer())[kTile] {
+    __shared__ T xs[kGroups][kTile];
+    return xs;
+}
+
 template <typename T, int W>
 __device__ void smooth_block(const LevelView<T>& lv, int tile, int gid, int lane, const T* PSGB_PHASE_RESTRICT b,
                              const T* PSGB_PHASE_RESTRICT x, T* PSGB_PHASE_RESTRICT y, T omega, int inner,
                              const InstanceScalars* sc, int gate) {
-    __shared__ T xs[kGroups][kTile];
+    T (*xs)[kTile] = tile_buffer<T>();
     const TileSet<1> ts = tile_set<1>(lv.tile_meta, lv.tiles, tile);
     if (!ts.sweep[0] || !gate_open(sc, ts.inst[0], gate)) return;
     const std::uint32_t P = lv.rows;

@@ -223,6 +223,11 @@ struct Batch {
     // One block per planet with the tail levels' vectors in shared memory (wins over spread);
     // per tail level the largest planet's padded rows summed down to its coarsest level.
     bool tail_shared = false;
+    // A thread-block cluster of this many blocks per planet (2, 4 or 8; 0: none) with the
+    // tail levels' vectors in the cluster's distributed shared memory (wins over both).
+    unsigned tail_cluster = 0;
+    // Blocks of the tail launch last built (0: none built under the current settings).
+    unsigned tail_launch_blocks = 0;
     std::vector<unsigned> tail_rows_at;
     std::vector<std::uint32_t*> tail_cta_at;
     std::vector<unsigned> tail_ctas_at;

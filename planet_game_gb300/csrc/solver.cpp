@@ -479,6 +479,39 @@ bool tail_fits_shared(const Batch& b, int level) {
 template bool tail_fits_shared<float>(const Batch&, int);
 template bool tail_fits_shared<double>(const Batch&, int);
 
+unsigned tail_cluster_rows(const Batch& b, int level, unsigned cluster) {
+    if (level <= 0 || static_cast<std::size_t>(level) >= b.levels.size() || cluster == 0) return 0;
+    unsigned most = 0;
+    for (std::uint32_t i = 0; i < b.instances; ++i) {
+        unsigned rows = 0;
+        for (std::size_t k = static_cast<std::size_t>(level); k < b.levels.size() && b.levels[k].base[i] >= 0; ++k) {
+            const unsigned tiles = pad_rows(b.levels[k].count[i]) / kTileRows;
+            rows += (tiles + cluster - 1) / cluster * kTileRows;
+        }
+        most = std::max(most, rows);
+    }
+    return most;
+}
+
+template <typename T>
+bool tail_fits_cluster(const Batch& b, int level, unsigned cluster) {
+    const unsigned rows = tail_cluster_rows(b, level, cluster);
+    return rows != 0 && cluster_tail_fits<T>(cluster, rows);
+}
+template bool tail_fits_cluster<float>(const Batch&, int, unsigned);
+template bool tail_fits_cluster<double>(const Batch&, int, unsigned);
+
+template <typename T>
+TailForm tail_form(const Batch& b) {
+    if (b.tail_level <= 0) return TailForm::kNone;
+    if (b.tail_cluster != 0 && tail_fits_cluster<T>(b, b.tail_level, b.tail_cluster)) return TailForm::kCluster;
+    if (b.tail_shared && tail_fits_shared<T>(b, b.tail_level)) return TailForm::kShared;
+    if (b.tail_spread && b.tail_cta_at[b.tail_level] != nullptr) return TailForm::kSpread;
+    return TailForm::kBlock;
+}
+template TailForm tail_form<float>(const Batch&);
+template TailForm tail_form<double>(const Batch&);
+
 StepView step_view(const Batch& b) {
     const BatchLevel& F = b.levels[0];
     return StepView{F.rows, F.tiles, b.instances, F.tile_inst, F.tile_rows, b.tile_begin, F.col, b.w, b.area,
@@ -563,16 +596,26 @@ TailArgs<T> tail_args(Batch& b, int gate) {
     a.sc = b.scalars;
     a.gate = gate;
     a.shared_rows = 0;
-    if (b.tail_shared && tail_fits_shared<T>(b, b.tail_level)) {
+    a.cluster = 0;
+    const TailForm form = tail_form<T>(b);
+    b.tail_launch_blocks = b.instances;
+    if (form == TailForm::kCluster) {
+        a.cluster = b.tail_cluster;
+        a.shared_rows = tail_cluster_rows(b, b.tail_level, b.tail_cluster);
+        b.tail_launch_blocks = b.instances * b.tail_cluster;
+        return a;
+    }
+    if (form == TailForm::kShared) {
         a.shared_rows = b.tail_rows_at[b.tail_level];
         return a;
     }
     // Per-planet blocks in proportion to the planets' rows at the tail level.
-    if (b.tail_spread && b.tail_cta_at[b.tail_level] != nullptr) {
+    if (form == TailForm::kSpread) {
         a.cta = b.tail_cta_at[b.tail_level];
         a.ctas = b.tail_ctas_at[b.tail_level];
         a.barrier = b.tail_barrier;
         a.error = b.sync + 3;
+        b.tail_launch_blocks = a.ctas;
     }
     return a;
 }
@@ -717,6 +760,7 @@ std::vector<int> shape_of(const Batch& b) {
     shape.push_back(b.tail_level);
     shape.push_back(b.tail_spread ? 1 : 0);
     shape.push_back(b.tail_shared ? 1 : 0);
+    shape.push_back(static_cast<int>(b.tail_cluster));
     return shape;
 }
 
@@ -918,9 +962,8 @@ void solve(Batch& b, const SolveOptions& opt, const double* rhs, double* x, cuda
     InstanceScalars* host = b.pinned_scalars != nullptr ? b.pinned_scalars : b.host_scalars.data();
     PSGB_CUDA(cudaMemcpyAsync(host, b.scalars, b.instances * sizeof(InstanceScalars), cudaMemcpyDeviceToHost, st));
     unsigned barrier_error[2] = {0, 0};
-    const bool spread_tail = !persistent && b.tail_level > 0 && b.tail_spread && b.tail_cta_at[b.tail_level] != nullptr &&
-                             !(b.tail_shared && (opt.precision == kMixed ? tail_fits_shared<float>(b, b.tail_level)
-                                                                          : tail_fits_shared<double>(b, b.tail_level)));
+    const bool spread_tail = !persistent && (opt.precision == kMixed ? tail_form<float>(b) : tail_form<double>(b)) ==
+                                                TailForm::kSpread;
     if (persistent || spread_tail) {
         PSGB_CUDA(cudaMemcpyAsync(barrier_error, b.sync + 2, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     }

@@ -71,4 +71,17 @@ StepView step_view(const Batch& b);
 template <typename T>
 bool tail_fits_shared(const Batch& b, int level);
 
+// Rows of each vector one block of a `cluster`-block cluster holds for the largest planet
+// (per level from `level` down, the planet's tiles shared out over the cluster).
+unsigned tail_cluster_rows(const Batch& b, int level, unsigned cluster);
+// The levels from `level` down fit clusters of `cluster` blocks in precision T.
+template <typename T>
+bool tail_fits_cluster(const Batch& b, int level, unsigned cluster);
+
+// The form the coarse tail of a solve in precision T takes: the batch's choice where it
+// fits, else the next one down (cluster, shared memory, spread, one block per planet).
+enum class TailForm { kNone, kBlock, kSpread, kShared, kCluster };
+template <typename T>
+TailForm tail_form(const Batch& b);
+
 }  // namespace psgb

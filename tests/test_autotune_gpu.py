@@ -189,3 +189,49 @@ def test_shared_memory_coarse_tail_equals_no_tail(planets):
             for out, its in runs[1:]:
                 assert its == runs[0][1]
                 assert all(np.array_equal(a, b) for a, b in zip(runs[0][0], out))
+
+
+def test_cluster_coarse_tail_equals_no_tail(planets):
+    """The tail on a thread-block cluster of 2, 4 or 8 blocks per planet, the levels'
+    vectors spread over the cluster's distributed shared memory, gives the same bits as no
+    tail at every tail level and cluster size that fit, with plain and block-local sweeps,
+    in both precisions; tails that do not fit fall back to another form, same bits."""
+    import planet_game_gb300 as pg
+
+    ms, inputs = planets
+    batch = pg.Batch(ms)
+    t = batch.tuning
+    depth = t["levels"]
+    for block in (1, 4):
+        t["block_sweeps"] = [1] + [block] * (depth - 1)
+        for precision, method in (("mixed", "bicgstab"), ("fp64", "pcg")):
+            runs, clustered = [], set()
+            for tail, mode, cluster in [(0, 0, 0)] + [(l, 3, c) for l in range(1, depth) for c in (2, 4, 8)]:
+                t["coarse_tail_level"], t["coarse_tail_single"], t["coarse_tail_cluster"] = tail, mode, cluster
+                batch.set_tuning(t)
+                out, reps = step(batch, inputs, precision=precision, method=method)
+                for r in reps:
+                    assert r.status == 0 and r.relative_residual <= 1e-10
+                got = batch.tuning
+                assert got["coarse_tail_single"] == mode and got["coarse_tail_cluster"] == cluster
+                if cluster and got["coarse_tail_blocks"] == len(ms) * cluster:
+                    clustered.add((tail, cluster))
+                runs.append((out, [r.iterations for r in reps]))
+            # every cluster size ran from the coarsest tail levels at least
+            assert {c for _, c in clustered} == {2, 4, 8}
+            for out, its in runs[1:]:
+                assert its == runs[0][1]
+                assert all(np.array_equal(a, b) for a, b in zip(runs[0][0], out))
+
+
+def test_cluster_tail_settings_are_checked(planets):
+    import planet_game_gb300 as pg
+
+    ms, _ = planets
+    batch = pg.Batch(ms)
+    t = batch.tuning
+    t["coarse_tail_level"], t["coarse_tail_single"] = 1, 3
+    for bad in (0, 1, 3, 16):
+        t["coarse_tail_cluster"] = bad
+        with pytest.raises(Exception, match="coarse_tail_cluster"):
+            batch.set_tuning(t)
