@@ -42,17 +42,31 @@ __device__ __forceinline__ void cluster_widths(unsigned width, F&& f) {
 // tiles. The holder of a row is its tile (within the planet) over q, by a multiply with
 // inv_q = ceil(2^16 / q) and a shift: exact while tile * q < 2^16, which the shared memory
 // bounds (q tiles of four vectors per block: q <= 55 and tiles <= 8 q).
+//
+// Every lookup is checked: a row outside the planet's slices (which no valid input makes)
+// records kClusterIndexError in the launch's error word and is redirected to a scratch
+// slot of this block, so a bad index never reaches another block's shared memory; the
+// host turns the error word into an exception after the solve.
+constexpr unsigned kClusterIndexError = 2u;
+
 template <typename T>
 struct DistVec {
     T* local;
+    T* scratch;       // this block's scratch slot for refused lookups
+    unsigned* error;  // the launch's error word
     int base;
     int span;
+    int clusters;     // blocks of the cluster
     unsigned inv_q;
-    int me;   // this block's rank in the cluster
+    int me;           // this block's rank in the cluster
     __device__ __forceinline__ T* at(int row, cg::cluster_group& cl) const {
         const int d = row - base;
         const int rank = static_cast<int>((static_cast<unsigned>(d >> 8) * inv_q) >> 16);
         const int off = d - rank * span;
+        if (d < 0 || rank >= clusters || off >= span) {
+            atomicCAS(error, 0u, kClusterIndexError);
+            return scratch;
+        }
         T* p = rank == me ? local : cl.map_shared_rank(local, static_cast<unsigned>(rank));
         return p + off;
     }
@@ -241,6 +255,7 @@ __global__ void __launch_bounds__(1024, 1) k_coarse_cluster(const __grid_constan
     // this planet's slices: per level four vectors of `span` rows in every block
     __shared__ DistLevel<T> lv[kMaxLevels];
     __shared__ int total_rows;
+    __shared__ T scratch;
     if (threadIdx.x == 0) {
     int total = 0;
     for (int l = a.first; l <= coarsest; ++l) {
@@ -250,10 +265,10 @@ __global__ void __launch_bounds__(1024, 1) k_coarse_cluster(const __grid_constan
         const int span = q * kTile;
         const unsigned inv_q = (65536u + static_cast<unsigned>(q) - 1u) / static_cast<unsigned>(q);
         T* slice = vec + total;
-        lv[l].x = DistVec<T>{slice, t0 * kTile, span, inv_q, rank};
-        lv[l].y = DistVec<T>{slice + span, t0 * kTile, span, inv_q, rank};
-        lv[l].b = DistVec<T>{slice + 2 * span, t0 * kTile, span, inv_q, rank};
-        lv[l].r = DistVec<T>{slice + 3 * span, t0 * kTile, span, inv_q, rank};
+        for (int v = 0; v < 4; ++v) {
+            DistVec<T>& dv = v == 0 ? lv[l].x : v == 1 ? lv[l].y : v == 2 ? lv[l].b : lv[l].r;
+            dv = DistVec<T>{slice + v * span, &scratch, a.error, t0 * kTile, span, C, inv_q, rank};
+        }
         lv[l].tile0 = t0;
         lv[l].tiles = nt;
         lv[l].own0 = t0 + ::min(nt, rank * q);

@@ -289,8 +289,10 @@ std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* ar
         BatchLevel& F = b.levels[l];
         BatchLevel& C = b.levels[l + 1];
         const std::size_t Pf = F.rows, Wf = F.width, Pc = C.rows, Wc = C.width;
-        // Rows without an aggregate (padding; planets whose coarsest level this is) point at
-        // coarse row 0 so that the phases may load through them; they never store.
+        // Rows without an aggregate may be loaded through but never store: a planet's padding
+        // rows point at its own first coarse row, so that every load stays within the
+        // planet's rows (the shared-memory tails hold only those); rows of planets whose
+        // coarsest level this is point at coarse row 0.
         std::vector<std::int32_t> agg(Pf, 0);
         std::vector<std::vector<std::uint32_t>> members(Pc);
         std::vector<std::vector<std::uint32_t>> lists((Wc + 1) * Pc);
@@ -299,6 +301,7 @@ std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* ar
             const HostLevel& hf = planets[i]->hierarchy.levels[l];
             const HostLevel& hc = planets[i]->hierarchy.levels[l + 1];
             const std::int64_t bf = F.base[i], bc = C.base[i];
+            for (std::uint32_t r = hf.size; r < pad_rows(hf.size); ++r) agg[bf + r] = static_cast<std::int32_t>(bc);
             for (std::uint32_t r = 0; r < hf.size; ++r) {
                 const std::uint32_t a = hf.aggregate[r];
                 const std::size_t gr = bf + r, ga = bc + a;
@@ -602,6 +605,7 @@ TailArgs<T> tail_args(Batch& b, int gate) {
     if (form == TailForm::kCluster) {
         a.cluster = b.tail_cluster;
         a.shared_rows = tail_cluster_rows(b, b.tail_level, b.tail_cluster);
+        a.error = b.sync + 3;
         b.tail_launch_blocks = b.instances * b.tail_cluster;
         return a;
     }
@@ -962,9 +966,9 @@ void solve(Batch& b, const SolveOptions& opt, const double* rhs, double* x, cuda
     InstanceScalars* host = b.pinned_scalars != nullptr ? b.pinned_scalars : b.host_scalars.data();
     PSGB_CUDA(cudaMemcpyAsync(host, b.scalars, b.instances * sizeof(InstanceScalars), cudaMemcpyDeviceToHost, st));
     unsigned barrier_error[2] = {0, 0};
-    const bool spread_tail = !persistent && (opt.precision == kMixed ? tail_form<float>(b) : tail_form<double>(b)) ==
-                                                TailForm::kSpread;
-    if (persistent || spread_tail) {
+    const TailForm form = persistent ? TailForm::kNone
+                                     : (opt.precision == kMixed ? tail_form<float>(b) : tail_form<double>(b));
+    if (persistent || form == TailForm::kSpread || form == TailForm::kCluster) {
         PSGB_CUDA(cudaMemcpyAsync(barrier_error, b.sync + 2, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     }
     PSGB_CUDA(cudaStreamSynchronize(st));
@@ -975,6 +979,8 @@ void solve(Batch& b, const SolveOptions& opt, const double* rhs, double* x, cuda
         // the per-planet barriers' state is unknown after a timeout: start them afresh
         PSGB_CUDA(cudaMemset(b.tail_barrier, 0, 2 * std::size_t(b.instances) * sizeof(unsigned)));
         PSGB_CUDA(cudaMemset(b.sync + 3, 0, sizeof(unsigned)));
+        if (form == TailForm::kCluster)
+            throw std::runtime_error("coarse tail: a row index fell outside its planet's slices of the cluster");
         throw std::runtime_error("coarse tail: a per-planet barrier wait ran past its limit");
     }
     if (host != b.host_scalars.data()) {

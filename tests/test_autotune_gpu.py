@@ -235,3 +235,34 @@ def test_cluster_tail_settings_are_checked(planets):
         t["coarse_tail_cluster"] = bad
         with pytest.raises(Exception, match="coarse_tail_cluster"):
             batch.set_tuning(t)
+
+
+def test_shared_memory_tails_on_many_planets_stay_within_each_planet(meshes):
+    """Twelve L5 planets: the later planets' coarse rows start far past their own slices
+    of the shared-memory tails, so a load through a padding row's aggregate index that
+    left the planet would fall outside the block's shared memory. Padding rows point at
+    their own planet's first coarse row; the shared-memory and cluster tails give the
+    same bits as no tail at every tail level, in both precisions."""
+    import planet_game_gb300 as pg
+    from planet_game_gb300 import workloads as W
+
+    ms = [meshes(5, 4.0e6 + 2.5e5 * i) for i in range(12)]
+    inputs = [W.step_inputs(m, seed=70 + i, edge_diffusivity=W.lognormal_edge_diffusivity(m.edge_count, 700 + i))
+              for i, m in enumerate(ms)]
+    batch = pg.Batch(ms)
+    t = batch.tuning
+    depth = t["levels"]
+    for precision, method in (("mixed", "bicgstab"), ("fp64", "pcg")):
+        runs = []
+        forms = [(0, 0, 0)] + [(l, 2, 0) for l in range(1, depth)] + [(l, 3, c) for l in range(1, depth) for c in (2, 8)]
+        for tail, mode, cluster in forms:
+            t["coarse_tail_level"], t["coarse_tail_single"], t["coarse_tail_cluster"] = tail, mode, cluster
+            batch.set_tuning(t)
+            out, reps = step(batch, inputs, precision=precision, method=method)
+            assert all(r.status == 0 and r.relative_residual <= 1e-10 for r in reps)
+            if cluster:
+                assert batch.tuning["coarse_tail_blocks"] == len(ms) * cluster
+            runs.append((out, [r.iterations for r in reps]))
+        for out, its in runs[1:]:
+            assert its == runs[0][1]
+            assert all(np.array_equal(a, b) for a, b in zip(runs[0][0], out))
