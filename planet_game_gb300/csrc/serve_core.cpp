@@ -244,11 +244,12 @@ bool Server::admit(LaneState* L, std::unique_lock<std::mutex>& lock) {
         fail_queued(L, PSGB_ERR_BUDGET, "serve: the lane's device memory exceeds the budget");
         return false;
     }
-    // idle lanes go first (least recently used first), then lanes yielding to this one
+    // idle lanes go first (least recently used first), then lanes yielding to this one;
+    // the bytes promised to lanes being admitted right now count as taken
     const double now = now_s();
     std::vector<LaneState*> victims;
     std::uint64_t freed = 0;
-    while (static_cast<double>(resident_bytes_ - freed + need) > budget_) {
+    while (static_cast<double>(resident_bytes_ + pending_bytes_ - freed + need) > budget_) {
         LaneState* victim = nullptr;
         bool victim_idle = false;
         for (auto& [level, other] : lanes_) {
@@ -274,6 +275,9 @@ bool Server::admit(LaneState* L, std::unique_lock<std::mutex>& lock) {
     stop_waiting(L);
     for (LaneState* v : victims) v->phase = Phase::Evicting;
     L->phase = Phase::Admitting;
+    // promised before the lock is let go, so that a lane admitted while the victims are
+    // evicted sees these bytes as taken (the budget holds at every moment)
+    pending_bytes_ += need;
     lock.unlock();
     for (LaneState* v : victims) {
         for (std::size_t i = 0; i < v->planets.size(); ++i) {
@@ -294,6 +298,7 @@ bool Server::admit(LaneState* L, std::unique_lock<std::mutex>& lock) {
         ++counts_.evictions;
         v->cv.notify_all();
     }
+    pending_bytes_ -= need;
     resident_bytes_ += need;
     L->bytes = need;
     lock.unlock();

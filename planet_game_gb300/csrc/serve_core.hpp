@@ -160,7 +160,8 @@ class Server {
     std::unordered_map<std::uint64_t, std::shared_ptr<Request>> requests_;
     std::vector<double> latencies_ms_;
     std::uint64_t next_request_ = 1;
-    std::uint64_t resident_bytes_ = 0;
+    std::uint64_t resident_bytes_ = 0;   // lanes holding device memory (resident, evicting or being built)
+    std::uint64_t pending_bytes_ = 0;    // promised to lanes whose victims are still being evicted
     Stats counts_;
     bool stopping_ = false;
     const std::chrono::steady_clock::time_point start_;
