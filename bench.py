@@ -542,11 +542,13 @@ def serving_sweep(args, dev, rates=SERVE_RATES) -> dict:
     srv = serve.Server(pop_b, budget_bytes=150e9, precision="mixed", **SOLVER_SERVE)
     one = serve.OneAtATime(pop_o, tuned=True, **SOLVER_SERVE)
     try:
-        srv.prepare()                                    # admit and tune every lane
-        for planets in pop_o.values():                   # one-planet batches and per-level tunings
-            for p in planets:
-                zero = torch.zeros_like(p.state)
-                one.solo.batch_of(p.mesh, p.state, zero, p.heat_capacity, p.dt, p.conductance, p.edge_conductance)
+        # both arms tuned ahead of traffic on the same representative sources
+        srv.prepare(sources=serve.typical_sources(pop_b, seed=args.seed + 5))   # admit and tune every lane
+        typical_o = serve.typical_sources(pop_o, seed=args.seed + 5)
+        for level, planets in pop_o.items():             # one-planet batches and per-level tunings
+            for p, src in zip(planets, typical_o[level]):
+                one.solo.batch_of(p.mesh, p.state, torch.from_numpy(src).to(p.state.device), p.heat_capacity, p.dt,
+                                  p.conductance, p.edge_conductance)
         warm = serve_trace(args, 5000.0, 60)
         srv.run_trace(serve.make_requests(warm, pop_b, seed=args.seed + 3), realtime=False)   # record graphs
         one.run_trace(serve.make_requests(warm, pop_o, seed=args.seed + 3), realtime=False)
@@ -597,9 +599,10 @@ def native_serving_point(args, dev, rate: float, count: int) -> dict:
             for i, p in enumerate(planets):
                 ids[(level, i)] = srv.add_planet(level, p.radius, p.heat_capacity, p.dt, p.conductance,
                                                  p.state.cpu().numpy(), p.edge_conductance)
-        for level in pop:   # admit and tune every lane
+        typical = serve.typical_sources(pop, seed=args.seed + 5)
+        for level in pop:   # admit and tune every lane, on a representative source
             pid = ids[(level, 0)]
-            srv.wait(srv.submit(pid, np.zeros(pop[level][0].mesh.cell_count)), pid)
+            srv.wait(srv.submit(pid, typical[level][0]), pid)
         for r in warm:
             pid = ids[(r.level, r.planet)]
             srv.wait(srv.submit(pid, r.source), pid)

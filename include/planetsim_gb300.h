@@ -24,7 +24,8 @@
  * PSGB_ERR_TIMEOUT. Version 4: the block step of one planet (psgb_transport_step_multi),
  * per-step reassembly (psgb_batch_set_reassembly), coarse_tail_single = 2 (the
  * shared-memory coarse tail). Version 5: coarse_tail_single = 3 and psgb_tuning's
- * coarse_tail_cluster (the coarse tail on a thread-block cluster per planet).
+ * coarse_tail_cluster (the coarse tail on a thread-block cluster per planet). Version 6:
+ * psgb_tuning's coarse_correction (the V-cycle's coarse-grid correction scale).
  *
  * A server's calls may come from any thread; its lanes step on threads of their own.
  */
@@ -38,7 +39,7 @@
 extern "C" {
 #endif
 
-#define PSGB_ABI_VERSION 5
+#define PSGB_ABI_VERSION 6
 
 /* status codes */
 #define PSGB_OK 0
@@ -497,11 +498,13 @@ typedef struct psgb_tuning {
     uint32_t coarse_tail_blocks;          /* out: blocks of the tail launch last built under these settings
                                              (before one: the launch they ask for; 0: no tail) */
     uint32_t coarse_tail_cluster;         /* coarse_tail_single = 3: blocks per planet's cluster, 2, 4 or 8 */
+    double coarse_correction;             /* scale of the coarse-grid correction, x += s P e (0 or 1: plain;
+                                             over-correction, 1.5 to 2, cuts the Krylov iterations) */
 } psgb_tuning;
 
 /* Times trial solves of one sub-step (the inputs as for psgb_batch_transport_step, every
- * planet taking part; nothing is written back) and keeps the fastest settings that meet
- * the options' tolerance on every planet. While a batch holds a tuning, its solves use
+ * planet taking part, each solve from the step's own initial guess; nothing is written
+ * back) and keeps the fastest settings that meet the options' tolerance on every planet. While a batch holds a tuning, its solves use
  * it instead of the options' uniform sweeps and damping. */
 int psgb_batch_autotune(psgb_batch* batch, const psgb_step_params* params, const psgb_solve_options* options,
                         const double* const* t0_K, const double* const* source_W_m2, int memory, void* stream,

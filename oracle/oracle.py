@@ -44,7 +44,7 @@ def lib() -> C.CDLL:
         L.orc_hierarchy_set_matrix.argtypes = [P, P, P]
         L.orc_hierarchy_values.argtypes = [P, C.c_uint64, P, P]
         L.orc_vcycle_sgs.argtypes = [P, P, P]
-        L.orc_vcycle_jacobi.argtypes = [P, C.c_int, C.c_int, C.c_double, P, P]
+        L.orc_vcycle_jacobi.argtypes = [P, C.c_int, C.c_int, C.c_double, C.c_double, P, P]
         L.orc_pcg.restype = C.c_int
         L.orc_pcg.argtypes = [P, P, C.c_double, P, P, P, C.c_double, C.c_int, P]
         L.orc_bicgstab.restype = C.c_int
@@ -251,9 +251,10 @@ class OracleHierarchy:
         lib().orc_vcycle_sgs(self.h, _p(np.ascontiguousarray(rhs, np.float64)), _p(out))
         return out
 
-    def vcycle_jacobi(self, rhs, pre=2, post=2, omega=0.8):
+    def vcycle_jacobi(self, rhs, pre=2, post=2, omega=0.8, correction=1.0):
         out = np.empty(self.om.n)
-        lib().orc_vcycle_jacobi(self.h, pre, post, omega, _p(np.ascontiguousarray(rhs, np.float64)), _p(out))
+        lib().orc_vcycle_jacobi(self.h, pre, post, omega, correction, _p(np.ascontiguousarray(rhs, np.float64)),
+                                _p(out))
         return out
 
     def pcg(self, K, slope, rhs, tol=1e-12, max_it=2000, edge_g=None):

@@ -284,8 +284,9 @@ void vcycle_sgs(const Hierarchy& h, std::size_t l, const std::vector<double>& b,
 }
 
 // The GB300 V-cycle's algorithm: damped Jacobi (pre sweeps from zero, post sweeps),
-// residual, restriction in ascending fine-row order, prolongation, dense coarsest solve.
-void vcycle_jacobi(const Hierarchy& h, std::size_t l, int pre, int post, double omega,
+// residual, restriction in ascending fine-row order, prolongation scaled by `correction`
+// (the product rounded, then added), dense coarsest solve.
+void vcycle_jacobi(const Hierarchy& h, std::size_t l, int pre, int post, double omega, double correction,
                    const std::vector<double>& b, std::vector<double>& x) {
     const Level& L = h.levels[l];
     if (l + 1 == h.levels.size()) {
@@ -311,8 +312,11 @@ void vcycle_jacobi(const Hierarchy& h, std::size_t l, int pre, int post, double 
         bc[L.agg[i]] += v;
     }
     std::vector<double> xc;
-    vcycle_jacobi(h, l + 1, pre, post, omega, bc, xc);
-    for (std::size_t i = 0; i < L.size; ++i) x[i] += xc[L.agg[i]];
+    vcycle_jacobi(h, l + 1, pre, post, omega, correction, bc, xc);
+    for (std::size_t i = 0; i < L.size; ++i) {
+        const double e = correction * xc[L.agg[i]];
+        x[i] += e;
+    }
     for (int k = 0; k < post; ++k) sweep(x);
 }
 
@@ -578,10 +582,11 @@ void orc_vcycle_sgs(void* hp, const double* rhs, double* out) {
     std::copy(x.begin(), x.end(), out);
 }
 
-void orc_vcycle_jacobi(void* hp, int pre, int post, double omega, const double* rhs, double* out) {
+void orc_vcycle_jacobi(void* hp, int pre, int post, double omega, double correction, const double* rhs,
+                       double* out) {
     const Hierarchy& h = *static_cast<Hierarchy*>(hp);
     std::vector<double> b(rhs, rhs + h.levels[0].size), x;
-    vcycle_jacobi(h, 0, pre, post, omega, b, x);
+    vcycle_jacobi(h, 0, pre, post, omega, correction, b, x);
     std::copy(x.begin(), x.end(), out);
 }
 

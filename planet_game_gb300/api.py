@@ -633,7 +633,7 @@ def _tuning_dict(t) -> dict:
             "default_solve_ms": float(t.default_solve_ms), "trial_solves": int(t.trial_solves),
             "coarse_tail_level": int(t.coarse_tail_level), "block_sweeps": list(t.block_sweeps[:n]),
             "coarse_tail_single": int(t.coarse_tail_single), "coarse_tail_blocks": int(t.coarse_tail_blocks),
-            "coarse_tail_cluster": int(t.coarse_tail_cluster)}
+            "coarse_tail_cluster": int(t.coarse_tail_cluster), "coarse_correction": float(t.coarse_correction)}
 
 
 class Batch:
@@ -717,6 +717,7 @@ class Batch:
         t.coarse_tail_level = int(tuning.get("coarse_tail_level", 0))
         t.coarse_tail_single = int(tuning.get("coarse_tail_single", 0))
         t.coarse_tail_cluster = int(tuning.get("coarse_tail_cluster", 0))
+        t.coarse_correction = float(tuning.get("coarse_correction", 1.0))
         _raise(capi.load().psgb_batch_set_tuning(self._h, C.byref(t)))
 
     def transport_step(self, t0, sources, heat_capacity, dt, conductance=None, edge_conductance=None,

@@ -115,7 +115,7 @@ class Tuning(C.Structure):
                 ("jacobi_omega", C.c_double), ("tuned_solve_ms", C.c_double), ("default_solve_ms", C.c_double),
                 ("trial_solves", C.c_int), ("coarse_tail_level", C.c_int), ("block_sweeps", C.c_int * MAX_LEVELS),
                 ("coarse_tail_single", C.c_int), ("coarse_tail_blocks", C.c_uint32),
-                ("coarse_tail_cluster", C.c_uint32)]
+                ("coarse_tail_cluster", C.c_uint32), ("coarse_correction", C.c_double)]
 
 
 class SolveReport(C.Structure):

@@ -116,7 +116,8 @@ void tune_shapes(Batch& b, cudaStream_t st) {
 struct Sweeps {
     std::vector<int> pre, post;
     double omega;
-    std::vector<int> inner;   // empty: one sweep per launch everywhere
+    std::vector<int> inner;    // empty: one sweep per launch everywhere
+    double correction = 1.0;   // coarse-grid correction scale
 };
 
 void set_sweeps(Batch& b, const Sweeps& s) {
@@ -124,6 +125,7 @@ void set_sweeps(Batch& b, const Sweeps& s) {
     b.smoother.level_post = s.post;
     b.smoother.level_inner = s.inner;
     b.smoother.omega = s.omega;
+    b.smoother.correction = s.correction;
 }
 
 bool all_ok(const Batch& b) {
@@ -132,11 +134,16 @@ bool all_ok(const Batch& b) {
     return true;
 }
 
-// Wall time of one solve from x = 0 (ms); negative if some planet missed its tolerance.
-double trial(Batch& b, const SolveOptions& opt, const double* rhs, double* x, std::size_t rows, cudaStream_t st,
-             int& count) {
+// Wall time of one solve (ms) from the initial guess x0 (null: zero); negative if some
+// planet missed its tolerance.
+double trial(Batch& b, const SolveOptions& opt, const double* rhs, const double* x0, double* x, std::size_t rows,
+             cudaStream_t st, int& count) {
     ++count;
-    PSGB_CUDA(cudaMemsetAsync(x, 0, rows * sizeof(double), st));
+    if (x0 != nullptr) {
+        PSGB_CUDA(cudaMemcpyAsync(x, x0, rows * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    } else {
+        PSGB_CUDA(cudaMemsetAsync(x, 0, rows * sizeof(double), st));
+    }
     PSGB_CUDA(cudaStreamSynchronize(st));
     const auto t0 = std::chrono::steady_clock::now();
     solve(b, opt, rhs, x, st);
@@ -158,6 +165,7 @@ Tuning current_tuning(const Batch& b) {
         t.sets_vector.push_back(b.levels[l].sets_vector);
     }
     t.omega = b.smoother.omega;
+    t.correction = b.smoother.correction;
     t.tail_level = b.tail_level;
     t.tail_spread = b.tail_spread;
     t.tail_shared = b.tail_shared;
@@ -186,6 +194,8 @@ void apply_tuning(Batch& b, const Tuning& t) {
             throw std::invalid_argument("tuned tile sets must be 1 or 2 (stencil) and 1 or 4 (vector)");
     }
     if (!(t.omega > 0.0 && t.omega < 2.0)) throw std::invalid_argument("tuned damping must be in (0, 2)");
+    if (!(t.correction > 0.0 && t.correction <= 4.0))
+        throw std::invalid_argument("the coarse-grid correction scale must be in (0, 4]");
     if (t.tail_level < 0 || static_cast<std::size_t>(t.tail_level) >= depth)
         throw std::invalid_argument("the coarse tail level must be 0 (none) or a level below the fine one");
     if (t.tail_cluster != 0 && t.tail_cluster != 2 && t.tail_cluster != 4 && t.tail_cluster != 8)
@@ -198,6 +208,7 @@ void apply_tuning(Batch& b, const Tuning& t) {
     b.smoother.level_post = t.post;
     b.smoother.level_inner = t.inner;
     b.smoother.omega = t.omega;
+    b.smoother.correction = t.correction;
     b.tail_level = t.tail_level;
     b.tail_spread = t.tail_spread;
     b.tail_shared = t.tail_shared;
@@ -210,11 +221,12 @@ void clear_tuning(Batch& b) {
     b.smoother.level_pre.clear();
     b.smoother.level_post.clear();
     b.smoother.level_inner.clear();
+    b.smoother.correction = 1.0;
     default_launch_shapes(b);
     b.tuned = false;
 }
 
-Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x, cudaStream_t st) {
+Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, const double* x0, double* x, cudaStream_t st) {
     if (!b.matrix_ready) throw std::logic_error("autotune before the matrix was set");
     if (profile_active()) throw std::logic_error("autotune while a profile records");
     const std::size_t depth = b.levels.size(), rows = b.levels[0].rows;
@@ -224,8 +236,8 @@ Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x,
                         b.smoother.omega, {}};
     set_sweeps(b, before);
     default_launch_shapes(b);
-    trial(b, opt, rhs, x, rows, st, result.trials);
-    result.default_ms = trial(b, opt, rhs, x, rows, st, result.trials);
+    trial(b, opt, rhs, x0, x, rows, st, result.trials);
+    result.default_ms = trial(b, opt, rhs, x0, x, rows, st, result.trials);
 
     // 1. launch shapes (result-neutral)
     if (opt.precision == kMixed) tune_shapes<float>(b, st);
@@ -234,8 +246,8 @@ Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x,
     // 2. sweeps: uniform candidates, then coarse-level variants of the best
     auto run = [&](const Sweeps& s) {
         set_sweeps(b, s);
-        if (trial(b, opt, rhs, x, rows, st, result.trials) < 0.0) return -1.0;
-        return trial(b, opt, rhs, x, rows, st, result.trials);
+        if (trial(b, opt, rhs, x0, x, rows, st, result.trials) < 0.0) return -1.0;
+        return trial(b, opt, rhs, x0, x, rows, st, result.trials);
     };
     Sweeps best = before;
     double best_ms = run(before);
@@ -273,18 +285,22 @@ Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x,
         }
     }
     // block-local sweeps on the coarse levels: several Jacobi sweeps per launch
-    if (depth > 1) {
-        // (pre launches + 1, post launches + 1, sweeps per launch): fewer, longer launches
-        // trade the latency of a launch against tile-local coupling
-        const int block[][3] = {{2, 2, 2}, {2, 2, 3}, {2, 2, 4}, {3, 3, 2}, {3, 3, 3},
-                                {2, 2, 6}, {2, 2, 8}, {2, 1, 6}, {2, 1, 8}};
+    // (pre launches + 1, post launches + 1, sweeps per launch): fewer, longer launches trade
+    // the latency of a launch against tile-local coupling
+    const int block[][3] = {{2, 2, 2}, {2, 2, 3}, {2, 2, 4}, {3, 3, 2}, {3, 3, 3},
+                            {2, 2, 6}, {2, 2, 8}, {2, 1, 6}, {2, 1, 8}};
+    const auto try_block_sweeps = [&] {
         const Sweeps base = best;
         for (const auto& c : block) {
             Sweeps s = base;
             s.inner.assign(depth, 1);
             for (std::size_t l = 1; l < depth; ++l) { s.pre[l] = c[0]; s.post[l] = c[1]; s.inner[l] = c[2]; }
+            if (s.pre == base.pre && s.post == base.post && s.inner == base.inner) continue;
             consider(s);
         }
+    };
+    if (depth > 1) {
+        try_block_sweeps();
         // then the levels below the first coarse one on their own: the smallest levels
         // are pure latency, fewer launches may beat more smoothing there
         if (depth > 2 && !best.inner.empty()) {
@@ -304,6 +320,17 @@ Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x,
         Sweeps s = best;
         s.omega = omega;
         consider(s);
+    }
+    // over-correction of the coarse-grid correction, then the coarse sweeps again under the
+    // chosen scale (a stronger correction may do with fewer or shorter sweeps)
+    if (depth > 1) {
+        const Sweeps base = best;
+        for (double c : {1.5, 2.0}) {
+            Sweeps s = base;
+            s.correction = c;
+            consider(s);
+        }
+        if (best.correction != base.correction) try_block_sweeps();
     }
     // where the coarse tail starts, with the chosen sweeps (whole solves: the tail's cost
     // depends on how many sweeps its levels run)
@@ -353,6 +380,7 @@ Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x,
     result.post = best.post;
     result.inner = best.inner.empty() ? std::vector<int>(depth, 1) : best.inner;
     result.omega = best.omega;
+    result.correction = best.correction;
     for (std::size_t l = 0; l < depth; ++l) {
         result.sets_stencil.push_back(b.levels[l].sets_stencil);
         result.sets_vector.push_back(b.levels[l].sets_vector);

@@ -16,6 +16,7 @@ struct Tuning {
     std::vector<std::uint8_t> sets_stencil;        // per level: 1 or 2
     std::vector<std::uint8_t> sets_vector;         // per level: 1 or 4
     double omega = 0.8;
+    double correction = 1.0;                       // coarse-grid correction scale
     int tail_level = 0;                            // coarse tail from this level (0: none)
     bool tail_spread = true;                       // several blocks per large planet in the tail
     bool tail_shared = false;                      // one block per planet, the tail levels' vectors in shared memory
@@ -28,9 +29,10 @@ struct Tuning {
 };
 
 // Tunes `b` on the system its matrix holds with right-hand side `rhs` (device, fine
-// layout); `x` is device scratch of the fine layout. Leaves the chosen settings applied
-// (b.tuned) and returns them.
-Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, double* x, cudaStream_t st);
+// layout), every trial solve starting from `x0` (the step's own initial guess, the
+// temperature before the step; null: zero); `x` is device scratch of the fine layout.
+// Leaves the chosen settings applied (b.tuned) and returns them.
+Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, const double* x0, double* x, cudaStream_t st);
 
 // The batch's current settings.
 Tuning current_tuning(const Batch& b);

@@ -914,6 +914,7 @@ void fill_tuning(const psgb::Tuning& t, psgb_tuning* out) {
     out->coarse_tail_single = t.tail_cluster != 0 ? 3 : t.tail_shared ? 2 : (t.tail_spread ? 0 : 1);
     out->coarse_tail_blocks = t.tail_blocks;
     out->coarse_tail_cluster = t.tail_cluster;
+    out->coarse_correction = t.correction;
 }
 
 }  // namespace
@@ -942,8 +943,10 @@ int psgb_batch_autotune(psgb_batch* h, const psgb_step_params* params, const psg
             copy_in(b.t0 + b.fine_base[i], t0_K[i], n * 8, memory, st);
             copy_in(b.src + b.fine_base[i], source_W_m2[i], n * 8, memory, st);
         }
+        // the trials solve exactly what a step solves: its right-hand side, from its
+        // initial guess (the temperature before the step)
         psgb::launch_step_rhs(step_view(b), b.t0, b.src, b.bb, b.tmp, b.xr, st);
-        const psgb::Tuning t = psgb::autotune(b, opt, b.bb, b.tmp2, st);
+        const psgb::Tuning t = psgb::autotune(b, opt, b.bb, b.xr, b.tmp2, st);
         if (out != nullptr) fill_tuning(t, out);
         return PSGB_OK;
     });
@@ -1008,6 +1011,7 @@ int psgb_batch_set_tuning(psgb_batch* h, const psgb_tuning* tuning) {
             t.inner.push_back(tuning->block_sweeps[l] == 0 ? 1 : tuning->block_sweeps[l]);
         }
         t.omega = tuning->jacobi_omega;
+        t.correction = tuning->coarse_correction == 0.0 ? 1.0 : tuning->coarse_correction;
         t.tail_level = tuning->coarse_tail_level;
         require(tuning->coarse_tail_single >= 0 && tuning->coarse_tail_single <= 3,
                 "coarse_tail_single must be 0, 1, 2 or 3");

@@ -206,13 +206,13 @@ __device__ void c_prolong_smooth(const LevelView<T>& lv, int tile, int lane, con
 #pragma unroll
     for (int j = 0; j < W; ++j) {
         const int c = lv.col[j * P + row];
-        s -= lv.vd[j * P + row] * (*x.at(c, cl) + *e.at(agg[c], cl));
+        s -= lv.vd[j * P + row] * (*x.at(c, cl) + ph::prod(lv.correction, *e.at(agg[c], cl)));
     }
     T out;
     if (omega == T(1)) {
         out = lv.inv[row] * s;
     } else {
-        const T xo = *x.at(row, cl) + *e.at(agg[row], cl);
+        const T xo = *x.at(row, cl) + ph::prod(lv.correction, *e.at(agg[row], cl));
         out = xo + omega * (lv.inv[row] * s - xo);
     }
     *y.at(row, cl) = out;
@@ -224,7 +224,7 @@ __device__ void c_prolong(const LevelView<T>& lv, int tile, int lane, const std:
     const ph::TileSet<1> ts = ph::tile_set<1>(lv.tile_meta, lv.tiles, tile);
     if (lane >= ts.rows[0] || !ts.sweep[0]) return;
     const int row = ts.tile[0] * kTile + lane;
-    *x.at(row, cl) += *xc.at(agg[row], cl);
+    *x.at(row, cl) += ph::prod(lv.correction, *xc.at(agg[row], cl));
 }
 
 template <typename T>

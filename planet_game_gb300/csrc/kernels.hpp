@@ -57,6 +57,7 @@ struct LevelView {
     std::uint8_t sets_stencil;        // tiles per tile set of the stencil launches (1 or 2)
     std::uint8_t sets_vector;         // tiles per tile set of the vector launches (1 or 4)
     std::uint8_t level;               // multigrid level (0: fine)
+    T correction = T(1);              // scale of the coarse-grid correction prolongated into this level
 };
 
 struct ReduceCtx {

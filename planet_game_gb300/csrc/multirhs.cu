@@ -252,12 +252,12 @@ __global__ void k_prolong_smooth(LevelView<T> L, const std::int32_t* __restrict_
 #pragma unroll
             for (int j = 0; j < W; ++j) {
                 const int c = m.col[j][local];
-                s -= m.val[j][local] * (x[at(c, lane)] + e[at(agg[c], lane)]);
+                s -= m.val[j][local] * (x[at(c, lane)] + ph::prod(L.correction, e[at(agg[c], lane)]));
             }
             if (omega == T(1)) {
                 out[i] = m.inv[local] * s;
             } else {
-                const T xo = x[at(row, lane)] + e[at(agg[row], lane)];
+                const T xo = x[at(row, lane)] + ph::prod(L.correction, e[at(agg[row], lane)]);
                 out[i] = xo + omega * (m.inv[local] * s - xo);
             }
         }
@@ -282,7 +282,7 @@ __global__ void k_prolong(LevelView<T> L, const std::int32_t* __restrict__ agg, 
         const int local = warp * 32 + k;
         if (local >= ti.rows) break;
         const int row = tile * kTile + local;
-        x[at(row, lane)] += xc[at(agg[row], lane)];
+        x[at(row, lane)] += ph::prod(L.correction, xc[at(agg[row], lane)]);
     }
 }
 

@@ -581,12 +581,12 @@ __device__ void prolong_smooth(const LevelView<T>& lv, int t0, int lane, const s
 #pragma unroll
         for (int j = 0; j < W; ++j) {
             const int c = lv.col[j * P + row];
-            s -= lv.vd[j * P + row] * (x[c] + e[agg[c]]);
+            s -= lv.vd[j * P + row] * (x[c] + prod(lv.correction, e[agg[c]]));
         }
         if (omega == T(1)) {
             out[k] = lv.inv[row] * s;
         } else {
-            const T xo = x[row] + e[agg[row]];
+            const T xo = x[row] + prod(lv.correction, e[agg[row]]);
             out[k] = xo + omega * (lv.inv[row] * s - xo);
         }
     }
@@ -611,7 +611,7 @@ __device__ void prolong(const LevelView<T>& lv, int t0, int lane, const std::int
         count_bytes(lv.bytes, lane, static_cast<unsigned long long>(ts.rows[k]) * (4ull + 2ull * sizeof(T)));
         if (lane >= ts.rows[k]) continue;
         const int row = ts.tile[k] * kTile + lane;
-        x[row] += xc[agg[row]];
+        x[row] += prod(lv.correction, xc[agg[row]]);
     }
 }
 

@@ -54,10 +54,10 @@ struct Tunings {
 class GpuLane final : public Lane {
   public:
     GpuLane(const psgb_server_config& cfg, std::uint32_t level, const std::vector<PlanetRecord*>& planets,
-            Tunings& tunings)
+            const std::vector<const double*>& first_sources, Tunings& tunings)
         : options_(cfg.options) {
         try {
-            build(cfg, level, planets, tunings);
+            build(cfg, level, planets, first_sources, tunings);
         } catch (...) {
             release();   // a partly built lane frees what it holds
             throw;
@@ -101,7 +101,7 @@ class GpuLane final : public Lane {
 
   private:
     void build(const psgb_server_config& cfg, std::uint32_t level, const std::vector<PlanetRecord*>& planets,
-               Tunings& tunings) {
+               const std::vector<const double*>& first_sources, Tunings& tunings) {
         const std::size_t n = planets.size();
         std::vector<psgb_planet*> handles(n);
         std::size_t total = 0;
@@ -118,6 +118,12 @@ class GpuLane final : public Lane {
             PSGB_CUDA(cudaMemcpyAsync(states_ + offset_[i], planets[i]->state_K.data(), cells_[i] * sizeof(double),
                                       cudaMemcpyHostToDevice, stream_));
         PSGB_CUDA(cudaMemsetAsync(sources_, 0, total * sizeof(double), stream_));
+        // a lane tuned at admission tunes on the requests it was admitted for (zero
+        // sources elsewhere: those planets converge at once and do not set the pace)
+        for (std::size_t i = 0; i < n && i < first_sources.size(); ++i)
+            if (first_sources[i] != nullptr)
+                PSGB_CUDA(cudaMemcpyAsync(sources_ + offset_[i], first_sources[i], cells_[i] * sizeof(double),
+                                          cudaMemcpyHostToDevice, stream_));
         check(psgb_batch_create(handles.data(), static_cast<std::uint32_t>(n), &batch_));
         params_.resize(n);
         std::vector<const double*> edges(n, nullptr);
@@ -196,8 +202,9 @@ class GpuBackend final : public Backend {
         for (const PlanetRecord* p : planets) cells += p->cells;
         return static_cast<std::uint64_t>(std::ceil(cells * cfg_.bytes_per_cell));
     }
-    std::unique_ptr<Lane> admit(std::uint32_t level, const std::vector<PlanetRecord*>& planets) override {
-        return std::make_unique<GpuLane>(cfg_, level, planets, tunings_);
+    std::unique_ptr<Lane> admit(std::uint32_t level, const std::vector<PlanetRecord*>& planets,
+                                const std::vector<const double*>& first_sources) override {
+        return std::make_unique<GpuLane>(cfg_, level, planets, first_sources, tunings_);
     }
     void thread_start() override { PSGB_CUDA(cudaSetDevice(cfg_.device)); }
 

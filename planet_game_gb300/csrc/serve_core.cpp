@@ -273,6 +273,15 @@ bool Server::admit(LaneState* L, std::unique_lock<std::mutex>& lock) {
         freed += victim->bytes;
     }
     stop_waiting(L);
+    // the requests the lane is admitted for (held, so their sources outlive the unlock;
+    // they leave the queue only in this lane's own rounds)
+    std::vector<std::shared_ptr<Request>> firsts(L->planets.size());
+    std::vector<const double*> first_sources(L->planets.size(), nullptr);
+    for (std::size_t i = 0; i < L->planets.size(); ++i) {
+        if (L->queue[i].empty()) continue;
+        firsts[i] = L->queue[i].front();
+        first_sources[i] = firsts[i]->source.data();
+    }
     for (LaneState* v : victims) v->phase = Phase::Evicting;
     L->phase = Phase::Admitting;
     // promised before the lock is let go, so that a lane admitted while the victims are
@@ -306,7 +315,7 @@ bool Server::admit(LaneState* L, std::unique_lock<std::mutex>& lock) {
     int status = PSGB_OK;
     std::string message;
     try {
-        made = backend_->admit(L->level, recs);
+        made = backend_->admit(L->level, recs, first_sources);
         if (!made) throw std::logic_error("serve: the backend admitted no lane");
     } catch (...) {
         status = mapper_(std::current_exception(), message);

@@ -71,7 +71,10 @@ class Backend {
     // Device bytes reserved for a lane of these planets while it is resident.
     virtual std::uint64_t lane_bytes(const std::vector<const PlanetRecord*>& planets) = 0;
     // Makes the lane resident: its planets' batch, and their states taken from state_K.
-    virtual std::unique_ptr<Lane> admit(std::uint32_t level, const std::vector<PlanetRecord*>& planets) = 0;
+    // `first_sources`: per planet, the source of its oldest queued request (null: none),
+    // the work the lane is admitted for (a backend that tunes its lanes tunes on these).
+    virtual std::unique_ptr<Lane> admit(std::uint32_t level, const std::vector<PlanetRecord*>& planets,
+                                        const std::vector<const double*>& first_sources) = 0;
     // Called on a lane's worker thread before its first round (the GPU backend selects
     // the device there).
     virtual void thread_start() {}

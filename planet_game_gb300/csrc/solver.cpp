@@ -523,12 +523,16 @@ StepView step_view(const Batch& b) {
 
 LevelView<double> view64(const Batch& b, std::size_t level) {
     const BatchLevel& L = b.levels[level];
-    return make_view<double>(L, L.vd64, L.inv64, level);
+    LevelView<double> v = make_view<double>(L, L.vd64, L.inv64, level);
+    v.correction = b.smoother.correction;
+    return v;
 }
 
 LevelView<float> view32(const Batch& b, std::size_t level) {
     const BatchLevel& L = b.levels[level];
-    return make_view<float>(L, L.vd32, L.inv32, level);
+    LevelView<float> v = make_view<float>(L, L.vd32, L.inv32, level);
+    v.correction = static_cast<float>(b.smoother.correction);
+    return v;
 }
 
 namespace {
@@ -812,7 +816,8 @@ void krylov_chunk(Batch& b, int method, int count, T* rhs_unused, T* x, cudaStre
 // The chunk as a CUDA graph, recorded once per (precision, method, chunk, smoother).
 template <typename T>
 GraphEntry& chunk_graph(Batch& b, int method, int count, T* x, cudaStream_t st) {
-    const GraphKey key{static_cast<int>(sizeof(T)), method, count, shape_of(b), b.smoother.omega};
+    const GraphKey key{static_cast<int>(sizeof(T)), method, count, shape_of(b), b.smoother.omega,
+                       b.smoother.correction};
     GraphEntry& g = b.graphs[key];
     if (g.exec != nullptr) return g;
     cudaGraph_t graph = nullptr;

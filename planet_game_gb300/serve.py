@@ -78,20 +78,31 @@ def build_population(per_level: int, levels=(4, 5, 6, 7, 8), seed: int = 7, devi
     return population
 
 
+def request_source(p: PlanetState, rng) -> np.ndarray:
+    """A request's source term for planet `p` (W/m^2): absorbed sub-step-mean insolation
+    less a linearised outgoing flux of a latitude-dependent temperature, plus noise."""
+    if not hasattr(p, "_q"):
+        p._lat = W.latitude(p.mesh.arrays()["center"])
+        p._q = p.mesh.substep_mean_insolation(0).astype(np.float64)
+    base_t = 288.0 - 40.0 * np.sin(p._lat) ** 2
+    return 0.7 * p._q - (203.3 + 2.09 * (base_t - 273.15)) + rng.normal(0.0, 5.0, len(p._lat))
+
+
 def make_requests(trace, population, seed: int = 11):
     """Requests of a trace: each carries a source term for its planet (seeded)."""
     rng = np.random.default_rng(seed)
     out = []
     for r in trace:
-        p = population[r.level][r.planet % len(population[r.level])]
-        if not hasattr(p, "_q"):
-            p._lat = W.latitude(p.mesh.arrays()["center"])
-            p._q = p.mesh.substep_mean_insolation(0).astype(np.float64)
-        lat = p._lat
-        base_t = 288.0 - 40.0 * np.sin(lat) ** 2
-        src = 0.7 * p._q - (203.3 + 2.09 * (base_t - 273.15)) + rng.normal(0.0, 5.0, len(lat))
-        out.append(ServedRequest(r.arrival_s, r.level, r.planet % len(population[r.level]), src))
+        k = r.planet % len(population[r.level])
+        out.append(ServedRequest(r.arrival_s, r.level, k, request_source(population[r.level][k], rng)))
     return out
+
+
+def typical_sources(population, seed: int = 13) -> dict:
+    """One source per planet, drawn as requests draw theirs: what lanes (and the
+    comparator's one-planet batches) are tuned on ahead of traffic."""
+    rng = np.random.default_rng(seed)
+    return {level: [request_source(p, rng) for p in planets] for level, planets in sorted(population.items())}
 
 
 class _Lane:
@@ -191,8 +202,10 @@ class Server:
         cells = sum(p.mesh.cell_count for p in self.population[level])
         return int(cells * 700)   # measured layout cost per cell of a mixed-precision batch, with margin
 
-    def _admit(self, level) -> _Lane | None:
-        """Lane of `level`, built if the budget allows (evicting idle lanes); None: wait."""
+    def _admit(self, level, sources=None) -> _Lane | None:
+        """Lane of `level`, built if the budget allows (evicting idle lanes); None: wait.
+        `sources` ({planet index: host source}): the work the lane is admitted for, which a
+        lane tuned at admission is tuned on (zero sources elsewhere)."""
         lane = self.lanes.get(level)
         if lane is not None and lane.batch is not None:
             return lane
@@ -218,34 +231,41 @@ class Server:
             lane.edge_conductance = "stored"
         if self.autotune:
             if level not in self.tunings:
-                self.tunings[level] = self._tune(lane.batch, level)
+                self.tunings[level] = self._tune(lane.batch, level, sources)
             else:
                 lane.batch.set_tuning(self.tunings[level])
         lane.bytes = need
         self.resident_bytes += need
         return lane
 
-    def _tune(self, batch, level) -> dict:
-        """Per-level settings for a lane, from trial solves of a step of its planets."""
+    def _tune(self, batch, level, sources=None) -> dict:
+        """Per-level settings for a lane, from trial solves of a step of its planets with
+        `sources` ({planet index: host source}; zero for the others: they converge at once
+        and do not set the pace)."""
         import torch
 
         planets = self.population[level]
-        zeros = [torch.zeros_like(p.state) for p in planets]
-        return batch.autotune([p.state for p in planets], zeros, [p.heat_capacity for p in planets],
+        sources = sources or {}
+        src = [torch.from_numpy(np.ascontiguousarray(sources[i], np.float64)).to(p.state.device) if i in sources
+               else torch.zeros_like(p.state) for i, p in enumerate(planets)]
+        return batch.autotune([p.state for p in planets], src, [p.heat_capacity for p in planets],
                               [p.dt for p in planets], conductance=[p.conductance for p in planets],
                               edge_conductance=self.lanes[level].edge_conductance, **self.options)
 
-    def prepare(self, levels=None):
-        """Admit (and tune) the lanes of `levels` ahead of traffic, as far as the budget allows."""
+    def prepare(self, levels=None, sources=None):
+        """Admit (and tune) the lanes of `levels` ahead of traffic, as far as the budget
+        allows; `sources` ({level: [host source per planet]}, e.g. typical_sources) is what
+        they are tuned on."""
         with self.lock:
             for level in (levels if levels is not None else sorted(self.population)):
-                if self._admit(level) is None:
+                per = dict(enumerate(sources[level])) if sources is not None and level in sources else None
+                if self._admit(level, per) is None:
                     break
 
     def submit(self, req: ServedRequest) -> bool:
         """Queue a request; False if its lane cannot be admitted yet (memory)."""
         with self.lock:
-            lane = self._admit(req.level)
+            lane = self._admit(req.level, {req.planet: req.source})
             if lane is None:
                 return False
             lane.pending[req.planet].append(req)

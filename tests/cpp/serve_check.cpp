@@ -31,6 +31,7 @@ struct Counters {
     std::atomic<int> fail_level{-1};          // a step of this level throws
     std::atomic<int> fail_admit_level{-1};    // admission of this level throws
     std::atomic<int> max_round_size{0};
+    std::atomic<int> admitted_with_work{0};
 };
 
 class FakeLane final : public Lane {
@@ -84,9 +85,14 @@ class FakeBackend final : public Backend {
         for (const PlanetRecord* p : planets) cells += p->cells;
         return cells * per_cell_;
     }
-    std::unique_ptr<Lane> admit(std::uint32_t level, const std::vector<PlanetRecord*>& planets) override {
+    std::unique_ptr<Lane> admit(std::uint32_t level, const std::vector<PlanetRecord*>& planets,
+                                const std::vector<const double*>& first_sources) override {
         if (static_cast<int>(level) == c_.fail_admit_level.load()) throw std::invalid_argument("cannot build the lane");
         ++c_.admissions;
+        // a lane is admitted for queued work: some planet's oldest source comes along
+        bool any = false;
+        for (const double* s : first_sources) any = any || s != nullptr;
+        if (any && first_sources.size() == planets.size()) ++c_.admitted_with_work;
         return std::make_unique<FakeLane>(c_, level, planets);
     }
 
@@ -163,6 +169,7 @@ void continuous_batching_and_order() {
     const Stats st = s.stats();
     CHECK(st.submitted == ids.size() * per_planet && st.completed == st.submitted && st.failed == 0);
     CHECK(st.admissions == 3 && st.evictions == 0 && st.resident_lanes == 3);
+    CHECK(c.admitted_with_work.load() == 3);     // each lane admitted with its first requests' sources
     CHECK(st.rounds < st.submitted);                 // requests of several planets shared rounds
     CHECK(c.max_round_size.load() == 3);             // a round steps every planet of its level with work
     CHECK(c.max_concurrent.load() >= 2);             // lanes stepped side by side

@@ -266,3 +266,44 @@ def test_shared_memory_tails_on_many_planets_stay_within_each_planet(meshes):
         for out, its in runs[1:]:
             assert its == runs[0][1]
             assert all(np.array_equal(a, b) for a, b in zip(runs[0][0], out))
+
+
+def test_scaled_coarse_correction_same_bits_on_every_schedule_and_meets_the_oracle(planets):
+    """With the V-cycle's coarse-grid correction scaled (over-correction, 1.5 and 2), every
+    tail form and the persistent schedule give the kernel schedule's bits, in both
+    precisions, and every planet's step meets the oracle's FP64 solve within 2e-6 K."""
+    import planet_game_gb300 as pg
+    from oracle import oracle as O
+
+    ms, inputs = planets
+    batch = pg.Batch(ms)
+    t = batch.tuning
+    for correction in (1.5, 2.0):
+        t["coarse_correction"] = correction
+        for precision, method in (("mixed", "bicgstab"), ("fp64", "pcg")):
+            runs = []
+            for tail, mode, cluster in ((0, 0, 0), (1, 1, 0), (1, 0, 0), (1, 2, 0), (1, 3, 4), (2, 2, 0)):
+                t["coarse_tail_level"], t["coarse_tail_single"], t["coarse_tail_cluster"] = tail, mode, cluster
+                batch.set_tuning(t)
+                assert batch.tuning["coarse_correction"] == correction
+                out, reps = step(batch, inputs, precision=precision, method=method)
+                assert all(r.status == 0 and r.relative_residual <= 1e-10 and r.closure <= 1e-12 for r in reps)
+                runs.append((out, [r.iterations for r in reps]))
+            t["coarse_tail_level"], t["coarse_tail_single"], t["coarse_tail_cluster"] = 0, 0, 0
+            batch.set_tuning(t)
+            out, reps = step(batch, inputs, precision=precision, method=method, schedule="persistent")
+            runs.append((out, [r.iterations for r in reps]))
+            for out, its in runs[1:]:
+                assert its == runs[0][1]
+                assert all(np.array_equal(a, b) for a, b in zip(runs[0][0], out))
+            if correction == 2.0 and precision == "mixed":
+                for m, inp, got in zip(ms, inputs, runs[0][0]):
+                    om = O.OracleMesh(m.arrays())
+                    ref = O.OracleHierarchy(om).transport_step(
+                        0.0, 4e7, inputs[0].dt, inp.t0, inp.source, tol=1e-13,
+                        edge_g=om.directed_conductance(inp.edge_conductance))
+                    assert np.max(np.abs(got - ref["t_new"])) <= 2e-6
+    # the plain V-cycle again: the scale is part of the settings, not left behind
+    t["coarse_correction"] = 1.0
+    batch.set_tuning(t)
+    assert batch.tuning["coarse_correction"] == 1.0
