@@ -237,8 +237,8 @@ def run_gb300(args, rank, world, local_rank):
     meshes = [m for m, _ in planets]
     cells = sum(m.cell_count for m in meshes)
     prec = precision_for(args.workload)
-    # the planets of the mix's highest level in a lane of their own (pg.default_lanes):
-    # they need the most Krylov iterations, and the lanes run side by side
+    # the planets of the mix's highest level in lanes of their own, at most four each
+    # (pg.default_lanes): they need the most Krylov iterations, and the lanes run side by side
     batch = pg.LaneBatch(meshes)
     batch.concurrent = not args.serial_lanes
     t0_d = [torch.from_numpy(inp.t0).to(dev) for _, inp in planets]

@@ -127,3 +127,9 @@ def test_default_lanes_split_the_highest_level():
     assert pg.default_lanes(ms) == [[0, 2, 3, 5], [1, 4]]
     assert pg.default_lanes([SimpleNamespace(subdivision=l) for l in (5, 6, 5)]) == [[0, 1, 2]]
     assert pg.default_lanes([SimpleNamespace(subdivision=8)]) == [[0]]
+    # the highest level's planets in lanes of at most four, split evenly
+    mix = [SimpleNamespace(subdivision=l) for l in [4, 5, 6] + [7] * 8]
+    assert pg.default_lanes(mix) == [[0, 1, 2], [3, 5, 7, 9], [4, 6, 8, 10]]
+    mix = [SimpleNamespace(subdivision=l) for l in [4, 6] + [7] * 5]
+    assert pg.default_lanes(mix) == [[0, 1], [2, 4, 6], [3, 5]]
+    assert pg.default_lanes(mix, top_lane_planets=8) == [[0, 1], [2, 3, 4, 5, 6]]
