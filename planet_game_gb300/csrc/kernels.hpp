@@ -128,6 +128,13 @@ template <typename T>
 void launch_restrict_zero(const LevelView<T>& coarse, const std::uint32_t* member_offset,
                           const std::uint32_t* member, const T* r, T* bc, T* xc, T omega,
                           const InstanceScalars* sc, int gate, cudaStream_t stream);
+// A coarse level's residual fused with the restriction into the next level and that
+// level's zero-start sweep (same bits as launch_residual then launch_restrict_zero; the
+// residual is not stored), with the dense blocks of launch_residual.
+template <typename T>
+void launch_residual_restrict(const LevelView<T>& lv, const LevelView<T>& coarse, const std::uint32_t* member_offset,
+                              const std::uint32_t* member, const T* b, const T* x, T* bc, T* xc, T omega,
+                              const InstanceScalars* sc, int gate, cudaStream_t stream, const DenseTask<T>& dense);
 template <typename T>
 void launch_prolong_smooth(const LevelView<T>& lv, const std::int32_t* agg, const T* e, const T* b, const T* x,
                            T* y, T omega, const InstanceScalars* sc, int gate, cudaStream_t stream);

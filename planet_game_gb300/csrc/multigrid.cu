@@ -230,6 +230,53 @@ __global__ void k_restrict_zero(LevelView<T> coarse, const std::uint32_t* __rest
                                           sc, gate);
 }
 
+// A coarse level's residual and the restriction into the next level in one launch: a warp
+// per next-level row, lane m forming the residual of the row's member m exactly as
+// k_residual does (same terms, same order), then the members' residuals summed in
+// ascending order as k_restrict_zero sums them, and the next level's zero-start sweep.
+// The residual vector is never stored. Extra blocks past the rows solve the dense
+// coarsest levels of planets whose coarsest level is this one, as k_residual's do.
+constexpr int kWarpsPerBlock = kTile / 32;
+
+template <typename T, int W>
+__global__ void k_residual_restrict(LevelView<T> lv, LevelView<T> coarse, const std::uint32_t* __restrict__ moff,
+                                    const std::uint32_t* __restrict__ member, const T* __restrict__ b,
+                                    const T* __restrict__ x, T* __restrict__ bc, T* __restrict__ xc, T omega,
+                                    const InstanceScalars* sc, int gate, DenseTask<T> dense) {
+    pdl_begin();
+    const unsigned blocks = (coarse.rows + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    if (blockIdx.x >= blocks) {
+        ph::dense_block<T>(dense, blockIdx.x - blocks, threadIdx.x, sc, gate);
+        return;
+    }
+    const int lane = static_cast<int>(threadIdx.x & 31);
+    const int row = static_cast<int>(blockIdx.x) * kWarpsPerBlock + static_cast<int>(threadIdx.x >> 5);
+    const ph::TileSet<1> ts = ph::tile_set<1>(coarse.tile_meta, coarse.tiles, row / kTile);
+    if (row % kTile >= ts.rows[0] || !ph::gate_open(sc, ts.inst[0], gate)) return;   // the whole warp
+    const std::uint32_t P = lv.rows, k0 = moff[row], k1 = moff[row + 1];
+    T s = T(0);
+    unsigned moved = 0;
+    for (std::uint32_t base = k0; base < k1; base += 32) {
+        const std::uint32_t k = base + static_cast<std::uint32_t>(lane);
+        T rm = T(0);
+        if (k < k1) {
+            const int f = static_cast<int>(member[k]);
+            rm = b[f] - lv.vd[W * P + f] * x[f];
+#pragma unroll
+            for (int j = 0; j < W; ++j) rm -= lv.vd[j * P + f] * x[lv.col[j * P + f]];
+            moved += 4u * W + static_cast<unsigned>(sizeof(T)) * (W + 3u) + 4u;
+        }
+        const int n = static_cast<int>(k1 - base < 32u ? k1 - base : 32u);
+        for (int i = 0; i < n; ++i) s += __shfl_sync(0xffffffffu, rm, i);
+    }
+    if (lane == 0) {
+        bc[row] = s;
+        if (ts.sweep[0]) xc[row] = omega * coarse.inv[row] * s;
+        moved += 4u + 3u * static_cast<unsigned>(sizeof(T));
+    }
+    ph::count_bytes_warp(coarse.bytes, moved);
+}
+
 template <typename T, int W, int R>
 __global__ void k_prolong_smooth(LevelView<T> lv, const std::int32_t* __restrict__ agg,
                                  const T* __restrict__ e, const T* __restrict__ b, const T* __restrict__ x,
@@ -359,6 +406,18 @@ void launch_restrict_zero(const LevelView<T>& coarse, const std::uint32_t* membe
 }
 
 template <typename T>
+void launch_residual_restrict(const LevelView<T>& lv, const LevelView<T>& coarse, const std::uint32_t* member_offset,
+                              const std::uint32_t* member, const T* b, const T* x, T* bc, T* xc, T omega,
+                              const InstanceScalars* sc, int gate, cudaStream_t stream, const DenseTask<T>& dense) {
+    const unsigned blocks = (coarse.rows + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    PSGB_LAUNCH(kFamRestrictCoarse, stream,
+                PSGB_WIDTHS(lv.width,
+                    launch_pdl(k_residual_restrict<T, W>, blocks + dense.count, kTile, stream, lv,
+                               counted(coarse, kFamRestrictCoarse), member_offset, member, b, x, bc, xc, omega, sc,
+                               gate, dense)));
+}
+
+template <typename T>
 void launch_prolong_smooth(const LevelView<T>& lv, const std::int32_t* agg, const T* e, const T* b, const T* x,
                            T* y, T omega, const InstanceScalars* sc, int gate, cudaStream_t stream) {
     PSGB_LAUNCH(smooth_family(lv), stream,
@@ -395,6 +454,9 @@ void launch_dense_solve(const DenseTask<T>& dense, const InstanceScalars* sc, in
                                      const T*, T*, const InstanceScalars*, int, cudaStream_t);        \
     template void launch_restrict_zero<T>(const LevelView<T>&, const std::uint32_t*, const std::uint32_t*, \
                                           const T*, T*, T*, T, const InstanceScalars*, int, cudaStream_t); \
+    template void launch_residual_restrict<T>(const LevelView<T>&, const LevelView<T>&, const std::uint32_t*,   \
+                                              const std::uint32_t*, const T*, const T*, T*, T*, T,             \
+                                              const InstanceScalars*, int, cudaStream_t, const DenseTask<T>&); \
     template void launch_prolong_smooth<T>(const LevelView<T>&, const std::int32_t*, const T*, const T*,    \
                                            const T*, T*, T, const InstanceScalars*, int, cudaStream_t);    \
     template void launch_prolong<T>(const LevelView<T>&, const std::int32_t*, const T*, T*,            \

@@ -706,11 +706,17 @@ void vcycle(Batch& b, const T* rhs, T* x, int gate, bool first_sweep_done, cudaS
             dense = DenseTask<T>{};
             std::swap(cur[l], other[l]);
         }
-        launch_residual<T>(lv, rhs_of[l], cur[l], Pick<T>::r(L), b.scalars, gate, st, dense);
         BatchLevel& C = b.levels[l + 1];
         const LevelView<T> cv = Pick<T>::view(b, l + 1);
-        launch_restrict_zero<T>(cv, L.member_offset, L.member, Pick<T>::r(L), Pick<T>::bvec(C), cur[l + 1], omega,
-                                b.scalars, gate, st);
+        if (l > 0) {
+            // coarse levels: latency-bound, the residual formed inside the restriction
+            launch_residual_restrict<T>(lv, cv, L.member_offset, L.member, rhs_of[l], cur[l], Pick<T>::bvec(C),
+                                        cur[l + 1], omega, b.scalars, gate, st, dense);
+        } else {
+            launch_residual<T>(lv, rhs_of[l], cur[l], Pick<T>::r(L), b.scalars, gate, st, dense);
+            launch_restrict_zero<T>(cv, L.member_offset, L.member, Pick<T>::r(L), Pick<T>::bvec(C), cur[l + 1], omega,
+                                    b.scalars, gate, st);
+        }
         // The deepest level has no smoothing launch: its dense solves run on their own.
         if (tail == 0 && l + 2 == depth && b.dense_at[l + 1]) {
             launch_dense_solve<T>(dense_task<T>(b, l + 1, Pick<T>::bvec(C), Pick<T>::x(C)), b.scalars, gate, st);
