@@ -206,8 +206,12 @@ def smoother_desc(tuning) -> str:
         return "damped Jacobi 2+2 on every level, omega 0.8 (untuned)"
     if isinstance(tuning, list):
         return " | ".join(f"lane {k}: {smoother_desc(t)}" for k, t in enumerate(tuning))
-    per = ", ".join(f"L{l}: {a}+{b}" for l, (a, b) in enumerate(zip(tuning["pre_sweeps"], tuning["post_sweeps"])))
-    return f"damped Jacobi, autotuned sweeps per level ({per}), omega {tuning['jacobi_omega']}"
+    per = ", ".join(f"L{l}: {a}+{b}" + (f" x{k}" if k > 1 else "") for l, (a, b, k) in
+                    enumerate(zip(tuning["pre_sweeps"], tuning["post_sweeps"],
+                                  tuning.get("block_sweeps", [1] * len(tuning["pre_sweeps"])))))
+    scale = tuning.get("coarse_correction", 1.0)
+    return (f"damped Jacobi, autotuned sweeps per level ({per}), omega {tuning['jacobi_omega']}"
+            + (f", coarse-grid correction x{scale}" if scale != 1.0 else ""))
 
 
 def precision_for(kind: str) -> str:
@@ -953,15 +957,27 @@ def run_l8rhs(args, rank, local_rank):
     src = [torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in sources]
     lib = capi.load()
     peak, peak_kind = peaks()
+    # per precision, the planet's settings autotuned on a one-planet batch (setup, not
+    # timed): the block step and the one-at-a-time comparator use the same tuning
+    tunings = {}
+    if not args.no_autotune:
+        tb = pg.Batch([m])
+        for precision in ("fp64", "mixed"):
+            if precision == "fp64" or precision in args.l8rhs_variants:
+                tunings[precision] = tb.autotune([t0], [src[0]], [inp.heat_capacity], [inp.dt],
+                                                 conductance=[inp.conductance], precision=precision, **SOLVER)
+        del tb
     out = {"metric": "sub-steps/s of 32 sub-steps of one L8 planet at 1e-10 relative residual", "unit": "sub-steps/s",
            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "data": "synthetic", "higher_is_better": True,
            "config": {"workload": "one L8 planet (655,362 cells), 32 right-hand sides S + N(0, 5^2) W/m^2",
                       "cells": m.cell_count, "rhs": rhs, "tolerance": 1e-10, "krylov": "BiCGSTAB",
-                      "smoother": "damped Jacobi 2+2, omega 0.8 (untuned)"}}
+                      "smoother": {p: smoother_desc(t) for p, t in tunings.items()} or smoother_desc(None),
+                      "tuning": tunings or None}}
     results = {}
     for name, precision in (("A_fp64", "fp64"), ("B_mixed", "mixed")):
         if precision not in args.l8rhs_variants:
             continue
+        m.set_tuning(tunings.get(precision))
         step = lambda: pg.transport_step_multi(m, t0, src, inp.heat_capacity, inp.dt, inp.conductance,
                                                precision=precision, **SOLVER)
         for _ in range(args.warmup):
@@ -990,15 +1006,22 @@ def run_l8rhs(args, rank, local_rank):
                                               "unit": "GB/s", "frac": achieved / peak if achieved else None,
                                               "launches": int(nl.value), "bytes_per_launch": nbytes.value / max(1, nl.value),
                                               "bytes": "matrix and indices once per row, the 32 right-hand sides' vectors"}}
-    # the same 32 sub-steps one per call through the plain FP64 drop-in
-    for _ in range(2):
-        pg.transport_step(m, t0, src[0], inp.heat_capacity, inp.dt, inp.conductance, precision="fp64", **SOLVER)
-    torch.cuda.synchronize()
-    t = time.perf_counter()
-    for j in range(rhs):
-        pg.transport_step(m, t0, src[j], inp.heat_capacity, inp.dt, inp.conductance, precision="fp64", **SOLVER)
-    torch.cuda.synchronize()
-    out["one_at_a_time_fp64"] = {"value": rhs / (time.perf_counter() - t), "unit": "sub-steps/s"}
+    # the same 32 sub-steps one per call through the plain FP64 drop-in, with the FP64 tuning
+    # (the comparator) and with the options' untuned sweeps
+    for key, tuning in (("one_at_a_time_fp64", tunings.get("fp64")), ("one_at_a_time_fp64_untuned", None)):
+        if key == "one_at_a_time_fp64_untuned" and tuning is None and not tunings:
+            continue
+        m.set_tuning(tuning)
+        for _ in range(2):
+            pg.transport_step(m, t0, src[0], inp.heat_capacity, inp.dt, inp.conductance, precision="fp64", **SOLVER)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for j in range(rhs):
+            pg.transport_step(m, t0, src[j], inp.heat_capacity, inp.dt, inp.conductance, precision="fp64", **SOLVER)
+        torch.cuda.synchronize()
+        out[key] = {"value": rhs / (time.perf_counter() - t), "unit": "sub-steps/s",
+                    "settings": "autotuned (the block's FP64 tuning)" if tuning is not None else "untuned"}
+    m.set_tuning(None)
     for name in ("A_fp64", "B_mixed"):
         if name in out:
             out["value"] = out[name]["value"]

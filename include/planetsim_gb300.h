@@ -25,7 +25,8 @@
  * per-step reassembly (psgb_batch_set_reassembly), coarse_tail_single = 2 (the
  * shared-memory coarse tail). Version 5: coarse_tail_single = 3 and psgb_tuning's
  * coarse_tail_cluster (the coarse tail on a thread-block cluster per planet). Version 6:
- * psgb_tuning's coarse_correction (the V-cycle's coarse-grid correction scale).
+ * psgb_tuning's coarse_correction (the V-cycle's coarse-grid correction scale). Version 7:
+ * psgb_planet_set_tuning / psgb_planet_get_tuning; block-local sweeps in the block step.
  *
  * A server's calls may come from any thread; its lanes step on threads of their own.
  */
@@ -39,7 +40,7 @@
 extern "C" {
 #endif
 
-#define PSGB_ABI_VERSION 6
+#define PSGB_ABI_VERSION 7
 
 /* status codes */
 #define PSGB_OK 0
@@ -514,6 +515,12 @@ int psgb_batch_get_tuning(const psgb_batch* batch, psgb_tuning* out);
 /* Applies settings (e.g. a tuning kept from an earlier run); NULL returns to the options'
  * uniform sweeps and the default launch shapes. */
 int psgb_batch_set_tuning(psgb_batch* batch, const psgb_tuning* tuning);
+/* The same settings for a planet's own solves (psgb_transport_step,
+ * psgb_transport_step_multi, psgb_multigrid_precondition, psgb_solve_newton_system): a
+ * tuning of a one-planet batch of this planet carries over bit for bit; NULL returns to
+ * the options' uniform sweeps. */
+int psgb_planet_set_tuning(psgb_planet* planet, const psgb_tuning* tuning);
+int psgb_planet_get_tuning(psgb_planet* planet, psgb_tuning* out);
 
 /* ---- column radiation: sim/planet/atmosphere/atmosphere_column.hpp ----------------
  * column_radiation (humidity variant, :85-104) + cloud_optics (:599-623) +

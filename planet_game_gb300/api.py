@@ -163,6 +163,19 @@ class PlanetMesh:
         _raise(capi.load().psgb_planet_group_of_cell(self._h, _ptr(out)))
         return out
 
+    @property
+    def tuning(self) -> dict:
+        """The per-level settings of this planet's own solves (transport_step,
+        transport_step_multi, GraphMultigrid.precondition, solve_newton_system)."""
+        t = capi.Tuning()
+        _raise(capi.load().psgb_planet_get_tuning(self._h, C.byref(t)))
+        return _tuning_dict(t)
+
+    def set_tuning(self, tuning: dict | None) -> None:
+        """Per-level settings for this planet's own solves: a one-planet Batch's tuning of
+        this planet carries over bit for bit; None returns to the options' sweeps."""
+        _raise(capi.load().psgb_planet_set_tuning(self._h, None if tuning is None else C.byref(_tuning_struct(tuning))))
+
     def hierarchy_level(self, level: int) -> dict[str, np.ndarray]:
         sizes = (C.c_uint64 * 4)()
         ptrs = [C.c_void_p() for _ in range(4)]
@@ -636,6 +649,21 @@ def _tuning_dict(t) -> dict:
             "coarse_tail_cluster": int(t.coarse_tail_cluster), "coarse_correction": float(t.coarse_correction)}
 
 
+def _tuning_struct(tuning: dict) -> capi.Tuning:
+    t = capi.Tuning()
+    t.levels = len(tuning["pre_sweeps"])
+    for k in ("pre_sweeps", "post_sweeps", "stencil_tiles", "vector_tiles", "block_sweeps"):
+        arr = getattr(t, k)
+        for l, v in enumerate(tuning.get(k, [1] * t.levels)):
+            arr[l] = int(v)
+    t.jacobi_omega = float(tuning["jacobi_omega"])
+    t.coarse_tail_level = int(tuning.get("coarse_tail_level", 0))
+    t.coarse_tail_single = int(tuning.get("coarse_tail_single", 0))
+    t.coarse_tail_cluster = int(tuning.get("coarse_tail_cluster", 0))
+    t.coarse_correction = float(tuning.get("coarse_correction", 1.0))
+    return t
+
+
 class Batch:
     """Many planets of uneven levels in one concatenated layout, solved together."""
 
@@ -704,21 +732,7 @@ class Batch:
 
     def set_tuning(self, tuning: dict | None) -> None:
         """Apply per-level settings (a dict from `autotune`/`tuning`); None clears them."""
-        if tuning is None:
-            _raise(capi.load().psgb_batch_set_tuning(self._h, None))
-            return
-        t = capi.Tuning()
-        t.levels = len(tuning["pre_sweeps"])
-        for k in ("pre_sweeps", "post_sweeps", "stencil_tiles", "vector_tiles", "block_sweeps"):
-            arr = getattr(t, k)
-            for l, v in enumerate(tuning.get(k, [1] * t.levels)):
-                arr[l] = int(v)
-        t.jacobi_omega = float(tuning["jacobi_omega"])
-        t.coarse_tail_level = int(tuning.get("coarse_tail_level", 0))
-        t.coarse_tail_single = int(tuning.get("coarse_tail_single", 0))
-        t.coarse_tail_cluster = int(tuning.get("coarse_tail_cluster", 0))
-        t.coarse_correction = float(tuning.get("coarse_correction", 1.0))
-        _raise(capi.load().psgb_batch_set_tuning(self._h, C.byref(t)))
+        _raise(capi.load().psgb_batch_set_tuning(self._h, None if tuning is None else C.byref(_tuning_struct(tuning))))
 
     def transport_step(self, t0, sources, heat_capacity, dt, conductance=None, edge_conductance=None,
                        out=None, transport_out=None, active=None, **options):

@@ -198,6 +198,8 @@ _SIGNATURES = {
     "psgb_batch_get_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
     "psgb_batch_set_edge_conductance": (C.c_int, [P, C.POINTER(P)]),
     "psgb_batch_set_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
+    "psgb_planet_set_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
+    "psgb_planet_get_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
     "psgb_transport_settings_default": (None, [C.POINTER(TransportSettings)]),
     "psgb_solve_implicit_transport": (C.c_int, [P, C.c_double, P, TransportResponse, P, C.POINTER(TransportSettings),
                                                 C.POINTER(SolveOptions), P, P, P, C.POINTER(TransportResult)]),

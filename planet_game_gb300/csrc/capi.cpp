@@ -993,36 +993,62 @@ int psgb_batch_get_tuning(const psgb_batch* h, psgb_tuning* out) {
     });
 }
 
+namespace {
+
+// A psgb_tuning applied to a batch (NULL: back to the options' uniform sweeps).
+void set_tuning_of(psgb::Batch& b, const psgb_tuning* tuning) {
+    if (tuning == nullptr) {
+    psgb::clear_tuning(b);
+    return;
+    }
+    require(tuning->levels == b.levels.size(), "tuning levels do not match the batch");
+    psgb::Tuning t;
+    for (std::uint32_t l = 0; l < tuning->levels; ++l) {
+        t.pre.push_back(tuning->pre_sweeps[l]);
+        t.post.push_back(tuning->post_sweeps[l]);
+        t.sets_stencil.push_back(static_cast<std::uint8_t>(tuning->stencil_tiles[l]));
+        t.sets_vector.push_back(static_cast<std::uint8_t>(tuning->vector_tiles[l]));
+        t.inner.push_back(tuning->block_sweeps[l] == 0 ? 1 : tuning->block_sweeps[l]);
+    }
+    t.omega = tuning->jacobi_omega;
+    t.correction = tuning->coarse_correction == 0.0 ? 1.0 : tuning->coarse_correction;
+    t.tail_level = tuning->coarse_tail_level;
+    require(tuning->coarse_tail_single >= 0 && tuning->coarse_tail_single <= 3,
+            "coarse_tail_single must be 0, 1, 2 or 3");
+    t.tail_spread = tuning->coarse_tail_single == 0;
+    t.tail_shared = tuning->coarse_tail_single == 2;
+    if (tuning->coarse_tail_single == 3) {
+        const std::uint32_t c = tuning->coarse_tail_cluster;
+        require(c == 2 || c == 4 || c == 8, "coarse_tail_cluster must be 2, 4 or 8 blocks");
+        t.tail_cluster = c;
+    }
+    psgb::apply_tuning(b, t);
+}
+
+}  // namespace
+
 int psgb_batch_set_tuning(psgb_batch* h, const psgb_tuning* tuning) {
     return guarded([&] {
         require(h != nullptr, "null argument");
-        psgb::Batch& b = *h->batch;
-        if (tuning == nullptr) {
-            psgb::clear_tuning(b);
-            return PSGB_OK;
-        }
-        require(tuning->levels == b.levels.size(), "tuning levels do not match the batch");
-        psgb::Tuning t;
-        for (std::uint32_t l = 0; l < tuning->levels; ++l) {
-            t.pre.push_back(tuning->pre_sweeps[l]);
-            t.post.push_back(tuning->post_sweeps[l]);
-            t.sets_stencil.push_back(static_cast<std::uint8_t>(tuning->stencil_tiles[l]));
-            t.sets_vector.push_back(static_cast<std::uint8_t>(tuning->vector_tiles[l]));
-            t.inner.push_back(tuning->block_sweeps[l] == 0 ? 1 : tuning->block_sweeps[l]);
-        }
-        t.omega = tuning->jacobi_omega;
-        t.correction = tuning->coarse_correction == 0.0 ? 1.0 : tuning->coarse_correction;
-        t.tail_level = tuning->coarse_tail_level;
-        require(tuning->coarse_tail_single >= 0 && tuning->coarse_tail_single <= 3,
-                "coarse_tail_single must be 0, 1, 2 or 3");
-        t.tail_spread = tuning->coarse_tail_single == 0;
-        t.tail_shared = tuning->coarse_tail_single == 2;
-        if (tuning->coarse_tail_single == 3) {
-            const std::uint32_t c = tuning->coarse_tail_cluster;
-            require(c == 2 || c == 4 || c == 8, "coarse_tail_cluster must be 2, 4 or 8 blocks");
-            t.tail_cluster = c;
-        }
-        psgb::apply_tuning(b, t);
+        set_tuning_of(*h->batch, tuning);
+        return PSGB_OK;
+    });
+}
+
+int psgb_planet_set_tuning(psgb_planet* h, const psgb_tuning* tuning) {
+    return guarded([&] {
+        require(h != nullptr, "null argument");
+        set_tuning_of(solo(h), tuning);
+        return PSGB_OK;
+    });
+}
+
+int psgb_planet_get_tuning(psgb_planet* h, psgb_tuning* out) {
+    return guarded([&] {
+        require(h != nullptr && out != nullptr, "null argument");
+        psgb::Batch& b = solo(h);
+        require(b.levels.size() <= PSGB_MAX_LEVELS, "planet deeper than PSGB_MAX_LEVELS levels");
+        fill_tuning(psgb::current_tuning(b), out);
         return PSGB_OK;
     });
 }

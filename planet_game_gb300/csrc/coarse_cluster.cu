@@ -134,8 +134,8 @@ __device__ void c_smooth_block(const LevelView<T>& lv, int tile, int gid, int la
         if (live) {
             T s = bv;
 #pragma unroll
-            for (int j = 0; j < W; ++j) s -= a[j] * (local[j] >= 0 ? xs[gid][local[j]] : h[j]);
-            out = omega == T(1) ? inv * s : xo + omega * (inv * s - xo);
+            for (int j = 0; j < W; ++j) s = ph::fnma(a[j], local[j] >= 0 ? xs[gid][local[j]] : h[j], s);
+            out = ph::jacobi_update(xo, omega, inv, s);
         }
         ph::group_sync(gid);
         xs[gid][lane] = out;

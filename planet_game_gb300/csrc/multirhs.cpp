@@ -104,7 +104,7 @@ void vcycle(Batch& b, Space& s, const T* rhs, T* x, int gate, cudaStream_t st) {
     for (std::size_t l = 0; l + 1 < depth; ++l) {
         const LevelView<T> lv = Sel<T>::view(b, l);
         for (int k = 1; k < sm.pre_at(l); ++k) {
-            L::smooth(lv, rhs_of[l], cur[l], other[l], omega, s.sc, gate, st);
+            L::smooth(lv, rhs_of[l], cur[l], other[l], omega, s.sc, gate, st, sm.inner_at(l));
             std::swap(cur[l], other[l]);
         }
         L::residual(lv, rhs_of[l], cur[l], Sel<T>::r(s)[l], s.sc, gate, st);
@@ -119,7 +119,7 @@ void vcycle(Batch& b, Space& s, const T* rhs, T* x, int gate, cudaStream_t st) {
         if (sm.post_at(l) == 0 || split) {
             L::prolong(lv, b.levels[l].agg, e, cur[l], s.sc, gate, st);
             for (int k = 0; k < sm.post_at(l); ++k) {
-                L::smooth(lv, rhs_of[l], cur[l], other[l], omega, s.sc, gate, st);
+                L::smooth(lv, rhs_of[l], cur[l], other[l], omega, s.sc, gate, st, sm.inner_at(l));
                 std::swap(cur[l], other[l]);
             }
             continue;
@@ -127,7 +127,7 @@ void vcycle(Batch& b, Space& s, const T* rhs, T* x, int gate, cudaStream_t st) {
         L::prolong_smooth(lv, b.levels[l].agg, e, rhs_of[l], cur[l], other[l], omega, s.sc, gate, st);
         std::swap(cur[l], other[l]);
         for (int k = 1; k < sm.post_at(l); ++k) {
-            L::smooth(lv, rhs_of[l], cur[l], other[l], omega, s.sc, gate, st);
+            L::smooth(lv, rhs_of[l], cur[l], other[l], omega, s.sc, gate, st, sm.inner_at(l));
             std::swap(cur[l], other[l]);
         }
     }

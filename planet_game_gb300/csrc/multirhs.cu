@@ -169,6 +169,93 @@ __global__ void k_smooth(LevelView<T> L, const T* __restrict__ b, const T* __res
     }
 }
 
+// Block-local Jacobi for every right-hand side: `inner` sweeps of one tile in one launch,
+// the tile's own rows updated in shared memory between sweeps (double-buffered) and the
+// neighbours in other tiles held at x, the single solve's block sweep (ph::smooth_block)
+// term for term. Dynamic shared memory: the tile's columns, values, 1/diag and two copies
+// of its 256 rows x 32 right-hand sides. A right-hand side whose solve is not running still
+// computes (the block's barriers need every thread) but stores nothing.
+template <typename T, int W>
+struct BlockSweepSmem {
+    static constexpr std::size_t kCol = std::size_t(W) * kTile * sizeof(int);
+    static constexpr std::size_t kVal = std::size_t(W) * kTile * sizeof(T);
+    static constexpr std::size_t kInv = std::size_t(kTile) * sizeof(T);
+    static constexpr std::size_t kX = std::size_t(kTile) * kRhs * sizeof(T);
+    static constexpr std::size_t bytes = kCol + kVal + kInv + 2 * kX;
+};
+
+template <typename T, int W>
+__global__ void __launch_bounds__(kTile) k_smooth_block(LevelView<T> L, const T* __restrict__ b,
+                                                        const T* __restrict__ x, T* __restrict__ y, T omega, int inner,
+                                                        const InstanceScalars* sc, int gate) {
+    pdl_begin();
+    using S = BlockSweepSmem<T, W>;
+    extern __shared__ __align__(16) unsigned char block_sweep_bytes[];
+    int(*col)[kTile] = reinterpret_cast<int(*)[kTile]>(block_sweep_bytes);
+    T(*val)[kTile] = reinterpret_cast<T(*)[kTile]>(block_sweep_bytes + S::kCol);
+    T* inv = reinterpret_cast<T*>(block_sweep_bytes + S::kCol + S::kVal);
+    T(*xs[2])[kRhs] = {reinterpret_cast<T(*)[kRhs]>(block_sweep_bytes + S::kCol + S::kVal + S::kInv),
+                       reinterpret_cast<T(*)[kRhs]>(block_sweep_bytes + S::kCol + S::kVal + S::kInv + S::kX)};
+    const int tile = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const TileInfo ti = tile_info(L.tile_meta, tile);
+    if (!ti.sweep) return;   // the whole block
+    const std::uint32_t P = L.rows;
+    const int first = tile * kTile;
+    {
+        const int t = threadIdx.x, row = first + t;
+#pragma unroll
+        for (int j = 0; j < W; ++j) {
+            col[j][t] = L.col[j * P + row];
+            val[j][t] = L.vd[j * P + row];
+        }
+        inv[t] = L.inv[row];
+    }
+    count(L.bytes, static_cast<unsigned long long>(ti.rows) * (4ull * W + sizeof(T) * (W + 1ull) + 3ull * kRhs * sizeof(T)));
+    const bool on = ph::gate_open(sc, lane, gate);
+    // the iterate the sweeps start from: the tile's rows of x (0 on padding rows)
+    for (int k = 0; k < 32; ++k) {
+        const int local = warp * 32 + k;
+        xs[0][local][lane] = local < ti.rows ? x[at(first + local, lane)] : T(0);
+    }
+    __syncthreads();
+    int cur = 0;
+    for (int sweep = 0; sweep < inner; ++sweep) {
+        for (int k = 0; k < 32; ++k) {
+            const int local = warp * 32 + k;
+            const T xo = xs[cur][local][lane];
+            T out = xo;
+            if (local < ti.rows) {
+                T s = b[at(first + local, lane)];
+#pragma unroll
+                for (int j = 0; j < W; ++j) {
+                    const int c = col[j][local];
+                    const T v = (c >= first && c < first + kTile) ? xs[cur][c - first][lane] : x[at(c, lane)];
+                    s = ph::fnma(val[j][local], v, s);
+                }
+                out = ph::jacobi_update(xo, omega, inv[local], s);
+            }
+            xs[cur ^ 1][local][lane] = out;
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
+    if (!on) return;
+    for (int k = 0; k < 32; ++k) {
+        const int local = warp * 32 + k;
+        if (local < ti.rows) y[at(first + local, lane)] = xs[cur][local][lane];
+    }
+}
+
+template <typename T, int W>
+void set_block_sweep_smem() {
+    static const bool done = [] {
+        PSGB_CUDA(cudaFuncSetAttribute(k_smooth_block<T, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(BlockSweepSmem<T, W>::bytes)));
+        return true;
+    }();
+    (void)done;
+}
+
 template <typename T, int W>
 __global__ void k_residual(LevelView<T> L, const T* __restrict__ b, const T* __restrict__ x, T* __restrict__ r,
                            const InstanceScalars* sc, int gate) {
@@ -675,8 +762,27 @@ void Launch<T>::smooth_zero(const LevelView<T>& L, const T* b, T* x, T omega, co
 }
 template <typename T>
 void Launch<T>::smooth(const LevelView<T>& L, const T* b, const T* x, T* y, T omega, const InstanceScalars* sc,
-                       int gate, cudaStream_t st) {
+                       int gate, cudaStream_t st, int inner) {
     const int fam = L.level == 0 ? kFamSmooth : kFamSmoothCoarse;
+    if (inner > 1) {
+        PSGB_LAUNCH(fam, st, PSGB_MR_WIDTHS(L.width, {
+            set_block_sweep_smem<T, W>();
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            attr[0].val.programmaticStreamSerializationAllowed = 1;
+            cudaLaunchConfig_t cfg{};
+            cfg.gridDim = dim3(L.tiles);
+            cfg.blockDim = dim3(kTile);
+            cfg.dynamicSmemBytes = BlockSweepSmem<T, W>::bytes;
+            cfg.stream = st;
+            cfg.attrs = attr;
+            cfg.numAttrs = L.tiles <= kPdlMaxBlocks ? 1 : 0;
+            const cudaError_t e = cudaLaunchKernelEx(&cfg, k_smooth_block<T, W>, counted(L, fam), b, x, y, omega, inner,
+                                                     sc, gate);
+            if (e != cudaSuccess) throw std::runtime_error(std::string("block sweep launch: ") + cudaGetErrorString(e));
+        }));
+        return;
+    }
     PSGB_LAUNCH(fam, st, PSGB_MR_WIDTHS(L.width, launch_pdl(k_smooth<T, W>, L.tiles, kTile, st, counted(L, fam), b, x, y,
                                                             omega, sc, gate)));
 }

@@ -27,8 +27,10 @@ template <typename T>
 struct Launch {
     static void smooth_zero(const LevelView<T>& L, const T* b, T* x, T omega, const InstanceScalars* sc, int gate,
                             cudaStream_t st);
+    // inner > 1: that many block-local sweeps of each tile in the launch (the single solve's
+    // block sweep)
     static void smooth(const LevelView<T>& L, const T* b, const T* x, T* y, T omega, const InstanceScalars* sc,
-                       int gate, cudaStream_t st);
+                       int gate, cudaStream_t st, int inner = 1);
     static void residual(const LevelView<T>& L, const T* b, const T* x, T* r, const InstanceScalars* sc, int gate,
                          cudaStream_t st);
     static void restrict_zero(const LevelView<T>& C, const std::uint32_t* moff, const std::uint32_t* member,

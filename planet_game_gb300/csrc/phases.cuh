@@ -230,6 +230,20 @@ __device__ __forceinline__ bool running(const InstanceScalars& s) { return s.sta
 __device__ __forceinline__ float prod(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double prod(double a, double b) { return __dmul_rn(a, b); }
 
+// The block-local sweep's arithmetic spelled out, so that every kernel sweeping a tile
+// block-locally (the kernel schedule, the coarse tails, the block step of many right-hand
+// sides) forms the same bits whatever the compiler would fuse: s - a v as one fused
+// multiply-add, and the damped update as the product inv s and its difference with xo
+// each rounded, then xo + omega d as one fused multiply-add.
+__device__ __forceinline__ float fnma(float a, float v, float s) { return __fmaf_rn(-a, v, s); }
+__device__ __forceinline__ double fnma(double a, double v, double s) { return __fma_rn(-a, v, s); }
+__device__ __forceinline__ float jacobi_update(float xo, float omega, float inv, float s) {
+    return omega == 1.0f ? __fmul_rn(inv, s) : __fmaf_rn(omega, __fsub_rn(__fmul_rn(inv, s), xo), xo);
+}
+__device__ __forceinline__ double jacobi_update(double xo, double omega, double inv, double s) {
+    return omega == 1.0 ? __dmul_rn(inv, s) : __fma_rn(omega, __dsub_rn(__dmul_rn(inv, s), xo), xo);
+}
+
 __device__ __forceinline__ bool finite(double v) { return isfinite(v); }
 
 // Release/acquire fence at GPU scope: orders this thread's partial stores before its
@@ -456,8 +470,8 @@ __device__ void smooth_block(const LevelView<T>& lv, int tile, int gid, int lane
         if (live) {
             T s = bv;
 #pragma unroll
-            for (int j = 0; j < W; ++j) s -= a[j] * (local[j] >= 0 ? xs[gid][local[j]] : h[j]);
-            out = omega == T(1) ? inv * s : xo + omega * (inv * s - xo);
+            for (int j = 0; j < W; ++j) s = fnma(a[j], local[j] >= 0 ? xs[gid][local[j]] : h[j], s);
+            out = jacobi_update(xo, omega, inv, s);
         }
         group_sync(gid);
         xs[gid][lane] = out;

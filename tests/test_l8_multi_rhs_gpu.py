@@ -80,3 +80,36 @@ def test_all_32_sub_steps_against_the_oracle(l8, blocks):
     for j, (t_new, _, _) in enumerate(refs):
         assert np.max(np.abs(out["fp64"][0][j] - t_new)) <= 2e-6, j
         assert np.max(np.abs(out["mixed"][0][j] - t_new)) <= 2e-6, j
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_tuned_block_with_block_sweeps_equals_the_tuned_sub_steps_alone(l8, precision):
+    """With per-level settings on the planet (block-local sweeps on the coarse levels, the
+    coarse-grid correction scaled, ω = 1), the block step's sub-steps still equal the same
+    sub-steps solved alone with those settings, bit for bit."""
+    torch = pytest.importorskip("torch")
+    import planet_game_gb300 as pg
+
+    m, inp, sources = l8
+    t = m.tuning
+    depth = t["levels"]
+    t.update(pre_sweeps=[1] + [2] * (depth - 1), post_sweeps=[2] + [2] * (depth - 1),
+             block_sweeps=[1] + [6] * (depth - 1), jacobi_omega=1.0, coarse_correction=1.5)
+    m.set_tuning(t)
+    try:
+        assert m.tuning["block_sweeps"][1] == 6 and m.tuning["coarse_correction"] == 1.5
+        t0 = torch.from_numpy(inp.t0).cuda()
+        src = [torch.from_numpy(np.ascontiguousarray(s)).cuda() for s in sources[:8]]
+        tb, hb, rb = pg.transport_step_multi(m, t0, src, inp.heat_capacity, inp.dt, inp.conductance,
+                                             transport=True, precision=precision)
+        torch.cuda.synchronize()
+        for j in range(len(src)):
+            assert rb[j].status == 0 and rb[j].relative_residual <= 1e-10
+            t1, h1, r1 = pg.transport_step(m, t0, src[j], inp.heat_capacity, inp.dt, inp.conductance,
+                                           precision=precision)
+            assert np.array_equal(tb[j].cpu().numpy(), t1.cpu().numpy()), j
+            assert np.array_equal(hb[j].cpu().numpy(), h1.cpu().numpy()), j
+            assert (rb[j].iterations, rb[j].refinements) == (r1.iterations, r1.refinements)
+    finally:
+        m.set_tuning(None)
+    assert m.tuning["coarse_correction"] == 1.0
