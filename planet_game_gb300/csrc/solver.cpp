@@ -709,7 +709,10 @@ void vcycle(Batch& b, const T* rhs, T* x, int gate, bool first_sweep_done, cudaS
         BatchLevel& C = b.levels[l + 1];
         const LevelView<T> cv = Pick<T>::view(b, l + 1);
         if (l > 0) {
-            // coarse levels: latency-bound, the residual formed inside the restriction
+            // coarse levels: latency-bound, the residual formed inside the restriction (on
+            // the fine level, HBM-bound, the warp-per-coarse-row gathers of the members'
+            // rows cost more than the residual's own pass: 11.1 -> 12.7 ms on the 64-planet
+            // step, 8.7 -> 11.3 ms on one L8 planet in FP64)
             launch_residual_restrict<T>(lv, cv, L.member_offset, L.member, rhs_of[l], cur[l], Pick<T>::bvec(C),
                                         cur[l + 1], omega, b.scalars, gate, st, dense);
         } else {
