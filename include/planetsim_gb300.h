@@ -27,6 +27,7 @@
  * coarse_tail_cluster (the coarse tail on a thread-block cluster per planet). Version 6:
  * psgb_tuning's coarse_correction (the V-cycle's coarse-grid correction scale). Version 7:
  * psgb_planet_set_tuning / psgb_planet_get_tuning; block-local sweeps in the block step.
+ * Version 8: psgb_batch_set_priority.
  *
  * A server's calls may come from any thread; its lanes step on threads of their own.
  */
@@ -40,7 +41,7 @@
 extern "C" {
 #endif
 
-#define PSGB_ABI_VERSION 7
+#define PSGB_ABI_VERSION 8
 
 /* status codes */
 #define PSGB_OK 0
@@ -472,6 +473,12 @@ int psgb_batch_set_edge_conductance(psgb_batch* batch, const double* const* edge
  * matrix is reused while C, dt and the conductances are unchanged. Results are the same
  * either way. */
 int psgb_batch_set_reassembly(psgb_batch* batch, int every_step);
+
+/* Nonzero: the batch's solves run on a stream of the device's highest priority (its
+ * kernels are scheduled first where batches stepped side by side compete for the GPU, e.g.
+ * the lanes whose planets need the most iterations); zero (the default): normal priority.
+ * Not while a step of the batch runs. Results are the same either way. */
+int psgb_batch_set_priority(psgb_batch* batch, int high);
 
 /* Per-level settings of a batch's solve. The reference has no counterpart (its smoother
  * is fixed, heat_transport.cpp:258-286); the autotuner picks them for the batch's GPU:

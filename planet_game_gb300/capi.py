@@ -186,6 +186,7 @@ _SIGNATURES = {
     "psgb_batch_create": (C.c_int, [C.POINTER(P), C.c_uint32, C.POINTER(P)]),
     "psgb_batch_destroy": (None, [P]),
     "psgb_batch_set_reassembly": (C.c_int, [P, C.c_int]),
+    "psgb_batch_set_priority": (C.c_int, [P, C.c_int]),
     "psgb_batch_device_bytes": (C.c_uint64, [P]),
     "psgb_batch_transport_step": (C.c_int, [P, C.POINTER(StepParams), C.POINTER(SolveOptions), C.POINTER(P),
                                             C.POINTER(P), C.POINTER(P), C.POINTER(P), C.POINTER(StepReport),

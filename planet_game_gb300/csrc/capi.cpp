@@ -960,6 +960,22 @@ int psgb_batch_set_reassembly(psgb_batch* h, int every_step) {
     });
 }
 
+int psgb_batch_set_priority(psgb_batch* h, int high) {
+    return guarded([&] {
+        require(h != nullptr, "null argument");
+        psgb::Batch& b = *h->batch;
+        require(b.stream != nullptr, "this batch solves on its caller's stream (no stream of its own)");
+        int least = 0, greatest = 0;
+        PSGB_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        cudaStream_t fresh = nullptr;
+        PSGB_CUDA(cudaStreamCreateWithPriority(&fresh, cudaStreamNonBlocking, high != 0 ? greatest : least));
+        PSGB_CUDA(cudaStreamSynchronize(b.stream));
+        PSGB_CUDA(cudaStreamDestroy(b.stream));
+        b.stream = fresh;
+        return PSGB_OK;
+    });
+}
+
 int psgb_batch_set_edge_conductance(psgb_batch* h, const double* const* edge_conductance) {
     return guarded([&] {
         require(h != nullptr && edge_conductance != nullptr, "null argument");

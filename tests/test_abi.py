@@ -24,7 +24,7 @@ def test_library_loads_and_exports_every_declared_symbol():
     missing = [name for name in declared if not hasattr(lib, name)]
     assert not missing, missing
     assert sorted(capi.EXPORTED) == declared
-    assert lib.psgb_abi_version() == 7
+    assert lib.psgb_abi_version() == 8
 
 
 def test_library_is_in_tree_and_has_sm103a_code():
