@@ -532,9 +532,12 @@ def serve_trace(args, rate: float, count: int):
 
 
 def requests_at(args, rate: float) -> int:
-    """2,000 requests a point, fewer at the lowest rate (500 at 50 requests/s: 10 s of
-    offered traffic, where both arms keep up and only the latency differs)."""
-    return min(args.serve_requests, max(500, int(10 * rate)))
+    """10 s of offered traffic up to `--serve-requests` (500 at 50 requests/s, where both
+    arms keep up and only the latency differs; 2,000 at 200 requests/s), and three times as
+    many at the saturated top rate (6,000 at 5,000 requests/s: the arrivals span 1.2 s, so
+    the capacity is measured past the first rounds and the drain)."""
+    n = min(args.serve_requests, max(500, int(10 * rate)))
+    return 3 * n if rate >= max(SERVE_RATES) else n
 
 
 def serving_sweep(args, dev, rates=SERVE_RATES) -> dict:
@@ -578,6 +581,7 @@ def serving_sweep(args, dev, rates=SERVE_RATES) -> dict:
             out["points"].append({"offered_per_s": rate, "requests": count, "continuous_batching_mixed": a,
                                   "one_at_a_time_fp64_tuned": b,
                                   "speedup_sub_steps_per_s": a["sub_steps_per_s"] / b["sub_steps_per_s"]})
+        out["tunings"] = {f"L{k}": smoother_desc(t) for k, t in sorted(srv.tunings.items())}
     finally:
         srv.close()
     if getattr(args, "native_serve", False):

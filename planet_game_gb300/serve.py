@@ -273,7 +273,11 @@ class Server:
             return True
 
     def run_trace(self, requests: list[ServedRequest], realtime: bool = True):
-        """Replay arrivals (at their offered times when `realtime`), wait for completion."""
+        """Replay arrivals (at their offered times when `realtime`), wait for completion of
+        every request of this trace (the server's completion count is cumulative: only the
+        completions after this call's start count)."""
+        with self.done_cv:
+            base = self.completed
         self.t_start = time.perf_counter()
         waiting = collections.deque()
         for r in requests:
@@ -289,7 +293,7 @@ class Server:
             while waiting and self.submit(waiting[0]):
                 waiting.popleft()
         with self.done_cv:
-            while self.completed < len(requests) and not self.errors:
+            while self.completed - base < len(requests) and not self.errors:
                 self.done_cv.wait(timeout=1.0)
         if self.errors:
             raise self.errors[0]

@@ -123,3 +123,22 @@ def test_one_at_a_time_comparator_matches_the_oracle_gates(population):
     serve.OneAtATime(population).run_trace(reqs, realtime=False)
     assert all(r.status == 0 for r in reqs)
     assert serve.summarize(reqs)["sub_steps_per_s"] > 0
+
+
+def test_consecutive_traces_each_wait_for_all_of_their_own_requests(population):
+    """The server's completion count runs across traces: a second trace on the same server
+    returns only once every one of its own requests is done."""
+    from planet_game_gb300 import serve
+    from planet_game_gb300 import workloads as W
+
+    srv = serve.Server(population, precision="mixed", autotune=False)
+    try:
+        first = serve.make_requests(W.poisson_trace(30, 5000.0, seed=21, weights=((4, .5), (5, .5)),
+                                                    planets_per_level=3), population, seed=22)
+        srv.run_trace(first, realtime=False)
+        second = serve.make_requests(W.poisson_trace(90, 5000.0, seed=23, weights=((4, .3), (5, .3), (6, .4)),
+                                                     planets_per_level=3), population, seed=24)
+        srv.run_trace(second, realtime=False)
+        assert all(r.status == 0 and r.done_s >= 0.0 for r in first + second)
+    finally:
+        srv.close()
