@@ -122,25 +122,49 @@ class _Lane:
         self.busy = False
         self.thread = threading.Thread(target=self._run, daemon=True)
         self.rounds = 0
+        self._staging = None                # per planet: pinned source, device source, pinned result
+
+    def _stage(self):
+        """Page-locked host buffers and device buffers for every planet of the lane (made
+        once): sources go up and results come down asynchronously on the lane's stream, with
+        one synchronisation a round instead of two blocking copies a planet."""
+        import torch
+
+        if self._staging is None:
+            self._staging = []
+            for p in self.planets:
+                n = p.mesh.cell_count
+                self._staging.append((torch.empty(n, dtype=torch.float64, pin_memory=True),
+                                      torch.empty(n, dtype=torch.float64, device=self.server.device),
+                                      torch.empty(n, dtype=torch.float64, pin_memory=True)))
+        return self._staging
 
     def _round(self, reqs: dict[int, ServedRequest]):
         import torch
 
         n = len(self.planets)
         active = [i in reqs for i in range(n)]
+        staging = self._stage()
         with torch.cuda.stream(self.stream):
             t0 = [p.state if active[i] else None for i, p in enumerate(self.planets)]
-            src = [torch.from_numpy(reqs[i].source).to(self.server.device, non_blocking=False) if active[i] else None
-                   for i in range(n)]
+            src = [None] * n
+            for i in reqs:
+                host, dev, _ = staging[i]
+                np.copyto(host.numpy(), reqs[i].source)
+                dev.copy_(host, non_blocking=True)
+                src[i] = dev
             outs, reps = self.batch.transport_step(
                 t0, src, [p.heat_capacity for p in self.planets], [p.dt for p in self.planets],
                 conductance=[p.conductance for p in self.planets],
                 edge_conductance=self.edge_conductance, active=active, **self.server.options)
-            for i, r in reqs.items():
+            for i in reqs:
                 if self.server.keep_inputs:
-                    r.t_in = self.planets[i].state.cpu().numpy()
+                    reqs[i].t_in = self.planets[i].state.cpu().numpy()
+                staging[i][2].copy_(outs[i], non_blocking=True)
+            self.stream.synchronize()
+            for i, r in reqs.items():
                 self.planets[i].state = outs[i]
-                r.result = outs[i].cpu().numpy()
+                r.result = staging[i][2].numpy().copy()
                 r.status = reps[i].status
                 r.iterations = reps[i].iterations
         done = time.perf_counter() - self.server.t_start
