@@ -532,12 +532,10 @@ def serve_trace(args, rate: float, count: int):
 
 
 def requests_at(args, rate: float) -> int:
-    """10 s of offered traffic up to `--serve-requests` (500 at 50 requests/s, where both
-    arms keep up and only the latency differs; 2,000 at 200 requests/s), and three times as
-    many at the saturated top rate (6,000 at 5,000 requests/s: the arrivals span 1.2 s, so
-    the capacity is measured past the first rounds and the drain)."""
-    n = min(args.serve_requests, max(500, int(10 * rate)))
-    return 3 * n if rate >= max(SERVE_RATES) else n
+    """The serving configuration's 2,000 requests a point, fewer at the lowest rate (500 at
+    50 requests/s: 10 s of offered traffic, where both arms keep up and only the latency
+    differs)."""
+    return min(args.serve_requests, max(500, int(10 * rate)))
 
 
 def serving_sweep(args, dev, rates=SERVE_RATES) -> dict:
