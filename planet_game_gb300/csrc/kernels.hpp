@@ -58,6 +58,14 @@ struct LevelView {
     std::uint8_t sets_vector;         // tiles per tile set of the vector launches (1 or 4)
     std::uint8_t level;               // multigrid level (0: fine)
     T correction = T(1);              // scale of the coarse-grid correction prolongated into this level
+    // Columns shared by the planets of one mesh level (null: `col` holds every planet's own
+    // columns). The planets of a mesh level have the same graph, so their planet-local
+    // columns are stored once per distinct graph, slot-major with pitch `spitch`; a tile's
+    // shift gives its planet's first row (x, added to a local column) and that row minus
+    // the graph's first row in `scol` (y, taken from the row index).
+    const std::int32_t* scol = nullptr;
+    const int2* tile_shift = nullptr;
+    std::uint32_t spitch = 0;
 };
 
 struct ReduceCtx {

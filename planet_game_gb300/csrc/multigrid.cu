@@ -278,7 +278,7 @@ __global__ void k_residual_restrict(LevelView<T> lv, LevelView<T> coarse, const 
 }
 
 template <typename T, int W, int R>
-__global__ void k_prolong_smooth(LevelView<T> lv, const std::int32_t* __restrict__ agg,
+__global__ void __launch_bounds__(kTile, 8) k_prolong_smooth(LevelView<T> lv, const std::int32_t* __restrict__ agg,
                                  const T* __restrict__ e, const T* __restrict__ b, const T* __restrict__ x,
                                  T* __restrict__ y, T omega, const InstanceScalars* sc, int gate) {
     pdl_begin();

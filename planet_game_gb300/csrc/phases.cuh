@@ -195,6 +195,31 @@ __device__ __forceinline__ TileSet<R> tile_set(const std::uint32_t* meta, unsign
     return s;
 }
 
+// The ELL columns of one row: column j is `add + p[j * stride]`. A level without shared
+// columns reads its own (add 0); a level whose planets share their graph's planet-local
+// columns reads those and adds the planet's first row (the tile's shift), which gives the
+// same row indices.
+struct ColumnsOf {
+    const std::int32_t* p;
+    int stride;
+    int add;
+    __device__ __forceinline__ int operator[](int j) const { return add + p[j * stride]; }
+};
+template <typename T>
+__device__ __forceinline__ ColumnsOf columns_of(const LevelView<T>& lv, int tile, int row) {
+    if (lv.scol != nullptr) {
+        const int2 sh = lv.tile_shift[tile];
+        return ColumnsOf{lv.scol + (row - sh.y), static_cast<int>(lv.spitch), sh.x};
+    }
+    return ColumnsOf{lv.col + row, static_cast<int>(lv.rows), 0};
+}
+// Column-index bytes a row reads from HBM: none where the columns are shared (one small
+// copy per graph, which stays in L2).
+template <typename T>
+__device__ __forceinline__ unsigned long long col_bytes(const LevelView<T>& lv, int W) {
+    return lv.scol != nullptr ? 0ull : 4ull * static_cast<unsigned>(W);
+}
+
 // Algorithmic bytes of the open tiles of a tile set: `per_row` times their valid rows.
 template <int R>
 __device__ __forceinline__ void count_rows(unsigned long long* counter, int lane, const TileSet<R>& ts,
@@ -403,9 +428,10 @@ __device__ void smooth(const LevelView<T>& lv, int t0, int lane, const T* PSGB_P
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int row = ts.tile[k] * kTile + lane;
+        const ColumnsOf col = columns_of(lv, ts.tile[k], row);
         T s = b[row];
 #pragma unroll
-        for (int j = 0; j < W; ++j) s -= lv.vd[j * P + row] * x[lv.col[j * P + row]];
+        for (int j = 0; j < W; ++j) s -= lv.vd[j * P + row] * x[col[j]];
         if (omega == T(1)) {
             out[k] = lv.inv[row] * s;
         } else {
@@ -416,7 +442,7 @@ __device__ void smooth(const LevelView<T>& lv, int t0, int lane, const T* PSGB_P
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         if (!on[k]) continue;
-        count_bytes(lv.bytes, lane, static_cast<unsigned long long>(ts.rows[k]) * (4ull * W + sizeof(T) * (W + 4ull)));
+        count_bytes(lv.bytes, lane, static_cast<unsigned long long>(ts.rows[k]) * (col_bytes(lv, W) + sizeof(T) * (W + 4ull)));
         if (lane < ts.rows[k]) y[ts.tile[k] * kTile + lane] = out[k];
     }
 }
@@ -452,12 +478,13 @@ __device__ void smooth_block(const LevelView<T>& lv, int tile, int gid, int lane
     int local[W];
     T bv = T(0), inv = T(0), xo = T(0);
     if (live) {
+        const ColumnsOf col = columns_of(lv, ts.tile[0], row);
         bv = b[row];
         inv = lv.inv[row];
         xo = x[row];
 #pragma unroll
         for (int j = 0; j < W; ++j) {
-            const int c = lv.col[j * P + row];
+            const int c = col[j];
             a[j] = lv.vd[j * P + row];
             local[j] = (c >= first && c < first + kTile) ? c - first : -1;
             h[j] = local[j] < 0 ? x[c] : T(0);
@@ -478,7 +505,7 @@ __device__ void smooth_block(const LevelView<T>& lv, int tile, int gid, int lane
         xo = out;
         group_sync(gid);
     }
-    count_bytes(lv.bytes, lane, static_cast<unsigned long long>(ts.rows[0]) * (4ull * W + sizeof(T) * (W + 4ull)));
+    count_bytes(lv.bytes, lane, static_cast<unsigned long long>(ts.rows[0]) * (col_bytes(lv, W) + sizeof(T) * (W + 4ull)));
     if (live) y[row] = xo;
 }
 
@@ -496,15 +523,16 @@ __device__ void residual(const LevelView<T>& lv, int t0, int lane, const T* PSGB
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int row = ts.tile[k] * kTile + lane;
+        const ColumnsOf col = columns_of(lv, ts.tile[k], row);
         T s = b[row] - lv.vd[W * P + row] * x[row];
 #pragma unroll
-        for (int j = 0; j < W; ++j) s -= lv.vd[j * P + row] * x[lv.col[j * P + row]];
+        for (int j = 0; j < W; ++j) s -= lv.vd[j * P + row] * x[col[j]];
         out[k] = s;
     }
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         if (!on[k]) continue;
-        count_bytes(lv.bytes, lane, static_cast<unsigned long long>(ts.rows[k]) * (4ull * W + sizeof(T) * (W + 4ull)));
+        count_bytes(lv.bytes, lane, static_cast<unsigned long long>(ts.rows[k]) * (col_bytes(lv, W) + sizeof(T) * (W + 4ull)));
         if (lane < ts.rows[k]) r[ts.tile[k] * kTile + lane] = out[k];
     }
 }
@@ -518,14 +546,15 @@ __device__ void spmv(const LevelView<T>& lv, int t0, int lane, const T* PSGB_PHA
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int row = ts.tile[k] * kTile + lane;
+        const ColumnsOf col = columns_of(lv, ts.tile[k], row);
         T s = lv.vd[W * P + row] * x[row];
 #pragma unroll
-        for (int j = 0; j < W; ++j) s += lv.vd[j * P + row] * x[lv.col[j * P + row]];
+        for (int j = 0; j < W; ++j) s += lv.vd[j * P + row] * x[col[j]];
         out[k] = s;
     }
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-        count_bytes(lv.bytes, lane, static_cast<unsigned long long>(ts.rows[k]) * (4ull * W + sizeof(T) * (W + 3ull)));
+        count_bytes(lv.bytes, lane, static_cast<unsigned long long>(ts.rows[k]) * (col_bytes(lv, W) + sizeof(T) * (W + 3ull)));
         if (lane < ts.rows[k]) y[ts.tile[k] * kTile + lane] = out[k];
     }
 }
@@ -591,10 +620,11 @@ __device__ void prolong_smooth(const LevelView<T>& lv, int t0, int lane, const s
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int row = ts.tile[k] * kTile + lane;
+        const ColumnsOf col = columns_of(lv, ts.tile[k], row);
         T s = b[row];
 #pragma unroll
         for (int j = 0; j < W; ++j) {
-            const int c = lv.col[j * P + row];
+            const int c = col[j];
             s -= lv.vd[j * P + row] * (x[c] + prod(lv.correction, e[agg[c]]));
         }
         if (omega == T(1)) {
@@ -609,7 +639,7 @@ __device__ void prolong_smooth(const LevelView<T>& lv, int t0, int lane, const s
         if (!on[k]) continue;
         // each vector once: col, values, inv, b, x, y and the row's aggregate index (the
         // neighbours' x and agg are gathers of vectors already counted; e is 1/16 of a row)
-        count_bytes(lv.bytes, lane, static_cast<unsigned long long>(ts.rows[k]) * (4ull * W + sizeof(T) * (W + 4ull) + 4ull));
+        count_bytes(lv.bytes, lane, static_cast<unsigned long long>(ts.rows[k]) * (col_bytes(lv, W) + sizeof(T) * (W + 4ull) + 4ull));
         if (lane < ts.rows[k]) y[ts.tile[k] * kTile + lane] = out[k];
     }
 }
@@ -881,15 +911,16 @@ __device__ void bicg_v(const LevelView<T>& lv, int t0, int gid, int lane, const 
 #pragma unroll
     for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && running(ctx.sc[ts.inst[k]]);
     if (!any_of(on)) return;
-    count_rows<R>(lv.bytes, lane, ts, on, 4ull * W + sizeof(T) * (W + 4ull));
+    count_rows<R>(lv.bytes, lane, ts, on, col_bytes(lv, W) + sizeof(T) * (W + 4ull));
     const std::uint32_t P = lv.rows;
     T q[R], y[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int row = ts.tile[k] * kTile + lane;
+        const ColumnsOf col = columns_of(lv, ts.tile[k], row);
         T s = lv.vd[W * P + row] * in[row];
 #pragma unroll
-        for (int j = 0; j < W; ++j) s += lv.vd[j * P + row] * in[lv.col[j * P + row]];
+        for (int j = 0; j < W; ++j) s += lv.vd[j * P + row] * in[col[j]];
         y[k] = s;
         q[k] = prod(shadow[row], s);
     }
@@ -956,15 +987,16 @@ __device__ void bicg_t(const LevelView<T>& lv, int t0, int gid, int lane, const 
         on[k] = ts.rows[k] > 0 && running(sc) && !sc.half_done;
     }
     if (!any_of(on)) return;
-    count_rows<R>(lv.bytes, lane, ts, on, 4ull * W + sizeof(T) * (W + 4ull));
+    count_rows<R>(lv.bytes, lane, ts, on, col_bytes(lv, W) + sizeof(T) * (W + 4ull));
     const std::uint32_t P = lv.rows;
     T q[2 * R], y[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int row = ts.tile[k] * kTile + lane;
+        const ColumnsOf col = columns_of(lv, ts.tile[k], row);
         T s = lv.vd[W * P + row] * shat[row];
 #pragma unroll
-        for (int j = 0; j < W; ++j) s += lv.vd[j * P + row] * shat[lv.col[j * P + row]];
+        for (int j = 0; j < W; ++j) s += lv.vd[j * P + row] * shat[col[j]];
         y[k] = s;
         q[2 * k] = prod(s, s);
         q[2 * k + 1] = prod(s, s_vec[row]);
@@ -1115,15 +1147,16 @@ __device__ void pcg_q(const LevelView<T>& lv, int t0, int gid, int lane, const T
 #pragma unroll
     for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && running(ctx.sc[ts.inst[k]]);
     if (!any_of(on)) return;
-    count_rows<R>(lv.bytes, lane, ts, on, 4ull * W + sizeof(T) * (W + 3ull));
+    count_rows<R>(lv.bytes, lane, ts, on, col_bytes(lv, W) + sizeof(T) * (W + 3ull));
     const std::uint32_t P = lv.rows;
     T q[R], y[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int row = ts.tile[k] * kTile + lane;
+        const ColumnsOf col = columns_of(lv, ts.tile[k], row);
         T s = lv.vd[W * P + row] * p[row];
 #pragma unroll
-        for (int j = 0; j < W; ++j) s += lv.vd[j * P + row] * p[lv.col[j * P + row]];
+        for (int j = 0; j < W; ++j) s += lv.vd[j * P + row] * p[col[j]];
         y[k] = s;
         q[k] = prod(p[row], s);
     }
@@ -1230,15 +1263,16 @@ __device__ void outer_residual(const LevelView<double>& lv, int t0, int gid, int
 #pragma unroll
     for (int k = 0; k < R; ++k) on[k] = ts.rows[k] > 0 && ctx.sc[ts.inst[k]].outer_status == kRunning;
     if (!any_of(on)) return;
-    count_rows<R>(lv.bytes, lane, ts, on, 4ull * W + 8ull * (W + 4ull) + sizeof(TI));
+    count_rows<R>(lv.bytes, lane, ts, on, col_bytes(lv, W) + 8ull * (W + 4ull) + sizeof(TI));
     const std::uint32_t P = lv.rows;
     double q[R], rv[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int row = ts.tile[k] * kTile + lane;
+        const ColumnsOf col = columns_of(lv, ts.tile[k], row);
         double s = b[row] - lv.vd[W * P + row] * x[row];
 #pragma unroll
-        for (int j = 0; j < W; ++j) s -= lv.vd[j * P + row] * x[lv.col[j * P + row]];
+        for (int j = 0; j < W; ++j) s -= lv.vd[j * P + row] * x[col[j]];
         rv[k] = s;
     }
 #pragma unroll

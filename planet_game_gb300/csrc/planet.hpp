@@ -137,6 +137,12 @@ struct BatchLevel {
     std::uint32_t tiles = 0;
     std::uint32_t width = 0;           // device ELL width (6, 8, 12, 16)
     std::int32_t* col = nullptr;       // [width][P]
+    // planet-local columns once per distinct graph of the level's planets (null when no two
+    // planets share one): [width][spitch], and per tile (planet's first row, that row
+    // minus its graph's first row in scol)
+    std::int32_t* scol = nullptr;
+    int2* tile_shift = nullptr;
+    std::uint32_t spitch = 0;
     double* vd64 = nullptr;            // [width][P] off-diagonals, then [P] diagonal
     double* inv64 = nullptr;           // [P] 1 / diagonal
     float* vd32 = nullptr;

@@ -177,6 +177,56 @@ std::unique_ptr<Batch> make_batch_in(const std::vector<Planet*>& planets, void* 
 
 namespace {
 
+// The fine level's columns once per distinct graph: the planets of one mesh level have the
+// same graph whatever their radius, so a batch of many such planets streams one small copy
+// (L2-resident) instead of one copy a planet. Built only when two planets share a graph;
+// the level's own `col` stays for the kernels that read it (assembly, coarse tails).
+void share_columns(BatchLevel& L, const std::vector<Planet*>& planets, const std::vector<std::int32_t>& tile_inst,
+                   DeviceStore& store) {
+    const std::uint32_t I = static_cast<std::uint32_t>(planets.size());
+    const std::size_t W = L.width;
+    std::vector<int> graph_of(I, -1);
+    std::vector<std::uint32_t> holder;   // a planet holding each distinct graph
+    for (std::uint32_t i = 0; i < I; ++i) {
+        if (L.base[i] < 0) continue;
+        const HostLevel& h = planets[i]->hierarchy.levels[0];
+        for (std::size_t g = 0; g < holder.size() && graph_of[i] < 0; ++g) {
+            const HostLevel& o = planets[holder[g]]->hierarchy.levels[0];
+            if (h.size == o.size && h.offset == o.offset && h.column == o.column) graph_of[i] = static_cast<int>(g);
+        }
+        if (graph_of[i] < 0) {
+            graph_of[i] = static_cast<int>(holder.size());
+            holder.push_back(i);
+        }
+    }
+    if (holder.size() == I) return;
+    std::vector<std::uint32_t> start(holder.size());
+    std::uint32_t pitch = 0;
+    for (std::size_t g = 0; g < holder.size(); ++g) {
+        start[g] = pitch;
+        pitch += pad_rows(planets[holder[g]]->hierarchy.levels[0].size);
+    }
+    // local columns; a missing neighbour slot and every padding row point at the row itself
+    std::vector<std::int32_t> scol(W * pitch);
+    for (std::size_t g = 0; g < holder.size(); ++g) {
+        const HostLevel& h = planets[holder[g]]->hierarchy.levels[0];
+        for (std::uint32_t r = 0; r < pad_rows(h.size); ++r)
+            for (std::size_t j = 0; j < W; ++j) scol[j * pitch + start[g] + r] = static_cast<std::int32_t>(r);
+        for (std::uint32_t r = 0; r < h.size; ++r)
+            for (std::uint32_t k = h.offset[r]; k < h.offset[r + 1]; ++k)
+                scol[(k - h.offset[r]) * pitch + start[g] + r] = static_cast<std::int32_t>(h.column[k]);
+    }
+    std::vector<int2> shift(L.tiles);
+    for (std::uint32_t t = 0; t < L.tiles; ++t) {
+        const int i = tile_inst[t];
+        const auto base = static_cast<std::int32_t>(L.base[i]);
+        shift[t] = make_int2(base, base - static_cast<std::int32_t>(start[graph_of[i]]));
+    }
+    L.scol = store.upload(scol);
+    L.tile_shift = store.upload(shift);
+    L.spitch = pitch;
+}
+
 std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* arena, std::size_t arena_bytes) {
     if (planets.empty()) throw std::invalid_argument("a batch needs at least one planet");
     if (planets.size() >= kMaxInstances) throw std::invalid_argument("a batch holds fewer than 4,194,304 planets");
@@ -271,6 +321,7 @@ std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* ar
         L.tile_meta = b.store.upload(meta);
 
         L.col = b.store.upload(col);
+        if (l == 0 && arena == nullptr && I > 1) share_columns(L, planets, tile_inst, b.store);
         L.vd64 = b.store.alloc<double>((W + 1) * P);
         L.vd32 = b.store.alloc<float>((W + 1) * P);
         L.inv64 = b.store.alloc<double>(P);
@@ -468,10 +519,14 @@ std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* ar
 
 template <typename T>
 static LevelView<T> make_view(const BatchLevel& L, const T* vd, const T* inv, std::size_t level) {
-    return LevelView<T>{L.rows,         L.width,        L.tiles,      L.col,
-                        vd,             inv,            L.tile_inst,  L.tile_rows,
-                        L.tile_sweep,   L.tile_meta,    nullptr,
-                        L.sets_stencil, L.sets_vector,  static_cast<std::uint8_t>(level)};
+    LevelView<T> v{L.rows,         L.width,        L.tiles,      L.col,
+                   vd,             inv,            L.tile_inst,  L.tile_rows,
+                   L.tile_sweep,   L.tile_meta,    nullptr,
+                   L.sets_stencil, L.sets_vector,  static_cast<std::uint8_t>(level)};
+    v.scol = L.scol;
+    v.tile_shift = L.tile_shift;
+    v.spitch = L.spitch;
+    return v;
 }
 
 template <typename T>
