@@ -375,6 +375,26 @@ Tuning autotune(Batch& b, const SolveOptions& opt, const double* rhs, const doub
         b.tail_level = pick;
         set_mode(pick_mode);
     }
+    // the fine level's tile-set sizes again, by whole solves with everything else chosen: a
+    // sweep launch timed alone favours two tiles a thread, while whole solves (many short
+    // launches overlapping, lanes beside each other) measured faster with one on the
+    // 64-planet mix and on one L8 planet
+    if (best_ms > 0.0 && b.levels[0].tiles >= kMinTunedTiles) {
+        BatchLevel& F = b.levels[0];
+        const std::uint8_t s0 = F.sets_stencil, v0 = F.sets_vector;
+        std::uint8_t ps = s0, pv = v0;
+        for (std::uint8_t s : {std::uint8_t(1), std::uint8_t(2)}) {
+            for (std::uint8_t v : {std::uint8_t(1), std::uint8_t(4)}) {
+                if (s == s0 && v == v0) continue;
+                F.sets_stencil = s;
+                F.sets_vector = v;
+                const double ms = run(best);
+                if (ms > 0.0 && ms < best_ms) { best_ms = ms; ps = s; pv = v; }
+            }
+        }
+        F.sets_stencil = ps;
+        F.sets_vector = pv;
+    }
     if (best_ms < 0.0) {
         set_sweeps(b, before);
         throw std::runtime_error("autotune: no candidate met the tolerance on every planet");
