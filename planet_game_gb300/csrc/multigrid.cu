@@ -174,6 +174,7 @@ __global__ void k_smooth_zero(LevelView<T> lv, const T* __restrict__ b, T* __res
 template <typename T, int W, int R>
 __global__ void k_smooth(LevelView<T> lv, const T* __restrict__ b, const T* __restrict__ x, T* __restrict__ y,
                          T omega, const InstanceScalars* sc, int gate, DenseTask<T> dense) {
+    ph::prefetch_static<T, W, R>(lv, blockIdx.x * R, threadIdx.x);
     pdl_begin();
     const unsigned sets = ph::tile_sets(lv.tiles, R);
     if (blockIdx.x >= sets) {
@@ -186,6 +187,7 @@ __global__ void k_smooth(LevelView<T> lv, const T* __restrict__ b, const T* __re
 template <typename T, int W>
 __global__ void k_smooth_block(LevelView<T> lv, const T* __restrict__ b, const T* __restrict__ x, T* __restrict__ y,
                                T omega, int inner, const InstanceScalars* sc, int gate, DenseTask<T> dense) {
+    ph::prefetch_static<T, W, 1>(lv, blockIdx.x, threadIdx.x);
     pdl_begin();
     if (blockIdx.x >= lv.tiles) {
         ph::dense_block<T>(dense, blockIdx.x - lv.tiles, threadIdx.x, sc, gate);
@@ -197,6 +199,7 @@ __global__ void k_smooth_block(LevelView<T> lv, const T* __restrict__ b, const T
 template <typename T, int W, int R>
 __global__ void k_residual(LevelView<T> lv, const T* __restrict__ b, const T* __restrict__ x, T* __restrict__ r,
                            const InstanceScalars* sc, int gate, DenseTask<T> dense) {
+    ph::prefetch_static<T, W, R>(lv, blockIdx.x * R, threadIdx.x);
     pdl_begin();
     const unsigned sets = ph::tile_sets(lv.tiles, R);
     if (blockIdx.x >= sets) {
@@ -225,6 +228,14 @@ __global__ void k_restrict_zero(LevelView<T> coarse, const std::uint32_t* __rest
                                 const std::uint32_t* __restrict__ member, const T* __restrict__ r,
                                 T* __restrict__ bc, T* __restrict__ xc, T omega, const InstanceScalars* sc,
                                 int gate) {
+#pragma unroll
+    for (int k = 0; k < ph::kRowsCoarse; ++k) {
+        const unsigned tile = blockIdx.x * ph::kRowsCoarse + k;
+        if (tile < coarse.tiles) {
+            if (threadIdx.x == 0) ph::prefetch_l1(coarse.tile_meta + tile);
+            ph::prefetch_l1(moff + tile * kTile + threadIdx.x);
+        }
+    }
     pdl_begin();
     ph::restrict_zero<T, ph::kRowsCoarse>(coarse, blockIdx.x * ph::kRowsCoarse, threadIdx.x, moff, member, r, bc, xc, omega,
                                           sc, gate);
@@ -243,27 +254,45 @@ __global__ void k_residual_restrict(LevelView<T> lv, LevelView<T> coarse, const 
                                     const std::uint32_t* __restrict__ member, const T* __restrict__ b,
                                     const T* __restrict__ x, T* __restrict__ bc, T* __restrict__ xc, T omega,
                                     const InstanceScalars* sc, int gate, DenseTask<T> dense) {
-    pdl_begin();
     const unsigned blocks = (coarse.rows + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    const int lane = static_cast<int>(threadIdx.x & 31);
+    const int row = static_cast<int>(blockIdx.x) * kWarpsPerBlock + static_cast<int>(threadIdx.x >> 5);
+    const std::uint32_t P = lv.rows;
+    // Before the wait, what no kernel writes: the row's tile word, its member range, the
+    // first 32 members and their columns (rows past 32 members load theirs in the loop).
+    ph::TileSet<1> ts{};
+    std::uint32_t k0 = 0, k1 = 0;
+    int f0 = 0;
+    int c0[W];
+#pragma unroll
+    for (int j = 0; j < W; ++j) c0[j] = 0;
+    if (blockIdx.x < blocks) {
+        ts = ph::tile_set<1>(coarse.tile_meta, coarse.tiles, row / kTile);
+        k0 = moff[row];
+        k1 = moff[row + 1];
+        if (k0 + static_cast<std::uint32_t>(lane) < k1) {
+            f0 = static_cast<int>(member[k0 + lane]);
+#pragma unroll
+            for (int j = 0; j < W; ++j) c0[j] = lv.col[j * P + f0];
+        }
+    }
+    pdl_begin();
     if (blockIdx.x >= blocks) {
         ph::dense_block<T>(dense, blockIdx.x - blocks, threadIdx.x, sc, gate);
         return;
     }
-    const int lane = static_cast<int>(threadIdx.x & 31);
-    const int row = static_cast<int>(blockIdx.x) * kWarpsPerBlock + static_cast<int>(threadIdx.x >> 5);
-    const ph::TileSet<1> ts = ph::tile_set<1>(coarse.tile_meta, coarse.tiles, row / kTile);
     if (row % kTile >= ts.rows[0] || !ph::gate_open(sc, ts.inst[0], gate)) return;   // the whole warp
-    const std::uint32_t P = lv.rows, k0 = moff[row], k1 = moff[row + 1];
     T s = T(0);
     unsigned moved = 0;
     for (std::uint32_t base = k0; base < k1; base += 32) {
         const std::uint32_t k = base + static_cast<std::uint32_t>(lane);
         T rm = T(0);
         if (k < k1) {
-            const int f = static_cast<int>(member[k]);
+            const bool first = base == k0;
+            const int f = first ? f0 : static_cast<int>(member[k]);
             rm = b[f] - lv.vd[W * P + f] * x[f];
 #pragma unroll
-            for (int j = 0; j < W; ++j) rm -= lv.vd[j * P + f] * x[lv.col[j * P + f]];
+            for (int j = 0; j < W; ++j) rm -= lv.vd[j * P + f] * x[first ? c0[j] : lv.col[j * P + f]];
             moved += 4u * W + static_cast<unsigned>(sizeof(T)) * (W + 3u) + 4u;
         }
         const int n = static_cast<int>(k1 - base < 32u ? k1 - base : 32u);
@@ -281,6 +310,10 @@ template <typename T, int W, int R>
 __global__ void __launch_bounds__(kTile, 8) k_prolong_smooth(LevelView<T> lv, const std::int32_t* __restrict__ agg,
                                  const T* __restrict__ e, const T* __restrict__ b, const T* __restrict__ x,
                                  T* __restrict__ y, T omega, const InstanceScalars* sc, int gate) {
+    ph::prefetch_static<T, W, R>(lv, blockIdx.x * R, threadIdx.x);
+#pragma unroll
+    for (int k = 0; k < R; ++k)
+        if (blockIdx.x * R + k < lv.tiles) ph::prefetch_l1(agg + (blockIdx.x * R + k) * kTile + threadIdx.x);
     pdl_begin();
     ph::prolong_smooth<T, W, R>(lv, blockIdx.x * R, threadIdx.x, agg, e, b, x, y, omega, sc, gate);
 }
@@ -295,6 +328,7 @@ __global__ void k_prolong(LevelView<T> lv, const std::int32_t* __restrict__ agg,
 // Coarsest level: x = A^-1 b, one warp per row, eight rows per block.
 template <typename T>
 __global__ void k_dense_solve(DenseTask<T> dense, const InstanceScalars* sc, int gate) {
+    if (threadIdx.x == 0) ph::prefetch_l1(dense.blocks + blockIdx.x);
     pdl_begin();
     ph::dense_block<T>(dense, blockIdx.x, threadIdx.x, sc, gate);
 }

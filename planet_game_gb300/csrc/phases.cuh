@@ -220,6 +220,31 @@ __device__ __forceinline__ unsigned long long col_bytes(const LevelView<T>& lv, 
     return lv.scol != nullptr ? 0ull : 4ull * static_cast<unsigned>(W);
 }
 
+// ---- before griddepcontrol.wait --------------------------------------------------------
+// A launch scheduled early (programmatic dependent launch) waits for its predecessor in
+// pdl_begin(). Before that it may touch only what nothing writes once the batch is built -
+// tile words, ELL columns, aggregates, restriction lists, dense-block tables - and these
+// prefetches bring the lines a phase reads first into L1 there, so two dependent loads of
+// the phase's chain (tile word, then column) hit L1 after the wait. Never a value or a
+// vector: those are written by the solve's or the assembly's kernels, and an L1 line
+// fetched before the wait could be stale after it.
+__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
+template <typename T, int W, int R>
+__device__ __forceinline__ void prefetch_static(const LevelView<T>& lv, int t0, int lane) {
+    if (static_cast<unsigned>(t0) >= lv.tiles) return;
+    if (lane == 0) prefetch_l1(lv.tile_meta + t0);
+    if (lv.scol != nullptr) return;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int tile = t0 + k;
+        if (static_cast<unsigned>(tile) >= lv.tiles) break;
+        const int row = tile * kTile + lane;
+#pragma unroll
+        for (int j = 0; j < W; ++j) prefetch_l1(lv.col + static_cast<std::size_t>(j) * lv.rows + row);
+    }
+}
+
 // Algorithmic bytes of the open tiles of a tile set: `per_row` times their valid rows.
 template <int R>
 __device__ __forceinline__ void count_rows(unsigned long long* counter, int lane, const TileSet<R>& ts,
