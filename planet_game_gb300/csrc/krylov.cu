@@ -36,6 +36,7 @@ constexpr int kCompletion = ph::kDeferred;
 template <typename T, int R>
 __global__ void k_bicg_init(LevelView<T> lv, const T* __restrict__ b, T* x, T* r, T* shadow, T* p, T* v,
                             ReduceCtx ctx, double tol, int max_it) {
+    ph::prefetch_meta(lv, blockIdx.x * R, threadIdx.x);
     pdl_begin();
     ph::bicg_init<T, R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, b, x, r, shadow, p, v, ctx, tol, max_it);
 }
@@ -43,6 +44,7 @@ __global__ void k_bicg_init(LevelView<T> lv, const T* __restrict__ b, T* x, T* r
 template <typename T, int R>
 __global__ void k_bicg_p(LevelView<T> lv, const T* __restrict__ r, const T* __restrict__ v, T* p, T* xv, T omega_j,
                          const InstanceScalars* sc) {
+    ph::prefetch_meta(lv, blockIdx.x * R, threadIdx.x);
     pdl_begin();
     ph::bicg_p<T, R>(lv, blockIdx.x * R, threadIdx.x, r, v, p, xv, omega_j, sc);
 }
@@ -50,6 +52,7 @@ __global__ void k_bicg_p(LevelView<T> lv, const T* __restrict__ r, const T* __re
 template <typename T, int W, int R>
 __global__ void k_bicg_v(LevelView<T> lv, const T* __restrict__ in, T* __restrict__ out, const T* __restrict__ shadow,
                          ReduceCtx ctx) {
+    ph::prefetch_static<T, W, R>(lv, blockIdx.x * R, threadIdx.x);
     pdl_begin();
     ph::bicg_v<T, W, R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, in, out, shadow, ctx);
 }
@@ -57,6 +60,7 @@ __global__ void k_bicg_v(LevelView<T> lv, const T* __restrict__ in, T* __restric
 template <typename T, int R>
 __global__ void k_bicg_s(LevelView<T> lv, const T* __restrict__ r, const T* __restrict__ v, T* __restrict__ s_out,
                          T* xv, T omega_j, ReduceCtx ctx) {
+    ph::prefetch_meta(lv, blockIdx.x * R, threadIdx.x);
     pdl_begin();
     ph::bicg_s<T, R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, r, v, s_out, xv, omega_j, ctx);
 }
@@ -64,6 +68,7 @@ __global__ void k_bicg_s(LevelView<T> lv, const T* __restrict__ r, const T* __re
 template <typename T, int W, int R>
 __global__ void k_bicg_t(LevelView<T> lv, const T* __restrict__ shat, T* __restrict__ t, const T* __restrict__ s_vec,
                          ReduceCtx ctx) {
+    ph::prefetch_static<T, W, R>(lv, blockIdx.x * R, threadIdx.x);
     pdl_begin();
     ph::bicg_t<T, W, R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, shat, t, s_vec, ctx);
 }
@@ -72,6 +77,7 @@ template <typename T, int R>
 __global__ void k_bicg_x(LevelView<T> lv, const T* __restrict__ phat, const T* __restrict__ shat,
                          const T* __restrict__ s_vec, const T* __restrict__ t, T* x, T* r,
                          const T* __restrict__ shadow, ReduceCtx ctx) {
+    ph::prefetch_meta(lv, blockIdx.x * R, threadIdx.x);
     pdl_begin();
     ph::bicg_x<T, R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, phat, shat, s_vec, t, x, r, shadow, ctx);
 }
@@ -79,24 +85,28 @@ __global__ void k_bicg_x(LevelView<T> lv, const T* __restrict__ phat, const T* _
 template <typename T, int R>
 __global__ void k_pcg_init(LevelView<T> lv, const T* __restrict__ b, T* x, T* r, T* p, T* xv, T omega_j,
                            ReduceCtx ctx, double tol, int max_it) {
+    ph::prefetch_meta(lv, blockIdx.x * R, threadIdx.x);
     pdl_begin();
     ph::pcg_init<T, R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, b, x, r, p, xv, omega_j, ctx, tol, max_it);
 }
 
 template <typename T, int R>
 __global__ void k_pcg_rz(LevelView<T> lv, const T* __restrict__ r, const T* __restrict__ z, ReduceCtx ctx) {
+    ph::prefetch_meta(lv, blockIdx.x * R, threadIdx.x);
     pdl_begin();
     ph::pcg_rz<T, R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, r, z, ctx);
 }
 
 template <typename T, int R>
 __global__ void k_pcg_p(LevelView<T> lv, const T* __restrict__ z, T* p, const InstanceScalars* sc) {
+    ph::prefetch_meta(lv, blockIdx.x * R, threadIdx.x);
     pdl_begin();
     ph::pcg_p<T, R>(lv, blockIdx.x * R, threadIdx.x, z, p, sc);
 }
 
 template <typename T, int W, int R>
 __global__ void k_pcg_q(LevelView<T> lv, const T* __restrict__ p, T* __restrict__ q_out, ReduceCtx ctx) {
+    ph::prefetch_static<T, W, R>(lv, blockIdx.x * R, threadIdx.x);
     pdl_begin();
     ph::pcg_q<T, W, R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, p, q_out, ctx);
 }
@@ -104,6 +114,7 @@ __global__ void k_pcg_q(LevelView<T> lv, const T* __restrict__ p, T* __restrict_
 template <typename T, int R>
 __global__ void k_pcg_xr(LevelView<T> lv, const T* __restrict__ p, const T* __restrict__ q_in, T* x, T* r, T* xv,
                          T omega_j, ReduceCtx ctx) {
+    ph::prefetch_meta(lv, blockIdx.x * R, threadIdx.x);
     pdl_begin();
     ph::pcg_xr<T, R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, p, q_in, x, r, xv, omega_j, ctx);
 }
@@ -111,6 +122,7 @@ __global__ void k_pcg_xr(LevelView<T> lv, const T* __restrict__ p, const T* __re
 template <int R>
 __global__ void k_outer_init(LevelView<double> lv, const double* __restrict__ b, ReduceCtx ctx, double tol,
                              int max_refine, const std::uint8_t* __restrict__ active) {
+    ph::prefetch_meta(lv, blockIdx.x * R, threadIdx.x);
     pdl_begin();
     static_cast<void>(max_refine);
     ph::outer_init<R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, b, ctx, tol, active);
@@ -119,12 +131,14 @@ __global__ void k_outer_init(LevelView<double> lv, const double* __restrict__ b,
 template <typename TI, int W, int R>
 __global__ void k_outer_residual(LevelView<double> lv, const double* __restrict__ b, const double* __restrict__ x,
                                  double* __restrict__ r64, TI* __restrict__ rin, ReduceCtx ctx, int max_refine) {
+    ph::prefetch_static<double, W, R>(lv, blockIdx.x * R, threadIdx.x);
     pdl_begin();
     ph::outer_residual<TI, W, R, kCompletion>(lv, blockIdx.x * R, 0, threadIdx.x, b, x, r64, rin, ctx, max_refine);
 }
 
 template <typename TI, int R>
 __global__ void k_outer_update(LevelView<double> lv, const TI* __restrict__ delta, double* x, InstanceScalars* sc) {
+    ph::prefetch_meta(lv, blockIdx.x * R, threadIdx.x);
     pdl_begin();
     ph::outer_update<TI, R>(lv, blockIdx.x * R, threadIdx.x, delta, x, sc);
 }
@@ -132,8 +146,10 @@ __global__ void k_outer_update(LevelView<double> lv, const TI* __restrict__ delt
 // The scalar step of a reduction phase, one planet per block (after the phase's launch).
 template <int K>
 __global__ void k_finish(ReduceCtx ctx, ph::FinishParams p) {
+    const int inst = static_cast<int>(blockIdx.x);
+    const unsigned begin = ctx.tile_begin[inst], end = ctx.tile_begin[inst + 1];   // fixed at build
     pdl_begin();
-    ph::finish_planet<K>(ctx, static_cast<int>(blockIdx.x), static_cast<int>(threadIdx.x), p);
+    ph::finish_planet<K>(ctx, inst, static_cast<int>(threadIdx.x), p, begin, end);
 }
 
 template <int K>

@@ -165,6 +165,7 @@ __global__ void __launch_bounds__(1024) k_dense_invert(DenseView dense, int leve
 template <typename T, int R>
 __global__ void k_smooth_zero(LevelView<T> lv, const T* __restrict__ b, T* __restrict__ x, T omega,
                               const InstanceScalars* sc, int gate) {
+    ph::prefetch_meta(lv, blockIdx.x * R, threadIdx.x);
     pdl_begin();
     ph::smooth_zero<T, R>(lv, blockIdx.x * R, threadIdx.x, b, x, omega, sc, gate);
 }
@@ -321,6 +322,10 @@ __global__ void __launch_bounds__(kTile, 8) k_prolong_smooth(LevelView<T> lv, co
 template <typename T, int R>
 __global__ void k_prolong(LevelView<T> lv, const std::int32_t* __restrict__ agg, const T* __restrict__ xc,
                           T* __restrict__ x, const InstanceScalars* sc, int gate) {
+    ph::prefetch_meta(lv, blockIdx.x * R, threadIdx.x);
+#pragma unroll
+    for (int k = 0; k < R; ++k)
+        if (blockIdx.x * R + k < lv.tiles) ph::prefetch_l1(agg + (blockIdx.x * R + k) * kTile + threadIdx.x);
     pdl_begin();
     ph::prolong<T, R>(lv, blockIdx.x * R, threadIdx.x, agg, xc, x, sc, gate);
 }

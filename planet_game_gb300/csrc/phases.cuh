@@ -230,6 +230,11 @@ __device__ __forceinline__ unsigned long long col_bytes(const LevelView<T>& lv, 
 // fetched before the wait could be stale after it.
 __device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
 
+template <typename T>
+__device__ __forceinline__ void prefetch_meta(const LevelView<T>& lv, int t0, int lane) {
+    if (lane == 0 && static_cast<unsigned>(t0) < lv.tiles) prefetch_l1(lv.tile_meta + t0);
+}
+
 template <typename T, int W, int R>
 __device__ __forceinline__ void prefetch_static(const LevelView<T>& lv, int t0, int lane) {
     if (static_cast<unsigned>(t0) >= lv.tiles) return;
@@ -314,8 +319,8 @@ enum Completion : int { kTicket = 0, kDeferred = 1 };
 // A planet's tile partials in tile order: lane l sums tiles begin + l, + 256, ... (four
 // loads in flight at a time), then the group's fixed tree; result in lane 0.
 template <int NQ>
-__device__ __forceinline__ void sum_partials(const ReduceCtx& ctx, int inst, int gid, int lane, double (&acc)[NQ]) {
-    const unsigned begin = ctx.tile_begin[inst], end = ctx.tile_begin[inst + 1];
+__device__ __forceinline__ void sum_partials(const ReduceCtx& ctx, unsigned begin, unsigned end, int gid, int lane,
+                                             double (&acc)[NQ]) {
 #pragma unroll
     for (int q = 0; q < NQ; ++q) acc[q] = 0.0;
     for (unsigned t0 = begin + lane; t0 < end; t0 += 4 * kTile) {
@@ -335,6 +340,11 @@ __device__ __forceinline__ void sum_partials(const ReduceCtx& ctx, int inst, int
         }
     }
     group_sum<double, NQ>(acc, gid, lane);
+}
+
+template <int NQ>
+__device__ __forceinline__ void sum_partials(const ReduceCtx& ctx, int inst, int gid, int lane, double (&acc)[NQ]) {
+    sum_partials<NQ>(ctx, ctx.tile_begin[inst], ctx.tile_begin[inst + 1], gid, lane, acc);
 }
 
 // Tile partial sums (in the tiles' precision A) to FP64 partials, then completion C.
@@ -861,13 +871,17 @@ __device__ __forceinline__ void finish_step(InstanceScalars& s, const double* su
     else finish_outer_residual(s, sum, p.max_refine);
 }
 
-// One planet per 256-thread block: its partials in tile order, then its scalar step.
+// One planet per 256-thread block: its partials in tile order, then its scalar step. The
+// planet's tile range [begin, end) is fixed when the batch is built (the finish launch
+// reads it before its programmatic-launch wait); the partials are summed whether or not
+// the planet took part, so that their loads need not wait for its status word.
 template <int K>
-__device__ void finish_planet(const ReduceCtx& ctx, int inst, int lane, const FinishParams& p) {
-    if (!finish_gate<K>(ctx.sc[inst], inst, p)) return;
+__device__ void finish_planet(const ReduceCtx& ctx, int inst, int lane, const FinishParams& p, unsigned begin,
+                              unsigned end) {
+    const bool open = finish_gate<K>(ctx.sc[inst], inst, p);
     double acc[FinishSums<K>::value];
-    sum_partials(ctx, inst, 0, lane, acc);
-    if (lane == 0) finish_step<K>(ctx.sc[inst], acc, p);
+    sum_partials(ctx, begin, end, 0, lane, acc);
+    if (open && lane == 0) finish_step<K>(ctx.sc[inst], acc, p);
 }
 
 // ---- Krylov phases (fine level) ----------------------------------------------------------
