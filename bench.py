@@ -363,13 +363,20 @@ def run_gb300(args, rank, world, local_rank):
         capi.check(lib.psgb_profile_end(C.byref(ms), C.byref(nl), C.byref(nbytes)))
         batch.concurrent = not args.serial_lanes
         achieved = nbytes.value / (ms.value / 1e3) / 1e9 if ms.value > 0 and nbytes.value > 0 else None
-        traffic = (traffic_all.get(args.workload) or {}).get(family.decode())
+        per_launch = nbytes.value / max(1, nl.value)
+        # DRAM bytes per algorithmic byte of the family's dominant kernel, from a committed
+        # ncu capture of a few launches, applied to this run's algorithmic bytes per launch
+        entry = (traffic_all.get(args.workload) or {}).get(family.decode())
+        traffic = source = None
+        if isinstance(entry, dict) and per_launch > 0:
+            traffic = entry["dram_per_algorithmic"] * per_launch
+            source = (f"ncu dram__bytes_read+write per algorithmic byte of {entry['kernel']} "
+                      f"({entry['launches']} launches, {entry['summary']}) x this run's algorithmic bytes per launch")
         return {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
                 "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                "traffic_source": "ncu dram__bytes per launch of this family, profiles/launches_*.md (constant)"
-                                  if traffic is not None else None,
+                "traffic_source": source,
                 "launches": int(nl.value), "avg_launch_us": ms.value * 1e3 / max(1, nl.value),
-                "bytes_per_launch": nbytes.value / max(1, nl.value),
+                "bytes_per_launch": per_launch,
                 "share_of_step": ms.value / args.steps / (elapsed * 1e3 / args.steps)}
 
     kernels = {}
