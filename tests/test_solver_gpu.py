@@ -172,7 +172,9 @@ def test_l7_planet_with_per_edge_conductance_against_the_oracle(meshes, precisio
 
 
 def test_batch_equals_solo_bit_for_bit(meshes):
-    """Each result is the same alone and in the mix (uneven levels, radii, conductances)."""
+    """Each result is the same alone and in the mix (uneven levels, radii, conductances).
+    The two L4 planets share one copy of their fine-level columns in the batch; alone, each
+    reads its own."""
     import planet_game_gb300 as pg
     from planet_game_gb300 import workloads as W
 
