@@ -28,7 +28,7 @@ CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 CU_SOURCES = ["multigrid.cu", "krylov.cu", "operators.cu", "column.cu", "noalloc.cu", "persistent.cu",
               "persistent_f32.cu", "persistent_f64.cu", "coarse_tail.cu",
               "newton.cu", "nonsym.cu", "insolation.cu", "multirhs.cu", "coarse_cluster.cu"]
-CPP_SOURCES = ["solver.cpp", "multirhs.cpp", "autotune.cpp", "capi.cpp", "profile.cpp", "host/icosphere.cpp", "host/agglomerate.cpp", "host/ilu_pattern.cpp", "host/tail_blocks.cpp", "host/hierarchy.cpp", "host/insolation.cpp",
+CPP_SOURCES = ["solver.cpp", "multirhs.cpp", "autotune.cpp", "capi.cpp", "profile.cpp", "host/icosphere.cpp", "host/agglomerate.cpp", "host/ilu_pattern.cpp", "host/tail_blocks.cpp", "host/shared_columns.cpp", "host/hierarchy.cpp", "host/insolation.cpp",
                "serve_core.cpp", "serve.cpp"]
 # Files compiled without FMA contraction (reference operation order).
 NO_FMAD = {"column.cu", "newton.cu", "nonsym.cu", "insolation.cu"}

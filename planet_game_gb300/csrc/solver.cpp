@@ -11,6 +11,7 @@
 #include "kernels.hpp"
 #include "coarse_tail.hpp"
 #include "host/agglomerate.hpp"
+#include "host/shared_columns.hpp"
 #include "krylov.hpp"
 #include "persistent.hpp"
 #include "profile.hpp"
@@ -177,54 +178,21 @@ std::unique_ptr<Batch> make_batch_in(const std::vector<Planet*>& planets, void* 
 
 namespace {
 
-// The fine level's columns once per distinct graph: the planets of one mesh level have the
-// same graph whatever their radius, so a batch of many such planets streams one small copy
-// (L2-resident) instead of one copy a planet. Built only when two planets share a graph;
-// the level's own `col` stays for the kernels that read it (assembly, coarse tails).
+// The fine level's columns once per distinct graph (host/shared_columns.hpp): a batch of
+// many planets of one mesh level streams one small copy (L2-resident) instead of one copy
+// a planet. The level's own `col` stays for the kernels that read it (assembly, coarse
+// tails).
 void share_columns(BatchLevel& L, const std::vector<Planet*>& planets, const std::vector<std::int32_t>& tile_inst,
                    DeviceStore& store) {
-    const std::uint32_t I = static_cast<std::uint32_t>(planets.size());
-    const std::size_t W = L.width;
-    std::vector<int> graph_of(I, -1);
-    std::vector<std::uint32_t> holder;   // a planet holding each distinct graph
-    for (std::uint32_t i = 0; i < I; ++i) {
-        if (L.base[i] < 0) continue;
-        const HostLevel& h = planets[i]->hierarchy.levels[0];
-        for (std::size_t g = 0; g < holder.size() && graph_of[i] < 0; ++g) {
-            const HostLevel& o = planets[holder[g]]->hierarchy.levels[0];
-            if (h.size == o.size && h.offset == o.offset && h.column == o.column) graph_of[i] = static_cast<int>(g);
-        }
-        if (graph_of[i] < 0) {
-            graph_of[i] = static_cast<int>(holder.size());
-            holder.push_back(i);
-        }
-    }
-    if (holder.size() == I) return;
-    std::vector<std::uint32_t> start(holder.size());
-    std::uint32_t pitch = 0;
-    for (std::size_t g = 0; g < holder.size(); ++g) {
-        start[g] = pitch;
-        pitch += pad_rows(planets[holder[g]]->hierarchy.levels[0].size);
-    }
-    // local columns; a missing neighbour slot and every padding row point at the row itself
-    std::vector<std::int32_t> scol(W * pitch);
-    for (std::size_t g = 0; g < holder.size(); ++g) {
-        const HostLevel& h = planets[holder[g]]->hierarchy.levels[0];
-        for (std::uint32_t r = 0; r < pad_rows(h.size); ++r)
-            for (std::size_t j = 0; j < W; ++j) scol[j * pitch + start[g] + r] = static_cast<std::int32_t>(r);
-        for (std::uint32_t r = 0; r < h.size; ++r)
-            for (std::uint32_t k = h.offset[r]; k < h.offset[r + 1]; ++k)
-                scol[(k - h.offset[r]) * pitch + start[g] + r] = static_cast<std::int32_t>(h.column[k]);
-    }
-    std::vector<int2> shift(L.tiles);
-    for (std::uint32_t t = 0; t < L.tiles; ++t) {
-        const int i = tile_inst[t];
-        const auto base = static_cast<std::int32_t>(L.base[i]);
-        shift[t] = make_int2(base, base - static_cast<std::int32_t>(start[graph_of[i]]));
-    }
-    L.scol = store.upload(scol);
+    std::vector<const HostLevel*> fine(planets.size());
+    for (std::size_t i = 0; i < planets.size(); ++i) fine[i] = &planets[i]->hierarchy.levels[0];
+    const SharedColumns s = shared_columns(fine, L.base, tile_inst, L.width);
+    if (s.pitch == 0) return;
+    std::vector<int2> shift(tile_inst.size());
+    for (std::size_t t = 0; t < shift.size(); ++t) shift[t] = make_int2(s.shift[2 * t], s.shift[2 * t + 1]);
+    L.scol = store.upload(s.scol);
     L.tile_shift = store.upload(shift);
-    L.spitch = pitch;
+    L.spitch = s.pitch;
 }
 
 std::unique_ptr<Batch> build_batch(const std::vector<Planet*>& planets, void* arena, std::size_t arena_bytes) {
